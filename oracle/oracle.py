@@ -1,0 +1,284 @@
+"""ctypes bindings for the C oracle (tsstat_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+as the checker and by ``bench.py`` for the CPU baseline.  The product never
+imports this module.
+
+The functions mirror the reference Python API for the statistics path
+(python/tskit/trees.py) closely enough for parity tests: each takes a
+``tskit_gb300.tables.Tables`` and returns float64 arrays shaped as the
+low-level reference call returns them (always with window and output
+dimensions; no dimension dropping).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+STAT_SITE = 1 << 0
+STAT_BRANCH = 1 << 1
+STAT_NODE = 1 << 2
+STAT_POLARISED = 1 << 10
+STAT_SPAN_NORMALISE = 1 << 11
+STAT_NONCENTRED = 1 << 14
+
+DIVERSITY, SEGSITES, Y1, DIVERGENCE, Y2, F2, Y3, F3, F4, RELATEDNESS, RELATEDNESS_NC = range(1, 12)
+
+
+class _TS(ctypes.Structure):
+    _fields_ = [
+        ("num_nodes", ctypes.c_int32),
+        ("num_edges", ctypes.c_int32),
+        ("num_sites", ctypes.c_int32),
+        ("num_mutations", ctypes.c_int32),
+        ("num_samples", ctypes.c_int32),
+        ("sequence_length", ctypes.c_double),
+        ("node_time", ctypes.c_void_p),
+        ("samples", ctypes.c_void_p),
+        ("edge_left", ctypes.c_void_p),
+        ("edge_right", ctypes.c_void_p),
+        ("edge_parent", ctypes.c_void_p),
+        ("edge_child", ctypes.c_void_p),
+        ("ins", ctypes.c_void_p),
+        ("rem", ctypes.c_void_p),
+        ("site_position", ctypes.c_void_p),
+        ("mutation_site", ctypes.c_void_p),
+        ("mutation_node", ctypes.c_void_p),
+        ("mutation_allele", ctypes.c_void_p),
+        ("mutation_alt", ctypes.c_void_p),
+    ]
+
+
+class _Output(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("idx", ctypes.c_int32 * 4)]
+
+
+_lib = None
+
+
+def build():
+    """Compile liboracle.so for this machine (gcc)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
+            os.path.join(HERE, "tsstat_oracle.c")
+        ):
+            build()
+        lib = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        lib.orc_sample_count_stat.argtypes = [
+            ctypes.POINTER(_TS), ctypes.c_int32, P, P, ctypes.c_int32, P,
+            ctypes.c_int32, P, ctypes.c_uint32, P,
+        ]
+        lib.orc_afs.argtypes = [
+            ctypes.POINTER(_TS), ctypes.c_int32, P, P, ctypes.c_int32, P,
+            ctypes.c_int32, P, ctypes.c_uint32, P,
+        ]
+        lib.orc_relatedness_vector.argtypes = [
+            ctypes.POINTER(_TS), ctypes.c_int32, P, ctypes.c_int32, P,
+            ctypes.c_int32, P, ctypes.c_uint32, P,
+        ]
+        lib.orc_genotype_matrix.argtypes = [ctypes.POINTER(_TS), P]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+class OracleTS:
+    """Holds the arrays a C call needs (kept alive for the call's duration)."""
+
+    def __init__(self, tables):
+        t = tables
+        self.tables = t
+        self.samples = t.samples().astype(np.int32)
+        allele, alt, _ = t.allele_codes()
+        self.arrays = dict(
+            node_time=np.ascontiguousarray(t.node_time, np.float64),
+            samples=self.samples,
+            edge_left=np.ascontiguousarray(t.edge_left, np.float64),
+            edge_right=np.ascontiguousarray(t.edge_right, np.float64),
+            edge_parent=np.ascontiguousarray(t.edge_parent, np.int32),
+            edge_child=np.ascontiguousarray(t.edge_child, np.int32),
+            ins=np.ascontiguousarray(t.edge_insertion_order, np.int32),
+            rem=np.ascontiguousarray(t.edge_removal_order, np.int32),
+            site_position=np.ascontiguousarray(t.site_position, np.float64),
+            mutation_site=np.ascontiguousarray(t.mutation_site, np.int32),
+            mutation_node=np.ascontiguousarray(t.mutation_node, np.int32),
+            mutation_allele=np.ascontiguousarray(allele, np.int32),
+            mutation_alt=np.ascontiguousarray(alt, np.int32),
+        )
+        s = _TS()
+        s.num_nodes = t.num_nodes
+        s.num_edges = t.num_edges
+        s.num_sites = t.num_sites
+        s.num_mutations = t.num_mutations
+        s.num_samples = len(self.samples)
+        s.sequence_length = t.sequence_length
+        for k, v in self.arrays.items():
+            setattr(s, k, _ptr(v))
+        self.struct = s
+        self.sample_index = np.full(t.num_nodes, -1, dtype=np.int64)
+        self.sample_index[self.samples] = np.arange(len(self.samples))
+
+    @property
+    def num_samples(self):
+        return len(self.samples)
+
+
+def _windows(ts, windows):
+    if windows is None:
+        return np.array([0.0, ts.tables.sequence_length])
+    return np.asarray(windows, dtype=np.float64)
+
+
+def _mode_flags(mode):
+    return {"branch": STAT_BRANCH, "site": STAT_SITE, None: STAT_SITE}[mode]
+
+
+def sample_count_stat(ts, sample_sets, outputs, windows=None, mode="site",
+                      span_normalise=True, polarised=False):
+    """Run a sample-count statistic.
+
+    ``outputs`` is a list of (type, (i, j, k, l)) summary terms over the K
+    sample sets.  Returns float64 (num_windows, len(outputs)).
+    """
+    lib = _load()
+    K = len(sample_sets)
+    W = np.zeros((ts.num_samples, K))
+    for k, s in enumerate(sample_sets):
+        W[ts.sample_index[np.asarray(s, dtype=np.int64)], k] = 1
+    n = np.array([len(s) for s in sample_sets], dtype=np.float64)
+    outs = (_Output * len(outputs))()
+    for r, (typ, idx) in enumerate(outputs):
+        outs[r].type = typ
+        idx = list(idx) + [0] * (4 - len(idx))
+        for q in range(4):
+            outs[r].idx[q] = idx[q]
+    win = _windows(ts, windows)
+    Wn = len(win) - 1
+    res = np.zeros((Wn, len(outputs)))
+    opts = _mode_flags(mode)
+    if span_normalise:
+        opts |= STAT_SPAN_NORMALISE
+    if polarised:
+        opts |= STAT_POLARISED
+    err = lib.orc_sample_count_stat(
+        ctypes.byref(ts.struct), K, _ptr(W), _ptr(n), len(outputs),
+        ctypes.cast(outs, ctypes.c_void_p), Wn, _ptr(win), opts, _ptr(res),
+    )
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return res
+
+
+def one_way(ts, typ, sample_sets, **kw):
+    return sample_count_stat(ts, sample_sets, [(typ, (k,)) for k in range(len(sample_sets))], **kw)
+
+
+def k_way(ts, typ, sample_sets, indexes, **kw):
+    return sample_count_stat(ts, sample_sets, [(typ, tuple(ix)) for ix in indexes], **kw)
+
+
+def allele_frequency_spectrum(ts, sample_sets, windows=None, time_windows=None,
+                              mode="site", span_normalise=True, polarised=False):
+    lib = _load()
+    K = len(sample_sets)
+    sizes = np.array([len(s) for s in sample_sets], dtype=np.int64)
+    flat = np.concatenate([np.asarray(s, dtype=np.int32) for s in sample_sets]).astype(np.int32)
+    win = _windows(ts, windows)
+    tw = np.array([0.0, np.inf]) if time_windows is None else np.asarray(time_windows, np.float64)
+    Wn, TW = len(win) - 1, len(tw) - 1
+    shape = (Wn, TW) + tuple(int(s) + 1 for s in sizes)
+    res = np.zeros(shape)
+    opts = _mode_flags(mode)
+    if span_normalise:
+        opts |= STAT_SPAN_NORMALISE
+    if polarised:
+        opts |= STAT_POLARISED
+    err = lib.orc_afs(ctypes.byref(ts.struct), K, _ptr(sizes), _ptr(flat), Wn, _ptr(win),
+                      TW, _ptr(tw), opts, _ptr(res))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return res
+
+
+def genetic_relatedness_vector(ts, W, windows=None, span_normalise=True, centre=True,
+                               nodes=None):
+    lib = _load()
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    if W.ndim == 1:
+        W = W[:, None]
+    nw = W.shape[1]
+    focal = ts.samples if nodes is None else np.asarray(nodes, dtype=np.int32)
+    win = _windows(ts, windows)
+    Wn = len(win) - 1
+    res = np.zeros((Wn, len(focal), nw))
+    opts = STAT_BRANCH
+    if span_normalise:
+        opts |= STAT_SPAN_NORMALISE
+    if not centre:
+        opts |= STAT_NONCENTRED
+    err = lib.orc_relatedness_vector(ctypes.byref(ts.struct), nw, _ptr(W), Wn, _ptr(win),
+                                     len(focal), _ptr(focal), opts, _ptr(res))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return res
+
+
+def genotype_matrix(ts):
+    """int8 (num_sites, num_samples) allele indexes."""
+    lib = _load()
+    G = np.zeros((ts.tables.num_sites, ts.num_samples), dtype=np.int8)
+    err = lib.orc_genotype_matrix(ctypes.byref(ts.struct), _ptr(G))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return G
+
+
+def divergence_matrix_site(ts, windows=None, span_normalise=True):
+    """Site-mode divergence matrix with every sample its own set
+    (trees.c:8753-8899), computed from the decoded genotype matrix."""
+    G = genotype_matrix(ts)
+    win = _windows(ts, windows)
+    pos = ts.tables.site_position
+    n = ts.num_samples
+    out = np.zeros((len(win) - 1, n, n))
+    for w in range(len(win) - 1):
+        sel = (pos >= win[w]) & (pos < win[w + 1])
+        Gw = G[sel].astype(np.int64)
+        # pairs carrying different alleles = sites - pairs carrying the same
+        same = np.zeros((n, n), dtype=np.int64)
+        for a in np.unique(Gw):
+            Xa = (Gw == a).astype(np.int64)
+            same += Xa.T @ Xa
+        D = (Gw.shape[0] - same).astype(np.float64)
+        np.fill_diagonal(D, 0.0)
+        if span_normalise:
+            D /= win[w + 1] - win[w]
+        out[w] = D
+    return out
+
+
+def relatedness_from_divergence(D):
+    """genetic_relatedness_matrix's normalisation (python/tskit/trees.py:9086-9095)
+    for singleton sample sets."""
+    n = np.ones(D.shape[-1])
+    B = D.copy()
+    np.fill_diagonal(B, np.diag(B) * (n - 1) / n)
+    K = B + np.mean(B)
+    y = np.mean(B, axis=0)
+    K -= y[:, None] + y[None, :]
+    return K / -2

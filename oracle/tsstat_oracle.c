@@ -1,0 +1,929 @@
+/*
+ * CPU oracle for the tree-sequence statistics path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C99 and double
+ * precision, the reference tskit algorithms that the GPU kernels replace; it
+ * is the checker for the parity tests and the timed CPU baseline ("port") on
+ * machines where the reference cannot be built.  The product never links or
+ * calls it.  Parity of this restatement is pinned against the reference
+ * library itself (oracle/Makefile builds it) and against golden vectors
+ * generated from it (tests/golden/).
+ *
+ * Restated reference functions (paths inside the tskit project):
+ *   branch sweep       c/tskit/trees.c:1352-1523  tsk_treeseq_branch_general_stat
+ *   site sweep         c/tskit/trees.c:1654-1776  tsk_treeseq_site_general_stat
+ *   allele weights     c/tskit/trees.c:1525-1652  get_allele_weights / site result
+ *   unpolarised f      c/tskit/trees.c:1944-1972
+ *   span normalise     c/tskit/trees.c:1920-1934
+ *   summary functions  c/tskit/trees.c:3934 (diversity), 4221 (segsites),
+ *                      4248 (Y1), 4690 (divergence), 4729/4755 (relatedness),
+ *                      4899 (Y2), 4938 (f2), 5177 (Y3), 5219 (f3), 5266 (f4)
+ *   AFS                c/tskit/trees.c:3469-3928
+ *   relatedness matvec c/tskit/trees.c:10402-10816
+ *   divergence matrix  c/tskit/trees.c:8684-8899 (site mode)
+ *
+ * Integer allele codes per mutation replace the reference's derived-state
+ * string comparisons; they are computed on the host with the same numbering
+ * (tskit_gb300/tables.py: Tables.allele_codes).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_STAT_SITE (1u << 0)
+#define ORC_STAT_BRANCH (1u << 1)
+#define ORC_STAT_NODE (1u << 2)
+#define ORC_STAT_POLARISED (1u << 10)
+#define ORC_STAT_SPAN_NORMALISE (1u << 11)
+#define ORC_STAT_NONCENTRED (1u << 14)
+
+#define ORC_ERR_NO_MEMORY (-2)
+#define ORC_ERR_BAD_PARAM (-4)
+
+enum {
+    ORC_DIVERSITY = 1,
+    ORC_SEGSITES = 2,
+    ORC_Y1 = 3,
+    ORC_DIVERGENCE = 4,
+    ORC_Y2 = 5,
+    ORC_F2 = 6,
+    ORC_Y3 = 7,
+    ORC_F3 = 8,
+    ORC_F4 = 9,
+    ORC_RELATEDNESS = 10,
+    ORC_RELATEDNESS_NONCENTRED = 11,
+};
+
+typedef struct {
+    int32_t num_nodes, num_edges, num_sites, num_mutations, num_samples;
+    double sequence_length;
+    const double *node_time;
+    const int32_t *samples; /* sample node ids in increasing id order */
+    const double *edge_left, *edge_right;
+    const int32_t *edge_parent, *edge_child;
+    const int32_t *ins, *rem;
+    const double *site_position;
+    const int32_t *mutation_site, *mutation_node, *mutation_allele, *mutation_alt;
+} orc_ts_t;
+
+typedef struct {
+    int32_t type;
+    int32_t idx[4];
+} orc_output_t;
+
+/* --------------------------------------------------------- summary funcs */
+static void eval_summary(int32_t K, const double *x, const double *n, int32_t R,
+    const orc_output_t *outs, double *y)
+{
+    double meanx = 0;
+    int need_mean = 0;
+    for (int32_t r = 0; r < R; r++) {
+        if (outs[r].type == ORC_RELATEDNESS) {
+            need_mean = 1;
+        }
+    }
+    if (need_mean) {
+        double s = 0;
+        for (int32_t k = 0; k < K; k++) {
+            s += x[k] / n[k];
+        }
+        meanx = s / (double) K;
+    }
+    for (int32_t r = 0; r < R; r++) {
+        const int32_t *ix = outs[r].idx;
+        const int32_t i = ix[0], j = ix[1], k = ix[2], l = ix[3];
+        double v = 0;
+        switch (outs[r].type) {
+            case ORC_DIVERSITY:
+                v = x[i] * (n[i] - x[i]) / (n[i] * (n[i] - 1));
+                break;
+            case ORC_SEGSITES:
+                v = (x[i] > 0) * (1 - x[i] / n[i]);
+                break;
+            case ORC_Y1:
+                v = x[i] * (n[i] - x[i]) * (n[i] - x[i] - 1)
+                    / (n[i] * (n[i] - 1) * (n[i] - 2));
+                break;
+            case ORC_DIVERGENCE:
+                v = x[i] * (n[j] - x[j]) / (n[i] * (n[j] - (i == j)));
+                break;
+            case ORC_Y2:
+                v = x[i] * (n[j] - x[j]) * (n[j] - x[j] - 1) / (n[i] * n[j] * (n[j] - 1));
+                break;
+            case ORC_F2:
+                v = (x[i] * (x[i] - 1) * (n[j] - x[j]) * (n[j] - x[j] - 1)
+                        - x[i] * (n[i] - x[i]) * (n[j] - x[j]) * x[j])
+                    / (n[i] * (n[i] - 1) * n[j] * (n[j] - 1));
+                break;
+            case ORC_Y3:
+                v = x[i] * (n[j] - x[j]) * (n[k] - x[k]) / (n[i] * n[j] * n[k]);
+                break;
+            case ORC_F3:
+                v = (x[i] * (x[i] - 1) * (n[j] - x[j]) * (n[k] - x[k])
+                        - x[i] * (n[i] - x[i]) * (n[j] - x[j]) * x[k])
+                    / (n[i] * (n[i] - 1) * n[j] * n[k]);
+                break;
+            case ORC_F4:
+                v = (x[i] * x[k] * (n[j] - x[j]) * (n[l] - x[l])
+                        - x[i] * x[l] * (n[j] - x[j]) * (n[k] - x[k]))
+                    / (n[i] * n[j] * n[k] * n[l]);
+                break;
+            case ORC_RELATEDNESS:
+                v = (x[i] / n[i] - meanx) * (x[j] / n[j] - meanx);
+                break;
+            case ORC_RELATEDNESS_NONCENTRED:
+                v = x[i] * x[j] / (n[i] * n[j]);
+                break;
+            default:
+                v = NAN;
+        }
+        y[r] = v;
+    }
+}
+
+typedef struct {
+    int32_t K, R;
+    const double *n;
+    const orc_output_t *outs;
+    int polarised;
+    const double *total;
+    double *tmp_x, *tmp_y;
+} summary_ctx_t;
+
+/* f, or f(x) + f(total - x) when unpolarised (trees.c:1944-1972) */
+static void summary(summary_ctx_t *c, const double *x, double *y, int unpolarised_wrap)
+{
+    eval_summary(c->K, x, c->n, c->R, c->outs, y);
+    if (unpolarised_wrap) {
+        for (int32_t k = 0; k < c->K; k++) {
+            c->tmp_x[k] = c->total[k] - x[k];
+        }
+        eval_summary(c->K, c->tmp_x, c->n, c->R, c->outs, c->tmp_y);
+        for (int32_t r = 0; r < c->R; r++) {
+            y[r] += c->tmp_y[r];
+        }
+    }
+}
+
+static void span_normalise(int32_t Wn, const double *windows, int64_t row, double *a)
+{
+    for (int32_t w = 0; w < Wn; w++) {
+        double span = windows[w + 1] - windows[w];
+        for (int64_t k = 0; k < row; k++) {
+            a[w * row + k] /= span;
+        }
+    }
+}
+
+/* --------------------------------------------------------- branch sweep */
+static int branch_stat(const orc_ts_t *ts, summary_ctx_t *c, const double *W,
+    int32_t Wn, const double *windows, double *result)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, K = c->K, R = c->R;
+    const int unpol = !c->polarised;
+    int32_t *parent = malloc((size_t) N * sizeof(int32_t));
+    double *bl = calloc((size_t) N, sizeof(double));
+    double *x = calloc((size_t) N * K, sizeof(double));
+    double *s = calloc((size_t) N * R, sizeof(double));
+    double *run = calloc((size_t) R, sizeof(double));
+    double *zero = calloc((size_t) K, sizeof(double));
+    double *fz = calloc((size_t) R, sizeof(double));
+    int ret = ORC_ERR_NO_MEMORY;
+    if (!parent || !bl || !x || !s || !run || !zero || !fz) {
+        goto out;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    summary(c, zero, fz, unpol);
+    for (int32_t u = 0; u < N; u++) {
+        memcpy(s + (int64_t) u * R, fz, (size_t) R * sizeof(double));
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        int32_t u = ts->samples[j];
+        memcpy(x + (int64_t) u * K, W + (int64_t) j * K, (size_t) K * sizeof(double));
+        summary(c, x + (int64_t) u * K, s + (int64_t) u * R, unpol);
+    }
+    memset(result, 0, (size_t) Wn * R * sizeof(double));
+    int32_t tj = 0, tk = 0, w = 0;
+    double left = 0, L = ts->sequence_length;
+    while (tj < E || left < L) {
+        while (tk < E && ts->edge_right[ts->rem[tk]] == left) {
+            int32_t e = ts->rem[tk++];
+            int32_t ch = ts->edge_child[e];
+            for (int32_t r = 0; r < R; r++) {
+                run[r] -= bl[ch] * s[(int64_t) ch * R + r];
+            }
+            parent[ch] = -1;
+            bl[ch] = 0;
+            for (int32_t u = ts->edge_parent[e]; u != -1; u = parent[u]) {
+                double *su = s + (int64_t) u * R;
+                for (int32_t r = 0; r < R; r++) {
+                    run[r] -= bl[u] * su[r];
+                }
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] -= x[(int64_t) ch * K + k];
+                }
+                summary(c, x + (int64_t) u * K, su, unpol);
+                for (int32_t r = 0; r < R; r++) {
+                    run[r] += bl[u] * su[r];
+                }
+            }
+        }
+        while (tj < E && ts->edge_left[ts->ins[tj]] == left) {
+            int32_t e = ts->ins[tj++];
+            int32_t ch = ts->edge_child[e], p = ts->edge_parent[e];
+            parent[ch] = p;
+            bl[ch] = ts->node_time[p] - ts->node_time[ch];
+            for (int32_t r = 0; r < R; r++) {
+                run[r] += bl[ch] * s[(int64_t) ch * R + r];
+            }
+            for (int32_t u = p; u != -1; u = parent[u]) {
+                double *su = s + (int64_t) u * R;
+                for (int32_t r = 0; r < R; r++) {
+                    run[r] -= bl[u] * su[r];
+                }
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] += x[(int64_t) ch * K + k];
+                }
+                summary(c, x + (int64_t) u * K, su, unpol);
+                for (int32_t r = 0; r < R; r++) {
+                    run[r] += bl[u] * su[r];
+                }
+            }
+        }
+        double right = L;
+        if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+            right = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+            right = ts->edge_right[ts->rem[tk]];
+        }
+        while (w < Wn && windows[w] < right) {
+            double a = left > windows[w] ? left : windows[w];
+            double b = right < windows[w + 1] ? right : windows[w + 1];
+            for (int32_t r = 0; r < R; r++) {
+                result[(int64_t) w * R + r] += run[r] * (b - a);
+            }
+            if (windows[w + 1] <= right) {
+                w++;
+            } else {
+                break;
+            }
+        }
+        left = right;
+    }
+    ret = 0;
+out:
+    free(parent);
+    free(bl);
+    free(x);
+    free(s);
+    free(run);
+    free(zero);
+    free(fz);
+    return ret;
+}
+
+/* ----------------------------------------------------------- site sweep */
+/* allele states for one site: states[a*K + k] (trees.c:1525-1612) */
+static int32_t site_allele_states(const orc_ts_t *ts, int32_t m0, int32_t m1,
+    const double *x, int32_t K, const double *total, double *states)
+{
+    int32_t A = 1;
+    for (int32_t m = m0; m < m1; m++) {
+        if (ts->mutation_allele[m] + 1 > A) {
+            A = ts->mutation_allele[m] + 1;
+        }
+    }
+    memset(states, 0, (size_t) A * K * sizeof(double));
+    memcpy(states, total, (size_t) K * sizeof(double));
+    for (int32_t m = m0; m < m1; m++) {
+        const double *xm = x + (int64_t) ts->mutation_node[m] * K;
+        double *sa = states + (int64_t) ts->mutation_allele[m] * K;
+        double *sb = states + (int64_t) ts->mutation_alt[m] * K;
+        for (int32_t k = 0; k < K; k++) {
+            sa[k] += xm[k];
+        }
+        for (int32_t k = 0; k < K; k++) {
+            sb[k] -= xm[k];
+        }
+    }
+    return A;
+}
+
+typedef void (*site_visit_fn)(void *ctx, int32_t site, int32_t m0, int32_t m1,
+    const double *x, const int32_t *parent);
+
+/* Shared tree sweep that keeps x up to date and visits each site. */
+static int site_sweep(const orc_ts_t *ts, int32_t K, const double *Wnode_init,
+    site_visit_fn visit, void *ctx)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges;
+    int32_t *parent = malloc((size_t) N * sizeof(int32_t));
+    double *x = calloc((size_t) N * K, sizeof(double));
+    if (!parent || !x) {
+        free(parent);
+        free(x);
+        return ORC_ERR_NO_MEMORY;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        memcpy(x + (int64_t) ts->samples[j] * K, Wnode_init + (int64_t) j * K,
+            (size_t) K * sizeof(double));
+    }
+    int32_t tj = 0, tk = 0, site = 0, mut = 0;
+    double left = 0, L = ts->sequence_length;
+    while (tj < E || left < L) {
+        while (tk < E && ts->edge_right[ts->rem[tk]] == left) {
+            int32_t e = ts->rem[tk++];
+            int32_t ch = ts->edge_child[e];
+            for (int32_t u = ts->edge_parent[e]; u != -1; u = parent[u]) {
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] -= x[(int64_t) ch * K + k];
+                }
+            }
+            parent[ch] = -1;
+        }
+        while (tj < E && ts->edge_left[ts->ins[tj]] == left) {
+            int32_t e = ts->ins[tj++];
+            int32_t ch = ts->edge_child[e];
+            parent[ch] = ts->edge_parent[e];
+            for (int32_t u = parent[ch]; u != -1; u = parent[u]) {
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] += x[(int64_t) ch * K + k];
+                }
+            }
+        }
+        double right = L;
+        if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+            right = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+            right = ts->edge_right[ts->rem[tk]];
+        }
+        while (site < ts->num_sites && ts->site_position[site] < right) {
+            int32_t m0 = mut;
+            while (mut < ts->num_mutations && ts->mutation_site[mut] == site) {
+                mut++;
+            }
+            visit(ctx, site, m0, mut, x, parent);
+            site++;
+        }
+        left = right;
+    }
+    free(parent);
+    free(x);
+    return 0;
+}
+
+typedef struct {
+    const orc_ts_t *ts;
+    summary_ctx_t *c;
+    const double *windows;
+    int32_t Wn, w;
+    double *result, *states, *y;
+} site_stat_ctx_t;
+
+static void site_stat_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
+    const double *x, const int32_t *parent)
+{
+    (void) parent;
+    site_stat_ctx_t *s = (site_stat_ctx_t *) vctx;
+    summary_ctx_t *c = s->c;
+    const double pos = s->ts->site_position[site];
+    int32_t A = site_allele_states(s->ts, m0, m1, x, c->K, c->total, s->states);
+    while (s->windows[s->w + 1] <= pos) {
+        s->w++;
+    }
+    double *row = s->result + (int64_t) s->w * c->R;
+    /* accumulate the per-site result first, as trees.c:1614-1652 does */
+    double *acc = s->y + c->R;
+    memset(acc, 0, (size_t) c->R * sizeof(double));
+    for (int32_t a = c->polarised ? 1 : 0; a < A; a++) {
+        eval_summary(c->K, s->states + (int64_t) a * c->K, c->n, c->R, c->outs, s->y);
+        for (int32_t r = 0; r < c->R; r++) {
+            acc[r] += s->y[r];
+        }
+    }
+    for (int32_t r = 0; r < c->R; r++) {
+        row[r] += acc[r];
+    }
+}
+
+/*
+ * Sample-count statistic (tsk_treeseq_sample_count_stat + general_stat).
+ * W: num_samples x K weights indexed by sample order; n: K set sizes.
+ * windows: Wn+1 breakpoints.  result: Wn x R.
+ */
+int orc_sample_count_stat(const orc_ts_t *ts, int32_t K, const double *W,
+    const double *n, int32_t R, const orc_output_t *outs, int32_t Wn,
+    const double *windows, uint32_t options, double *result)
+{
+    int ret;
+    summary_ctx_t c;
+    double *total = calloc((size_t) K, sizeof(double));
+    double *tmp = calloc((size_t) (K + 2 * R + 8), sizeof(double));
+    if (!total || !tmp) {
+        free(total);
+        free(tmp);
+        return ORC_ERR_NO_MEMORY;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        for (int32_t k = 0; k < K; k++) {
+            total[k] += W[(int64_t) j * K + k];
+        }
+    }
+    c.K = K;
+    c.R = R;
+    c.n = n;
+    c.outs = outs;
+    c.polarised = !!(options & ORC_STAT_POLARISED);
+    c.total = total;
+    c.tmp_x = tmp;
+    c.tmp_y = tmp + K;
+    if (options & ORC_STAT_BRANCH) {
+        ret = branch_stat(ts, &c, W, Wn, windows, result);
+    } else {
+        site_stat_ctx_t s;
+        int32_t max_alleles = 2;
+        for (int32_t m = 0; m < ts->num_mutations; m++) {
+            if (ts->mutation_allele[m] + 1 > max_alleles) {
+                max_alleles = ts->mutation_allele[m] + 1;
+            }
+        }
+        s.ts = ts;
+        s.c = &c;
+        s.windows = windows;
+        s.Wn = Wn;
+        s.w = 0;
+        s.result = result;
+        s.states = calloc((size_t) max_alleles * K, sizeof(double));
+        s.y = calloc((size_t) 2 * R, sizeof(double));
+        memset(result, 0, (size_t) Wn * R * sizeof(double));
+        ret = (!s.states || !s.y) ? ORC_ERR_NO_MEMORY
+                                  : site_sweep(ts, K, W, site_stat_visit, &s);
+        free(s.states);
+        free(s.y);
+    }
+    if (ret == 0 && (options & ORC_STAT_SPAN_NORMALISE)) {
+        span_normalise(Wn, windows, R, result);
+    }
+    free(total);
+    free(tmp);
+    return ret;
+}
+
+/* ------------------------------------------------------------------ AFS */
+/* fold a coordinate (trees.c:3469-3496) */
+static void afs_fold(int64_t *coord, const int64_t *dims, int32_t K)
+{
+    double n = 0;
+    int64_t s = 0;
+    for (int32_t k = 0; k < K; k++) {
+        n += (double) dims[k] - 1;
+        s += coord[k];
+    }
+    n /= 2;
+    int32_t k = K;
+    while ((double) s == n && k > 0) {
+        k--;
+        n -= ((double) (dims[k] - 1)) / 2;
+        s -= coord[k];
+    }
+    if ((double) s > n) {
+        for (k = 0; k < K; k++) {
+            coord[k] = dims[k] - 1 - coord[k];
+        }
+    }
+}
+
+static int64_t afs_index(const int64_t *coord, const int64_t *dims, int32_t K)
+{
+    int64_t idx = 0;
+    for (int32_t k = 0; k < K; k++) {
+        idx = idx * dims[k] + coord[k];
+    }
+    return idx;
+}
+
+typedef struct {
+    const orc_ts_t *ts;
+    int32_t K; /* number of sample sets; state has K+1 columns */
+    const int64_t *dims;
+    int64_t afs_size;
+    const double *windows;
+    int32_t Wn, w;
+    int polarised;
+    double *result, *states, *total;
+    int64_t *coord;
+} site_afs_ctx_t;
+
+static void site_afs_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
+    const double *x, const int32_t *parent)
+{
+    (void) parent;
+    site_afs_ctx_t *s = (site_afs_ctx_t *) vctx;
+    const int32_t K1 = s->K + 1;
+    const double pos = s->ts->site_position[site];
+    while (s->windows[s->w + 1] <= pos) {
+        s->w++;
+    }
+    int32_t A = site_allele_states(s->ts, m0, m1, x, K1, s->total, s->states);
+    double inc = s->polarised ? 1.0 : 0.5;
+    double *afs = s->result + (int64_t) s->w * s->afs_size;
+    for (int32_t a = s->polarised ? 1 : 0; a < A; a++) {
+        const double *st = s->states + (int64_t) a * K1;
+        int64_t all = (int64_t) st[s->K];
+        if (all > 0 && all < s->ts->num_samples) {
+            for (int32_t k = 0; k < s->K; k++) {
+                s->coord[k] = (int64_t) st[k];
+            }
+            if (!s->polarised) {
+                afs_fold(s->coord, s->dims, s->K);
+            }
+            afs[afs_index(s->coord, s->dims, s->K)] += inc;
+        }
+    }
+}
+
+/* lazy per-node flush of branch AFS (trees.c:3650-3694) */
+static void branch_afs_flush(const orc_ts_t *ts, int32_t u, double right,
+    double *last, const int32_t *parent, const double *x, int32_t K,
+    const int64_t *dims, int64_t afs_size, int32_t TW, const double *tw, int32_t w,
+    int polarised, int64_t *coord, double *result)
+{
+    const double *row = x + (int64_t) u * (K + 1);
+    int64_t all = (int64_t) row[K];
+    if (parent[u] != -1 && all > 0 && all < ts->num_samples) {
+        double tu = ts->node_time[u], tv = ts->node_time[parent[u]];
+        for (int32_t t = 0; t < TW && tw[t] < tv; t++) {
+            for (int32_t k = 0; k < K; k++) {
+                coord[k] = (int64_t) row[k];
+            }
+            if (!polarised) {
+                afs_fold(coord, dims, K);
+            }
+            double hi = tw[t + 1] < tv ? tw[t + 1] : tv;
+            double lo = tw[t] > tu ? tw[t] : tu;
+            double bl = hi - lo > 0 ? hi - lo : 0;
+            result[((int64_t) w * TW + t) * afs_size + afs_index(coord, dims, K)]
+                += (right - last[u]) * bl;
+        }
+    }
+    last[u] = right;
+}
+
+/*
+ * Allele frequency spectrum.  sets: concatenated sample node ids with
+ * set_sizes[K].  Result: Wn x TW x prod(set_sizes + 1).
+ */
+int orc_afs(const orc_ts_t *ts, int32_t K, const int64_t *set_sizes,
+    const int32_t *sets, int32_t Wn, const double *windows, int32_t TW,
+    const double *time_windows, uint32_t options, double *result)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, K1 = K + 1;
+    const int polarised = !!(options & ORC_STAT_POLARISED);
+    int64_t *dims = malloc((size_t) K * sizeof(int64_t));
+    int64_t *coord = malloc((size_t) K * sizeof(int64_t));
+    double *x = calloc((size_t) N * K1, sizeof(double));
+    int ret = ORC_ERR_NO_MEMORY;
+    int64_t afs_size = 1;
+    if (!dims || !coord || !x) {
+        goto out;
+    }
+    {
+        int64_t j = 0;
+        for (int32_t k = 0; k < K; k++) {
+            dims[k] = set_sizes[k] + 1;
+            afs_size *= dims[k];
+            for (int64_t l = 0; l < set_sizes[k]; l++) {
+                x[(int64_t) sets[j++] * K1 + k] = 1;
+            }
+        }
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        x[(int64_t) ts->samples[j] * K1 + K] = 1;
+    }
+    memset(result, 0, (size_t) Wn * TW * afs_size * sizeof(double));
+    if (options & ORC_STAT_BRANCH) {
+        int32_t *parent = malloc((size_t) N * sizeof(int32_t));
+        double *last = calloc((size_t) N, sizeof(double));
+        if (!parent || !last) {
+            free(parent);
+            free(last);
+            goto out;
+        }
+        for (int32_t u = 0; u < N; u++) {
+            parent[u] = -1;
+        }
+        int32_t tj = 0, tk = 0, w = 0;
+        double left = 0, L = ts->sequence_length;
+        while (tj < E || left < L) {
+            while (tk < E && ts->edge_right[ts->rem[tk]] == left) {
+                int32_t e = ts->rem[tk++];
+                int32_t ch = ts->edge_child[e];
+                branch_afs_flush(ts, ch, left, last, parent, x, K, dims, afs_size, TW,
+                    time_windows, w, polarised, coord, result);
+                for (int32_t v = ts->edge_parent[e]; v != -1; v = parent[v]) {
+                    branch_afs_flush(ts, v, left, last, parent, x, K, dims, afs_size,
+                        TW, time_windows, w, polarised, coord, result);
+                    for (int32_t k = 0; k < K1; k++) {
+                        x[(int64_t) v * K1 + k] -= x[(int64_t) ch * K1 + k];
+                    }
+                }
+                parent[ch] = -1;
+            }
+            while (tj < E && ts->edge_left[ts->ins[tj]] == left) {
+                int32_t e = ts->ins[tj++];
+                int32_t ch = ts->edge_child[e];
+                parent[ch] = ts->edge_parent[e];
+                for (int32_t v = parent[ch]; v != -1; v = parent[v]) {
+                    branch_afs_flush(ts, v, left, last, parent, x, K, dims, afs_size,
+                        TW, time_windows, w, polarised, coord, result);
+                    for (int32_t k = 0; k < K1; k++) {
+                        x[(int64_t) v * K1 + k] += x[(int64_t) ch * K1 + k];
+                    }
+                }
+            }
+            double right = L;
+            if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+                right = ts->edge_left[ts->ins[tj]];
+            }
+            if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+                right = ts->edge_right[ts->rem[tk]];
+            }
+            while (w < Wn && windows[w + 1] <= right) {
+                for (int32_t u = 0; u < N; u++) {
+                    branch_afs_flush(ts, u, windows[w + 1], last, parent, x, K, dims,
+                        afs_size, TW, time_windows, w, polarised, coord, result);
+                }
+                w++;
+            }
+            left = right;
+        }
+        free(parent);
+        free(last);
+        ret = 0;
+    } else {
+        site_afs_ctx_t s;
+        int32_t max_alleles = 2;
+        for (int32_t m = 0; m < ts->num_mutations; m++) {
+            if (ts->mutation_allele[m] + 1 > max_alleles) {
+                max_alleles = ts->mutation_allele[m] + 1;
+            }
+        }
+        s.ts = ts;
+        s.K = K;
+        s.dims = dims;
+        s.afs_size = afs_size;
+        s.windows = windows;
+        s.Wn = Wn;
+        s.w = 0;
+        s.polarised = polarised;
+        s.result = result;
+        s.states = calloc((size_t) max_alleles * K1, sizeof(double));
+        s.total = calloc((size_t) K1, sizeof(double));
+        s.coord = coord;
+        if (!s.states || !s.total) {
+            free(s.states);
+            free(s.total);
+            goto out;
+        }
+        for (int32_t k = 0; k < K; k++) {
+            s.total[k] = (double) set_sizes[k];
+        }
+        s.total[K] = (double) ts->num_samples;
+        /* the sweep wants weights by sample order: gather them from x */
+        double *Wsamp = malloc((size_t) ts->num_samples * K1 * sizeof(double));
+        if (!Wsamp) {
+            free(s.states);
+            free(s.total);
+            goto out;
+        }
+        for (int32_t j = 0; j < ts->num_samples; j++) {
+            memcpy(Wsamp + (int64_t) j * K1, x + (int64_t) ts->samples[j] * K1,
+                (size_t) K1 * sizeof(double));
+        }
+        ret = site_sweep(ts, K1, Wsamp, site_afs_visit, &s);
+        free(Wsamp);
+        free(s.states);
+        free(s.total);
+    }
+    if (ret == 0 && (options & ORC_STAT_SPAN_NORMALISE)) {
+        span_normalise(Wn, windows, afs_size * TW, result);
+    }
+out:
+    free(dims);
+    free(coord);
+    free(x);
+    return ret;
+}
+
+/* ------------------------------------------------- relatedness matvec */
+/*
+ * Branch-mode genetic relatedness times a weight matrix
+ * (tsk_treeseq_genetic_relatedness_vector, trees.c:10402-10816), restated
+ * with the same lazy per-node accumulation.  W: num_samples x nw.
+ * focal: num_focal node ids.  result: Wn x num_focal x nw.
+ */
+int orc_relatedness_vector(const orc_ts_t *ts, int32_t nw, const double *W, int32_t Wn,
+    const double *windows, int32_t num_focal, const int32_t *focal, uint32_t options,
+    double *result)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, n = ts->num_samples;
+    const double *t = ts->node_time;
+    int32_t *parent = malloc((size_t) N * sizeof(int32_t));
+    double *xl = calloc((size_t) N, sizeof(double));
+    double *v = calloc((size_t) N * nw, sizeof(double));
+    double *w = calloc((size_t) N * nw, sizeof(double));
+    double *mean = calloc((size_t) nw, sizeof(double));
+    int ret = ORC_ERR_NO_MEMORY;
+    if (!parent || !xl || !v || !w || !mean) {
+        goto out;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    memset(result, 0, (size_t) Wn * num_focal * nw * sizeof(double));
+    if (!(options & ORC_STAT_NONCENTRED)) {
+        for (int32_t j = 0; j < n; j++) {
+            for (int32_t k = 0; k < nw; k++) {
+                mean[k] += W[(int64_t) j * nw + k];
+            }
+        }
+        for (int32_t k = 0; k < nw; k++) {
+            mean[k] /= (double) n;
+        }
+    }
+    for (int32_t j = 0; j < n; j++) {
+        for (int32_t k = 0; k < nw; k++) {
+            w[(int64_t) ts->samples[j] * nw + k] = W[(int64_t) j * nw + k] - mean[k];
+        }
+    }
+    double pos = windows[0];
+#define ADD_Z(u)                                                                        \
+    do {                                                                                \
+        int32_t _u = (u);                                                               \
+        if (parent[_u] != -1) {                                                         \
+            double _f = (t[parent[_u]] - t[_u]) * (pos - xl[_u]);                       \
+            for (int32_t k = 0; k < nw; k++) {                                          \
+                v[(int64_t) _u * nw + k] += _f * w[(int64_t) _u * nw + k];              \
+            }                                                                           \
+        }                                                                               \
+        xl[_u] = pos;                                                                   \
+    } while (0)
+#define ADJUST_UP(p0, c0, sign)                                                          \
+    do {                                                                                \
+        for (int32_t _p = (p0); _p != -1; _p = parent[_p]) {                            \
+            ADD_Z(_p);                                                                  \
+            for (int32_t k = 0; k < nw; k++) {                                          \
+                v[(int64_t) (c0) *nw + k] -= (sign) *v[(int64_t) _p * nw + k];          \
+                w[(int64_t) _p * nw + k] += (sign) *w[(int64_t) (c0) *nw + k];          \
+            }                                                                           \
+        }                                                                               \
+    } while (0)
+    /* position the tree at windows[0]: apply all edges covering it */
+    int32_t tj = 0, tk = 0;
+    while (tj < E && ts->edge_left[ts->ins[tj]] <= pos) {
+        int32_t e = ts->ins[tj++];
+        if (pos < ts->edge_right[e]) {
+            int32_t p = ts->edge_parent[e], c = ts->edge_child[e];
+            ADJUST_UP(p, c, +1.0);
+            xl[c] = pos;
+            parent[c] = p;
+        }
+    }
+    while (tk < E && ts->edge_right[ts->rem[tk]] <= pos) {
+        tk++;
+    }
+    for (int32_t m = 0; m < Wn;) {
+        /* apply removals and insertions at pos */
+        while (tk < E && ts->edge_right[ts->rem[tk]] == pos) {
+            int32_t e = ts->rem[tk++];
+            int32_t p = ts->edge_parent[e], c = ts->edge_child[e];
+            ADD_Z(c);
+            parent[c] = -1;
+            ADJUST_UP(p, c, -1.0);
+        }
+        while (tj < E && ts->edge_left[ts->ins[tj]] == pos) {
+            int32_t e = ts->ins[tj++];
+            int32_t p = ts->edge_parent[e], c = ts->edge_child[e];
+            ADJUST_UP(p, c, +1.0);
+            xl[c] = pos;
+            parent[c] = p;
+        }
+        double next = windows[m + 1];
+        if (tj < E && ts->edge_left[ts->ins[tj]] < next) {
+            next = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < next) {
+            next = ts->edge_right[ts->rem[tk]];
+        }
+        pos = next;
+        if (pos == windows[m + 1]) {
+            double *y = result + (int64_t) m * num_focal * nw;
+            for (int32_t j = 0; j < num_focal; j++) {
+                for (int32_t u = focal[j]; u != -1; u = parent[u]) {
+                    if (xl[u] != pos) {
+                        ADD_Z(u);
+                    }
+                    for (int32_t k = 0; k < nw; k++) {
+                        y[(int64_t) j * nw + k] += v[(int64_t) u * nw + k];
+                    }
+                }
+            }
+            if (!(options & ORC_STAT_NONCENTRED)) {
+                for (int32_t k = 0; k < nw; k++) {
+                    double s = 0;
+                    for (int32_t j = 0; j < num_focal; j++) {
+                        s += y[(int64_t) j * nw + k];
+                    }
+                    s /= (double) num_focal;
+                    for (int32_t j = 0; j < num_focal; j++) {
+                        y[(int64_t) j * nw + k] -= s;
+                    }
+                }
+            }
+            memset(v, 0, (size_t) N * nw * sizeof(double));
+            m++;
+        }
+    }
+#undef ADD_Z
+#undef ADJUST_UP
+    if (options & ORC_STAT_SPAN_NORMALISE) {
+        span_normalise(Wn, windows, (int64_t) num_focal * nw, result);
+    }
+    ret = 0;
+out:
+    free(parent);
+    free(xl);
+    free(v);
+    free(w);
+    free(mean);
+    return ret;
+}
+
+/* ------------------------------------------------------ genotype matrix */
+typedef struct {
+    const orc_ts_t *ts;
+    const int32_t *latest; /* scratch: latest mutation index per node, -1 */
+    int32_t *mut_at_node;
+    int8_t *G;             /* num_sites x num_samples */
+} geno_ctx_t;
+
+static void geno_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
+    const double *x, const int32_t *parent)
+{
+    (void) x;
+    geno_ctx_t *g = (geno_ctx_t *) vctx;
+    const orc_ts_t *ts = g->ts;
+    for (int32_t m = m0; m < m1; m++) {
+        g->mut_at_node[ts->mutation_node[m]] = m;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        int32_t a = 0;
+        for (int32_t u = ts->samples[j]; u != -1; u = parent[u]) {
+            if (g->mut_at_node[u] >= m0 && g->mut_at_node[u] < m1) {
+                a = ts->mutation_allele[g->mut_at_node[u]];
+                break;
+            }
+        }
+        g->G[(int64_t) site * ts->num_samples + j] = (int8_t) a;
+    }
+    for (int32_t m = m0; m < m1; m++) {
+        g->mut_at_node[ts->mutation_node[m]] = -1;
+    }
+}
+
+/*
+ * Allele index per (site, sample): the allele of the nearest mutation above
+ * the sample at the site (later mutations on the same node win), 0 if none
+ * (c/tskit/genotypes.c, decoding with isolated samples not missing).
+ */
+int orc_genotype_matrix(const orc_ts_t *ts, int8_t *G)
+{
+    geno_ctx_t g;
+    int32_t *mut_at_node = malloc((size_t) ts->num_nodes * sizeof(int32_t));
+    double *Wz = calloc((size_t) ts->num_samples, sizeof(double));
+    int ret;
+    if (!mut_at_node || !Wz) {
+        free(mut_at_node);
+        free(Wz);
+        return ORC_ERR_NO_MEMORY;
+    }
+    for (int32_t u = 0; u < ts->num_nodes; u++) {
+        mut_at_node[u] = -1;
+    }
+    g.ts = ts;
+    g.latest = NULL;
+    g.mut_at_node = mut_at_node;
+    g.G = G;
+    ret = site_sweep(ts, 1, Wz, geno_visit, &g);
+    free(mut_at_node);
+    free(Wz);
+    return ret;
+}
