@@ -1,0 +1,539 @@
+"""Benchmark: batched windowed tree-sequence statistics on one GB300.
+
+Workload "windowed_n10k": a seeded SMC tree sequence with n=10,000 samples,
+L=1e8 and 100,000 breakpoints (~5 sites per breakpoint), four disjoint random
+sample sets of 2,500 and 1,000 equal windows.  One step computes diversity
+(4 sets), divergence (6 pairs), Fst (6 pairs), Tajima's D (4 sets) and Y3
+(4 triples) in both branch and site modes with span normalisation, as ONE
+fused sweep (FP32-Kahan bulk, FP64 windows).
+
+Metric: edge-updates/s, counted as the reference runs the same queries: each
+low-level call is one traversal applying every edge insertion and removal
+(diversity 1, divergence 1, Fst 2, Tajima's D 2, Y3 1 traversal per mode; 14
+in all).  `value` is measured with the tree sequence and the prepared query
+resident in HBM; `e2e` goes through the C ABI host-pointer entry point with
+host inputs and a host result.  L2 is flushed (256 MiB write) before every
+timed step.
+
+--impl reference times the reference's CPU implementation of the same
+queries on the host cores (the C oracle restatement when the reference
+library cannot be built on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOAD = "windowed_n10k"
+NUM_SETS = 4
+NUM_WINDOWS = 1000
+# per mode: diversity 1, divergence 1, Fst 2, Tajima's D 2, Y3 1 traversals
+REFERENCE_TRAVERSALS_PER_MODE = 7
+MODES = ("branch", "site")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload():
+    from tskit_gb300 import sim
+
+    tables = sim.workload(WORKLOAD)
+    rng = np.random.default_rng(sim.WORKLOADS[WORKLOAD]["seed"] + 1)
+    perm = rng.permutation(tables.samples())
+    size = tables.num_samples if hasattr(tables, "num_samples") else len(tables.samples())
+    k = len(perm) // NUM_SETS
+    sets = [np.sort(perm[j * k:(j + 1) * k]).astype(np.int32) for j in range(NUM_SETS)]
+    del size
+    windows = np.linspace(0, tables.sequence_length, NUM_WINDOWS + 1)
+    return tables, sets, windows
+
+
+def term_list():
+    from tskit_gb300 import _native as nat
+
+    pairs = [(i, j) for i in range(NUM_SETS) for j in range(i + 1, NUM_SETS)]
+    triples = [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
+    terms = [(nat.DIVERSITY, (k,)) for k in range(NUM_SETS)]
+    terms += [(nat.SEGREGATING_SITES, (k,)) for k in range(NUM_SETS)]
+    terms += [(nat.DIVERGENCE, p) for p in pairs]
+    terms += [(nat.Y3, t) for t in triples]
+    return terms, pairs, triples
+
+
+def edge_events(tables):
+    return int(tables.num_edges + np.count_nonzero(tables.edge_right < tables.sequence_length))
+
+
+def algorithmic_bytes(tables, sets, num_terms):
+    """Compulsory HBM bytes of one fused both-mode traversal."""
+    E, N, S, M = tables.num_edges, tables.num_nodes, tables.num_sites, tables.num_mutations
+    return (32 * E + 12 * N + 8 * S + 13 * M + 4 * sum(len(s) for s in sets)
+            + 8 * NUM_WINDOWS * num_terms * 2)
+
+
+def finish(raw, windows, sets, pairs):
+    """Derived statistics from the fused raw (not span-normalised) terms."""
+    span = np.diff(windows)[:, None]
+    K = NUM_SETS
+    out = {}
+    for m, mode in enumerate(MODES):
+        r = raw[m]
+        div, seg = r[:, :K] / span, r[:, K:2 * K]
+        dvg = r[:, 2 * K:2 * K + len(pairs)] / span
+        y3 = r[:, 2 * K + len(pairs):] / span
+        fst = np.ones_like(dvg)
+        for i, (u, v) in enumerate(pairs):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                fst[:, i] -= 2 * (div[:, u] + div[:, v]) / (div[:, u] + div[:, v] + 2 * dvg[:, i])
+        n = np.array([len(s) for s in sets], dtype=np.float64)
+        T = r[:, :K]
+        h = np.array([np.sum(1 / np.arange(1, nn)) for nn in n])
+        g = np.array([np.sum(1 / np.arange(1, nn) ** 2) for nn in n])
+        with np.errstate(invalid="ignore", divide="ignore"):
+            a = (n + 1) / (3 * (n - 1) * h) - 1 / h**2
+            b = 2 * (n**2 + n + 3) / (9 * n * (n - 1)) - (n + 2) / (h * n) + g / h**2
+            tajd = (T - seg / h) / np.sqrt(a * seg + (b / (h**2 + g)) * seg * (seg - 1))
+        out[mode] = dict(diversity=div, divergence=dvg, Fst=fst, Tajimas_D=tajd, Y3=y3)
+    return out
+
+
+def rel_err(got, exp):
+    """Max over entries of |got-exp| relative to the magnitude of each statistic
+    column (entries near zero are measured against the column's scale)."""
+    got, exp = np.asarray(got), np.asarray(exp)
+    scale = np.maximum(np.abs(exp), 1e-6 * np.nanmax(np.abs(exp), axis=0, keepdims=True))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        e = np.abs(got - exp) / scale
+    return float(np.nanmax(e)) if e.size else 0.0
+
+
+# --------------------------------------------------------------- CPU side
+def _oracle_queries(ots, sets, windows, pairs, triples):
+    """The reference's decomposition of the workload: one traversal per
+    low-level call, unnormalised raw terms (Fst and Tajima's D reuse them)."""
+    import oracle as O
+
+    calls = []
+    for mode in MODES:
+        calls.append((mode, "diversity", [(O.DIVERSITY, (k,)) for k in range(NUM_SETS)]))
+        calls.append((mode, "divergence", [(O.DIVERGENCE, p) for p in pairs]))
+        calls.append((mode, "Fst.divergence", [(O.DIVERGENCE, p) for p in pairs]))
+        calls.append((mode, "Fst.diversity", [(O.DIVERSITY, (k,)) for k in range(NUM_SETS)]))
+        calls.append((mode, "TajD.diversity", [(O.DIVERSITY, (k,)) for k in range(NUM_SETS)]))
+        calls.append((mode, "TajD.segsites", [(O.SEGSITES, (k,)) for k in range(NUM_SETS)]))
+        calls.append((mode, "Y3", [(O.Y3, t) for t in triples]))
+    return calls
+
+
+_worker_state = {}
+
+
+def _worker_init(npz_path):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from tskit_gb300.tables import Tables
+
+    data = np.load(npz_path)
+    tables = Tables.from_npz(data, prefix="tables/")
+    _worker_state["ots"] = O.OracleTS(tables)
+    _worker_state["sets"] = [data[f"set{k}"] for k in range(NUM_SETS)]
+    _worker_state["windows"] = data["windows"]
+
+
+def _worker_run(call):
+    import oracle as O
+
+    mode, _, terms = call
+    t0 = time.perf_counter()
+    r = O.sample_count_stat(_worker_state["ots"], _worker_state["sets"], terms,
+                            windows=_worker_state["windows"], mode=mode, span_normalise=False)
+    return time.perf_counter() - t0, r
+
+
+def cpu_oracle_run(tables, sets, windows, pairs, triples):
+    """Single-core oracle over the whole workload; returns (seconds, raw)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    ots = O.OracleTS(tables)
+    calls = _oracle_queries(ots, sets, windows, pairs, triples)
+    t0 = time.perf_counter()
+    outs = {}
+    for mode, name, terms in calls:
+        outs[(mode, name)] = O.sample_count_stat(ots, sets, terms, windows=windows, mode=mode,
+                                                 span_normalise=False)
+    dt = time.perf_counter() - t0
+    raw = np.zeros((2, NUM_WINDOWS, 2 * NUM_SETS + len(pairs) + len(triples)))
+    for m, mode in enumerate(MODES):
+        raw[m] = np.concatenate([outs[(mode, "diversity")], outs[(mode, "TajD.segsites")],
+                                 outs[(mode, "divergence")], outs[(mode, "Y3")]], axis=1)
+    return dt, raw, len(calls)
+
+
+def run_reference(args):
+    """--impl reference: the CPU path with all host threads, rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import tempfile
+
+    tables, sets, windows = make_workload()
+    terms, pairs, triples = term_list()
+    events = edge_events(tables)
+    logical = events * REFERENCE_TRAVERSALS_PER_MODE * len(MODES)
+    kind = "port"
+    tmp = tempfile.NamedTemporaryFile(suffix=".npz", delete=False)
+    arrays = tables.save_npz_dict("tables/")
+    for k, s in enumerate(sets):
+        arrays[f"set{k}"] = s
+    arrays["windows"] = windows
+    np.savez(tmp.name, **arrays)
+    cores = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    calls = _oracle_queries(O.OracleTS(tables), sets, windows, pairs, triples)
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(min(cores, len(calls)), initializer=_worker_init, initargs=(tmp.name,)) as pool:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_worker_run, calls, chunksize=1)
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                times.append(dt)
+    os.unlink(tmp.name)
+    ms = 1e3 * float(np.mean(times))
+    value = logical / (ms / 1e3)
+    line = {
+        "impl": "reference",
+        "metric": "edge-updates/s",
+        "value": value,
+        "unit": "edge-updates/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded SMC generator)",
+        "config": workload_config(tables),
+        "cpu_baseline": {
+            "value": value, "unit": "edge-updates/s", "cores": min(cores, len(calls)),
+            "kind": kind,
+            "sample": f"the full workload ({len(calls)} single-stat traversals, as the "
+                      "reference runs them) spread over a process pool, one traversal per task",
+        },
+        "e2e": {"value": value, "unit": "edge-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config(tables):
+    return {
+        "workload": f"{WORKLOAD}: batched windowed stats, n=10000 samples, L=1e8, 100000 "
+                    f"breakpoints -> {tables.num_edges} edges, {tables.num_sites} sites; "
+                    f"{NUM_SETS} disjoint sets of 2500, {NUM_WINDOWS} windows; diversity, "
+                    "divergence (6 pairs), Fst (6 pairs), Tajima's D, Y3 (4 triples); branch "
+                    "and site modes",
+        "num_edges": int(tables.num_edges),
+        "num_nodes": int(tables.num_nodes),
+        "num_sites": int(tables.num_sites),
+        "num_samples": int(len(tables.samples())),
+        "l2": "flushed between timed steps (256 MiB write)",
+        "traversals_counted_per_step": REFERENCE_TRAVERSALS_PER_MODE * len(MODES),
+    }
+
+
+# --------------------------------------------------------------- GPU side
+class ClockSampler:
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(REPO, ".cache", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 7:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[3:7]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except FileNotFoundError:
+            pass
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "sweep_windowed_n10k.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def run_gpu(args):
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _build, _native as nat
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    _build.build_all()
+    lib = nat.load()
+
+    tables, sets, windows = make_workload()
+    terms, pairs, triples = term_list()
+    events = edge_events(tables)
+    traversals = REFERENCE_TRAVERSALS_PER_MODE * len(MODES)
+    logical = events * traversals
+
+    ts = tskit_gb300.TreeSequence(tables)
+    q = ts.query(sets, terms, windows=windows, both_modes=True, span_normalise=False,
+                 precision="f32")
+    ws = tskit_gb300.Workspace(q.workspace_bytes)
+    res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ev_sweep0, ev_sweep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        q.launch(ws, res, stream)
+    torch.cuda.synchronize()
+    q.check(ws)
+
+    step_ms, sweep_ms = [], []
+    launches0 = lib.tsg_launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            q.launch(ws, res, stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            sweep_ms.append(ev_sweep0.elapsed_time(ev_sweep1))
+        torch.cuda.synchronize()
+    launches = (lib.tsg_launch_count() - launches0) / args.steps
+    q.check(ws)
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * logical / (ms / 1e3)
+    raw_batched = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
+
+    # plain FP64 per-query form: one launch per low-level call, FP64 throughout
+    plain = []
+    for mode in MODES:
+        for name, tl in (("diversity", terms[:NUM_SETS]),
+                         ("divergence", terms[2 * NUM_SETS:2 * NUM_SETS + len(pairs)]),
+                         ("Fst.divergence", terms[2 * NUM_SETS:2 * NUM_SETS + len(pairs)]),
+                         ("Fst.diversity", terms[:NUM_SETS]),
+                         ("TajD.diversity", terms[:NUM_SETS]),
+                         ("TajD.segsites", terms[NUM_SETS:2 * NUM_SETS]),
+                         ("Y3", terms[2 * NUM_SETS + len(pairs):])):
+            pq = ts.query(sets, tl, windows=windows, mode=mode, span_normalise=False,
+                          precision="f64")
+            pres = torch.zeros(pq.result_size, dtype=torch.float64, device="cuda")
+            plain.append((mode, name, pq, pres))
+    pws = tskit_gb300.Workspace(max(p[2].workspace_bytes for p in plain))
+    for _, _, pq, pres in plain:
+        pq.launch(pws, pres, stream)
+    torch.cuda.synchronize()
+    plain_ms = []
+    for _ in range(max(1, min(args.steps, 5))):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _, _, pq, pres in plain:
+            pq.launch(pws, pres, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain_step_ms = float(np.mean(plain_ms))
+    pout = {(m, n): r.cpu().numpy().reshape(NUM_WINDOWS, -1) for m, n, _, r in plain}
+    raw_plain = np.zeros_like(raw_batched)
+    for m, mode in enumerate(MODES):
+        raw_plain[m] = np.concatenate([pout[(mode, "diversity")], pout[(mode, "TajD.segsites")],
+                                       pout[(mode, "divergence")], pout[(mode, "Y3")]], axis=1)
+
+    # e2e through the host-pointer C ABI: host sample sets/windows in, host result out
+    flags = nat.STAT_BOTH_MODES | nat.PRECISION_F32_KAHAN
+    sizes = np.array([len(s) for s in sets], dtype=np.uint64)
+    flat = np.concatenate(sets).astype(np.int32)
+    e2e_ms = []
+    for j in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host = ts._ll_terms(terms, sizes, flat, windows, None, False, False, extra=flags)
+        dt = time.perf_counter() - t0
+        if j >= args.warmup:
+            e2e_ms.append(dt * 1e3)
+    e2e_value = world * logical / (float(np.mean(e2e_ms)) / 1e3)
+    h2d = int(sizes.nbytes + flat.nbytes + windows.nbytes + ts.num_samples * 4)
+    d2h = int(host.nbytes)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    peaks, peak_kind = measured_peaks()
+    sweep = float(np.mean(sweep_ms))
+    algo = algorithmic_bytes(tables, sets, len(terms))
+    achieved = algo / (sweep / 1e3) / 1e9
+    line = {
+        "metric": "edge-updates/s",
+        "value": value,
+        "unit": "edge-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-kahan bulk, f64 windows; int32 counts",
+        "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
+        "config": workload_config(tables),
+        "queries_per_s": world * traversals / (ms / 1e3),
+        "physical_edge_updates_per_s": world * events / (ms / 1e3),
+        "plain_fp64": {
+            "ms_per_step": plain_step_ms,
+            "value": world * logical / (plain_step_ms / 1e3),
+            "launches": len(plain),
+            "speedup_batched_vs_plain": plain_step_ms / ms,
+        },
+        "e2e": {"value": e2e_value, "unit": "edge-updates/s", "ms_per_step": float(np.mean(e2e_ms)),
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peaks["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"],
+            "traffic": profile_traffic(),
+            "kernel": "k_sweep<float>",
+            "algorithmic_bytes_per_launch": algo,
+            "kernel_ms": sweep,
+            "peak_source": peak_kind,
+        },
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    # error of the batched FP32-Kahan form and of the plain FP64 form
+    if not args.no_cpu_baseline:
+        cpu_s, raw_oracle, ncalls = cpu_oracle_run(tables, sets, windows, pairs, triples)
+        line["cpu_baseline"] = {
+            "value": logical / cpu_s, "unit": "edge-updates/s", "cores": 1, "kind": "port",
+            "sample": f"the full workload: {ncalls} single-stat traversals of the C oracle "
+                      "(restated reference algorithm), one core",
+        }
+        fin_b, fin_p, fin_o = (finish(r, windows, sets, pairs)
+                               for r in (raw_batched, raw_plain, raw_oracle))
+        err = {}
+        for mode in MODES:
+            for stat in fin_o[mode]:
+                err[f"{mode}.{stat}.batched_f32k"] = rel_err(fin_b[mode][stat], fin_o[mode][stat])
+                err[f"{mode}.{stat}.plain_f64"] = rel_err(fin_p[mode][stat], fin_o[mode][stat])
+        line["error_vs_fp64_oracle"] = err
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,247 @@
+/*
+ * tskit_gb300: GPU (sm_103a) tree-sequence statistics behind a C ABI.
+ *
+ * The entry points mirror the reference C library's statistics functions
+ * (c/tskit/trees.h) one for one: same argument order and meaning, the same
+ * TSK_STAT_* option bits, the same negative TSK_ERR_* return codes for the
+ * same conditions, caller-allocated results that are zeroed and filled.  The
+ * tree sequence itself is device resident (tsg_treeseq_t, built once by
+ * tsg_treeseq_init) in place of the reference's host tsk_treeseq_t.
+ *
+ * Host-pointer entry points (tsg_treeseq_<stat>) take host arrays and a host
+ * result, exactly as the reference does, and synchronise before returning.
+ * The device-resident query interface (tsg_query_*) takes device arrays, a
+ * workspace and a CUDA stream and does not synchronise; it is what the
+ * batched and serving paths use.
+ *
+ * No exceptions cross this boundary; every function returns 0 or a negative
+ * error code, and tsg_strerror() gives a message.
+ */
+#ifndef TSKIT_GB300_H
+#define TSKIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Option bits: same values as c/tskit/trees.h:47-56. */
+#define TSG_STAT_SITE (1u << 0)
+#define TSG_STAT_BRANCH (1u << 1)
+#define TSG_STAT_NODE (1u << 2)
+#define TSG_STAT_POLARISED (1u << 10)
+#define TSG_STAT_SPAN_NORMALISE (1u << 11)
+#define TSG_STAT_ALLOW_TIME_UNCALIBRATED (1u << 12)
+#define TSG_STAT_PAIR_NORMALISE (1u << 13)
+#define TSG_STAT_NONCENTRED (1u << 14)
+/* Extension bits (no reference counterpart): run both modes in one sweep,
+ * and the arithmetic of the bulk accumulation. */
+#define TSG_STAT_BOTH_MODES (1u << 20)
+#define TSG_PRECISION_F32_KAHAN (1u << 21)
+
+/* tsg_treeseq_init options */
+#define TSG_TABLES_ON_DEVICE (1u << 0)
+
+/* Error codes: the reference's values (c/tskit/core.h:255-751) where the
+ * condition is the same; GPU-specific conditions below -20000. */
+#define TSG_ERR_GENERIC (-1)
+#define TSG_ERR_NO_MEMORY (-2)
+#define TSG_ERR_BAD_PARAM_VALUE (-4)
+#define TSG_ERR_NODE_OUT_OF_BOUNDS (-202)
+#define TSG_ERR_BAD_NODE_TIME_ORDERING (-306)
+#define TSG_ERR_DUPLICATE_SAMPLE (-600)
+#define TSG_ERR_BAD_SAMPLES (-601)
+#define TSG_ERR_TABLES_NOT_INDEXED (-702)
+#define TSG_ERR_BAD_NUM_WINDOWS (-900)
+#define TSG_ERR_BAD_WINDOWS (-901)
+#define TSG_ERR_MULTIPLE_STAT_MODES (-902)
+#define TSG_ERR_BAD_STATE_DIMS (-903)
+#define TSG_ERR_BAD_RESULT_DIMS (-904)
+#define TSG_ERR_INSUFFICIENT_SAMPLE_SETS (-905)
+#define TSG_ERR_INSUFFICIENT_INDEX_TUPLES (-906)
+#define TSG_ERR_BAD_SAMPLE_SET_INDEX (-907)
+#define TSG_ERR_EMPTY_SAMPLE_SET (-908)
+#define TSG_ERR_UNSUPPORTED_STAT_MODE (-909)
+#define TSG_ERR_TIME_UNCALIBRATED (-910)
+#define TSG_ERR_INSUFFICIENT_WEIGHTS (-913)
+#define TSG_ERR_BAD_TIME_WINDOWS_DIM (-922)
+#define TSG_ERR_BAD_TIME_WINDOWS (-924)
+#define TSG_ERR_CUDA (-20001)
+#define TSG_ERR_DEVICE_CHECK (-20002)
+#define TSG_ERR_TOO_MANY_SAMPLE_SETS (-20003)
+#define TSG_ERR_TOO_MANY_OUTPUTS (-20004)
+#define TSG_ERR_BAD_TREE_SEQUENCE (-20005)
+#define TSG_ERR_WORKSPACE_TOO_SMALL (-20006)
+
+/* Summary terms of the named statistics (c/tskit/trees.c summary funcs). */
+#define TSG_DIVERSITY 1                  /* trees.c:3934  idx: i       */
+#define TSG_SEGREGATING_SITES 2          /* trees.c:4221  idx: i       */
+#define TSG_Y1 3                         /* trees.c:4248  idx: i       */
+#define TSG_DIVERGENCE 4                 /* trees.c:4690  idx: i,j     */
+#define TSG_Y2 5                         /* trees.c:4899  idx: i,j     */
+#define TSG_F2 6                         /* trees.c:4938  idx: i,j     */
+#define TSG_Y3 7                         /* trees.c:5177  idx: i,j,k   */
+#define TSG_F3 8                         /* trees.c:5219  idx: i,j,k   */
+#define TSG_F4 9                         /* trees.c:5266  idx: i,j,k,l */
+#define TSG_RELATEDNESS 10               /* trees.c:4729  idx: i,j     */
+#define TSG_RELATEDNESS_NONCENTRED 11    /* trees.c:4755  idx: i,j     */
+
+/* Limits of the device sweep. */
+#define TSG_MAX_SAMPLE_SETS 32
+#define TSG_MAX_OUTPUTS 64
+
+typedef struct tsg_treeseq tsg_treeseq_t;
+typedef struct tsg_workspace tsg_workspace_t;
+
+/*
+ * Columns of a tree sequence (the subset of tsk_table_collection_t the
+ * statistics read).  With TSG_TABLES_ON_DEVICE every pointer is a device
+ * pointer that must outlive the tsg_treeseq_t; otherwise they are host
+ * pointers that are copied.  Edges must be sorted as the reference requires
+ * and the two edge indexes built (c/tskit/tables.c:11393-11450).  Mutation
+ * alleles are integer codes per site: 0 is the ancestral state, each new
+ * derived state string takes the next code in mutation order; alt is the code
+ * of the parent mutation's derived state (0 without parent).
+ */
+typedef struct {
+    double sequence_length;
+    int64_t num_nodes;
+    int64_t num_edges;
+    int64_t num_sites;
+    int64_t num_mutations;
+    const double *node_time;
+    const uint32_t *node_flags;
+    const double *edge_left;
+    const double *edge_right;
+    const int32_t *edge_parent;
+    const int32_t *edge_child;
+    const int32_t *edge_insertion_order;
+    const int32_t *edge_removal_order;
+    const double *site_position;
+    const int32_t *mutation_site;
+    const int32_t *mutation_node;
+    const int32_t *mutation_allele;
+    const int32_t *mutation_alt_allele;
+} tsg_tables_t;
+
+/* Replaces tsk_treeseq_init (c/tskit/trees.c:455-545): validates the tables
+ * on the device and builds the derived per-tree-sequence state (samples,
+ * tree breakpoints, per-tree edge and site ranges, span plan).  num_spans 0
+ * picks a default.  Synchronous. */
+int tsg_treeseq_init(tsg_treeseq_t **ts, const tsg_tables_t *tables, int64_t num_spans,
+    uint32_t options);
+int tsg_treeseq_free(tsg_treeseq_t *ts);
+int64_t tsg_treeseq_get_num_trees(const tsg_treeseq_t *ts);
+int64_t tsg_treeseq_get_num_samples(const tsg_treeseq_t *ts);
+int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts);
+/* breakpoints: host array of num_trees + 1 doubles */
+int tsg_treeseq_get_breakpoints(const tsg_treeseq_t *ts, double *breakpoints);
+const char *tsg_strerror(int err);
+
+/* ---------------------------------------------------------------- one-way
+ * Same arguments as tsk_treeseq_diversity / segregating_sites / Y1
+ * (c/tskit/trees.h, "One way sample set stats"). Host pointers. */
+int tsg_treeseq_diversity(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_segregating_sites(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_Y1(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+
+/* ---------------------------------------------------------------- k-way
+ * Same arguments as tsk_treeseq_divergence / Y2 / f2 / Y3 / f3 / f4 /
+ * genetic_relatedness (c/tskit/trees.h, "Two/Three/Four way sample set
+ * stats"); index_tuples has num_index_tuples * k entries. */
+int tsg_treeseq_divergence(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_Y2(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_f2(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_Y3(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_f3(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_f4(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+int tsg_treeseq_genetic_relatedness(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+
+/* ------------------------------------------------------ fused sample-count
+ * Generalises tsk_treeseq_sample_count_stat (c/tskit/trees.c:2174-2220) to a
+ * list of summary terms evaluated in one sweep.  With TSG_STAT_BOTH_MODES the
+ * result holds the branch block (num_windows x num_outputs) followed by the
+ * site block.  Host pointers. */
+typedef struct {
+    int32_t type;   /* TSG_DIVERSITY ... */
+    int32_t idx[4]; /* sample-set indexes the term reads */
+} tsg_output_t;
+
+int tsg_treeseq_sample_count_stat(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_outputs,
+    const tsg_output_t *outputs, uint64_t num_windows, const double *windows,
+    uint32_t options, double *result);
+
+/* ----------------------------------------------- device-resident queries
+ * A query is prepared once (validates and uploads sample sets, summary terms
+ * and windows) and launched any number of times on a stream with a
+ * workspace.  tsg_query_launch enqueues kernels only: the result (device
+ * pointer, same layout as tsg_treeseq_sample_count_stat) is ready when the
+ * stream reaches that point.  Launches that share a workspace must be
+ * ordered on one stream. */
+typedef struct tsg_query tsg_query_t;
+
+int tsg_query_create(tsg_query_t **query, const tsg_treeseq_t *self,
+    uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_outputs, const tsg_output_t *outputs, uint64_t num_windows,
+    const double *windows, uint32_t options);
+int tsg_query_free(tsg_query_t *query);
+/* Device bytes the query needs in a workspace. */
+int64_t tsg_query_workspace_bytes(const tsg_query_t *query);
+/* Number of result doubles. */
+int64_t tsg_query_result_size(const tsg_query_t *query);
+int tsg_query_launch(const tsg_query_t *query, tsg_workspace_t *ws, double *result_device,
+    void *cuda_stream);
+/* Record cudaEvent_t `start_event` / `stop_event` (either may be NULL) on the
+ * launch stream immediately before and after the sweep kernel of every later
+ * launch of `query`, so callers can time the dominant kernel alone. */
+int tsg_query_set_sweep_events(tsg_query_t *query, void *start_event, void *stop_event);
+/* Synchronous read of the device-side check word left by the last launch of
+ * `query` on `ws`: 0, or TSG_ERR_DEVICE_CHECK when a kernel found an
+ * inconsistent tree sequence (node id out of range, a cycle). */
+int tsg_workspace_check(const tsg_workspace_t *ws, const tsg_query_t *query);
+
+/* Workspaces are device scratch owned by the caller; they grow on demand in
+ * tsg_workspace_reserve (which allocates) and never inside a launch. */
+int tsg_workspace_create(tsg_workspace_t **ws);
+int tsg_workspace_reserve(tsg_workspace_t *ws, int64_t bytes);
+int64_t tsg_workspace_bytes(const tsg_workspace_t *ws);
+int tsg_workspace_free(tsg_workspace_t *ws);
+
+/* Number of kernel launches issued by this library since load (counter used
+ * by the benchmarks to report launches). */
+int64_t tsg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

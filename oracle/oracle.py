@@ -282,3 +282,114 @@ def relatedness_from_divergence(D):
     y = np.mean(B, axis=0)
     K -= y[:, None] + y[None, :]
     return K / -2
+
+
+# ------------------------------------------------------------------------
+# Adapter from the reference's high-level method names to the oracle.  The
+# outputs keep the low-level shapes; callers reshape to the expected shape
+# (the reference only drops length-1 dimensions).
+# ------------------------------------------------------------------------
+_ONE_WAY = {"diversity": DIVERSITY, "segregating_sites": SEGSITES, "Y1": Y1}
+_K_WAY = {"divergence": (DIVERGENCE, 2), "Y2": (Y2, 2), "f2": (F2, 2), "Y3": (Y3, 3),
+          "f3": (F3, 3), "f4": (F4, 4)}
+
+
+def _sets(ots, sample_sets):
+    if sample_sets is None:
+        return [ots.samples]
+    a = sample_sets
+    try:
+        arr = np.array(a, dtype=np.int64)
+        if arr.ndim == 1:
+            return [arr]
+    except ValueError:
+        pass
+    return [np.asarray(s, dtype=np.int64) for s in a]
+
+
+def _tuples(indexes, k, nsets):
+    if indexes is None:
+        return [tuple(range(k))]
+    idx = np.asarray(indexes, dtype=np.int64).reshape(-1, k)
+    return [tuple(int(v) for v in row) for row in idx]
+
+
+def call(ots, method, kwargs):
+    """Evaluate one reference API call with the oracle."""
+    kw = dict(kwargs)
+    mode = kw.pop("mode", "site")
+    windows = kw.pop("windows", None)
+    if isinstance(windows, str):
+        raise ValueError("string windows are resolved by the caller")
+    span_normalise = kw.pop("span_normalise", True)
+    if method in _ONE_WAY:
+        sets = _sets(ots, kw.pop("sample_sets", None))
+        return one_way(ots, _ONE_WAY[method], sets, windows=windows, mode=mode,
+                       span_normalise=span_normalise)
+    if method in _K_WAY:
+        typ, k = _K_WAY[method]
+        sets = _sets(ots, kw.pop("sample_sets"))
+        return k_way(ots, typ, sets, _tuples(kw.pop("indexes", None), k, len(sets)),
+                     windows=windows, mode=mode, span_normalise=span_normalise)
+    if method == "genetic_relatedness":
+        sets = _sets(ots, kw.pop("sample_sets"))
+        typ = RELATEDNESS if kw.pop("centre", True) else RELATEDNESS_NC
+        polarised = kw.pop("polarised", True)
+        num = k_way(ots, typ, sets, _tuples(kw.pop("indexes", None), 2, len(sets)),
+                    windows=windows, mode=mode, span_normalise=span_normalise,
+                    polarised=polarised)
+        if kw.pop("proportion", True):
+            union = np.array(sorted({int(u) for s in sets for u in s}))
+            den = one_way(ots, SEGSITES, [union], windows=windows, mode=mode,
+                          span_normalise=span_normalise)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                num = num / den
+        return num
+    if method == "Fst":
+        sets = _sets(ots, kw.pop("sample_sets"))
+        tuples = _tuples(kw.pop("indexes", None), 2, len(sets))
+        dvg = k_way(ots, DIVERGENCE, sets, tuples, windows=windows, mode=mode,
+                    span_normalise=span_normalise)
+        dvs = one_way(ots, DIVERSITY, sets, windows=windows, mode=mode,
+                      span_normalise=span_normalise)
+        out = np.ones_like(dvg)
+        for i, (u, v) in enumerate(tuples):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                out[:, i] -= 2 * (dvs[:, u] + dvs[:, v]) / (dvs[:, u] + dvs[:, v] + 2 * dvg[:, i])
+        return out
+    if method == "Tajimas_D":
+        sets = _sets(ots, kw.pop("sample_sets", None))
+        T = one_way(ots, DIVERSITY, sets, windows=windows, mode=mode, span_normalise=False)
+        S = one_way(ots, SEGSITES, sets, windows=windows, mode=mode, span_normalise=False)
+        n = np.array([len(s) for s in sets], dtype=np.float64)
+        h = np.array([np.sum(1 / np.arange(1, nn)) for nn in n])
+        g = np.array([np.sum(1 / np.arange(1, nn) ** 2) for nn in n])
+        with np.errstate(invalid="ignore", divide="ignore"):
+            a = (n + 1) / (3 * (n - 1) * h) - 1 / h**2
+            b = 2 * (n**2 + n + 3) / (9 * n * (n - 1)) - (n + 2) / (h * n) + g / h**2
+            return (T - S / h) / np.sqrt(a * S + (b / (h**2 + g)) * S * (S - 1))
+    if method == "allele_frequency_spectrum":
+        sets = kw.pop("sample_sets", None)
+        if sets is None:
+            sets = [ots.samples]
+        else:
+            try:
+                arr = np.array(sets, dtype=np.int64)
+                sets = [arr] if arr.ndim == 1 else list(arr)
+            except ValueError:
+                pass
+        return allele_frequency_spectrum(ots, [np.asarray(s) for s in sets], windows=windows,
+                                         time_windows=kw.pop("time_windows", None), mode=mode,
+                                         span_normalise=span_normalise,
+                                         polarised=kw.pop("polarised", False))
+    if method == "genetic_relatedness_vector":
+        return genetic_relatedness_vector(ots, kw.pop("W"), windows=windows,
+                                          span_normalise=span_normalise,
+                                          centre=kw.pop("centre", True),
+                                          nodes=kw.pop("nodes", None))
+    if method == "genetic_relatedness_matrix":
+        D = divergence_matrix_site(ots, windows=windows, span_normalise=span_normalise)
+        return np.stack([relatedness_from_divergence(d) for d in D])
+    if method == "genotype_matrix":
+        return genotype_matrix(ots)
+    raise NotImplementedError(method)

@@ -1,0 +1,141 @@
+"""GPU parity: the CUDA path against the reference's golden outputs and the
+oracle (FP64 form within 1e-12 relative; FP32-Kahan form within the stated
+bound; integer-derived site statistics identical to the FP64 form)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_cases import all_cases, load, resolve
+
+pytestmark = pytest.mark.gpu
+
+GPU_METHODS = {
+    "diversity", "segregating_sites", "Y1", "divergence", "Y2", "f2", "Y3", "f3", "f4",
+    "genetic_relatedness", "Fst", "Tajimas_D",
+}
+CASES = [(n, c) for n, c in all_cases() if c["method"] in GPU_METHODS]
+_ts = {}
+
+RTOL_F64 = 1e-12
+# FP32-compensated bulk accumulation: stated bound on relative error against
+# the FP64 oracle (per-window values, relative to the window's magnitude).
+RTOL_F32 = 2e-6
+
+
+def gpu_ts(name, cuda_lib):
+    if name not in _ts:
+        import tskit_gb300
+
+        tables, data = load(name)
+        _ts[name] = (tskit_gb300.TreeSequence(tables), data)
+    return _ts[name]
+
+
+@pytest.mark.parametrize("name,case", CASES, ids=[f"{n}-{c['key']}-{c['method']}" for n, c in CASES])
+def test_golden(name, case, cuda_lib):
+    ts, data = gpu_ts(name, cuda_lib)
+    expected = data[case["key"]]
+    got = np.asarray(getattr(ts, case["method"])(**resolve(case["kwargs"], data)))
+    assert got.shape == expected.shape
+    np.testing.assert_allclose(got, expected, rtol=RTOL_F64, atol=1e-13, equal_nan=True)
+
+
+def test_known_answer_paper_ex(cuda_lib):
+    """c/tests/test_stats.c:1718-1742"""
+    ts, _ = gpu_ts("paper_ex", cuda_lib)
+    assert abs(ts.diversity([0, 1, 2, 3], mode="site", span_normalise=False) - 1.5) < 1e-12
+    assert np.isnan(ts.diversity([0], mode="site", span_normalise=False))
+
+
+@pytest.fixture(scope="module")
+def medium(cuda_lib):
+    import tskit_gb300
+    from tskit_gb300 import sim
+
+    tables = sim.simulate(400, 1e6, 3000, 15000, 11)
+    return tskit_gb300.TreeSequence(tables), O.OracleTS(tables), tables
+
+
+def _sets(tables, k, seed=0):
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(tables.samples())
+    return [np.sort(p) for p in np.array_split(perm, k)]
+
+
+def _fused_terms(K):
+    terms = [(O.DIVERSITY, (k,)) for k in range(K)]
+    terms += [(O.SEGSITES, (k,)) for k in range(K)]
+    terms += [(O.DIVERGENCE, (i, j)) for i in range(K) for j in range(i + 1, K)]
+    terms += [(O.Y3, (0, 1, 2)), (O.Y3, (1, 2, 3)), (O.F4, (0, 1, 2, 3))]
+    return terms
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("polarised", [False, True])
+def test_fused_both_modes_vs_oracle(medium, precision, polarised):
+    import torch
+
+    ts, ots, tables = medium
+    sets = _sets(tables, 4)
+    terms = _fused_terms(4)
+    windows = np.linspace(0, tables.sequence_length, 17)
+    q = ts.query(sets, terms, windows=windows, both_modes=True, polarised=polarised,
+                 precision=precision)
+    ws = __import__("tskit_gb300").Workspace()
+    res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+    q.launch(ws, res)
+    torch.cuda.synchronize()
+    q.check(ws)
+    got = res.cpu().numpy().reshape(2, len(windows) - 1, len(terms))
+    for m, mode in enumerate(["branch", "site"]):
+        exp = O.sample_count_stat(ots, sets, terms, windows=windows, mode=mode,
+                                  polarised=polarised)
+        rtol = RTOL_F64 if (precision == "f64" or mode == "site") else RTOL_F32
+        scale = np.maximum(np.abs(exp), np.abs(exp).max(axis=0, keepdims=True) * 1e-3)
+        err = np.abs(got[m] - exp) / scale
+        assert np.nanmax(err) < rtol, (mode, precision, np.nanmax(err))
+
+
+def test_deterministic(medium):
+    ts, _, tables = medium
+    sets = _sets(tables, 3, seed=5)
+    a = ts.divergence(sets, indexes=[(0, 1), (1, 2)], windows=np.linspace(0, 1e6, 9),
+                      mode="branch")
+    b = ts.divergence(sets, indexes=[(0, 1), (1, 2)], windows=np.linspace(0, 1e6, 9),
+                      mode="branch")
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("num_spans", [1, 2, 7, 64, 1000])
+def test_span_count_invariance(cuda_lib, num_spans):
+    """The span decomposition changes only the summation order."""
+    import tskit_gb300
+    from tskit_gb300 import sim
+
+    tables = sim.simulate(60, 1e5, 300, 1500, 4)
+    ts = tskit_gb300.TreeSequence(tables, num_spans=num_spans)
+    ots = O.OracleTS(tables)
+    sets = _sets(tables, 2, seed=1)
+    w = np.linspace(0, 1e5, 5)
+    for mode in ("branch", "site"):
+        got = ts.divergence(sets, windows=w, mode=mode)
+        exp = O.k_way(ots, O.DIVERGENCE, sets, [(0, 1)], windows=w, mode=mode)[:, 0]
+        np.testing.assert_allclose(got, exp, rtol=RTOL_F64)
+
+
+def test_errors_match_reference_codes(medium):
+    import tskit_gb300
+
+    ts, _, tables = medium
+    s = list(tables.samples()[:10])
+    with pytest.raises(tskit_gb300.LibraryError) as e:
+        ts.diversity([s + [s[0]]])
+    assert e.value.code == -600  # TSK_ERR_DUPLICATE_SAMPLE
+    with pytest.raises(tskit_gb300.LibraryError) as e:
+        ts.diversity([s], windows=[0, 10, 5, tables.sequence_length])
+    assert e.value.code == -901  # TSK_ERR_BAD_WINDOWS
+    with pytest.raises(tskit_gb300.LibraryError) as e:
+        ts.diversity([[tables.num_nodes - 1]])
+    assert e.value.code == -601  # TSK_ERR_BAD_SAMPLES
+    with pytest.raises(ValueError):
+        ts.diversity([s], mode="nonsense")

@@ -1,0 +1,142 @@
+// Internal definitions shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tskit_gb300.h"
+
+namespace tsg {
+
+extern std::atomic<int64_t> g_launches;
+void set_cuda_error(cudaError_t e, const char *where);
+
+#define TSG_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t _e = (call);                                                         \
+        if (_e != cudaSuccess) {                                                         \
+            ::tsg::set_cuda_error(_e, #call);                                            \
+            return TSG_ERR_CUDA;                                                         \
+        }                                                                                \
+    } while (0)
+
+#define TSG_LAUNCHED()                                                                   \
+    do {                                                                                 \
+        ::tsg::g_launches.fetch_add(1, std::memory_order_relaxed);                       \
+        cudaError_t _e = cudaGetLastError();                                             \
+        if (_e != cudaSuccess) {                                                         \
+            ::tsg::set_cuda_error(_e, "kernel launch");                                  \
+            return TSG_ERR_CUDA;                                                         \
+        }                                                                                \
+    } while (0)
+
+// Device-side error codes written to a flag word (first writer wins).
+enum DeviceError : int32_t {
+    DEV_OK = 0,
+    DEV_NODE_OUT_OF_BOUNDS = 1,
+    DEV_PATH_TOO_LONG = 2,
+    DEV_BAD_EDGE = 3,
+    DEV_BAD_TIME_ORDER = 4,
+    DEV_UNSORTED_INDEX = 5,
+    DEV_BAD_SITE = 6,
+    DEV_BAD_MUTATION = 7,
+};
+
+__device__ __forceinline__ void dev_error(int32_t *flag, int32_t code)
+{
+    atomicCAS(flag, 0, code);
+}
+
+// Smallest index i in [0, n) with a[i] >= x (n if none).
+template <typename T>
+__host__ __device__ __forceinline__ int64_t lower_bound(const T *a, int64_t n, T x)
+{
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < x) {
+            lo = mid + 1;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
+}
+
+// Smallest index i in [0, n) with a[i] > x (n if none).
+template <typename T>
+__host__ __device__ __forceinline__ int64_t upper_bound(const T *a, int64_t n, T x)
+{
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (a[mid] <= x) {
+            lo = mid + 1;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
+}
+
+// Read-only view of a device-resident tree sequence, passed to kernels by value.
+struct TSView {
+    int64_t num_nodes, num_edges, num_sites, num_mutations, num_samples, num_trees;
+    int64_t num_spans;
+    double sequence_length;
+    const double *node_time;
+    const int32_t *sample_index;  // node -> sample index or -1
+    const int32_t *samples;       // sample index -> node
+    const double *breakpoints;    // num_trees + 1
+    const int32_t *tree_in;       // num_trees + 1: insertion-order offsets
+    const int32_t *tree_out;      // num_trees + 1: removal-order offsets
+    const int32_t *tree_sites;    // num_trees + 1
+    const int32_t *site_mut;      // num_sites + 1
+    const int32_t *ins_parent, *ins_child;  // edges in insertion order
+    const int32_t *rem_parent, *rem_child;  // edges in removal order
+    const double *site_position;
+    const int32_t *mutation_node, *mutation_allele, *mutation_alt;
+    const int32_t *span_tree;     // num_spans + 1
+    const int64_t *span_alive_off;  // num_spans + 1
+    const int2 *span_alive;       // (parent, child) alive at each span start
+};
+
+// Device-wide exclusive scan of int64 values (in may alias out).  `tmp` must
+// hold scan_tmp_elems(n) int64.
+int64_t scan_tmp_elems(int64_t n);
+int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp,
+    cudaStream_t stream);
+
+int device_count_sms();
+
+}  // namespace tsg
+
+// Opaque handle definitions.
+struct tsg_treeseq {
+    tsg::TSView v;
+    uint32_t options;
+    // host copies of small derived arrays
+    std::vector<double> h_breakpoints;
+    std::vector<int32_t> h_span_tree;
+    std::vector<uint32_t> h_node_flags;
+    std::vector<int32_t> h_sample_index;
+    int64_t max_alive;
+    // device allocations owned by this object
+    std::vector<void *> owned;
+    // state of the synchronous (host-pointer) entry points
+    std::mutex sync_mutex;
+    tsg_workspace *sync_ws = nullptr;
+    void *stage = nullptr;
+    int64_t stage_bytes = 0;
+    cudaStream_t sync_stream = nullptr;
+};
+
+struct tsg_workspace {
+    void *ptr;
+    int64_t bytes;
+};

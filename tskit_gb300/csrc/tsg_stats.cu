@@ -1,0 +1,1138 @@
+// Sample-count statistics on the GPU: branch and site modes.
+//
+// Replaces tsk_treeseq_branch_general_stat / tsk_treeseq_site_general_stat
+// (c/tskit/trees.c:1352-1523, 1654-1776) for the named summary functions
+// (c/tskit/trees.c:3934-5309) with a span-parallel sweep:
+//
+//   * The trees are cut into spans (tree ranges).  One CTA takes a span,
+//     rebuilds the tree at the span start from the span's alive-edge list
+//     (parallel bottom-up accumulation of per-node sample-set counts x[u],
+//     integer atomics, a "last child to arrive continues upward" climb), and
+//     then one warp replays the span's edge removals and insertions exactly
+//     as the reference does, walking root paths.  Lanes hold the K count
+//     components (lane k owns x[.][k]) and evaluate the summary terms (lane r
+//     owns term r), exchanging counts by shuffles.
+//   * Branch mode is accumulated as the change of the reference's running sum
+//     (sum over nodes of branch_length * f(x)) within the span: per window the
+//     span reports A = covered length and B = sum of (running-sum change so
+//     far) * length, plus the span's total change D.  A fixed-order scan of D
+//     over spans recovers the running sum at every span start from its value
+//     on the first tree, and result[w] = sum_s RS_s * A_sw + B_sw.
+//   * Site mode reads the integer counts at each mutation node (exact) and
+//     sums f over the alleles of each site (trees.c:1525-1652).
+//   * Every reduction runs in a fixed order, so results are bitwise
+//     reproducible; FP64 accumulates windows and the cross-span scan.  With
+//     TSG_PRECISION_F32_KAHAN the per-node summary changes are evaluated in
+//     FP32 and summed with Kahan compensation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+struct Term {
+    int32_t type;
+    int32_t idx[4];
+};
+
+struct QueryParams {
+    int32_t K, KP, R, Wn;
+    int32_t branch, site, polarised, f32, need_mean;
+    int32_t num_slots;
+    double set_size[TSG_MAX_SAMPLE_SETS];
+    Term term[TSG_MAX_OUTPUTS];
+};
+
+struct QueryDev {
+    const uint32_t *sample_mask;  // per sample index: bit k = member of set k
+    const double *windows;        // Wn + 1
+    const int32_t *span_wlo;      // per span: first window overlapping it
+    const int64_t *span_woff;     // per span: offset into span-window arrays
+    const int32_t *win_span_lo;   // per window: first overlapping span
+    const int32_t *win_span_hi;   // per window: last overlapping span
+};
+
+struct WsDev {
+    int32_t *parent;  // num_slots * N
+    int32_t *nchild;  // num_slots * N: children in the tree at the span start
+    int32_t *arrive;  // num_slots * N: children whose counts have been added
+    int32_t *x;       // num_slots * N * KP
+    double *A;        // span windows
+    double *B;        // span windows * R
+    double *SITE;     // span windows * R
+    double *D;        // spans * R
+    double *RS;       // spans * R
+    double *rs0;      // R
+    int32_t *err;
+    int32_t *counter;
+};
+
+// ----------------------------------------------------------------- summary
+template <typename F>
+__device__ __forceinline__ F term_value(int type, F xi, F xj, F xk, F xl, F ni, F nj, F nk,
+    F nl, bool ieqj, F meanx)
+{
+    switch (type) {
+        case TSG_DIVERSITY:
+            return xi * (ni - xi) / (ni * (ni - 1));
+        case TSG_SEGREGATING_SITES:
+            return (F) (xi > 0) * (1 - xi / ni);
+        case TSG_Y1:
+            return xi * (ni - xi) * (ni - xi - 1) / (ni * (ni - 1) * (ni - 2));
+        case TSG_DIVERGENCE:
+            return xi * (nj - xj) / (ni * (nj - (F) (ieqj ? 1 : 0)));
+        case TSG_Y2:
+            return xi * (nj - xj) * (nj - xj - 1) / (ni * nj * (nj - 1));
+        case TSG_F2:
+            return (xi * (xi - 1) * (nj - xj) * (nj - xj - 1) - xi * (ni - xi) * (nj - xj) * xj)
+                / (ni * (ni - 1) * nj * (nj - 1));
+        case TSG_Y3:
+            return xi * (nj - xj) * (nk - xk) / (ni * nj * nk);
+        case TSG_F3:
+            return (xi * (xi - 1) * (nj - xj) * (nk - xk) - xi * (ni - xi) * (nj - xj) * xk)
+                / (ni * (ni - 1) * nj * nk);
+        case TSG_F4:
+            return (xi * xk * (nj - xj) * (nl - xl) - xi * xl * (nj - xj) * (nk - xk))
+                / (ni * nj * nk * nl);
+        case TSG_RELATEDNESS:
+            return (xi / ni - meanx) * (xj / nj - meanx);
+        case TSG_RELATEDNESS_NONCENTRED:
+            return xi * xj / (ni * nj);
+        default:
+            return (F) NAN;
+    }
+}
+
+template <typename F>
+__device__ __forceinline__ F warp_sum(F v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// Evaluate f at the count vector held one component per lane (xk on lane k)
+// for the terms of pass p (term index lane + 32 p).  All 32 lanes must call.
+template <typename F>
+__device__ __forceinline__ F eval_f(const QueryParams &q, F xk, int pass)
+{
+    const int lane = threadIdx.x & 31;
+    F meanx = 0;
+    if (q.need_mean) {
+        F c = lane < q.K ? xk / (F) q.set_size[lane] : (F) 0;
+        meanx = warp_sum(c) / (F) q.K;
+    }
+    const int r = lane + 32 * pass;
+    const Term &t = q.term[r < q.R ? r : 0];
+    F xi = __shfl_sync(0xffffffffu, xk, t.idx[0]);
+    F xj = __shfl_sync(0xffffffffu, xk, t.idx[1]);
+    F xkk = __shfl_sync(0xffffffffu, xk, t.idx[2]);
+    F xl = __shfl_sync(0xffffffffu, xk, t.idx[3]);
+    if (r >= q.R) {
+        return 0;
+    }
+    return term_value<F>(t.type, xi, xj, xkk, xl, (F) q.set_size[t.idx[0]],
+        (F) q.set_size[t.idx[1]], (F) q.set_size[t.idx[2]], (F) q.set_size[t.idx[3]],
+        t.idx[0] == t.idx[1], meanx);
+}
+
+// The branch summary: f(x), plus f(total - x) when unpolarised
+// (c/tskit/trees.c:1944-1972).
+template <typename F>
+__device__ __forceinline__ F eval_branch(const QueryParams &q, int xk_int, int pass)
+{
+    const int lane = threadIdx.x & 31;
+    F xk = (F) xk_int;
+    F v = eval_f<F>(q, xk, pass);
+    if (!q.polarised) {
+        F ck = lane < q.K ? (F) q.set_size[lane] - xk : (F) 0;
+        v += eval_f<F>(q, ck, pass);
+    }
+    return v;
+}
+
+template <typename F>
+struct Acc {
+    F s, c;
+    __device__ __forceinline__ void zero()
+    {
+        s = 0;
+        c = 0;
+    }
+    __device__ __forceinline__ void add(F v)
+    {
+        if (sizeof(F) == sizeof(float)) {
+            F y = v - c;
+            F t = s + y;
+            c = (t - s) - y;
+            s = t;
+        } else {
+            s += v;
+        }
+    }
+    __device__ __forceinline__ double value() const { return (double) s - (double) c; }
+};
+
+__device__ __forceinline__ int32_t node_weight(const TSView &ts, const QueryDev &qd, int32_t u,
+    int k)
+{
+    int32_t si = ts.sample_index[u];
+    return si >= 0 ? (int32_t) ((qd.sample_mask[si] >> k) & 1u) : 0;
+}
+
+// ------------------------------------------------------------------ sweep
+template <typename F>
+__global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDev qd, WsDev w)
+{
+    __shared__ int s_span;
+    __shared__ double s_red[8][64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int64_t N = ts.num_nodes;
+    const int K = q.K, KP = q.KP;
+    int32_t *parent = w.parent + (int64_t) blockIdx.x * N;
+    int32_t *nchild = w.nchild + (int64_t) blockIdx.x * N;
+    int32_t *arrive = w.arrive + (int64_t) blockIdx.x * N;
+    int32_t *x = w.x + (int64_t) blockIdx.x * N * KP;
+    const double *time = ts.node_time;
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_span = atomicAdd(w.counter, 1);
+        }
+        __syncthreads();
+        const int s = s_span;
+        __syncthreads();
+        if (s >= ts.num_spans) {
+            break;
+        }
+        const int32_t t0 = ts.span_tree[s], t1 = ts.span_tree[s + 1];
+        const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
+        const int2 *alive = ts.span_alive;
+
+        // ---- phase 0: reset every node the span can touch
+        auto init_node = [&](int32_t u) {
+            if (u < 0 || u >= N) {
+                dev_error(w.err, DEV_NODE_OUT_OF_BOUNDS);
+                return;
+            }
+            parent[u] = -1;
+            nchild[u] = 0;
+            arrive[u] = 0;
+            for (int k = 0; k < K; k++) {
+                x[(int64_t) u * KP + k] = node_weight(ts, qd, u, k);
+            }
+        };
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+            int2 pc = alive[i];
+            init_node(pc.x);
+            init_node(pc.y);
+        }
+        const int32_t ie0 = ts.tree_in[t0 + 1 <= t1 ? t0 + 1 : t1], ie1 = ts.tree_in[t1];
+        for (int32_t i = ie0 + threadIdx.x; i < ie1; i += blockDim.x) {
+            init_node(ts.ins_parent[i]);
+            init_node(ts.ins_child[i]);
+        }
+        const int32_t m0 = ts.site_mut[ts.tree_sites[t0]], m1 = ts.site_mut[ts.tree_sites[t1]];
+        for (int32_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+            init_node(ts.mutation_node[m]);
+        }
+        __syncthreads();
+        // ---- phase 1: link the tree at the span start
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+            int2 pc = alive[i];
+            if (pc.x >= 0 && pc.x < N && pc.y >= 0 && pc.y < N) {
+                parent[pc.y] = pc.x;
+                atomicAdd(&nchild[pc.x], 1);
+            }
+        }
+        __syncthreads();
+        // ---- phase 2: bottom-up counts; the last child to finish climbs on
+        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+            int32_t v = alive[i].y;
+            if (v < 0 || v >= N || nchild[v] != 0) {
+                continue;
+            }
+            for (int64_t iter = 0;; iter++) {
+                int32_t p = parent[v];
+                if (p < 0) {
+                    break;
+                }
+                if (iter > N) {
+                    dev_error(w.err, DEV_PATH_TOO_LONG);
+                    break;
+                }
+                for (int k = 0; k < K; k++) {
+                    int32_t xv = __ldcg(&x[(int64_t) v * KP + k]);
+                    if (xv != 0) {
+                        atomicAdd(&x[(int64_t) p * KP + k], xv);
+                    }
+                }
+                __threadfence();
+                if (atomicAdd(&arrive[p], 1) + 1 != nchild[p]) {
+                    break;
+                }
+                __threadfence();
+                v = p;
+            }
+        }
+        __syncthreads();
+
+        // ---- phase 3: running sum on the first tree (span 0 only), fixed order
+        if (s == 0 && q.branch) {
+            double part0 = 0, part1 = 0;
+            for (int32_t i = warp; i < ts.tree_in[1]; i += nwarps) {
+                int32_t c = ts.ins_child[i], p = ts.ins_parent[i];
+                double bl = time[p] - time[c];
+                int xc = lane < K ? __ldcg(&x[(int64_t) c * KP + lane]) : 0;
+                part0 += bl * eval_branch<double>(q, xc, 0);
+                if (q.R > 32) {
+                    part1 += bl * eval_branch<double>(q, xc, 1);
+                }
+            }
+            s_red[warp][lane] = part0;
+            s_red[warp][lane + 32] = part1;
+            __syncthreads();
+            if (warp == 0) {
+                double a = 0, b = 0;
+                for (int j = 0; j < nwarps; j++) {
+                    a += s_red[j][lane];
+                    b += s_red[j][lane + 32];
+                }
+                if (lane < q.R) {
+                    w.rs0[lane] = a;
+                }
+                if (lane + 32 < q.R) {
+                    w.rs0[lane + 32] = b;
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- phase 4: replay the span (warp 0)
+        if (warp == 0) {
+            const int R = q.R;
+            const int passes = R > 32 ? 2 : 1;
+            const int32_t wlo = qd.span_wlo[s];
+            const int64_t woff = qd.span_woff[s];
+            const int64_t nwin = qd.span_woff[s + 1] - woff;
+            const double *win = qd.windows;
+            for (int64_t j = lane; j < nwin; j += 32) {
+                w.A[woff + j] = 0;
+            }
+            for (int64_t j = lane; j < nwin * R; j += 32) {
+                if (q.branch) {
+                    w.B[woff * R + j] = 0;
+                }
+                if (q.site) {
+                    w.SITE[woff * R + j] = 0;
+                }
+            }
+            __syncwarp();
+            Acc<F> cum[2];
+            cum[0].zero();
+            cum[1].zero();
+            int32_t wi = wlo;   // branch window cursor
+            int32_t ws = wlo;   // site window cursor
+
+            auto walk = [&](int32_t v, int xc, int sign) {
+                for (int64_t iter = 0; v >= 0; iter++) {
+                    if (iter > N || v >= N) {
+                        dev_error(w.err, DEV_PATH_TOO_LONG);
+                        break;
+                    }
+                    int32_t pv = parent[v];
+                    int xo = lane < K ? x[(int64_t) v * KP + lane] : 0;
+                    int xn = xo + sign * xc;
+                    double tv = time[v];
+                    double tp = pv >= 0 ? time[pv] : tv;
+                    if (q.branch) {
+                        F bl = (F) (tp - tv);
+                        for (int p = 0; p < passes; p++) {
+                            F d = eval_branch<F>(q, xn, p) - eval_branch<F>(q, xo, p);
+                            cum[p].add(bl * d);
+                        }
+                    }
+                    if (lane < K) {
+                        x[(int64_t) v * KP + lane] = xn;
+                    }
+                    v = pv;
+                }
+            };
+
+            for (int32_t t = t0; t < t1; t++) {
+                if (t > t0) {
+                    // removals entering tree t (O order), then insertions (I order)
+                    for (int32_t i = ts.tree_out[t]; i < ts.tree_out[t + 1]; i++) {
+                        int32_t c = ts.rem_child[i], p = ts.rem_parent[i];
+                        int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
+                        if (q.branch) {
+                            F bl = (F) (time[p] - time[c]);
+                            for (int pp = 0; pp < passes; pp++) {
+                                cum[pp].add(-bl * eval_branch<F>(q, xc, pp));
+                            }
+                        }
+                        parent[c] = -1;
+                        walk(p, xc, -1);
+                    }
+                    for (int32_t i = ts.tree_in[t]; i < ts.tree_in[t + 1]; i++) {
+                        int32_t c = ts.ins_child[i], p = ts.ins_parent[i];
+                        parent[c] = p;
+                        int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
+                        if (q.branch) {
+                            F bl = (F) (time[p] - time[c]);
+                            for (int pp = 0; pp < passes; pp++) {
+                                cum[pp].add(bl * eval_branch<F>(q, xc, pp));
+                            }
+                        }
+                        walk(p, xc, +1);
+                    }
+                }
+                const double tl = ts.breakpoints[t], tr = ts.breakpoints[t + 1];
+                if (q.branch) {
+                    while (wi < q.Wn && win[wi] < tr) {
+                        double a = tl > win[wi] ? tl : win[wi];
+                        double b = tr < win[wi + 1] ? tr : win[wi + 1];
+                        double len = b - a;
+                        int64_t li = woff + (wi - wlo);
+                        if (lane == 0) {
+                            w.A[li] += len;
+                        }
+                        for (int p = 0; p < passes; p++) {
+                            int r = lane + 32 * p;
+                            if (r < R) {
+                                w.B[li * R + r] += cum[p].value() * len;
+                            }
+                        }
+                        if (win[wi + 1] <= tr) {
+                            wi++;
+                        } else {
+                            break;
+                        }
+                    }
+                }
+                if (q.site) {
+                    for (int32_t site = ts.tree_sites[t]; site < ts.tree_sites[t + 1]; site++) {
+                        const double pos = ts.site_position[site];
+                        while (ws + 1 < q.Wn && win[ws + 1] <= pos) {
+                            ws++;
+                        }
+                        const int32_t sm0 = ts.site_mut[site], sm1 = ts.site_mut[site + 1];
+                        int32_t A = 1;
+                        for (int32_t m = sm0; m < sm1; m++) {
+                            A = max(A, ts.mutation_allele[m] + 1);
+                        }
+                        double val[2] = { 0, 0 };
+                        for (int32_t a = q.polarised ? 1 : 0; a < A; a++) {
+                            int st = (a == 0 && lane < K) ? (int) q.set_size[lane] : 0;
+                            for (int32_t m = sm0; m < sm1; m++) {
+                                int32_t u = ts.mutation_node[m];
+                                int xm = lane < K ? x[(int64_t) u * KP + lane] : 0;
+                                if (ts.mutation_allele[m] == a) {
+                                    st += xm;
+                                }
+                                if (ts.mutation_alt[m] == a) {
+                                    st -= xm;
+                                }
+                            }
+                            for (int p = 0; p < passes; p++) {
+                                val[p] += eval_f<double>(q, (double) st, p);
+                            }
+                        }
+                        int64_t li = woff + (ws - wlo);
+                        for (int p = 0; p < passes; p++) {
+                            int r = lane + 32 * p;
+                            if (r < R) {
+                                w.SITE[li * R + r] += val[p];
+                            }
+                        }
+                    }
+                }
+            }
+            if (q.branch) {
+                for (int p = 0; p < passes; p++) {
+                    int r = lane + 32 * p;
+                    if (r < R) {
+                        w.D[(int64_t) s * R + r] = cum[p].value();
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r], one block per r, fixed order.
+__global__ void k_span_scan(const double *D, const double *rs0, double *RS, int64_t NS, int R)
+{
+    __shared__ double sm[1024];
+    const int r = blockIdx.x;
+    const int64_t chunk = (NS + blockDim.x - 1) / blockDim.x;
+    const int64_t b = (int64_t) threadIdx.x * chunk;
+    const int64_t e = b + chunk < NS ? b + chunk : NS;
+    double s = 0;
+    for (int64_t i = b; i < e; i++) {
+        s += D[i * R + r];
+    }
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = rs0[r];
+        for (int j = 0; j < (int) blockDim.x; j++) {
+            double v = sm[j];
+            sm[j] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    double acc = sm[threadIdx.x];
+    for (int64_t i = b; i < e; i++) {
+        RS[i * R + r] = acc;
+        acc += D[i * R + r];
+    }
+}
+
+__global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_normalise,
+    double *result)
+{
+    const int R = q.R;
+    const int64_t total = (int64_t) q.Wn * R;
+    for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t) gridDim.x * blockDim.x) {
+        const int wdx = (int) (idx / R), r = (int) (idx % R);
+        const int32_t s0 = qd.win_span_lo[wdx], s1 = qd.win_span_hi[wdx];
+        double vb = 0, vs = 0;
+        for (int32_t s = s0; s <= s1; s++) {
+            int64_t li = qd.span_woff[s] + (wdx - qd.span_wlo[s]);
+            if (q.branch) {
+                vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
+            }
+            if (q.site) {
+                vs += w.SITE[li * R + r];
+            }
+        }
+        double span = qd.windows[wdx + 1] - qd.windows[wdx];
+        if (span_normalise) {
+            vb /= span;
+            vs /= span;
+        }
+        int64_t o = 0;
+        if (q.branch) {
+            result[idx] = vb;
+            o = total;
+        }
+        if (q.site) {
+            result[o + idx] = vs;
+        }
+    }
+}
+
+static int grid_for(int64_t n, int block = 256)
+{
+    int64_t g = (n + block - 1) / block;
+    return (int) std::max<int64_t>(1, std::min<int64_t>(g, 65535LL * 4));
+}
+
+static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace tsg
+
+using namespace tsg;
+
+struct tsg_query {
+    const tsg_treeseq_t *ts;
+    QueryParams p;
+    QueryDev d;
+    void *dbuf;              // device copy of per-query arrays (owned), or null
+    std::vector<char> blob;  // host image of the per-query arrays
+    int64_t off[6];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh
+    cudaEvent_t ev_start, ev_stop;  // optional events around the sweep kernel
+    int64_t total_span_windows;
+    int64_t num_slots;
+    int64_t ws_bytes;
+    int span_normalise;
+    uint32_t options;
+};
+
+namespace tsg {
+
+// Check the sample sets (c/tskit/trees.c:2114-2149 and the duplicate check of
+// 2174-2220) and build per-sample membership masks.
+static int check_sample_sets(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, std::vector<uint32_t> &mask)
+{
+    if (K == 0) {
+        return TSG_ERR_INSUFFICIENT_SAMPLE_SETS;
+    }
+    if (K > TSG_MAX_SAMPLE_SETS) {
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    mask.assign((size_t) ts->v.num_samples, 0u);
+    uint64_t j = 0;
+    for (uint64_t k = 0; k < K; k++) {
+        if (sizes[k] == 0) {
+            return TSG_ERR_EMPTY_SAMPLE_SET;
+        }
+        for (uint64_t l = 0; l < sizes[k]; l++) {
+            int32_t u = sets[j++];
+            if (u < 0 || u >= ts->v.num_nodes) {
+                return TSG_ERR_NODE_OUT_OF_BOUNDS;
+            }
+            int32_t si = ts->h_sample_index[(size_t) u];
+            if (si < 0) {
+                return TSG_ERR_BAD_SAMPLES;
+            }
+            if (mask[(size_t) si] & (1u << k)) {
+                return TSG_ERR_DUPLICATE_SAMPLE;
+            }
+            mask[(size_t) si] |= 1u << k;
+        }
+    }
+    return 0;
+}
+
+// trees.c:1244-1286 with TSK_REQUIRE_FULL_SPAN
+static int check_windows(const tsg_treeseq_t *ts, uint64_t Wn, const double *windows)
+{
+    if (Wn < 1) {
+        return TSG_ERR_BAD_NUM_WINDOWS;
+    }
+    if (windows[0] != 0 || windows[Wn] != ts->v.sequence_length) {
+        return TSG_ERR_BAD_WINDOWS;
+    }
+    for (uint64_t j = 0; j < Wn; j++) {
+        if (!(windows[j] < windows[j + 1])) {
+            return TSG_ERR_BAD_WINDOWS;
+        }
+    }
+    return 0;
+}
+
+static int tuple_width(int32_t type)
+{
+    switch (type) {
+        case TSG_DIVERSITY:
+        case TSG_SEGREGATING_SITES:
+        case TSG_Y1:
+            return 1;
+        case TSG_DIVERGENCE:
+        case TSG_Y2:
+        case TSG_F2:
+        case TSG_RELATEDNESS:
+        case TSG_RELATEDNESS_NONCENTRED:
+            return 2;
+        case TSG_Y3:
+        case TSG_F3:
+            return 3;
+        case TSG_F4:
+            return 4;
+        default:
+            return 0;
+    }
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_query_free(tsg_query_t *q)
+{
+    if (q != nullptr) {
+        cudaFree(q->dbuf);
+        delete q;
+    }
+    return 0;
+}
+
+int64_t tsg_query_workspace_bytes(const tsg_query_t *q) { return q->ws_bytes; }
+
+int64_t tsg_query_result_size(const tsg_query_t *q)
+{
+    return (int64_t) q->p.Wn * q->p.R * ((q->p.branch ? 1 : 0) + (q->p.site ? 1 : 0));
+}
+
+}  // extern "C"
+
+namespace tsg {
+
+static void query_bind(tsg_query_t *q, void *dev)
+{
+    char *b = (char *) dev;
+    q->d.sample_mask = (const uint32_t *) (b + q->off[0]);
+    q->d.windows = (const double *) (b + q->off[1]);
+    q->d.span_wlo = (const int32_t *) (b + q->off[2]);
+    q->d.span_woff = (const int64_t *) (b + q->off[3]);
+    q->d.win_span_lo = (const int32_t *) (b + q->off[4]);
+    q->d.win_span_hi = (const int32_t *) (b + q->off[5]);
+}
+
+// Validate the query and build its host image; the device copy is made by
+// the caller (its own allocation, or the tree sequence's staging buffer).
+static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t R, const tsg_output_t *outputs,
+    uint64_t Wn, const double *windows, uint32_t options)
+{
+    *out = nullptr;
+    int ret;
+    const uint32_t modes = options & (TSG_STAT_SITE | TSG_STAT_BRANCH | TSG_STAT_NODE);
+    bool site = options & TSG_STAT_SITE, branch = options & TSG_STAT_BRANCH;
+    if (options & TSG_STAT_NODE) {
+        return TSG_ERR_UNSUPPORTED_STAT_MODE;
+    }
+    if (options & TSG_STAT_BOTH_MODES) {
+        site = branch = true;
+    } else {
+        if (modes == 0) {
+            site = true;  // default mode is site (trees.c:2046-2049)
+        }
+        if (site && branch) {
+            return TSG_ERR_MULTIPLE_STAT_MODES;
+        }
+    }
+    if (R < 1) {
+        return TSG_ERR_BAD_RESULT_DIMS;
+    }
+    if (R > TSG_MAX_OUTPUTS) {
+        return TSG_ERR_TOO_MANY_OUTPUTS;
+    }
+    double default_windows[2] = { 0, ts->v.sequence_length };
+    if (windows == nullptr) {
+        Wn = 1;
+        windows = default_windows;
+    } else if ((ret = check_windows(ts, Wn, windows)) != 0) {
+        return ret;
+    }
+    std::vector<uint32_t> mask;
+    if ((ret = check_sample_sets(ts, K, sizes, sets, mask)) != 0) {
+        return ret;
+    }
+    tsg_query_t *q = new tsg_query_t();
+    std::memset(&q->p, 0, sizeof(q->p));
+    q->dbuf = nullptr;
+    q->ev_start = nullptr;
+    q->ev_stop = nullptr;
+    q->ts = ts;
+    q->options = options;
+    q->span_normalise = !!(options & TSG_STAT_SPAN_NORMALISE);
+    QueryParams &p = q->p;
+    p.K = (int32_t) K;
+    p.KP = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
+    p.R = (int32_t) R;
+    p.Wn = (int32_t) Wn;
+    p.branch = branch;
+    p.site = site;
+    p.polarised = !!(options & TSG_STAT_POLARISED);
+    p.f32 = !!(options & TSG_PRECISION_F32_KAHAN);
+    for (uint64_t k = 0; k < K; k++) {
+        p.set_size[k] = (double) sizes[k];
+    }
+    for (uint64_t r = 0; r < R; r++) {
+        int wdt = tuple_width(outputs[r].type);
+        if (wdt == 0) {
+            delete q;
+            return TSG_ERR_BAD_PARAM_VALUE;
+        }
+        p.term[r].type = outputs[r].type;
+        for (int j = 0; j < 4; j++) {
+            int32_t ix = j < wdt ? outputs[r].idx[j] : 0;
+            if (ix < 0 || ix >= (int32_t) K) {
+                delete q;
+                return TSG_ERR_BAD_SAMPLE_SET_INDEX;
+            }
+            p.term[r].idx[j] = ix;
+        }
+        if (outputs[r].type == TSG_RELATEDNESS) {
+            p.need_mean = 1;
+        }
+    }
+
+    // span <-> window overlap tables (host; spans and windows are few)
+    const int64_t NS = ts->v.num_spans;
+    const auto &bp = ts->h_breakpoints;
+    const auto &st = ts->h_span_tree;
+    std::vector<int32_t> wlo((size_t) NS), whi((size_t) NS);
+    std::vector<int64_t> woff((size_t) NS + 1);
+    woff[0] = 0;
+    for (int64_t s = 0; s < NS; s++) {
+        double b0 = bp[(size_t) st[(size_t) s]], b1 = bp[(size_t) st[(size_t) s + 1]];
+        int64_t lo = upper_bound(windows, (int64_t) Wn + 1, b0) - 1;
+        int64_t hi = lower_bound(windows, (int64_t) Wn + 1, b1) - 1;
+        lo = std::max<int64_t>(0, std::min<int64_t>(lo, (int64_t) Wn - 1));
+        hi = std::max<int64_t>(lo, std::min<int64_t>(hi, (int64_t) Wn - 1));
+        wlo[(size_t) s] = (int32_t) lo;
+        whi[(size_t) s] = (int32_t) hi;
+        woff[(size_t) s + 1] = woff[(size_t) s] + (hi - lo + 1);
+    }
+    std::vector<int32_t> wsl((size_t) Wn), wsh((size_t) Wn);
+    {
+        int64_t s = 0;
+        for (int64_t wdx = 0; wdx < (int64_t) Wn; wdx++) {
+            while (s < NS && whi[(size_t) s] < wdx) {
+                s++;
+            }
+            wsl[(size_t) wdx] = (int32_t) s;
+            int64_t e = s;
+            while (e + 1 < NS && wlo[(size_t) e + 1] <= wdx) {
+                e++;
+            }
+            wsh[(size_t) wdx] = (int32_t) e;
+        }
+    }
+    q->total_span_windows = woff[(size_t) NS];
+
+    // device copy of the per-query arrays, one allocation
+    const int64_t n = ts->v.num_samples;
+    int64_t off_mask = 0;
+    int64_t off_win = align_up(off_mask + std::max<int64_t>(n, 1) * 4, 256);
+    int64_t off_wlo = align_up(off_win + ((int64_t) Wn + 1) * 8, 256);
+    int64_t off_woff = align_up(off_wlo + NS * 4, 256);
+    int64_t off_wsl = align_up(off_woff + (NS + 1) * 8, 256);
+    int64_t off_wsh = align_up(off_wsl + (int64_t) Wn * 4, 256);
+    int64_t total = align_up(off_wsh + (int64_t) Wn * 4, 256);
+    q->blob.assign((size_t) total, 0);
+    char *h = q->blob.data();
+    std::memcpy(h + off_mask, mask.data(), (size_t) n * 4);
+    std::memcpy(h + off_win, windows, ((size_t) Wn + 1) * 8);
+    std::memcpy(h + off_wlo, wlo.data(), (size_t) NS * 4);
+    std::memcpy(h + off_woff, woff.data(), ((size_t) NS + 1) * 8);
+    std::memcpy(h + off_wsl, wsl.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_wsh, wsh.data(), (size_t) Wn * 4);
+    q->off[0] = off_mask;
+    q->off[1] = off_win;
+    q->off[2] = off_wlo;
+    q->off[3] = off_woff;
+    q->off[4] = off_wsl;
+    q->off[5] = off_wsh;
+
+    // workspace: per-slot node state + per-span accumulators
+    int blocks_per_sm = 0;
+    if (p.f32) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_sweep<float>, 256, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_sweep<double>, 256, 0);
+    }
+    int64_t slots = (int64_t) std::max(1, blocks_per_sm) * std::max(1, device_count_sms());
+    const int64_t per_slot = align_up(ts->v.num_nodes * (12 + 4 * (int64_t) p.KP), 256);
+    const int64_t budget = (int64_t) 24 << 30;  // node state at most 24 GiB
+    slots = std::min<int64_t>(slots, std::max<int64_t>(1, budget / std::max<int64_t>(per_slot, 1)));
+    slots = std::min<int64_t>(slots, std::max<int64_t>(NS, 1));
+    q->num_slots = slots;
+    p.num_slots = (int32_t) slots;
+    const int64_t TSW = q->total_span_windows;
+    int64_t bytes = 0;
+    bytes += align_up(slots * ts->v.num_nodes * 4, 256) * 3;          // parent, nchild, arrive
+    bytes += align_up(slots * ts->v.num_nodes * 4 * p.KP, 256);       // x
+    bytes += align_up(TSW * 8, 256);                                  // A
+    bytes += align_up(TSW * R * 8, 256) * 2;                          // B, SITE
+    bytes += align_up(NS * R * 8, 256) * 2;                           // D, RS
+    bytes += align_up((int64_t) R * 8, 256);                          // rs0
+    bytes += 256;                                                     // err, counter
+    q->ws_bytes = bytes;
+    *out = q;
+    return 0;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_query_create(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t R, const tsg_output_t *outputs,
+    uint64_t Wn, const double *windows, uint32_t options)
+{
+    tsg_query_t *q = nullptr;
+    int ret = query_build(&q, ts, K, sizes, sets, R, outputs, Wn, windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    if (cudaMalloc(&q->dbuf, q->blob.size()) != cudaSuccess) {
+        cudaGetLastError();
+        delete q;
+        return TSG_ERR_NO_MEMORY;
+    }
+    if (cudaMemcpy(q->dbuf, q->blob.data(), q->blob.size(), cudaMemcpyHostToDevice)
+        != cudaSuccess) {
+        tsg_query_free(q);
+        return TSG_ERR_CUDA;
+    }
+    query_bind(q, q->dbuf);
+    *out = q;
+    return 0;
+}
+
+int tsg_query_set_sweep_events(tsg_query_t *q, void *start_event, void *stop_event)
+{
+    q->ev_start = (cudaEvent_t) start_event;
+    q->ev_stop = (cudaEvent_t) stop_event;
+    return 0;
+}
+
+int tsg_workspace_create(tsg_workspace_t **ws)
+{
+    *ws = new tsg_workspace_t();
+    (*ws)->ptr = nullptr;
+    (*ws)->bytes = 0;
+    return 0;
+}
+
+int tsg_workspace_reserve(tsg_workspace_t *ws, int64_t bytes)
+{
+    if (bytes <= ws->bytes) {
+        return 0;
+    }
+    if (ws->ptr != nullptr) {
+        TSG_CUDA(cudaFree(ws->ptr));
+        ws->ptr = nullptr;
+        ws->bytes = 0;
+    }
+    if (cudaMalloc(&ws->ptr, (size_t) bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return TSG_ERR_NO_MEMORY;
+    }
+    ws->bytes = bytes;
+    return 0;
+}
+
+int64_t tsg_workspace_bytes(const tsg_workspace_t *ws) { return ws->bytes; }
+
+int tsg_workspace_free(tsg_workspace_t *ws)
+{
+    if (ws != nullptr) {
+        cudaFree(ws->ptr);
+        delete ws;
+    }
+    return 0;
+}
+
+int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
+    void *cuda_stream)
+{
+    if (ws == nullptr || ws->bytes < q->ws_bytes) {
+        return TSG_ERR_WORKSPACE_TOO_SMALL;
+    }
+    cudaStream_t st = (cudaStream_t) cuda_stream;
+    const tsg_treeseq_t *ts = q->ts;
+    const QueryParams &p = q->p;
+    const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans, TSW = q->total_span_windows;
+    const int64_t R = p.R, slots = q->num_slots;
+    char *b = (char *) ws->ptr;
+    WsDev w;
+    int64_t off = 0;
+    w.parent = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.nchild = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.arrive = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.x = (int32_t *) (b + off);
+    off += align_up(slots * N * 4 * p.KP, 256);
+    w.A = (double *) (b + off);
+    off += align_up(TSW * 8, 256);
+    w.B = (double *) (b + off);
+    off += align_up(TSW * R * 8, 256);
+    w.SITE = (double *) (b + off);
+    off += align_up(TSW * R * 8, 256);
+    w.D = (double *) (b + off);
+    off += align_up(NS * R * 8, 256);
+    w.RS = (double *) (b + off);
+    off += align_up(NS * R * 8, 256);
+    w.rs0 = (double *) (b + off);
+    off += align_up(R * 8, 256);
+    w.err = (int32_t *) (b + off);
+    w.counter = w.err + 1;
+
+    TSG_CUDA(cudaMemsetAsync(w.err, 0, 2 * sizeof(int32_t), st));
+    TSG_CUDA(cudaMemsetAsync(w.rs0, 0, (size_t) R * 8, st));
+    if (q->ev_start != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_start, st));
+    }
+    if (p.f32) {
+        k_sweep<float><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
+    } else {
+        k_sweep<double><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
+    }
+    TSG_LAUNCHED();
+    if (q->ev_stop != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_stop, st));
+    }
+    if (p.branch) {
+        k_span_scan<<<(unsigned) R, 1024, 0, st>>>(w.D, w.rs0, w.RS, NS, (int) R);
+        TSG_LAUNCHED();
+    }
+    k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, q->d, w, q->span_normalise,
+        result);
+    TSG_LAUNCHED();
+    return 0;
+}
+
+// Error word of the last launch on this workspace (synchronous read).
+int tsg_workspace_check(const tsg_workspace_t *ws, const tsg_query_t *q)
+{
+    // the error word sits at the tail of the query's layout
+    int32_t h = 0;
+    const char *b = (const char *) ws->ptr;
+    const int64_t off = q->ws_bytes - 256;
+    TSG_CUDA(cudaMemcpy(&h, b + off, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return h == 0 ? 0 : TSG_ERR_DEVICE_CHECK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------- host entry points
+namespace tsg {
+
+// The synchronous entry points reuse the tree sequence's own workspace and
+// staging buffer (grown on demand, serialised by a mutex), so a call makes no
+// device allocation once they are large enough.
+static int run_sync(const tsg_treeseq_t *cts, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
+    const double *windows, uint32_t options, double *result)
+{
+    tsg_treeseq_t *ts = const_cast<tsg_treeseq_t *>(cts);
+    tsg_query_t *q = nullptr;
+    int ret = query_build(&q, ts, K, sizes, sets, R, outs, Wn, windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    std::lock_guard<std::mutex> lock(ts->sync_mutex);
+    const int64_t nres = tsg_query_result_size(q);
+    const int64_t blob = align_up((int64_t) q->blob.size(), 256);
+    const int64_t need = blob + nres * 8;
+    cudaStream_t st = ts->sync_stream;
+    if (ts->sync_ws == nullptr) {
+        tsg_workspace_create(&ts->sync_ws);
+    }
+    if ((ret = tsg_workspace_reserve(ts->sync_ws, q->ws_bytes)) != 0) {
+        tsg_query_free(q);
+        return ret;
+    }
+    if (need > ts->stage_bytes) {
+        cudaFree(ts->stage);
+        ts->stage = nullptr;
+        ts->stage_bytes = 0;
+        if (cudaMalloc(&ts->stage, (size_t) need) != cudaSuccess) {
+            cudaGetLastError();
+            tsg_query_free(q);
+            return TSG_ERR_NO_MEMORY;
+        }
+        ts->stage_bytes = need;
+    }
+    double *d_res = (double *) ((char *) ts->stage + blob);
+    if (cudaMemcpyAsync(ts->stage, q->blob.data(), q->blob.size(), cudaMemcpyHostToDevice, st)
+        != cudaSuccess) {
+        tsg_query_free(q);
+        return TSG_ERR_CUDA;
+    }
+    query_bind(q, ts->stage);
+    if ((ret = tsg_query_launch(q, ts->sync_ws, d_res, st)) == 0) {
+        if (cudaMemcpyAsync(result, d_res, (size_t) nres * 8, cudaMemcpyDeviceToHost, st)
+                != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else {
+            ret = tsg_workspace_check(ts->sync_ws, q);
+        }
+    }
+    tsg_query_free(q);
+    return ret;
+}
+
+static int one_way(const tsg_treeseq_t *ts, int32_t type, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t Wn, const double *windows, uint32_t options, double *result)
+{
+    if (K == 0) {
+        return TSG_ERR_INSUFFICIENT_SAMPLE_SETS;
+    }
+    std::vector<tsg_output_t> outs((size_t) K);
+    for (uint64_t k = 0; k < K; k++) {
+        outs[(size_t) k].type = type;
+        outs[(size_t) k].idx[0] = (int32_t) k;
+        outs[(size_t) k].idx[1] = outs[(size_t) k].idx[2] = outs[(size_t) k].idx[3] = 0;
+    }
+    return run_sync(ts, K, sizes, sets, K, outs.data(), Wn, windows, options, result);
+}
+
+static int k_way(const tsg_treeseq_t *ts, int32_t type, int width, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t num_tuples, const int32_t *tuples,
+    uint64_t Wn, const double *windows, uint32_t options, double *result)
+{
+    // check_sample_stat_inputs (c/tskit/trees.c:4667-4688)
+    if (K < 1) {
+        return TSG_ERR_INSUFFICIENT_SAMPLE_SETS;
+    }
+    if (num_tuples < 1) {
+        return TSG_ERR_INSUFFICIENT_INDEX_TUPLES;
+    }
+    std::vector<tsg_output_t> outs((size_t) num_tuples);
+    for (uint64_t r = 0; r < num_tuples; r++) {
+        outs[(size_t) r].type = type;
+        for (int j = 0; j < 4; j++) {
+            int32_t ix = j < width ? tuples[r * width + j] : 0;
+            if (ix < 0 || ix >= (int32_t) K) {
+                return TSG_ERR_BAD_SAMPLE_SET_INDEX;
+            }
+            outs[(size_t) r].idx[j] = ix;
+        }
+    }
+    return run_sync(ts, K, sizes, sets, num_tuples, outs.data(), Wn, windows, options, result);
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_treeseq_sample_count_stat(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t R, const tsg_output_t *outputs, uint64_t Wn,
+    const double *windows, uint32_t options, double *result)
+{
+    return run_sync(self, K, sizes, sets, R, outputs, Wn, windows, options, result);
+}
+
+int tsg_treeseq_diversity(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t Wn, const double *windows, uint32_t options, double *result)
+{
+    return one_way(self, TSG_DIVERSITY, K, sizes, sets, Wn, windows, options, result);
+}
+
+int tsg_treeseq_segregating_sites(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t Wn, const double *windows, uint32_t options, double *result)
+{
+    return one_way(self, TSG_SEGREGATING_SITES, K, sizes, sets, Wn, windows, options, result);
+}
+
+int tsg_treeseq_Y1(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t Wn, const double *windows, uint32_t options, double *result)
+{
+    return one_way(self, TSG_Y1, K, sizes, sets, Wn, windows, options, result);
+}
+
+#define TSG_K_WAY(name, type, width)                                                     \
+    int name(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,               \
+        const int32_t *sets, uint64_t nt, const int32_t *tuples, uint64_t Wn,            \
+        const double *windows, uint32_t options, double *result)                         \
+    {                                                                                    \
+        return k_way(self, type, width, K, sizes, sets, nt, tuples, Wn, windows, options, \
+            result);                                                                     \
+    }
+
+TSG_K_WAY(tsg_treeseq_divergence, TSG_DIVERGENCE, 2)
+TSG_K_WAY(tsg_treeseq_Y2, TSG_Y2, 2)
+TSG_K_WAY(tsg_treeseq_f2, TSG_F2, 2)
+TSG_K_WAY(tsg_treeseq_Y3, TSG_Y3, 3)
+TSG_K_WAY(tsg_treeseq_f3, TSG_F3, 3)
+TSG_K_WAY(tsg_treeseq_f4, TSG_F4, 4)
+
+int tsg_treeseq_genetic_relatedness(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t nt, const int32_t *tuples, uint64_t Wn, const double *windows,
+    uint32_t options, double *result)
+{
+    int32_t type = (options & TSG_STAT_NONCENTRED) ? TSG_RELATEDNESS_NONCENTRED : TSG_RELATEDNESS;
+    return k_way(self, type, 2, K, sizes, sets, nt, tuples, Wn, windows, options, result);
+}
+
+}  // extern "C"

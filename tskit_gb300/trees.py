@@ -1,0 +1,555 @@
+"""Drop-in ``TreeSequence`` statistics on the GPU.
+
+The methods keep the signatures, defaults, output shapes and dimension
+dropping of the reference's ``tskit.TreeSequence`` statistics
+(python/tskit/trees.py:7911-10430); the arithmetic runs in the CUDA kernels
+behind the C ABI (include/tskit_gb300.h).  The tables live on the device as
+PyTorch tensors; the derived per-tree-sequence state is built there once.
+
+Statistics that the reference computes with several traversals (Fst,
+Tajima's D, relatedness as a proportion) are computed here in one fused
+sweep whose summary terms are the same functions.
+"""
+from __future__ import annotations
+
+import ctypes
+import numbers
+
+import numpy as np
+
+from . import _native as nat
+from .tables import Tables
+
+
+def _require_torch_cuda():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "tskit_gb300 needs a CUDA device: the statistics have no CPU implementation"
+        )
+    return torch
+
+
+def safe_np_int_cast(int_array, dtype, copy=False):
+    """Cast to an integer dtype, refusing lossy conversions (same contract as
+    python/tskit/util.py:98-132)."""
+    if not isinstance(int_array, np.ndarray):
+        int_array = np.array(int_array)
+        copy = False
+    if int_array.size == 0:
+        return int_array.astype(dtype, copy=copy)
+    try:
+        return int_array.astype(dtype, casting="safe", copy=copy)
+    except TypeError:
+        if int_array.dtype == np.dtype("O"):
+            raise TypeError("Cannot convert to a rectangular array.")
+        bounds = np.iinfo(dtype)
+        if np.any(int_array < bounds.min) or np.any(int_array > bounds.max):
+            raise OverflowError(f"Cannot convert safely to {dtype} type")
+        if int_array.dtype.kind == "i" and np.dtype(dtype).kind == "u":
+            casting = "unsafe"
+        else:
+            casting = "same_kind"
+        return int_array.astype(dtype, casting=casting, copy=copy)
+
+
+def _parse_mode(mode):
+    if mode is None or mode == "site":
+        return nat.STAT_SITE
+    if mode == "branch":
+        return nat.STAT_BRANCH
+    if mode == "node":
+        return nat.STAT_NODE
+    raise ValueError("Unrecognised stats mode")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size > 0 else None
+
+
+class Workspace:
+    """Device scratch for query launches (owned by the caller)."""
+
+    def __init__(self, nbytes=0):
+        self._lib = nat.load()
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_workspace_create(ctypes.byref(h)))
+        self.handle = h
+        if nbytes:
+            self.reserve(nbytes)
+
+    def reserve(self, nbytes):
+        nat.check(self._lib.tsg_workspace_reserve(self.handle, int(nbytes)))
+
+    @property
+    def nbytes(self):
+        return self._lib.tsg_workspace_bytes(self.handle)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self._lib.tsg_workspace_free(h)
+            self.handle = None
+
+
+class Query:
+    """A prepared fused sample-count query (device resident).
+
+    ``terms`` is a list of (type, (i, j, k, l)) summary terms over the sample
+    sets.  ``launch(result, stream)`` enqueues the kernels; ``result`` is a
+    float64 CUDA tensor of ``result_size`` elements laid out
+    (modes, windows, terms).
+    """
+
+    def __init__(self, ts, sample_sets, terms, windows, flags):
+        self._lib = nat.load()
+        self.ts = ts
+        sizes = np.array([len(s) for s in sample_sets], dtype=np.uint64)
+        flat = (np.concatenate([np.asarray(s) for s in sample_sets])
+                if len(sample_sets) else np.zeros(0))
+        flat = safe_np_int_cast(flat, np.int32)
+        outs = (nat.Output_t * max(1, len(terms)))()
+        for r, (typ, idx) in enumerate(terms):
+            outs[r].type = int(typ)
+            idx = list(idx) + [0] * (4 - len(idx))
+            for q in range(4):
+                outs[r].idx[q] = int(idx[q])
+        win = None if windows is None else np.ascontiguousarray(windows, dtype=np.float64)
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_query_create(
+            ctypes.byref(h), ts._handle, len(sizes), _ptr(sizes), _ptr(flat), len(terms),
+            ctypes.cast(outs, ctypes.c_void_p), 0 if win is None else len(win) - 1, _ptr(win),
+            flags,
+        ))
+        self.handle = h
+        self.num_terms = len(terms)
+        self.num_windows = 1 if win is None else len(win) - 1
+        self.result_size = self._lib.tsg_query_result_size(h)
+        self.workspace_bytes = self._lib.tsg_query_workspace_bytes(h)
+
+    def launch(self, workspace, result, stream=None):
+        torch = _require_torch_cuda()
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        if workspace.nbytes < self.workspace_bytes:
+            workspace.reserve(self.workspace_bytes)
+        nat.check(self._lib.tsg_query_launch(
+            self.handle, workspace.handle, ctypes.c_void_p(result.data_ptr()),
+            ctypes.c_void_p(stream.cuda_stream),
+        ))
+
+    def check(self, workspace):
+        nat.check(self._lib.tsg_workspace_check(workspace.handle, self.handle))
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self._lib.tsg_query_free(h)
+            self.handle = None
+
+
+class TreeSequence:
+    """A tree sequence resident on the GPU with the reference's statistics API."""
+
+    def __init__(self, tables: Tables, num_spans=0):
+        torch = _require_torch_cuda()
+        self._lib = nat.load()
+        tables.check()
+        self.tables = tables
+        allele, alt, _ = tables.allele_codes()
+        dev = torch.device("cuda")
+
+        def up(a, dtype):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            if a.size == 0:
+                a = np.zeros(1, dtype=dtype)
+            return torch.from_numpy(a).to(dev)
+
+        t = tables
+        self._dev = dict(
+            node_time=up(t.node_time, np.float64),
+            node_flags=up(t.node_flags.astype(np.int32), np.int32),
+            edge_left=up(t.edge_left, np.float64),
+            edge_right=up(t.edge_right, np.float64),
+            edge_parent=up(t.edge_parent, np.int32),
+            edge_child=up(t.edge_child, np.int32),
+            edge_insertion_order=up(t.edge_insertion_order, np.int32),
+            edge_removal_order=up(t.edge_removal_order, np.int32),
+            site_position=up(t.site_position, np.float64),
+            mutation_site=up(t.mutation_site, np.int32),
+            mutation_node=up(t.mutation_node, np.int32),
+            mutation_allele=up(allele, np.int32),
+            mutation_alt_allele=up(alt, np.int32),
+        )
+        tt = nat.Tables_t()
+        tt.sequence_length = t.sequence_length
+        tt.num_nodes = t.num_nodes
+        tt.num_edges = t.num_edges
+        tt.num_sites = t.num_sites
+        tt.num_mutations = t.num_mutations
+        for k, v in self._dev.items():
+            setattr(tt, k, v.data_ptr())
+        torch.cuda.synchronize()
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_treeseq_init(ctypes.byref(h), ctypes.byref(tt), int(num_spans),
+                                             nat.TABLES_ON_DEVICE))
+        self._handle = h
+        self._samples = t.samples()
+        self._breakpoints = None
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            self._lib.tsg_treeseq_free(h)
+            self._handle = None
+
+    # ----------------------------------------------------------- properties
+    @property
+    def sequence_length(self):
+        return self.tables.sequence_length
+
+    @property
+    def num_samples(self):
+        return len(self._samples)
+
+    @property
+    def num_nodes(self):
+        return self.tables.num_nodes
+
+    @property
+    def num_edges(self):
+        return self.tables.num_edges
+
+    @property
+    def num_sites(self):
+        return self.tables.num_sites
+
+    @property
+    def num_mutations(self):
+        return self.tables.num_mutations
+
+    @property
+    def num_trees(self):
+        return self._lib.tsg_treeseq_get_num_trees(self._handle)
+
+    @property
+    def num_spans(self):
+        return self._lib.tsg_treeseq_get_num_spans(self._handle)
+
+    @property
+    def sites_position(self):
+        return self.tables.site_position
+
+    def samples(self):
+        return self._samples.copy()
+
+    def breakpoints(self, as_array=False):
+        if self._breakpoints is None:
+            bp = np.zeros(self.num_trees + 1)
+            nat.check(self._lib.tsg_treeseq_get_breakpoints(self._handle, _ptr(bp)))
+            self._breakpoints = bp
+        if as_array:
+            return self._breakpoints.copy()
+        return iter(self._breakpoints)
+
+    # ------------------------------------------------------- window parsing
+    def parse_windows(self, windows):
+        """Same rules as python/tskit/trees.py:8108-8131."""
+        if windows is None:
+            windows = [0.0, self.sequence_length]
+        elif isinstance(windows, str):
+            if windows == "trees":
+                windows = self.breakpoints(as_array=True)
+            elif windows == "sites":
+                windows = np.concatenate(
+                    [[] if self.num_sites > 0 else [0.0], self.sites_position,
+                     [self.sequence_length]]
+                )
+                windows[0] = 0.0
+            else:
+                raise ValueError(
+                    f"Unrecognized window specification {windows}:",
+                    "the only allowed strings are 'sites' or 'trees'",
+                )
+        return np.array(windows)
+
+    # --------------------------------------------------- low-level layer
+    def _ll_terms(self, terms, sample_set_sizes, sample_sets, windows, mode, span_normalise,
+                  polarised, extra=0):
+        """Low-level fused call: returns (num_windows, num_terms) float64 (or
+        (2, num_windows, num_terms) with both modes)."""
+        flags = _parse_mode(mode) if not (extra & nat.STAT_BOTH_MODES) else 0
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        flags |= extra
+        sizes = np.ascontiguousarray(sample_set_sizes, dtype=np.uint64)
+        flat = np.ascontiguousarray(sample_sets, dtype=np.int32)
+        if np.sum(sizes) != len(flat):
+            raise ValueError("Sum of sample_set_sizes must equal length of sample_sets array")
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        Wn = len(win) - 1
+        outs = (nat.Output_t * max(1, len(terms)))()
+        for r, (typ, idx) in enumerate(terms):
+            outs[r].type = int(typ)
+            idx = list(idx) + [0] * (4 - len(idx))
+            for q in range(4):
+                outs[r].idx[q] = int(idx[q])
+        nmodes = 2 if extra & nat.STAT_BOTH_MODES else 1
+        res = np.zeros((nmodes, Wn, len(terms)))
+        nat.check(self._lib.tsg_treeseq_sample_count_stat(
+            self._handle, len(sizes), _ptr(sizes), _ptr(flat), len(terms),
+            ctypes.cast(outs, ctypes.c_void_p), Wn, _ptr(win), flags, _ptr(res),
+        ))
+        return res if nmodes == 2 else res[0]
+
+    def _ll_one_way(self, typ):
+        def method(sample_set_sizes, sample_sets, windows, mode=None, span_normalise=True,
+                   polarised=False):
+            K = len(sample_set_sizes)
+            return self._ll_terms([(typ, (k,)) for k in range(K)], sample_set_sizes,
+                                  sample_sets, windows, mode, span_normalise, polarised)
+        return method
+
+    def _ll_k_way(self, typ, k):
+        def method(sample_set_sizes, sample_sets, indexes, windows, mode=None,
+                   span_normalise=True, polarised=False, centre=True):
+            indexes = np.asarray(indexes, dtype=np.int32).reshape(-1, k)
+            if len(indexes) < 1:
+                raise nat.LibraryError(nat.ERR_INSUFFICIENT_INDEX_TUPLES)
+            t = typ
+            if typ == nat.RELATEDNESS and not centre:
+                t = nat.RELATEDNESS_NONCENTRED
+            return self._ll_terms([(t, tuple(ix)) for ix in indexes], sample_set_sizes,
+                                  sample_sets, windows, mode, span_normalise, polarised)
+        return method
+
+    # ------------------------------------------------ python-level framework
+    def __run_windowed_stat(self, windows, method, *args, **kwargs):
+        strip_win = windows is None
+        windows = self.parse_windows(windows)
+        stat = method(*args, **kwargs, windows=windows)
+        if strip_win:
+            stat = stat[0]
+        return stat
+
+    def __one_way_sample_set_stat(self, ll_method, sample_sets, windows=None, mode=None,
+                                  span_normalise=True, polarised=False):
+        if sample_sets is None:
+            sample_sets = self.samples()
+        drop_dimension = False
+        try:
+            sample_sets = np.array(sample_sets, dtype=np.uint64)
+        except ValueError:
+            pass
+        else:
+            if len(sample_sets.shape) == 1:
+                sample_sets = [sample_sets]
+                drop_dimension = True
+        sample_set_sizes = np.array([len(s) for s in sample_sets], dtype=np.uint32)
+        if np.any(sample_set_sizes == 0):
+            raise ValueError("Sample sets must contain at least one element")
+        flattened = safe_np_int_cast(np.hstack(sample_sets), np.int32)
+        stat = self.__run_windowed_stat(windows, ll_method, sample_set_sizes, flattened,
+                                        mode=mode, span_normalise=span_normalise,
+                                        polarised=polarised)
+        if drop_dimension:
+            stat = stat.reshape(stat.shape[:-1])
+            if stat.shape == () and windows is None:
+                stat = stat[()]
+        return stat
+
+    def __k_way_sample_set_stat(self, ll_method, k, sample_sets, indexes=None, windows=None,
+                                mode=None, span_normalise=True, polarised=False, centre=True):
+        sample_set_sizes = np.array([len(s) for s in sample_sets], dtype=np.uint32)
+        if np.any(sample_set_sizes == 0):
+            raise ValueError("Sample sets must contain at least one element")
+        flattened = safe_np_int_cast(np.hstack(sample_sets), np.int32)
+        drop_based_on_index = False
+        if indexes is None:
+            drop_based_on_index = True
+            if len(sample_sets) != k:
+                raise ValueError(
+                    "Must specify indexes if there are not exactly {} sample sets.".format(k)
+                )
+            indexes = np.arange(k, dtype=np.int32)
+        drop_dimension = False
+        indexes = safe_np_int_cast(indexes, np.int32)
+        if len(indexes.shape) == 1:
+            indexes = indexes.reshape((1, indexes.shape[0]))
+            drop_dimension = True
+        if len(indexes.shape) != 2 or indexes.shape[1] != k:
+            raise ValueError(
+                "Indexes must be convertable to a 2D numpy array with {} columns".format(k)
+            )
+        stat = self.__run_windowed_stat(windows, ll_method, sample_set_sizes, flattened,
+                                        indexes, mode=mode, span_normalise=span_normalise,
+                                        polarised=polarised, centre=centre)
+        if drop_dimension:
+            stat = stat.reshape(stat.shape[:-1])
+            if stat.shape == () and windows is None and drop_based_on_index:
+                stat = stat[()]
+        return stat
+
+    # ------------------------------------------------------------ one-way
+    def diversity(self, sample_sets=None, windows=None, mode="site", span_normalise=True):
+        """Mean pairwise diversity (python/tskit/trees.py:8496-8556)."""
+        return self.__one_way_sample_set_stat(self._ll_one_way(nat.DIVERSITY), sample_sets,
+                                              windows=windows, mode=mode,
+                                              span_normalise=span_normalise)
+
+    def segregating_sites(self, sample_sets=None, windows=None, mode="site",
+                          span_normalise=True):
+        """python/tskit/trees.py:9790-9842"""
+        return self.__one_way_sample_set_stat(self._ll_one_way(nat.SEGREGATING_SITES),
+                                              sample_sets, windows=windows, mode=mode,
+                                              span_normalise=span_normalise)
+
+    def Y1(self, sample_sets, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:10235-10270"""
+        return self.__one_way_sample_set_stat(self._ll_one_way(nat.Y1), sample_sets,
+                                              windows=windows, mode=mode,
+                                              span_normalise=span_normalise)
+
+    # ------------------------------------------------------------- k-way
+    def divergence(self, sample_sets, indexes=None, windows=None, mode="site",
+                   span_normalise=True):
+        """python/tskit/trees.py:8558-8627"""
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.DIVERGENCE, 2), 2, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def Y2(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.Y2, 2), 2, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def f2(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.F2, 2), 2, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def Y3(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:10138-10189"""
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.Y3, 3), 3, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def f3(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.F3, 3), 3, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def f4(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        return self.__k_way_sample_set_stat(self._ll_k_way(nat.F4, 4), 4, sample_sets,
+                                            indexes=indexes, windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    def genetic_relatedness(self, sample_sets, indexes=None, windows=None, mode="site",
+                            span_normalise=True, polarised=True, proportion=True,
+                            centre=True):
+        """python/tskit/trees.py:8830-8976.  With proportion=True the
+        denominator (segregating sites of the union of the sets) is a fused
+        extra term of the same sweep."""
+        if not proportion:
+            return self.__k_way_sample_set_stat(
+                self._ll_k_way(nat.RELATEDNESS, 2), 2, sample_sets, indexes=indexes,
+                windows=windows, mode=mode, span_normalise=span_normalise,
+                polarised=polarised, centre=centre)
+        all_samples = np.array(list({u for s in sample_sets for u in s}))
+        K = len(sample_sets)
+
+        def ll(sample_set_sizes, flattened, indexes, windows, mode=None, span_normalise=True,
+               polarised=False, centre=True):
+            idx = np.asarray(indexes, dtype=np.int32).reshape(-1, 2)
+            t = nat.RELATEDNESS if centre else nat.RELATEDNESS_NONCENTRED
+            terms = [(t, tuple(ix)) for ix in idx]
+            # centred relatedness averages over the K original sets only, so the
+            # union set's term runs as a separate (polarised=False) query
+            num = self._ll_terms(terms, sample_set_sizes, flattened, windows, mode,
+                                 span_normalise, polarised)
+            den = self._ll_terms([(nat.SEGREGATING_SITES, (0,))], [len(all_samples)],
+                                 safe_np_int_cast(all_samples, np.int32), windows, mode,
+                                 span_normalise, False)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                return num / den
+        del K
+        return self.__k_way_sample_set_stat(ll, 2, sample_sets, indexes=indexes,
+                                            windows=windows, mode=mode,
+                                            span_normalise=span_normalise,
+                                            polarised=polarised, centre=centre)
+
+    # ------------------------------------------------------ derived stats
+    def Tajimas_D(self, sample_sets=None, windows=None, mode="site"):
+        """python/tskit/trees.py:9967-10022; diversity and segregating sites
+        come from one fused sweep."""
+
+        def tjd_func(sample_set_sizes, flattened, windows, mode=None, span_normalise=True,
+                     polarised=False):
+            n = np.asarray(sample_set_sizes)
+            K = len(n)
+            terms = [(nat.DIVERSITY, (k,)) for k in range(K)]
+            terms += [(nat.SEGREGATING_SITES, (k,)) for k in range(K)]
+            both = self._ll_terms(terms, sample_set_sizes, flattened, windows, mode,
+                                  span_normalise, polarised)
+            T, S = both[:, :K], both[:, K:]
+            h = np.array([np.sum(1 / np.arange(1, nn)) for nn in n])
+            g = np.array([np.sum(1 / np.arange(1, nn) ** 2) for nn in n])
+            with np.errstate(invalid="ignore", divide="ignore"):
+                a = (n + 1) / (3 * (n - 1) * h) - 1 / h**2
+                b = 2 * (n**2 + n + 3) / (9 * n * (n - 1)) - (n + 2) / (h * n) + g / h**2
+                D = (T - S / h) / np.sqrt(a * S + (b / (h**2 + g)) * S * (S - 1))
+            return D
+
+        return self.__one_way_sample_set_stat(tjd_func, sample_sets, windows=windows,
+                                              mode=mode, span_normalise=False)
+
+    def Fst(self, sample_sets, indexes=None, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:10024-10136; divergences and diversities come
+        from one fused sweep."""
+
+        def fst_func(sample_set_sizes, flattened, indexes, windows, mode, span_normalise,
+                     polarised, centre):
+            K = len(sample_set_sizes)
+            idx = np.asarray(indexes, dtype=np.int32).reshape(-1, 2)
+            terms = [(nat.DIVERGENCE, tuple(ix)) for ix in idx]
+            terms += [(nat.DIVERSITY, (k,)) for k in range(K)]
+            both = self._ll_terms(terms, sample_set_sizes, flattened, windows, mode,
+                                  span_normalise, polarised)
+            dvg, dvs = both[:, : len(idx)], both[:, len(idx):]
+            fst = np.ones_like(dvg)
+            for i, (u, v) in enumerate(idx):
+                denom = dvs[:, u] + dvs[:, v] + 2 * dvg[:, i]
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    fst[:, i] -= 2 * (dvs[:, u] + dvs[:, v]) / denom
+            return fst
+
+        return self.__k_way_sample_set_stat(fst_func, 2, sample_sets, indexes=indexes,
+                                            windows=windows, mode=mode,
+                                            span_normalise=span_normalise)
+
+    # ------------------------------------------------------- fused batches
+    def query(self, sample_sets, terms, windows=None, mode="branch", span_normalise=True,
+              polarised=False, both_modes=False, precision="f64"):
+        """Prepare a device-resident fused query (see :class:`Query`)."""
+        flags = 0
+        if both_modes:
+            flags |= nat.STAT_BOTH_MODES
+        else:
+            flags |= _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        if precision == "f32":
+            flags |= nat.PRECISION_F32_KAHAN
+        elif precision != "f64":
+            raise ValueError("precision must be 'f64' or 'f32'")
+        if isinstance(windows, (str,)) or (windows is not None and not isinstance(
+                windows, np.ndarray) and not isinstance(windows, numbers.Number)):
+            windows = self.parse_windows(windows)
+        return Query(self, sample_sets, terms, windows, flags)
