@@ -370,9 +370,14 @@ def run_gpu(args):
     ws = tskit_gb300.Workspace(q.workspace_bytes)
     res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    ev_sweep0, ev_sweep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
     stream = torch.cuda.current_stream()
+    ev_sweep0, ev_sweep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # torch creates the CUDA events on first record; the library re-records
+    # them around the sweep kernel of every launch
+    ev_sweep0.record(stream)
+    ev_sweep1.record(stream)
+    torch.cuda.synchronize()
+    lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
 
     for _ in range(args.warmup):
         flush.zero_()

@@ -37,6 +37,21 @@ def test_golden(name, case, cuda_lib):
     expected = data[case["key"]]
     got = np.asarray(getattr(ts, case["method"])(**resolve(case["kwargs"], data)))
     assert got.shape == expected.shape
+    if case["method"] == "Tajimas_D":
+        # D = (T - S/h) / sqrt(a S + b S (S-1)); for sets of 2-3 samples both
+        # numerator and denominator vanish in exact arithmetic, so the sign
+        # of the infinity depends on the last bit of T and S.  Where the
+        # reference's value is not finite, require ours not finite too and
+        # check T and S themselves.
+        bad = ~np.isfinite(expected)
+        assert np.all(~np.isfinite(got[bad]))
+        got, expected = got[~bad], expected[~bad]
+        kw = resolve(case["kwargs"], data)
+        for m in ("diversity", "segregating_sites"):
+            a = getattr(ts, m)(**dict(kw, span_normalise=False))
+            b = O.call(O.OracleTS(ts.tables), m, dict(kw, span_normalise=False))
+            np.testing.assert_allclose(np.ravel(a), np.ravel(b), rtol=RTOL_F64, atol=1e-13,
+                                       equal_nan=True)
     np.testing.assert_allclose(got, expected, rtol=RTOL_F64, atol=1e-13, equal_nan=True)
 
 

@@ -233,7 +233,10 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
             init_node(pc.x);
             init_node(pc.y);
         }
-        const int32_t ie0 = ts.tree_in[t0 + 1 <= t1 ? t0 + 1 : t1], ie1 = ts.tree_in[t1];
+        // the span also replays the transition into the next span's first tree
+        // (its running-sum change belongs to this span's total)
+        const int32_t t_end = t1 < ts.num_trees ? t1 + 1 : t1;
+        const int32_t ie0 = ts.tree_in[t0 + 1 <= t1 ? t0 + 1 : t1], ie1 = ts.tree_in[t_end];
         for (int32_t i = ie0 + threadIdx.x; i < ie1; i += blockDim.x) {
             init_node(ts.ins_parent[i]);
             init_node(ts.ins_child[i]);
@@ -365,33 +368,37 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
                 }
             };
 
+            // apply the removals (O order) and insertions (I order) entering tree t
+            auto transition = [&](int32_t t) {
+                for (int32_t i = ts.tree_out[t]; i < ts.tree_out[t + 1]; i++) {
+                    int32_t c = ts.rem_child[i], p = ts.rem_parent[i];
+                    int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
+                    if (q.branch) {
+                        F bl = (F) (time[p] - time[c]);
+                        for (int pp = 0; pp < passes; pp++) {
+                            cum[pp].add(-bl * eval_branch<F>(q, xc, pp));
+                        }
+                    }
+                    parent[c] = -1;
+                    walk(p, xc, -1);
+                }
+                for (int32_t i = ts.tree_in[t]; i < ts.tree_in[t + 1]; i++) {
+                    int32_t c = ts.ins_child[i], p = ts.ins_parent[i];
+                    parent[c] = p;
+                    int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
+                    if (q.branch) {
+                        F bl = (F) (time[p] - time[c]);
+                        for (int pp = 0; pp < passes; pp++) {
+                            cum[pp].add(bl * eval_branch<F>(q, xc, pp));
+                        }
+                    }
+                    walk(p, xc, +1);
+                }
+            };
+
             for (int32_t t = t0; t < t1; t++) {
                 if (t > t0) {
-                    // removals entering tree t (O order), then insertions (I order)
-                    for (int32_t i = ts.tree_out[t]; i < ts.tree_out[t + 1]; i++) {
-                        int32_t c = ts.rem_child[i], p = ts.rem_parent[i];
-                        int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
-                        if (q.branch) {
-                            F bl = (F) (time[p] - time[c]);
-                            for (int pp = 0; pp < passes; pp++) {
-                                cum[pp].add(-bl * eval_branch<F>(q, xc, pp));
-                            }
-                        }
-                        parent[c] = -1;
-                        walk(p, xc, -1);
-                    }
-                    for (int32_t i = ts.tree_in[t]; i < ts.tree_in[t + 1]; i++) {
-                        int32_t c = ts.ins_child[i], p = ts.ins_parent[i];
-                        parent[c] = p;
-                        int xc = lane < K ? x[(int64_t) c * KP + lane] : 0;
-                        if (q.branch) {
-                            F bl = (F) (time[p] - time[c]);
-                            for (int pp = 0; pp < passes; pp++) {
-                                cum[pp].add(bl * eval_branch<F>(q, xc, pp));
-                            }
-                        }
-                        walk(p, xc, +1);
-                    }
+                    transition(t);
                 }
                 const double tl = ts.breakpoints[t], tr = ts.breakpoints[t + 1];
                 if (q.branch) {
@@ -455,6 +462,9 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
                 }
             }
             if (q.branch) {
+                if (t1 < ts.num_trees) {
+                    transition(t1);
+                }
                 for (int p = 0; p < passes; p++) {
                     int r = lane + 32 * p;
                     if (r < R) {
