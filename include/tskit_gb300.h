@@ -40,6 +40,9 @@ extern "C" {
  * and the arithmetic of the bulk accumulation. */
 #define TSG_STAT_BOTH_MODES (1u << 20)
 #define TSG_PRECISION_F32_KAHAN (1u << 21)
+/* Use the global-memory sweep even when a span's node state fits in shared
+ * memory (for testing the general path). */
+#define TSG_FORCE_GLOBAL_SWEEP (1u << 22)
 
 /* tsg_treeseq_init options */
 #define TSG_TABLES_ON_DEVICE (1u << 0)

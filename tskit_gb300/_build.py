@@ -21,6 +21,7 @@ INCLUDE = os.path.join(REPO, "include")
 
 CUDA_SOURCES = [
     "tsg_treeseq.cu",
+    "tsg_plan.cu",
     "tsg_stats.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -20,6 +20,7 @@ STAT_PAIR_NORMALISE = 1 << 13
 STAT_NONCENTRED = 1 << 14
 STAT_BOTH_MODES = 1 << 20
 PRECISION_F32_KAHAN = 1 << 21
+FORCE_GLOBAL_SWEEP = 1 << 22
 TABLES_ON_DEVICE = 1 << 0
 
 (DIVERSITY, SEGREGATING_SITES, Y1, DIVERGENCE, Y2, F2, Y3, F3, F4, RELATEDNESS,

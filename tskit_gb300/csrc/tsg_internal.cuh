@@ -45,6 +45,7 @@ enum DeviceError : int32_t {
     DEV_UNSORTED_INDEX = 5,
     DEV_BAD_SITE = 6,
     DEV_BAD_MUTATION = 7,
+    DEV_ITEM_PLAN = 8,
 };
 
 __device__ __forceinline__ void dev_error(int32_t *flag, int32_t code)
@@ -103,8 +104,36 @@ struct TSView {
     const int32_t *mutation_node, *mutation_allele, *mutation_alt;
     const int32_t *span_tree;     // num_spans + 1
     const int64_t *span_alive_off;  // num_spans + 1
-    const int2 *span_alive;       // (parent, child) alive at each span start
+    const int2 *span_alive;       // (parent, child) alive at each span start, edge order
+    const int2 *span_alive_enc;   // same edges, span-local encoding
+    const int64_t *span_local_off;  // num_spans + 1: offsets into span_l2g
+    const int32_t *span_l2g;      // stateful nodes of each span (global ids)
+    const int2 *ins_enc;          // insertion order: (parent, child) span-local encoding
+    const int2 *rem_enc;          // removal order: (parent, child) span-local encoding
+    const int32_t *mut_enc;       // per mutation: span-local encoding of its node
+    int64_t max_local;            // largest number of stateful nodes in a span
+    const int64_t *tree_item_off; // num_trees + 1: replay items of each tree
+    int64_t num_items;
+    const int64_t *chunk_begin;   // evaluation chunks of items (within one tree)
+    const int64_t *chunk_end;
+    const int64_t *tree_chunk_off;  // num_trees + 1: first chunk of each tree
+    int64_t num_chunks;
 };
+
+// items per evaluation chunk (one warp)
+#define TSG_ITEM_CHUNK 256
+
+// Host copies of the topology the span plan is built from.
+struct HostTopology {
+    std::vector<double> left, right;           // edge order
+    std::vector<int32_t> parent, child;        // edge order
+    std::vector<int32_t> ins_parent, ins_child, rem_parent, rem_child;  // index orders
+    std::vector<int32_t> tree_in, tree_out, tree_sites;  // num_trees + 1
+    std::vector<int32_t> site_mut;             // num_sites + 1
+    std::vector<int32_t> mut_node;             // num_mutations
+};
+
+
 
 // Device-wide exclusive scan of int64 values (in may alias out).  `tmp` must
 // hold scan_tmp_elems(n) int64.
@@ -116,6 +145,11 @@ int device_count_sms();
 
 }  // namespace tsg
 
+struct tsg_treeseq;
+namespace tsg {
+int build_span_plan(tsg_treeseq *ts, const HostTopology &h, int64_t num_spans);
+}
+
 // Opaque handle definitions.
 struct tsg_treeseq {
     tsg::TSView v;
@@ -125,7 +159,10 @@ struct tsg_treeseq {
     std::vector<int32_t> h_span_tree;
     std::vector<uint32_t> h_node_flags;
     std::vector<int32_t> h_sample_index;
+    std::vector<int64_t> h_local_off;
+    std::vector<double> h_site_position;
     int64_t max_alive;
+    int64_t max_children = 0;  // most children of a node in any span's seek tree
     // device allocations owned by this object
     std::vector<void *> owned;
     // state of the synchronous (host-pointer) entry points

@@ -1,0 +1,311 @@
+// Span plan: the topology-only, per-tree-sequence part of the span seek.
+//
+// Built once on the host (multi-threaded C++) when a tree sequence is
+// loaded, deterministic, and uploaded to the device:
+//
+//   * span boundaries (tree indexes) with about equal edge-event work;
+//   * for every span start b, the edges with left <= b < right in edge-table
+//     order, i.e. by increasing parent time (the tree a seek must rebuild,
+//     tsk_tree_position_seek_forward, c/tskit/trees.c:5701-5763);
+//   * per span, a compact numbering of its "stateful" nodes: the nodes that
+//     are a parent in the span (in the seek tree or in an inserted edge).
+//     Only those carry per-node state (parent, counts, time) during the
+//     replay; every other node the span meets is a leaf throughout the span,
+//     whose counts are its own sample-set weights.  Node references in the
+//     span's edges, edge events and mutations are encoded as the local id
+//     (>= 0) of a stateful node or -(global id + 1) of a leaf.
+//
+// A span replays the transitions into its trees after the first and into
+// the first tree of the next span, so every transition belongs to exactly
+// one span and the event encodings can live in arrays parallel to the
+// insertion and removal orders.
+#include <algorithm>
+#include <thread>
+#include <vector>
+
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+static void plan_boundaries(const std::vector<int32_t> &tree_in,
+    const std::vector<int32_t> &tree_out, int64_t T, int64_t want, std::vector<int32_t> &span_tree)
+{
+    span_tree.clear();
+    span_tree.push_back(0);
+    want = std::max<int64_t>(1, std::min<int64_t>(want, T));
+    const double total = (double) tree_in[(size_t) T] + (double) tree_out[(size_t) T];
+    for (int64_t s = 1; s < want; s++) {
+        double target = total * (double) s / (double) want;
+        int64_t lo = 0, hi = T;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) / 2;
+            if ((double) tree_in[(size_t) mid] + (double) tree_out[(size_t) mid] < target) {
+                lo = mid + 1;
+            } else {
+                hi = mid;
+            }
+        }
+        if (lo > span_tree.back() && lo < T) {
+            span_tree.push_back((int32_t) lo);
+        }
+    }
+    span_tree.push_back((int32_t) T);
+}
+
+template <typename T>
+static int upload_vec(tsg_treeseq_t *ts, const std::vector<T> &h, T **out)
+{
+    void *d = nullptr;
+    size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    TSG_CUDA(cudaMalloc(&d, bytes));
+    ts->owned.push_back(d);
+    if (!h.empty()) {
+        TSG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    *out = (T *) d;
+    return 0;
+}
+
+int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
+{
+    int ret;
+    const int64_t E = (int64_t) h.left.size(), T = ts->v.num_trees, N = ts->v.num_nodes;
+    plan_boundaries(h.tree_in, h.tree_out, T, num_spans, ts->h_span_tree);
+    const int64_t NS = (int64_t) ts->h_span_tree.size() - 1;
+    const auto &st = ts->h_span_tree;
+    std::vector<double> span_pos((size_t) NS);
+    for (int64_t s = 0; s < NS; s++) {
+        span_pos[(size_t) s] = ts->h_breakpoints[(size_t) st[(size_t) s]];
+    }
+
+    // alive lists in edge order: count, offsets, fill
+    std::vector<int32_t> lo((size_t) E), hi((size_t) E);
+    std::vector<int64_t> cnt((size_t) NS + 1, 0);
+    for (int64_t e = 0; e < E; e++) {
+        int64_t a = std::lower_bound(span_pos.begin(), span_pos.end(), h.left[(size_t) e])
+            - span_pos.begin();
+        int64_t b = std::lower_bound(span_pos.begin(), span_pos.end(), h.right[(size_t) e])
+            - span_pos.begin();
+        lo[(size_t) e] = (int32_t) a;
+        hi[(size_t) e] = (int32_t) b;
+        for (int64_t s = a; s < b; s++) {
+            cnt[(size_t) s]++;
+        }
+    }
+    std::vector<int64_t> alive_off((size_t) NS + 1, 0);
+    int64_t max_alive = 0;
+    for (int64_t s = 0; s < NS; s++) {
+        alive_off[(size_t) s + 1] = alive_off[(size_t) s] + cnt[(size_t) s];
+        max_alive = std::max(max_alive, cnt[(size_t) s]);
+    }
+    std::vector<int32_t> alive_edge((size_t) alive_off[(size_t) NS]);
+    {
+        std::vector<int64_t> cur(alive_off.begin(), alive_off.end() - 1);
+        for (int64_t e = 0; e < E; e++) {
+            for (int32_t s = lo[(size_t) e]; s < hi[(size_t) e]; s++) {
+                alive_edge[(size_t) cur[(size_t) s]++] = (int32_t) e;
+            }
+        }
+    }
+
+    // per-span local numbering and encodings, spans in parallel
+    std::vector<int2> alive_global(alive_edge.size()), alive_enc(alive_edge.size());
+    std::vector<int2> ins_enc((size_t) E), rem_enc((size_t) E);
+    std::vector<int32_t> mut_enc(h.mut_node.size());
+    std::vector<std::vector<int32_t>> l2g((size_t) NS);
+    unsigned nthreads = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    nthreads = (unsigned) std::min<int64_t>(nthreads, NS);
+    std::vector<std::thread> pool;
+    for (unsigned tid = 0; tid < nthreads; tid++) {
+        pool.emplace_back([&, tid]() {
+            std::vector<int32_t> stamp((size_t) N, -1), map((size_t) N, 0);
+            for (int64_t s = tid; s < NS; s += nthreads) {
+                const int32_t t0 = st[(size_t) s], t1 = st[(size_t) s + 1];
+                const int32_t tend = t1 < T ? t1 + 1 : t1;
+                auto &list = l2g[(size_t) s];
+                auto assign = [&](int32_t u) {
+                    if (stamp[(size_t) u] != (int32_t) s) {
+                        stamp[(size_t) u] = (int32_t) s;
+                        map[(size_t) u] = (int32_t) list.size();
+                        list.push_back(u);
+                    }
+                };
+                auto enc = [&](int32_t u) {
+                    return stamp[(size_t) u] == (int32_t) s ? map[(size_t) u] : -(u + 1);
+                };
+                const int64_t a0 = alive_off[(size_t) s], a1 = alive_off[(size_t) s + 1];
+                for (int64_t i = a0; i < a1; i++) {
+                    assign(h.parent[(size_t) alive_edge[(size_t) i]]);
+                }
+                const int32_t i0 = h.tree_in[(size_t) t0 + (t0 < t1 ? 1 : 0)];
+                const int32_t i1 = h.tree_in[(size_t) tend];
+                for (int32_t i = i0; i < i1; i++) {
+                    assign(h.ins_parent[(size_t) i]);
+                }
+                for (int64_t i = a0; i < a1; i++) {
+                    int32_t e = alive_edge[(size_t) i];
+                    alive_global[(size_t) i] = make_int2(h.parent[(size_t) e], h.child[(size_t) e]);
+                    alive_enc[(size_t) i] = make_int2(enc(h.parent[(size_t) e]), enc(h.child[(size_t) e]));
+                }
+                for (int32_t i = i0; i < i1; i++) {
+                    ins_enc[(size_t) i] = make_int2(enc(h.ins_parent[(size_t) i]),
+                        enc(h.ins_child[(size_t) i]));
+                }
+                const int32_t r0 = h.tree_out[(size_t) t0 + (t0 < t1 ? 1 : 0)];
+                const int32_t r1 = h.tree_out[(size_t) tend];
+                for (int32_t i = r0; i < r1; i++) {
+                    rem_enc[(size_t) i] = make_int2(enc(h.rem_parent[(size_t) i]),
+                        enc(h.rem_child[(size_t) i]));
+                }
+                const int32_t m0 = h.site_mut[(size_t) h.tree_sites[(size_t) t0]];
+                const int32_t m1 = h.site_mut[(size_t) h.tree_sites[(size_t) t1]];
+                for (int32_t m = m0; m < m1; m++) {
+                    mut_enc[(size_t) m] = enc(h.mut_node[(size_t) m]);
+                }
+            }
+        });
+    }
+    for (auto &th : pool) {
+        th.join();
+    }
+    // Item plan of the shared-memory sweep: per tree, the number of items the
+    // replay emits -- one per node alive at the span start (first tree of the
+    // span) and, for each edge event entering a later tree of the span, one
+    // for the edge's child plus one per node on the parent's root path.  The
+    // path lengths are topology-only, so the replay is simulated here.
+    std::vector<int64_t> tree_items((size_t) T + 1, 0);
+    std::vector<int64_t> span_max_children((size_t) NS, 0);
+    {
+        std::vector<std::thread> pool2;
+        for (unsigned tid = 0; tid < nthreads; tid++) {
+            pool2.emplace_back([&, tid]() {
+                std::vector<int32_t> par, nch;
+                for (int64_t s = tid; s < NS; s += nthreads) {
+                    const int32_t t0 = st[(size_t) s], t1 = st[(size_t) s + 1];
+                    par.assign(l2g[(size_t) s].size(), -1);
+                    nch.assign(l2g[(size_t) s].size(), 0);
+                    const int64_t a0 = alive_off[(size_t) s], a1 = alive_off[(size_t) s + 1];
+                    for (int64_t i = a0; i < a1; i++) {
+                        const int2 pc = alive_enc[(size_t) i];
+                        if (pc.y >= 0) {
+                            par[(size_t) pc.y] = pc.x;
+                        }
+                        span_max_children[(size_t) s] = std::max<int64_t>(
+                            span_max_children[(size_t) s], ++nch[(size_t) pc.x]);
+                    }
+                    tree_items[(size_t) t0] = a1 - a0;
+                    auto depth = [&](int32_t v) {
+                        int64_t d = 0;
+                        while (v >= 0 && d <= (int64_t) par.size()) {
+                            d++;
+                            v = par[(size_t) v];
+                        }
+                        return d;
+                    };
+                    for (int32_t t = t0 + 1; t < t1; t++) {
+                        int64_t cnt = 0;
+                        for (int32_t i = h.tree_out[(size_t) t]; i < h.tree_out[(size_t) t + 1]; i++) {
+                            const int2 pc = rem_enc[(size_t) i];
+                            if (pc.y >= 0) {
+                                par[(size_t) pc.y] = -1;
+                            }
+                            cnt += 1 + depth(pc.x);
+                        }
+                        for (int32_t i = h.tree_in[(size_t) t]; i < h.tree_in[(size_t) t + 1]; i++) {
+                            const int2 pc = ins_enc[(size_t) i];
+                            if (pc.y >= 0) {
+                                par[(size_t) pc.y] = pc.x;
+                            }
+                            cnt += 1 + depth(pc.x);
+                        }
+                        tree_items[(size_t) t] = cnt;
+                    }
+                }
+            });
+        }
+        for (auto &th : pool2) {
+            th.join();
+        }
+    }
+    std::vector<int64_t> tree_item_off((size_t) T + 1, 0);
+    for (int64_t t = 0; t < T; t++) {
+        tree_item_off[(size_t) t + 1] = tree_item_off[(size_t) t] + tree_items[(size_t) t];
+    }
+    // evaluation chunks: at most TSG_ITEM_CHUNK items, never across trees,
+    // at least one per tree
+    std::vector<int64_t> chunk_begin, tree_chunk_off((size_t) T + 1, 0);
+    for (int64_t t = 0; t < T; t++) {
+        tree_chunk_off[(size_t) t] = (int64_t) chunk_begin.size();
+        const int64_t b = tree_item_off[(size_t) t], e = tree_item_off[(size_t) t + 1];
+        int64_t c = b;
+        do {
+            chunk_begin.push_back(c);
+            c += TSG_ITEM_CHUNK;
+        } while (c < e);
+    }
+    tree_chunk_off[(size_t) T] = (int64_t) chunk_begin.size();
+    chunk_begin.push_back(tree_item_off[(size_t) T]);
+    // chunk ends: the next chunk's begin, clipped to the chunk's tree
+    std::vector<int64_t> chunk_end(chunk_begin.size() - 1);
+    for (int64_t t = 0; t < T; t++) {
+        for (int64_t c = tree_chunk_off[(size_t) t]; c < tree_chunk_off[(size_t) t + 1]; c++) {
+            chunk_end[(size_t) c] = std::min(chunk_begin[(size_t) c] + TSG_ITEM_CHUNK,
+                tree_item_off[(size_t) t + 1]);
+        }
+    }
+
+    std::vector<int64_t> local_off((size_t) NS + 1, 0);
+    int64_t max_local = 0;
+    for (int64_t s = 0; s < NS; s++) {
+        local_off[(size_t) s + 1] = local_off[(size_t) s] + (int64_t) l2g[(size_t) s].size();
+        max_local = std::max<int64_t>(max_local, (int64_t) l2g[(size_t) s].size());
+    }
+    std::vector<int32_t> l2g_flat((size_t) local_off[(size_t) NS]);
+    for (int64_t s = 0; s < NS; s++) {
+        std::copy(l2g[(size_t) s].begin(), l2g[(size_t) s].end(),
+            l2g_flat.begin() + local_off[(size_t) s]);
+    }
+
+    int32_t *d_span_tree, *d_l2g, *d_mut_enc;
+    int64_t *d_alive_off, *d_local_off, *d_tree_item_off, *d_chunk_begin, *d_chunk_end,
+        *d_tree_chunk_off;
+    int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
+    std::vector<int32_t> span_tree_v(st.begin(), st.end());
+    if ((ret = upload_vec(ts, span_tree_v, &d_span_tree)) || (ret = upload_vec(ts, alive_off, &d_alive_off))
+        || (ret = upload_vec(ts, alive_global, &d_alive)) || (ret = upload_vec(ts, alive_enc, &d_alive_enc))
+        || (ret = upload_vec(ts, local_off, &d_local_off)) || (ret = upload_vec(ts, l2g_flat, &d_l2g))
+        || (ret = upload_vec(ts, ins_enc, &d_ins_enc)) || (ret = upload_vec(ts, rem_enc, &d_rem_enc))
+        || (ret = upload_vec(ts, mut_enc, &d_mut_enc))
+        || (ret = upload_vec(ts, tree_item_off, &d_tree_item_off))
+        || (ret = upload_vec(ts, chunk_begin, &d_chunk_begin))
+        || (ret = upload_vec(ts, chunk_end, &d_chunk_end))
+        || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))) {
+        return ret;
+    }
+    ts->v.num_spans = NS;
+    ts->v.span_tree = d_span_tree;
+    ts->v.span_alive_off = d_alive_off;
+    ts->v.span_alive = d_alive;
+    ts->v.span_alive_enc = d_alive_enc;
+    ts->v.span_local_off = d_local_off;
+    ts->v.span_l2g = d_l2g;
+    ts->v.ins_enc = d_ins_enc;
+    ts->v.rem_enc = d_rem_enc;
+    ts->v.mut_enc = d_mut_enc;
+    ts->v.max_local = max_local;
+    ts->v.tree_item_off = d_tree_item_off;
+    ts->max_children = 0;
+    for (int64_t s = 0; s < NS; s++) {
+        ts->max_children = std::max(ts->max_children, span_max_children[(size_t) s]);
+    }
+    ts->v.chunk_begin = d_chunk_begin;
+    ts->v.chunk_end = d_chunk_end;
+    ts->v.tree_chunk_off = d_tree_chunk_off;
+    ts->v.num_chunks = (int64_t) chunk_end.size();
+    ts->v.num_items = tree_item_off[(size_t) T];
+    ts->max_alive = max_alive;
+    ts->h_local_off = local_off;
+    return 0;
+}
+
+}  // namespace tsg

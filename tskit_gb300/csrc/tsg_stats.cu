@@ -43,12 +43,17 @@ struct QueryParams {
     int32_t K, KP, R, Wn;
     int32_t branch, site, polarised, f32, need_mean;
     int32_t num_slots;
+    double inv_K;
     double set_size[TSG_MAX_SAMPLE_SETS];
+    double inv_size[TSG_MAX_SAMPLE_SETS];  // 1 / n_k
+    double inv[TSG_MAX_OUTPUTS];           // reciprocal denominator of each term
     Term term[TSG_MAX_OUTPUTS];
 };
 
 struct QueryDev {
     const uint32_t *sample_mask;  // per sample index: bit k = member of set k
+    const uint32_t *node_mask;    // per node: its sample-set membership bits (workspace)
+    const int32_t *win_site_lo;   // per window: first site (num_windows + 1 entries)
     const double *windows;        // Wn + 1
     const int32_t *span_wlo;      // per span: first window overlapping it
     const int64_t *span_woff;     // per span: offset into span-window arrays
@@ -67,6 +72,12 @@ struct WsDev {
     double *D;        // spans * R
     double *RS;       // spans * R
     double *rs0;      // R
+    void *items;      // replay items (shared-memory sweep)
+    uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)
+    double *dD;       // chunks * R: running-sum change of each item chunk
+    uint32_t *node_mask;  // per node sample-set bits
+    double *site_val;     // sites * R: per-site summary (shared-memory sweep)
+    double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
     int32_t *err;
     int32_t *counter;
 };
@@ -158,7 +169,7 @@ __device__ __forceinline__ F eval_branch(const QueryParams &q, int xk_int, int p
 
 template <typename F>
 struct Acc {
-    F s, c;
+    F s, c;  // c: Kahan compensation (FP32 only; the FP64 specialisation has none)
     __device__ __forceinline__ void zero()
     {
         s = 0;
@@ -176,6 +187,14 @@ struct Acc {
         }
     }
     __device__ __forceinline__ double value() const { return (double) s - (double) c; }
+};
+
+template <>
+struct Acc<double> {
+    double s;
+    __device__ __forceinline__ void zero() { s = 0; }
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double value() const { return s; }
 };
 
 __device__ __forceinline__ int32_t node_weight(const TSView &ts, const QueryDev &qd, int32_t u,
@@ -477,6 +496,29 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
     }
 }
 
+#include "tsg_terms.cuh"
+#include "tsg_items.cuh"
+
+// term budget of the item evaluation (accumulators per lane)
+#define TSG_ITEM_RMAX 32
+
+static void *replay_kernel(int KQ)
+{
+    return KQ == 1 ? (void *) k_replay_items<1> : (void *) k_replay_items<2>;
+}
+
+static int64_t smem_budget()
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    // static shared memory of k_replay_items (span id)
+    return (int64_t) optin - 64;
+}
+
 // RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r], one block per r, fixed order.
 __global__ void k_span_scan(const double *D, const double *rs0, double *RS, int64_t NS, int R)
 {
@@ -508,7 +550,7 @@ __global__ void k_span_scan(const double *D, const double *rs0, double *RS, int6
 }
 
 __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_normalise,
-    double *result)
+    int items_mode, double *result)
 {
     const int R = q.R;
     const int64_t total = (int64_t) q.Wn * R;
@@ -520,11 +562,15 @@ __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_no
         for (int32_t s = s0; s <= s1; s++) {
             int64_t li = qd.span_woff[s] + (wdx - qd.span_wlo[s]);
             if (q.branch) {
-                vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
+                vb += items_mode ? w.B[li * R + r]
+                                 : w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
             }
-            if (q.site) {
+            if (q.site && !items_mode) {
                 vs += w.SITE[li * R + r];
             }
+        }
+        if (q.site && items_mode) {
+            vs = w.site_win[(int64_t) wdx * R + r];
         }
         double span = qd.windows[wdx + 1] - qd.windows[wdx];
         if (span_normalise) {
@@ -560,11 +606,14 @@ struct tsg_query {
     QueryDev d;
     void *dbuf;              // device copy of per-query arrays (owned), or null
     std::vector<char> blob;  // host image of the per-query arrays
-    int64_t off[6];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh
+    int64_t off[7];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite
     cudaEvent_t ev_start, ev_stop;  // optional events around the sweep kernel
     int64_t total_span_windows;
     int64_t num_slots;
     int64_t ws_bytes;
+    bool smem;
+    int KQ;
+    int64_t smem_bytes, smem_grid;
     int span_normalise;
     uint32_t options;
 };
@@ -679,6 +728,8 @@ static void query_bind(tsg_query_t *q, void *dev)
     q->d.span_woff = (const int64_t *) (b + q->off[3]);
     q->d.win_span_lo = (const int32_t *) (b + q->off[4]);
     q->d.win_span_hi = (const int32_t *) (b + q->off[5]);
+    q->d.win_site_lo = (const int32_t *) (b + q->off[6]);
+    q->d.node_mask = nullptr;
 }
 
 // Validate the query and build its host image; the device copy is made by
@@ -759,7 +810,52 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         if (outputs[r].type == TSG_RELATEDNESS) {
             p.need_mean = 1;
         }
+        // reciprocal denominators of the terms (the summary functions of
+        // c/tskit/trees.c divide by these products of set sizes)
+        const int32_t *ix = p.term[r].idx;
+        const double ni = (double) sizes[ix[0]], nj = (double) sizes[ix[1]];
+        const double nk = (double) sizes[ix[2]], nl = (double) sizes[ix[3]];
+        double den = 1;
+        switch (outputs[r].type) {
+            case TSG_DIVERSITY:
+                den = ni * (ni - 1);
+                break;
+            case TSG_SEGREGATING_SITES:
+                den = ni;
+                break;
+            case TSG_Y1:
+                den = ni * (ni - 1) * (ni - 2);
+                break;
+            case TSG_DIVERGENCE:
+                den = ni * (nj - (ix[0] == ix[1] ? 1 : 0));
+                break;
+            case TSG_Y2:
+                den = ni * nj * (nj - 1);
+                break;
+            case TSG_F2:
+                den = ni * (ni - 1) * nj * (nj - 1);
+                break;
+            case TSG_Y3:
+                den = ni * nj * nk;
+                break;
+            case TSG_F3:
+                den = ni * (ni - 1) * nj * nk;
+                break;
+            case TSG_F4:
+                den = ni * nj * nk * nl;
+                break;
+            case TSG_RELATEDNESS_NONCENTRED:
+                den = ni * nj;
+                break;
+            default:
+                den = 1;
+        }
+        p.inv[r] = 1.0 / den;
     }
+    for (uint64_t k = 0; k < K; k++) {
+        p.inv_size[k] = 1.0 / (double) sizes[k];
+    }
+    p.inv_K = 1.0 / (double) K;
 
     // span <-> window overlap tables (host; spans and windows are few)
     const int64_t NS = ts->v.num_spans;
@@ -803,7 +899,16 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     int64_t off_woff = align_up(off_wlo + NS * 4, 256);
     int64_t off_wsl = align_up(off_woff + (NS + 1) * 8, 256);
     int64_t off_wsh = align_up(off_wsl + (int64_t) Wn * 4, 256);
-    int64_t total = align_up(off_wsh + (int64_t) Wn * 4, 256);
+    int64_t off_wsite = align_up(off_wsh + (int64_t) Wn * 4, 256);
+    int64_t total = align_up(off_wsite + ((int64_t) Wn + 1) * 4, 256);
+    std::vector<int32_t> wsite((size_t) Wn + 1);
+    {
+        const auto &sp = ts->h_site_position;
+        for (uint64_t wdx = 0; wdx <= Wn; wdx++) {
+            wsite[(size_t) wdx] = (int32_t) (std::lower_bound(sp.begin(), sp.end(), windows[wdx])
+                - sp.begin());
+        }
+    }
     q->blob.assign((size_t) total, 0);
     char *h = q->blob.data();
     std::memcpy(h + off_mask, mask.data(), (size_t) n * 4);
@@ -812,6 +917,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     std::memcpy(h + off_woff, woff.data(), ((size_t) NS + 1) * 8);
     std::memcpy(h + off_wsl, wsl.data(), (size_t) Wn * 4);
     std::memcpy(h + off_wsh, wsh.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_wsite, wsite.data(), ((size_t) Wn + 1) * 4);
+    q->off[6] = off_wsite;
     q->off[0] = off_mask;
     q->off[1] = off_win;
     q->off[2] = off_wlo;
@@ -833,6 +940,30 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     slots = std::min<int64_t>(slots, std::max<int64_t>(NS, 1));
     q->num_slots = slots;
     p.num_slots = (int32_t) slots;
+
+    // shared-memory sweep when the span state fits: u16 counts and ids,
+    // f64 times, at most 8 sets and 32 terms
+    uint64_t max_size = 0;
+    for (uint64_t k = 0; k < K; k++) {
+        max_size = std::max<uint64_t>(max_size, sizes[k]);
+    }
+    const int64_t L = std::max<int64_t>(ts->v.max_local, 1);
+    const int64_t KQ = ((int64_t) K + 3) / 4;
+    q->smem_bytes = align_up(L * 8 + L * 8 * KQ + L * 4 + L * 2, 16);
+    q->smem = !(options & TSG_FORCE_GLOBAL_SWEEP) && K <= 8 && (int64_t) R <= TSG_ITEM_RMAX
+        && max_size <= 65535 && ts->v.max_local <= 65534 && ts->max_children < 65535
+        && q->smem_bytes <= smem_budget();
+    q->KQ = (int) KQ;
+    if (q->smem) {
+        int per_sm = 0;
+        void *fn = replay_kernel((int) KQ);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
+        q->smem_grid = std::min<int64_t>((int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()),
+            std::max<int64_t>(NS, 1));
+        slots = 0;  // no per-slot node arrays
+        q->num_slots = 0;
+    }
     const int64_t TSW = q->total_span_windows;
     int64_t bytes = 0;
     bytes += align_up(slots * ts->v.num_nodes * 4, 256) * 3;          // parent, nchild, arrive
@@ -841,6 +972,15 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     bytes += align_up(TSW * R * 8, 256) * 2;                          // B, SITE
     bytes += align_up(NS * R * 8, 256) * 2;                           // D, RS
     bytes += align_up((int64_t) R * 8, 256);                          // rs0
+    if (q->smem) {
+        const int64_t item_bytes = KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
+        bytes += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);  // items
+        bytes += align_up(ts->v.num_mutations * 8 * KQ, 256);                   // mcnt
+        bytes += align_up(ts->v.num_chunks * R * 8, 256);                        // dD (per chunk)
+        bytes += align_up(ts->v.num_nodes * 4, 256);                             // node_mask
+        bytes += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);          // site_val
+        bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
+    }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
     *out = q;
@@ -953,6 +1093,27 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     off += align_up(NS * R * 8, 256);
     w.rs0 = (double *) (b + off);
     off += align_up(R * 8, 256);
+    w.items = nullptr;
+    w.mcnt = nullptr;
+    w.dD = nullptr;
+    w.node_mask = nullptr;
+    w.site_val = nullptr;
+    w.site_win = nullptr;
+    if (q->smem) {
+        const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
+        w.items = b + off;
+        off += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);
+        w.mcnt = (uint64_t *) (b + off);
+        off += align_up(ts->v.num_mutations * 8 * q->KQ, 256);
+        w.dD = (double *) (b + off);
+        off += align_up(ts->v.num_chunks * R * 8, 256);
+        w.node_mask = (uint32_t *) (b + off);
+        off += align_up(ts->v.num_nodes * 4, 256);
+        w.site_val = (double *) (b + off);
+        off += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);
+        w.site_win = (double *) (b + off);
+        off += align_up((int64_t) p.Wn * R * 8, 256);
+    }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
 
@@ -961,7 +1122,55 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->ev_start != nullptr) {
         TSG_CUDA(cudaEventRecord(q->ev_start, st));
     }
-    if (p.f32) {
+    const bool anchored = q->smem;
+    QueryDev d = q->d;
+    d.node_mask = w.node_mask;
+    if (q->smem) {
+        k_node_mask<<<grid_for(N), 256, 0, st>>>(ts->v, d, w.node_mask);
+        TSG_LAUNCHED();
+        const unsigned g = (unsigned) q->smem_grid;
+        const size_t sb = (size_t) q->smem_bytes;
+        if (q->KQ == 1) {
+            k_replay_items<1><<<g, 512, sb, st>>>(ts->v, p, d, w);
+        } else {
+            k_replay_items<2><<<g, 512, sb, st>>>(ts->v, p, d, w);
+        }
+        TSG_LAUNCHED();
+        if (p.branch) {
+            const unsigned ge = (unsigned) ((ts->v.num_chunks + 7) / 8);
+            const int sel = (p.f32 ? 4 : 0) + (p.polarised ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+            switch (sel) {
+                case 0: k_eval_items<double, false, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 1: k_eval_items<double, false, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 2: k_eval_items<double, true, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 3: k_eval_items<double, true, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 4: k_eval_items<float, false, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 5: k_eval_items<float, false, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                case 6: k_eval_items<float, true, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+                default: k_eval_items<float, true, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+            }
+            TSG_LAUNCHED();
+            k_span_windows<<<(unsigned) ((ts->v.num_spans + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
+            TSG_LAUNCHED();
+        }
+        if (p.site && ts->v.num_sites > 0) {
+            const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
+            if (q->KQ == 1) {
+                k_site_eval<TSG_ITEM_RMAX, 1><<<gsite, 256, 0, st>>>(ts->v, p, w);
+            } else {
+                k_site_eval<TSG_ITEM_RMAX, 2><<<gsite, 256, 0, st>>>(ts->v, p, w);
+            }
+            TSG_LAUNCHED();
+        }
+        if (p.site) {
+            if (ts->v.num_sites > 0) {
+                k_site_windows<<<(unsigned) ((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w);
+                TSG_LAUNCHED();
+            } else {
+                TSG_CUDA(cudaMemsetAsync(w.site_win, 0, (size_t) p.Wn * R * 8, st));
+            }
+        }
+    } else if (p.f32) {
         k_sweep<float><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
     } else {
         k_sweep<double><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
@@ -970,12 +1179,12 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->ev_stop != nullptr) {
         TSG_CUDA(cudaEventRecord(q->ev_stop, st));
     }
-    if (p.branch) {
+    if (p.branch && !anchored) {
         k_span_scan<<<(unsigned) R, 1024, 0, st>>>(w.D, w.rs0, w.RS, NS, (int) R);
         TSG_LAUNCHED();
     }
-    k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, q->d, w, q->span_normalise,
-        result);
+    k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w, q->span_normalise,
+        anchored ? 1 : 0, result);
     TSG_LAUNCHED();
     return 0;
 }

@@ -1,0 +1,158 @@
+// Summary terms on packed counts, and the shared-memory span state
+// (included by tsg_stats.cu after its definitions).
+//
+// A span's stateful nodes live in shared memory: time (f64), per-set sample
+// counts (16-bit fields packed into 64-bit words) and parent (16-bit local
+// id).  Leaves are never stored: their counts are their own sample-set
+// memberships.  Summary terms use precomputed reciprocal denominators (no
+// divisions) and read counts with register shifts (no indexed arrays).
+
+#define TSG_NO_PARENT 0xFFFFu
+#define TSG_SMEM_KMAX 8
+
+// Per-node sample-set counts packed as 16-bit fields: sets 0-3 in lo, 4-7 in
+// hi.  Counts stay in [0, set size] through every update, so packed adds and
+// subtracts never carry between fields.
+struct Pack {
+    uint64_t lo, hi;
+};
+
+__device__ __forceinline__ uint32_t pk_get(const Pack &p, int k)
+{
+    const uint64_t w = k < 4 ? p.lo : p.hi;
+    return (uint32_t) ((w >> (16 * (k & 3))) & 0xFFFFull);
+}
+
+__device__ __forceinline__ Pack pk_from_mask(uint32_t m, int K)
+{
+    Pack p{0, 0};
+#pragma unroll
+    for (int k = 0; k < TSG_SMEM_KMAX; k++) {
+        if (k < K && ((m >> k) & 1u)) {
+            if (k < 4) {
+                p.lo |= 1ull << (16 * k);
+            } else {
+                p.hi |= 1ull << (16 * (k - 4));
+            }
+        }
+    }
+    return p;
+}
+
+template <typename F>
+__device__ __forceinline__ F term_inv(int type, F xi, F xj, F xk, F xl, F ni, F nj, F nk, F nl,
+    F inv, F ri, F rj, F meanx)
+{
+    switch (type) {
+        case TSG_DIVERSITY:
+            return xi * (ni - xi) * inv;
+        case TSG_SEGREGATING_SITES:
+            return (F) (xi > 0) * (1 - xi * inv);
+        case TSG_Y1:
+            return xi * (ni - xi) * (ni - xi - 1) * inv;
+        case TSG_DIVERGENCE:
+            return xi * (nj - xj) * inv;
+        case TSG_Y2:
+            return xi * (nj - xj) * (nj - xj - 1) * inv;
+        case TSG_F2:
+            return (xi * (xi - 1) * (nj - xj) * (nj - xj - 1) - xi * (ni - xi) * (nj - xj) * xj)
+                * inv;
+        case TSG_Y3:
+            return xi * (nj - xj) * (nk - xk) * inv;
+        case TSG_F3:
+            return (xi * (xi - 1) * (nj - xj) * (nk - xk) - xi * (ni - xi) * (nj - xj) * xk) * inv;
+        case TSG_F4:
+            return (xi * xk * (nj - xj) * (nl - xl) - xi * xl * (nj - xj) * (nk - xk)) * inv;
+        case TSG_RELATEDNESS:
+            return (xi * ri - meanx) * (xj * rj - meanx);
+        case TSG_RELATEDNESS_NONCENTRED:
+            return xi * xj * inv;
+        default:
+            return (F) NAN;
+    }
+}
+
+// Means over the sets of x_k / n_k and of (n_k - x_k) / n_k (centred
+// relatedness only).
+template <typename F>
+__device__ __forceinline__ void pk_means(const QueryParams &q, const Pack &P, F &mx, F &mc)
+{
+    mx = 0;
+    mc = 0;
+    if (q.need_mean) {
+#pragma unroll
+        for (int k = 0; k < TSG_SMEM_KMAX; k++) {
+            if (k < q.K) {
+                const F x = (F) pk_get(P, k), n = (F) q.set_size[k], r = (F) q.inv_size[k];
+                mx += x * r;
+                mc += (n - x) * r;
+            }
+        }
+        mx *= (F) q.inv_K;
+        mc *= (F) q.inv_K;
+    }
+}
+
+// F_r(x): f_r(x), plus f_r(n - x) when unpolarised (c/tskit/trees.c:1944-1972).
+template <typename F, bool UNPOL>
+__device__ __forceinline__ F term_F(const QueryParams &q, int r, const Pack &P, F mx, F mc)
+{
+    const Term &t = q.term[r];
+    const F ni = (F) q.set_size[t.idx[0]], nj = (F) q.set_size[t.idx[1]];
+    const F nk = (F) q.set_size[t.idx[2]], nl = (F) q.set_size[t.idx[3]];
+    const F ri = (F) q.inv_size[t.idx[0]], rj = (F) q.inv_size[t.idx[1]];
+    const F xi = (F) pk_get(P, t.idx[0]), xj = (F) pk_get(P, t.idx[1]);
+    const F xk = (F) pk_get(P, t.idx[2]), xl = (F) pk_get(P, t.idx[3]);
+    const F inv = (F) q.inv[r];
+    F v = term_inv<F>(t.type, xi, xj, xk, xl, ni, nj, nk, nl, inv, ri, rj, mx);
+    if (UNPOL) {
+        v += term_inv<F>(t.type, ni - xi, nj - xj, nk - xk, nl - xl, ni, nj, nk, nl, inv, ri, rj, mc);
+    }
+    return v;
+}
+
+struct SmemSpan {
+    double *time;
+    uint64_t *xq;   // KQ words per node
+    uint32_t *cnt;  // seek counters: children (low 16 bits), arrivals (high 16 bits)
+    uint16_t *par;
+    int KQ;
+};
+
+__device__ __forceinline__ Pack pk_load(const SmemSpan &sp, int32_t l)
+{
+    Pack p;
+    p.lo = sp.xq[l * sp.KQ];
+    p.hi = sp.KQ > 1 ? sp.xq[l * sp.KQ + 1] : 0ull;
+    return p;
+}
+
+__device__ __forceinline__ void pk_store(const SmemSpan &sp, int32_t l, const Pack &p)
+{
+    sp.xq[l * sp.KQ] = p.lo;
+    if (sp.KQ > 1) {
+        sp.xq[l * sp.KQ + 1] = p.hi;
+    }
+}
+
+__device__ __forceinline__ uint32_t leaf_mask(const TSView &ts, const QueryDev &qd, int32_t g)
+{
+    (void) ts;
+    return qd.node_mask[g];
+}
+
+// counts of an encoded node (local stateful id >= 0, or -(global + 1))
+__device__ __forceinline__ Pack load_counts(const SmemSpan &sp, const TSView &ts,
+    const QueryDev &qd, int32_t enc, int K)
+{
+    if (enc >= 0) {
+        return pk_load(sp, enc);
+    }
+    return pk_from_mask(leaf_mask(ts, qd, -enc - 1), K);
+}
+
+__device__ __forceinline__ double node_time_enc(const SmemSpan &sp, const TSView &ts, int32_t enc)
+{
+    return enc >= 0 ? sp.time[enc] : ts.node_time[-enc - 1];
+}
+

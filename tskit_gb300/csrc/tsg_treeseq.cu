@@ -315,36 +315,6 @@ __global__ void k_sample_index(const uint32_t *flags, const int64_t *pos, int64_
     }
 }
 
-// For each edge, the spans whose start position lies in [left, right).
-__global__ void k_span_edge_range(const double *left, const double *right, int64_t E,
-    const double *span_pos, int64_t num_spans, int32_t *lo, int32_t *hi, int64_t *count_diff)
-{
-    for (int64_t e = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; e < E;
-         e += (int64_t) gridDim.x * blockDim.x) {
-        int64_t a = lower_bound(span_pos, num_spans, left[e]);
-        int64_t b = lower_bound(span_pos, num_spans, right[e]);
-        lo[e] = (int32_t) a;
-        hi[e] = (int32_t) b;
-        if (a < b) {
-            atomicAdd((unsigned long long *) &count_diff[a], 1ull);
-            atomicAdd((unsigned long long *) &count_diff[b], (unsigned long long) -1ll);
-        }
-    }
-}
-
-__global__ void k_span_fill(const int32_t *parent, const int32_t *child, int64_t E,
-    const int32_t *lo, const int32_t *hi, const int64_t *offsets, int32_t *cursor, int2 *alive)
-{
-    for (int64_t e = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; e < E;
-         e += (int64_t) gridDim.x * blockDim.x) {
-        int2 pc = make_int2(parent[e], child[e]);
-        for (int32_t s = lo[e]; s < hi[e]; s++) {
-            int32_t k = atomicAdd(&cursor[s], 1);
-            alive[offsets[s] + k] = pc;
-        }
-    }
-}
-
 static int grid_for(int64_t n, int block = 256)
 {
     int64_t g = (n + block - 1) / block;
@@ -399,38 +369,6 @@ static int map_device_error(int32_t code)
         default:
             return TSG_ERR_BAD_TREE_SEQUENCE;
     }
-}
-
-// Choose span boundaries (tree indexes) splitting edge events evenly.
-static void plan_spans(const std::vector<int32_t> &tree_in, const std::vector<int32_t> &tree_out,
-    int64_t T, int64_t want, std::vector<int32_t> &span_tree)
-{
-    span_tree.clear();
-    span_tree.push_back(0);
-    if (want < 1) {
-        want = 1;
-    }
-    if (want > T) {
-        want = T;
-    }
-    const double total = (double) tree_in[T] + (double) tree_out[T];
-    for (int64_t s = 1; s < want; s++) {
-        double target = total * (double) s / (double) want;
-        // first tree whose cumulative work reaches the target
-        int64_t lo = 0, hi = T;
-        while (lo < hi) {
-            int64_t mid = (lo + hi) / 2;
-            if ((double) tree_in[mid] + (double) tree_out[mid] < target) {
-                lo = mid + 1;
-            } else {
-                hi = mid;
-            }
-        }
-        if (lo > span_tree.back() && lo < T) {
-            span_tree.push_back((int32_t) lo);
-        }
-    }
-    span_tree.push_back((int32_t) T);
 }
 
 }  // namespace tsg
@@ -736,96 +674,38 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         ts->v.mutation_allele = t.mut_allele;
         ts->v.mutation_alt = t.mut_alt;
 
-        // ---- span plan
-        std::vector<int32_t> h_in((size_t) T + 1), h_out((size_t) T + 1);
-        TSG_CUDA(cudaMemcpy(h_in.data(), tree_in, (size_t) (T + 1) * sizeof(int32_t),
-            cudaMemcpyDeviceToHost));
-        TSG_CUDA(cudaMemcpy(h_out.data(), tree_out, (size_t) (T + 1) * sizeof(int32_t),
-            cudaMemcpyDeviceToHost));
+        // ---- span plan (host, deterministic)
+        HostTopology h;
+        auto d2h = [&](auto &vec, const auto *src, int64_t count) -> int {
+            vec.resize((size_t) count);
+            if (count > 0) {
+                TSG_CUDA(cudaMemcpy(vec.data(), src, (size_t) count * sizeof(vec[0]),
+                    cudaMemcpyDeviceToHost));
+            }
+            return 0;
+        };
+        if ((ret = d2h(h.left, t.left, E)) || (ret = d2h(h.right, t.right, E))
+            || (ret = d2h(h.parent, t.parent, E)) || (ret = d2h(h.child, t.child, E))
+            || (ret = d2h(h.ins_parent, ins_parent, E)) || (ret = d2h(h.ins_child, ins_child, E))
+            || (ret = d2h(h.rem_parent, rem_parent, E)) || (ret = d2h(h.rem_child, rem_child, E))
+            || (ret = d2h(h.tree_in, tree_in, T + 1)) || (ret = d2h(h.tree_out, tree_out, T + 1))
+            || (ret = d2h(h.tree_sites, tree_sites, T + 1))
+            || (ret = d2h(h.site_mut, site_mut, S + 1)) || (ret = d2h(h.mut_node, t.mut_node, M))) {
+            goto fail;
+        }
         if (num_spans <= 0) {
-            // default: about 24 edge events per span, at most 16 spans per SM
-            // slot budget, never fewer than one per tree boundary group
-            int sms = device_count_sms();
-            int64_t cap = (int64_t) std::max(sms, 1) * 64;
-            num_spans = std::min<int64_t>(cap, std::max<int64_t>(1, 2 * E / 24));
+            // default: about two spans per SM plus one per 2,000 edge events;
+            // a span's seek touches about two nodes per sample, its replay about
+            // a dozen per event, and its node state must fit in shared memory
+            const int64_t sms = std::max(device_count_sms(), 1);
+            num_spans = std::min<int64_t>(T, std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms));
         }
-        plan_spans(h_in, h_out, T, num_spans, ts->h_span_tree);
-        const int64_t NS = (int64_t) ts->h_span_tree.size() - 1;
-        std::vector<double> h_span_pos((size_t) NS);
-        for (int64_t s = 0; s < NS; s++) {
-            h_span_pos[(size_t) s] = ts->h_breakpoints[(size_t) ts->h_span_tree[(size_t) s]];
-        }
-        int32_t *span_tree = nullptr;
-        double *span_pos = nullptr;
-        int64_t *span_off = nullptr;
-        int32_t *lo = nullptr, *hi = nullptr, *cursor = nullptr;
-        int2 *alive = nullptr;
-        if ((ret = dev_alloc(ts, &span_tree, NS + 1)) || (ret = dev_alloc(ts, &span_off, NS + 1))) {
+        if ((ret = build_span_plan(ts, h, num_spans)) != 0) {
             goto fail;
         }
-        TSG_CUDA(cudaMemcpy(span_tree, ts->h_span_tree.data(), (size_t) (NS + 1) * sizeof(int32_t),
-            cudaMemcpyHostToDevice));
-        if (cudaMalloc(&span_pos, (size_t) NS * sizeof(double)) != cudaSuccess
-            || cudaMalloc(&lo, (size_t) std::max<int64_t>(E, 1) * sizeof(int32_t)) != cudaSuccess
-            || cudaMalloc(&hi, (size_t) std::max<int64_t>(E, 1) * sizeof(int32_t)) != cudaSuccess
-            || cudaMalloc(&cursor, (size_t) NS * sizeof(int32_t)) != cudaSuccess) {
-            cudaFree(span_pos);
-            cudaFree(lo);
-            cudaFree(hi);
-            cudaFree(cursor);
-            ret = TSG_ERR_NO_MEMORY;
+        if ((ret = d2h(ts->h_site_position, t.site_pos, S)) != 0) {
             goto fail;
         }
-        TSG_CUDA(cudaMemcpy(span_pos, h_span_pos.data(), (size_t) NS * sizeof(double),
-            cudaMemcpyHostToDevice));
-        TSG_CUDA(cudaMemset(span_off, 0, (size_t) (NS + 1) * sizeof(int64_t)));
-        TSG_CUDA(cudaMemset(cursor, 0, (size_t) NS * sizeof(int32_t)));
-        if (E > 0) {
-            k_span_edge_range<<<grid_for(E), 256, 0, st>>>(t.left, t.right, E, span_pos, NS, lo,
-                hi, span_off);
-            TSG_LAUNCHED();
-        }
-        // span_off currently holds a difference array: counts = inclusive prefix
-        if ((ret = scan_exclusive_i64(span_off, span_off, NS + 1, tmp, st))) {
-            goto fail;
-        }
-        // exclusive prefix of differences gives counts shifted by one: count[s] =
-        // prefix[s + 1].  Convert to offsets on the host (NS is small).
-        std::vector<int64_t> h_pref((size_t) NS + 1);
-        TSG_CUDA(cudaMemcpy(h_pref.data(), span_off, (size_t) (NS + 1) * sizeof(int64_t),
-            cudaMemcpyDeviceToHost));
-        std::vector<int64_t> h_off((size_t) NS + 1);
-        h_off[0] = 0;
-        int64_t max_alive = 0;
-        for (int64_t s = 0; s < NS; s++) {
-            int64_t cnt = h_pref[(size_t) s + 1];
-            max_alive = std::max(max_alive, cnt);
-            h_off[(size_t) s + 1] = h_off[(size_t) s] + cnt;
-        }
-        ts->max_alive = max_alive;
-        TSG_CUDA(cudaMemcpy(span_off, h_off.data(), (size_t) (NS + 1) * sizeof(int64_t),
-            cudaMemcpyHostToDevice));
-        if ((ret = dev_alloc(ts, &alive, h_off[(size_t) NS]))) {
-            cudaFree(span_pos);
-            cudaFree(lo);
-            cudaFree(hi);
-            cudaFree(cursor);
-            goto fail;
-        }
-        if (E > 0) {
-            k_span_fill<<<grid_for(E), 256, 0, st>>>(t.parent, t.child, E, lo, hi, span_off,
-                cursor, alive);
-            TSG_LAUNCHED();
-        }
-        TSG_CUDA(cudaStreamSynchronize(st));
-        cudaFree(span_pos);
-        cudaFree(lo);
-        cudaFree(hi);
-        cudaFree(cursor);
-        ts->v.num_spans = NS;
-        ts->v.span_tree = span_tree;
-        ts->v.span_alive_off = span_off;
-        ts->v.span_alive = alive;
     }
     TSG_CUDA(cudaDeviceSynchronize());
     cudaFree(d_err);

@@ -534,9 +534,16 @@ class TreeSequence:
 
     # ------------------------------------------------------- fused batches
     def query(self, sample_sets, terms, windows=None, mode="branch", span_normalise=True,
-              polarised=False, both_modes=False, precision="f64"):
-        """Prepare a device-resident fused query (see :class:`Query`)."""
+              polarised=False, both_modes=False, precision="f64", sweep="auto"):
+        """Prepare a device-resident fused query (see :class:`Query`).
+
+        ``sweep="global"`` forces the global-memory sweep even where a span's
+        node state fits in shared memory."""
         flags = 0
+        if sweep == "global":
+            flags |= nat.FORCE_GLOBAL_SWEEP
+        elif sweep != "auto":
+            raise ValueError("sweep must be 'auto' or 'global'")
         if both_modes:
             flags |= nat.STAT_BOTH_MODES
         else:
