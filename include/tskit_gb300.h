@@ -77,6 +77,7 @@ extern "C" {
 #define TSG_ERR_TOO_MANY_OUTPUTS (-20004)
 #define TSG_ERR_BAD_TREE_SEQUENCE (-20005)
 #define TSG_ERR_WORKSPACE_TOO_SMALL (-20006)
+#define TSG_ERR_NOALLOC_TOO_LARGE (-20007)
 
 /* Summary terms of the named statistics (c/tskit/trees.c summary funcs). */
 #define TSG_DIVERSITY 1                  /* trees.c:3934  idx: i       */
@@ -239,6 +240,31 @@ int tsg_workspace_create(tsg_workspace_t **ws);
 int tsg_workspace_reserve(tsg_workspace_t *ws, int64_t bytes);
 int64_t tsg_workspace_bytes(const tsg_workspace_t *ws);
 int tsg_workspace_free(tsg_workspace_t *ws);
+
+/* ------------------------------------------ launch without any allocation
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory while a query runs -- a host that gives this library a fixed
+ * device-memory budget and owns all allocations, or a latency-critical
+ * serving path that cannot afford cudaMalloc -- this runs a prepared query
+ * (same result as tsg_query_launch) with its scratch in a fixed array that is
+ * part of the library's device image: TSG_NOALLOC_SCRATCH_BYTES (32 MiB) on
+ * every GPU that loads the library, held until the process exits.  It calls
+ * no cudaMalloc, cudaFree or allocating library routine.
+ *   - A query whose tsg_query_workspace_bytes exceeds the array is refused
+ *     with TSG_ERR_NOALLOC_TOO_LARGE (small tree sequences and few windows
+ *     fit; the benchmark-sized workloads need a tsg_workspace_t).
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture.
+ *   - All calls on a device share the one array and the launch clears what it
+ *     needs cleared: calls whose kernels overlap on the GPU (different
+ *     streams, or different host threads) race and corrupt each other's
+ *     results.  Order them on one stream.
+ * tsg_noalloc_check reads the device-side check word of the last such
+ * launch of `query` (synchronous), like tsg_workspace_check. */
+#define TSG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int tsg_query_launch_noalloc(const tsg_query_t *query, double *result_device, void *cuda_stream);
+int tsg_noalloc_check(const tsg_query_t *query);
 
 /* Number of kernel launches issued by this library since load (counter used
  * by the benchmarks to report launches). */

@@ -45,6 +45,8 @@ ERR_EMPTY_SAMPLE_SET = -908
 ERR_UNSUPPORTED_STAT_MODE = -909
 ERR_CUDA = -20001
 ERR_DEVICE_CHECK = -20002
+ERR_NOALLOC_TOO_LARGE = -20007
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
 class Tables_t(ctypes.Structure):
@@ -112,6 +114,8 @@ SIGNATURES = {
     "tsg_workspace_free": (ctypes.c_int, [_P]),
     "tsg_workspace_check": (ctypes.c_int, [_P, _P]),
     "tsg_launch_count": (_I64, []),
+    "tsg_query_launch_noalloc": (ctypes.c_int, [_P, _P, _P]),
+    "tsg_noalloc_check": (ctypes.c_int, [_P]),
 }
 
 _lib = None

@@ -1355,3 +1355,81 @@ int tsg_treeseq_genetic_relatedness(const tsg_treeseq_t *self, uint64_t K, const
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ launch without allocation
+//
+// Some callers cannot allocate device memory while they run a query: a host
+// application that hands this library a fixed device-memory budget and owns
+// every allocation itself, or a latency-critical serving path where a
+// cudaMalloc (with its implicit synchronisation) is not acceptable.  For them
+// tsg_query_launch_noalloc runs a prepared query with its scratch taken from
+// a fixed array that is part of this library's device image instead of a
+// tsg_workspace_t.  The array is TSG_NOALLOC_SCRATCH_BYTES on every GPU that
+// loads the library, for as long as the process lives.
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TSG_NOALLOC_SCRATCH_BYTES];
+
+namespace tsg {
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (the host-side symbol is not a device address).
+static std::mutex g_noalloc_mutex;
+static void *g_noalloc_ptr[64];
+
+static int noalloc_scratch(void **out)
+{
+    int dev = 0;
+    TSG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            return TSG_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return 0;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_query_launch_noalloc(const tsg_query_t *q, double *result_device, void *cuda_stream)
+{
+    if (q->ws_bytes > (int64_t) TSG_NOALLOC_SCRATCH_BYTES) {
+        return TSG_ERR_NOALLOC_TOO_LARGE;
+    }
+    void *scratch = nullptr;
+    int ret = noalloc_scratch(&scratch);
+    if (ret != 0) {
+        return ret;
+    }
+    // a workspace descriptor over the static array: no device allocation;
+    // every word the launch needs zeroed is cleared by the launch itself
+    tsg_workspace_t ws;
+    ws.ptr = scratch;
+    ws.bytes = (int64_t) TSG_NOALLOC_SCRATCH_BYTES;
+    return tsg_query_launch(q, &ws, result_device, cuda_stream);
+}
+
+int tsg_noalloc_check(const tsg_query_t *q)
+{
+    void *scratch = nullptr;
+    int ret = noalloc_scratch(&scratch);
+    if (ret != 0) {
+        return ret;
+    }
+    tsg_workspace_t ws;
+    ws.ptr = scratch;
+    ws.bytes = (int64_t) TSG_NOALLOC_SCRATCH_BYTES;
+    return tsg_workspace_check(&ws, q);
+}
+
+}  // extern "C"

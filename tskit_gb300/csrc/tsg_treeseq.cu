@@ -437,6 +437,8 @@ const char *tsg_strerror(int err)
             return "Too many summary outputs for the device sweep (maximum 64)";
         case TSG_ERR_BAD_TREE_SEQUENCE:
             return "Tables do not describe a valid tree sequence";
+        case TSG_ERR_NOALLOC_TOO_LARGE:
+            return "Query needs more scratch than the static no-allocation array holds (32 MiB)";
         case TSG_ERR_WORKSPACE_TOO_SMALL:
             return "Workspace too small for this query";
         default:
