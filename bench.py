@@ -331,7 +331,7 @@ def measured_peaks():
 
 def profile_traffic():
     """DRAM bytes per sweep launch from the committed ncu summary, if any."""
-    p = os.path.join(REPO, "profiles", "sweep_windowed_n10k.json")
+    p = os.path.join(REPO, "profiles", "sweep_pipeline_windowed_n10k.json")
     try:
         with open(p) as f:
             return json.load(f).get("dram_bytes_per_launch")
@@ -503,7 +503,9 @@ def run_gpu(args):
             "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"],
             "traffic": profile_traffic(),
-            "kernel": "k_sweep<float>",
+            "kernel": "sweep pipeline (k_node_mask, k_replay_items, k_eval_items, "
+                      "k_span_windows, k_site_eval, k_site_windows), timed between events on "
+                      "the launch stream",
             "algorithmic_bytes_per_launch": algo,
             "kernel_ms": sweep,
             "peak_source": peak_kind,

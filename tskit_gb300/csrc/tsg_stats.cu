@@ -1170,12 +1170,14 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 TSG_CUDA(cudaMemsetAsync(w.site_win, 0, (size_t) p.Wn * R * 8, st));
             }
         }
-    } else if (p.f32) {
-        k_sweep<float><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
     } else {
-        k_sweep<double><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
+        if (p.f32) {
+            k_sweep<float><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
+        } else {
+            k_sweep<double><<<(unsigned) slots, 256, 0, st>>>(ts->v, p, q->d, w);
+        }
+        TSG_LAUNCHED();
     }
-    TSG_LAUNCHED();
     if (q->ev_stop != nullptr) {
         TSG_CUDA(cudaEventRecord(q->ev_stop, st));
     }
