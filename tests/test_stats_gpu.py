@@ -162,3 +162,33 @@ def test_errors_match_reference_codes(medium):
     assert e.value.code == -601  # TSK_ERR_BAD_SAMPLES
     with pytest.raises(ValueError):
         ts.diversity([s], mode="nonsense")
+
+
+def test_large_branch_only_repeatable(cuda_lib):
+    """Spans with thousands of alive nodes: repeated single-mode launches are
+    bit-identical and match the oracle (guards the ordering between the seek,
+    the first-tree items and the replay)."""
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import sim
+
+    tables = sim.simulate(3000, 1e7, 20000, 60000, 8)
+    ts = tskit_gb300.TreeSequence(tables)
+    ots = O.OracleTS(tables)
+    sets = _sets(tables, 4, seed=2)
+    windows = np.linspace(0, tables.sequence_length, 101)
+    terms = [(O.DIVERSITY, (k,)) for k in range(4)]
+    exp = O.sample_count_stat(ots, sets, terms, windows=windows, mode="branch")
+    q = ts.query(sets, terms, windows=windows, mode="branch", precision="f64")
+    ws = tskit_gb300.Workspace(q.workspace_bytes)
+    outs = []
+    for _ in range(3):
+        r = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+        q.launch(ws, r)
+        torch.cuda.synchronize()
+        q.check(ws)
+        outs.append(r.cpu().numpy().reshape(exp.shape))
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+    np.testing.assert_allclose(outs[0], exp, rtol=RTOL_F64)

@@ -203,6 +203,10 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             }
         }
 
+        // the anchor items read the first tree's counts: finish them before
+        // the replay starts changing counts and parents
+        __syncthreads();
+
         // ---- replay (warp 0)
         if (threadIdx.x < 32) {
             int64_t cursor = ibase + (a1 - a0);
