@@ -40,9 +40,12 @@ extern "C" {
  * and the arithmetic of the bulk accumulation. */
 #define TSG_STAT_BOTH_MODES (1u << 20)
 #define TSG_PRECISION_F32_KAHAN (1u << 21)
-/* Use the global-memory sweep even when a span's node state fits in shared
- * memory (for testing the general path). */
+/* Use the general sweep even when the item pipeline applies (for testing
+ * the general path). */
 #define TSG_FORCE_GLOBAL_SWEEP (1u << 22)
+/* Run the item pipeline with its span node state in global memory (32-bit
+ * counts) even when it fits in shared memory (for testing that form). */
+#define TSG_FORCE_GLOBAL_STATE (1u << 23)
 
 /* tsg_treeseq_init options */
 #define TSG_TABLES_ON_DEVICE (1u << 0)
@@ -190,6 +193,20 @@ int tsg_treeseq_genetic_relatedness(const tsg_treeseq_t *self, uint64_t num_samp
     uint64_t num_index_tuples, const int32_t *index_tuples, uint64_t num_windows,
     const double *windows, uint32_t options, double *result);
 
+/* ------------------------------------------------ allele frequency spectrum
+ * Replaces tsk_treeseq_allele_frequency_spectrum (c/tskit/trees.c:3830-3928):
+ * same arguments, option bits and error codes; the result holds
+ * num_windows x num_time_windows x prod(sample_set_sizes[k] + 1) doubles (C
+ * order).  windows / time_windows may be NULL (whole genome / [0, inf)).
+ * Up to 7 sample sets while every sample count fits 16 bits and a span's
+ * node state fits in shared memory, else up to 3.  Branch areas are summed
+ * exactly (fixed point, 2^-128 resolution) and rounded once per bin.  Host
+ * pointers. */
+int tsg_treeseq_allele_frequency_spectrum(const tsg_treeseq_t *self,
+    uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_windows, const double *windows, uint64_t num_time_windows,
+    const double *time_windows, uint32_t options, double *result);
+
 /* ------------------------------------------------------ fused sample-count
  * Generalises tsk_treeseq_sample_count_stat (c/tskit/trees.c:2174-2220) to a
  * list of summary terms evaluated in one sweep.  With TSG_STAT_BOTH_MODES the
@@ -218,6 +235,12 @@ int tsg_query_create(tsg_query_t **query, const tsg_treeseq_t *self,
     uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
     uint64_t num_outputs, const tsg_output_t *outputs, uint64_t num_windows,
     const double *windows, uint32_t options);
+/* The allele frequency spectrum as a device-resident query (result layout as
+ * tsg_treeseq_allele_frequency_spectrum). */
+int tsg_query_create_afs(tsg_query_t **query, const tsg_treeseq_t *self,
+    uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_windows, const double *windows, uint64_t num_time_windows,
+    const double *time_windows, uint32_t options);
 int tsg_query_free(tsg_query_t *query);
 /* Device bytes the query needs in a workspace. */
 int64_t tsg_query_workspace_bytes(const tsg_query_t *query);

@@ -5,6 +5,8 @@ Pins the oracle: every fixture of the reference's C test library
 tests/golden/cases.json, must match the reference's output.  Genotypes are
 compared exactly, floating point at 1e-12 relative.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -44,3 +46,44 @@ def test_paper_ex_known_answers():
     assert abs(pi[0, 0] - 1.5) < 1e-12
     pi1 = O.one_way(ots, O.DIVERSITY, [[0]], mode="site", span_normalise=False)
     assert np.isnan(pi1[0, 0])
+
+
+@pytest.mark.parametrize("mode", ["site", "branch"])
+def test_oracle_afs_parentless_stretches_vs_reference(mode):
+    """The reference credits a child that regains a parent from its last
+    update (c/tskit/trees.c:3639-3800); the oracle follows it on inputs with
+    isolated leaves and temporary extra roots."""
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "oracle"))
+    import ref_import
+
+    if not ref_import.available():
+        pytest.skip("reference not built here")
+    tskit = ref_import.import_tskit()
+    from tskit_gb300 import sim
+    from ts_gaps import with_gaps
+
+    g = with_gaps(sim.simulate(40, 1e5, 150, 500, 6), 2, frac=0.25)
+    tc = tskit.TableCollection(g.sequence_length)
+    for t, f in zip(g.node_time, g.node_flags):
+        tc.nodes.add_row(flags=int(f), time=float(t))
+    for l, r, p, c in zip(g.edge_left, g.edge_right, g.edge_parent, g.edge_child):
+        tc.edges.add_row(l, r, p, c)
+    for x in g.site_position:
+        tc.sites.add_row(x, "0")
+    for s, n in zip(g.mutation_site, g.mutation_node):
+        tc.mutations.add_row(site=int(s), node=int(n), derived_state="1")
+    tc.sort()
+    tc.build_index()
+    tc.compute_mutation_parents()
+    ref = tc.tree_sequence()
+    ots = O.OracleTS(g)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(g.samples())
+    for sets in ([g.samples()], [np.sort(perm[:15]), np.sort(perm[15:])]):
+        for pol in (False, True):
+            kw = dict(windows=[0, 3e4, 7e4, 1e5], mode=mode, polarised=pol)
+            a = ref.allele_frequency_spectrum([list(s) for s in sets], **kw)
+            b = O.allele_frequency_spectrum(ots, sets, **kw).reshape(a.shape)
+            np.testing.assert_allclose(b, a, rtol=1e-12, atol=1e-15)

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 GPU_METHODS = {
     "diversity", "segregating_sites", "Y1", "divergence", "Y2", "f2", "Y3", "f3", "f4",
-    "genetic_relatedness", "Fst", "Tajimas_D",
+    "genetic_relatedness", "Fst", "Tajimas_D", "allele_frequency_spectrum",
 }
 CASES = [(n, c) for n, c in all_cases() if c["method"] in GPU_METHODS]
 _ts = {}
@@ -91,7 +91,8 @@ def _fused_terms(K):
 
 
 @pytest.mark.parametrize("precision,sweep", [("f64", "auto"), ("f32", "auto"),
-                                             ("f64", "global")])
+                                             ("f64", "global"), ("f64", "global_state"),
+                                             ("f32", "global_state")])
 @pytest.mark.parametrize("polarised", [False, True])
 def test_fused_both_modes_vs_oracle(medium, precision, sweep, polarised):
     import torch
@@ -192,3 +193,36 @@ def test_large_branch_only_repeatable(cuda_lib):
     for o in outs[1:]:
         np.testing.assert_array_equal(o, outs[0])
     np.testing.assert_allclose(outs[0], exp, rtol=RTOL_F64)
+
+
+@pytest.mark.parametrize("n,breaks", [(20000, 400), (70000, 60)])
+def test_global_state_form_large_n(cuda_lib, n, breaks):
+    """Spans whose node state exceeds shared memory (n = 20000), and sample
+    sets above the 16-bit count range (n = 70000), run the item pipeline with
+    node state in global memory and 32-bit counts."""
+    import tskit_gb300
+    from tskit_gb300 import sim
+
+    tables = sim.simulate(n, 1e6, breaks, 3000, 12)
+    ts = tskit_gb300.TreeSequence(tables)
+    ots = O.OracleTS(tables)
+    sets = [tables.samples()] if n > 65535 else _sets(tables, 3, seed=4)
+    terms = [(O.DIVERSITY, (k,)) for k in range(len(sets))]
+    terms += [(O.SEGSITES, (0,))]
+    if len(sets) > 1:
+        terms += [(O.DIVERGENCE, (0, 1)), (O.Y3, (0, 1, 2))]
+    windows = np.linspace(0, tables.sequence_length, 5)
+    for mode in ("branch", "site"):
+        exp = O.sample_count_stat(ots, sets, terms, windows=windows, mode=mode)
+        for precision in ("f64", "f32"):
+            import torch
+
+            q = ts.query(sets, terms, windows=windows, mode=mode, precision=precision)
+            ws = tskit_gb300.Workspace(q.workspace_bytes)
+            r = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+            q.launch(ws, r)
+            torch.cuda.synchronize()
+            q.check(ws)
+            got = r.cpu().numpy().reshape(exp.shape)
+            rtol = RTOL_F64 if (precision == "f64" or mode == "site") else RTOL_F32
+            np.testing.assert_allclose(got, exp, rtol=rtol, err_msg=f"{mode} {precision}")

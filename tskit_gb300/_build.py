@@ -23,6 +23,11 @@ CUDA_SOURCES = [
     "tsg_treeseq.cu",
     "tsg_plan.cu",
     "tsg_stats.cu",
+    "tsg_eval_f32_pol.cu",
+    "tsg_eval_f32_unpol.cu",
+    "tsg_eval_f64_pol.cu",
+    "tsg_eval_f64_unpol.cu",
+    "tsg_afs.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -21,6 +21,7 @@ STAT_NONCENTRED = 1 << 14
 STAT_BOTH_MODES = 1 << 20
 PRECISION_F32_KAHAN = 1 << 21
 FORCE_GLOBAL_SWEEP = 1 << 22
+FORCE_GLOBAL_STATE = 1 << 23
 TABLES_ON_DEVICE = 1 << 0
 
 (DIVERSITY, SEGREGATING_SITES, Y1, DIVERGENCE, Y2, F2, Y3, F3, F4, RELATEDNESS,
@@ -103,6 +104,10 @@ SIGNATURES = {
     "tsg_treeseq_genetic_relatedness": (ctypes.c_int, _K_WAY),
     "tsg_treeseq_sample_count_stat": (ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U64, _P, _U32, _P]),
     "tsg_query_create": (ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
+    "tsg_treeseq_allele_frequency_spectrum": (
+        ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U64, _P, _U32, _P]),
+    "tsg_query_create_afs": (
+        ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),
     "tsg_query_workspace_bytes": (_I64, [_P]),
     "tsg_query_result_size": (_I64, [_P]),

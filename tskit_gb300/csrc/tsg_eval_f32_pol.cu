@@ -1,0 +1,5 @@
+// Item evaluation, FP32 per lane, polarised.
+#define TSG_EVAL_F float
+#define TSG_EVAL_UNPOL false
+#define TSG_EVAL_NAME launch_eval_f32_pol
+#include "tsg_eval_inst.cuh"

@@ -1,0 +1,5 @@
+// Item evaluation, FP64 per lane, polarised.
+#define TSG_EVAL_F double
+#define TSG_EVAL_UNPOL false
+#define TSG_EVAL_NAME launch_eval_f64_pol
+#include "tsg_eval_inst.cuh"

@@ -1,0 +1,5 @@
+// Item evaluation, FP64 per lane, unpolarised.
+#define TSG_EVAL_F double
+#define TSG_EVAL_UNPOL true
+#define TSG_EVAL_NAME launch_eval_f64_unpol
+#include "tsg_eval_inst.cuh"

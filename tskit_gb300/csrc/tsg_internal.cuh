@@ -46,6 +46,7 @@ enum DeviceError : int32_t {
     DEV_BAD_SITE = 6,
     DEV_BAD_MUTATION = 7,
     DEV_ITEM_PLAN = 8,
+    DEV_AFS_RANGE = 9,
 };
 
 __device__ __forceinline__ void dev_error(int32_t *flag, int32_t code)
@@ -118,6 +119,12 @@ struct TSView {
     const int64_t *chunk_end;
     const int64_t *tree_chunk_off;  // num_trees + 1: first chunk of each tree
     int64_t num_chunks;
+    // the reference allele frequency spectrum's lazy branch accounting
+    const uint8_t *node_is_parent;  // per node: a parent in some edge
+    const double *ins_left;       // insertion order: edge left
+    const double *ins_right;      // insertion order: edge right
+    const double *ins_lu;         // insertion order: the child's last update before the
+                                  // insertion (null when always the insertion position)
 };
 
 // items per evaluation chunk (one warp)
@@ -128,6 +135,7 @@ struct HostTopology {
     std::vector<double> left, right;           // edge order
     std::vector<int32_t> parent, child;        // edge order
     std::vector<int32_t> ins_parent, ins_child, rem_parent, rem_child;  // index orders
+    std::vector<int32_t> ins_edge;             // insertion order (edge ids)
     std::vector<int32_t> tree_in, tree_out, tree_sites;  // num_trees + 1
     std::vector<int32_t> site_mut;             // num_sites + 1
     std::vector<int32_t> mut_node;             // num_mutations

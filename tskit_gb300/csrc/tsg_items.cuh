@@ -31,60 +31,11 @@
 // Item values are differences of the summary function at integer counts, so
 // no rounding accumulates across spans.
 
-#define TSG_ITEM_PATH 0
-#define TSG_ITEM_PLUS 1
-#define TSG_ITEM_MINUS 2
-#define TSG_ITEM_LEAF_PLUS 3
-#define TSG_ITEM_LEAF_MINUS 4
-#define TSG_LEAF_TABLE_KMAX 4
+#pragma once
 
-template <int KQ>
-struct Item {
-    uint64_t xo[KQ];
-    uint64_t xn[KQ];
-    double bl;
-    int32_t kind;
-    int32_t pad;
-};
+#include "tsg_replay.cuh"
 
-template <int KQ>
-__device__ __forceinline__ Pack item_pack(const uint64_t *a)
-{
-    Pack p;
-    p.lo = a[0];
-    p.hi = KQ > 1 ? a[KQ > 1 ? 1 : 0] : 0ull;
-    return p;
-}
-
-template <int KQ>
-__device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &xo, const Pack &xn, double bl,
-    int kind)
-{
-    Item<KQ> v;
-    v.xo[0] = xo.lo;
-    v.xn[0] = xn.lo;
-    if (KQ > 1) {
-        v.xo[KQ > 1 ? 1 : 0] = xo.hi;
-        v.xn[KQ > 1 ? 1 : 0] = xn.hi;
-    }
-    v.bl = bl;
-    v.kind = kind;
-    v.pad = 0;
-    *it = v;
-}
-
-// item for an edge's child: a leaf (leaf_table) stores its membership bits
-template <int KQ>
-__device__ __forceinline__ void child_item(Item<KQ> *it, int32_t enc, uint32_t mask,
-    const Pack &x, double bl, int sign, bool leaf_table)
-{
-    if (enc < 0 && leaf_table) {
-        item_put<KQ>(it, Pack{0, 0}, Pack{(uint64_t) mask, 0}, bl,
-            sign > 0 ? TSG_ITEM_LEAF_PLUS : TSG_ITEM_LEAF_MINUS);
-    } else {
-        item_put<KQ>(it, Pack{0, 0}, x, bl, sign > 0 ? TSG_ITEM_PLUS : TSG_ITEM_MINUS);
-    }
-}
+namespace tsg {
 
 // node -> sample-set membership bits for this query
 __global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
@@ -96,19 +47,18 @@ __global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
     }
 }
 
-template <int KQ>
+template <int W, int KQ, typename IdxT>
 __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams q, QueryDev qd,
-    WsDev w)
+    WsDev w, int64_t slot_bytes)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_span;
     const int64_t L = ts.max_local;
-    SmemSpan sp;
-    sp.KQ = KQ;
-    sp.time = (double *) smem_raw;
-    sp.xq = (uint64_t *) (sp.time + L);
-    sp.cnt = (uint32_t *) (sp.xq + L * KQ);
-    sp.par = (uint16_t *) (sp.cnt + L);
+    constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
+    SpanState<IdxT> sp = span_state_at<IdxT>(sizeof(IdxT) == 2
+            ? smem_raw
+            : (unsigned char *) w.state + (int64_t) blockIdx.x * slot_bytes,
+        L, KQ);
     const int K = q.K;
     const int lane = threadIdx.x & 31;
     const bool leaf_table = K <= TSG_LEAF_TABLE_KMAX;
@@ -130,64 +80,7 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
         const int32_t *l2g = ts.span_l2g + lo;
         const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
 
-        // ---- seek: local nodes start as roots carrying their own weights
-        for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
-            const int32_t g = l2g[l];
-            sp.time[l] = ts.node_time[g];
-            sp.par[l] = (uint16_t) TSG_NO_PARENT;
-            sp.cnt[l] = 0;
-            pk_store(sp, l, pk_from_mask(qd.node_mask[g], K));
-        }
-        __syncthreads();
-        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
-            const int2 pc = ts.span_alive_enc[i];
-            if (pc.y >= 0) {
-                sp.par[pc.y] = (uint16_t) pc.x;
-            }
-        }
-        __syncthreads();
-        // bottom-up counts: every node is added to its parent once, by the
-        // last of the parent's children to complete (counter word per node:
-        // children in the low half, arrivals in the high half)
-        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
-            const int2 pc = ts.span_alive_enc[i];
-            atomicAdd(&sp.cnt[pc.x], 1u);
-        }
-        __syncthreads();
-        for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
-            const int2 pc = ts.span_alive_enc[i];
-            if (pc.y >= 0 && (sp.cnt[pc.y] & 0xFFFFu) != 0) {
-                continue;  // an internal child: completed by its own children
-            }
-            Pack contrib = pc.y >= 0 ? pk_load(sp, pc.y)
-                                     : pk_from_mask(qd.node_mask[-pc.y - 1], K);
-            uint32_t v = (uint32_t) pc.x;
-            for (int32_t guard = 0; v != TSG_NO_PARENT; guard++) {
-                if (guard > Ls) {
-                    dev_error(w.err, DEV_PATH_TOO_LONG);
-                    break;
-                }
-                if (contrib.lo) {
-                    atomicAdd((unsigned long long *) &sp.xq[v * KQ], (unsigned long long) contrib.lo);
-                }
-                if (KQ > 1 && contrib.hi) {
-                    atomicAdd((unsigned long long *) &sp.xq[v * KQ + (KQ > 1 ? 1 : 0)],
-                        (unsigned long long) contrib.hi);
-                }
-                __threadfence_block();
-                const uint32_t old = atomicAdd(&sp.cnt[v], 0x10000u);
-                if ((old >> 16) + 1 != (old & 0xFFFFu)) {
-                    break;
-                }
-                __threadfence_block();
-                contrib.lo = *(volatile unsigned long long *) &sp.xq[v * KQ];
-                if (KQ > 1) {
-                    contrib.hi = *(volatile unsigned long long *) &sp.xq[v * KQ + (KQ > 1 ? 1 : 0)];
-                }
-                v = sp.par[v];
-            }
-        }
-        __syncthreads();
+        span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
 
         // ---- anchor items: every node alive at the span start
         const int64_t ibase = ts.tree_item_off[t0];
@@ -196,9 +89,9 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                 const int2 pc = ts.span_alive_enc[i];
                 const int32_t g = pc.y >= 0 ? l2g[pc.y] : -pc.y - 1;
                 const uint32_t m = qd.node_mask[g];
-                const Pack x = pc.y >= 0 ? pk_load(sp, pc.y) : pk_from_mask(m, K);
+                const Pack x = pc.y >= 0 ? st_load(sp, pc.y) : pk_from_mask<W>(m, K);
                 const double tc = pc.y >= 0 ? sp.time[pc.y] : ts.node_time[g];
-                child_item<KQ>(items + ibase + (i - a0), pc.y, m, x, sp.time[pc.x] - tc, +1,
+                child_item<KQ>(items + ibase + (i - a0), pc.y, m, x, tc, sp.time[pc.x], +1,
                     leaf_table);
             }
         }
@@ -212,14 +105,14 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             int64_t cursor = ibase + (a1 - a0);
             // one edge event; cm / ct: membership bits and time of a leaf child
             auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm, double ct) {
-                const Pack xc = c >= 0 ? pk_load(sp, c) : pk_from_mask(cm, K);
+                const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
                 if (q.branch && lane == 0) {
                     const double tc = c >= 0 ? sp.time[c] : ct;
-                    child_item<KQ>(items + cursor, c, cm, xc, sp.time[p] - tc, sign, leaf_table);
+                    child_item<KQ>(items + cursor, c, cm, xc, tc, sp.time[p], sign, leaf_table);
                 }
                 cursor++;
                 if (c >= 0) {
-                    sp.par[c] = sign > 0 ? (uint16_t) p : (uint16_t) TSG_NO_PARENT;
+                    sp.par[c] = sign > 0 ? (IdxT) p : (IdxT) TSG_NO_PARENT;
                 }
                 uint32_t v = (uint32_t) p;
                 int32_t guard = 0;
@@ -242,7 +135,7 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                     }
                     const unsigned active = __ballot_sync(0xffffffffu, mine != TSG_NO_PARENT);
                     if (mine != TSG_NO_PARENT) {
-                        const Pack xo = pk_load(sp, (int32_t) mine);
+                        const Pack xo = st_load(sp, (int64_t) mine);
                         Pack xn;
                         if (sign > 0) {
                             xn.lo = xo.lo + xc.lo;
@@ -252,10 +145,11 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                             xn.hi = xo.hi - xc.hi;
                         }
                         if (q.branch) {
-                            const double bl = up != TSG_NO_PARENT ? sp.time[up] - sp.time[mine] : 0.0;
-                            item_put<KQ>(items + cursor + lane, xo, xn, bl, TSG_ITEM_PATH);
+                            const double tu = sp.time[mine];
+                            const double tp = up != TSG_NO_PARENT ? sp.time[up] : tu;
+                            item_put<KQ>(items + cursor + lane, xo, xn, tu, tp, TSG_ITEM_PATH);
                         }
-                        pk_store(sp, (int32_t) mine, xn);
+                        pk_store(sp, (int64_t) mine, xn);
                     }
                     cursor += __popc(active);
                 }
@@ -296,8 +190,8 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                     const int32_t m1 = ts.site_mut[ts.tree_sites[t + 1]];
                     for (int32_t m = m0 + lane; m < m1; m += 32) {
                         const int32_t enc = ts.mut_enc[m];
-                        const Pack x = enc >= 0 ? pk_load(sp, enc)
-                                                : pk_from_mask(qd.node_mask[-enc - 1], K);
+                        const Pack x = enc >= 0 ? st_load(sp, enc)
+                                                : pk_from_mask<W>(qd.node_mask[-enc - 1], K);
                         w.mcnt[(int64_t) m * KQ] = x.lo;
                         if (KQ > 1) {
                             w.mcnt[(int64_t) m * KQ + (KQ > 1 ? 1 : 0)] = x.hi;
@@ -308,87 +202,6 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             }
         }
         __syncthreads();
-    }
-}
-
-// Value of every item of a chunk for every term, summed per chunk (one
-// warp per chunk; chunks never cross trees).
-template <typename F, bool UNPOL, int RMAX, int KQ>
-__global__ void __launch_bounds__(256, 2) k_eval_items(TSView ts, QueryParams q, WsDev w)
-{
-    __shared__ F s_leaf[1 << TSG_LEAF_TABLE_KMAX][RMAX];
-    const int lane = threadIdx.x & 31;
-    const int R = q.R;
-    if (q.K <= TSG_LEAF_TABLE_KMAX) {
-        // F of every membership pattern a leaf can have
-        const int npat = 1 << q.K;
-        for (int i = threadIdx.x; i < npat * R; i += blockDim.x) {
-            const int pat = i / R, r = i % R;
-            const Pack x = pk_from_mask((uint32_t) pat, q.K);
-            F mx, mc;
-            pk_means<F>(q, x, mx, mc);
-            s_leaf[pat][r] = term_F<F, UNPOL>(q, r, x, mx, mc);
-        }
-        __syncthreads();
-    }
-    const int64_t c = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (c >= ts.num_chunks) {
-        return;
-    }
-    const Item<KQ> *items = (const Item<KQ> *) w.items;
-    const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
-    // at most TSG_ITEM_CHUNK / 32 items per lane: plain sums in F, then FP64
-    F acc[RMAX];
-#pragma unroll
-    for (int r = 0; r < RMAX; r++) {
-        acc[r] = 0;
-    }
-    for (int64_t i = b + lane; i < e; i += 32) {
-        const Item<KQ> it = items[i];
-        const F bl = (F) it.bl;
-        if (it.kind >= TSG_ITEM_LEAF_PLUS) {
-            const int pat = (int) it.xn[0];
-            const F sb = it.kind == TSG_ITEM_LEAF_PLUS ? bl : -bl;
-#pragma unroll
-            for (int r = 0; r < RMAX; r++) {
-                if (r < R) {
-                    acc[r] += sb * s_leaf[pat][r];
-                }
-            }
-            continue;
-        }
-        const Pack xn = item_pack<KQ>(it.xn);
-        F mxn, mcn;
-        pk_means<F>(q, xn, mxn, mcn);
-        if (it.kind == TSG_ITEM_PATH) {
-            const Pack xo = item_pack<KQ>(it.xo);
-            F mxo, mco;
-            pk_means<F>(q, xo, mxo, mco);
-#pragma unroll
-            for (int r = 0; r < RMAX; r++) {
-                if (r < R) {
-                    acc[r] += bl * (term_F<F, UNPOL>(q, r, xn, mxn, mcn)
-                        - term_F<F, UNPOL>(q, r, xo, mxo, mco));
-                }
-            }
-        } else {
-            const F sb = it.kind == TSG_ITEM_PLUS ? bl : -bl;
-#pragma unroll
-            for (int r = 0; r < RMAX; r++) {
-                if (r < R) {
-                    acc[r] += sb * term_F<F, UNPOL>(q, r, xn, mxn, mcn);
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < RMAX; r++) {
-        if (r < R) {
-            const double v = warp_sum((double) acc[r]);
-            if (lane == r) {
-                w.dD[c * R + r] = v;
-            }
-        }
     }
 }
 
@@ -438,7 +251,7 @@ __global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, 
 
 // Each site's summary, summed over its alleles (skipping the ancestral one
 // when polarised), from the integer counts under its mutations.
-template <int RMAX, int KQ>
+template <int RMAX, int W, int KQ>
 __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsDev w)
 {
     const int64_t site = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
@@ -460,10 +273,11 @@ __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsD
         // allele state: the set sizes for the ancestral allele, plus the counts
         // under mutations to a, minus those under mutations away from a
         // (c/tskit/trees.c:1525-1612), in integers
-        int32_t st[TSG_SMEM_KMAX];
+        constexpr int KM = 2 * (64 / W);
+        int64_t st[KM];
 #pragma unroll
-        for (int k = 0; k < TSG_SMEM_KMAX; k++) {
-            st[k] = (a == 0 && k < K) ? (int32_t) q.set_size[k] : 0;
+        for (int k = 0; k < KM; k++) {
+            st[k] = (a == 0 && k < K) ? (int64_t) q.set_size[k] : 0;
         }
         for (int32_t m = m0; m < m1; m++) {
             Pack xm;
@@ -471,27 +285,22 @@ __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsD
             xm.hi = KQ > 1 ? w.mcnt[(int64_t) m * KQ + (KQ > 1 ? 1 : 0)] : 0ull;
             const int al = ts.mutation_allele[m], alt = ts.mutation_alt[m];
 #pragma unroll
-            for (int k = 0; k < TSG_SMEM_KMAX; k++) {
-                const int32_t v = (int32_t) pk_get(xm, k);
+            for (int k = 0; k < KM; k++) {
+                const int64_t v = (int64_t) pk_get<W>(xm, k);
                 st[k] += (al == a ? v : 0) - (alt == a ? v : 0);
             }
         }
         Pack ps{0, 0};
 #pragma unroll
-        for (int k = 0; k < TSG_SMEM_KMAX; k++) {
-            const uint64_t v = (uint64_t) (st[k] & 0xFFFF);
-            if (k < 4) {
-                ps.lo |= v << (16 * k);
-            } else {
-                ps.hi |= v << (16 * (k - 4));
-            }
+        for (int k = 0; k < KM; k++) {
+            pk_set<W>(ps, k, (uint64_t) st[k] & ((1ull << W) - 1ull));
         }
         double mx, mc;
-        pk_means<double>(q, ps, mx, mc);
+        pk_means<double, W>(q, ps, mx, mc);
 #pragma unroll
         for (int r = 0; r < RMAX; r++) {
             if (r < R) {
-                val[r] += term_F<double, false>(q, r, ps, mx, mc);
+                val[r] += term_F<double, false, W>(q, r, ps, mx, mc);
             }
         }
     }
@@ -531,3 +340,5 @@ __global__ void __launch_bounds__(256) k_site_windows(QueryParams q, QueryDev qd
         w.site_win[wdx * q.R + r] = red[0];
     }
 }
+
+}  // namespace tsg

@@ -20,6 +20,7 @@
 // one span and the event encodings can live in arrays parallel to the
 // insertion and removal orders.
 #include <algorithm>
+#include <cmath>
 #include <thread>
 #include <vector>
 
@@ -108,6 +109,13 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         }
     }
 
+    // nodes that are a parent in some edge; every other node is a leaf in
+    // every tree
+    std::vector<uint8_t> is_parent((size_t) N, 0);
+    for (int64_t e = 0; e < E; e++) {
+        is_parent[(size_t) h.parent[(size_t) e]] = 1;
+    }
+
     // per-span local numbering and encodings, spans in parallel
     std::vector<int2> alive_global(alive_edge.size()), alive_enc(alive_edge.size());
     std::vector<int2> ins_enc((size_t) E), rem_enc((size_t) E);
@@ -142,6 +150,19 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                 for (int32_t i = i0; i < i1; i++) {
                     assign(h.ins_parent[(size_t) i]);
                 }
+                // children that are parents elsewhere carry state too, so that
+                // the span's leaves are exactly the tree sequence's leaves
+                for (int64_t i = a0; i < a1; i++) {
+                    const int32_t c = h.child[(size_t) alive_edge[(size_t) i]];
+                    if (is_parent[(size_t) c]) {
+                        assign(c);
+                    }
+                }
+                for (int32_t i = i0; i < i1; i++) {
+                    if (is_parent[(size_t) h.ins_child[(size_t) i]]) {
+                        assign(h.ins_child[(size_t) i]);
+                    }
+                }
                 for (int64_t i = a0; i < a1; i++) {
                     int32_t e = alive_edge[(size_t) i];
                     alive_global[(size_t) i] = make_int2(h.parent[(size_t) e], h.child[(size_t) e]);
@@ -168,22 +189,42 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     for (auto &th : pool) {
         th.join();
     }
-    // Item plan of the shared-memory sweep: per tree, the number of items the
-    // replay emits -- one per node alive at the span start (first tree of the
-    // span) and, for each edge event entering a later tree of the span, one
-    // for the edge's child plus one per node on the parent's root path.  The
-    // path lengths are topology-only, so the replay is simulated here.
+    // Item plan: per tree, the number of items the replay emits -- one per
+    // node alive at the span start (first tree of the span) and, for each edge
+    // event entering a later tree of the span, one for the edge's child plus
+    // one per node on the parent's root path.  The path lengths are
+    // topology-only, so the replay is simulated here.
+    //
+    // The same simulation records the "touches" of the reference's branch
+    // allele frequency spectrum (c/tskit/trees.c:3640-3800), which settles a
+    // node's accumulated area whenever the node's own edge is removed or a root
+    // path walk passes through it, and not when its edge is inserted: a child
+    // inserted after a parentless stretch is credited for that stretch too,
+    // from its last touch.  ins_lu records that last touch for every insertion
+    // where it precedes the insertion position.  A span simulates the
+    // transitions into its trees after the first and into the next span's
+    // first tree; a child untouched in the span before its insertion takes its
+    // last touch from the earlier spans (resolved in span order below).
     std::vector<int64_t> tree_items((size_t) T + 1, 0);
     std::vector<int64_t> span_max_children((size_t) NS, 0);
+    const double nan = std::nan("");
+    std::vector<double> ins_lu((size_t) E, nan);
+    std::vector<std::vector<std::pair<int32_t, double>>> span_touch((size_t) NS);
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> span_pending((size_t) NS);
     {
         std::vector<std::thread> pool2;
         for (unsigned tid = 0; tid < nthreads; tid++) {
             pool2.emplace_back([&, tid]() {
                 std::vector<int32_t> par, nch;
+                std::vector<double> lt;
+                std::vector<uint8_t> touched;
                 for (int64_t s = tid; s < NS; s += nthreads) {
                     const int32_t t0 = st[(size_t) s], t1 = st[(size_t) s + 1];
-                    par.assign(l2g[(size_t) s].size(), -1);
-                    nch.assign(l2g[(size_t) s].size(), 0);
+                    const size_t Ls = l2g[(size_t) s].size();
+                    par.assign(Ls, -1);
+                    nch.assign(Ls, 0);
+                    lt.assign(Ls, 0.0);
+                    touched.assign(Ls, 0);
                     const int64_t a0 = alive_off[(size_t) s], a1 = alive_off[(size_t) s + 1];
                     for (int64_t i = a0; i < a1; i++) {
                         const int2 pc = alive_enc[(size_t) i];
@@ -194,31 +235,53 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                             span_max_children[(size_t) s], ++nch[(size_t) pc.x]);
                     }
                     tree_items[(size_t) t0] = a1 - a0;
-                    auto depth = [&](int32_t v) {
+                    double x = 0;
+                    auto touch = [&](int32_t l) {
+                        lt[(size_t) l] = x;
+                        touched[(size_t) l] = 1;
+                    };
+                    // nodes on the root path from v (inclusive), touching them
+                    auto walk = [&](int32_t v) {
                         int64_t d = 0;
-                        while (v >= 0 && d <= (int64_t) par.size()) {
+                        while (v >= 0 && d <= (int64_t) Ls) {
                             d++;
+                            touch(v);
                             v = par[(size_t) v];
                         }
                         return d;
                     };
-                    for (int32_t t = t0 + 1; t < t1; t++) {
+                    const int32_t tlast = t1 < T ? t1 : t1 - 1;
+                    for (int32_t t = t0 + 1; t <= tlast; t++) {
+                        x = ts->h_breakpoints[(size_t) t];
                         int64_t cnt = 0;
                         for (int32_t i = h.tree_out[(size_t) t]; i < h.tree_out[(size_t) t + 1]; i++) {
                             const int2 pc = rem_enc[(size_t) i];
                             if (pc.y >= 0) {
+                                touch(pc.y);
                                 par[(size_t) pc.y] = -1;
                             }
-                            cnt += 1 + depth(pc.x);
+                            cnt += 1 + walk(pc.x);
                         }
                         for (int32_t i = h.tree_in[(size_t) t]; i < h.tree_in[(size_t) t + 1]; i++) {
                             const int2 pc = ins_enc[(size_t) i];
                             if (pc.y >= 0) {
+                                if (!touched[(size_t) pc.y]) {
+                                    span_pending[(size_t) s].emplace_back(i, l2g[(size_t) s][(size_t) pc.y]);
+                                } else if (lt[(size_t) pc.y] < x) {
+                                    ins_lu[(size_t) i] = lt[(size_t) pc.y];
+                                }
                                 par[(size_t) pc.y] = pc.x;
                             }
-                            cnt += 1 + depth(pc.x);
+                            cnt += 1 + walk(pc.x);
                         }
-                        tree_items[(size_t) t] = cnt;
+                        if (t < t1) {
+                            tree_items[(size_t) t] = cnt;
+                        }
+                    }
+                    for (size_t l = 0; l < Ls; l++) {
+                        if (touched[l]) {
+                            span_touch[(size_t) s].emplace_back(l2g[(size_t) s][l], lt[l]);
+                        }
                     }
                 }
             });
@@ -226,6 +289,54 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         for (auto &th : pool2) {
             th.join();
         }
+    }
+    {
+        // last touches before each span, in span order (the reference starts
+        // every node's last update at 0)
+        std::vector<double> last((size_t) N, 0.0);
+        for (int64_t s = 0; s < NS; s++) {
+            for (const auto &pg : span_pending[(size_t) s]) {
+                const double xi = h.left[(size_t) h.ins_edge[(size_t) pg.first]];
+                if (last[(size_t) pg.second] < xi) {
+                    ins_lu[(size_t) pg.first] = last[(size_t) pg.second];
+                }
+            }
+            for (const auto &tc : span_touch[(size_t) s]) {
+                last[(size_t) tc.first] = tc.second;
+            }
+        }
+        // leaves are touched only by the removal of their own edges
+        std::vector<int32_t> inv((size_t) E);
+        for (int64_t i = 0; i < E; i++) {
+            inv[(size_t) h.ins_edge[(size_t) i]] = (int32_t) i;
+        }
+        std::vector<int32_t> order;
+        order.reserve((size_t) E);
+        for (int64_t e = 0; e < E; e++) {
+            if (!is_parent[(size_t) h.child[(size_t) e]]) {
+                order.push_back((int32_t) e);
+            }
+        }
+        std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            const int32_t ca = h.child[(size_t) a], cb = h.child[(size_t) b];
+            return ca != cb ? ca < cb : h.left[(size_t) a] < h.left[(size_t) b];
+        });
+        for (size_t k = 0; k < order.size(); k++) {
+            const int32_t e = order[k];
+            const bool first = k == 0 || h.child[(size_t) order[k - 1]] != h.child[(size_t) e];
+            const double lu = first ? 0.0 : h.right[(size_t) order[k - 1]];
+            if (lu < h.left[(size_t) e]) {
+                ins_lu[(size_t) inv[(size_t) e]] = lu;
+            }
+        }
+    }
+    bool any_gap = false;
+    for (int64_t i = 0; i < E && !any_gap; i++) {
+        any_gap = !std::isnan(ins_lu[(size_t) i]);
+    }
+    std::vector<double> ins_right((size_t) E);
+    for (int64_t i = 0; i < E; i++) {
+        ins_right[(size_t) i] = h.right[(size_t) h.ins_edge[(size_t) i]];
     }
     std::vector<int64_t> tree_item_off((size_t) T + 1, 0);
     for (int64_t t = 0; t < T; t++) {
@@ -270,6 +381,8 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     int64_t *d_alive_off, *d_local_off, *d_tree_item_off, *d_chunk_begin, *d_chunk_end,
         *d_tree_chunk_off;
     int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
+    uint8_t *d_is_parent = nullptr;
+    double *d_ins_right = nullptr, *d_ins_lu = nullptr;
     std::vector<int32_t> span_tree_v(st.begin(), st.end());
     if ((ret = upload_vec(ts, span_tree_v, &d_span_tree)) || (ret = upload_vec(ts, alive_off, &d_alive_off))
         || (ret = upload_vec(ts, alive_global, &d_alive)) || (ret = upload_vec(ts, alive_enc, &d_alive_enc))
@@ -279,9 +392,15 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         || (ret = upload_vec(ts, tree_item_off, &d_tree_item_off))
         || (ret = upload_vec(ts, chunk_begin, &d_chunk_begin))
         || (ret = upload_vec(ts, chunk_end, &d_chunk_end))
-        || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))) {
+        || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))
+        || (ret = upload_vec(ts, is_parent, &d_is_parent))
+        || (ret = upload_vec(ts, ins_right, &d_ins_right))
+        || (any_gap && (ret = upload_vec(ts, ins_lu, &d_ins_lu)))) {
         return ret;
     }
+    ts->v.node_is_parent = d_is_parent;
+    ts->v.ins_right = d_ins_right;
+    ts->v.ins_lu = any_gap ? d_ins_lu : nullptr;
     ts->v.num_spans = NS;
     ts->v.span_tree = d_span_tree;
     ts->v.span_alive_off = d_alive_off;

@@ -1,0 +1,114 @@
+// Query parameters and workspace views shared by the statistics kernels.
+#pragma once
+
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+struct Term {
+    int32_t type;
+    int32_t idx[4];
+};
+
+struct QueryParams {
+    int32_t K, KP, R, Wn;
+    int32_t branch, site, polarised, f32, need_mean;
+    int32_t num_slots;
+    double inv_K;
+    double set_size[TSG_MAX_SAMPLE_SETS];
+    double inv_size[TSG_MAX_SAMPLE_SETS];  // 1 / n_k
+    double inv[TSG_MAX_OUTPUTS];           // reciprocal denominator of each term
+    Term term[TSG_MAX_OUTPUTS];
+};
+
+struct QueryDev {
+    const uint32_t *sample_mask;  // per sample index: bit k = member of set k
+    const uint32_t *node_mask;    // per node: its sample-set membership bits (workspace)
+    const int32_t *win_site_lo;   // per window: first site (num_windows + 1 entries)
+    const double *windows;        // Wn + 1
+    const int32_t *span_wlo;      // per span: first window overlapping it
+    const int64_t *span_woff;     // per span: offset into span-window arrays
+    const int32_t *win_span_lo;   // per window: first overlapping span
+    const int32_t *win_span_hi;   // per window: last overlapping span
+};
+
+struct WsDev {
+    int32_t *parent;  // num_slots * N
+    int32_t *nchild;  // num_slots * N: children in the tree at the span start
+    int32_t *arrive;  // num_slots * N: children whose counts have been added
+    int32_t *x;       // num_slots * N * KP
+    double *A;        // span windows
+    double *B;        // span windows * R
+    double *SITE;     // span windows * R
+    double *D;        // spans * R
+    double *RS;       // spans * R
+    double *rs0;      // R
+    void *items;      // replay items (item pipeline)
+    void *state;      // per-CTA span node state (item pipeline, global-memory form)
+    uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)
+    double *dD;       // chunks * R: running-sum change of each item chunk
+    uint32_t *node_mask;  // per node sample-set bits
+    double *site_val;     // sites * R: per-site summary (shared-memory sweep)
+    double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
+    int32_t *err;
+    int32_t *counter;
+};
+
+
+template <typename F>
+__device__ __forceinline__ F warp_sum(F v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// Allele frequency spectrum of one query.  Counts carry the K sample sets
+// plus a last field with all of the tree sequence's samples.
+#define TSG_AFS_KMAX 7
+// fixed-point accumulation of branch areas: 8 limbs of 32 bits at 2^-128
+#define TSG_FX_LIMBS 8
+#define TSG_FX_FRAC 128
+struct AfsParams {
+    int32_t K;              // sample sets
+    int32_t Wn, TW;         // windows, time windows
+    int32_t polarised;
+    int64_t num_samples;
+    int64_t afs_size;       // prod (n_k + 1)
+    int64_t dims[TSG_AFS_KMAX];    // n_k + 1
+    int64_t stride[TSG_AFS_KMAX];  // C order
+    const double *windows;       // Wn + 1
+    const double *time_windows;  // TW + 1
+    unsigned long long *acc;     // branch: Wn * TW * afs_size bins x TSG_FX_LIMBS
+    double *out;                 // site: Wn * afs_size (the result)
+    int32_t *err;
+    int32_t *counter;
+};
+
+// Allele frequency spectrum launchers (tsg_afs.cu).  form as for the item
+// evaluation; slot_bytes: per-CTA node state in global memory (0: shared).
+int launch_afs_branch(int form, unsigned grid, size_t smem, int64_t slot_bytes, void *state,
+    cudaStream_t st, const TSView &v, const QueryDev &qd, const AfsParams &a);
+int launch_afs_site(int form, cudaStream_t st, const TSView &v, const AfsParams &a,
+    const uint64_t *mcnt);
+int launch_afs_finish(cudaStream_t st, const AfsParams &a, int span_normalise, int branch,
+    double *result);
+void *afs_replay_kernel(int form);
+
+// term budget of the item evaluation (accumulators per lane)
+#define TSG_ITEM_RMAX 32
+
+// Item evaluation launchers (tsg_eval_*.cu), FP32/FP64 x polarised/unpolarised.
+// form: count width and words, (W == 16 ? 0 : 2) + (KQ == 1 ? 0 : 1).
+#define TSG_EVAL_LAUNCHER(name)                                                          \
+    void name(int form, unsigned grid, cudaStream_t st, const TSView &v,                 \
+        const QueryParams &p, const WsDev &w)
+TSG_EVAL_LAUNCHER(launch_eval_f32_pol);
+TSG_EVAL_LAUNCHER(launch_eval_f32_unpol);
+TSG_EVAL_LAUNCHER(launch_eval_f64_pol);
+TSG_EVAL_LAUNCHER(launch_eval_f64_unpol);
+
+}  // namespace tsg
+
+#include "tsg_terms.cuh"

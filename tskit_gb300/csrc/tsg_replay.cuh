@@ -1,0 +1,176 @@
+// Replay items and span-state access shared by the item pipeline kernels.
+#pragma once
+
+#include "tsg_query.cuh"
+
+namespace tsg {
+
+#define TSG_ITEM_PATH 0
+#define TSG_ITEM_PLUS 1
+#define TSG_ITEM_MINUS 2
+#define TSG_ITEM_LEAF_PLUS 3
+#define TSG_ITEM_LEAF_MINUS 4
+#define TSG_LEAF_TABLE_KMAX 4
+
+template <int KQ>
+struct Item {
+    uint64_t xo[KQ];
+    uint64_t xn[KQ];
+    double tu, tp;  // node time and parent time (branch length tp - tu; 0 at a root)
+    int32_t kind;
+    int32_t pad;
+};
+
+template <int KQ>
+__device__ __forceinline__ Pack item_pack(const uint64_t *a)
+{
+    Pack p;
+    p.lo = a[0];
+    p.hi = KQ > 1 ? a[KQ > 1 ? 1 : 0] : 0ull;
+    return p;
+}
+
+template <int KQ>
+__device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &xo, const Pack &xn, double tu,
+    double tp, int kind)
+{
+    Item<KQ> v;
+    v.xo[0] = xo.lo;
+    v.xn[0] = xn.lo;
+    if (KQ > 1) {
+        v.xo[KQ > 1 ? 1 : 0] = xo.hi;
+        v.xn[KQ > 1 ? 1 : 0] = xn.hi;
+    }
+    v.tu = tu;
+    v.tp = tp;
+    v.kind = kind;
+    v.pad = 0;
+    *it = v;
+}
+
+// item for an edge's child: a leaf (leaf_table) stores its membership bits
+template <int KQ>
+__device__ __forceinline__ void child_item(Item<KQ> *it, int32_t enc, uint32_t mask,
+    const Pack &x, double tu, double tp, int sign, bool leaf_table)
+{
+    if (enc < 0 && leaf_table) {
+        item_put<KQ>(it, Pack{0, 0}, Pack{(uint64_t) mask, 0}, tu, tp,
+            sign > 0 ? TSG_ITEM_LEAF_PLUS : TSG_ITEM_LEAF_MINUS);
+    } else {
+        item_put<KQ>(it, Pack{0, 0}, x, tu, tp, sign > 0 ? TSG_ITEM_PLUS : TSG_ITEM_MINUS);
+    }
+}
+
+// loads of span state that atomics also update: shared memory is coherent;
+// in global memory they must bypass L1
+template <typename IdxT>
+__device__ __forceinline__ uint64_t st_ld(const uint64_t *p)
+{
+    if (sizeof(IdxT) == 2) {
+        return *p;
+    }
+    return __ldcg((const unsigned long long *) p);
+}
+
+template <typename IdxT>
+__device__ __forceinline__ uint32_t st_ld32(const uint32_t *p)
+{
+    if (sizeof(IdxT) == 2) {
+        return *p;
+    }
+    return __ldcg(p);
+}
+
+template <typename IdxT>
+__device__ __forceinline__ Pack st_load(const SpanState<IdxT> &sp, int64_t l)
+{
+    Pack p;
+    p.lo = st_ld<IdxT>(sp.xq + l * sp.KQ);
+    p.hi = sp.KQ > 1 ? st_ld<IdxT>(sp.xq + l * sp.KQ + 1) : 0ull;
+    return p;
+}
+
+// Layout of one span's node state at `base` (L nodes, KQ count words each):
+// time f64, counts, seek counter u32, parent IdxT.
+template <typename IdxT>
+__device__ __forceinline__ SpanState<IdxT> span_state_at(unsigned char *base, int64_t L, int KQ)
+{
+    SpanState<IdxT> sp;
+    sp.KQ = KQ;
+    sp.time = (double *) base;
+    sp.xq = (uint64_t *) (sp.time + L);
+    sp.cnt = (uint32_t *) (sp.xq + L * KQ);
+    sp.par = (IdxT *) (sp.cnt + L);
+    return sp;
+}
+
+// Rebuild the tree at a span's start in the span state (all threads of the
+// block): every stateful node starts as a root carrying its own sample-set
+// bits; the alive edges set the parents; counts accumulate bottom-up.  Ends
+// with the block synchronised.
+template <int W, int KQ, typename IdxT>
+__device__ void span_seek(const TSView &ts, const QueryDev &qd, int32_t *err,
+    const SpanState<IdxT> &sp, int K, int32_t Ls, const int32_t *l2g, int64_t a0, int64_t a1)
+{
+    constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
+    // ---- seek: local nodes start as roots carrying their own weights
+    for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
+        const int32_t g = l2g[l];
+        sp.time[l] = ts.node_time[g];
+        sp.par[l] = (IdxT) TSG_NO_PARENT;
+        sp.cnt[l] = 0;
+        pk_store(sp, (int64_t) l, pk_from_mask<W>(qd.node_mask[g], K));
+    }
+    __syncthreads();
+    for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+        const int2 pc = ts.span_alive_enc[i];
+        if (pc.y >= 0) {
+            sp.par[pc.y] = (IdxT) pc.x;
+        }
+    }
+    __syncthreads();
+    // bottom-up counts: every node is added to its parent once, by the
+    // last of the parent's children to complete (counter word per node:
+    // children in the low half, arrivals in the high half)
+    for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+        const int2 pc = ts.span_alive_enc[i];
+        atomicAdd(&sp.cnt[pc.x], 1u);
+    }
+    __syncthreads();
+    for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+        const int2 pc = ts.span_alive_enc[i];
+        if (pc.y >= 0 && (st_ld32<IdxT>(&sp.cnt[pc.y]) & 0xFFFFu) != 0) {
+            continue;  // an internal child: completed by its own children
+        }
+        Pack contrib = pc.y >= 0 ? st_load(sp, pc.y)
+                                 : pk_from_mask<W>(qd.node_mask[-pc.y - 1], K);
+        uint32_t v = (uint32_t) pc.x;
+        for (int32_t guard = 0; v != TSG_NO_PARENT; guard++) {
+            if (guard > Ls) {
+                dev_error(err, DEV_PATH_TOO_LONG);
+                break;
+            }
+            if (contrib.lo) {
+                atomicAdd((unsigned long long *) &sp.xq[(int64_t) v * KQ], (unsigned long long) contrib.lo);
+            }
+            if (KQ > 1 && contrib.hi) {
+                atomicAdd((unsigned long long *) &sp.xq[(int64_t) v * KQ + (KQ > 1 ? 1 : 0)],
+                    (unsigned long long) contrib.hi);
+            }
+            __threadfence_block();
+            const uint32_t old = atomicAdd(&sp.cnt[v], 0x10000u);
+            if ((old >> 16) + 1 != (old & 0xFFFFu)) {
+                break;
+            }
+            __threadfence_block();
+            contrib.lo = *(volatile unsigned long long *) &sp.xq[(int64_t) v * KQ];
+            if (KQ > 1) {
+                contrib.hi = *(volatile unsigned long long *) &sp.xq[(int64_t) v * KQ + (KQ > 1 ? 1 : 0)];
+            }
+            v = sp.par[v];
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace tsg

@@ -30,57 +30,10 @@
 #include <mutex>
 #include <vector>
 
-#include "tsg_internal.cuh"
+#include "tsg_items.cuh"
+#include "tsg_query.cuh"
 
 namespace tsg {
-
-struct Term {
-    int32_t type;
-    int32_t idx[4];
-};
-
-struct QueryParams {
-    int32_t K, KP, R, Wn;
-    int32_t branch, site, polarised, f32, need_mean;
-    int32_t num_slots;
-    double inv_K;
-    double set_size[TSG_MAX_SAMPLE_SETS];
-    double inv_size[TSG_MAX_SAMPLE_SETS];  // 1 / n_k
-    double inv[TSG_MAX_OUTPUTS];           // reciprocal denominator of each term
-    Term term[TSG_MAX_OUTPUTS];
-};
-
-struct QueryDev {
-    const uint32_t *sample_mask;  // per sample index: bit k = member of set k
-    const uint32_t *node_mask;    // per node: its sample-set membership bits (workspace)
-    const int32_t *win_site_lo;   // per window: first site (num_windows + 1 entries)
-    const double *windows;        // Wn + 1
-    const int32_t *span_wlo;      // per span: first window overlapping it
-    const int64_t *span_woff;     // per span: offset into span-window arrays
-    const int32_t *win_span_lo;   // per window: first overlapping span
-    const int32_t *win_span_hi;   // per window: last overlapping span
-};
-
-struct WsDev {
-    int32_t *parent;  // num_slots * N
-    int32_t *nchild;  // num_slots * N: children in the tree at the span start
-    int32_t *arrive;  // num_slots * N: children whose counts have been added
-    int32_t *x;       // num_slots * N * KP
-    double *A;        // span windows
-    double *B;        // span windows * R
-    double *SITE;     // span windows * R
-    double *D;        // spans * R
-    double *RS;       // spans * R
-    double *rs0;      // R
-    void *items;      // replay items (shared-memory sweep)
-    uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)
-    double *dD;       // chunks * R: running-sum change of each item chunk
-    uint32_t *node_mask;  // per node sample-set bits
-    double *site_val;     // sites * R: per-site summary (shared-memory sweep)
-    double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
-    int32_t *err;
-    int32_t *counter;
-};
 
 // ----------------------------------------------------------------- summary
 template <typename F>
@@ -118,14 +71,6 @@ __device__ __forceinline__ F term_value(int type, F xi, F xj, F xk, F xl, F ni, 
     }
 }
 
-template <typename F>
-__device__ __forceinline__ F warp_sum(F v)
-{
-    for (int o = 16; o > 0; o >>= 1) {
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    }
-    return v;
-}
 
 // Evaluate f at the count vector held one component per lane (xk on lane k)
 // for the terms of pass p (term index lane + 32 p).  All 32 lanes must call.
@@ -496,15 +441,22 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
     }
 }
 
-#include "tsg_terms.cuh"
-#include "tsg_items.cuh"
 
-// term budget of the item evaluation (accumulators per lane)
-#define TSG_ITEM_RMAX 32
-
-static void *replay_kernel(int KQ)
+// Item pipeline forms: node state in shared memory (16-bit counts and ids)
+// or in a per-CTA slice of global memory (32-bit counts and ids).
+static void *replay_kernel(int W, int KQ)
 {
-    return KQ == 1 ? (void *) k_replay_items<1> : (void *) k_replay_items<2>;
+    if (W == 16) {
+        return KQ == 1 ? (void *) k_replay_items<16, 1, uint16_t>
+                       : (void *) k_replay_items<16, 2, uint16_t>;
+    }
+    return KQ == 1 ? (void *) k_replay_items<32, 1, int32_t> : (void *) k_replay_items<32, 2, int32_t>;
+}
+
+// bytes of one span's node state: time, packed counts, seek counter, parent
+static int64_t span_state_bytes(int64_t L, int W, int KQ)
+{
+    return L * 8 + L * 8 * KQ + L * 4 + L * (W == 16 ? 2 : 4);
 }
 
 static int64_t smem_budget()
@@ -606,17 +558,25 @@ struct tsg_query {
     QueryDev d;
     void *dbuf;              // device copy of per-query arrays (owned), or null
     std::vector<char> blob;  // host image of the per-query arrays
-    int64_t off[7];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite
+    int64_t off[8];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite,
+                             // time windows (allele frequency spectrum)
     cudaEvent_t ev_start, ev_stop;  // optional events around the sweep kernel
     int64_t total_span_windows;
     int64_t num_slots;
     int64_t ws_bytes;
-    bool smem;
-    int KQ;
-    int64_t smem_bytes, smem_grid;
+    bool smem;               // item pipeline (either form); else the general sweep
+    bool gstate;             // item pipeline with node state in global memory
+    int W, KQ;               // count field width, 64-bit count words per node
+    int64_t smem_bytes, smem_grid, slot_bytes;
     int span_normalise;
     uint32_t options;
+    int kind;                // TSG_KIND_STATS or TSG_KIND_AFS
+    AfsParams afs;           // allele frequency spectrum (device pointers bound at launch)
+    int64_t afs_bins;        // windows x time windows x afs_size
 };
+
+#define TSG_KIND_STATS 0
+#define TSG_KIND_AFS 1
 
 namespace tsg {
 
@@ -712,6 +672,9 @@ int64_t tsg_query_workspace_bytes(const tsg_query_t *q) { return q->ws_bytes; }
 
 int64_t tsg_query_result_size(const tsg_query_t *q)
 {
+    if (q->kind == TSG_KIND_AFS) {
+        return q->afs_bins;
+    }
     return (int64_t) q->p.Wn * q->p.R * ((q->p.branch ? 1 : 0) + (q->p.site ? 1 : 0));
 }
 
@@ -730,6 +693,10 @@ static void query_bind(tsg_query_t *q, void *dev)
     q->d.win_span_hi = (const int32_t *) (b + q->off[5]);
     q->d.win_site_lo = (const int32_t *) (b + q->off[6]);
     q->d.node_mask = nullptr;
+    if (q->kind == TSG_KIND_AFS) {
+        q->afs.windows = q->d.windows;
+        q->afs.time_windows = (const double *) (b + q->off[7]);
+    }
 }
 
 // Validate the query and build its host image; the device copy is made by
@@ -774,6 +741,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     }
     tsg_query_t *q = new tsg_query_t();
     std::memset(&q->p, 0, sizeof(q->p));
+    q->kind = TSG_KIND_STATS;
     q->dbuf = nullptr;
     q->ev_start = nullptr;
     q->ev_stop = nullptr;
@@ -941,27 +909,48 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->num_slots = slots;
     p.num_slots = (int32_t) slots;
 
-    // shared-memory sweep when the span state fits: u16 counts and ids,
-    // f64 times, at most 8 sets and 32 terms
+    // item pipeline when the terms fit its accumulators: node state in shared
+    // memory when it fits (16-bit counts and ids, up to 8 sets), else in
+    // global memory (32-bit counts and ids, up to 4 sets)
     uint64_t max_size = 0;
     for (uint64_t k = 0; k < K; k++) {
         max_size = std::max<uint64_t>(max_size, sizes[k]);
     }
     const int64_t L = std::max<int64_t>(ts->v.max_local, 1);
-    const int64_t KQ = ((int64_t) K + 3) / 4;
-    q->smem_bytes = align_up(L * 8 + L * 8 * KQ + L * 4 + L * 2, 16);
-    q->smem = !(options & TSG_FORCE_GLOBAL_SWEEP) && K <= 8 && (int64_t) R <= TSG_ITEM_RMAX
-        && max_size <= 65535 && ts->v.max_local <= 65534 && ts->max_children < 65535
-        && q->smem_bytes <= smem_budget();
-    q->KQ = (int) KQ;
+    const bool forced = (options & TSG_FORCE_GLOBAL_SWEEP) != 0;
+    const bool items_ok = !forced && (int64_t) R <= TSG_ITEM_RMAX && ts->max_children < 65535;
+    q->smem = false;
+    q->gstate = false;
+    q->W = 16;
+    q->KQ = (int) (((int64_t) K + 3) / 4);
+    q->smem_bytes = align_up(span_state_bytes(L, 16, q->KQ), 16);
+    q->slot_bytes = 0;
+    if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 65534
+        && q->smem_bytes <= smem_budget() && !(options & TSG_FORCE_GLOBAL_STATE)) {
+        q->smem = true;
+    } else if (items_ok && K <= 4 && ts->v.max_local < INT32_MAX) {
+        q->smem = true;
+        q->gstate = true;
+        q->W = 32;
+        q->KQ = K <= 2 ? 1 : 2;
+        q->smem_bytes = 0;
+        q->slot_bytes = align_up(span_state_bytes(L, 32, q->KQ), 256);
+    }
+    const int64_t KQ = q->KQ;
     if (q->smem) {
         int per_sm = 0;
-        void *fn = replay_kernel((int) KQ);
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+        void *fn = replay_kernel(q->W, q->KQ);
+        if (!q->gstate) {
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+        }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
-        q->smem_grid = std::min<int64_t>((int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()),
-            std::max<int64_t>(NS, 1));
-        slots = 0;  // no per-slot node arrays
+        int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
+        if (q->gstate) {
+            // node state of every resident CTA at most 8 GiB
+            grid = std::min<int64_t>(grid, std::max<int64_t>(1, ((int64_t) 8 << 30) / q->slot_bytes));
+        }
+        q->smem_grid = std::min<int64_t>(grid, std::max<int64_t>(NS, 1));
+        slots = 0;  // no per-slot node arrays of the general sweep
         q->num_slots = 0;
     }
     const int64_t TSW = q->total_span_windows;
@@ -980,6 +969,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up(ts->v.num_nodes * 4, 256);                             // node_mask
         bytes += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);          // site_val
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
+        bytes += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);    // node state
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -987,19 +977,270 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     return 0;
 }
 
+// trees.c:1289-1313
+static int check_time_windows(uint64_t TW, const double *tw)
+{
+    if (TW < 1) {
+        return TSG_ERR_BAD_TIME_WINDOWS_DIM;
+    }
+    if (tw[0] != 0.0) {
+        return TSG_ERR_BAD_TIME_WINDOWS;
+    }
+    for (uint64_t j = 0; j < TW; j++) {
+        if (tw[j] >= tw[j + 1]) {
+            return TSG_ERR_BAD_TIME_WINDOWS;
+        }
+    }
+    return 0;
+}
+
+// Workspace layout of an allele frequency spectrum query.
+struct AfsLayout {
+    int64_t node_mask, mcnt, state, acc, err, total;
+};
+
+static AfsLayout afs_layout(const tsg_query_t *q)
+{
+    const TSView &v = q->ts->v;
+    AfsLayout l;
+    int64_t off = 0;
+    l.node_mask = off;
+    off += align_up(v.num_nodes * 4, 256);
+    l.mcnt = off;
+    off += align_up(q->p.site ? v.num_mutations * 8 * q->KQ : 0, 256);
+    l.state = off;
+    off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
+    l.acc = off;
+    off += align_up(q->p.branch ? q->afs_bins * TSG_FX_LIMBS * 8 : 0, 256);
+    l.err = off;
+    off += 256;
+    l.total = off;
+    return l;
+}
+
+// Validate an allele frequency spectrum query (the checks and their order
+// of c/tskit/trees.c:3830-3900) and build its host image.
+static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t Wn, const double *windows,
+    uint64_t TW, const double *time_windows, uint32_t options)
+{
+    *out = nullptr;
+    int ret;
+    if (options & TSG_STAT_NODE) {
+        return TSG_ERR_UNSUPPORTED_STAT_MODE;
+    }
+    bool site = options & TSG_STAT_SITE, branch = options & TSG_STAT_BRANCH;
+    if (!site && !branch) {
+        site = true;
+    }
+    if (site && branch) {
+        return TSG_ERR_MULTIPLE_STAT_MODES;
+    }
+    double default_windows[2] = { 0, ts->v.sequence_length };
+    if (windows == nullptr) {
+        Wn = 1;
+        windows = default_windows;
+    } else if ((ret = check_windows(ts, Wn, windows)) != 0) {
+        return ret;
+    }
+    double default_tw[2] = { 0, INFINITY };
+    if (time_windows == nullptr) {
+        TW = 1;
+        time_windows = default_tw;
+    } else {
+        if ((ret = check_time_windows(TW, time_windows)) != 0) {
+            return ret;
+        }
+        if (site && !(time_windows[0] == 0.0 && std::isinf((float) time_windows[1]))) {
+            return TSG_ERR_UNSUPPORTED_STAT_MODE;
+        }
+    }
+    std::vector<uint32_t> mask;
+    if ((ret = check_sample_sets(ts, K, sizes, sets, mask)) != 0) {
+        return ret;
+    }
+    if (K > TSG_AFS_KMAX) {
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    // the last count field: every sample of the tree sequence
+    for (auto &m : mask) {
+        m |= 1u << K;
+    }
+    const int64_t n = ts->v.num_samples;
+    int64_t afs_size = 1;
+    for (uint64_t k = 0; k < K; k++) {
+        if (afs_size > ((int64_t) 1 << 40) / (int64_t) (sizes[k] + 1)) {
+            return TSG_ERR_NO_MEMORY;
+        }
+        afs_size *= (int64_t) (sizes[k] + 1);
+    }
+    const int64_t bins = (int64_t) Wn * (int64_t) TW * afs_size;
+
+    tsg_query_t *q = new tsg_query_t();
+    std::memset(&q->p, 0, sizeof(q->p));
+    std::memset(&q->afs, 0, sizeof(q->afs));
+    q->kind = TSG_KIND_AFS;
+    q->dbuf = nullptr;
+    q->ev_start = nullptr;
+    q->ev_stop = nullptr;
+    q->ts = ts;
+    q->options = options;
+    q->span_normalise = !!(options & TSG_STAT_SPAN_NORMALISE);
+    q->total_span_windows = 0;
+    q->num_slots = 0;
+    q->afs_bins = bins;
+    QueryParams &p = q->p;
+    const int KC = (int) K + 1;
+    p.K = KC;  // count fields of the replay
+    p.Wn = (int32_t) Wn;
+    p.branch = branch;
+    p.site = site;
+    p.polarised = !!(options & TSG_STAT_POLARISED);
+    AfsParams &a = q->afs;
+    a.K = (int32_t) K;
+    a.Wn = (int32_t) Wn;
+    a.TW = (int32_t) TW;
+    a.polarised = p.polarised;
+    a.num_samples = n;
+    a.afs_size = afs_size;
+    {
+        int64_t stride = 1;
+        for (int k = (int) K - 1; k >= 0; k--) {
+            a.dims[k] = (int64_t) sizes[k] + 1;
+            a.stride[k] = stride;
+            stride *= a.dims[k];
+        }
+    }
+
+    // node state form: shared memory (16-bit counts) or global memory
+    // (32-bit counts, up to 3 sets); the branch replay adds a last-touch
+    // position per node
+    const int64_t L = std::max<int64_t>(ts->v.max_local, 1);
+    q->W = 16;
+    q->KQ = (KC + 3) / 4;
+    q->smem_bytes = align_up(span_state_bytes(L, 16, q->KQ), 8) + (branch ? L * 8 : 0);
+    q->smem_bytes = align_up(q->smem_bytes, 16);
+    q->gstate = false;
+    q->smem = true;
+    q->slot_bytes = 0;
+    if (!(n <= 65535 && ts->v.max_local <= 65534 && q->smem_bytes <= smem_budget())) {
+        if (KC > 4 || ts->v.max_local >= INT32_MAX) {
+            delete q;
+            return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+        }
+        q->gstate = true;
+        q->W = 32;
+        q->KQ = KC <= 2 ? 1 : 2;
+        q->smem_bytes = 0;
+        q->slot_bytes = align_up(align_up(span_state_bytes(L, 32, q->KQ), 8) + (branch ? L * 8 : 0), 256);
+    }
+    if (ts->max_children >= 65535) {
+        delete q;
+        return TSG_ERR_BAD_TREE_SEQUENCE;
+    }
+    if (branch && ts->v.num_items + ts->v.num_edges >= ((int64_t) 1 << 31)) {
+        // each bin's limb counters take at most 2^31 adds
+        delete q;
+        return TSG_ERR_NO_MEMORY;
+    }
+    const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+    {
+        void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ);
+        if (!q->gstate) {
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+        }
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
+        cudaGetLastError();
+        int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
+        if (q->gstate) {
+            grid = std::min<int64_t>(grid, std::max<int64_t>(1, ((int64_t) 8 << 30) / q->slot_bytes));
+        }
+        q->smem_grid = std::min<int64_t>(grid, std::max<int64_t>(ts->v.num_spans, 1));
+    }
+
+    // per-query arrays: sample masks, windows, time windows
+    int64_t off_mask = 0;
+    int64_t off_win = align_up(off_mask + std::max<int64_t>(n, 1) * 4, 256);
+    int64_t off_tw = align_up(off_win + ((int64_t) Wn + 1) * 8, 256);
+    int64_t total = align_up(off_tw + ((int64_t) TW + 1) * 8, 256);
+    q->blob.assign((size_t) total, 0);
+    char *h = q->blob.data();
+    std::memcpy(h + off_mask, mask.data(), (size_t) n * 4);
+    std::memcpy(h + off_win, windows, ((size_t) Wn + 1) * 8);
+    std::memcpy(h + off_tw, time_windows, ((size_t) TW + 1) * 8);
+    for (int j = 0; j < 8; j++) {
+        q->off[j] = off_win;  // unused span tables point at valid memory
+    }
+    q->off[0] = off_mask;
+    q->off[1] = off_win;
+    q->off[7] = off_tw;
+    q->ws_bytes = afs_layout(q).total;
+    *out = q;
+    return 0;
+}
+
+static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result, cudaStream_t st)
+{
+    const tsg_treeseq_t *ts = q->ts;
+    const AfsLayout l = afs_layout(q);
+    char *b = (char *) ws->ptr;
+    WsDev w;
+    std::memset(&w, 0, sizeof(w));
+    w.node_mask = (uint32_t *) (b + l.node_mask);
+    w.mcnt = (uint64_t *) (b + l.mcnt);
+    w.state = b + l.state;
+    w.err = (int32_t *) (b + l.err);
+    w.counter = w.err + 1;
+    AfsParams a = q->afs;
+    a.acc = (unsigned long long *) (b + l.acc);
+    a.out = result;
+    a.err = w.err;
+    a.counter = w.counter;
+    QueryDev d = q->d;
+    d.node_mask = w.node_mask;
+    const QueryParams &p = q->p;
+    const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+    int ret;
+    TSG_CUDA(cudaMemsetAsync(w.err, 0, 2 * sizeof(int32_t), st));
+    if (q->ev_start != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_start, st));
+    }
+    k_node_mask<<<grid_for(ts->v.num_nodes), 256, 0, st>>>(ts->v, d, w.node_mask);
+    TSG_LAUNCHED();
+    const unsigned g = (unsigned) q->smem_grid;
+    if (p.site) {
+        TSG_CUDA(cudaMemsetAsync(result, 0, (size_t) q->afs_bins * 8, st));
+        const size_t sb = (size_t) q->smem_bytes;
+        switch (form) {
+            case 0: k_replay_items<16, 1, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 1: k_replay_items<16, 2, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 2: k_replay_items<32, 1, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+            default: k_replay_items<32, 2, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+        }
+        TSG_LAUNCHED();
+        if ((ret = launch_afs_site(form, st, ts->v, a, w.mcnt)) != 0) {
+            return ret;
+        }
+    } else {
+        TSG_CUDA(cudaMemsetAsync(a.acc, 0, (size_t) q->afs_bins * TSG_FX_LIMBS * 8, st));
+        if ((ret = launch_afs_branch(form, g, (size_t) q->smem_bytes, q->slot_bytes, w.state, st,
+                 ts->v, d, a)) != 0) {
+            return ret;
+        }
+    }
+    if (q->ev_stop != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_stop, st));
+    }
+    return launch_afs_finish(st, a, q->span_normalise, p.branch, result);
+}
+
 }  // namespace tsg
 
 extern "C" {
 
-int tsg_query_create(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
-    const uint64_t *sizes, const int32_t *sets, uint64_t R, const tsg_output_t *outputs,
-    uint64_t Wn, const double *windows, uint32_t options)
+static int query_upload(tsg_query_t *q, tsg_query_t **out)
 {
-    tsg_query_t *q = nullptr;
-    int ret = query_build(&q, ts, K, sizes, sets, R, outputs, Wn, windows, options);
-    if (ret != 0) {
-        return ret;
-    }
     if (cudaMalloc(&q->dbuf, q->blob.size()) != cudaSuccess) {
         cudaGetLastError();
         delete q;
@@ -1013,6 +1254,30 @@ int tsg_query_create(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     query_bind(q, q->dbuf);
     *out = q;
     return 0;
+}
+
+int tsg_query_create(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t R, const tsg_output_t *outputs,
+    uint64_t Wn, const double *windows, uint32_t options)
+{
+    tsg_query_t *q = nullptr;
+    int ret = query_build(&q, ts, K, sizes, sets, R, outputs, Wn, windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return query_upload(q, out);
+}
+
+int tsg_query_create_afs(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t Wn, const double *windows, uint64_t TW,
+    const double *time_windows, uint32_t options)
+{
+    tsg_query_t *q = nullptr;
+    int ret = afs_build(&q, ts, K, sizes, sets, Wn, windows, TW, time_windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return query_upload(q, out);
 }
 
 int tsg_query_set_sweep_events(tsg_query_t *q, void *start_event, void *stop_event)
@@ -1066,6 +1331,9 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         return TSG_ERR_WORKSPACE_TOO_SMALL;
     }
     cudaStream_t st = (cudaStream_t) cuda_stream;
+    if (q->kind == TSG_KIND_AFS) {
+        return afs_launch(q, ws, result, st);
+    }
     const tsg_treeseq_t *ts = q->ts;
     const QueryParams &p = q->p;
     const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans, TSW = q->total_span_windows;
@@ -1094,6 +1362,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     w.rs0 = (double *) (b + off);
     off += align_up(R * 8, 256);
     w.items = nullptr;
+    w.state = nullptr;
     w.mcnt = nullptr;
     w.dD = nullptr;
     w.node_mask = nullptr;
@@ -1113,6 +1382,8 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         off += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);
         w.site_win = (double *) (b + off);
         off += align_up((int64_t) p.Wn * R * 8, 256);
+        w.state = b + off;
+        off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
@@ -1130,24 +1401,20 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         TSG_LAUNCHED();
         const unsigned g = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
-        if (q->KQ == 1) {
-            k_replay_items<1><<<g, 512, sb, st>>>(ts->v, p, d, w);
-        } else {
-            k_replay_items<2><<<g, 512, sb, st>>>(ts->v, p, d, w);
+        const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+        switch (form) {
+            case 0: k_replay_items<16, 1, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 1: k_replay_items<16, 2, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 2: k_replay_items<32, 1, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+            default: k_replay_items<32, 2, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
         }
         TSG_LAUNCHED();
         if (p.branch) {
             const unsigned ge = (unsigned) ((ts->v.num_chunks + 7) / 8);
-            const int sel = (p.f32 ? 4 : 0) + (p.polarised ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
-            switch (sel) {
-                case 0: k_eval_items<double, false, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 1: k_eval_items<double, false, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 2: k_eval_items<double, true, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 3: k_eval_items<double, true, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 4: k_eval_items<float, false, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 5: k_eval_items<float, false, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                case 6: k_eval_items<float, true, TSG_ITEM_RMAX, 1><<<ge, 256, 0, st>>>(ts->v, p, w); break;
-                default: k_eval_items<float, true, TSG_ITEM_RMAX, 2><<<ge, 256, 0, st>>>(ts->v, p, w); break;
+            if (p.f32) {
+                (p.polarised ? launch_eval_f32_pol : launch_eval_f32_unpol)(form, ge, st, ts->v, p, w);
+            } else {
+                (p.polarised ? launch_eval_f64_pol : launch_eval_f64_unpol)(form, ge, st, ts->v, p, w);
             }
             TSG_LAUNCHED();
             k_span_windows<<<(unsigned) ((ts->v.num_spans + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
@@ -1155,10 +1422,11 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         }
         if (p.site && ts->v.num_sites > 0) {
             const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
-            if (q->KQ == 1) {
-                k_site_eval<TSG_ITEM_RMAX, 1><<<gsite, 256, 0, st>>>(ts->v, p, w);
-            } else {
-                k_site_eval<TSG_ITEM_RMAX, 2><<<gsite, 256, 0, st>>>(ts->v, p, w);
+            switch (form) {
+                case 0: k_site_eval<TSG_ITEM_RMAX, 16, 1><<<gsite, 256, 0, st>>>(ts->v, p, w); break;
+                case 1: k_site_eval<TSG_ITEM_RMAX, 16, 2><<<gsite, 256, 0, st>>>(ts->v, p, w); break;
+                case 2: k_site_eval<TSG_ITEM_RMAX, 32, 1><<<gsite, 256, 0, st>>>(ts->v, p, w); break;
+                default: k_site_eval<TSG_ITEM_RMAX, 32, 2><<<gsite, 256, 0, st>>>(ts->v, p, w); break;
             }
             TSG_LAUNCHED();
         }
@@ -1207,19 +1475,10 @@ int tsg_workspace_check(const tsg_workspace_t *ws, const tsg_query_t *q)
 // ----------------------------------------------------------- host entry points
 namespace tsg {
 
-// The synchronous entry points reuse the tree sequence's own workspace and
-// staging buffer (grown on demand, serialised by a mutex), so a call makes no
-// device allocation once they are large enough.
-static int run_sync(const tsg_treeseq_t *cts, uint64_t K, const uint64_t *sizes,
-    const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
-    const double *windows, uint32_t options, double *result)
+static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *result)
 {
     tsg_treeseq_t *ts = const_cast<tsg_treeseq_t *>(cts);
-    tsg_query_t *q = nullptr;
-    int ret = query_build(&q, ts, K, sizes, sets, R, outs, Wn, windows, options);
-    if (ret != 0) {
-        return ret;
-    }
+    int ret;
     std::lock_guard<std::mutex> lock(ts->sync_mutex);
     const int64_t nres = tsg_query_result_size(q);
     const int64_t blob = align_up((int64_t) q->blob.size(), 256);
@@ -1261,6 +1520,21 @@ static int run_sync(const tsg_treeseq_t *cts, uint64_t K, const uint64_t *sizes,
     }
     tsg_query_free(q);
     return ret;
+}
+
+// The synchronous entry points reuse the tree sequence's own workspace and
+// staging buffer (grown on demand, serialised by a mutex), so a call makes no
+// device allocation once they are large enough.
+static int run_sync(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
+    const double *windows, uint32_t options, double *result)
+{
+    tsg_query_t *q = nullptr;
+    int ret = query_build(&q, ts, K, sizes, sets, R, outs, Wn, windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return run_sync_query(ts, q, result);
 }
 
 static int one_way(const tsg_treeseq_t *ts, int32_t type, uint64_t K, const uint64_t *sizes,
@@ -1312,6 +1586,18 @@ int tsg_treeseq_sample_count_stat(const tsg_treeseq_t *self, uint64_t K, const u
     const double *windows, uint32_t options, double *result)
 {
     return run_sync(self, K, sizes, sets, R, outputs, Wn, windows, options, result);
+}
+
+int tsg_treeseq_allele_frequency_spectrum(const tsg_treeseq_t *self, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t Wn, const double *windows, uint64_t TW,
+    const double *time_windows, uint32_t options, double *result)
+{
+    tsg_query_t *q = nullptr;
+    int ret = afs_build(&q, self, K, sizes, sets, Wn, windows, TW, time_windows, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return run_sync_query(self, q, result);
 }
 
 int tsg_treeseq_diversity(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,

@@ -1,39 +1,57 @@
-// Summary terms on packed counts, and the shared-memory span state
+// Summary terms on packed counts, and the per-span node state
 // (included by tsg_stats.cu after its definitions).
 //
-// A span's stateful nodes live in shared memory: time (f64), per-set sample
-// counts (16-bit fields packed into 64-bit words) and parent (16-bit local
-// id).  Leaves are never stored: their counts are their own sample-set
-// memberships.  Summary terms use precomputed reciprocal denominators (no
-// divisions) and read counts with register shifts (no indexed arrays).
+// A span's stateful nodes carry: time (f64), per-set sample counts packed as
+// W-bit fields in two 64-bit words (W = 16: up to 8 sets, W = 32: up to 4),
+// a seek counter word and a parent local id.  The state lives in shared
+// memory (W = 16, 16-bit ids) when it fits, else in a per-CTA slice of global
+// memory (W = 32, 32-bit ids).  Leaves are never stored: their counts are
+// their own sample-set memberships.  Summary terms use precomputed
+// reciprocal denominators (no divisions) and read counts with register
+// shifts (no indexed arrays).
 
-#define TSG_NO_PARENT 0xFFFFu
-#define TSG_SMEM_KMAX 8
+#pragma once
 
-// Per-node sample-set counts packed as 16-bit fields: sets 0-3 in lo, 4-7 in
-// hi.  Counts stay in [0, set size] through every update, so packed adds and
+#include "tsg_query.cuh"
+
+namespace tsg {
+
+#define TSG_KMAX 8
+
+// Counts stay in [0, set size] through every update, so packed adds and
 // subtracts never carry between fields.
 struct Pack {
     uint64_t lo, hi;
 };
 
+template <int W>
 __device__ __forceinline__ uint32_t pk_get(const Pack &p, int k)
 {
-    const uint64_t w = k < 4 ? p.lo : p.hi;
-    return (uint32_t) ((w >> (16 * (k & 3))) & 0xFFFFull);
+    constexpr int FPW = 64 / W;
+    const uint64_t w = k < FPW ? p.lo : p.hi;
+    return (uint32_t) ((w >> (W * (k % FPW))) & ((1ull << W) - 1ull));
 }
 
+template <int W>
+__device__ __forceinline__ void pk_set(Pack &p, int k, uint64_t v)
+{
+    constexpr int FPW = 64 / W;
+    if (k < FPW) {
+        p.lo |= v << (W * k);
+    } else {
+        p.hi |= v << (W * (k - FPW));
+    }
+}
+
+template <int W>
 __device__ __forceinline__ Pack pk_from_mask(uint32_t m, int K)
 {
+    constexpr int KM = 2 * (64 / W);
     Pack p{0, 0};
 #pragma unroll
-    for (int k = 0; k < TSG_SMEM_KMAX; k++) {
+    for (int k = 0; k < KM; k++) {
         if (k < K && ((m >> k) & 1u)) {
-            if (k < 4) {
-                p.lo |= 1ull << (16 * k);
-            } else {
-                p.hi |= 1ull << (16 * (k - 4));
-            }
+            pk_set<W>(p, k, 1ull);
         }
     }
     return p;
@@ -74,16 +92,17 @@ __device__ __forceinline__ F term_inv(int type, F xi, F xj, F xk, F xl, F ni, F 
 
 // Means over the sets of x_k / n_k and of (n_k - x_k) / n_k (centred
 // relatedness only).
-template <typename F>
+template <typename F, int W>
 __device__ __forceinline__ void pk_means(const QueryParams &q, const Pack &P, F &mx, F &mc)
 {
+    constexpr int KM = 2 * (64 / W);
     mx = 0;
     mc = 0;
     if (q.need_mean) {
 #pragma unroll
-        for (int k = 0; k < TSG_SMEM_KMAX; k++) {
+        for (int k = 0; k < KM; k++) {
             if (k < q.K) {
-                const F x = (F) pk_get(P, k), n = (F) q.set_size[k], r = (F) q.inv_size[k];
+                const F x = (F) pk_get<W>(P, k), n = (F) q.set_size[k], r = (F) q.inv_size[k];
                 mx += x * r;
                 mc += (n - x) * r;
             }
@@ -94,15 +113,15 @@ __device__ __forceinline__ void pk_means(const QueryParams &q, const Pack &P, F 
 }
 
 // F_r(x): f_r(x), plus f_r(n - x) when unpolarised (c/tskit/trees.c:1944-1972).
-template <typename F, bool UNPOL>
+template <typename F, bool UNPOL, int W>
 __device__ __forceinline__ F term_F(const QueryParams &q, int r, const Pack &P, F mx, F mc)
 {
     const Term &t = q.term[r];
     const F ni = (F) q.set_size[t.idx[0]], nj = (F) q.set_size[t.idx[1]];
     const F nk = (F) q.set_size[t.idx[2]], nl = (F) q.set_size[t.idx[3]];
     const F ri = (F) q.inv_size[t.idx[0]], rj = (F) q.inv_size[t.idx[1]];
-    const F xi = (F) pk_get(P, t.idx[0]), xj = (F) pk_get(P, t.idx[1]);
-    const F xk = (F) pk_get(P, t.idx[2]), xl = (F) pk_get(P, t.idx[3]);
+    const F xi = (F) pk_get<W>(P, t.idx[0]), xj = (F) pk_get<W>(P, t.idx[1]);
+    const F xk = (F) pk_get<W>(P, t.idx[2]), xl = (F) pk_get<W>(P, t.idx[3]);
     const F inv = (F) q.inv[r];
     F v = term_inv<F>(t.type, xi, xj, xk, xl, ni, nj, nk, nl, inv, ri, rj, mx);
     if (UNPOL) {
@@ -111,15 +130,20 @@ __device__ __forceinline__ F term_F(const QueryParams &q, int r, const Pack &P, 
     return v;
 }
 
-struct SmemSpan {
+// Node state of one span.  IdxT: 16-bit ids in shared memory, 32-bit ids in
+// global memory; the all-ones id means "no parent".
+template <typename IdxT>
+struct SpanState {
     double *time;
     uint64_t *xq;   // KQ words per node
     uint32_t *cnt;  // seek counters: children (low 16 bits), arrivals (high 16 bits)
-    uint16_t *par;
+    IdxT *par;
     int KQ;
+    static constexpr uint32_t NONE = (uint32_t) (IdxT) ~(IdxT) 0;
 };
 
-__device__ __forceinline__ Pack pk_load(const SmemSpan &sp, int32_t l)
+template <typename IdxT>
+__device__ __forceinline__ Pack pk_load(const SpanState<IdxT> &sp, int64_t l)
 {
     Pack p;
     p.lo = sp.xq[l * sp.KQ];
@@ -127,7 +151,8 @@ __device__ __forceinline__ Pack pk_load(const SmemSpan &sp, int32_t l)
     return p;
 }
 
-__device__ __forceinline__ void pk_store(const SmemSpan &sp, int32_t l, const Pack &p)
+template <typename IdxT>
+__device__ __forceinline__ void pk_store(const SpanState<IdxT> &sp, int64_t l, const Pack &p)
 {
     sp.xq[l * sp.KQ] = p.lo;
     if (sp.KQ > 1) {
@@ -135,24 +160,15 @@ __device__ __forceinline__ void pk_store(const SmemSpan &sp, int32_t l, const Pa
     }
 }
 
-__device__ __forceinline__ uint32_t leaf_mask(const TSView &ts, const QueryDev &qd, int32_t g)
-{
-    (void) ts;
-    return qd.node_mask[g];
-}
-
 // counts of an encoded node (local stateful id >= 0, or -(global + 1))
-__device__ __forceinline__ Pack load_counts(const SmemSpan &sp, const TSView &ts,
-    const QueryDev &qd, int32_t enc, int K)
+template <int W, typename IdxT>
+__device__ __forceinline__ Pack load_counts(const SpanState<IdxT> &sp, const QueryDev &qd,
+    int32_t enc, int K)
 {
     if (enc >= 0) {
         return pk_load(sp, enc);
     }
-    return pk_from_mask(leaf_mask(ts, qd, -enc - 1), K);
+    return pk_from_mask<W>(qd.node_mask[-enc - 1], K);
 }
 
-__device__ __forceinline__ double node_time_enc(const SmemSpan &sp, const TSView &ts, int32_t enc)
-{
-    return enc >= 0 ? sp.time[enc] : ts.node_time[-enc - 1];
-}
-
+}  // namespace tsg

@@ -668,6 +668,7 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         ts->v.tree_sites = tree_sites;
         ts->v.site_mut = site_mut;
         ts->v.ins_parent = ins_parent;
+        ts->v.ins_left = ins_left;
         ts->v.ins_child = ins_child;
         ts->v.rem_parent = rem_parent;
         ts->v.rem_child = rem_child;
@@ -690,6 +691,7 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
             || (ret = d2h(h.parent, t.parent, E)) || (ret = d2h(h.child, t.child, E))
             || (ret = d2h(h.ins_parent, ins_parent, E)) || (ret = d2h(h.ins_child, ins_child, E))
             || (ret = d2h(h.rem_parent, rem_parent, E)) || (ret = d2h(h.rem_child, rem_child, E))
+            || (ret = d2h(h.ins_edge, t.I, E))
             || (ret = d2h(h.tree_in, tree_in, T + 1)) || (ret = d2h(h.tree_out, tree_out, T + 1))
             || (ret = d2h(h.tree_sites, tree_sites, T + 1))
             || (ret = d2h(h.site_mut, site_mut, S + 1)) || (ret = d2h(h.mut_node, t.mut_node, M))) {
@@ -698,9 +700,16 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         if (num_spans <= 0) {
             // default: about two spans per SM plus one per 2,000 edge events;
             // a span's seek touches about two nodes per sample, its replay about
-            // a dozen per event, and its node state must fit in shared memory
+            // a dozen per event, and its node state must fit in shared memory.
+            // Large trees (node state in global memory) cap the seek work: all
+            // spans' alive edges at most 16 times the edge count.
             const int64_t sms = std::max(device_count_sms(), 1);
-            num_spans = std::min<int64_t>(T, std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms));
+            num_spans = std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms);
+            const int64_t alive0 = T > 0 ? (int64_t) (h.tree_in[1] - h.tree_in[0]) : 0;
+            if (alive0 > 30000) {
+                num_spans = std::min(num_spans, std::max<int64_t>(4 * sms, 16 * E / alive0));
+            }
+            num_spans = std::min<int64_t>(T, num_spans);
         }
         if ((ret = build_span_plan(ts, h, num_spans)) != 0) {
             goto fail;

@@ -13,6 +13,7 @@ sweep whose summary terms are the same functions.
 from __future__ import annotations
 
 import ctypes
+import math
 import numbers
 
 import numpy as np
@@ -274,6 +275,12 @@ class TreeSequence:
                 )
         return np.array(windows)
 
+    def parse_time_windows(self, time_windows):
+        """python/tskit/trees.py:8133-8136."""
+        if time_windows is None:
+            time_windows = [0.0, math.inf]
+        return np.array(time_windows)
+
     # --------------------------------------------------- low-level layer
     def _ll_terms(self, terms, sample_set_sizes, sample_sets, windows, mode, span_normalise,
                   polarised, extra=0):
@@ -307,6 +314,32 @@ class TreeSequence:
         ))
         return res if nmodes == 2 else res[0]
 
+    def _ll_allele_frequency_spectrum(self, sample_set_sizes, sample_sets, windows,
+                                      time_windows, mode=None, span_normalise=True,
+                                      polarised=False):
+        """Low-level call (python/_tskitmodule.c:6977-7062): result shape
+        (num_windows, num_time_windows, *(1 + sample_set_sizes))."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        sizes = np.ascontiguousarray(sample_set_sizes, dtype=np.uint64)
+        flat = np.ascontiguousarray(sample_sets, dtype=np.int32)
+        if np.sum(sizes) != len(flat):
+            raise ValueError("Sum of sample_set_sizes must equal length of sample_sets array")
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        tw = np.ascontiguousarray(time_windows, dtype=np.float64)
+        for a in (win, tw):
+            if a.ndim != 1 or len(a) < 2:
+                raise ValueError("Windows arrays must have at least 2 elements")
+        shape = (len(win) - 1, len(tw) - 1) + tuple(int(n) + 1 for n in sizes)
+        res = np.zeros(shape)
+        nat.check(self._lib.tsg_treeseq_allele_frequency_spectrum(
+            self._handle, len(sizes), _ptr(sizes), _ptr(flat), len(win) - 1, _ptr(win),
+            len(tw) - 1, _ptr(tw), flags, _ptr(res)))
+        return res
+
     def _ll_one_way(self, typ):
         def method(sample_set_sizes, sample_sets, windows, mode=None, span_normalise=True,
                    polarised=False):
@@ -337,8 +370,23 @@ class TreeSequence:
             stat = stat[0]
         return stat
 
+    def __run_windowed_stat_tw(self, windows, time_windows, method, *args, **kwargs):
+        strip_win = windows is None
+        strip_timewin = time_windows is None
+        windows = self.parse_windows(windows)
+        time_windows = self.parse_time_windows(time_windows)
+        stat = method(*args, **kwargs, windows=windows, time_windows=time_windows)
+        if strip_win and strip_timewin:
+            stat = stat[0, 0, :]
+        elif strip_win:
+            stat = stat[0, :, :]
+        elif strip_timewin:
+            stat = stat[:, 0, :]
+        return stat
+
     def __one_way_sample_set_stat(self, ll_method, sample_sets, windows=None, mode=None,
-                                  span_normalise=True, polarised=False):
+                                  span_normalise=True, polarised=False, time_windows=None,
+                                  use_tw=False):
         if sample_sets is None:
             sample_sets = self.samples()
         drop_dimension = False
@@ -354,12 +402,18 @@ class TreeSequence:
         if np.any(sample_set_sizes == 0):
             raise ValueError("Sample sets must contain at least one element")
         flattened = safe_np_int_cast(np.hstack(sample_sets), np.int32)
-        stat = self.__run_windowed_stat(windows, ll_method, sample_set_sizes, flattened,
-                                        mode=mode, span_normalise=span_normalise,
-                                        polarised=polarised)
+        if use_tw:
+            stat = self.__run_windowed_stat_tw(windows, time_windows, ll_method,
+                                               sample_set_sizes, flattened, mode=mode,
+                                               span_normalise=span_normalise,
+                                               polarised=polarised)
+        else:
+            stat = self.__run_windowed_stat(windows, ll_method, sample_set_sizes, flattened,
+                                            mode=mode, span_normalise=span_normalise,
+                                            polarised=polarised)
         if drop_dimension:
             stat = stat.reshape(stat.shape[:-1])
-            if stat.shape == () and windows is None:
+            if stat.shape == () and windows is None and time_windows is None:
                 stat = stat[()]
         return stat
 
@@ -396,6 +450,25 @@ class TreeSequence:
         return stat
 
     # ------------------------------------------------------------ one-way
+    def allele_frequency_spectrum(self, sample_sets=None, windows=None, time_windows=None,
+                                  mode="site", span_normalise=True, polarised=False):
+        """python/tskit/trees.py:9844-9965: the joint allele frequency spectrum
+        of the sample sets, shape (windows, time windows, *(1 + set sizes)),
+        window dimensions dropped when not given."""
+        if sample_sets is None:
+            sample_sets = [self.samples()]
+        try:
+            sample_sets = np.array(sample_sets, dtype=np.uint64)
+        except ValueError:
+            pass
+        else:
+            if len(sample_sets.shape) == 1:
+                sample_sets = [sample_sets]
+        return self.__one_way_sample_set_stat(
+            self._ll_allele_frequency_spectrum, sample_sets, windows=windows,
+            time_windows=time_windows, mode=mode, span_normalise=span_normalise,
+            polarised=polarised, use_tw=True)
+
     def diversity(self, sample_sets=None, windows=None, mode="site", span_normalise=True):
         """Mean pairwise diversity (python/tskit/trees.py:8496-8556)."""
         return self.__one_way_sample_set_stat(self._ll_one_way(nat.DIVERSITY), sample_sets,
@@ -537,13 +610,17 @@ class TreeSequence:
               polarised=False, both_modes=False, precision="f64", sweep="auto"):
         """Prepare a device-resident fused query (see :class:`Query`).
 
-        ``sweep="global"`` forces the global-memory sweep even where a span's
-        node state fits in shared memory."""
+        ``sweep`` picks the kernels for testing: ``"global"`` forces the
+        general sweep, ``"global_state"`` the item pipeline with its span node
+        state in global memory (32-bit counts), where "auto" would choose
+        shared memory."""
         flags = 0
         if sweep == "global":
             flags |= nat.FORCE_GLOBAL_SWEEP
+        elif sweep == "global_state":
+            flags |= nat.FORCE_GLOBAL_STATE
         elif sweep != "auto":
-            raise ValueError("sweep must be 'auto' or 'global'")
+            raise ValueError("sweep must be 'auto', 'global' or 'global_state'")
         if both_modes:
             flags |= nat.STAT_BOTH_MODES
         else:
