@@ -36,8 +36,16 @@ namespace tsg {
 
 // The reference's fold (trees.c:3469-3497) in integers: with every count
 // doubled the half-integer comparisons become exact integer ones.
+// Returns -1 when a count lies outside [0, n_k] (an inconsistent tree
+// sequence), so that no access goes outside the result.
 __device__ __forceinline__ int64_t afs_bin(const AfsParams &a, int64_t *c)
 {
+#pragma unroll
+    for (int k = 0; k < TSG_AFS_KMAX; k++) {
+        if (k < a.K && (c[k] < 0 || c[k] >= a.dims[k])) {
+            return -1;
+        }
+    }
     if (!a.polarised) {
         int64_t n2 = 0, s2 = 0;
 #pragma unroll
@@ -187,6 +195,10 @@ __device__ void afs_record(const AfsParams &a, const Pack &x, double tu, double 
         c[k] = k < a.K ? (int64_t) pk_get<W>(x, k) : 0;
     }
     const int64_t bin = afs_bin(a, c);
+    if (bin < 0) {
+        dev_error(a.err, DEV_NODE_OUT_OF_BOUNDS);
+        return;
+    }
     for (int w = afs_window(a, xs); w < a.Wn && a.windows[w] < xe; w++) {
         const double lo = xs > a.windows[w] ? xs : a.windows[w];
         const double hi = xe < a.windows[w + 1] ? xe : a.windows[w + 1];
@@ -431,7 +443,11 @@ __global__ void __launch_bounds__(256) k_afs_site(TSView ts, AfsParams a, const 
         }
         if (all > 0 && all < a.num_samples) {
             const int64_t bin = afs_bin(a, c);
-            atomicAdd(a.out + (int64_t) w * a.afs_size + bin, inc);
+            if (bin < 0) {
+                dev_error(a.err, DEV_NODE_OUT_OF_BOUNDS);
+            } else {
+                atomicAdd(a.out + (int64_t) w * a.afs_size + bin, inc);
+            }
         }
     }
 }

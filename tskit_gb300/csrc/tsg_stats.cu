@@ -941,7 +941,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         int per_sm = 0;
         void *fn = replay_kernel(q->W, q->KQ);
         if (!q->gstate) {
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+            // a cap, not a reservation: every query of every tree sequence fits
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget());
         }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
         int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
@@ -1147,7 +1148,8 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     {
         void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ);
         if (!q->gstate) {
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) q->smem_bytes);
+            // a cap, not a reservation: every query of every tree sequence fits
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget());
         }
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
