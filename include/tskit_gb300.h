@@ -207,6 +207,17 @@ int tsg_treeseq_allele_frequency_spectrum(const tsg_treeseq_t *self,
     uint64_t num_windows, const double *windows, uint64_t num_time_windows,
     const double *time_windows, uint32_t options, double *result);
 
+/* ------------------------------------------ genetic relatedness x vectors
+ * Replaces tsk_treeseq_genetic_relatedness_vector (c/tskit/trees.c:
+ * 10782-10816): branch mode only (site and node modes return
+ * TSG_ERR_UNSUPPORTED_STAT_MODE, as the reference does).  weights:
+ * num_samples x num_weights (row-major); result: num_windows x num_focal x
+ * num_weights.  Options: TSG_STAT_SPAN_NORMALISE, TSG_STAT_NONCENTRED.
+ * windows may be NULL (whole genome); they need not cover it.  Host pointers. */
+int tsg_treeseq_genetic_relatedness_vector(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows,
+    uint64_t num_focal_nodes, const int32_t *focal_nodes, double *result, uint32_t options);
+
 /* ------------------------------------------------------ fused sample-count
  * Generalises tsk_treeseq_sample_count_stat (c/tskit/trees.c:2174-2220) to a
  * list of summary terms evaluated in one sweep.  With TSG_STAT_BOTH_MODES the
@@ -241,6 +252,13 @@ int tsg_query_create_afs(tsg_query_t **query, const tsg_treeseq_t *self,
     uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
     uint64_t num_windows, const double *windows, uint64_t num_time_windows,
     const double *time_windows, uint32_t options);
+/* The relatedness-vector product as a device-resident query; its weights
+ * (device pointer, num_samples x num_weights) are set with
+ * tsg_query_set_weights before a launch and read by every later launch. */
+int tsg_query_create_relatedness_vector(tsg_query_t **query, const tsg_treeseq_t *self,
+    uint64_t num_weights, uint64_t num_windows, const double *windows,
+    uint64_t num_focal_nodes, const int32_t *focal_nodes, uint32_t options);
+int tsg_query_set_weights(tsg_query_t *query, const double *weights_device);
 int tsg_query_free(tsg_query_t *query);
 /* Device bytes the query needs in a workspace. */
 int64_t tsg_query_workspace_bytes(const tsg_query_t *query);

@@ -28,6 +28,7 @@ CUDA_SOURCES = [
     "tsg_eval_f64_pol.cu",
     "tsg_eval_f64_unpol.cu",
     "tsg_afs.cu",
+    "tsg_matvec.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

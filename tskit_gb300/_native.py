@@ -106,6 +106,11 @@ SIGNATURES = {
     "tsg_query_create": (ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_treeseq_allele_frequency_spectrum": (
         ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U64, _P, _U32, _P]),
+    "tsg_treeseq_genetic_relatedness_vector": (
+        ctypes.c_int, [_P, _U64, _P, _U64, _P, _U64, _P, _P, _U32]),
+    "tsg_query_create_relatedness_vector": (
+        ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _U64, _P, _U64, _P, _U32]),
+    "tsg_query_set_weights": (ctypes.c_int, [_P, _P]),
     "tsg_query_create_afs": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),

@@ -121,6 +121,9 @@ struct TSView {
     int64_t num_chunks;
     // the reference allele frequency spectrum's lazy branch accounting
     const uint8_t *node_is_parent;  // per node: a parent in some edge
+    const int32_t *leaf_index;    // per node: index among the leaves (never a parent), or -1
+    const int32_t *leaves;        // the leaves, by index
+    int64_t num_leaves;
     const double *ins_left;       // insertion order: edge left
     const double *ins_right;      // insertion order: edge right
     const double *ins_lu;         // insertion order: the child's last update before the

@@ -115,6 +115,14 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     for (int64_t e = 0; e < E; e++) {
         is_parent[(size_t) h.parent[(size_t) e]] = 1;
     }
+    std::vector<int32_t> leaf_index((size_t) N, -1), leaves;
+    for (int64_t u = 0; u < N; u++) {
+        if (!is_parent[(size_t) u]) {
+            leaf_index[(size_t) u] = (int32_t) leaves.size();
+            leaves.push_back((int32_t) u);
+        }
+    }
+    const int64_t num_leaves = (int64_t) leaves.size();
 
     // per-span local numbering and encodings, spans in parallel
     std::vector<int2> alive_global(alive_edge.size()), alive_enc(alive_edge.size());
@@ -382,6 +390,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         *d_tree_chunk_off;
     int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
     uint8_t *d_is_parent = nullptr;
+    int32_t *d_leaf_index = nullptr, *d_leaves = nullptr;
     double *d_ins_right = nullptr, *d_ins_lu = nullptr;
     std::vector<int32_t> span_tree_v(st.begin(), st.end());
     if ((ret = upload_vec(ts, span_tree_v, &d_span_tree)) || (ret = upload_vec(ts, alive_off, &d_alive_off))
@@ -394,11 +403,16 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         || (ret = upload_vec(ts, chunk_end, &d_chunk_end))
         || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))
         || (ret = upload_vec(ts, is_parent, &d_is_parent))
+        || (ret = upload_vec(ts, leaf_index, &d_leaf_index))
+        || (ret = upload_vec(ts, leaves, &d_leaves))
         || (ret = upload_vec(ts, ins_right, &d_ins_right))
         || (any_gap && (ret = upload_vec(ts, ins_lu, &d_ins_lu)))) {
         return ret;
     }
     ts->v.node_is_parent = d_is_parent;
+    ts->v.leaf_index = d_leaf_index;
+    ts->v.leaves = d_leaves;
+    ts->v.num_leaves = num_leaves;
     ts->v.ins_right = d_ins_right;
     ts->v.ins_lu = any_gap ? d_ins_lu : nullptr;
     ts->v.num_spans = NS;

@@ -96,6 +96,40 @@ int launch_afs_finish(cudaStream_t st, const AfsParams &a, int span_normalise, i
     double *result);
 void *afs_replay_kernel(int form);
 
+// Branch genetic relatedness matrix-vector product (one query).  Work item:
+// a group of consecutive spans x a block of 32 weight columns (one column
+// per lane), with node state in a per-CTA slot of global memory.
+#define TSG_MV_WARPS 4
+struct MvParams {
+    int32_t W;          // weight columns
+    int32_t ncb;        // blocks of 32 columns
+    int32_t Wn;         // windows
+    int32_t G;          // span groups
+    int64_t nf;         // focal nodes
+    int64_t L;          // stateful nodes per span, at most
+    int64_t slot_bytes;
+    const double *windows;     // Wn + 1
+    const int32_t *focal;      // nf
+    const int32_t *group_span; // G + 1: first span of each group
+    const int32_t *group_wlo;  // G: first window of each group (-1: none)
+    const int64_t *pair_off;   // G + 1: (group, window) partial blocks
+    const int32_t *win_glo;    // Wn: first group contributing to each window
+    const int32_t *win_ghi;    // Wn: last group contributing (win_glo > win_ghi: none)
+    const double *weights;     // n x W, as given
+    double *wc;                // n x W: weights centred over samples (or as given)
+    double *partial;           // pairs x nf x W
+    unsigned char *slots;      // grid x slot_bytes
+    int32_t *err;
+    int32_t *counter;
+    int32_t centre;
+};
+
+// Relatedness-vector launchers (tsg_matvec.cu).
+int launch_matvec(unsigned grid, cudaStream_t st, const TSView &v, const MvParams &m,
+    int span_normalise, double *result);
+int64_t matvec_slot_bytes(const TSView &v, int64_t L);
+const void *k_matvec_ptr();
+
 // term budget of the item evaluation (accumulators per lane)
 #define TSG_ITEM_RMAX 32
 

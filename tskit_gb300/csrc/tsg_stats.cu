@@ -570,13 +570,18 @@ struct tsg_query {
     int64_t smem_bytes, smem_grid, slot_bytes;
     int span_normalise;
     uint32_t options;
-    int kind;                // TSG_KIND_STATS or TSG_KIND_AFS
+    int kind;                // TSG_KIND_STATS, TSG_KIND_AFS or TSG_KIND_MATVEC
     AfsParams afs;           // allele frequency spectrum (device pointers bound at launch)
     int64_t afs_bins;        // windows x time windows x afs_size
+    MvParams mv;             // relatedness vector (device pointers bound at launch)
+    int64_t mv_grid;
+    int64_t mv_pairs;        // (group, window) partial blocks
+    const double *weights;   // relatedness vector: device weights (num_samples x W)
 };
 
 #define TSG_KIND_STATS 0
 #define TSG_KIND_AFS 1
+#define TSG_KIND_MATVEC 2
 
 namespace tsg {
 
@@ -675,6 +680,9 @@ int64_t tsg_query_result_size(const tsg_query_t *q)
     if (q->kind == TSG_KIND_AFS) {
         return q->afs_bins;
     }
+    if (q->kind == TSG_KIND_MATVEC) {
+        return (int64_t) q->mv.Wn * q->mv.nf * q->mv.W;
+    }
     return (int64_t) q->p.Wn * q->p.R * ((q->p.branch ? 1 : 0) + (q->p.site ? 1 : 0));
 }
 
@@ -696,6 +704,16 @@ static void query_bind(tsg_query_t *q, void *dev)
     if (q->kind == TSG_KIND_AFS) {
         q->afs.windows = q->d.windows;
         q->afs.time_windows = (const double *) (b + q->off[7]);
+    }
+    if (q->kind == TSG_KIND_MATVEC) {
+        // windows, focal, group_span, group_wlo, pair_off, win_glo, win_ghi
+        q->mv.windows = (const double *) (b + q->off[1]);
+        q->mv.focal = (const int32_t *) (b + q->off[2]);
+        q->mv.group_span = (const int32_t *) (b + q->off[3]);
+        q->mv.group_wlo = (const int32_t *) (b + q->off[4]);
+        q->mv.pair_off = (const int64_t *) (b + q->off[5]);
+        q->mv.win_glo = (const int32_t *) (b + q->off[6]);
+        q->mv.win_ghi = (const int32_t *) (b + q->off[7]);
     }
 }
 
@@ -1182,6 +1200,207 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     return 0;
 }
 
+// Workspace layout of a relatedness-vector query.
+struct MvLayout {
+    int64_t wc, partial, slots, err, total;
+};
+
+static MvLayout mv_layout_ws(const tsg_query_t *q)
+{
+    MvLayout l;
+    int64_t off = 0;
+    l.wc = off;
+    off += align_up(q->ts->v.num_samples * (int64_t) q->mv.W * 8, 256);
+    l.partial = off;
+    off += align_up(q->mv_pairs * q->mv.nf * (int64_t) q->mv.W * 8, 256);
+    l.slots = off;
+    off += align_up(q->mv_grid * q->mv.slot_bytes, 256);
+    l.err = off;
+    off += 256;
+    l.total = off;
+    return l;
+}
+
+// Validate a relatedness-vector query (c/tskit/trees.c:10782-10816, windows
+// checked without requiring the full span, trees.c:1244-1286) and plan it:
+// span groups, their (group, window) partial blocks, per-CTA slots.
+static int matvec_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t W, uint64_t Wn,
+    const double *windows, uint64_t nf, const int32_t *focal, uint32_t options)
+{
+    *out = nullptr;
+    if (options & (TSG_STAT_NODE | TSG_STAT_SITE)) {
+        return TSG_ERR_UNSUPPORTED_STAT_MODE;
+    }
+    const double Lg = ts->v.sequence_length;
+    double default_windows[2] = { 0, Lg };
+    if (windows == nullptr) {
+        Wn = 1;
+        windows = default_windows;
+    }
+    if (Wn < 1) {
+        return TSG_ERR_BAD_NUM_WINDOWS;
+    }
+    if (windows[0] < 0 || windows[Wn] > Lg) {
+        return TSG_ERR_BAD_WINDOWS;
+    }
+    for (uint64_t j = 0; j < Wn; j++) {
+        if (windows[j] >= windows[j + 1]) {
+            return TSG_ERR_BAD_WINDOWS;
+        }
+    }
+    for (uint64_t j = 0; j < nf; j++) {
+        if (focal[j] < 0 || focal[j] >= ts->v.num_nodes) {
+            return TSG_ERR_NODE_OUT_OF_BOUNDS;
+        }
+    }
+    tsg_query_t *q = new tsg_query_t();
+    std::memset(&q->p, 0, sizeof(q->p));
+    std::memset(&q->afs, 0, sizeof(q->afs));
+    std::memset(&q->mv, 0, sizeof(q->mv));
+    q->kind = TSG_KIND_MATVEC;
+    q->dbuf = nullptr;
+    q->ev_start = nullptr;
+    q->ev_stop = nullptr;
+    q->ts = ts;
+    q->options = options;
+    q->span_normalise = !!(options & TSG_STAT_SPAN_NORMALISE);
+    q->weights = nullptr;
+    q->smem = false;
+    MvParams &m = q->mv;
+    m.W = (int32_t) W;
+    m.ncb = (int32_t) ((W + 31) / 32);
+    m.Wn = (int32_t) Wn;
+    m.nf = (int64_t) nf;
+    m.centre = !(options & TSG_STAT_NONCENTRED);
+    m.L = std::max<int64_t>(ts->v.max_local, 1);
+    m.slot_bytes = align_up(matvec_slot_bytes(ts->v, m.L), 256);
+
+    // resident CTAs, bounded by 16 GiB of node state
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec_ptr(), TSG_MV_WARPS * 32, 0);
+    cudaGetLastError();
+    int64_t slots = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
+    slots = std::min<int64_t>(slots, std::max<int64_t>(1, ((int64_t) 16 << 30) / m.slot_bytes));
+    const int64_t NS = ts->v.num_spans;
+    const auto &bp = ts->h_breakpoints;
+    const auto &st = ts->h_span_tree;
+    const double W0 = windows[0], WE = windows[Wn];
+    int64_t G = std::max<int64_t>(1, std::min<int64_t>(NS, slots / std::max(1, m.ncb)));
+    std::vector<int32_t> gspan, gwlo, gwhi;
+    std::vector<int64_t> poff;
+    for (;;) {
+        gspan.assign((size_t) G + 1, 0);
+        gwlo.assign((size_t) G, -1);
+        gwhi.assign((size_t) G, -2);
+        poff.assign((size_t) G + 1, 0);
+        for (int64_t g = 0; g <= G; g++) {
+            gspan[(size_t) g] = (int32_t) (g * NS / G);
+        }
+        for (int64_t g = 0; g < G; g++) {
+            const double xs = bp[(size_t) st[(size_t) gspan[(size_t) g]]];
+            const double xe = bp[(size_t) st[(size_t) gspan[(size_t) g + 1]]];
+            int64_t np = 0;
+            if (gspan[(size_t) g] < gspan[(size_t) g + 1] && xe > W0 && xs < WE) {
+                const double a = std::max(xs, W0), b = std::min(xe, WE);
+                const int64_t lo = upper_bound(windows, (int64_t) Wn + 1, a) - 1;
+                const int64_t hi = lower_bound(windows, (int64_t) Wn + 1, b) - 1;
+                gwlo[(size_t) g] = (int32_t) lo;
+                gwhi[(size_t) g] = (int32_t) hi;
+                np = hi - lo + 1;
+            }
+            poff[(size_t) g + 1] = poff[(size_t) g] + np;
+        }
+        const int64_t bytes = poff[(size_t) G] * (int64_t) nf * (int64_t) W * 8;
+        if (bytes <= ((int64_t) 24 << 30) || G == 1) {
+            if (bytes > ((int64_t) 48 << 30)) {
+                delete q;
+                return TSG_ERR_NO_MEMORY;
+            }
+            break;
+        }
+        G = std::max<int64_t>(1, G / 2);
+    }
+    std::vector<int32_t> wglo((size_t) Wn, 0), wghi((size_t) Wn, -1);
+    for (int64_t mw = 0; mw < (int64_t) Wn; mw++) {
+        int32_t lo = -1, hi = -2;
+        for (int64_t g = 0; g < G; g++) {
+            if (gwlo[(size_t) g] >= 0 && gwlo[(size_t) g] <= mw && mw <= gwhi[(size_t) g]) {
+                if (lo < 0) {
+                    lo = (int32_t) g;
+                }
+                hi = (int32_t) g;
+            }
+        }
+        wglo[(size_t) mw] = lo < 0 ? 0 : lo;
+        wghi[(size_t) mw] = hi;
+    }
+    m.G = (int32_t) G;
+    q->mv_pairs = poff[(size_t) G];
+    q->mv_grid = std::min<int64_t>(G * m.ncb, slots);
+
+    int64_t off_win = 0;
+    int64_t off_focal = align_up(off_win + ((int64_t) Wn + 1) * 8, 256);
+    int64_t off_gspan = align_up(off_focal + std::max<int64_t>((int64_t) nf, 1) * 4, 256);
+    int64_t off_gwlo = align_up(off_gspan + (G + 1) * 4, 256);
+    int64_t off_poff = align_up(off_gwlo + G * 4, 256);
+    int64_t off_wglo = align_up(off_poff + (G + 1) * 8, 256);
+    int64_t off_wghi = align_up(off_wglo + (int64_t) Wn * 4, 256);
+    int64_t total = align_up(off_wghi + (int64_t) Wn * 4, 256);
+    q->blob.assign((size_t) total, 0);
+    char *h = q->blob.data();
+    std::memcpy(h + off_win, windows, ((size_t) Wn + 1) * 8);
+    if (nf > 0) {
+        std::memcpy(h + off_focal, focal, (size_t) nf * 4);
+    }
+    std::memcpy(h + off_gspan, gspan.data(), (size_t) (G + 1) * 4);
+    std::memcpy(h + off_gwlo, gwlo.data(), (size_t) G * 4);
+    std::memcpy(h + off_poff, poff.data(), (size_t) (G + 1) * 8);
+    std::memcpy(h + off_wglo, wglo.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_wghi, wghi.data(), (size_t) Wn * 4);
+    q->off[0] = off_win;
+    q->off[1] = off_win;
+    q->off[2] = off_focal;
+    q->off[3] = off_gspan;
+    q->off[4] = off_gwlo;
+    q->off[5] = off_poff;
+    q->off[6] = off_wglo;
+    q->off[7] = off_wghi;
+    q->ws_bytes = mv_layout_ws(q).total;
+    *out = q;
+    return 0;
+}
+
+static int matvec_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
+    cudaStream_t st)
+{
+    const int64_t nres = tsg_query_result_size(q);
+    if (q->mv.W == 0 || q->mv.nf == 0) {
+        return 0;
+    }
+    if (q->weights == nullptr) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    const MvLayout l = mv_layout_ws(q);
+    char *b = (char *) ws->ptr;
+    MvParams m = q->mv;
+    m.weights = q->weights;
+    m.wc = (double *) (b + l.wc);
+    m.partial = (double *) (b + l.partial);
+    m.slots = (unsigned char *) (b + l.slots);
+    m.err = (int32_t *) (b + l.err);
+    m.counter = m.err + 1;
+    TSG_CUDA(cudaMemsetAsync(m.err, 0, 2 * sizeof(int32_t), st));
+    if (q->ev_start != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_start, st));
+    }
+    int ret = launch_matvec((unsigned) q->mv_grid, st, q->ts->v, m, q->span_normalise, result);
+    if (ret == 0 && q->ev_stop != nullptr) {
+        TSG_CUDA(cudaEventRecord(q->ev_stop, st));
+    }
+    (void) nres;
+    return ret;
+}
+
 static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result, cudaStream_t st)
 {
     const tsg_treeseq_t *ts = q->ts;
@@ -1282,6 +1501,27 @@ int tsg_query_create_afs(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     return query_upload(q, out);
 }
 
+int tsg_query_create_relatedness_vector(tsg_query_t **out, const tsg_treeseq_t *ts,
+    uint64_t num_weights, uint64_t num_windows, const double *windows, uint64_t num_focal,
+    const int32_t *focal, uint32_t options)
+{
+    tsg_query_t *q = nullptr;
+    int ret = matvec_build(&q, ts, num_weights, num_windows, windows, num_focal, focal, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return query_upload(q, out);
+}
+
+int tsg_query_set_weights(tsg_query_t *q, const double *weights_device)
+{
+    if (q->kind != TSG_KIND_MATVEC) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    q->weights = weights_device;
+    return 0;
+}
+
 int tsg_query_set_sweep_events(tsg_query_t *q, void *start_event, void *stop_event)
 {
     q->ev_start = (cudaEvent_t) start_event;
@@ -1335,6 +1575,9 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     cudaStream_t st = (cudaStream_t) cuda_stream;
     if (q->kind == TSG_KIND_AFS) {
         return afs_launch(q, ws, result, st);
+    }
+    if (q->kind == TSG_KIND_MATVEC) {
+        return matvec_launch(q, ws, result, st);
     }
     const tsg_treeseq_t *ts = q->ts;
     const QueryParams &p = q->p;
@@ -1477,14 +1720,18 @@ int tsg_workspace_check(const tsg_workspace_t *ws, const tsg_query_t *q)
 // ----------------------------------------------------------- host entry points
 namespace tsg {
 
-static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *result)
+// extra: host data staged after the query's arrays (the relatedness
+// vector's weights), bound as the query's weights.
+static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *result,
+    const void *extra = nullptr, int64_t extra_bytes = 0)
 {
     tsg_treeseq_t *ts = const_cast<tsg_treeseq_t *>(cts);
     int ret;
     std::lock_guard<std::mutex> lock(ts->sync_mutex);
     const int64_t nres = tsg_query_result_size(q);
     const int64_t blob = align_up((int64_t) q->blob.size(), 256);
-    const int64_t need = blob + nres * 8;
+    const int64_t xb = align_up(extra_bytes, 256);
+    const int64_t need = blob + xb + nres * 8;
     cudaStream_t st = ts->sync_stream;
     if (ts->sync_ws == nullptr) {
         tsg_workspace_create(&ts->sync_ws);
@@ -1504,13 +1751,19 @@ static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *resu
         }
         ts->stage_bytes = need;
     }
-    double *d_res = (double *) ((char *) ts->stage + blob);
+    double *d_res = (double *) ((char *) ts->stage + blob + xb);
     if (cudaMemcpyAsync(ts->stage, q->blob.data(), q->blob.size(), cudaMemcpyHostToDevice, st)
-        != cudaSuccess) {
+            != cudaSuccess
+        || (extra_bytes > 0
+            && cudaMemcpyAsync((char *) ts->stage + blob, extra, (size_t) extra_bytes,
+                   cudaMemcpyHostToDevice, st) != cudaSuccess)) {
         tsg_query_free(q);
         return TSG_ERR_CUDA;
     }
     query_bind(q, ts->stage);
+    if (extra_bytes > 0) {
+        q->weights = (const double *) ((char *) ts->stage + blob);
+    }
     if ((ret = tsg_query_launch(q, ts->sync_ws, d_res, st)) == 0) {
         if (cudaMemcpyAsync(result, d_res, (size_t) nres * 8, cudaMemcpyDeviceToHost, st)
                 != cudaSuccess
@@ -1600,6 +1853,19 @@ int tsg_treeseq_allele_frequency_spectrum(const tsg_treeseq_t *self, uint64_t K,
         return ret;
     }
     return run_sync_query(self, q, result);
+}
+
+int tsg_treeseq_genetic_relatedness_vector(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows, uint64_t num_focal,
+    const int32_t *focal, double *result, uint32_t options)
+{
+    tsg_query_t *q = nullptr;
+    int ret = matvec_build(&q, self, num_weights, num_windows, windows, num_focal, focal, options);
+    if (ret != 0) {
+        return ret;
+    }
+    return run_sync_query(self, q, result, weights,
+        self->v.num_samples * (int64_t) num_weights * 8);
 }
 
 int tsg_treeseq_diversity(const tsg_treeseq_t *self, uint64_t K, const uint64_t *sizes,

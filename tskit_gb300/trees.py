@@ -340,6 +340,30 @@ class TreeSequence:
             len(tw) - 1, _ptr(tw), flags, _ptr(res)))
         return res
 
+    def _ll_genetic_relatedness_vector(self, weights, windows, mode=None, span_normalise=True,
+                                       centre=True, nodes=None):
+        """Low-level call (python/_tskitmodule.c:7196-7282): result shape
+        (num_windows, num_focal_nodes, num_weights)."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if not centre:
+            flags |= nat.STAT_NONCENTRED
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.ndim != 2:
+            raise ValueError("Weights must be a 2D array")
+        if w.shape[0] != self.num_samples:
+            raise ValueError("First dimension must be num_samples")
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        focal = np.ascontiguousarray(nodes, dtype=np.int32)
+        res = np.zeros((len(win) - 1, len(focal), w.shape[1]))
+        nat.check(self._lib.tsg_treeseq_genetic_relatedness_vector(
+            self._handle, w.shape[1], _ptr(w), len(win) - 1, _ptr(win), len(focal),
+            _ptr(focal), _ptr(res), flags))
+        return res
+
     def _ll_one_way(self, typ):
         def method(sample_set_sizes, sample_sets, windows, mode=None, span_normalise=True,
                    polarised=False):
@@ -450,6 +474,29 @@ class TreeSequence:
         return stat
 
     # ------------------------------------------------------------ one-way
+    def genetic_relatedness_vector(self, W, windows=None, mode="site", span_normalise=True,
+                                   centre=True, nodes=None):
+        """python/tskit/trees.py:9157-9218: the genetic relatedness matrix
+        times the weight columns W (one row per sample); shape (windows,
+        focal nodes, columns), the window dimension dropped when not given.
+        Branch mode only, as in the reference's C library."""
+        if (not hasattr(W, "__len__")) or (len(W) != self.num_samples):
+            raise ValueError("First weight dimension must be equal to number of samples.")
+        W = np.asarray(W)
+        if len(W.shape) == 1:
+            W = W.reshape(W.shape[0], 1)
+        if nodes is None:
+            nodes = list(self.samples())
+        elif centre:
+            raise ValueError("If `nodes` is provided, must have centre=False.")
+        try:
+            nodes = safe_np_int_cast(nodes, np.int32)
+        except Exception:
+            raise ValueError("Could not interpret `nodes` as a list of node IDs.")
+        return self.__run_windowed_stat(windows, self._ll_genetic_relatedness_vector, W,
+                                        mode=mode, span_normalise=span_normalise,
+                                        centre=centre, nodes=nodes)
+
     def allele_frequency_spectrum(self, sample_sets=None, windows=None, time_windows=None,
                                   mode="site", span_normalise=True, polarised=False):
         """python/tskit/trees.py:9844-9965: the joint allele frequency spectrum
