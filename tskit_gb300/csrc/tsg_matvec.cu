@@ -352,18 +352,27 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                             vc += (S.time[pc] - tc) * (pos - *xp) * wc;
                         }
                     }
+                    // one root-path step per iteration; the next node's state is
+                    // loaded before this node's is stored
                     uint32_t a = (uint32_t) p;
                     uint32_t pa = S.par[a];
+                    double va = S.v[(int64_t) a * 32 + lane];
+                    double wa = S.w[(int64_t) a * 32 + lane];
+                    double xa = S.x[a], ta = S.time[a];
                     for (int32_t guard = 0; a != MV_NONE; guard++) {
                         if (guard > Ls) {
                             dev_error(m.err, DEV_PATH_TOO_LONG);
                             break;
                         }
-                        const uint32_t ppa = pa != MV_NONE ? S.par[pa] : MV_NONE;
-                        double va = S.v[(int64_t) a * 32 + lane];
-                        double wa = S.w[(int64_t) a * 32 + lane];
+                        uint32_t ppa = MV_NONE;
+                        double vn = 0, wn = 0, xn = 0, tn = 0;
                         if (pa != MV_NONE) {
-                            va += (S.time[pa] - S.time[a]) * (pos - S.x[a]) * wa;
+                            ppa = S.par[pa];
+                            vn = S.v[(int64_t) pa * 32 + lane];
+                            wn = S.w[(int64_t) pa * 32 + lane];
+                            xn = S.x[pa];
+                            tn = S.time[pa];
+                            va += (tn - ta) * (pos - xa) * wa;
                         }
                         vc -= sign * va;
                         wa += sign * wc;
@@ -376,6 +385,10 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                         __syncwarp();
                         a = pa;
                         pa = ppa;
+                        va = vn;
+                        wa = wn;
+                        xa = xn;
+                        ta = tn;
                     }
                     *vrow = vc;
                     __syncwarp();

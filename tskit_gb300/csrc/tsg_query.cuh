@@ -99,7 +99,7 @@ void *afs_replay_kernel(int form);
 // Branch genetic relatedness matrix-vector product (one query).  Work item:
 // a group of consecutive spans x a block of 32 weight columns (one column
 // per lane), with node state in a per-CTA slot of global memory.
-#define TSG_MV_WARPS 4
+#define TSG_MV_WARPS 16
 struct MvParams {
     int32_t W;          // weight columns
     int32_t ncb;        // blocks of 32 columns

@@ -1275,12 +1275,12 @@ static int matvec_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t W, 
     m.L = std::max<int64_t>(ts->v.max_local, 1);
     m.slot_bytes = align_up(matvec_slot_bytes(ts->v, m.L), 256);
 
-    // resident CTAs, bounded by 16 GiB of node state
+    // resident CTAs, bounded by 64 GiB of node state
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec_ptr(), TSG_MV_WARPS * 32, 0);
     cudaGetLastError();
     int64_t slots = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
-    slots = std::min<int64_t>(slots, std::max<int64_t>(1, ((int64_t) 16 << 30) / m.slot_bytes));
+    slots = std::min<int64_t>(slots, std::max<int64_t>(1, ((int64_t) 64 << 30) / m.slot_bytes));
     const int64_t NS = ts->v.num_spans;
     const auto &bp = ts->h_breakpoints;
     const auto &st = ts->h_span_tree;
