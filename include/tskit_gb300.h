@@ -71,6 +71,7 @@ extern "C" {
 #define TSG_ERR_EMPTY_SAMPLE_SET (-908)
 #define TSG_ERR_UNSUPPORTED_STAT_MODE (-909)
 #define TSG_ERR_TIME_UNCALIBRATED (-910)
+#define TSG_ERR_STAT_POLARISED_UNSUPPORTED (-911)
 #define TSG_ERR_INSUFFICIENT_WEIGHTS (-913)
 #define TSG_ERR_BAD_TIME_WINDOWS_DIM (-922)
 #define TSG_ERR_BAD_TIME_WINDOWS (-924)
@@ -217,6 +218,30 @@ int tsg_treeseq_allele_frequency_spectrum(const tsg_treeseq_t *self,
 int tsg_treeseq_genetic_relatedness_vector(const tsg_treeseq_t *self, uint64_t num_weights,
     const double *weights, uint64_t num_windows, const double *windows,
     uint64_t num_focal_nodes, const int32_t *focal_nodes, double *result, uint32_t options);
+
+/* ------------------------------------------------- divergence matrix (site)
+ * Replaces tsk_treeseq_divergence_matrix (c/tskit/trees.c:8900-9001) for
+ * site mode: same arguments, option bits, error codes and result
+ * (num_windows x K x K, K = num_sample_sets, or every sample alone when
+ * sample_sets is NULL).  Branch mode returns TSG_ERR_UNSUPPORTED_STAT_MODE
+ * (not on this path).  The pair counts come from an exact Gram matrix of
+ * the 0/1 genotypes on the tensor cores.  Host pointers; synchronous. */
+int tsg_treeseq_divergence_matrix(const tsg_treeseq_t *self, uint64_t num_sample_sets,
+    const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_windows,
+    const double *windows, uint32_t options, double *result);
+/* genetic_relatedness_matrix (python/tskit/trees.py:8978-9102, site mode):
+ * the divergence matrix followed by the same normalisation, on the device.
+ * No C counterpart in the reference (its normalisation is Python code). */
+int tsg_treeseq_genetic_relatedness_matrix(const tsg_treeseq_t *self,
+    uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_windows, const double *windows, uint32_t options, double *result);
+/* P = G G^T (int32, upper-triangle 128 x 256 tiles written; P is n x ldp,
+ * device) for a device operand G of n rows x ld bytes holding E4M3 0 or 1
+ * (0x00 / 0x38), K = k columns (a multiple of 128; ld a multiple of 16).
+ * Exact.  Synchronous on `cuda_stream`.  No reference counterpart: the
+ * contraction behind the divergence matrix, exposed for testing. */
+int tsg_gram_e4m3(const uint8_t *G, int64_t n, int64_t ld, int64_t k, int32_t *P, int64_t ldp,
+    void *cuda_stream);
 
 /* ------------------------------------------------------ fused sample-count
  * Generalises tsk_treeseq_sample_count_stat (c/tskit/trees.c:2174-2220) to a

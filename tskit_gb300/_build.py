@@ -29,6 +29,8 @@ CUDA_SOURCES = [
     "tsg_eval_f64_unpol.cu",
     "tsg_afs.cu",
     "tsg_matvec.cu",
+    "tsg_gram.cu",
+    "tsg_grm.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

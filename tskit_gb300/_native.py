@@ -111,6 +111,11 @@ SIGNATURES = {
     "tsg_query_create_relatedness_vector": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _U64, _P, _U64, _P, _U32]),
     "tsg_query_set_weights": (ctypes.c_int, [_P, _P]),
+    "tsg_treeseq_divergence_matrix": (
+        ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U32, _P]),
+    "tsg_treeseq_genetic_relatedness_matrix": (
+        ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U32, _P]),
+    "tsg_gram_e4m3": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
     "tsg_query_create_afs": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),

@@ -142,6 +142,7 @@ struct HostTopology {
     std::vector<int32_t> tree_in, tree_out, tree_sites;  // num_trees + 1
     std::vector<int32_t> site_mut;             // num_sites + 1
     std::vector<int32_t> mut_node;             // num_mutations
+    std::vector<int32_t> mut_allele;           // num_mutations: allele codes
 };
 
 
@@ -174,6 +175,7 @@ struct tsg_treeseq {
     std::vector<double> h_site_position;
     int64_t max_alive;
     int64_t max_children = 0;  // most children of a node in any span's seek tree
+    tsg::HostTopology host;    // host copy of the topology (span plan, genotype decoding)
     // device allocations owned by this object
     std::vector<void *> owned;
     // state of the synchronous (host-pointer) entry points

@@ -421,6 +421,9 @@ const char *tsg_strerror(int err)
         case TSG_ERR_TIME_UNCALIBRATED:
             return "Statistics using branch lengths cannot be calculated when time_units "
                    "is 'uncalibrated'.";
+        case TSG_ERR_STAT_POLARISED_UNSUPPORTED:
+            return "The TSK_STAT_POLARISED option is not supported by this statistic. "
+                   "(TSK_ERR_STAT_POLARISED_UNSUPPORTED)";
         case TSG_ERR_INSUFFICIENT_WEIGHTS:
             return "Insufficient weights provided (at least 1 required).";
         case TSG_ERR_BAD_TIME_WINDOWS_DIM:
@@ -694,7 +697,8 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
             || (ret = d2h(h.ins_edge, t.I, E))
             || (ret = d2h(h.tree_in, tree_in, T + 1)) || (ret = d2h(h.tree_out, tree_out, T + 1))
             || (ret = d2h(h.tree_sites, tree_sites, T + 1))
-            || (ret = d2h(h.site_mut, site_mut, S + 1)) || (ret = d2h(h.mut_node, t.mut_node, M))) {
+            || (ret = d2h(h.site_mut, site_mut, S + 1)) || (ret = d2h(h.mut_node, t.mut_node, M))
+            || (ret = d2h(h.mut_allele, t.mut_allele, M))) {
             goto fail;
         }
         if (num_spans <= 0) {
@@ -714,6 +718,7 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         if ((ret = build_span_plan(ts, h, num_spans)) != 0) {
             goto fail;
         }
+        ts->host = std::move(h);
         if ((ret = d2h(ts->h_site_position, t.site_pos, S)) != 0) {
             goto fail;
         }

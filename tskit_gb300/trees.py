@@ -474,6 +474,69 @@ class TreeSequence:
         return stat
 
     # ------------------------------------------------------------ one-way
+    # ------------------------------------------------ divergence matrices
+    @staticmethod
+    def _parse_stat_matrix_sample_sets(ids):
+        """python/tskit/trees.py:8708-8737."""
+        id_dtype = np.int32
+        size_dtype = np.uint64
+        if isinstance(ids, (str, bytes, dict, numbers.Number)):
+            raise TypeError(f"ID specification cannot be a {type(ids)}")
+        if len(ids) == 0:
+            return np.array([], dtype=id_dtype), np.array([], dtype=size_dtype)
+        if isinstance(ids[0], numbers.Number):
+            flat = safe_np_int_cast(ids, id_dtype)
+            sizes = np.ones(len(flat), dtype=size_dtype)
+        else:
+            set_lists, sizes = [], []
+            for id_list in ids:
+                a = safe_np_int_cast(id_list, id_dtype)
+                if len(a.shape) != 1:
+                    raise ValueError("ID sets must be 1D integer arrays")
+                set_lists.append(a)
+                sizes.append(len(a))
+            flat = np.hstack(set_lists)
+            sizes = np.array(sizes, dtype=size_dtype)
+        return flat, sizes
+
+    def _divmat(self, fn, sample_sets, windows, mode, span_normalise):
+        windows_specified = windows is not None
+        windows = np.ascontiguousarray(self.parse_windows(windows), dtype=np.float64)
+        mode = "site" if mode is None else mode
+        if sample_sets is None:
+            flat = np.ascontiguousarray(self.samples(), dtype=np.int32)
+            sizes = np.ones(len(flat), dtype=np.uint64)
+        else:
+            flat, sizes = self._parse_stat_matrix_sample_sets(sample_sets)
+            flat = np.ascontiguousarray(flat, dtype=np.int32)
+            sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        K = len(sizes)
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        D = np.zeros((len(windows) - 1, K, K))
+        nat.check(fn(self._handle, K, _ptr(sizes), _ptr(flat), len(windows) - 1, _ptr(windows),
+                     flags, _ptr(D)))
+        if not windows_specified:
+            D = D[0]
+        return D
+
+    def divergence_matrix(self, sample_sets=None, *, windows=None, num_threads=0, mode=None,
+                          span_normalise=True):
+        """python/tskit/trees.py:8739-8829 (site mode): mean divergence between
+        the samples of each pair of sets, shape (windows, sets, sets), the
+        window dimension dropped when not given.  num_threads is accepted for
+        compatibility (the work runs on the GPU)."""
+        return self._divmat(self._lib.tsg_treeseq_divergence_matrix, sample_sets, windows, mode,
+                            span_normalise)
+
+    def genetic_relatedness_matrix(self, sample_sets=None, *, windows=None, num_threads=0,
+                                   mode=None, span_normalise=True):
+        """python/tskit/trees.py:8978-9102 (site mode): the divergence matrix
+        normalised to centred relatedness, on the GPU."""
+        return self._divmat(self._lib.tsg_treeseq_genetic_relatedness_matrix, sample_sets,
+                            windows, mode, span_normalise)
+
     def genetic_relatedness_vector(self, W, windows=None, mode="site", span_normalise=True,
                                    centre=True, nodes=None):
         """python/tskit/trees.py:9157-9218: the genetic relatedness matrix
