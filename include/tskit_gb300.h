@@ -258,6 +258,25 @@ int tsg_treeseq_sample_count_stat(const tsg_treeseq_t *self, uint64_t num_sample
     const tsg_output_t *outputs, uint64_t num_windows, const double *windows,
     uint32_t options, double *result);
 
+/* ------------------------------------------- arbitrary summary functions
+ * general_stat / sample_count_stat with a caller-supplied summary function
+ * (c/tskit/trees.c:2035-2095 with general_stat_func_t; the reference calls
+ * it once per state change).  Three steps: prepare runs the sweep for the
+ * sample sets (0/1 weights), windows and mode (one of site / branch) and
+ * collects the distinct count vectors it meets; states returns them
+ * (num_states x num_sample_sets int32); finish takes the summary values at
+ * those states (num_states x num_outputs doubles: for branch mode without
+ * TSG_STAT_POLARISED, f(x) + f(n - x) as the reference's unpolarised
+ * wrapper, trees.c:1944-1972) and writes num_windows x num_outputs. */
+typedef struct tsg_general tsg_general_t;
+int tsg_general_stat_prepare(tsg_general_t **general, const tsg_treeseq_t *self,
+    uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
+    uint64_t num_outputs, uint64_t num_windows, const double *windows, uint32_t options,
+    int64_t *num_states);
+int tsg_general_stat_states(tsg_general_t *general, int32_t *states);
+int tsg_general_stat_finish(tsg_general_t *general, const double *values, double *result);
+int tsg_general_stat_free(tsg_general_t *general);
+
 /* ----------------------------------------------- device-resident queries
  * A query is prepared once (validates and uploads sample sets, summary terms
  * and windows) and launched any number of times on a stream with a

@@ -31,6 +31,7 @@ CUDA_SOURCES = [
     "tsg_matvec.cu",
     "tsg_gram.cu",
     "tsg_grm.cu",
+    "tsg_general.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -116,6 +116,12 @@ SIGNATURES = {
     "tsg_treeseq_genetic_relatedness_matrix": (
         ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U32, _P]),
     "tsg_gram_e4m3": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
+    "tsg_general_stat_prepare": (
+        ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _U64, _P, _U32,
+                       ctypes.POINTER(_I64)]),
+    "tsg_general_stat_states": (ctypes.c_int, [_P, _P]),
+    "tsg_general_stat_finish": (ctypes.c_int, [_P, _P, _P]),
+    "tsg_general_stat_free": (ctypes.c_int, [_P]),
     "tsg_query_create_afs": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),

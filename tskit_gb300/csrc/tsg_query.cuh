@@ -130,6 +130,18 @@ int launch_matvec(unsigned grid, cudaStream_t st, const TSView &v, const MvParam
 int64_t matvec_slot_bytes(const TSView &v, int64_t L);
 const void *k_matvec_ptr();
 
+// Arbitrary summary functions (tsg_general.cu).
+int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
+    const int64_t *site_off, int64_t num_site_keys, uint64_t *klo, uint64_t *khi, uint64_t *tlo,
+    uint64_t *thi, int64_t *flag, int64_t *pos, void *cub_tmp, size_t cub_bytes, uint64_t *ulo,
+    uint64_t *uhi, int64_t *U, cudaStream_t st);
+size_t gen_cub_bytes(int64_t n);
+int gen_eval(int form, const TSView &v, const QueryParams &q, const WsDev &w,
+    const int64_t *site_off, const uint64_t *ulo, const uint64_t *uhi, int64_t U, const double *F,
+    int32_t R_total, int32_t r0, cudaStream_t st);
+int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K, int32_t *out,
+    cudaStream_t st);
+
 // term budget of the item evaluation (accumulators per lane)
 #define TSG_ITEM_RMAX 32
 

@@ -1460,6 +1460,73 @@ static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
 
 extern "C" {
 
+}  // extern "C"
+
+namespace tsg {
+
+// Views of a sample-count query's workspace (layout of query_build).
+static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
+{
+    const tsg_treeseq_t *ts = q->ts;
+    const QueryParams &p = q->p;
+    const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans, TSW = q->total_span_windows;
+    const int64_t R = p.R, slots = q->num_slots;
+    char *b = (char *) ws->ptr;
+    WsDev w;
+    int64_t off = 0;
+    w.parent = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.nchild = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.arrive = (int32_t *) (b + off);
+    off += align_up(slots * N * 4, 256);
+    w.x = (int32_t *) (b + off);
+    off += align_up(slots * N * 4 * p.KP, 256);
+    w.A = (double *) (b + off);
+    off += align_up(TSW * 8, 256);
+    w.B = (double *) (b + off);
+    off += align_up(TSW * R * 8, 256);
+    w.SITE = (double *) (b + off);
+    off += align_up(TSW * R * 8, 256);
+    w.D = (double *) (b + off);
+    off += align_up(NS * R * 8, 256);
+    w.RS = (double *) (b + off);
+    off += align_up(NS * R * 8, 256);
+    w.rs0 = (double *) (b + off);
+    off += align_up(R * 8, 256);
+    w.items = nullptr;
+    w.state = nullptr;
+    w.mcnt = nullptr;
+    w.dD = nullptr;
+    w.node_mask = nullptr;
+    w.site_val = nullptr;
+    w.site_win = nullptr;
+    if (q->smem) {
+        const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
+        w.items = b + off;
+        off += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);
+        w.mcnt = (uint64_t *) (b + off);
+        off += align_up(ts->v.num_mutations * 8 * q->KQ, 256);
+        w.dD = (double *) (b + off);
+        off += align_up(ts->v.num_chunks * R * 8, 256);
+        w.node_mask = (uint32_t *) (b + off);
+        off += align_up(ts->v.num_nodes * 4, 256);
+        w.site_val = (double *) (b + off);
+        off += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);
+        w.site_win = (double *) (b + off);
+        off += align_up((int64_t) p.Wn * R * 8, 256);
+        w.state = b + off;
+        off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
+    }
+    w.err = (int32_t *) (b + off);
+    w.counter = w.err + 1;
+    return w;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
 static int query_upload(tsg_query_t *q, tsg_query_t **out)
 {
     if (cudaMalloc(&q->dbuf, q->blob.size()) != cudaSuccess) {
@@ -1581,58 +1648,9 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     }
     const tsg_treeseq_t *ts = q->ts;
     const QueryParams &p = q->p;
-    const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans, TSW = q->total_span_windows;
+    const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans;
     const int64_t R = p.R, slots = q->num_slots;
-    char *b = (char *) ws->ptr;
-    WsDev w;
-    int64_t off = 0;
-    w.parent = (int32_t *) (b + off);
-    off += align_up(slots * N * 4, 256);
-    w.nchild = (int32_t *) (b + off);
-    off += align_up(slots * N * 4, 256);
-    w.arrive = (int32_t *) (b + off);
-    off += align_up(slots * N * 4, 256);
-    w.x = (int32_t *) (b + off);
-    off += align_up(slots * N * 4 * p.KP, 256);
-    w.A = (double *) (b + off);
-    off += align_up(TSW * 8, 256);
-    w.B = (double *) (b + off);
-    off += align_up(TSW * R * 8, 256);
-    w.SITE = (double *) (b + off);
-    off += align_up(TSW * R * 8, 256);
-    w.D = (double *) (b + off);
-    off += align_up(NS * R * 8, 256);
-    w.RS = (double *) (b + off);
-    off += align_up(NS * R * 8, 256);
-    w.rs0 = (double *) (b + off);
-    off += align_up(R * 8, 256);
-    w.items = nullptr;
-    w.state = nullptr;
-    w.mcnt = nullptr;
-    w.dD = nullptr;
-    w.node_mask = nullptr;
-    w.site_val = nullptr;
-    w.site_win = nullptr;
-    if (q->smem) {
-        const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
-        w.items = b + off;
-        off += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);
-        w.mcnt = (uint64_t *) (b + off);
-        off += align_up(ts->v.num_mutations * 8 * q->KQ, 256);
-        w.dD = (double *) (b + off);
-        off += align_up(ts->v.num_chunks * R * 8, 256);
-        w.node_mask = (uint32_t *) (b + off);
-        off += align_up(ts->v.num_nodes * 4, 256);
-        w.site_val = (double *) (b + off);
-        off += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);
-        w.site_win = (double *) (b + off);
-        off += align_up((int64_t) p.Wn * R * 8, 256);
-        w.state = b + off;
-        off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
-    }
-    w.err = (int32_t *) (b + off);
-    w.counter = w.err + 1;
-
+    const WsDev w = ws_bind(q, ws);
     TSG_CUDA(cudaMemsetAsync(w.err, 0, 2 * sizeof(int32_t), st));
     TSG_CUDA(cudaMemsetAsync(w.rs0, 0, (size_t) R * 8, st));
     if (q->ev_start != nullptr) {
@@ -1713,6 +1731,260 @@ int tsg_workspace_check(const tsg_workspace_t *ws, const tsg_query_t *q)
     const int64_t off = q->ws_bytes - 256;
     TSG_CUDA(cudaMemcpy(&h, b + off, sizeof(int32_t), cudaMemcpyDeviceToHost));
     return h == 0 ? 0 : TSG_ERR_DEVICE_CHECK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------- arbitrary summary functions
+struct tsg_general {
+    tsg_query_t *q = nullptr;
+    tsg_workspace_t *ws = nullptr;
+    cudaStream_t st = nullptr;
+    int form = 0;
+    int32_t R = 0, K = 0;
+    int64_t U = 0, num_site_keys = 0;
+    void *buf = nullptr;
+    uint64_t *ulo = nullptr, *uhi = nullptr;
+    int64_t *site_off = nullptr;
+    WsDev w;
+    QueryDev d;
+};
+
+namespace tsg {
+
+static void general_release(tsg_general *g)
+{
+    if (g == nullptr) {
+        return;
+    }
+    if (g->st != nullptr) {
+        cudaStreamSynchronize(g->st);
+    }
+    cudaFree(g->buf);
+    if (g->ws != nullptr) {
+        tsg_workspace_free(g->ws);
+    }
+    if (g->q != nullptr) {
+        tsg_query_free(g->q);
+    }
+    if (g->st != nullptr) {
+        cudaStreamDestroy(g->st);
+    }
+    delete g;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const uint64_t *sizes, const int32_t *sets, uint64_t R, uint64_t Wn, const double *windows,
+    uint32_t options, int64_t *num_states)
+{
+    *out = nullptr;
+    if (R < 1) {
+        return TSG_ERR_BAD_RESULT_DIMS;
+    }
+    if (options & TSG_STAT_BOTH_MODES) {
+        return TSG_ERR_MULTIPLE_STAT_MODES;
+    }
+    // the replay of a query with (up to 32) placeholder terms
+    const uint64_t Rb = std::min<uint64_t>(R, TSG_ITEM_RMAX);
+    std::vector<tsg_output_t> outs((size_t) Rb);
+    for (auto &o : outs) {
+        o.type = TSG_DIVERSITY;
+        o.idx[0] = o.idx[1] = o.idx[2] = o.idx[3] = 0;
+    }
+    tsg_general *g = new tsg_general();
+    g->R = (int32_t) R;
+    g->K = (int32_t) K;
+    int ret = tsg_query_create(&g->q, ts, K, sizes, sets, Rb, outs.data(), Wn, windows,
+        options & ~(uint32_t) (TSG_PRECISION_F32_KAHAN | TSG_FORCE_GLOBAL_SWEEP));
+    if (ret != 0) {
+        delete g;
+        return ret;
+    }
+    tsg_query_t *q = g->q;
+    if (!q->smem) {
+        general_release(g);
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    g->form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess
+        || tsg_workspace_create(&g->ws) != 0
+        || (ret = tsg_workspace_reserve(g->ws, q->ws_bytes)) != 0) {
+        cudaGetLastError();
+        general_release(g);
+        return ret != 0 ? ret : TSG_ERR_CUDA;
+    }
+    const TSView &v = ts->v;
+    const QueryParams &p = q->p;
+    g->w = ws_bind(q, g->ws);
+    g->d = q->d;
+    g->d.node_mask = g->w.node_mask;
+    // allele count of every site
+    std::vector<int64_t> site_off((size_t) v.num_sites + 1, 0);
+    for (int64_t s = 0; s < v.num_sites; s++) {
+        int32_t mx = 0;
+        for (int32_t m = ts->host.site_mut[(size_t) s]; m < ts->host.site_mut[(size_t) s + 1]; m++) {
+            mx = std::max(mx, ts->host.mut_allele[(size_t) m]);
+        }
+        site_off[(size_t) s + 1] = site_off[(size_t) s] + mx + 1;
+    }
+    g->num_site_keys = site_off[(size_t) v.num_sites];
+    const int64_t n = (p.branch ? 2 * v.num_items : 0) + (p.site ? g->num_site_keys : 0);
+    const int64_t nk = std::max<int64_t>(n, 1);
+    const size_t cub = gen_cub_bytes(nk);
+    const int64_t stride = align_up(nk, 32) * 8;
+    const int64_t bytes = 8 * stride + align_up((int64_t) cub, 256)
+        + align_up((v.num_sites + 1) * 8, 256);
+    if (cudaMalloc(&g->buf, (size_t) bytes) != cudaSuccess) {
+        cudaGetLastError();
+        general_release(g);
+        return TSG_ERR_NO_MEMORY;
+    }
+    char *b = (char *) g->buf;
+    uint64_t *klo = (uint64_t *) (b + 0 * stride), *khi = (uint64_t *) (b + 1 * stride);
+    uint64_t *tlo = (uint64_t *) (b + 2 * stride), *thi = (uint64_t *) (b + 3 * stride);
+    int64_t *flag = (int64_t *) (b + 4 * stride), *pos = (int64_t *) (b + 5 * stride);
+    g->ulo = (uint64_t *) (b + 6 * stride);
+    g->uhi = (uint64_t *) (b + 7 * stride);
+    void *cub_tmp = b + 8 * stride;
+    g->site_off = (int64_t *) (b + 8 * stride + align_up((int64_t) cub, 256));
+    cudaStream_t st = g->st;
+    const WsDev &w = g->w;
+    if (cudaMemcpyAsync(g->site_off, site_off.data(), site_off.size() * 8, cudaMemcpyHostToDevice,
+            st) != cudaSuccess
+        || cudaMemsetAsync(w.err, 0, 8, st) != cudaSuccess) {
+        general_release(g);
+        return TSG_ERR_CUDA;
+    }
+    k_node_mask<<<grid_for(v.num_nodes), 256, 0, st>>>(v, g->d, w.node_mask);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
+    if (ret == 0) {
+        const unsigned gr = (unsigned) q->smem_grid;
+        const size_t sb = (size_t) q->smem_bytes;
+        switch (g->form) {
+            case 0: k_replay_items<16, 1, uint16_t><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
+            case 1: k_replay_items<16, 2, uint16_t><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
+            case 2: k_replay_items<32, 1, int32_t><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
+            default: k_replay_items<32, 2, int32_t><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
+        }
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
+    }
+    if (ret == 0) {
+        ret = gen_collect(g->form, v, p, w, g->site_off, g->num_site_keys, klo, khi, tlo, thi,
+            flag, pos, cub_tmp, cub, g->ulo, g->uhi, &g->U, st);
+    }
+    if (ret == 0) {
+        int32_t herr = 0;
+        if (cudaMemcpyAsync(&herr, w.err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else if (herr != 0) {
+            ret = TSG_ERR_DEVICE_CHECK;
+        }
+    }
+    if (ret != 0) {
+        general_release(g);
+        return ret;
+    }
+    *num_states = g->U;
+    *out = g;
+    return 0;
+}
+
+int tsg_general_stat_states(tsg_general_t *g, int32_t *states)
+{
+    if (g->U == 0) {
+        return 0;
+    }
+    int32_t *d = nullptr;
+    if (cudaMalloc(&d, (size_t) (g->U * g->K * 4)) != cudaSuccess) {
+        cudaGetLastError();
+        return TSG_ERR_NO_MEMORY;
+    }
+    int ret = gen_unpack(g->q->W, g->ulo, g->uhi, g->U, g->K, d, g->st);
+    if (ret == 0
+        && (cudaMemcpyAsync(states, d, (size_t) (g->U * g->K * 4), cudaMemcpyDeviceToHost, g->st)
+                != cudaSuccess
+            || cudaStreamSynchronize(g->st) != cudaSuccess)) {
+        ret = TSG_ERR_CUDA;
+    }
+    cudaFree(d);
+    return ret;
+}
+
+int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *result)
+{
+    const tsg_query_t *q = g->q;
+    const TSView &v = q->ts->v;
+    const int64_t Wn = q->p.Wn, R = g->R;
+    const int64_t rb_max = q->p.R;
+    double *dF = nullptr, *dres = nullptr;
+    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(g->U * R * 8, 8)) != cudaSuccess
+        || cudaMalloc(&dres, (size_t) (Wn * rb_max * 8)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(dF);
+        return TSG_ERR_NO_MEMORY;
+    }
+    cudaStream_t st = g->st;
+    int ret = 0;
+    if (g->U > 0
+        && cudaMemcpyAsync(dF, values, (size_t) (g->U * R * 8), cudaMemcpyHostToDevice, st)
+            != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    }
+    std::vector<double> block((size_t) (Wn * rb_max));
+    for (int64_t r0 = 0; ret == 0 && r0 < R; r0 += rb_max) {
+        QueryParams pb = q->p;
+        pb.R = (int32_t) std::min<int64_t>(rb_max, R - r0);
+        if ((ret = gen_eval(g->form, v, pb, g->w, g->site_off, g->ulo, g->uhi, g->U, dF,
+                 (int32_t) R, (int32_t) r0, st))
+            != 0) {
+            break;
+        }
+        if (pb.branch) {
+            k_span_windows<<<(unsigned) ((v.num_spans + 7) / 8), 256, 0, st>>>(v, pb, g->d, g->w);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        }
+        if (pb.site) {
+            if (v.num_sites > 0) {
+                k_site_windows<<<(unsigned) ((int64_t) pb.Wn * pb.R), 256, 0, st>>>(pb, g->d, g->w);
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            } else if (cudaMemsetAsync(g->w.site_win, 0, (size_t) (pb.Wn * pb.R * 8), st)
+                != cudaSuccess) {
+                ret = TSG_ERR_CUDA;
+                break;
+            }
+        }
+        k_window_reduce<<<grid_for((int64_t) pb.Wn * pb.R), 256, 0, st>>>(pb, g->d, g->w,
+            q->span_normalise, 1, dres);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (cudaGetLastError() != cudaSuccess
+            || cudaMemcpyAsync(block.data(), dres, (size_t) (Wn * pb.R * 8),
+                   cudaMemcpyDeviceToHost, st) != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+            break;
+        }
+        for (int64_t wdx = 0; wdx < Wn; wdx++) {
+            for (int64_t r = 0; r < pb.R; r++) {
+                result[wdx * R + r0 + r] = block[(size_t) (wdx * pb.R + r)];
+            }
+        }
+    }
+    cudaFree(dF);
+    cudaFree(dres);
+    return ret;
+}
+
+int tsg_general_stat_free(tsg_general_t *g)
+{
+    general_release(g);
+    return 0;
 }
 
 }  // extern "C"

@@ -474,6 +474,107 @@ class TreeSequence:
         return stat
 
     # ------------------------------------------------------------ one-way
+    # ------------------------------------------- arbitrary summary functions
+    def _ll_general_stat(self, sample_set_sizes, sample_sets, f, output_dim, windows,
+                         mode=None, span_normalise=True, polarised=False):
+        """The sweep for 0/1 weights given as sample sets, with the summary
+        function evaluated on the host once per distinct count vector."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        sizes = np.ascontiguousarray(sample_set_sizes, dtype=np.uint64)
+        flat = np.ascontiguousarray(sample_sets, dtype=np.int32)
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        R = int(output_dim)
+        if R < 1:
+            raise ValueError("output_dim must be at least 1")
+        g = ctypes.c_void_p()
+        U = ctypes.c_int64()
+        nat.check(self._lib.tsg_general_stat_prepare(
+            ctypes.byref(g), self._handle, len(sizes), _ptr(sizes), _ptr(flat), R, len(win) - 1,
+            _ptr(win), flags, ctypes.byref(U)))
+        try:
+            K = len(sizes)
+            states = np.zeros((U.value, K), dtype=np.int32)
+            nat.check(self._lib.tsg_general_stat_states(g, _ptr(states)))
+            total = sizes.astype(np.float64)
+            branch = bool(flags & nat.STAT_BRANCH)
+            F = np.zeros((U.value, R))
+            for i in range(U.value):
+                x = states[i].astype(np.float64)
+                v = np.asarray(f(x), dtype=np.float64).reshape(-1)
+                if v.shape[0] != R:
+                    raise ValueError("summary function output has the wrong dimension")
+                if branch and not polarised:
+                    v = v + np.asarray(f(total - x), dtype=np.float64).reshape(-1)
+                F[i] = v
+            res = np.zeros((len(win) - 1, R))
+            nat.check(self._lib.tsg_general_stat_finish(g, _ptr(F), _ptr(res)))
+        finally:
+            self._lib.tsg_general_stat_free(g)
+        return res
+
+    def _check_summary(self, total, f, output_dim):
+        """python/tskit/trees.py:7983-7993."""
+        for x in [total, total * 0.0]:
+            with np.errstate(invalid="ignore", divide="ignore"):
+                fx = np.array(f(x))
+            fx[np.isnan(fx)] = 0.0
+            if not np.allclose(fx, np.zeros((output_dim,))):
+                raise ValueError("Summary function does not return zero for both "
+                                 "zero weight and total weight.")
+
+    def general_stat(self, W, f, output_dim, windows=None, polarised=False, mode=None,
+                     span_normalise=True, strict=True):
+        """python/tskit/trees.py:7917-8004 for 0/1 weights (each column is a
+        set of samples; samples may be in several columns).  Other weights
+        are not supported on this path and raise ValueError."""
+        if mode is None:
+            mode = "site"
+        W = np.asarray(W, dtype=np.float64)
+        if W.ndim != 2 or W.shape[0] != self.num_samples:
+            raise ValueError("First dimension of W must be number of samples")
+        if not np.all((W == 0) | (W == 1)):
+            raise ValueError("Only weights of 0 or 1 are supported on this path")
+        if strict:
+            self._check_summary(np.sum(W, axis=0), f, output_dim)
+        samples = self.samples()
+        sets = [samples[W[:, k] == 1] for k in range(W.shape[1])]
+        if any(len(s) == 0 for s in sets):
+            raise ValueError("Each weight column must select at least one sample")
+        sizes = np.array([len(s) for s in sets], dtype=np.uint64)
+        flat = safe_np_int_cast(np.hstack(sets), np.int32)
+        return self.__run_windowed_stat(windows, self._ll_general_stat, sizes, flat, f,
+                                        output_dim, polarised=polarised,
+                                        span_normalise=span_normalise, mode=mode)
+
+    def sample_count_stat(self, sample_sets, f, output_dim, windows=None, polarised=False,
+                          mode=None, span_normalise=True, strict=True):
+        """python/tskit/trees.py:8006-8105: a summary function of the sample
+        counts below each node (sample sets as 0/1 weights)."""
+        for U in sample_sets:
+            if len(U) != len(set(U)):
+                raise ValueError(
+                    "Elements of sample_sets must be lists without repeated elements.")
+            if len(U) == 0:
+                raise ValueError("Elements of sample_sets cannot be empty.")
+            for u in U:
+                if not (0 <= int(u) < self.num_nodes) or not (self.tables.node_flags[u] & 1):
+                    raise ValueError("Not all elements of sample_sets are samples.")
+        if mode is None:
+            mode = "site"
+        sizes = np.array([len(s) for s in sample_sets], dtype=np.uint64)
+        if strict:
+            self._check_summary(sizes.astype(np.float64), f, output_dim)
+        flat = safe_np_int_cast(np.hstack(sample_sets), np.int32)
+        return self.__run_windowed_stat(windows, self._ll_general_stat, sizes, flat, f,
+                                        output_dim, polarised=polarised,
+                                        span_normalise=span_normalise, mode=mode)
+
     # ------------------------------------------------ divergence matrices
     @staticmethod
     def _parse_stat_matrix_sample_sets(ids):
