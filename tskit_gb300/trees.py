@@ -150,6 +150,58 @@ class Query:
             self.handle = None
 
 
+class AfsQuery(Query):
+    """A prepared allele frequency spectrum (device resident); result layout
+    (windows, time windows, *(1 + set sizes))."""
+
+    def __init__(self, ts, sample_sets, windows, time_windows, flags):
+        self._lib = nat.load()
+        self.ts = ts
+        sizes = np.array([len(s) for s in sample_sets], dtype=np.uint64)
+        flat = safe_np_int_cast(np.concatenate([np.asarray(s) for s in sample_sets]), np.int32)
+        win = None if windows is None else np.ascontiguousarray(windows, dtype=np.float64)
+        tw = None if time_windows is None else np.ascontiguousarray(time_windows, np.float64)
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_query_create_afs(
+            ctypes.byref(h), ts._handle, len(sizes), _ptr(sizes), _ptr(flat),
+            0 if win is None else len(win) - 1, _ptr(win), 0 if tw is None else len(tw) - 1,
+            _ptr(tw), flags))
+        self.handle = h
+        self.num_windows = 1 if win is None else len(win) - 1
+        self.shape = ((self.num_windows, 1 if tw is None else len(tw) - 1)
+                      + tuple(int(n) + 1 for n in sizes))
+        self.result_size = self._lib.tsg_query_result_size(h)
+        self.workspace_bytes = self._lib.tsg_query_workspace_bytes(h)
+
+
+class RelatednessVectorQuery(Query):
+    """A prepared branch relatedness matrix-vector product (device
+    resident); ``set_weights`` binds a float64 CUDA tensor (num_samples x
+    columns) read by later launches.  Result layout (windows, focal nodes,
+    columns)."""
+
+    def __init__(self, ts, num_weights, windows, nodes, flags):
+        self._lib = nat.load()
+        self.ts = ts
+        win = None if windows is None else np.ascontiguousarray(windows, dtype=np.float64)
+        focal = np.ascontiguousarray(ts.samples() if nodes is None else nodes, dtype=np.int32)
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_query_create_relatedness_vector(
+            ctypes.byref(h), ts._handle, int(num_weights), 0 if win is None else len(win) - 1,
+            _ptr(win), len(focal), _ptr(focal), flags))
+        self.handle = h
+        self.num_windows = 1 if win is None else len(win) - 1
+        self.shape = (self.num_windows, len(focal), int(num_weights))
+        self.result_size = self._lib.tsg_query_result_size(h)
+        self.workspace_bytes = self._lib.tsg_query_workspace_bytes(h)
+        self._weights = None
+
+    def set_weights(self, weights):
+        self._weights = weights  # keep the tensor alive while launches read it
+        nat.check(self._lib.tsg_query_set_weights(self.handle,
+                                                  ctypes.c_void_p(weights.data_ptr())))
+
+
 class TreeSequence:
     """A tree sequence resident on the GPU with the reference's statistics API."""
 
