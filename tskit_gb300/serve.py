@@ -86,6 +86,11 @@ def poisson_requests(resident, num, rate, seed, window_choices=(1, 10, 100, 1000
         sets = [np.sort(perm[j * m:(j + 1) * m]) for j in range(nsets)]
         weights = None
         if stat == "relatedness_vector":
+            # an output of windows x samples x columns: at most 64 MiB
+            cap = max(1, (64 << 20) // (len(samples) * rv_columns * 8))
+            if nwin > cap:
+                nwin = 1
+                windows = None
             sets = []
             weights = rng.normal(size=(len(samples), rv_columns))
         out.append(Request(rid, t, key, stat, sets, windows, mode, weights))
@@ -127,11 +132,13 @@ class ServeStats:
 class Server:
     """The request loop over a backend (see GpuBackend for the interface)."""
 
-    def __init__(self, backend, num_slots=8, hbm_budget=64 << 30, max_batch=32):
+    def __init__(self, backend, num_slots=8, hbm_budget=64 << 30, max_batch=32,
+                 max_output_bytes=256 << 20):
         self.backend = backend
         self.num_slots = num_slots
         self.hbm_budget = hbm_budget
         self.max_batch = max_batch
+        self.max_output_bytes = max_output_bytes
 
     def _form_batch(self, pending):
         """The oldest waiting request and the compatible ones behind it."""
@@ -141,6 +148,8 @@ class Server:
         if head.kind != "afs":
             sets_cap = self.backend.max_sets(head.ts)
             nsets = len(head.sample_sets)
+            nwin = 1 if head.windows is None else len(head.windows) - 1
+            cols = 0 if head.weights is None else head.weights.shape[1]
             for r in pending[1:]:
                 if len(taken) >= self.max_batch:
                     break
@@ -151,6 +160,11 @@ class Server:
                     if nsets + len(r.sample_sets) > sets_cap:
                         continue
                     nsets += len(r.sample_sets)
+                else:
+                    c = cols + r.weights.shape[1]
+                    if nwin * len(r.weights) * c * 8 > self.max_output_bytes:
+                        continue
+                    cols = c
                 taken.append(r)
         return taken
 
