@@ -48,6 +48,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=[WORKLOAD, "afs_n200k", "grm_n20k", "serve_mix"],
+                    help="the headline workload (default) or one of the other "
+                         "configurations, each printing its own JSON line")
     return ap.parse_args()
 
 
@@ -534,9 +538,258 @@ def run_gpu(args):
         torch.distributed.barrier()
 
 
+
+# ------------------------------------------------------- other configurations
+def _timed_steps(fn, steps, warmup, flush, stream):
+    import torch
+
+    for _ in range(warmup):
+        flush.zero_()
+        fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return float(np.mean(out))
+
+
+def run_afs_n200k(args):
+    """AFS (site, branch; all samples and a joint 2 x 500) in 10 windows and
+    the branch relatedness-vector product with 64 N(0,1) columns, centred, on
+    n=200,000, L=1e8, 1,000,000 breakpoints."""
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _build, _native as nat, sim
+    from tskit_gb300.trees import AfsQuery, RelatednessVectorQuery
+
+    torch.cuda.set_device(0)
+    _build.build_all()
+    lib = nat.load()
+    tables = sim.workload("afs_n200k")
+    seed = sim.WORKLOADS["afs_n200k"]["seed"]
+    rng = np.random.default_rng(seed + 1)
+    perm = rng.permutation(tables.samples())
+    joint = [np.sort(perm[:500]), np.sort(perm[500:1000])]
+    allset = [tables.samples()]
+    L = tables.sequence_length
+    windows = np.linspace(0, L, 11)
+    W = np.random.default_rng(seed + 2).normal(size=(len(tables.samples()), 64))
+    ts = tskit_gb300.TreeSequence(tables)
+    stream = torch.cuda.current_stream()
+    span = nat.STAT_SPAN_NORMALISE
+    qs = [AfsQuery(ts, s, windows, None, m | span)
+          for s in (allset, joint) for m in (nat.STAT_SITE, nat.STAT_BRANCH)]
+    mv = RelatednessVectorQuery(ts, 64, None, None, nat.STAT_BRANCH | span)
+    Wd = torch.from_numpy(W).cuda()
+    mv.set_weights(Wd)
+    qs.append(mv)
+    ws = tskit_gb300.Workspace(max(q.workspace_bytes for q in qs))
+    outs = [torch.zeros(q.result_size, dtype=torch.float64, device="cuda") for q in qs]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        for q, o in zip(qs, outs):
+            q.launch(ws, o, stream)
+
+    launches0 = lib.tsg_launch_count()
+    with ClockSampler(0) as clocks:
+        ms = _timed_steps(step, args.steps, args.warmup, flush, stream)
+    launches = (lib.tsg_launch_count() - launches0) / (args.steps + args.warmup)
+    per_q = []
+    for q, o in zip(qs, outs):
+        per_q.append(_timed_steps(lambda q=q, o=o: q.launch(ws, o, stream), 2, 1, flush, stream))
+    events = edge_events(tables)
+    value = len(qs) * events / (ms / 1e3)
+    # end to end through the host-pointer entry points
+    t0 = time.perf_counter()
+    host = [ts.allele_frequency_spectrum(s, windows=windows, mode=m)
+            for s in (allset, joint) for m in ("site", "branch")]
+    host.append(ts.genetic_relatedness_vector(W, mode="branch"))
+    e2e_s = time.perf_counter() - t0
+    peaks, peak_kind = measured_peaks()
+    algo = len(qs) * (32 * tables.num_edges + 12 * tables.num_nodes + 8 * tables.num_sites
+                      + 13 * tables.num_mutations)
+    line = {
+        "metric": "edge-updates/s", "value": value, "unit": "edge-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int counts; f64 (AFS branch areas exact in 2^-128 fixed point)",
+        "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
+        "config": {"workload": "afs_n200k: n=200000, L=1e8, 1000000 breakpoints -> "
+                               f"{tables.num_edges} edges, {tables.num_sites} sites; AFS "
+                               "site+branch (all samples; joint 2 x 500), 10 windows; "
+                               "relatedness x 64 vectors, branch, centred",
+                   "queries_per_step": len(qs),
+                   "ms_per_query": dict(zip(["afs_site_all", "afs_branch_all", "afs_site_joint",
+                                             "afs_branch_joint", "relatedness_vector_w64"],
+                                            per_q)),
+                   "l2": "flushed between timed steps (256 MiB write)"},
+        "queries_per_s": len(qs) / (ms / 1e3),
+        "e2e": {"value": len(qs) * events / e2e_s, "unit": "edge-updates/s",
+                "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": int(W.nbytes + sum(s.nbytes for s in joint)
+                                          + 2 * allset[0].nbytes),
+                "d2h_bytes_per_step": int(sum(h.nbytes for h in host))},
+        "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": algo / (ms / 1e3) / 1e9 / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peak_kind},
+        "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        ots = O.OracleTS(tables)
+        t0 = time.perf_counter()
+        ref = [O.allele_frequency_spectrum(ots, s, windows=windows, mode=m)
+               for s in (allset, joint) for m in ("site", "branch")]
+        ref.append(O.genetic_relatedness_vector(ots, W))
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(qs) * events / cpu_s, "unit": "edge-updates/s",
+                                "cores": 1, "kind": "port",
+                                "sample": "the full step (4 AFS + 1 relatedness-vector call) "
+                                          "through the C oracle, one core"}
+        line["error_vs_fp64_oracle"] = {
+            name: rel_err(np.asarray(h).reshape(-1), np.asarray(r).reshape(-1))
+            for name, h, r in zip(["afs_site_all", "afs_branch_all", "afs_site_joint",
+                                   "afs_branch_joint", "relatedness_vector_w64"], host, ref)}
+    print(json.dumps(line))
+
+
+def run_grm_n20k(args):
+    """Site-mode genetic relatedness matrix, n=20,000 samples, ~500,000
+    sites: the exact E4M3 Gram on tcgen05 (timed alone on the resident
+    operand) and the whole call (decode, operand, Gram, normalisation, 3.2 GB
+    result to the host)."""
+    import ctypes
+
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _build, _native as nat, sim
+
+    torch.cuda.set_device(0)
+    _build.build_all()
+    lib = nat.load()
+    tables = sim.workload("grm_n20k")
+    ts = tskit_gb300.TreeSequence(tables)
+    n, S = len(tables.samples()), tables.num_sites
+    kp = (S + 127) // 128 * 128
+    G = torch.zeros((n, kp), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_void_p(stream.cuda_stream)
+    nat.check(lib.tsg_treeseq_genotype_operand(ts._handle, 0, S, ctypes.c_void_p(G.data_ptr()),
+                                               kp, st))
+    P = torch.zeros((n, n), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def gram():
+        nat.check(lib.tsg_gram_e4m3(ctypes.c_void_p(G.data_ptr()), n, kp, kp,
+                                    ctypes.c_void_p(P.data_ptr()), n, st))
+
+    with ClockSampler(0) as clocks:
+        ms = _timed_steps(gram, args.steps, args.warmup, flush, stream)
+    tiles = sum(1 for r in range(0, n, 128) for c in range(0, n, 256) if c + 256 > r)
+    executed = tiles * 128 * 256 * kp * 2
+    t0 = time.perf_counter()
+    K = ts.genetic_relatedness_matrix()
+    e2e_s = time.perf_counter() - t0
+    pairs = n * (n - 1) / 2 * S
+    line = {
+        "metric": "sample-pair site comparisons/s", "value": pairs / (ms / 1e3),
+        "unit": "pair-sites/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "e4m3 0/1 operands, fp32 accumulation (exact integers), int32 result",
+        "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
+        "config": {"workload": f"grm_n20k: n={n} samples, {S} sites (L=1e8, 100000 "
+                               "breakpoints); site-mode genetic_relatedness_matrix",
+                   "gram_tiles": tiles, "operand_bytes": int(n * kp),
+                   "l2": "flushed between timed steps (256 MiB write); operand 10 GB"},
+        "e2e": {"value": pairs / e2e_s, "unit": "pair-sites/s", "ms_per_step": e2e_s * 1e3,
+                "h2d_bytes_per_step": int(S * n), "d2h_bytes_per_step": int(K.nbytes)},
+        "roofline": {"bound": "tensor", "achieved": executed / (ms / 1e3) / 1e12,
+                     "peak": 4500.0, "unit": "TFLOP/s",
+                     "frac": executed / (ms / 1e3) / 1e12 / 4500.0, "traffic": None,
+                     "peak_source": "nominal dense FP8 (no measured FP8 peak); "
+                                    "measured bf16 burst " +
+                                    str(measured_peaks()[0].get("bf16_tflops"))},
+        "gpu_launches": 1, "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        # all host cores: FP64 BLAS Gram (exact for these integers) of a site sample
+        sample = 512
+        rng = np.random.default_rng(0)
+        Xs = (rng.random((sample, n)) < 0.05).astype(np.float64)
+        t0 = time.perf_counter()
+        Xs.T @ Xs
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n * (n - 1) / 2 * sample / cpu_s,
+                                "unit": "pair-sites/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": f"FP64 BLAS X^T X over {sample} sites x {n} samples "
+                                          "(numpy, all host threads); the reference's own pair "
+                                          "loop is far slower"}
+    print(json.dumps(line))
+
+
+def run_serve_mix(args):
+    """Eight resident tree sequences (n = 1k..200k, breakpoints = 5n); a
+    Poisson stream of diversity / divergence / Fst / AFS / relatedness x 8
+    requests, served batched and one at a time."""
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _build, sim
+    from tskit_gb300.serve import GpuBackend, Server, poisson_requests
+
+    torch.cuda.set_device(0)
+    _build.build_all()
+    ns = [1000, 2000, 5000, 20000, 20000, 50000, 100000, 200000]
+    resident = {f"n{n}_{i}": tskit_gb300.TreeSequence(sim.simulate(n, 1e8, 5 * n, 5 * n, 2000 + i))
+                for i, n in enumerate(ns)}
+    num = max(50, args.steps * 40)
+    reqs = poisson_requests(resident, num, 50.0, 7)
+    be = GpuBackend(resident, num_slots=8)
+    Server(be, num_slots=8).run(poisson_requests(resident, 40, 1e4, 8))  # warm-up
+    with ClockSampler(0) as clocks:
+        b = Server(be, num_slots=8).run(reqs)
+    p = Server(GpuBackend(resident, num_slots=1), num_slots=1).run(reqs, mode="plain")
+    line = {
+        "metric": "queries/s", "value": b.queries_per_s, "unit": "queries/s", "n_gpus": 1,
+        "steps": num, "warmup": 40, "ms_per_step": 1e3 / b.queries_per_s,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded SMC generator; Poisson arrivals, 50 requests/s)",
+        "config": {"workload": "serve_mix: 8 resident tree sequences n=" + ",".join(map(str, ns))
+                               + ", L=1e8, breakpoints=5n; requests diversity / divergence / Fst "
+                                 "/ AFS / relatedness x 8, sets of 10-10000, 1/10/100/1000 "
+                                 "windows, branch or site",
+                   "batched": b.summary(), "plain_one_at_a_time": p.summary()},
+        "p50_ms": b.percentile_ms(50), "p99_ms": b.percentile_ms(99),
+        "plain": {"queries_per_s": p.queries_per_s, "p50_ms": p.percentile_ms(50),
+                  "p99_ms": p.percentile_ms(99)},
+        "e2e": {"value": b.queries_per_s, "unit": "queries/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+        "gpu_launches": b.launches, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.workload == "afs_n200k":
+        run_afs_n200k(args)
+    elif args.workload == "grm_n20k":
+        run_grm_n20k(args)
+    elif args.workload == "serve_mix":
+        run_serve_mix(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

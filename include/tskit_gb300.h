@@ -235,6 +235,14 @@ int tsg_treeseq_divergence_matrix(const tsg_treeseq_t *self, uint64_t num_sample
 int tsg_treeseq_genetic_relatedness_matrix(const tsg_treeseq_t *self,
     uint64_t num_sample_sets, const uint64_t *sample_set_sizes, const int32_t *sample_sets,
     uint64_t num_windows, const double *windows, uint32_t options, double *result);
+/* The derived-allele indicator of every sample at sites [site_start,
+ * site_stop) as E4M3 bytes (0x38 when the sample carries a derived allele,
+ * else 0x00), one row per sample (G: num_samples x ld bytes, device, column
+ * s - site_start for site s; other columns untouched).  Genotypes as the
+ * reference's variant decoder gives them with isolated samples ancestral
+ * (c/tskit/genotypes.c).  Synchronous on `cuda_stream`. */
+int tsg_treeseq_genotype_operand(const tsg_treeseq_t *self, int64_t site_start,
+    int64_t site_stop, uint8_t *G, int64_t ld, void *cuda_stream);
 /* P = G G^T (int32, upper-triangle 128 x 256 tiles written; P is n x ldp,
  * device) for a device operand G of n rows x ld bytes holding E4M3 0 or 1
  * (0x00 / 0x38), K = k columns (a multiple of 128; ld a multiple of 16).

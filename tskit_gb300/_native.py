@@ -116,6 +116,7 @@ SIGNATURES = {
     "tsg_treeseq_genetic_relatedness_matrix": (
         ctypes.c_int, [_P, _U64, _P, _P, _U64, _P, _U32, _P]),
     "tsg_gram_e4m3": (ctypes.c_int, [_P, _I64, _I64, _I64, _P, _I64, _P]),
+    "tsg_treeseq_genotype_operand": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P]),
     "tsg_general_stat_prepare": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _U64, _P, _U32,
                        ctypes.POINTER(_I64)]),

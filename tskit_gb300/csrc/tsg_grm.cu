@@ -682,6 +682,58 @@ int tsg_treeseq_genetic_relatedness_matrix(const tsg_treeseq_t *self, uint64_t n
         options, true, result);
 }
 
+int tsg_treeseq_genotype_operand(const tsg_treeseq_t *self, int64_t site_start,
+    int64_t site_stop, uint8_t *G, int64_t ld, void *cuda_stream)
+{
+    const int64_t n = self->v.num_samples;
+    if (site_start < 0 || site_stop > self->v.num_sites || site_stop < site_start
+        || ld < site_stop - site_start) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    const int64_t ns = site_stop - site_start;
+    std::unique_ptr<uint8_t[]> A(new (std::nothrow) uint8_t[(size_t) std::max<int64_t>(ns * n, 1)]);
+    if (!A) {
+        return TSG_ERR_NO_MEMORY;
+    }
+    int max_allele = 0;
+    int ret;
+    {
+        tsg_treeseq_t *mts = const_cast<tsg_treeseq_t *>(self);
+        std::lock_guard<std::mutex> lock(mts->sync_mutex);
+        ret = decode_genotypes(self, site_start, site_stop, A.get(), &max_allele);
+    }
+    if (ret != 0 || ns == 0) {
+        return ret;
+    }
+    cudaStream_t st = (cudaStream_t) cuda_stream;
+    uint8_t *dA = nullptr;
+    int64_t *dkb = nullptr;
+    std::vector<int64_t> kb((size_t) ns);
+    for (int64_t s = 0; s < ns; s++) {
+        kb[(size_t) s] = s;
+    }
+    if (cudaMalloc(&dA, (size_t) (ns * n)) != cudaSuccess || cudaMalloc(&dkb, (size_t) ns * 8) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(dA);
+        return TSG_ERR_NO_MEMORY;
+    }
+    ret = 0;
+    if (cudaMemcpyAsync(dA, A.get(), (size_t) (ns * n), cudaMemcpyHostToDevice, st) != cudaSuccess
+        || cudaMemcpyAsync(dkb, kb.data(), (size_t) ns * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    } else {
+        dim3 grid((unsigned) ((ns + 31) / 32), (unsigned) ((n + 31) / 32));
+        k_pack_biallelic<<<grid, 256, 0, st>>>(dA, ns, n, dkb, G, ld);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        }
+    }
+    cudaFree(dA);
+    cudaFree(dkb);
+    return ret;
+}
+
 int tsg_gram_e4m3(const uint8_t *G, int64_t n, int64_t ld, int64_t k, int32_t *P, int64_t ldp,
     void *cuda_stream)
 {
