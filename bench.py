@@ -644,6 +644,7 @@ def run_afs_n200k(args):
         "gpu_launches": launches, "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle as O
 
         ots = O.OracleTS(tables)
