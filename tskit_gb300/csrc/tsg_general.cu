@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256) k_gen_eval_items(TSView ts, QueryParams q
     }
     for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
         const Item<KQ> it = items[i];
-        const double bl = it.tp - it.tu;
+        const double bl = it.bl;
         Pack xn;
         if (it.kind >= TSG_ITEM_LEAF_PLUS) {
             xn = pk_from_mask<W>((uint32_t) it.xn[0], q.K);

@@ -16,7 +16,7 @@ template <int KQ>
 struct Item {
     uint64_t xo[KQ];
     uint64_t xn[KQ];
-    double tu, tp;  // node time and parent time (branch length tp - tu; 0 at a root)
+    double bl;      // branch length: parent time - node time (0 at a root)
     int32_t kind;
     int32_t pad;
 };
@@ -41,8 +41,7 @@ __device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &xo, const Pac
         v.xo[KQ > 1 ? 1 : 0] = xo.hi;
         v.xn[KQ > 1 ? 1 : 0] = xn.hi;
     }
-    v.tu = tu;
-    v.tp = tp;
+    v.bl = tp - tu;
     v.kind = kind;
     v.pad = 0;
     *it = v;
