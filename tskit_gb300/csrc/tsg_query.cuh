@@ -18,6 +18,11 @@ struct QueryParams {
     double set_size[TSG_MAX_SAMPLE_SETS];
     double inv_size[TSG_MAX_SAMPLE_SETS];  // 1 / n_k
     double inv[TSG_MAX_OUTPUTS];           // reciprocal denominator of each term
+    // the same in FP32 (rounded once on the host) for the FP32 evaluation
+    float set_size_f[TSG_MAX_SAMPLE_SETS];
+    float inv_size_f[TSG_MAX_SAMPLE_SETS];
+    float inv_f[TSG_MAX_OUTPUTS];
+    float inv_K_f;
     Term term[TSG_MAX_OUTPUTS];
 };
 

@@ -777,6 +777,9 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     p.f32 = !!(options & TSG_PRECISION_F32_KAHAN);
     for (uint64_t k = 0; k < K; k++) {
         p.set_size[k] = (double) sizes[k];
+        if (sizes[k] >= ((uint64_t) 1 << 23)) {
+            p.f32 = 0;  // the FP32 form needs every count exact in FP32
+        }
     }
     for (uint64_t r = 0; r < R; r++) {
         int wdt = tuple_width(outputs[r].type);
@@ -842,6 +845,14 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         p.inv_size[k] = 1.0 / (double) sizes[k];
     }
     p.inv_K = 1.0 / (double) K;
+    for (uint64_t k = 0; k < K; k++) {
+        p.set_size_f[k] = (float) p.set_size[k];
+        p.inv_size_f[k] = (float) p.inv_size[k];
+    }
+    for (uint64_t r = 0; r < R; r++) {
+        p.inv_f[r] = (float) p.inv[r];
+    }
+    p.inv_K_f = (float) p.inv_K;
 
     // span <-> window overlap tables (host; spans and windows are few)
     const int64_t NS = ts->v.num_spans;

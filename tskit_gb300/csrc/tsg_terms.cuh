@@ -57,6 +57,48 @@ __device__ __forceinline__ Pack pk_from_mask(uint32_t m, int K)
     return p;
 }
 
+// query constants in the evaluation's arithmetic
+template <typename F>
+__device__ __forceinline__ F q_size(const QueryParams &q, int k);
+template <>
+__device__ __forceinline__ float q_size<float>(const QueryParams &q, int k) { return q.set_size_f[k]; }
+template <>
+__device__ __forceinline__ double q_size<double>(const QueryParams &q, int k) { return q.set_size[k]; }
+template <typename F>
+__device__ __forceinline__ F q_rsize(const QueryParams &q, int k);
+template <>
+__device__ __forceinline__ float q_rsize<float>(const QueryParams &q, int k) { return q.inv_size_f[k]; }
+template <>
+__device__ __forceinline__ double q_rsize<double>(const QueryParams &q, int k) { return q.inv_size[k]; }
+template <typename F>
+__device__ __forceinline__ F q_inv(const QueryParams &q, int r);
+template <>
+__device__ __forceinline__ float q_inv<float>(const QueryParams &q, int r) { return q.inv_f[r]; }
+template <>
+__device__ __forceinline__ double q_inv<double>(const QueryParams &q, int r) { return q.inv[r]; }
+template <typename F>
+__device__ __forceinline__ F q_invK(const QueryParams &q);
+template <>
+__device__ __forceinline__ float q_invK<float>(const QueryParams &q) { return q.inv_K_f; }
+template <>
+__device__ __forceinline__ double q_invK<double>(const QueryParams &q) { return q.inv_K; }
+
+// A count (below 2^23, which the FP32 form requires of every set size) as
+// F: for FP32 by placing it in the significand of 2^23 and subtracting 2^23
+// (exact, and on the FP32 pipe).
+template <typename F>
+__device__ __forceinline__ F cnt_to(uint32_t v);
+template <>
+__device__ __forceinline__ float cnt_to<float>(uint32_t v)
+{
+    return __int_as_float((int) (0x4B000000u | v)) - 8388608.0f;
+}
+template <>
+__device__ __forceinline__ double cnt_to<double>(uint32_t v)
+{
+    return (double) v;
+}
+
 template <typename F>
 __device__ __forceinline__ F term_inv(int type, F xi, F xj, F xk, F xl, F ni, F nj, F nk, F nl,
     F inv, F ri, F rj, F meanx)
@@ -102,13 +144,13 @@ __device__ __forceinline__ void pk_means(const QueryParams &q, const Pack &P, F 
 #pragma unroll
         for (int k = 0; k < KM; k++) {
             if (k < q.K) {
-                const F x = (F) pk_get<W>(P, k), n = (F) q.set_size[k], r = (F) q.inv_size[k];
+                const F x = cnt_to<F>(pk_get<W>(P, k)), n = q_size<F>(q, k), r = q_rsize<F>(q, k);
                 mx += x * r;
                 mc += (n - x) * r;
             }
         }
-        mx *= (F) q.inv_K;
-        mc *= (F) q.inv_K;
+        mx *= q_invK<F>(q);
+        mc *= q_invK<F>(q);
     }
 }
 
@@ -117,12 +159,12 @@ template <typename F, bool UNPOL, int W>
 __device__ __forceinline__ F term_F(const QueryParams &q, int r, const Pack &P, F mx, F mc)
 {
     const Term &t = q.term[r];
-    const F ni = (F) q.set_size[t.idx[0]], nj = (F) q.set_size[t.idx[1]];
-    const F nk = (F) q.set_size[t.idx[2]], nl = (F) q.set_size[t.idx[3]];
-    const F ri = (F) q.inv_size[t.idx[0]], rj = (F) q.inv_size[t.idx[1]];
-    const F xi = (F) pk_get<W>(P, t.idx[0]), xj = (F) pk_get<W>(P, t.idx[1]);
-    const F xk = (F) pk_get<W>(P, t.idx[2]), xl = (F) pk_get<W>(P, t.idx[3]);
-    const F inv = (F) q.inv[r];
+    const F ni = q_size<F>(q, t.idx[0]), nj = q_size<F>(q, t.idx[1]);
+    const F nk = q_size<F>(q, t.idx[2]), nl = q_size<F>(q, t.idx[3]);
+    const F ri = q_rsize<F>(q, t.idx[0]), rj = q_rsize<F>(q, t.idx[1]);
+    const F xi = cnt_to<F>(pk_get<W>(P, t.idx[0])), xj = cnt_to<F>(pk_get<W>(P, t.idx[1]));
+    const F xk = cnt_to<F>(pk_get<W>(P, t.idx[2])), xl = cnt_to<F>(pk_get<W>(P, t.idx[3]));
+    const F inv = q_inv<F>(q, r);
     F v = term_inv<F>(t.type, xi, xj, xk, xl, ni, nj, nk, nl, inv, ri, rj, mx);
     if (UNPOL) {
         v += term_inv<F>(t.type, ni - xi, nj - xj, nk - xk, nl - xl, ni, nj, nk, nl, inv, ri, rj, mc);
