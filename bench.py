@@ -119,13 +119,20 @@ def finish(raw, windows, sets, pairs):
 
 
 def rel_err(got, exp):
-    """Max over entries of |got-exp| relative to the magnitude of each statistic
-    column (entries near zero are measured against the column's scale)."""
-    got, exp = np.asarray(got), np.asarray(exp)
-    scale = np.maximum(np.abs(exp), 1e-6 * np.nanmax(np.abs(exp), axis=0, keepdims=True))
+    """Normwise relative error per statistic column, worst column: the
+    largest |got - exp| over the windows divided by the largest |exp| (values
+    near zero, such as Fst between samples of one population, are measured
+    against the statistic's scale)."""
+    got, exp = np.asarray(got, dtype=np.float64), np.asarray(exp, dtype=np.float64)
+    if got.size == 0:
+        return 0.0
+    if got.ndim == 1:
+        got, exp = got[:, None], exp[:, None]
     with np.errstate(invalid="ignore", divide="ignore"):
-        e = np.abs(got - exp) / scale
-    return float(np.nanmax(e)) if e.size else 0.0
+        num = np.nanmax(np.abs(got - exp), axis=0)
+        den = np.nanmax(np.abs(exp), axis=0)
+        e = np.where(den > 0, num / den, num)
+    return float(np.nanmax(e))
 
 
 # --------------------------------------------------------------- CPU side

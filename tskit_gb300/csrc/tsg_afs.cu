@@ -226,8 +226,9 @@ __global__ void __launch_bounds__(512, 1) k_afs_replay(TSView ts, QueryDev qd, A
     constexpr uint32_t NONE = SpanState<IdxT>::NONE;
     unsigned char *base =
         sizeof(IdxT) == 2 ? smem_raw : (unsigned char *) state + (int64_t) blockIdx.x * slot_bytes;
-    const SpanState<IdxT> sp = span_state_at<IdxT>(base, L, KQ);
-    double *last = (double *) (((uintptr_t) (sp.par + L) + 7) & ~(uintptr_t) 7);
+    SpanState<IdxT> sp = span_state_at<IdxT>(base, L, KQ);
+    double *last = (double *) span_state_end(sp, L);
+    sp.cnt = a.seekcnt + (int64_t) blockIdx.x * L;
     const int KC = a.K + 1;
     const int lane = threadIdx.x & 31;
 
@@ -247,6 +248,7 @@ __global__ void __launch_bounds__(512, 1) k_afs_replay(TSView ts, QueryDev qd, A
         const int32_t *l2g = ts.span_l2g + lo;
         const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
         const double xs0 = ts.breakpoints[t0], xe0 = ts.breakpoints[t1];
+        sp.time = ts.span_time + lo;
 
         span_seek<W, KQ, IdxT>(ts, qd, a.err, sp, KC, Ls, l2g, a0, a1);
         for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {

@@ -109,6 +109,7 @@ struct TSView {
     const int2 *span_alive_enc;   // same edges, span-local encoding
     const int64_t *span_local_off;  // num_spans + 1: offsets into span_l2g
     const int32_t *span_l2g;      // stateful nodes of each span (global ids)
+    const double *span_time;      // their times, in the same order
     const int2 *ins_enc;          // insertion order: (parent, child) span-local encoding
     const int2 *rem_enc;          // removal order: (parent, child) span-local encoding
     const int32_t *mut_enc;       // per mutation: span-local encoding of its node
@@ -143,6 +144,7 @@ struct HostTopology {
     std::vector<int32_t> site_mut;             // num_sites + 1
     std::vector<int32_t> mut_node;             // num_mutations
     std::vector<int32_t> mut_allele;           // num_mutations: allele codes
+    std::vector<double> node_time;             // num_nodes
 };
 
 

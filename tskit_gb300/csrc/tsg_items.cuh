@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             ? smem_raw
             : (unsigned char *) w.state + (int64_t) blockIdx.x * slot_bytes,
         L, KQ);
+    sp.cnt = w.seekcnt + (int64_t) blockIdx.x * L;
     const int K = q.K;
     const int lane = threadIdx.x & 31;
     const bool leaf_table = K <= TSG_LEAF_TABLE_KMAX;
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
         const int32_t Ls = (int32_t) (ts.span_local_off[s + 1] - lo);
         const int32_t *l2g = ts.span_l2g + lo;
         const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
+        sp.time = ts.span_time + lo;
 
         span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
 

@@ -384,6 +384,10 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         std::copy(l2g[(size_t) s].begin(), l2g[(size_t) s].end(),
             l2g_flat.begin() + local_off[(size_t) s]);
     }
+    std::vector<double> span_time(l2g_flat.size());
+    for (size_t i = 0; i < l2g_flat.size(); i++) {
+        span_time[i] = h.node_time[(size_t) l2g_flat[i]];
+    }
 
     int32_t *d_span_tree, *d_l2g, *d_mut_enc;
     int64_t *d_alive_off, *d_local_off, *d_tree_item_off, *d_chunk_begin, *d_chunk_end,
@@ -391,6 +395,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
     uint8_t *d_is_parent = nullptr;
     int32_t *d_leaf_index = nullptr, *d_leaves = nullptr;
+    double *d_span_time = nullptr;
     double *d_ins_right = nullptr, *d_ins_lu = nullptr;
     std::vector<int32_t> span_tree_v(st.begin(), st.end());
     if ((ret = upload_vec(ts, span_tree_v, &d_span_tree)) || (ret = upload_vec(ts, alive_off, &d_alive_off))
@@ -405,6 +410,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         || (ret = upload_vec(ts, is_parent, &d_is_parent))
         || (ret = upload_vec(ts, leaf_index, &d_leaf_index))
         || (ret = upload_vec(ts, leaves, &d_leaves))
+        || (ret = upload_vec(ts, span_time, &d_span_time))
         || (ret = upload_vec(ts, ins_right, &d_ins_right))
         || (any_gap && (ret = upload_vec(ts, ins_lu, &d_ins_lu)))) {
         return ret;
@@ -412,6 +418,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     ts->v.node_is_parent = d_is_parent;
     ts->v.leaf_index = d_leaf_index;
     ts->v.leaves = d_leaves;
+    ts->v.span_time = d_span_time;
     ts->v.num_leaves = num_leaves;
     ts->v.ins_right = d_ins_right;
     ts->v.ins_lu = any_gap ? d_ins_lu : nullptr;

@@ -50,6 +50,7 @@ struct WsDev {
     double *rs0;      // R
     void *items;      // replay items (item pipeline)
     void *state;      // per-CTA span node state (item pipeline, global-memory form)
+    uint32_t *seekcnt;    // per-CTA seek counters (item pipeline)
     uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)
     double *dD;       // chunks * R: running-sum change of each item chunk
     uint32_t *node_mask;  // per node sample-set bits
@@ -89,6 +90,7 @@ struct AfsParams {
     double *out;                 // site: Wn * afs_size (the result)
     int32_t *err;
     int32_t *counter;
+    uint32_t *seekcnt;           // per-CTA seek counters
 };
 
 // Allele frequency spectrum launchers (tsg_afs.cu).  form as for the item

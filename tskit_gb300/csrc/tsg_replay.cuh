@@ -71,12 +71,10 @@ __device__ __forceinline__ uint64_t st_ld(const uint64_t *p)
     return __ldcg((const unsigned long long *) p);
 }
 
+// seek counters are in global memory and updated by atomics
 template <typename IdxT>
 __device__ __forceinline__ uint32_t st_ld32(const uint32_t *p)
 {
-    if (sizeof(IdxT) == 2) {
-        return *p;
-    }
     return __ldcg(p);
 }
 
@@ -90,17 +88,24 @@ __device__ __forceinline__ Pack st_load(const SpanState<IdxT> &sp, int64_t l)
 }
 
 // Layout of one span's node state at `base` (L nodes, KQ count words each):
-// time f64, counts, seek counter u32, parent IdxT.
+// counts, then parent ids; the times and seek counters are bound per span.
 template <typename IdxT>
 __device__ __forceinline__ SpanState<IdxT> span_state_at(unsigned char *base, int64_t L, int KQ)
 {
     SpanState<IdxT> sp;
     sp.KQ = KQ;
-    sp.time = (double *) base;
-    sp.xq = (uint64_t *) (sp.time + L);
-    sp.cnt = (uint32_t *) (sp.xq + L * KQ);
-    sp.par = (IdxT *) (sp.cnt + L);
+    sp.time = nullptr;
+    sp.cnt = nullptr;
+    sp.xq = (uint64_t *) base;
+    sp.par = (IdxT *) (sp.xq + L * KQ);
     return sp;
+}
+
+// end of the state area (8-byte aligned), for kernels that add arrays
+template <typename IdxT>
+__device__ __forceinline__ unsigned char *span_state_end(const SpanState<IdxT> &sp, int64_t L)
+{
+    return (unsigned char *) (((uintptr_t) (sp.par + L) + 7) & ~(uintptr_t) 7);
 }
 
 // Rebuild the tree at a span's start in the span state (all threads of the
@@ -115,7 +120,6 @@ __device__ void span_seek(const TSView &ts, const QueryDev &qd, int32_t *err,
     // ---- seek: local nodes start as roots carrying their own weights
     for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
         const int32_t g = l2g[l];
-        sp.time[l] = ts.node_time[g];
         sp.par[l] = (IdxT) TSG_NO_PARENT;
         sp.cnt[l] = 0;
         pk_store(sp, (int64_t) l, pk_from_mask<W>(qd.node_mask[g], K));

@@ -453,10 +453,11 @@ static void *replay_kernel(int W, int KQ)
     return KQ == 1 ? (void *) k_replay_items<32, 1, int32_t> : (void *) k_replay_items<32, 2, int32_t>;
 }
 
-// bytes of one span's node state: time, packed counts, seek counter, parent
+// bytes of one span's node state: packed counts and parent ids (node times
+// come from the span plan, seek counters from per-CTA scratch)
 static int64_t span_state_bytes(int64_t L, int W, int KQ)
 {
-    return L * 8 + L * 8 * KQ + L * 4 + L * (W == 16 ? 2 : 4);
+    return L * 8 * KQ + L * (W == 16 ? 2 : 4);
 }
 
 static int64_t smem_budget()
@@ -1000,6 +1001,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);          // site_val
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
         bytes += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);    // node state
+        bytes += align_up(q->smem_grid * L * 4, 256);                            // seek counters
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -1026,7 +1028,7 @@ static int check_time_windows(uint64_t TW, const double *tw)
 
 // Workspace layout of an allele frequency spectrum query.
 struct AfsLayout {
-    int64_t node_mask, mcnt, state, acc, err, total;
+    int64_t node_mask, mcnt, state, seekcnt, acc, err, total;
 };
 
 static AfsLayout afs_layout(const tsg_query_t *q)
@@ -1040,6 +1042,8 @@ static AfsLayout afs_layout(const tsg_query_t *q)
     off += align_up(q->p.site ? v.num_mutations * 8 * q->KQ : 0, 256);
     l.state = off;
     off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
+    l.seekcnt = off;
+    off += align_up(q->smem_grid * std::max<int64_t>(v.max_local, 1) * 4, 256);
     l.acc = off;
     off += align_up(q->p.branch ? q->afs_bins * TSG_FX_LIMBS * 8 : 0, 256);
     l.err = off;
@@ -1422,6 +1426,7 @@ static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     w.node_mask = (uint32_t *) (b + l.node_mask);
     w.mcnt = (uint64_t *) (b + l.mcnt);
     w.state = b + l.state;
+    w.seekcnt = (uint32_t *) (b + l.seekcnt);
     w.err = (int32_t *) (b + l.err);
     w.counter = w.err + 1;
     AfsParams a = q->afs;
@@ -1429,6 +1434,7 @@ static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     a.out = result;
     a.err = w.err;
     a.counter = w.counter;
+    a.seekcnt = w.seekcnt;
     QueryDev d = q->d;
     d.node_mask = w.node_mask;
     const QueryParams &p = q->p;
@@ -1507,6 +1513,7 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     off += align_up(R * 8, 256);
     w.items = nullptr;
     w.state = nullptr;
+    w.seekcnt = nullptr;
     w.mcnt = nullptr;
     w.dD = nullptr;
     w.node_mask = nullptr;
@@ -1528,6 +1535,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up((int64_t) p.Wn * R * 8, 256);
         w.state = b + off;
         off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
+        w.seekcnt = (uint32_t *) (b + off);
+        off += align_up(q->smem_grid * std::max<int64_t>(ts->v.max_local, 1) * 4, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;

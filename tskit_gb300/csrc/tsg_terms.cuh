@@ -173,12 +173,14 @@ __device__ __forceinline__ F term_F(const QueryParams &q, int r, const Pack &P, 
 }
 
 // Node state of one span.  IdxT: 16-bit ids in shared memory, 32-bit ids in
-// global memory; the all-ones id means "no parent".
+// global memory; the all-ones id means "no parent".  Counts and parents live
+// in the span's state area; node times come from the span plan (read-only,
+// global) and the seek counters from per-CTA global scratch.
 template <typename IdxT>
 struct SpanState {
-    double *time;
-    uint64_t *xq;   // KQ words per node
-    uint32_t *cnt;  // seek counters: children (low 16 bits), arrivals (high 16 bits)
+    const double *time;  // span-local node times
+    uint64_t *xq;        // KQ words per node
+    uint32_t *cnt;       // seek counters: children (low 16 bits), arrivals (high 16 bits)
     IdxT *par;
     int KQ;
     static constexpr uint32_t NONE = (uint32_t) (IdxT) ~(IdxT) 0;

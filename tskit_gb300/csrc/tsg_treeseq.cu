@@ -698,7 +698,8 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
             || (ret = d2h(h.tree_in, tree_in, T + 1)) || (ret = d2h(h.tree_out, tree_out, T + 1))
             || (ret = d2h(h.tree_sites, tree_sites, T + 1))
             || (ret = d2h(h.site_mut, site_mut, S + 1)) || (ret = d2h(h.mut_node, t.mut_node, M))
-            || (ret = d2h(h.mut_allele, t.mut_allele, M))) {
+            || (ret = d2h(h.mut_allele, t.mut_allele, M))
+            || (ret = d2h(h.node_time, t.node_time, N))) {
             goto fail;
         }
         if (num_spans <= 0) {
