@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q,
         }
         for (int64_t i = b + lane; i < e; i += 32) {
             const Item<KQ> it = items[i];
-            const F bl = (F) it.bl;
+            const F bl = sizeof(F) == sizeof(float) ? (F) it.blf : (F) it.bl;
             if (it.kind >= TSG_ITEM_LEAF_PLUS) {
                 const int pat = (int) it.xn[0];
                 const F sb = it.kind == TSG_ITEM_LEAF_PLUS ? bl : -bl;

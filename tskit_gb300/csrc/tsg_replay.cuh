@@ -18,7 +18,7 @@ struct Item {
     uint64_t xn[KQ];
     double bl;      // branch length: parent time - node time (0 at a root)
     int32_t kind;
-    int32_t pad;
+    float blf;      // the branch length rounded to FP32 (for the FP32 evaluation)
 };
 
 template <int KQ>
@@ -43,7 +43,7 @@ __device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &xo, const Pac
     }
     v.bl = tp - tu;
     v.kind = kind;
-    v.pad = 0;
+    v.blf = (float) v.bl;
     *it = v;
 }
 
