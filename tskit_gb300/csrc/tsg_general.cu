@@ -13,6 +13,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include "tsg_fixed.cuh"
 #include "tsg_replay.cuh"
 
 namespace tsg {
@@ -90,6 +91,17 @@ __global__ void __launch_bounds__(256) k_gen_keys_sites(TSView ts, QueryParams q
     const int64_t o = base + site_off[s];
     site_states<W, KQ>(ts, q, mcnt, s, (int32_t) (site_off[s + 1] - site_off[s]),
         [&](int32_t a, const Pack &x) { key_put(klo, khi, o + a, x); });
+}
+
+// the membership pattern of every possible leaf (branch mode: leaves are
+// accounted per pattern)
+template <int W>
+__global__ void k_gen_keys_patterns(int K, uint64_t *klo, uint64_t *khi, int64_t base)
+{
+    const int np = 1 << K;
+    for (int pat = blockIdx.x * blockDim.x + threadIdx.x; pat < np; pat += gridDim.x * blockDim.x) {
+        key_put(klo, khi, base + pat, pk_from_mask<W>((uint32_t) pat, K));
+    }
 }
 
 __global__ void k_gen_flags(const uint64_t *lo, const uint64_t *hi, int64_t n, int64_t *flag)
@@ -226,6 +238,31 @@ __global__ void __launch_bounds__(256) k_gen_eval_sites(TSView ts, QueryParams q
     }
 }
 
+// The leaves' window sums from the table: sum over patterns of F(pattern) x
+// the pattern's branch area in the window.
+template <int W>
+__global__ void __launch_bounds__(256) k_gen_leaf_terms(QueryParams q, WsDev w,
+    const uint64_t *ulo, const uint64_t *uhi, int64_t U, const double *F, int32_t R_total,
+    int32_t r0)
+{
+    const int NP = 1 << q.K;
+    const int64_t total = (int64_t) q.Wn * q.R;
+    for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t) gridDim.x * blockDim.x) {
+        const int64_t wi = idx / q.R;
+        const int r = (int) (idx % q.R);
+        double v = 0;
+        for (int pat = 0; pat < NP; pat++) {
+            const double area = fx_value(w.leaf_area + (wi * NP + pat) * TSG_FX_LIMBS);
+            if (area != 0.0) {
+                const Pack x = pk_from_mask<W>((uint32_t) pat, q.K);
+                v += F[gen_lookup(ulo, uhi, U, x) * R_total + r0 + r] * area;
+            }
+        }
+        w.leaf_win[idx] = v;
+    }
+}
+
 static unsigned gen_grid(int64_t n)
 {
     const int64_t g = (n + 255) / 256;
@@ -240,7 +277,7 @@ int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
     uint64_t *thi, int64_t *flag, int64_t *pos, void *cub_tmp, size_t cub_bytes, uint64_t *ulo,
     uint64_t *uhi, int64_t *U, cudaStream_t st)
 {
-    const int64_t ni = q.branch ? 2 * v.num_items : 0;
+    const int64_t ni = q.branch ? 2 * v.num_items + ((int64_t) 1 << q.K) : 0;
     const int64_t n = ni + (q.site ? num_site_keys : 0);
     if (n == 0) {
         *U = 0;
@@ -252,6 +289,15 @@ int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
             case 1: k_gen_keys_items<16, 2><<<gen_grid(v.num_items), 256, 0, st>>>(v, q, w, klo, khi); break;
             case 2: k_gen_keys_items<32, 1><<<gen_grid(v.num_items), 256, 0, st>>>(v, q, w, klo, khi); break;
             default: k_gen_keys_items<32, 2><<<gen_grid(v.num_items), 256, 0, st>>>(v, q, w, klo, khi); break;
+        }
+        TSG_LAUNCHED();
+    }
+    if (q.branch) {
+        const int64_t base = 2 * v.num_items;
+        if (form < 2) {
+            k_gen_keys_patterns<16><<<gen_grid((int64_t) 1 << q.K), 256, 0, st>>>(q.K, klo, khi, base);
+        } else {
+            k_gen_keys_patterns<32><<<gen_grid((int64_t) 1 << q.K), 256, 0, st>>>(q.K, klo, khi, base);
         }
         TSG_LAUNCHED();
     }
@@ -312,6 +358,15 @@ int gen_eval(int form, const TSView &v, const QueryParams &q, const WsDev &w,
             case 1: k_gen_eval_items<16, 2, 32><<<ge, 256, 0, st>>>(v, q, w, ulo, uhi, U, F, R_total, r0); break;
             case 2: k_gen_eval_items<32, 1, 32><<<ge, 256, 0, st>>>(v, q, w, ulo, uhi, U, F, R_total, r0); break;
             default: k_gen_eval_items<32, 2, 32><<<ge, 256, 0, st>>>(v, q, w, ulo, uhi, U, F, R_total, r0); break;
+        }
+        TSG_LAUNCHED();
+    }
+    if (q.branch) {
+        const unsigned gl = gen_grid((int64_t) q.Wn * q.R);
+        if (form < 2) {
+            k_gen_leaf_terms<16><<<gl, 256, 0, st>>>(q, w, ulo, uhi, U, F, R_total, r0);
+        } else {
+            k_gen_leaf_terms<32><<<gl, 256, 0, st>>>(q, w, ulo, uhi, U, F, R_total, r0);
         }
         TSG_LAUNCHED();
     }

@@ -33,6 +33,7 @@
 
 #pragma once
 
+#include "tsg_fixed.cuh"
 #include "tsg_replay.cuh"
 
 namespace tsg {
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_span;
+    __shared__ int s_scan[32];
     const int64_t L = ts.max_local;
     constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
     SpanState<IdxT> sp = span_state_at<IdxT>(sizeof(IdxT) == 2
@@ -84,17 +86,36 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
 
         span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
 
-        // ---- anchor items: every node alive at the span start
+        // ---- anchor items: every stateful node alive at the span start, in
+        // alive-list order (leaves are accounted per edge, k_leaf_areas)
         const int64_t ibase = ts.tree_item_off[t0];
+        int64_t nanchor = 0;
         if (q.branch) {
-            for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
-                const int2 pc = ts.span_alive_enc[i];
-                const int32_t g = pc.y >= 0 ? l2g[pc.y] : -pc.y - 1;
-                const uint32_t m = qd.node_mask[g];
-                const Pack x = pc.y >= 0 ? st_load(sp, pc.y) : pk_from_mask<W>(m, K);
-                const double tc = pc.y >= 0 ? sp.time[pc.y] : ts.node_time[g];
-                child_item<KQ>(items + ibase + (i - a0), pc.y, m, x, tc, sp.time[pc.x], +1,
-                    leaf_table);
+            for (int64_t base = a0; base < a1; base += blockDim.x) {
+                const int64_t i = base + threadIdx.x;
+                int2 pc = make_int2(0, -1);
+                if (i < a1) {
+                    pc = ts.span_alive_enc[i];
+                }
+                const bool mine = i < a1 && pc.y >= 0;
+                // block-wide exclusive scan of the stateful flags
+                const unsigned bal = __ballot_sync(0xffffffffu, mine);
+                if (lane == 0) {
+                    s_scan[threadIdx.x >> 5] = __popc(bal);
+                }
+                __syncthreads();
+                int64_t before = 0, total = 0;
+                for (int j = 0; j < (int) (blockDim.x >> 5); j++) {
+                    before += j < (int) (threadIdx.x >> 5) ? s_scan[j] : 0;
+                    total += s_scan[j];
+                }
+                __syncthreads();
+                if (mine) {
+                    const int64_t at = nanchor + before + __popc(bal & ((1u << lane) - 1u));
+                    child_item<KQ>(items + ibase + at, pc.y, 0u, st_load(sp, pc.y),
+                        sp.time[pc.y], sp.time[pc.x], +1, leaf_table);
+                }
+                nanchor += total;
             }
         }
 
@@ -104,15 +125,18 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
 
         // ---- replay (warp 0)
         if (threadIdx.x < 32) {
-            int64_t cursor = ibase + (a1 - a0);
-            // one edge event; cm / ct: membership bits and time of a leaf child
+            int64_t cursor = ibase + nanchor;
+            // one edge event; cm: membership bits of a leaf child (whose branch
+            // is accounted per edge, k_leaf_areas)
             auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm, double ct) {
                 const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
-                if (q.branch && lane == 0) {
-                    const double tc = c >= 0 ? sp.time[c] : ct;
-                    child_item<KQ>(items + cursor, c, cm, xc, tc, sp.time[p], sign, leaf_table);
+                if (c >= 0) {
+                    if (q.branch && lane == 0) {
+                        child_item<KQ>(items + cursor, c, cm, xc, sp.time[c], sp.time[p], sign,
+                            leaf_table);
+                    }
+                    cursor++;
                 }
-                cursor++;
                 if (c >= 0) {
                     sp.par[c] = sign > 0 ? (IdxT) p : (IdxT) TSG_NO_PARENT;
                 }
@@ -204,6 +228,64 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             }
         }
         __syncthreads();
+    }
+}
+
+// Leaves (nodes that are never a parent) keep their sample-set bits and
+// their branch is constant while their edge lives, so their part of the
+// branch running sum needs no replay: per window w and membership pattern p,
+// A[w][p] = sum over leaf edges of pattern p of branch length x (the edge's
+// overlap with w), accumulated exactly (tsg_fixed.cuh).
+__global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, QueryDev qd,
+    WsDev w)
+{
+    const int NP = 1 << q.K;
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < ts.num_edges;
+         i += (int64_t) gridDim.x * blockDim.x) {
+        const int32_t c = ts.ins_child[i];
+        if (ts.node_is_parent[c]) {
+            continue;
+        }
+        const uint32_t pat = qd.node_mask[c] & (uint32_t) (NP - 1);
+        const double bl = ts.node_time[ts.ins_parent[i]] - ts.node_time[c];
+        const double left = ts.ins_left[i], right = ts.ins_right[i];
+        int wi = (int) upper_bound(qd.windows, (int64_t) q.Wn + 1, left) - 1;
+        wi = wi < 0 ? 0 : wi;
+        for (; wi < q.Wn && qd.windows[wi] < right; wi++) {
+            const double lo = left > qd.windows[wi] ? left : qd.windows[wi];
+            const double hi = right < qd.windows[wi + 1] ? right : qd.windows[wi + 1];
+            if (hi > lo) {
+                fx_add(w.leaf_area + ((int64_t) wi * NP + pat) * TSG_FX_LIMBS, bl * (hi - lo),
+                    w.err);
+            }
+        }
+    }
+}
+
+// The leaves' window sums: sum over patterns of F_r(pattern) x A[w][pattern]
+// (FP64), one thread per (window, term).
+template <int W>
+__global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
+{
+    const int NP = 1 << q.K;
+    const int64_t total = (int64_t) q.Wn * q.R;
+    for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t) gridDim.x * blockDim.x) {
+        const int64_t wi = idx / q.R;
+        const int r = (int) (idx % q.R);
+        double v = 0;
+        for (int pat = 0; pat < NP; pat++) {
+            const double area = fx_value(w.leaf_area + (wi * NP + pat) * TSG_FX_LIMBS);
+            if (area != 0.0) {
+                const Pack x = pk_from_mask<W>((uint32_t) pat, q.K);
+                double mx, mc;
+                pk_means<double, W>(q, x, mx, mc);
+                const double f = q.polarised ? term_F<double, false, W>(q, r, x, mx, mc)
+                                             : term_F<double, true, W>(q, r, x, mx, mc);
+                v += f * area;
+            }
+        }
+        w.leaf_win[idx] = v;
     }
 }
 

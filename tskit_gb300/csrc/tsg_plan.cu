@@ -198,9 +198,10 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         th.join();
     }
     // Item plan: per tree, the number of items the replay emits -- one per
-    // node alive at the span start (first tree of the span) and, for each edge
-    // event entering a later tree of the span, one for the edge's child plus
-    // one per node on the parent's root path.  The path lengths are
+    // stateful node alive at the span start (first tree of the span) and, for
+    // each edge event entering a later tree of the span, one for the edge's
+    // child when it is stateful (leaves are accounted per edge) plus one per
+    // node on the parent's root path.  The path lengths are
     // topology-only, so the replay is simulated here.
     //
     // The same simulation records the "touches" of the reference's branch
@@ -242,7 +243,11 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                         span_max_children[(size_t) s] = std::max<int64_t>(
                             span_max_children[(size_t) s], ++nch[(size_t) pc.x]);
                     }
-                    tree_items[(size_t) t0] = a1 - a0;
+                    int64_t anchors = 0;
+                    for (int64_t i = a0; i < a1; i++) {
+                        anchors += alive_enc[(size_t) i].y >= 0 ? 1 : 0;
+                    }
+                    tree_items[(size_t) t0] = anchors;
                     double x = 0;
                     auto touch = [&](int32_t l) {
                         lt[(size_t) l] = x;
@@ -268,7 +273,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                                 touch(pc.y);
                                 par[(size_t) pc.y] = -1;
                             }
-                            cnt += 1 + walk(pc.x);
+                            cnt += (pc.y >= 0 ? 1 : 0) + walk(pc.x);
                         }
                         for (int32_t i = h.tree_in[(size_t) t]; i < h.tree_in[(size_t) t + 1]; i++) {
                             const int2 pc = ins_enc[(size_t) i];
@@ -280,7 +285,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                                 }
                                 par[(size_t) pc.y] = pc.x;
                             }
-                            cnt += 1 + walk(pc.x);
+                            cnt += (pc.y >= 0 ? 1 : 0) + walk(pc.x);
                         }
                         if (t < t1) {
                             tree_items[(size_t) t] = cnt;

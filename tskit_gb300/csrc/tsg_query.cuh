@@ -56,6 +56,8 @@ struct WsDev {
     uint32_t *node_mask;  // per node sample-set bits
     double *site_val;     // sites * R: per-site summary (shared-memory sweep)
     double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
+    unsigned long long *leaf_area;  // windows * 2^K patterns: leaf branch areas (fixed point)
+    double *leaf_win;     // windows * R: the leaves' part of the branch sums
     int32_t *err;
     int32_t *counter;
 };
@@ -73,9 +75,11 @@ __device__ __forceinline__ F warp_sum(F v)
 // Allele frequency spectrum of one query.  Counts carry the K sample sets
 // plus a last field with all of the tree sequence's samples.
 #define TSG_AFS_KMAX 7
-// fixed-point accumulation of branch areas: 8 limbs of 32 bits at 2^-128
+// fixed-point accumulation of branch areas (tsg_fixed.cuh)
+#ifndef TSG_FX_LIMBS
 #define TSG_FX_LIMBS 8
 #define TSG_FX_FRAC 128
+#endif
 struct AfsParams {
     int32_t K;              // sample sets
     int32_t Wn, TW;         // windows, time windows

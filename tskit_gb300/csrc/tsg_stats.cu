@@ -525,6 +525,9 @@ __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_no
         if (q.site && items_mode) {
             vs = w.site_win[(int64_t) wdx * R + r];
         }
+        if (q.branch && items_mode && w.leaf_win != nullptr) {
+            vb += w.leaf_win[(int64_t) wdx * R + r];
+        }
         double span = qd.windows[wdx + 1] - qd.windows[wdx];
         if (span_normalise) {
             vb /= span;
@@ -1002,6 +1005,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
         bytes += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);    // node state
         bytes += align_up(q->smem_grid * L * 4, 256);                            // seek counters
+        bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * TSG_FX_LIMBS * 8, 256);  // leaf areas
+        bytes += align_up((int64_t) Wn * R * 8, 256);                            // leaf_win
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -1514,6 +1519,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.items = nullptr;
     w.state = nullptr;
     w.seekcnt = nullptr;
+    w.leaf_area = nullptr;
+    w.leaf_win = nullptr;
     w.mcnt = nullptr;
     w.dD = nullptr;
     w.node_mask = nullptr;
@@ -1537,6 +1544,10 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);
         w.seekcnt = (uint32_t *) (b + off);
         off += align_up(q->smem_grid * std::max<int64_t>(ts->v.max_local, 1) * 4, 256);
+        w.leaf_area = (unsigned long long *) (b + off);
+        off += align_up((p.branch ? (int64_t) p.Wn << p.K : 0) * TSG_FX_LIMBS * 8, 256);
+        w.leaf_win = (double *) (b + off);
+        off += align_up((int64_t) p.Wn * R * 8, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
@@ -1702,6 +1713,18 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             TSG_LAUNCHED();
             k_span_windows<<<(unsigned) ((ts->v.num_spans + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
+            TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
+                (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8, st));
+            if (ts->v.num_edges > 0) {
+                k_leaf_areas<<<grid_for(ts->v.num_edges), 256, 0, st>>>(ts->v, p, d, w);
+                TSG_LAUNCHED();
+            }
+            if (q->W == 16) {
+                k_leaf_terms<16><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
+            } else {
+                k_leaf_terms<32><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
+            }
+            TSG_LAUNCHED();
         }
         if (p.site && ts->v.num_sites > 0) {
             const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
@@ -1852,7 +1875,8 @@ int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint6
         site_off[(size_t) s + 1] = site_off[(size_t) s] + mx + 1;
     }
     g->num_site_keys = site_off[(size_t) v.num_sites];
-    const int64_t n = (p.branch ? 2 * v.num_items : 0) + (p.site ? g->num_site_keys : 0);
+    const int64_t n = (p.branch ? 2 * v.num_items + ((int64_t) 1 << p.K) : 0)
+        + (p.site ? g->num_site_keys : 0);
     const int64_t nk = std::max<int64_t>(n, 1);
     const size_t cub = gen_cub_bytes(nk);
     const int64_t stride = align_up(nk, 32) * 8;
@@ -1893,6 +1917,17 @@ int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint6
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
+    }
+    if (ret == 0 && p.branch) {
+        // the leaves' branch areas per window and membership pattern
+        if (cudaMemsetAsync(w.leaf_area, 0, (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8,
+                st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else if (v.num_edges > 0) {
+            k_leaf_areas<<<grid_for(v.num_edges), 256, 0, st>>>(v, p, g->d, w);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+            ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
+        }
     }
     if (ret == 0) {
         ret = gen_collect(g->form, v, p, w, g->site_off, g->num_site_keys, klo, khi, tlo, thi,
