@@ -460,16 +460,19 @@ static int64_t span_state_bytes(int64_t L, int W, int KQ)
     return L * 8 * KQ + L * (W == 16 ? 2 : 4);
 }
 
-static int64_t smem_budget()
+// Dynamic shared memory a block of `kernel` may have: the device's opt-in
+// maximum less the kernel's static shared memory.
+static int64_t smem_budget(const void *kernel)
 {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaFuncAttributes attr;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess
+        || cudaFuncGetAttributes(&attr, kernel) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
-    // static shared memory of k_replay_items (span id)
-    return (int64_t) optin - 64;
+    return (int64_t) optin - (int64_t) attr.sharedSizeBytes;
 }
 
 // RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r], one block per r, fixed order.
@@ -959,7 +962,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->smem_bytes = align_up(span_state_bytes(L, 16, q->KQ), 16);
     q->slot_bytes = 0;
     if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 65534
-        && q->smem_bytes <= smem_budget() && !(options & TSG_FORCE_GLOBAL_STATE)) {
+        && q->smem_bytes <= smem_budget(replay_kernel(16, q->KQ))
+        && !(options & TSG_FORCE_GLOBAL_STATE)) {
         q->smem = true;
     } else if (items_ok && K <= 4 && ts->v.max_local < INT32_MAX) {
         q->smem = true;
@@ -975,7 +979,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         void *fn = replay_kernel(q->W, q->KQ);
         if (!q->gstate) {
             // a cap, not a reservation: every query of every tree sequence fits
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget());
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
         }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
         int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
@@ -1162,7 +1166,9 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->gstate = false;
     q->smem = true;
     q->slot_bytes = 0;
-    if (!(n <= 65535 && ts->v.max_local <= 65534 && q->smem_bytes <= smem_budget())) {
+    if (!(n <= 65535 && ts->v.max_local <= 65534
+            && q->smem_bytes <= smem_budget(branch ? afs_replay_kernel((KC + 3) / 4 == 1 ? 0 : 1)
+                                                   : replay_kernel(16, (KC + 3) / 4)))) {
         if (KC > 4 || ts->v.max_local >= INT32_MAX) {
             delete q;
             return TSG_ERR_TOO_MANY_SAMPLE_SETS;
@@ -1187,7 +1193,7 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ);
         if (!q->gstate) {
             // a cap, not a reservation: every query of every tree sequence fits
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget());
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
         }
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
