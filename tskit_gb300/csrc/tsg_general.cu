@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_gen_leaf_terms(QueryParams q, WsDev w,
         const int r = (int) (idx % q.R);
         double v = 0;
         for (int pat = 0; pat < NP; pat++) {
-            const double area = fx_value(w.leaf_area + (wi * NP + pat) * TSG_FX_LIMBS);
+            const double area = w.leaf_dbl[wi * NP + pat];
             if (area != 0.0) {
                 const Pack x = pk_from_mask<W>((uint32_t) pat, q.K);
                 v += F[gen_lookup(ulo, uhi, U, x) * R_total + r0 + r] * area;

@@ -233,13 +233,20 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
 
 // Leaves (nodes that are never a parent) keep their sample-set bits and
 // their branch is constant while their edge lives, so their part of the
-// branch running sum needs no replay: per window w and membership pattern p,
-// A[w][p] = sum over leaf edges of pattern p of branch length x (the edge's
-// overlap with w), accumulated exactly (tsg_fixed.cuh).
+// branch running sum needs no replay: per window w and membership pattern p
+// the area A[w][p] = sum over leaf edges of pattern p of branch length x (the
+// edge's overlap with w).  Per edge: the first and last windows it reaches
+// get exact partial areas; the windows in between get its branch length in
+// a difference array (added where they start, subtracted past their end),
+// so that an edge costs at most four exact fixed-point adds
+// (tsg_fixed.cuh) whatever its length.  Layout of w.leaf_area: partial,
+// plus and minus arrays of windows x patterns counters each.
 __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, QueryDev qd,
     WsDev w)
 {
     const int NP = 1 << q.K;
+    const int64_t block = (int64_t) q.Wn * NP * TSG_FX_LIMBS;
+    unsigned long long *part = w.leaf_area, *plus = part + block, *minus = plus + block;
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < ts.num_edges;
          i += (int64_t) gridDim.x * blockDim.x) {
         const int32_t c = ts.ins_child[i];
@@ -249,16 +256,60 @@ __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, Qu
         const uint32_t pat = qd.node_mask[c] & (uint32_t) (NP - 1);
         const double bl = ts.node_time[ts.ins_parent[i]] - ts.node_time[c];
         const double left = ts.ins_left[i], right = ts.ins_right[i];
-        int wi = (int) upper_bound(qd.windows, (int64_t) q.Wn + 1, left) - 1;
-        wi = wi < 0 ? 0 : wi;
-        for (; wi < q.Wn && qd.windows[wi] < right; wi++) {
-            const double lo = left > qd.windows[wi] ? left : qd.windows[wi];
-            const double hi = right < qd.windows[wi + 1] ? right : qd.windows[wi + 1];
-            if (hi > lo) {
-                fx_add(w.leaf_area + ((int64_t) wi * NP + pat) * TSG_FX_LIMBS, bl * (hi - lo),
-                    w.err);
-            }
+        int w0 = (int) upper_bound(qd.windows, (int64_t) q.Wn + 1, left) - 1;
+        int w1 = (int) lower_bound(qd.windows, (int64_t) q.Wn + 1, right) - 1;
+        w0 = w0 < 0 ? 0 : (w0 >= q.Wn ? q.Wn - 1 : w0);
+        w1 = w1 < w0 ? w0 : (w1 >= q.Wn ? q.Wn - 1 : w1);
+        if (w0 == w1) {
+            fx_add(part + ((int64_t) w0 * NP + pat) * TSG_FX_LIMBS, bl * (right - left), w.err);
+            continue;
         }
+        fx_add(part + ((int64_t) w0 * NP + pat) * TSG_FX_LIMBS,
+            bl * (qd.windows[w0 + 1] - left), w.err);
+        fx_add(part + ((int64_t) w1 * NP + pat) * TSG_FX_LIMBS, bl * (right - qd.windows[w1]),
+            w.err);
+        if (w1 > w0 + 1) {
+            fx_add(plus + ((int64_t) (w0 + 1) * NP + pat) * TSG_FX_LIMBS, bl, w.err);
+            fx_add(minus + ((int64_t) w1 * NP + pat) * TSG_FX_LIMBS, bl, w.err);
+        }
+    }
+}
+
+// Per pattern (one thread each): the running sum over windows of the
+// difference array, kept exact as signed 32-bit limbs, gives the branch
+// length alive over each whole window; area = that x window length + the
+// window's partial areas.  w.leaf_dbl: windows x patterns doubles.
+__global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd, WsDev w)
+{
+    const int NP = 1 << q.K;
+    const int pat = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pat >= NP) {
+        return;
+    }
+    const int64_t block = (int64_t) q.Wn * NP * TSG_FX_LIMBS;
+    const unsigned long long *part = w.leaf_area, *plus = part + block, *minus = plus + block;
+    long long run[TSG_FX_LIMBS + 2];
+    for (int i = 0; i < TSG_FX_LIMBS + 2; i++) {
+        run[i] = 0;
+    }
+    for (int wi = 0; wi < q.Wn; wi++) {
+        const int64_t o = ((int64_t) wi * NP + pat) * TSG_FX_LIMBS;
+        for (int i = 0; i < TSG_FX_LIMBS; i++) {
+            run[i] += (long long) plus[o + i] - (long long) minus[o + i];
+        }
+        // carries: every limb but the top back into [0, 2^32)
+        for (int i = 0; i < TSG_FX_LIMBS + 1; i++) {
+            const long long cy = run[i] >> 32;
+            run[i] -= cy * (1ll << 32);
+            run[i + 1] += cy;
+        }
+        double active = 0;
+        for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
+            active = active * 4294967296.0 + (double) run[i];
+        }
+        active = ldexp(active, -TSG_FX_FRAC);
+        w.leaf_dbl[(int64_t) wi * NP + pat] =
+            active * (qd.windows[wi + 1] - qd.windows[wi]) + fx_value(part + o);
     }
 }
 
@@ -275,7 +326,7 @@ __global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
         const int r = (int) (idx % q.R);
         double v = 0;
         for (int pat = 0; pat < NP; pat++) {
-            const double area = fx_value(w.leaf_area + (wi * NP + pat) * TSG_FX_LIMBS);
+            const double area = w.leaf_dbl[wi * NP + pat];
             if (area != 0.0) {
                 const Pack x = pk_from_mask<W>((uint32_t) pat, q.K);
                 double mx, mc;

@@ -56,7 +56,8 @@ struct WsDev {
     uint32_t *node_mask;  // per node sample-set bits
     double *site_val;     // sites * R: per-site summary (shared-memory sweep)
     double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
-    unsigned long long *leaf_area;  // windows * 2^K patterns: leaf branch areas (fixed point)
+    unsigned long long *leaf_area;  // 3 x windows x 2^K patterns: leaf branch areas (fixed point)
+    double *leaf_dbl;     // windows x 2^K patterns: the areas
     double *leaf_win;     // windows * R: the leaves' part of the branch sums
     int32_t *err;
     int32_t *counter;

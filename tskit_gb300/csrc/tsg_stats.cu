@@ -1009,7 +1009,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
         bytes += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);    // node state
         bytes += align_up(q->smem_grid * L * 4, 256);                            // seek counters
-        bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * TSG_FX_LIMBS * 8, 256);  // leaf areas
+        bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * TSG_FX_LIMBS * 8 * 3, 256);  // leaf areas
+        bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * 8, 256);          // leaf_dbl
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // leaf_win
     }
     bytes += 256;                                                     // err, counter
@@ -1526,6 +1527,7 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.state = nullptr;
     w.seekcnt = nullptr;
     w.leaf_area = nullptr;
+    w.leaf_dbl = nullptr;
     w.leaf_win = nullptr;
     w.mcnt = nullptr;
     w.dD = nullptr;
@@ -1551,7 +1553,9 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         w.seekcnt = (uint32_t *) (b + off);
         off += align_up(q->smem_grid * std::max<int64_t>(ts->v.max_local, 1) * 4, 256);
         w.leaf_area = (unsigned long long *) (b + off);
-        off += align_up((p.branch ? (int64_t) p.Wn << p.K : 0) * TSG_FX_LIMBS * 8, 256);
+        off += align_up((p.branch ? (int64_t) p.Wn << p.K : 0) * TSG_FX_LIMBS * 8 * 3, 256);
+        w.leaf_dbl = (double *) (b + off);
+        off += align_up((p.branch ? (int64_t) p.Wn << p.K : 0) * 8, 256);
         w.leaf_win = (double *) (b + off);
         off += align_up((int64_t) p.Wn * R * 8, 256);
     }
@@ -1720,11 +1724,13 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             k_span_windows<<<(unsigned) ((ts->v.num_spans + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
             TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
-                (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8, st));
+                (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, st));
             if (ts->v.num_edges > 0) {
                 k_leaf_areas<<<grid_for(ts->v.num_edges), 256, 0, st>>>(ts->v, p, d, w);
                 TSG_LAUNCHED();
             }
+            k_leaf_prefix<<<(unsigned) (((1 << p.K) + 255) / 256), 256, 0, st>>>(p, d, w);
+            TSG_LAUNCHED();
             if (q->W == 16) {
                 k_leaf_terms<16><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
             } else {
@@ -1926,11 +1932,15 @@ int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint6
     }
     if (ret == 0 && p.branch) {
         // the leaves' branch areas per window and membership pattern
-        if (cudaMemsetAsync(w.leaf_area, 0, (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8,
-                st) != cudaSuccess) {
+        if (cudaMemsetAsync(w.leaf_area, 0,
+                (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, st) != cudaSuccess) {
             ret = TSG_ERR_CUDA;
-        } else if (v.num_edges > 0) {
-            k_leaf_areas<<<grid_for(v.num_edges), 256, 0, st>>>(v, p, g->d, w);
+        } else {
+            if (v.num_edges > 0) {
+                k_leaf_areas<<<grid_for(v.num_edges), 256, 0, st>>>(v, p, g->d, w);
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
+            k_leaf_prefix<<<(unsigned) (((1 << p.K) + 255) / 256), 256, 0, st>>>(p, g->d, w);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
         }
