@@ -275,39 +275,61 @@ __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, Qu
     }
 }
 
-// Per pattern (one thread each): the running sum over windows of the
-// difference array, kept exact as signed 32-bit limbs, gives the branch
-// length alive over each whole window; area = that x window length + the
-// window's partial areas.  w.leaf_dbl: windows x patterns doubles.
+// One block per pattern: the running sum over windows of the difference
+// array (each window's exact plus - minus rounded once, then an FP64 prefix
+// in a fixed order: per-thread runs of windows, a block scan of the run
+// totals) gives the branch length alive over each whole window; area = that
+// x window length + the window's partial areas.  w.leaf_dbl: windows x
+// patterns doubles.
+__device__ __forceinline__ double fx_diff_value(const unsigned long long *a,
+    const unsigned long long *b)
+{
+    long long run[TSG_FX_LIMBS + 2];
+    for (int i = 0; i < TSG_FX_LIMBS; i++) {
+        run[i] = (long long) a[i] - (long long) b[i];
+    }
+    run[TSG_FX_LIMBS] = run[TSG_FX_LIMBS + 1] = 0;
+    for (int i = 0; i < TSG_FX_LIMBS + 1; i++) {
+        const long long cy = run[i] >> 32;
+        run[i] -= cy * (1ll << 32);
+        run[i + 1] += cy;
+    }
+    double v = 0;
+    for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
+        v = v * 4294967296.0 + (double) run[i];
+    }
+    return ldexp(v, -TSG_FX_FRAC);
+}
+
 __global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd, WsDev w)
 {
+    __shared__ double s_run[256];
     const int NP = 1 << q.K;
-    const int pat = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pat >= NP) {
-        return;
-    }
+    const int pat = blockIdx.x;
     const int64_t block = (int64_t) q.Wn * NP * TSG_FX_LIMBS;
     const unsigned long long *part = w.leaf_area, *plus = part + block, *minus = plus + block;
-    long long run[TSG_FX_LIMBS + 2];
-    for (int i = 0; i < TSG_FX_LIMBS + 2; i++) {
-        run[i] = 0;
-    }
-    for (int wi = 0; wi < q.Wn; wi++) {
+    const int per = (q.Wn + blockDim.x - 1) / blockDim.x;
+    const int w0 = threadIdx.x * per, w1 = min(q.Wn, w0 + per);
+    double run = 0;
+    for (int wi = w0; wi < w1; wi++) {
         const int64_t o = ((int64_t) wi * NP + pat) * TSG_FX_LIMBS;
-        for (int i = 0; i < TSG_FX_LIMBS; i++) {
-            run[i] += (long long) plus[o + i] - (long long) minus[o + i];
+        run += fx_diff_value(plus + o, minus + o);
+    }
+    s_run[threadIdx.x] = run;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0;
+        for (int j = 0; j < (int) blockDim.x; j++) {
+            const double v = s_run[j];
+            s_run[j] = acc;
+            acc += v;
         }
-        // carries: every limb but the top back into [0, 2^32)
-        for (int i = 0; i < TSG_FX_LIMBS + 1; i++) {
-            const long long cy = run[i] >> 32;
-            run[i] -= cy * (1ll << 32);
-            run[i + 1] += cy;
-        }
-        double active = 0;
-        for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
-            active = active * 4294967296.0 + (double) run[i];
-        }
-        active = ldexp(active, -TSG_FX_FRAC);
+    }
+    __syncthreads();
+    double active = s_run[threadIdx.x];
+    for (int wi = w0; wi < w1; wi++) {
+        const int64_t o = ((int64_t) wi * NP + pat) * TSG_FX_LIMBS;
+        active += fx_diff_value(plus + o, minus + o);
         w.leaf_dbl[(int64_t) wi * NP + pat] =
             active * (qd.windows[wi + 1] - qd.windows[wi]) + fx_value(part + o);
     }

@@ -1729,7 +1729,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 k_leaf_areas<<<grid_for(ts->v.num_edges), 256, 0, st>>>(ts->v, p, d, w);
                 TSG_LAUNCHED();
             }
-            k_leaf_prefix<<<(unsigned) (((1 << p.K) + 255) / 256), 256, 0, st>>>(p, d, w);
+            k_leaf_prefix<<<(unsigned) (1 << p.K), 256, 0, st>>>(p, d, w);
             TSG_LAUNCHED();
             if (q->W == 16) {
                 k_leaf_terms<16><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
@@ -1940,7 +1940,7 @@ int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint6
                 k_leaf_areas<<<grid_for(v.num_edges), 256, 0, st>>>(v, p, g->d, w);
                 g_launches.fetch_add(1, std::memory_order_relaxed);
             }
-            k_leaf_prefix<<<(unsigned) (((1 << p.K) + 255) / 256), 256, 0, st>>>(p, g->d, w);
+            k_leaf_prefix<<<(unsigned) (1 << p.K), 256, 0, st>>>(p, g->d, w);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
         }
