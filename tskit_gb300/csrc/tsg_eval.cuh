@@ -8,75 +8,98 @@ namespace tsg {
 
 #define TSG_EVAL_GROUP 8
 
+// FP32 compensated accumulation.  The item value bl1 * f1 - bl0 * f0 is
+// formed without rounding as a sum of FP32 terms -- each product split into
+// its rounded value and its exact error by an FMA, their difference by
+// Knuth's TwoSum -- and added to a (hi, lo) pair by TwoSum again.  Item
+// values along one node's history then telescope to the value at the node's
+// current state, so rounding does not build up along the running sum.  The
+// __f*_rn intrinsics keep the compiler from contracting the steps into FMAs.
+__device__ __forceinline__ void acc2_add(float &hi, float &lo, float bl1, float f1, float bl0,
+    float f0)
+{
+    const float p1 = __fmul_rn(bl1, f1);
+    const float e1 = __fmaf_rn(bl1, f1, -p1);
+    const float p0 = __fmul_rn(bl0, f0);
+    const float e0 = __fmaf_rn(bl0, f0, -p0);
+    // s + d == p1 - p0
+    const float s = __fsub_rn(p1, p0);
+    const float z = __fsub_rn(s, p1);
+    const float d = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, z)), __fsub_rn(-p0, z));
+    // t + g == hi + s
+    const float t = __fadd_rn(hi, s);
+    const float y = __fsub_rn(t, hi);
+    const float g = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, y)), __fsub_rn(s, y));
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(g, d), __fsub_rn(e1, e0)));
+}
+
 // Value of every item of a chunk for every term, summed per chunk (one
-// warp per chunk; chunks never cross trees).
+// warp per chunk; chunks never cross trees).  An item is worth
+// F(x1) * bl1 - F(x0) * bl0 (F(x0) is not evaluated when there was no branch
+// before, nor when the counts did not change).  FP64: evaluated as
+// bl * (F(x1) - F(x0)) when the branch length is unchanged (root paths),
+// (bl1 - bl0) * F(x) when the counts are unchanged (moved subtrees), else
+// directly.  FP32: every item exactly, compensated sums (acc2_add).
 template <typename F, bool UNPOL, int RMAX, int W, int KQ>
 __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q, WsDev w)
 {
-    __shared__ F s_leaf[1 << TSG_LEAF_TABLE_KMAX][RMAX];
+    constexpr bool F32 = sizeof(F) == sizeof(float);
     const int lane = threadIdx.x & 31;
     const int R = q.R;
-    if (q.K <= TSG_LEAF_TABLE_KMAX) {
-        // F of every membership pattern a leaf can have
-        const int npat = 1 << q.K;
-        for (int i = threadIdx.x; i < npat * R; i += blockDim.x) {
-            const int pat = i / R, r = i % R;
-            const Pack x = pk_from_mask<W>((uint32_t) pat, q.K);
-            F mx, mc;
-            pk_means<F, W>(q, x, mx, mc);
-            s_leaf[pat][r] = term_F<F, UNPOL, W>(q, r, x, mx, mc);
-        }
-        __syncthreads();
-    }
     const int64_t c = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (c >= ts.num_chunks) {
         return;
     }
     const Item<KQ> *items = (const Item<KQ> *) w.items;
     const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
+    const double *time = ts.span_time + ts.span_local_off[ts.chunk_span[c]];
     // terms in groups of TSG_EVAL_GROUP (accumulators stay in registers); the
     // chunk's items (at most TSG_ITEM_CHUNK / 32 per lane) are re-read from
-    // cache for every group.  Plain sums in F per lane, then FP64.
+    // cache for every group.  Sums in F per lane, then FP64.
     for (int g0 = 0; g0 < R; g0 += TSG_EVAL_GROUP) {
-        F acc[TSG_EVAL_GROUP];
+        F acc[TSG_EVAL_GROUP], lo[TSG_EVAL_GROUP];
 #pragma unroll
         for (int j = 0; j < TSG_EVAL_GROUP; j++) {
             acc[j] = 0;
+            lo[j] = 0;
         }
         for (int64_t i = b + lane; i < e; i += 32) {
             const Item<KQ> it = items[i];
-            const F bl = sizeof(F) == sizeof(float) ? (F) it.blf : (F) it.bl;
-            if (it.kind >= TSG_ITEM_LEAF_PLUS) {
-                const int pat = (int) it.xn[0];
-                const F sb = it.kind == TSG_ITEM_LEAF_PLUS ? bl : -bl;
+            double b0, b1;
+            item_branches<KQ>(it, time, b0, b1);
+            const F bl0 = (F) b0, bl1 = (F) b1;
+            const Pack x0 = item_pack<KQ>(it.x0);
+            const Pack x1 = item_pack<KQ>(it.x1);
+            const bool same = x0.lo == x1.lo && x0.hi == x1.hi;
+            F m1x, m1c;
+            pk_means<F, W>(q, x1, m1x, m1c);
+            if (!same && bl0 != 0) {
+                F m0x, m0c;
+                pk_means<F, W>(q, x0, m0x, m0c);
+                const bool path = bl0 == bl1;
 #pragma unroll
                 for (int j = 0; j < TSG_EVAL_GROUP; j++) {
                     if (g0 + j < R) {
-                        acc[j] += sb * s_leaf[pat][g0 + j];
-                    }
-                }
-                continue;
-            }
-            const Pack xn = item_pack<KQ>(it.xn);
-            F mxn, mcn;
-            pk_means<F, W>(q, xn, mxn, mcn);
-            if (it.kind == TSG_ITEM_PATH) {
-                const Pack xo = item_pack<KQ>(it.xo);
-                F mxo, mco;
-                pk_means<F, W>(q, xo, mxo, mco);
-#pragma unroll
-                for (int j = 0; j < TSG_EVAL_GROUP; j++) {
-                    if (g0 + j < R) {
-                        acc[j] += bl * (term_F<F, UNPOL, W>(q, g0 + j, xn, mxn, mcn)
-                            - term_F<F, UNPOL, W>(q, g0 + j, xo, mxo, mco));
+                        const F f1 = term_F<F, UNPOL, W>(q, g0 + j, x1, m1x, m1c);
+                        const F f0 = term_F<F, UNPOL, W>(q, g0 + j, x0, m0x, m0c);
+                        if constexpr (F32) {
+                            acc2_add(acc[j], lo[j], bl1, f1, bl0, f0);
+                        } else {
+                            acc[j] += path ? bl1 * (f1 - f0) : bl1 * f1 - bl0 * f0;
+                        }
                     }
                 }
             } else {
-                const F sb = it.kind == TSG_ITEM_PLUS ? bl : -bl;
 #pragma unroll
                 for (int j = 0; j < TSG_EVAL_GROUP; j++) {
                     if (g0 + j < R) {
-                        acc[j] += sb * term_F<F, UNPOL, W>(q, g0 + j, xn, mxn, mcn);
+                        const F f1 = term_F<F, UNPOL, W>(q, g0 + j, x1, m1x, m1c);
+                        if constexpr (F32) {
+                            acc2_add(acc[j], lo[j], bl1, f1, bl0, same ? f1 : (F) 0);
+                        } else {
+                            acc[j] += (same ? bl1 - bl0 : bl1) * f1;
+                        }
                     }
                 }
             }
@@ -84,7 +107,7 @@ __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q,
 #pragma unroll
         for (int j = 0; j < TSG_EVAL_GROUP; j++) {
             if (g0 + j < R) {
-                const double v = warp_sum((double) acc[j]);
+                const double v = warp_sum((double) acc[j] + (double) lo[j]);
                 if (lane == j) {
                     w.dD[c * R + g0 + j] = v;
                 }

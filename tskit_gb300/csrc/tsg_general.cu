@@ -24,8 +24,9 @@ __device__ __forceinline__ void key_put(uint64_t *klo, uint64_t *khi, int64_t i,
     khi[i] = x.hi;
 }
 
-// Two keys per item: the counts the item's value reads (old and new for a
-// root-path item, the child's counts twice otherwise).
+// Two keys per item: the counts its value reads (before and after; the
+// "after" counts twice when there was no branch before or the counts did
+// not change).
 template <int W, int KQ>
 __global__ void __launch_bounds__(256) k_gen_keys_items(TSView ts, QueryParams q, WsDev w,
     uint64_t *klo, uint64_t *khi)
@@ -34,13 +35,8 @@ __global__ void __launch_bounds__(256) k_gen_keys_items(TSView ts, QueryParams q
     for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < ts.num_items;
          i += (int64_t) gridDim.x * blockDim.x) {
         const Item<KQ> it = items[i];
-        Pack a, b;
-        if (it.kind >= TSG_ITEM_LEAF_PLUS) {
-            a = b = pk_from_mask<W>((uint32_t) it.xn[0], q.K);
-        } else {
-            b = item_pack<KQ>(it.xn);
-            a = it.kind == TSG_ITEM_PATH ? item_pack<KQ>(it.xo) : b;
-        }
+        const Pack b = item_pack<KQ>(it.x1);
+        const Pack a = it.p0 >= 0 ? item_pack<KQ>(it.x0) : b;
         key_put(klo, khi, 2 * i, a);
         key_put(klo, khi, 2 * i + 1, b);
     }
@@ -156,6 +152,7 @@ __global__ void __launch_bounds__(256) k_gen_eval_items(TSView ts, QueryParams q
         return;
     }
     const Item<KQ> *items = (const Item<KQ> *) w.items;
+    const double *time = ts.span_time + ts.span_local_off[ts.chunk_span[c]];
     double acc[RMAX];
 #pragma unroll
     for (int r = 0; r < RMAX; r++) {
@@ -163,28 +160,26 @@ __global__ void __launch_bounds__(256) k_gen_eval_items(TSView ts, QueryParams q
     }
     for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
         const Item<KQ> it = items[i];
-        const double bl = it.bl;
-        Pack xn;
-        if (it.kind >= TSG_ITEM_LEAF_PLUS) {
-            xn = pk_from_mask<W>((uint32_t) it.xn[0], q.K);
-        } else {
-            xn = item_pack<KQ>(it.xn);
-        }
-        const double *fn = F + gen_lookup(ulo, uhi, U, xn) * R_total + r0;
-        if (it.kind == TSG_ITEM_PATH) {
-            const double *fo = F + gen_lookup(ulo, uhi, U, item_pack<KQ>(it.xo)) * R_total + r0;
+        double bl0, bl1;
+        item_branches<KQ>(it, time, bl0, bl1);
+        const Pack x0 = item_pack<KQ>(it.x0), x1 = item_pack<KQ>(it.x1);
+        const bool same = x0.lo == x1.lo && x0.hi == x1.hi;
+        const double *f1 = F + gen_lookup(ulo, uhi, U, x1) * R_total + r0;
+        if (!same && bl0 != 0) {
+            const double *f0 = F + gen_lookup(ulo, uhi, U, x0) * R_total + r0;
+            const bool path = bl0 == bl1;
 #pragma unroll
             for (int r = 0; r < RMAX; r++) {
                 if (r < R) {
-                    acc[r] += bl * (fn[r] - fo[r]);
+                    acc[r] += path ? bl1 * (f1[r] - f0[r]) : bl1 * f1[r] - bl0 * f0[r];
                 }
             }
         } else {
-            const double sb = (it.kind == TSG_ITEM_PLUS || it.kind == TSG_ITEM_LEAF_PLUS) ? bl : -bl;
+            const double c1 = same ? bl1 - bl0 : bl1;
 #pragma unroll
             for (int r = 0; r < RMAX; r++) {
                 if (r < R) {
-                    acc[r] += sb * fn[r];
+                    acc[r] += c1 * f1[r];
                 }
             }
         }

@@ -118,6 +118,8 @@ struct TSView {
     int64_t num_items;
     const int64_t *chunk_begin;   // evaluation chunks of items (within one tree)
     const int64_t *chunk_end;
+    const int32_t *chunk_span;    // the span whose replay wrote the chunk's items (their
+                                  // node ids are that span's local ids)
     const int64_t *tree_chunk_off;  // num_trees + 1: first chunk of each tree
     int64_t num_chunks;
     // the reference allele frequency spectrum's lazy branch accounting
@@ -133,6 +135,10 @@ struct TSView {
 
 // items per evaluation chunk (one warp)
 #define TSG_ITEM_CHUNK 256
+// nodes one touch list of the item replay holds (a transition touching more
+// stateful nodes closes the list and opens another); the span plan counts
+// items with the same rule
+#define TSG_TOUCH_CAP 256
 
 // Host copies of the topology the span plan is built from.
 struct HostTopology {

@@ -3,33 +3,34 @@
 // The sweep is split so that the sequential part carries no floating point:
 //
 //   k_replay_items  (one CTA per span, state in shared memory, integer only)
-//       seek: rebuild the tree at the span start (parallel); emit one item per
-//       node alive there (its counts and branch length: the running sum of the
-//       first tree is the sum of these items' values, so every span restarts
-//       the sum exactly); then warp 0 replays the span's edge removals and
-//       insertions in reference order, emitting one item for the edge's child
-//       and one per node on the parent's root path (old counts, new counts,
-//       branch length); it also records the counts under every mutation at its
-//       site's tree.  Items land at positions fixed by the span plan, grouped
-//       by tree.  The edge events of a transition are fetched by all lanes at
-//       once (encodings, leaf weights, leaf times) before the sequential part.
-//   k_eval_items    (one warp per tree, fully parallel)
+//       seek: rebuild the tree at the span start (parallel); the first span
+//       also emits one item per stateful node alive in the first tree (its
+//       counts and branch length: the running sum of that tree is the sum of
+//       their values).  Then warp 0 replays the edge removals and insertions
+//       of the transitions into the span's later trees and into the next
+//       span's first tree, in reference order, and emits one item per
+//       stateful node each transition touches (an edge's child, a node on a
+//       root path): counts and branch length before the transition's first
+//       touch and after the transition.  It also records the counts under
+//       every mutation at its site's tree.  Items land at positions fixed by
+//       the span plan, grouped by tree.  The edge events of a transition are
+//       fetched by all lanes at once before the sequential part.
+//   k_eval_items    (one warp per chunk, fully parallel)
 //       the value of every item for every summary term,
-//         path item    bl * (F(new) - F(old))
-//         child item   +- bl * F(x)
-//         leaf item    +- bl * F(pattern), F from a per-block table (K <= 4)
-//       summed per chunk of at most 256 items of one tree (one warp per
-//       chunk, FP32 or FP64 per lane, FP64 across lanes).
+//         F(x1) * bl1 - F(x0) * bl0
+//       summed per chunk of at most 256 items of one tree (FP32 or FP64 per
+//       lane, FP64 across lanes).
 //   k_span_windows  (one warp per span)
 //       the running-sum change of each tree is the sum of its chunks; the
-//       running sum of each tree is the prefix sum of those changes over the
-//       span's trees (FP64); windows accumulate sum * overlap length.
+//       running sum of each tree relative to the span's first tree is the
+//       prefix sum of those changes (FP64); windows accumulate sum * overlap
+//       length; the span's total change goes to k_span_scan, which gives
+//       every span its starting sum (FP64, fixed order).
+//   k_leaf_areas / k_leaf_prefix / k_leaf_terms
+//       the branches of leaves, per edge (below).
 //   k_site_eval / k_site_windows
 //       every site's summary from the integer counts under its mutations
 //       (FP64, one thread per site), then per-window sums in a fixed order.
-//
-// Item values are differences of the summary function at integer counts, so
-// no rounding accumulates across spans.
 
 #pragma once
 
@@ -49,12 +50,13 @@ __global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
 }
 
 template <int W, int KQ, typename IdxT>
-__global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams q, QueryDev qd,
+__global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams q, QueryDev qd,
     WsDev w, int64_t slot_bytes)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_span;
     __shared__ int s_scan[32];
+    __shared__ TouchEntry<KQ> s_list[TSG_TOUCH_CAP];  // the open touch list
     const int64_t L = ts.max_local;
     constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
     SpanState<IdxT> sp = span_state_at<IdxT>(sizeof(IdxT) == 2
@@ -62,9 +64,10 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
             : (unsigned char *) w.state + (int64_t) blockIdx.x * slot_bytes,
         L, KQ);
     sp.cnt = w.seekcnt + (int64_t) blockIdx.x * L;
+    // one bit per stateful node: touched since the touch list was opened
+    uint32_t *touched = (uint32_t *) span_state_end(sp, L);
     const int K = q.K;
     const int lane = threadIdx.x & 31;
-    const bool leaf_table = K <= TSG_LEAF_TABLE_KMAX;
     Item<KQ> *items = (Item<KQ> *) w.items;
 
     for (;;) {
@@ -85,12 +88,18 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
         sp.time = ts.span_time + lo;
 
         span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
-
-        // ---- anchor items: every stateful node alive at the span start, in
-        // alive-list order (leaves are accounted per edge, k_leaf_areas)
-        const int64_t ibase = ts.tree_item_off[t0];
-        int64_t nanchor = 0;
         if (q.branch) {
+            for (int32_t i = threadIdx.x; i < (Ls + 31) / 32; i += blockDim.x) {
+                touched[i] = 0;
+            }
+        }
+
+        // ---- first tree of the sequence: one item per stateful node alive
+        // there, in alive-list order (leaves are accounted per edge,
+        // k_leaf_areas); every later tree's sum follows from the items of
+        // the transitions before it
+        if (q.branch && s == 0) {
+            int64_t nanchor = 0;
             for (int64_t base = a0; base < a1; base += blockDim.x) {
                 const int64_t i = base + threadIdx.x;
                 int2 pc = make_int2(0, -1);
@@ -111,33 +120,87 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                 }
                 __syncthreads();
                 if (mine) {
-                    const int64_t at = nanchor + before + __popc(bal & ((1u << lane) - 1u));
-                    child_item<KQ>(items + ibase + at, pc.y, 0u, st_load(sp, pc.y),
-                        sp.time[pc.y], sp.time[pc.x], +1, leaf_table);
+                    const int64_t at = ts.tree_item_off[t0] + nanchor + before
+                        + __popc(bal & ((1u << lane) - 1u));
+                    if (at < ts.tree_item_off[t0 + 1]) {
+                        item_put<KQ>(items + at, Pack{0, 0}, st_load(sp, pc.y), pc.y, -1, pc.x);
+                    }
                 }
                 nanchor += total;
             }
+            if (threadIdx.x == 0 && ts.tree_item_off[t0] + nanchor != ts.tree_item_off[t0 + 1]) {
+                dev_error(w.err, DEV_ITEM_PLAN);
+            }
         }
 
-        // the anchor items read the first tree's counts: finish them before
-        // the replay starts changing counts and parents
+        // the first-tree items read the first tree's counts and the touch
+        // bits must be clear: both before the replay starts
         __syncthreads();
 
-        // ---- replay (warp 0)
+        // ---- replay (warp 0).  A span replays the transitions into its
+        // trees after the first and, for branch items, into the next span's
+        // first tree.  Every stateful node a transition touches (an edge's
+        // child, a node on a root path) gets one item: its state before the
+        // first touch and after the transition.  The touch list holds at
+        // most TSG_TOUCH_CAP nodes; a longer transition closes the list and
+        // opens a new one (the span plan counts items the same way).
         if (threadIdx.x < 32) {
-            int64_t cursor = ibase + nanchor;
+            int64_t cursor = 0;  // first item of the open list
+            int64_t climit = 0;  // end of the transition's items in the plan
+            int32_t nopen = 0;   // nodes in the open list
+            auto close_list = [&]() {
+                __syncwarp();
+                for (int32_t i = lane; i < nopen; i += 32) {
+                    const TouchEntry<KQ> en = s_list[i];
+                    const uint32_t pu = sp.par[en.u];
+                    if (cursor + i < climit) {
+                        item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
+                            st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
+                            pu != TSG_NO_PARENT ? (int32_t) pu : -1);
+                    }
+                    atomicAnd(&touched[en.u >> 5], ~(1u << (en.u & 31)));
+                }
+                __syncwarp();
+                cursor += nopen;
+                nopen = 0;
+            };
+            // lanes with `active` set touch node u (distinct per lane) whose
+            // counts and parent are still x0, p0.  A node is touched at most
+            // once per edge event and every event ends with __syncwarp, so the
+            // touch bits need no barrier here.
+            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t p0) {
+                bool fresh = active && !((touched[u >> 5] >> (u & 31)) & 1u);
+                unsigned m = __ballot_sync(0xffffffffu, fresh);
+                if (nopen + __popc(m) > TSG_TOUCH_CAP) {
+                    close_list();
+                    fresh = active;
+                    m = __ballot_sync(0xffffffffu, fresh);
+                }
+                if (fresh) {
+                    const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
+                    TouchEntry<KQ> en;
+                    en.x0[0] = x0.lo;
+                    if (KQ > 1) {
+                        en.x0[KQ > 1 ? 1 : 0] = x0.hi;
+                    }
+                    en.u = u;
+                    en.p0 = p0 != TSG_NO_PARENT ? (int32_t) p0 : -1;
+                    s_list[at] = en;
+                    atomicOr(&touched[u >> 5], 1u << (u & 31));
+                    if (cursor + at >= climit) {
+                        dev_error(w.err, DEV_ITEM_PLAN);
+                    }
+                }
+                nopen += __popc(m);
+            };
             // one edge event; cm: membership bits of a leaf child (whose branch
             // is accounted per edge, k_leaf_areas)
-            auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm, double ct) {
+            auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
                 const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
                 if (c >= 0) {
-                    if (q.branch && lane == 0) {
-                        child_item<KQ>(items + cursor, c, cm, xc, sp.time[c], sp.time[p], sign,
-                            leaf_table);
+                    if (q.branch) {
+                        touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c]);
                     }
-                    cursor++;
-                }
-                if (c >= 0) {
                     sp.par[c] = sign > 0 ? (IdxT) p : (IdxT) TSG_NO_PARENT;
                 }
                 uint32_t v = (uint32_t) p;
@@ -159,9 +222,15 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                     if (lane == 31) {
                         up = v;
                     }
-                    const unsigned active = __ballot_sync(0xffffffffu, mine != TSG_NO_PARENT);
-                    if (mine != TSG_NO_PARENT) {
-                        const Pack xo = st_load(sp, (int64_t) mine);
+                    const bool act = mine != TSG_NO_PARENT;
+                    Pack xo{0, 0};
+                    if (act) {
+                        xo = st_load(sp, (int64_t) mine);
+                    }
+                    if (q.branch) {
+                        touch(act, mine, xo, up);
+                    }
+                    if (act) {
                         Pack xn;
                         if (sign > 0) {
                             xn.lo = xo.lo + xc.lo;
@@ -170,19 +239,16 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                             xn.lo = xo.lo - xc.lo;
                             xn.hi = xo.hi - xc.hi;
                         }
-                        if (q.branch) {
-                            const double tu = sp.time[mine];
-                            const double tp = up != TSG_NO_PARENT ? sp.time[up] : tu;
-                            item_put<KQ>(items + cursor + lane, xo, xn, tu, tp, TSG_ITEM_PATH);
-                        }
                         pk_store(sp, (int64_t) mine, xn);
                     }
-                    cursor += __popc(active);
                 }
                 __syncwarp();
             };
-            for (int32_t t = t0; t < t1; t++) {
+            const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;
+            for (int32_t t = t0; t < tend; t++) {
                 if (t > t0) {
+                    cursor = ts.tree_item_off[t];
+                    climit = ts.tree_item_off[t + 1];
                     const int32_t r0 = ts.tree_out[t], nr = ts.tree_out[t + 1] - r0;
                     const int32_t i0 = ts.tree_in[t], ni = ts.tree_in[t + 1] - i0;
                     for (int32_t base = 0; base < nr + ni; base += 32) {
@@ -190,12 +256,10 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                         const int32_t j = base + lane;
                         int2 pc = make_int2(0, 0);
                         uint32_t cm = 0;
-                        double ct = 0;
                         if (j < nr + ni) {
                             pc = j < nr ? ts.rem_enc[r0 + j] : ts.ins_enc[i0 + (j - nr)];
                             if (pc.y < 0) {
                                 cm = qd.node_mask[-pc.y - 1];
-                                ct = ts.node_time[-pc.y - 1];
                             }
                         }
                         const int32_t cnt = min(32, nr + ni - base);
@@ -203,15 +267,17 @@ __global__ void __launch_bounds__(512, 1) k_replay_items(TSView ts, QueryParams 
                             const int32_t p = __shfl_sync(0xffffffffu, pc.x, e);
                             const int32_t c = __shfl_sync(0xffffffffu, pc.y, e);
                             const uint32_t m = __shfl_sync(0xffffffffu, cm, e);
-                            const double tc = __shfl_sync(0xffffffffu, ct, e);
-                            event(p, c, base + e < nr ? -1 : +1, m, tc);
+                            event(p, c, base + e < nr ? -1 : +1, m);
                         }
                     }
-                    if (q.branch && cursor != ts.tree_item_off[t + 1]) {
-                        dev_error(w.err, DEV_ITEM_PLAN);
+                    if (q.branch) {
+                        close_list();
+                        if (cursor != ts.tree_item_off[t + 1]) {
+                            dev_error(w.err, DEV_ITEM_PLAN);
+                        }
                     }
                 }
-                if (q.site) {
+                if (q.site && t < t1) {
                     const int32_t m0 = ts.site_mut[ts.tree_sites[t]];
                     const int32_t m1 = ts.site_mut[ts.tree_sites[t + 1]];
                     for (int32_t m = m0 + lane; m < m1; m += 32) {
@@ -377,15 +443,23 @@ __global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, 
     const int64_t woff = qd.span_woff[s];
     const int64_t nwin = qd.span_woff[s + 1] - woff;
     const double *win = qd.windows;
+    const double slo = ts.breakpoints[t0], shi = ts.breakpoints[t1];
     for (int64_t j = lane; j < nwin * R; j += 32) {
         w.B[woff * R + j] = 0;
     }
+    for (int64_t j = lane; j < nwin; j += 32) {
+        const double a = slo > win[wlo + j] ? slo : win[wlo + j];
+        const double b = shi < win[wlo + j + 1] ? shi : win[wlo + j + 1];
+        w.A[woff + j] = b - a;
+    }
     __syncwarp();
+    // running sum relative to the span's first tree (the first span's first
+    // tree carries the absolute sum)
     double cum = 0;
     int32_t wi = wlo;
     for (int32_t t = t0; t < t1; t++) {
         const double tl = ts.breakpoints[t], tr = ts.breakpoints[t + 1];
-        if (lane < R) {
+        if (lane < R && (t > t0 || s == 0)) {
             for (int64_t c = ts.tree_chunk_off[t]; c < ts.tree_chunk_off[t + 1]; c++) {
                 cum += w.dD[c * R + lane];
             }
@@ -403,6 +477,15 @@ __global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, 
                 break;
             }
         }
+    }
+    // the change into the next span's first tree completes the span's change
+    if (lane < R) {
+        if (t1 < ts.num_trees) {
+            for (int64_t c = ts.tree_chunk_off[t1]; c < ts.tree_chunk_off[t1 + 1]; c++) {
+                cum += w.dD[c * R + lane];
+            }
+        }
+        w.D[s * R + lane] = cum;
     }
 }
 

@@ -197,11 +197,16 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     for (auto &th : pool) {
         th.join();
     }
-    // Item plan: per tree, the number of items the replay emits -- one per
-    // stateful node alive at the span start (first tree of the span) and, for
-    // each edge event entering a later tree of the span, one for the edge's
-    // child when it is stateful (leaves are accounted per edge) plus one per
-    // node on the parent's root path.  The path lengths are
+    // Item plan: per tree, the number of items the replay emits.  The first
+    // tree of the sequence has one per stateful node alive in it; every
+    // later tree t has one per stateful node the transition into t touches
+    // (the child of an edge event when stateful -- leaves are accounted per
+    // edge -- and every node on the parent's root path), counted once per
+    // touch list: the replay keeps at most TSG_TOUCH_CAP nodes in a list
+    // and, when a touch (a single child, or a batch of up to 32 consecutive
+    // path nodes) would overflow it, closes the list and opens a new one.
+    // The transitions into a span's trees after the first and into the next
+    // span's first tree belong to the span.  The path lengths are
     // topology-only, so the replay is simulated here.
     //
     // The same simulation records the "touches" of the reference's branch
@@ -224,9 +229,9 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         std::vector<std::thread> pool2;
         for (unsigned tid = 0; tid < nthreads; tid++) {
             pool2.emplace_back([&, tid]() {
-                std::vector<int32_t> par, nch;
+                std::vector<int32_t> par, nch, path, list;
                 std::vector<double> lt;
-                std::vector<uint8_t> touched;
+                std::vector<uint8_t> touched, listed;
                 for (int64_t s = tid; s < NS; s += nthreads) {
                     const int32_t t0 = st[(size_t) s], t1 = st[(size_t) s + 1];
                     const size_t Ls = l2g[(size_t) s].size();
@@ -234,6 +239,8 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                     nch.assign(Ls, 0);
                     lt.assign(Ls, 0.0);
                     touched.assign(Ls, 0);
+                    listed.assign(Ls, 0);
+                    list.clear();
                     const int64_t a0 = alive_off[(size_t) s], a1 = alive_off[(size_t) s + 1];
                     for (int64_t i = a0; i < a1; i++) {
                         const int2 pc = alive_enc[(size_t) i];
@@ -243,37 +250,71 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                         span_max_children[(size_t) s] = std::max<int64_t>(
                             span_max_children[(size_t) s], ++nch[(size_t) pc.x]);
                     }
-                    int64_t anchors = 0;
-                    for (int64_t i = a0; i < a1; i++) {
-                        anchors += alive_enc[(size_t) i].y >= 0 ? 1 : 0;
+                    if (s == 0) {
+                        int64_t anchors = 0;
+                        for (int64_t i = a0; i < a1; i++) {
+                            anchors += alive_enc[(size_t) i].y >= 0 ? 1 : 0;
+                        }
+                        tree_items[(size_t) t0] = anchors;
                     }
-                    tree_items[(size_t) t0] = anchors;
                     double x = 0;
                     auto touch = [&](int32_t l) {
                         lt[(size_t) l] = x;
                         touched[(size_t) l] = 1;
                     };
-                    // nodes on the root path from v (inclusive), touching them
-                    auto walk = [&](int32_t v) {
-                        int64_t d = 0;
-                        while (v >= 0 && d <= (int64_t) Ls) {
-                            d++;
+                    int64_t cnt = 0;
+                    auto close_list = [&]() {
+                        cnt += (int64_t) list.size();
+                        for (int32_t u : list) {
+                            listed[(size_t) u] = 0;
+                        }
+                        list.clear();
+                    };
+                    // one touch of the nodes path[b, e) (distinct)
+                    auto list_touch = [&](size_t b, size_t e) {
+                        size_t fresh = 0;
+                        for (size_t k = b; k < e; k++) {
+                            fresh += listed[(size_t) path[k]] ? 0 : 1;
+                        }
+                        if (list.size() + fresh > (size_t) TSG_TOUCH_CAP) {
+                            close_list();
+                        }
+                        for (size_t k = b; k < e; k++) {
+                            if (!listed[(size_t) path[k]]) {
+                                listed[(size_t) path[k]] = 1;
+                                list.push_back(path[k]);
+                            }
+                        }
+                    };
+                    // the stateful child c (if any), then the root path from v
+                    auto event = [&](int32_t c, int32_t v) {
+                        if (c >= 0) {
+                            path.assign(1, c);
+                            list_touch(0, 1);
+                        }
+                        path.clear();
+                        while (v >= 0 && path.size() <= Ls) {
                             touch(v);
+                            path.push_back(v);
                             v = par[(size_t) v];
                         }
-                        return d;
+                        for (size_t b = 0; b < path.size(); b += 32) {
+                            list_touch(b, std::min(path.size(), b + 32));
+                        }
                     };
                     const int32_t tlast = t1 < T ? t1 : t1 - 1;
                     for (int32_t t = t0 + 1; t <= tlast; t++) {
                         x = ts->h_breakpoints[(size_t) t];
-                        int64_t cnt = 0;
+                        cnt = 0;
                         for (int32_t i = h.tree_out[(size_t) t]; i < h.tree_out[(size_t) t + 1]; i++) {
                             const int2 pc = rem_enc[(size_t) i];
                             if (pc.y >= 0) {
                                 touch(pc.y);
+                            }
+                            event(pc.y, pc.x);
+                            if (pc.y >= 0) {
                                 par[(size_t) pc.y] = -1;
                             }
-                            cnt += (pc.y >= 0 ? 1 : 0) + walk(pc.x);
                         }
                         for (int32_t i = h.tree_in[(size_t) t]; i < h.tree_in[(size_t) t + 1]; i++) {
                             const int2 pc = ins_enc[(size_t) i];
@@ -285,11 +326,10 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                                 }
                                 par[(size_t) pc.y] = pc.x;
                             }
-                            cnt += (pc.y >= 0 ? 1 : 0) + walk(pc.x);
+                            event(pc.y, pc.x);
                         }
-                        if (t < t1) {
-                            tree_items[(size_t) t] = cnt;
-                        }
+                        close_list();
+                        tree_items[(size_t) t] = cnt;
                     }
                     for (size_t l = 0; l < Ls; l++) {
                         if (touched[l]) {
@@ -378,6 +418,17 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         }
     }
 
+    // the span whose replay writes each chunk's items: the first span for the
+    // first tree, else the span replaying the transition into the tree
+    std::vector<int32_t> chunk_span(chunk_end.size());
+    for (int64_t sidx = 0; sidx < NS; sidx++) {
+        const int32_t ta = sidx == 0 ? 0 : st[(size_t) sidx] + 1;
+        const int32_t tb = sidx + 1 < NS ? st[(size_t) sidx + 1] + 1 : (int32_t) T;
+        for (int64_t c = tree_chunk_off[(size_t) ta]; c < tree_chunk_off[(size_t) tb]; c++) {
+            chunk_span[(size_t) c] = (int32_t) sidx;
+        }
+    }
+
     std::vector<int64_t> local_off((size_t) NS + 1, 0);
     int64_t max_local = 0;
     for (int64_t s = 0; s < NS; s++) {
@@ -395,6 +446,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     }
 
     int32_t *d_span_tree, *d_l2g, *d_mut_enc;
+    int32_t *d_chunk_span;
     int64_t *d_alive_off, *d_local_off, *d_tree_item_off, *d_chunk_begin, *d_chunk_end,
         *d_tree_chunk_off;
     int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
@@ -411,6 +463,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         || (ret = upload_vec(ts, tree_item_off, &d_tree_item_off))
         || (ret = upload_vec(ts, chunk_begin, &d_chunk_begin))
         || (ret = upload_vec(ts, chunk_end, &d_chunk_end))
+        || (ret = upload_vec(ts, chunk_span, &d_chunk_span))
         || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))
         || (ret = upload_vec(ts, is_parent, &d_is_parent))
         || (ret = upload_vec(ts, leaf_index, &d_leaf_index))
@@ -445,6 +498,7 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     }
     ts->v.chunk_begin = d_chunk_begin;
     ts->v.chunk_end = d_chunk_end;
+    ts->v.chunk_span = d_chunk_span;
     ts->v.tree_chunk_off = d_tree_chunk_off;
     ts->v.num_chunks = (int64_t) chunk_end.size();
     ts->v.num_items = tree_item_off[(size_t) T];

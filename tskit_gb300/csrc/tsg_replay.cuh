@@ -5,20 +5,17 @@
 
 namespace tsg {
 
-#define TSG_ITEM_PATH 0
-#define TSG_ITEM_PLUS 1
-#define TSG_ITEM_MINUS 2
-#define TSG_ITEM_LEAF_PLUS 3
-#define TSG_ITEM_LEAF_MINUS 4
-#define TSG_LEAF_TABLE_KMAX 4
-
+// One replay item: a node whose counts or parent changed across one
+// transition (or, at the first tree, a node alive there), with its counts
+// before (x0) and after (x1) and its parent before (p0) and after (p1), as
+// local ids of the span whose replay wrote the item (-1: no parent).  Its
+// value is F(x1) * bl1 - F(x0) * bl0 with bl = time[parent] - time[u]
+// (0 without a parent).
 template <int KQ>
-struct Item {
-    uint64_t xo[KQ];
-    uint64_t xn[KQ];
-    double bl;      // branch length: parent time - node time (0 at a root)
-    int32_t kind;
-    float blf;      // the branch length rounded to FP32 (for the FP32 evaluation)
+struct __align__(16) Item {
+    uint64_t x0[KQ];
+    uint64_t x1[KQ];
+    int32_t u, p0, p1, pad;
 };
 
 template <int KQ>
@@ -31,33 +28,39 @@ __device__ __forceinline__ Pack item_pack(const uint64_t *a)
 }
 
 template <int KQ>
-__device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &xo, const Pack &xn, double tu,
-    double tp, int kind)
+__device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &x0, const Pack &x1, int32_t u,
+    int32_t p0, int32_t p1)
 {
     Item<KQ> v;
-    v.xo[0] = xo.lo;
-    v.xn[0] = xn.lo;
+    v.x0[0] = x0.lo;
+    v.x1[0] = x1.lo;
     if (KQ > 1) {
-        v.xo[KQ > 1 ? 1 : 0] = xo.hi;
-        v.xn[KQ > 1 ? 1 : 0] = xn.hi;
+        v.x0[KQ > 1 ? 1 : 0] = x0.hi;
+        v.x1[KQ > 1 ? 1 : 0] = x1.hi;
     }
-    v.bl = tp - tu;
-    v.kind = kind;
-    v.blf = (float) v.bl;
+    v.u = u;
+    v.p0 = p0;
+    v.p1 = p1;
+    v.pad = 0;
     *it = v;
 }
 
-// item for an edge's child: a leaf (leaf_table) stores its membership bits
+// an entry of the replay's open touch list (shared memory)
 template <int KQ>
-__device__ __forceinline__ void child_item(Item<KQ> *it, int32_t enc, uint32_t mask,
-    const Pack &x, double tu, double tp, int sign, bool leaf_table)
+struct TouchEntry {
+    uint64_t x0[KQ];
+    uint32_t u;
+    int32_t p0;
+};
+
+// branch lengths of an item from its span's node times
+template <int KQ>
+__device__ __forceinline__ void item_branches(const Item<KQ> &it, const double *time, double &bl0,
+    double &bl1)
 {
-    if (enc < 0 && leaf_table) {
-        item_put<KQ>(it, Pack{0, 0}, Pack{(uint64_t) mask, 0}, tu, tp,
-            sign > 0 ? TSG_ITEM_LEAF_PLUS : TSG_ITEM_LEAF_MINUS);
-    } else {
-        item_put<KQ>(it, Pack{0, 0}, x, tu, tp, sign > 0 ? TSG_ITEM_PLUS : TSG_ITEM_MINUS);
-    }
+    const double tu = time[it.u];
+    bl0 = it.p0 >= 0 ? time[it.p0] - tu : 0.0;
+    bl1 = it.p1 >= 0 ? time[it.p1] - tu : 0.0;
 }
 
 // loads of span state that atomics also update: shared memory is coherent;

@@ -475,30 +475,31 @@ static int64_t smem_budget(const void *kernel)
     return (int64_t) optin - (int64_t) attr.sharedSizeBytes;
 }
 
-// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r], one block per r, fixed order.
+// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one warp per r, each lane a
+// contiguous run of spans, then a scan across the lanes (fixed order).
 __global__ void k_span_scan(const double *D, const double *rs0, double *RS, int64_t NS, int R)
 {
-    __shared__ double sm[1024];
-    const int r = blockIdx.x;
-    const int64_t chunk = (NS + blockDim.x - 1) / blockDim.x;
-    const int64_t b = (int64_t) threadIdx.x * chunk;
-    const int64_t e = b + chunk < NS ? b + chunk : NS;
-    double s = 0;
-    for (int64_t i = b; i < e; i++) {
-        s += D[i * R + r];
+    const int lane = threadIdx.x & 31;
+    const int r = (int) (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    if (r >= R) {
+        return;
     }
-    sm[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double acc = rs0[r];
-        for (int j = 0; j < (int) blockDim.x; j++) {
-            double v = sm[j];
-            sm[j] = acc;
-            acc += v;
+    const int64_t run = (NS + 31) / 32;
+    const int64_t b = lane * run < NS ? lane * run : NS;
+    const int64_t e = b + run < NS ? b + run : NS;
+    double sum = 0;
+    for (int64_t i = b; i < e; i++) {
+        sum += D[i * R + r];
+    }
+    double incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) {
+            incl += y;
         }
     }
-    __syncthreads();
-    double acc = sm[threadIdx.x];
+    double acc = __shfl_up_sync(0xffffffffu, incl, 1);
+    acc = rs0[r] + (lane > 0 ? acc : 0.0);
     for (int64_t i = b; i < e; i++) {
         RS[i * R + r] = acc;
         acc += D[i * R + r];
@@ -518,8 +519,7 @@ __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_no
         for (int32_t s = s0; s <= s1; s++) {
             int64_t li = qd.span_woff[s] + (wdx - qd.span_wlo[s]);
             if (q.branch) {
-                vb += items_mode ? w.B[li * R + r]
-                                 : w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
+                vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
             }
             if (q.site && !items_mode) {
                 vs += w.SITE[li * R + r];
@@ -554,6 +554,13 @@ static int grid_for(int64_t n, int block = 256)
 }
 
 static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+// bytes of the item replay's span state: the node state and one touch bit
+// per node
+static int64_t replay_state_bytes(int64_t L, int W, int KQ)
+{
+    return align_up(span_state_bytes(L, W, KQ), 8) + (L + 31) / 32 * 4;
+}
 
 }  // namespace tsg
 
@@ -959,7 +966,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->gstate = false;
     q->W = 16;
     q->KQ = (int) (((int64_t) K + 3) / 4);
-    q->smem_bytes = align_up(span_state_bytes(L, 16, q->KQ), 16);
+    q->smem_bytes = align_up(replay_state_bytes(L, 16, q->KQ), 16);
     q->slot_bytes = 0;
     if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 65534
         && q->smem_bytes <= smem_budget(replay_kernel(16, q->KQ))
@@ -971,7 +978,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         q->W = 32;
         q->KQ = K <= 2 ? 1 : 2;
         q->smem_bytes = 0;
-        q->slot_bytes = align_up(span_state_bytes(L, 32, q->KQ), 256);
+        q->slot_bytes = align_up(replay_state_bytes(L, 32, q->KQ), 256);
     }
     const int64_t KQ = q->KQ;
     if (q->smem) {
@@ -1697,7 +1704,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->ev_start != nullptr) {
         TSG_CUDA(cudaEventRecord(q->ev_start, st));
     }
-    const bool anchored = q->smem;
+    const bool item_pipeline = q->smem;
     QueryDev d = q->d;
     d.node_mask = w.node_mask;
     if (q->smem) {
@@ -1767,12 +1774,12 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->ev_stop != nullptr) {
         TSG_CUDA(cudaEventRecord(q->ev_stop, st));
     }
-    if (p.branch && !anchored) {
-        k_span_scan<<<(unsigned) R, 1024, 0, st>>>(w.D, w.rs0, w.RS, NS, (int) R);
+    if (p.branch) {
+        k_span_scan<<<(unsigned) ((R + 7) / 8), 256, 0, st>>>(w.D, w.rs0, w.RS, NS, (int) R);
         TSG_LAUNCHED();
     }
     k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w, q->span_normalise,
-        anchored ? 1 : 0, result);
+        item_pipeline ? 1 : 0, result);
     TSG_LAUNCHED();
     return 0;
 }
@@ -2019,6 +2026,13 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
         }
         if (pb.branch) {
             k_span_windows<<<(unsigned) ((v.num_spans + 7) / 8), 256, 0, st>>>(v, pb, g->d, g->w);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+            if (cudaMemsetAsync(g->w.rs0, 0, (size_t) pb.R * 8, st) != cudaSuccess) {
+                ret = TSG_ERR_CUDA;
+                break;
+            }
+            k_span_scan<<<(unsigned) ((pb.R + 7) / 8), 256, 0, st>>>(g->w.D, g->w.rs0, g->w.RS,
+                v.num_spans, (int) pb.R);
             g_launches.fetch_add(1, std::memory_order_relaxed);
         }
         if (pb.site) {
