@@ -1,12 +1,11 @@
-// Item evaluation kernel of the item pipeline (instantiated per arithmetic
-// in its own translation unit).
+// Item evaluation of the item pipeline (run by the replay kernel's
+// evaluating warps, instantiated per arithmetic in its own translation unit).
 #pragma once
 
 #include "tsg_replay.cuh"
 
 namespace tsg {
 
-#define TSG_EVAL_GROUP 8
 
 // FP32 compensated accumulation.  The item value bl1 * f1 - bl0 * f0 is
 // formed without rounding as a sum of FP32 terms -- each product split into
@@ -34,33 +33,28 @@ __device__ __forceinline__ void acc2_add(float &hi, float &lo, float bl1, float 
     lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(g, d), __fsub_rn(e1, e0)));
 }
 
-// Value of every item of a chunk for every term, summed per chunk (one
-// warp per chunk; chunks never cross trees).  An item is worth
+// Value of every item of chunk c for every term, summed over the chunk into
+// w.dD (one warp; chunks never cross trees).  An item is worth
 // F(x1) * bl1 - F(x0) * bl0 (F(x0) is not evaluated when there was no branch
 // before, nor when the counts did not change).  FP64: evaluated as
 // bl * (F(x1) - F(x0)) when the branch length is unchanged (root paths),
 // (bl1 - bl0) * F(x) when the counts are unchanged (moved subtrees), else
-// directly.  FP32: every item exactly, compensated sums (acc2_add).
-template <typename F, bool UNPOL, int RMAX, int W, int KQ>
-__global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q, WsDev w)
+// directly.  FP32: every item exactly, compensated sums (acc2_add).  Terms go
+// in groups of GROUP (accumulators in registers); the chunk's items (at most
+// TSG_ITEM_CHUNK / 32 per lane) are re-read from cache for every group.
+template <typename F, bool UNPOL, int W, int KQ, int GROUP>
+__device__ __forceinline__ void eval_chunk(const TSView &ts, const QueryParams &q, const WsDev &w,
+    int64_t c, int lane)
 {
     constexpr bool F32 = sizeof(F) == sizeof(float);
-    const int lane = threadIdx.x & 31;
     const int R = q.R;
-    const int64_t c = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (c >= ts.num_chunks) {
-        return;
-    }
     const Item<KQ> *items = (const Item<KQ> *) w.items;
     const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
     const double *time = ts.span_time + ts.span_local_off[ts.chunk_span[c]];
-    // terms in groups of TSG_EVAL_GROUP (accumulators stay in registers); the
-    // chunk's items (at most TSG_ITEM_CHUNK / 32 per lane) are re-read from
-    // cache for every group.  Sums in F per lane, then FP64.
-    for (int g0 = 0; g0 < R; g0 += TSG_EVAL_GROUP) {
-        F acc[TSG_EVAL_GROUP], lo[TSG_EVAL_GROUP];
+    for (int g0 = 0; g0 < R; g0 += GROUP) {
+        F acc[GROUP], lo[GROUP];
 #pragma unroll
-        for (int j = 0; j < TSG_EVAL_GROUP; j++) {
+        for (int j = 0; j < GROUP; j++) {
             acc[j] = 0;
             lo[j] = 0;
         }
@@ -79,7 +73,7 @@ __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q,
                 pk_means<F, W>(q, x0, m0x, m0c);
                 const bool path = bl0 == bl1;
 #pragma unroll
-                for (int j = 0; j < TSG_EVAL_GROUP; j++) {
+                for (int j = 0; j < GROUP; j++) {
                     if (g0 + j < R) {
                         const F f1 = term_F<F, UNPOL, W>(q, g0 + j, x1, m1x, m1c);
                         const F f0 = term_F<F, UNPOL, W>(q, g0 + j, x0, m0x, m0c);
@@ -92,7 +86,7 @@ __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q,
                 }
             } else {
 #pragma unroll
-                for (int j = 0; j < TSG_EVAL_GROUP; j++) {
+                for (int j = 0; j < GROUP; j++) {
                     if (g0 + j < R) {
                         const F f1 = term_F<F, UNPOL, W>(q, g0 + j, x1, m1x, m1c);
                         if constexpr (F32) {
@@ -105,7 +99,7 @@ __global__ void __launch_bounds__(256, 3) k_eval_items(TSView ts, QueryParams q,
             }
         }
 #pragma unroll
-        for (int j = 0; j < TSG_EVAL_GROUP; j++) {
+        for (int j = 0; j < GROUP; j++) {
             if (g0 + j < R) {
                 const double v = warp_sum((double) acc[j] + (double) lo[j]);
                 if (lane == j) {

@@ -1,5 +1,6 @@
-// Item evaluation, FP32 per lane, unpolarised.
+// Item replay with evaluation, FP32 per lane, unpolarised.
 #define TSG_EVAL_F float
 #define TSG_EVAL_UNPOL true
-#define TSG_EVAL_NAME launch_eval_f32_unpol
+#define TSG_EVAL_NAME launch_replay_eval_f32_unpol
+#define TSG_EVAL_FN replay_eval_fn_f32_unpol
 #include "tsg_eval_inst.cuh"

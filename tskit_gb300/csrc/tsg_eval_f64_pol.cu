@@ -1,5 +1,6 @@
-// Item evaluation, FP64 per lane, polarised.
+// Item replay with evaluation, FP64 per lane, polarised.
 #define TSG_EVAL_F double
 #define TSG_EVAL_UNPOL false
-#define TSG_EVAL_NAME launch_eval_f64_pol
+#define TSG_EVAL_NAME launch_replay_eval_f64_pol
+#define TSG_EVAL_FN replay_eval_fn_f64_pol
 #include "tsg_eval_inst.cuh"

@@ -1,5 +1,6 @@
-// Item evaluation, FP64 per lane, unpolarised.
+// Item replay with evaluation, FP64 per lane, unpolarised.
 #define TSG_EVAL_F double
 #define TSG_EVAL_UNPOL true
-#define TSG_EVAL_NAME launch_eval_f64_unpol
+#define TSG_EVAL_NAME launch_replay_eval_f64_unpol
+#define TSG_EVAL_FN replay_eval_fn_f64_unpol
 #include "tsg_eval_inst.cuh"

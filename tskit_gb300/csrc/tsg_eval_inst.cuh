@@ -1,27 +1,41 @@
-// One arithmetic x polarisation of the item evaluation: the instantiations
-// of k_eval_items for every count form and the launcher that picks one.
+// One arithmetic x polarisation of the item pipeline: the replay kernel with
+// item evaluation for every count form, its launcher and its kernel handle.
 // Included by a translation unit that defines TSG_EVAL_F (float or double),
-// TSG_EVAL_UNPOL (true or false) and TSG_EVAL_NAME (the launcher's name), so
-// that the instantiations compile in parallel.
-#include "tsg_eval.cuh"
+// TSG_EVAL_UNPOL (true or false), TSG_EVAL_NAME (the launcher's name) and
+// TSG_EVAL_FN (the handle's name), so that the instantiations compile in
+// parallel.
+#include "tsg_replay_kernel.cuh"
 
 namespace tsg {
 
-void TSG_EVAL_NAME(int form, unsigned grid, cudaStream_t st, const TSView &v,
-    const QueryParams &p, const WsDev &w)
+TSG_REPLAY_EVAL_FN(TSG_EVAL_FN)
+{
+    switch (form) {
+        case 0: return (void *) k_replay_items<16, 1, uint16_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>;
+        case 1: return (void *) k_replay_items<16, 2, uint16_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>;
+        case 2: return (void *) k_replay_items<32, 1, int32_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>;
+        default: return (void *) k_replay_items<32, 2, int32_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>;
+    }
+}
+
+TSG_REPLAY_EVAL_LAUNCHER(TSG_EVAL_NAME)
 {
     switch (form) {
         case 0:
-            k_eval_items<TSG_EVAL_F, TSG_EVAL_UNPOL, TSG_ITEM_RMAX, 16, 1><<<grid, 256, 0, st>>>(v, p, w);
+            k_replay_items<16, 1, uint16_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>
+                <<<grid, 512, smem, st>>>(v, p, d, w, 0);
             break;
         case 1:
-            k_eval_items<TSG_EVAL_F, TSG_EVAL_UNPOL, TSG_ITEM_RMAX, 16, 2><<<grid, 256, 0, st>>>(v, p, w);
+            k_replay_items<16, 2, uint16_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>
+                <<<grid, 512, smem, st>>>(v, p, d, w, 0);
             break;
         case 2:
-            k_eval_items<TSG_EVAL_F, TSG_EVAL_UNPOL, TSG_ITEM_RMAX, 32, 1><<<grid, 256, 0, st>>>(v, p, w);
+            k_replay_items<32, 1, int32_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>
+                <<<grid, 512, 0, st>>>(v, p, d, w, slot_bytes);
             break;
         default:
-            k_eval_items<TSG_EVAL_F, TSG_EVAL_UNPOL, TSG_ITEM_RMAX, 32, 2><<<grid, 256, 0, st>>>(v, p, w);
+            k_replay_items<32, 2, int32_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>
+                <<<grid, 512, 0, st>>>(v, p, d, w, slot_bytes);
             break;
     }
 }

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) k_gen_eval_sites(TSView ts, QueryParams q
 #pragma unroll
     for (int r = 0; r < RMAX; r++) {
         if (r < R) {
-            w.site_val[s * R + r] = val[r];
+            w.site_val[(int64_t) r * ts.num_sites + s] = val[r];
         }
     }
 }

@@ -47,6 +47,7 @@ enum DeviceError : int32_t {
     DEV_BAD_MUTATION = 7,
     DEV_ITEM_PLAN = 8,
     DEV_AFS_RANGE = 9,
+    DEV_WAIT_TIMEOUT = 10,
 };
 
 __device__ __forceinline__ void dev_error(int32_t *flag, int32_t code)
@@ -118,6 +119,12 @@ struct TSView {
     int64_t num_items;
     const int64_t *chunk_begin;   // evaluation chunks of items (within one tree)
     const int64_t *chunk_end;
+    const int4 *tree_ev;          // num_trees: the edge events into each tree (removal
+                                  // offset, removals, insertion offset, insertions)
+    const int2 *tree_mut;         // num_trees: each tree's mutations [first, end)
+    int64_t num_segs;             // window segments: runs of consecutive trees whose
+    const int32_t *seg_tree;      // running sums are windowed together (num_segs + 1)
+    const int32_t *chunk_tree;    // the tree of each chunk's items
     const int32_t *chunk_span;    // the span whose replay wrote the chunk's items (their
                                   // node ids are that span's local ids)
     const int64_t *tree_chunk_off;  // num_trees + 1: first chunk of each tree
@@ -177,6 +184,7 @@ struct tsg_treeseq {
     // host copies of small derived arrays
     std::vector<double> h_breakpoints;
     std::vector<int32_t> h_span_tree;
+    std::vector<int32_t> h_seg_tree;
     std::vector<uint32_t> h_node_flags;
     std::vector<int32_t> h_sample_index;
     std::vector<int64_t> h_local_off;

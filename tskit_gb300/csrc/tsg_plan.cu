@@ -418,9 +418,35 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         }
     }
 
+    // window segments: about 4,096 runs of consecutive trees, each windowed
+    // by one warp (k_span_windows)
+    const int64_t seg_len = std::max<int64_t>(1, (T + 4095) / 4096);
+    auto &seg_tree = ts->h_seg_tree;
+    seg_tree.clear();
+    for (int64_t t = 0; t < T; t += seg_len) {
+        seg_tree.push_back((int32_t) t);
+    }
+    seg_tree.push_back((int32_t) T);
+
+    // per tree: its edge events and its mutations, one load each for the replay
+    std::vector<int4> tree_ev((size_t) T);
+    std::vector<int2> tree_mut((size_t) T);
+    for (int64_t t = 0; t < T; t++) {
+        const int32_t r0 = h.tree_out[(size_t) t], i0 = h.tree_in[(size_t) t];
+        tree_ev[(size_t) t] = make_int4(r0, h.tree_out[(size_t) t + 1] - r0, i0,
+            h.tree_in[(size_t) t + 1] - i0);
+        tree_mut[(size_t) t] = make_int2(h.site_mut[(size_t) h.tree_sites[(size_t) t]],
+            h.site_mut[(size_t) h.tree_sites[(size_t) t + 1]]);
+    }
+
     // the span whose replay writes each chunk's items: the first span for the
     // first tree, else the span replaying the transition into the tree
-    std::vector<int32_t> chunk_span(chunk_end.size());
+    std::vector<int32_t> chunk_span(chunk_end.size()), chunk_tree(chunk_end.size());
+    for (int64_t t = 0; t < T; t++) {
+        for (int64_t c = tree_chunk_off[(size_t) t]; c < tree_chunk_off[(size_t) t + 1]; c++) {
+            chunk_tree[(size_t) c] = (int32_t) t;
+        }
+    }
     for (int64_t sidx = 0; sidx < NS; sidx++) {
         const int32_t ta = sidx == 0 ? 0 : st[(size_t) sidx] + 1;
         const int32_t tb = sidx + 1 < NS ? st[(size_t) sidx + 1] + 1 : (int32_t) T;
@@ -446,7 +472,9 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     }
 
     int32_t *d_span_tree, *d_l2g, *d_mut_enc;
-    int32_t *d_chunk_span;
+    int32_t *d_chunk_span, *d_chunk_tree, *d_seg_tree;
+    int4 *d_tree_ev;
+    int2 *d_tree_mut;
     int64_t *d_alive_off, *d_local_off, *d_tree_item_off, *d_chunk_begin, *d_chunk_end,
         *d_tree_chunk_off;
     int2 *d_alive, *d_alive_enc, *d_ins_enc, *d_rem_enc;
@@ -464,6 +492,10 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
         || (ret = upload_vec(ts, chunk_begin, &d_chunk_begin))
         || (ret = upload_vec(ts, chunk_end, &d_chunk_end))
         || (ret = upload_vec(ts, chunk_span, &d_chunk_span))
+        || (ret = upload_vec(ts, chunk_tree, &d_chunk_tree))
+        || (ret = upload_vec(ts, seg_tree, &d_seg_tree))
+        || (ret = upload_vec(ts, tree_ev, &d_tree_ev))
+        || (ret = upload_vec(ts, tree_mut, &d_tree_mut))
         || (ret = upload_vec(ts, tree_chunk_off, &d_tree_chunk_off))
         || (ret = upload_vec(ts, is_parent, &d_is_parent))
         || (ret = upload_vec(ts, leaf_index, &d_leaf_index))
@@ -499,6 +531,11 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     ts->v.chunk_begin = d_chunk_begin;
     ts->v.chunk_end = d_chunk_end;
     ts->v.chunk_span = d_chunk_span;
+    ts->v.chunk_tree = d_chunk_tree;
+    ts->v.seg_tree = d_seg_tree;
+    ts->v.num_segs = (int64_t) seg_tree.size() - 1;
+    ts->v.tree_ev = d_tree_ev;
+    ts->v.tree_mut = d_tree_mut;
     ts->v.tree_chunk_off = d_tree_chunk_off;
     ts->v.num_chunks = (int64_t) chunk_end.size();
     ts->v.num_items = tree_item_off[(size_t) T];

@@ -13,6 +13,7 @@ struct Term {
 struct QueryParams {
     int32_t K, KP, R, Wn;
     int32_t branch, site, polarised, f32, need_mean;
+    int32_t site_int;  // site summaries from exact integer numerators (term_num)
     int32_t num_slots;
     double inv_K;
     double set_size[TSG_MAX_SAMPLE_SETS];
@@ -35,6 +36,11 @@ struct QueryDev {
     const int64_t *span_woff;     // per span: offset into span-window arrays
     const int32_t *win_span_lo;   // per window: first overlapping span
     const int32_t *win_span_hi;   // per window: last overlapping span
+    // the same for the window segments (item pipeline)
+    const int32_t *seg_wlo;
+    const int64_t *seg_woff;
+    const int32_t *win_seg_lo;
+    const int32_t *win_seg_hi;
 };
 
 struct WsDev {
@@ -54,7 +60,7 @@ struct WsDev {
     uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)
     double *dD;       // chunks * R: running-sum change of each item chunk
     uint32_t *node_mask;  // per node sample-set bits
-    double *site_val;     // sites * R: per-site summary (shared-memory sweep)
+    double *site_val;     // R * sites: per-site summary, term-major (item pipeline)
     double *site_win;     // windows * R: per-window site sums (shared-memory sweep)
     unsigned long long *leaf_area;  // 3 x windows x 2^K patterns: leaf branch areas (fixed point)
     double *leaf_dbl;     // windows x 2^K patterns: the areas
@@ -157,15 +163,21 @@ int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K
 // term budget of the item evaluation (accumulators per lane)
 #define TSG_ITEM_RMAX 32
 
-// Item evaluation launchers (tsg_eval_*.cu), FP32/FP64 x polarised/unpolarised.
-// form: count width and words, (W == 16 ? 0 : 2) + (KQ == 1 ? 0 : 1).
-#define TSG_EVAL_LAUNCHER(name)                                                          \
-    void name(int form, unsigned grid, cudaStream_t st, const TSView &v,                 \
-        const QueryParams &p, const WsDev &w)
-TSG_EVAL_LAUNCHER(launch_eval_f32_pol);
-TSG_EVAL_LAUNCHER(launch_eval_f32_unpol);
-TSG_EVAL_LAUNCHER(launch_eval_f64_pol);
-TSG_EVAL_LAUNCHER(launch_eval_f64_unpol);
+// Item replay with evaluation (tsg_eval_*.cu), FP32/FP64 x polarised/unpolarised:
+// launchers and kernel handles.  form: count width and words,
+// (W == 16 ? 0 : 2) + (KQ == 1 ? 0 : 1).
+#define TSG_REPLAY_EVAL_LAUNCHER(name)                                                   \
+    void name(int form, unsigned grid, size_t smem, int64_t slot_bytes, cudaStream_t st, \
+        const TSView &v, const QueryParams &p, const QueryDev &d, const WsDev &w)
+#define TSG_REPLAY_EVAL_FN(name) void *name(int form)
+TSG_REPLAY_EVAL_LAUNCHER(launch_replay_eval_f32_pol);
+TSG_REPLAY_EVAL_LAUNCHER(launch_replay_eval_f32_unpol);
+TSG_REPLAY_EVAL_LAUNCHER(launch_replay_eval_f64_pol);
+TSG_REPLAY_EVAL_LAUNCHER(launch_replay_eval_f64_unpol);
+TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_pol);
+TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_unpol);
+TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_pol);
+TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_unpol);
 
 }  // namespace tsg
 

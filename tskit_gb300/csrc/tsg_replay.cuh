@@ -45,6 +45,43 @@ __device__ __forceinline__ void item_put(Item<KQ> *it, const Pack &x0, const Pac
     *it = v;
 }
 
+// Asynchronous global -> shared copies (cp.async, sm_80 and later): the
+// item replay stages each tree's inputs a few trees ahead of use.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// One tree's replay inputs, staged in shared memory ahead of use: the edge
+// events into the tree, its mutations, its item range, and the first 32
+// event encodings, mutation encodings and leaf sample-set masks of each.
+struct __align__(16) ReplayStage {
+    int4 ev;           // removal offset, removals, insertion offset, insertions
+    int2 mr;           // mutations [first, end)
+    int64_t ioff[2];   // items [first, end)
+    int2 pc[32];       // event (parent, child) encodings
+    uint32_t cm[32];   // leaf child masks
+    int32_t menc[32];  // mutation node encodings
+    uint32_t mmask[32];  // leaf mutation node masks
+};
+
 // an entry of the replay's open touch list (shared memory)
 template <int KQ>
 struct TouchEntry {

@@ -1,0 +1,412 @@
+// The item replay kernel (see tsg_items.cuh for the pipeline).  With EVAL
+// other warps value the span's items while the replay proceeds: warp 0
+// publishes its completed trees in shared memory and the evaluating warps
+// take the span's evaluation chunks in order, each once the replay has
+// completed its tree (a bounded wait), so the evaluation runs in the shadow
+// of the sequential replay.  The warps that would share warp 0's scheduler
+// (warp index a multiple of 4, as warps are dealt to the SM's four
+// schedulers) stay idle, leaving the replay its issue slots.  Included by tsg_stats.cu (EVAL off)
+// and by the evaluation translation units (EVAL on).
+#pragma once
+
+#include "tsg_eval.cuh"
+
+namespace tsg {
+
+// bound of an evaluating warp's wait for one tree (with 128 ns sleeps: far
+// longer than any span's replay); past it the kernel records an error
+#define TSG_REPLAY_SPIN_LIMIT (1u << 27)
+// terms per pass of the evaluating warps over a chunk's items: one term at a
+// time keeps their code small (they share the SM's instruction cache with
+// the latency-bound replay warp) and their registers within the replay's
+// launch bounds
+#define TSG_FUSED_EVAL_GROUP 1
+// the replay publishes its progress every few trees (a fence each time)
+#define TSG_PUBLISH_EVERY 8
+
+template <int W, int KQ, typename IdxT, typename F, bool UNPOL, bool EVAL>
+__global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams q, QueryDev qd,
+    WsDev w, int64_t slot_bytes)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_span;
+    __shared__ int s_scan[32];
+    __shared__ TouchEntry<KQ> s_list[TSG_TOUCH_CAP];  // the open touch list
+    __shared__ ReplayStage s_stage[4];                 // prefetch ring, trees t .. t + 3
+    __shared__ int s_ready;  // last tree whose items are complete (EVAL)
+    __shared__ int s_next;   // next chunk to evaluate, from the span's first (EVAL)
+    const int64_t L = ts.max_local;
+    constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
+    SpanState<IdxT> sp = span_state_at<IdxT>(sizeof(IdxT) == 2
+            ? smem_raw
+            : (unsigned char *) w.state + (int64_t) blockIdx.x * slot_bytes,
+        L, KQ);
+    sp.cnt = w.seekcnt + (int64_t) blockIdx.x * L;
+    // one bit per stateful node: touched since the touch list was opened
+    uint32_t *touched = (uint32_t *) span_state_end(sp, L);
+    const int K = q.K;
+    const int lane = threadIdx.x & 31;
+    Item<KQ> *items = (Item<KQ> *) w.items;
+
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_span = atomicAdd(w.counter, 1);
+        }
+        __syncthreads();
+        const int s = s_span;
+        __syncthreads();
+        if (s >= ts.num_spans) {
+            break;
+        }
+        const int32_t t0 = ts.span_tree[s], t1 = ts.span_tree[s + 1];
+        const int64_t lo = ts.span_local_off[s];
+        const int32_t Ls = (int32_t) (ts.span_local_off[s + 1] - lo);
+        const int32_t *l2g = ts.span_l2g + lo;
+        const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
+        sp.time = ts.span_time + lo;
+
+        span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
+        if (q.branch) {
+            for (int32_t i = threadIdx.x; i < (Ls + 31) / 32; i += blockDim.x) {
+                touched[i] = 0;
+            }
+        }
+
+        // ---- first tree of the sequence: one item per stateful node alive
+        // there, in alive-list order (leaves are accounted per edge,
+        // k_leaf_areas); every later tree's sum follows from the items of
+        // the transitions before it
+        if (q.branch && s == 0) {
+            int64_t nanchor = 0;
+            for (int64_t base = a0; base < a1; base += blockDim.x) {
+                const int64_t i = base + threadIdx.x;
+                int2 pc = make_int2(0, -1);
+                if (i < a1) {
+                    pc = ts.span_alive_enc[i];
+                }
+                const bool mine = i < a1 && pc.y >= 0;
+                // block-wide exclusive scan of the stateful flags
+                const unsigned bal = __ballot_sync(0xffffffffu, mine);
+                if (lane == 0) {
+                    s_scan[threadIdx.x >> 5] = __popc(bal);
+                }
+                __syncthreads();
+                int64_t before = 0, total = 0;
+                for (int j = 0; j < (int) (blockDim.x >> 5); j++) {
+                    before += j < (int) (threadIdx.x >> 5) ? s_scan[j] : 0;
+                    total += s_scan[j];
+                }
+                __syncthreads();
+                if (mine) {
+                    const int64_t at = ts.tree_item_off[t0] + nanchor + before
+                        + __popc(bal & ((1u << lane) - 1u));
+                    if (at < ts.tree_item_off[t0 + 1]) {
+                        item_put<KQ>(items + at, Pack{0, 0}, st_load(sp, pc.y), pc.y, -1, pc.x);
+                    }
+                }
+                nanchor += total;
+            }
+            if (threadIdx.x == 0 && ts.tree_item_off[t0] + nanchor != ts.tree_item_off[t0 + 1]) {
+                dev_error(w.err, DEV_ITEM_PLAN);
+            }
+        }
+
+        if (threadIdx.x == 0) {
+            s_ready = t0;
+            s_next = 0;
+        }
+        // the first-tree items read the first tree's counts and the touch
+        // bits must be clear: both before the replay starts
+        __syncthreads();
+
+        // ---- replay (warp 0).  A span replays the transitions into its
+        // trees after the first and, for branch items, into the next span's
+        // first tree.  Every stateful node a transition touches (an edge's
+        // child, a node on a root path) gets one item: its state before the
+        // first touch and after the transition.  The touch list holds at
+        // most TSG_TOUCH_CAP nodes; a longer transition closes the list and
+        // opens a new one (the span plan counts items the same way).
+        if (threadIdx.x < 32) {
+            int64_t cursor = 0;  // first item of the open list
+            int64_t climit = 0;  // end of the transition's items in the plan
+            int32_t nopen = 0;   // nodes in the open list
+            auto close_list = [&]() {
+                __syncwarp();
+                for (int32_t i = lane; i < nopen; i += 32) {
+                    const TouchEntry<KQ> en = s_list[i];
+                    const uint32_t pu = sp.par[en.u];
+                    if (cursor + i < climit) {
+                        item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
+                            st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
+                            pu != TSG_NO_PARENT ? (int32_t) pu : -1);
+                    }
+                    atomicAnd(&touched[en.u >> 5], ~(1u << (en.u & 31)));
+                }
+                __syncwarp();
+                cursor += nopen;
+                nopen = 0;
+            };
+            // lanes with `active` set touch node u (distinct per lane) whose
+            // counts and parent are still x0, p0.  A node is touched at most
+            // once per edge event and every event ends with __syncwarp, so the
+            // touch bits need no barrier here.
+            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t p0) {
+                bool fresh = active && !((touched[u >> 5] >> (u & 31)) & 1u);
+                unsigned m = __ballot_sync(0xffffffffu, fresh);
+                if (nopen + __popc(m) > TSG_TOUCH_CAP) {
+                    close_list();
+                    fresh = active;
+                    m = __ballot_sync(0xffffffffu, fresh);
+                }
+                if (fresh) {
+                    const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
+                    TouchEntry<KQ> en;
+                    en.x0[0] = x0.lo;
+                    if (KQ > 1) {
+                        en.x0[KQ > 1 ? 1 : 0] = x0.hi;
+                    }
+                    en.u = u;
+                    en.p0 = p0 != TSG_NO_PARENT ? (int32_t) p0 : -1;
+                    s_list[at] = en;
+                    atomicOr(&touched[u >> 5], 1u << (u & 31));
+                    if (cursor + at >= climit) {
+                        dev_error(w.err, DEV_ITEM_PLAN);
+                    }
+                }
+                nopen += __popc(m);
+            };
+            // one edge event; cm: membership bits of a leaf child (whose branch
+            // is accounted per edge, k_leaf_areas)
+            auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
+                const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
+                if (c >= 0) {
+                    if (q.branch) {
+                        touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c]);
+                    }
+                    sp.par[c] = sign > 0 ? (IdxT) p : (IdxT) TSG_NO_PARENT;
+                }
+                uint32_t v = (uint32_t) p;
+                int32_t batches = 0;
+                while (v != TSG_NO_PARENT) {
+                    // the next (up to) 32 nodes of the root path, lane j
+                    // taking the j-th
+                    uint32_t mine = TSG_NO_PARENT;
+#pragma unroll 4
+                    for (int j = 0; j < 32; j++) {
+                        if (v == TSG_NO_PARENT) {
+                            break;
+                        }
+                        mine = lane == j ? v : mine;
+                        v = sp.par[v];
+                    }
+                    // a root path has at most Ls nodes: more means a cycle
+                    if (++batches > (Ls >> 5) + 1) {
+                        dev_error(w.err, DEV_PATH_TOO_LONG);
+                        v = TSG_NO_PARENT;
+                    }
+                    uint32_t up = __shfl_down_sync(0xffffffffu, mine, 1);
+                    if (lane == 31) {
+                        up = v;
+                    }
+                    const bool act = mine != TSG_NO_PARENT;
+                    Pack xo{0, 0};
+                    if (act) {
+                        xo = st_load(sp, (int64_t) mine);
+                    }
+                    if (q.branch) {
+                        touch(act, mine, xo, up);
+                    }
+                    if (act) {
+                        Pack xn;
+                        if (sign > 0) {
+                            xn.lo = xo.lo + xc.lo;
+                            xn.hi = xo.hi + xc.hi;
+                        } else {
+                            xn.lo = xo.lo - xc.lo;
+                            xn.hi = xo.hi - xc.hi;
+                        }
+                        pk_store(sp, (int64_t) mine, xn);
+                    }
+                }
+                __syncwarp();
+            };
+            const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;
+            const bool site = q.site;
+            // Prefetch ring: tree t's inputs are staged in three dependent
+            // steps -- (a) its event, mutation and item ranges, (b) its event
+            // and mutation encodings, (c) the masks of its leaf children and
+            // leaf mutation nodes -- issued three, two and one trees ahead.
+            auto stage_a = [&](int32_t t) {
+                ReplayStage &S = s_stage[t & 3];
+                if (lane == 0) {
+                    cp_async16(&S.ev, &ts.tree_ev[t]);
+                } else if (lane == 1) {
+                    cp_async8(&S.mr, &ts.tree_mut[t]);
+                } else if (lane == 2) {
+                    cp_async8(&S.ioff[0], &ts.tree_item_off[t]);
+                } else if (lane == 3) {
+                    cp_async8(&S.ioff[1], &ts.tree_item_off[t + 1]);
+                }
+            };
+            auto stage_b = [&](int32_t t) {
+                ReplayStage &S = s_stage[t & 3];
+                const int4 ev = S.ev;
+                if (t > t0 && lane < ev.y + ev.w) {
+                    cp_async8(&S.pc[lane], lane < ev.y ? (const void *) &ts.rem_enc[ev.x + lane]
+                                                       : (const void *) &ts.ins_enc[ev.z + lane - ev.y]);
+                }
+                if (site && t < t1 && lane < S.mr.y - S.mr.x) {
+                    cp_async4(&S.menc[lane], &ts.mut_enc[S.mr.x + lane]);
+                }
+            };
+            auto stage_c = [&](int32_t t) {
+                ReplayStage &S = s_stage[t & 3];
+                const int4 ev = S.ev;
+                if (t > t0 && lane < ev.y + ev.w && S.pc[lane].y < 0) {
+                    cp_async4(&S.cm[lane], &qd.node_mask[-S.pc[lane].y - 1]);
+                }
+                if (site && t < t1 && lane < S.mr.y - S.mr.x && S.menc[lane] < 0) {
+                    cp_async4(&S.mmask[lane], &qd.node_mask[-S.menc[lane] - 1]);
+                }
+            };
+            for (int32_t k = 0; k < 3; k++) {
+                if (t0 + k < tend) {
+                    stage_a(t0 + k);
+                }
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            for (int32_t k = 0; k < 2; k++) {
+                if (t0 + k < tend) {
+                    stage_b(t0 + k);
+                }
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            if (t0 < tend) {
+                stage_c(t0);
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            for (int32_t t = t0; t < tend; t++) {
+                if (t + 3 < tend) {
+                    stage_a(t + 3);
+                }
+                if (t + 2 < tend) {
+                    stage_b(t + 2);
+                }
+                if (t + 1 < tend) {
+                    stage_c(t + 1);
+                }
+                cp_async_commit();
+                const ReplayStage &S = s_stage[t & 3];
+                if (t > t0) {
+                    cursor = S.ioff[0];
+                    climit = S.ioff[1];
+                    const int32_t r0 = S.ev.x, nr = S.ev.y, i0 = S.ev.z, ni = S.ev.w;
+                    for (int32_t base = 0; base < nr + ni; base += 32) {
+                        // up to 32 events of the transition at once (the
+                        // first 32 from the ring)
+                        const int32_t j = base + lane;
+                        int2 pc = make_int2(0, 0);
+                        uint32_t cm = 0;
+                        if (j < nr + ni) {
+                            if (base == 0) {
+                                pc = S.pc[lane];
+                                cm = pc.y < 0 ? S.cm[lane] : 0u;
+                            } else {
+                                pc = j < nr ? ts.rem_enc[r0 + j] : ts.ins_enc[i0 + (j - nr)];
+                                if (pc.y < 0) {
+                                    cm = qd.node_mask[-pc.y - 1];
+                                }
+                            }
+                        }
+                        const int32_t cnt = min(32, nr + ni - base);
+                        for (int32_t e = 0; e < cnt; e++) {
+                            const int32_t p = __shfl_sync(0xffffffffu, pc.x, e);
+                            const int32_t c = __shfl_sync(0xffffffffu, pc.y, e);
+                            const uint32_t m = __shfl_sync(0xffffffffu, cm, e);
+                            event(p, c, base + e < nr ? -1 : +1, m);
+                        }
+                    }
+                    if (q.branch) {
+                        close_list();
+                        if (cursor != climit) {
+                            dev_error(w.err, DEV_ITEM_PLAN);
+                        }
+                        if (EVAL && (t - t0) % TSG_PUBLISH_EVERY == 0) {
+                            // publish the tree's items to the evaluating warps
+                            __threadfence_block();
+                            __syncwarp();
+                            if (lane == 0) {
+                                *(volatile int *) &s_ready = t;
+                            }
+                        }
+                    }
+                }
+                if (site && t < t1) {
+                    const int32_t m0 = S.mr.x, m1 = S.mr.y;
+                    for (int32_t m = m0 + lane; m < m1; m += 32) {
+                        int32_t enc;
+                        uint32_t mask = 0;
+                        if (m - m0 < 32) {
+                            enc = S.menc[lane];
+                            if (enc < 0) {
+                                mask = S.mmask[lane];
+                            }
+                        } else {
+                            enc = ts.mut_enc[m];
+                            if (enc < 0) {
+                                mask = qd.node_mask[-enc - 1];
+                            }
+                        }
+                        const Pack x = enc >= 0 ? st_load(sp, enc) : pk_from_mask<W>(mask, K);
+                        w.mcnt[(int64_t) m * KQ] = x.lo;
+                        if (KQ > 1) {
+                            w.mcnt[(int64_t) m * KQ + (KQ > 1 ? 1 : 0)] = x.hi;
+                        }
+                    }
+                }
+                cp_async_wait_all();
+                __syncwarp();
+            }
+            if (EVAL && q.branch) {
+                __threadfence_block();
+                __syncwarp();
+                if (lane == 0) {
+                    *(volatile int *) &s_ready = tend;
+                }
+            }
+        } else if (EVAL && q.branch && (threadIdx.x >> 5) % 4 != 0) {
+            // ---- the other warps value the span's chunks as the replay
+            // completes their trees
+            const int32_t ta = s == 0 ? 0 : t0 + 1;
+            const int32_t tb = t1 < ts.num_trees ? t1 + 1 : t1;
+            const int64_t cfirst = ts.tree_chunk_off[ta], clast = ts.tree_chunk_off[tb];
+            for (;;) {
+                int c0 = 0;
+                if (lane == 0) {
+                    c0 = atomicAdd(&s_next, 1);
+                }
+                const int64_t c = cfirst + __shfl_sync(0xffffffffu, c0, 0);
+                if (c >= clast) {
+                    break;
+                }
+                const int32_t tc = ts.chunk_tree[c];
+                for (uint32_t spin = 0; *(volatile int *) &s_ready < tc; spin++) {
+                    if (spin > TSG_REPLAY_SPIN_LIMIT) {
+                        dev_error(w.err, DEV_WAIT_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+                __threadfence_block();
+                eval_chunk<F, UNPOL, W, KQ, TSG_FUSED_EVAL_GROUP>(ts, q, w, c, lane);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+
+}  // namespace tsg

@@ -443,14 +443,23 @@ __global__ void __launch_bounds__(256) k_sweep(TSView ts, QueryParams q, QueryDe
 
 
 // Item pipeline forms: node state in shared memory (16-bit counts and ids)
-// or in a per-CTA slice of global memory (32-bit counts and ids).
-static void *replay_kernel(int W, int KQ)
+// or in a per-CTA slice of global memory (32-bit counts and ids); the
+// replay values its items itself when the query has branch terms.
+static void *replay_kernel(int W, int KQ, const QueryParams &p)
 {
-    if (W == 16) {
-        return KQ == 1 ? (void *) k_replay_items<16, 1, uint16_t>
-                       : (void *) k_replay_items<16, 2, uint16_t>;
+    const int form = (W == 16 ? 0 : 2) + (KQ == 1 ? 0 : 1);
+    if (p.branch) {
+        if (p.f32) {
+            return p.polarised ? replay_eval_fn_f32_pol(form) : replay_eval_fn_f32_unpol(form);
+        }
+        return p.polarised ? replay_eval_fn_f64_pol(form) : replay_eval_fn_f64_unpol(form);
     }
-    return KQ == 1 ? (void *) k_replay_items<32, 1, int32_t> : (void *) k_replay_items<32, 2, int32_t>;
+    switch (form) {
+        case 0: return (void *) k_replay_items<16, 1, uint16_t, float, false, false>;
+        case 1: return (void *) k_replay_items<16, 2, uint16_t, float, false, false>;
+        case 2: return (void *) k_replay_items<32, 1, int32_t, float, false, false>;
+        default: return (void *) k_replay_items<32, 2, int32_t, float, false, false>;
+    }
 }
 
 // bytes of one span's node state: packed counts and parent ids (node times
@@ -475,17 +484,17 @@ static int64_t smem_budget(const void *kernel)
     return (int64_t) optin - (int64_t) attr.sharedSizeBytes;
 }
 
-// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one warp per r, each lane a
-// contiguous run of spans, then a scan across the lanes (fixed order).
-__global__ void k_span_scan(const double *D, const double *rs0, double *RS, int64_t NS, int R)
+// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one block per r, each thread a
+// contiguous run of units, then a scan of the run totals across the block
+// (warp shuffles, then the warp totals in shared memory); fixed order.
+__global__ void __launch_bounds__(512) k_span_scan(const double *D, const double *rs0, double *RS,
+    int64_t NS, int R)
 {
-    const int lane = threadIdx.x & 31;
-    const int r = (int) (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
-    if (r >= R) {
-        return;
-    }
-    const int64_t run = (NS + 31) / 32;
-    const int64_t b = lane * run < NS ? lane * run : NS;
+    __shared__ double s_warp[16];
+    const int r = blockIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t run = (NS + blockDim.x - 1) / blockDim.x;
+    const int64_t b = (int64_t) threadIdx.x * run < NS ? (int64_t) threadIdx.x * run : NS;
     const int64_t e = b + run < NS ? b + run : NS;
     double sum = 0;
     for (int64_t i = b; i < e; i++) {
@@ -498,8 +507,22 @@ __global__ void k_span_scan(const double *D, const double *rs0, double *RS, int6
             incl += y;
         }
     }
-    double acc = __shfl_up_sync(0xffffffffu, incl, 1);
-    acc = rs0[r] + (lane > 0 ? acc : 0.0);
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    excl = lane > 0 ? excl : 0.0;
+    if (lane == 31) {
+        s_warp[wid] = incl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = rs0[r];
+        for (int j = 0; j < (int) (blockDim.x >> 5); j++) {
+            const double v = s_warp[j];
+            s_warp[j] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    double acc = s_warp[wid] + excl;
     for (int64_t i = b; i < e; i++) {
         RS[i * R + r] = acc;
         acc += D[i * R + r];
@@ -514,10 +537,14 @@ __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_no
     for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
          idx += (int64_t) gridDim.x * blockDim.x) {
         const int wdx = (int) (idx / R), r = (int) (idx % R);
-        const int32_t s0 = qd.win_span_lo[wdx], s1 = qd.win_span_hi[wdx];
+        // units: window segments (item pipeline) or spans (general sweep)
+        const int32_t *uwlo = items_mode ? qd.seg_wlo : qd.span_wlo;
+        const int64_t *uwoff = items_mode ? qd.seg_woff : qd.span_woff;
+        const int32_t s0 = items_mode ? qd.win_seg_lo[wdx] : qd.win_span_lo[wdx];
+        const int32_t s1 = items_mode ? qd.win_seg_hi[wdx] : qd.win_span_hi[wdx];
         double vb = 0, vs = 0;
         for (int32_t s = s0; s <= s1; s++) {
-            int64_t li = qd.span_woff[s] + (wdx - qd.span_wlo[s]);
+            int64_t li = uwoff[s] + (wdx - uwlo[s]);
             if (q.branch) {
                 vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
             }
@@ -572,10 +599,11 @@ struct tsg_query {
     QueryDev d;
     void *dbuf;              // device copy of per-query arrays (owned), or null
     std::vector<char> blob;  // host image of the per-query arrays
-    int64_t off[8];          // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite,
+    int64_t off[12];         // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite,
                              // time windows (allele frequency spectrum)
     cudaEvent_t ev_start, ev_stop;  // optional events around the sweep kernel
     int64_t total_span_windows;
+    int64_t total_seg_windows;  // window segments x windows they overlap (item pipeline)
     int64_t num_slots;
     int64_t ws_bytes;
     bool smem;               // item pipeline (either form); else the general sweep
@@ -714,6 +742,10 @@ static void query_bind(tsg_query_t *q, void *dev)
     q->d.win_span_lo = (const int32_t *) (b + q->off[4]);
     q->d.win_span_hi = (const int32_t *) (b + q->off[5]);
     q->d.win_site_lo = (const int32_t *) (b + q->off[6]);
+    q->d.seg_wlo = (const int32_t *) (b + q->off[8]);
+    q->d.seg_woff = (const int64_t *) (b + q->off[9]);
+    q->d.win_seg_lo = (const int32_t *) (b + q->off[10]);
+    q->d.win_seg_hi = (const int32_t *) (b + q->off[11]);
     q->d.node_mask = nullptr;
     if (q->kind == TSG_KIND_AFS) {
         q->afs.windows = q->d.windows;
@@ -728,6 +760,46 @@ static void query_bind(tsg_query_t *q, void *dev)
         q->mv.pair_off = (const int64_t *) (b + q->off[5]);
         q->mv.win_glo = (const int32_t *) (b + q->off[6]);
         q->mv.win_ghi = (const int32_t *) (b + q->off[7]);
+    }
+}
+
+// Overlap tables of windows and units (runs of consecutive trees
+// [ut[u], ut[u + 1])): per unit its first window and its offset into the
+// unit-window arrays; per window its first and last overlapping unit.
+struct WindowUnits {
+    std::vector<int32_t> wlo, wsl, wsh;
+    std::vector<int64_t> woff;
+};
+
+static void window_units(const std::vector<double> &bp, const int32_t *ut, int64_t NU,
+    const double *windows, uint64_t Wn, WindowUnits &o)
+{
+    std::vector<int32_t> whi((size_t) NU);
+    o.wlo.assign((size_t) NU, 0);
+    o.woff.assign((size_t) NU + 1, 0);
+    for (int64_t u = 0; u < NU; u++) {
+        double b0 = bp[(size_t) ut[u]], b1 = bp[(size_t) ut[u + 1]];
+        int64_t lo = upper_bound(windows, (int64_t) Wn + 1, b0) - 1;
+        int64_t hi = lower_bound(windows, (int64_t) Wn + 1, b1) - 1;
+        lo = std::max<int64_t>(0, std::min<int64_t>(lo, (int64_t) Wn - 1));
+        hi = std::max<int64_t>(lo, std::min<int64_t>(hi, (int64_t) Wn - 1));
+        o.wlo[(size_t) u] = (int32_t) lo;
+        whi[(size_t) u] = (int32_t) hi;
+        o.woff[(size_t) u + 1] = o.woff[(size_t) u] + (hi - lo + 1);
+    }
+    o.wsl.assign((size_t) Wn, 0);
+    o.wsh.assign((size_t) Wn, 0);
+    int64_t u = 0;
+    for (int64_t wdx = 0; wdx < (int64_t) Wn; wdx++) {
+        while (u < NU && whi[(size_t) u] < wdx) {
+            u++;
+        }
+        o.wsl[(size_t) wdx] = (int32_t) u;
+        int64_t e = u;
+        while (e + 1 < NU && o.wlo[(size_t) e + 1] <= wdx) {
+            e++;
+        }
+        o.wsh[(size_t) wdx] = (int32_t) e;
     }
 }
 
@@ -858,6 +930,15 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     for (uint64_t k = 0; k < K; k++) {
         p.inv_size[k] = 1.0 / (double) sizes[k];
     }
+    // integer site summaries when every term is a polynomial and the set
+    // sizes keep its products within 64 bits
+    p.site_int = 1;
+    for (uint64_t k = 0; k < K; k++) {
+        p.site_int &= sizes[k] < ((uint64_t) 1 << 15) ? 1 : 0;
+    }
+    for (uint64_t r = 0; r < R; r++) {
+        p.site_int &= outputs[r].type != TSG_RELATEDNESS ? 1 : 0;
+    }
     p.inv_K = 1.0 / (double) K;
     for (uint64_t k = 0; k < K; k++) {
         p.set_size_f[k] = (float) p.set_size[k];
@@ -868,39 +949,14 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     }
     p.inv_K_f = (float) p.inv_K;
 
-    // span <-> window overlap tables (host; spans and windows are few)
-    const int64_t NS = ts->v.num_spans;
-    const auto &bp = ts->h_breakpoints;
-    const auto &st = ts->h_span_tree;
-    std::vector<int32_t> wlo((size_t) NS), whi((size_t) NS);
-    std::vector<int64_t> woff((size_t) NS + 1);
-    woff[0] = 0;
-    for (int64_t s = 0; s < NS; s++) {
-        double b0 = bp[(size_t) st[(size_t) s]], b1 = bp[(size_t) st[(size_t) s + 1]];
-        int64_t lo = upper_bound(windows, (int64_t) Wn + 1, b0) - 1;
-        int64_t hi = lower_bound(windows, (int64_t) Wn + 1, b1) - 1;
-        lo = std::max<int64_t>(0, std::min<int64_t>(lo, (int64_t) Wn - 1));
-        hi = std::max<int64_t>(lo, std::min<int64_t>(hi, (int64_t) Wn - 1));
-        wlo[(size_t) s] = (int32_t) lo;
-        whi[(size_t) s] = (int32_t) hi;
-        woff[(size_t) s + 1] = woff[(size_t) s] + (hi - lo + 1);
-    }
-    std::vector<int32_t> wsl((size_t) Wn), wsh((size_t) Wn);
-    {
-        int64_t s = 0;
-        for (int64_t wdx = 0; wdx < (int64_t) Wn; wdx++) {
-            while (s < NS && whi[(size_t) s] < wdx) {
-                s++;
-            }
-            wsl[(size_t) wdx] = (int32_t) s;
-            int64_t e = s;
-            while (e + 1 < NS && wlo[(size_t) e + 1] <= wdx) {
-                e++;
-            }
-            wsh[(size_t) wdx] = (int32_t) e;
-        }
-    }
-    q->total_span_windows = woff[(size_t) NS];
+    // span <-> window and segment <-> window overlap tables (host; spans,
+    // segments and windows are few)
+    const int64_t NS = ts->v.num_spans, NG = ts->v.num_segs;
+    WindowUnits su, gu;
+    window_units(ts->h_breakpoints, ts->h_span_tree.data(), NS, windows, Wn, su);
+    window_units(ts->h_breakpoints, ts->h_seg_tree.data(), NG, windows, Wn, gu);
+    q->total_span_windows = su.woff[(size_t) NS];
+    q->total_seg_windows = gu.woff[(size_t) NG];
 
     // device copy of the per-query arrays, one allocation
     const int64_t n = ts->v.num_samples;
@@ -911,7 +967,11 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     int64_t off_wsl = align_up(off_woff + (NS + 1) * 8, 256);
     int64_t off_wsh = align_up(off_wsl + (int64_t) Wn * 4, 256);
     int64_t off_wsite = align_up(off_wsh + (int64_t) Wn * 4, 256);
-    int64_t total = align_up(off_wsite + ((int64_t) Wn + 1) * 4, 256);
+    int64_t off_gwlo = align_up(off_wsite + ((int64_t) Wn + 1) * 4, 256);
+    int64_t off_gwoff = align_up(off_gwlo + NG * 4, 256);
+    int64_t off_gwsl = align_up(off_gwoff + (NG + 1) * 8, 256);
+    int64_t off_gwsh = align_up(off_gwsl + (int64_t) Wn * 4, 256);
+    int64_t total = align_up(off_gwsh + (int64_t) Wn * 4, 256);
     std::vector<int32_t> wsite((size_t) Wn + 1);
     {
         const auto &sp = ts->h_site_position;
@@ -924,11 +984,19 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     char *h = q->blob.data();
     std::memcpy(h + off_mask, mask.data(), (size_t) n * 4);
     std::memcpy(h + off_win, windows, ((size_t) Wn + 1) * 8);
-    std::memcpy(h + off_wlo, wlo.data(), (size_t) NS * 4);
-    std::memcpy(h + off_woff, woff.data(), ((size_t) NS + 1) * 8);
-    std::memcpy(h + off_wsl, wsl.data(), (size_t) Wn * 4);
-    std::memcpy(h + off_wsh, wsh.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_wlo, su.wlo.data(), (size_t) NS * 4);
+    std::memcpy(h + off_woff, su.woff.data(), ((size_t) NS + 1) * 8);
+    std::memcpy(h + off_wsl, su.wsl.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_wsh, su.wsh.data(), (size_t) Wn * 4);
     std::memcpy(h + off_wsite, wsite.data(), ((size_t) Wn + 1) * 4);
+    std::memcpy(h + off_gwlo, gu.wlo.data(), (size_t) NG * 4);
+    std::memcpy(h + off_gwoff, gu.woff.data(), ((size_t) NG + 1) * 8);
+    std::memcpy(h + off_gwsl, gu.wsl.data(), (size_t) Wn * 4);
+    std::memcpy(h + off_gwsh, gu.wsh.data(), (size_t) Wn * 4);
+    q->off[8] = off_gwlo;
+    q->off[9] = off_gwoff;
+    q->off[10] = off_gwsl;
+    q->off[11] = off_gwsh;
     q->off[6] = off_wsite;
     q->off[0] = off_mask;
     q->off[1] = off_win;
@@ -969,7 +1037,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->smem_bytes = align_up(replay_state_bytes(L, 16, q->KQ), 16);
     q->slot_bytes = 0;
     if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 65534
-        && q->smem_bytes <= smem_budget(replay_kernel(16, q->KQ))
+        && q->smem_bytes <= smem_budget(replay_kernel(16, q->KQ, p))
         && !(options & TSG_FORCE_GLOBAL_STATE)) {
         q->smem = true;
     } else if (items_ok && K <= 4 && ts->v.max_local < INT32_MAX) {
@@ -983,10 +1051,15 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     const int64_t KQ = q->KQ;
     if (q->smem) {
         int per_sm = 0;
-        void *fn = replay_kernel(q->W, q->KQ);
+        void *fn = replay_kernel(q->W, q->KQ, p);
         if (!q->gstate) {
             // a cap, not a reservation: every query of every tree sequence fits
+            // (the replay without evaluation serves general_stat's prepare step)
+            QueryParams plain;
+            std::memset(&plain, 0, sizeof(plain));
+            void *fn0 = replay_kernel(q->W, q->KQ, plain);
             cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
+            cudaFuncSetAttribute(fn0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn0));
         }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
         int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
@@ -998,13 +1071,16 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         slots = 0;  // no per-slot node arrays of the general sweep
         q->num_slots = 0;
     }
-    const int64_t TSW = q->total_span_windows;
+    // window accumulators: per span (general sweep) or per segment (item
+    // pipeline)
+    const int64_t TSW = std::max(q->total_span_windows, q->total_seg_windows);
+    const int64_t NU = std::max(NS, NG);
     int64_t bytes = 0;
     bytes += align_up(slots * ts->v.num_nodes * 4, 256) * 3;          // parent, nchild, arrive
     bytes += align_up(slots * ts->v.num_nodes * 4 * p.KP, 256);       // x
     bytes += align_up(TSW * 8, 256);                                  // A
     bytes += align_up(TSW * R * 8, 256) * 2;                          // B, SITE
-    bytes += align_up(NS * R * 8, 256) * 2;                           // D, RS
+    bytes += align_up(NU * R * 8, 256) * 2;                           // D, RS
     bytes += align_up((int64_t) R * 8, 256);                          // rs0
     if (q->smem) {
         const int64_t item_bytes = KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
@@ -1138,6 +1214,7 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->options = options;
     q->span_normalise = !!(options & TSG_STAT_SPAN_NORMALISE);
     q->total_span_windows = 0;
+    q->total_seg_windows = 0;
     q->num_slots = 0;
     q->afs_bins = bins;
     QueryParams &p = q->p;
@@ -1176,7 +1253,7 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->slot_bytes = 0;
     if (!(n <= 65535 && ts->v.max_local <= 65534
             && q->smem_bytes <= smem_budget(branch ? afs_replay_kernel((KC + 3) / 4 == 1 ? 0 : 1)
-                                                   : replay_kernel(16, (KC + 3) / 4)))) {
+                                                   : replay_kernel(16, (KC + 3) / 4, p)))) {
         if (KC > 4 || ts->v.max_local >= INT32_MAX) {
             delete q;
             return TSG_ERR_TOO_MANY_SAMPLE_SETS;
@@ -1198,7 +1275,7 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     }
     const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
     {
-        void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ);
+        void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ, p);
         if (!q->gstate) {
             // a cap, not a reservation: every query of every tree sequence fits
             cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
@@ -1223,7 +1300,7 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     std::memcpy(h + off_mask, mask.data(), (size_t) n * 4);
     std::memcpy(h + off_win, windows, ((size_t) Wn + 1) * 8);
     std::memcpy(h + off_tw, time_windows, ((size_t) TW + 1) * 8);
-    for (int j = 0; j < 8; j++) {
+    for (int j = 0; j < 12; j++) {
         q->off[j] = off_win;  // unused span tables point at valid memory
     }
     q->off[0] = off_mask;
@@ -1391,6 +1468,9 @@ static int matvec_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t W, 
     std::memcpy(h + off_poff, poff.data(), (size_t) (G + 1) * 8);
     std::memcpy(h + off_wglo, wglo.data(), (size_t) Wn * 4);
     std::memcpy(h + off_wghi, wghi.data(), (size_t) Wn * 4);
+    for (int j = 8; j < 12; j++) {
+        q->off[j] = off_win;  // unused window tables point at valid memory
+    }
     q->off[0] = off_win;
     q->off[1] = off_win;
     q->off[2] = off_focal;
@@ -1470,10 +1550,10 @@ static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         TSG_CUDA(cudaMemsetAsync(result, 0, (size_t) q->afs_bins * 8, st));
         const size_t sb = (size_t) q->smem_bytes;
         switch (form) {
-            case 0: k_replay_items<16, 1, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
-            case 1: k_replay_items<16, 2, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
-            case 2: k_replay_items<32, 1, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
-            default: k_replay_items<32, 2, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+            case 0: k_replay_items<16, 1, uint16_t, float, false, false><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 1: k_replay_items<16, 2, uint16_t, float, false, false><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+            case 2: k_replay_items<32, 1, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+            default: k_replay_items<32, 2, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
         }
         TSG_LAUNCHED();
         if ((ret = launch_afs_site(form, st, ts->v, a, w.mcnt)) != 0) {
@@ -1505,7 +1585,9 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
 {
     const tsg_treeseq_t *ts = q->ts;
     const QueryParams &p = q->p;
-    const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans, TSW = q->total_span_windows;
+    const int64_t N = ts->v.num_nodes;
+    const int64_t NS = std::max(ts->v.num_spans, ts->v.num_segs);
+    const int64_t TSW = std::max(q->total_span_windows, q->total_seg_windows);
     const int64_t R = p.R, slots = q->num_slots;
     char *b = (char *) ws->ptr;
     WsDev w;
@@ -1713,22 +1795,26 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         const unsigned g = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
         const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
-        switch (form) {
-            case 0: k_replay_items<16, 1, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
-            case 1: k_replay_items<16, 2, uint16_t><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
-            case 2: k_replay_items<32, 1, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
-            default: k_replay_items<32, 2, int32_t><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+        if (p.branch) {
+            // replay and item values in one kernel
+            if (p.f32) {
+                (p.polarised ? launch_replay_eval_f32_pol : launch_replay_eval_f32_unpol)(form, g, sb,
+                    q->slot_bytes, st, ts->v, p, d, w);
+            } else {
+                (p.polarised ? launch_replay_eval_f64_pol : launch_replay_eval_f64_unpol)(form, g, sb,
+                    q->slot_bytes, st, ts->v, p, d, w);
+            }
+        } else {
+            switch (form) {
+                case 0: k_replay_items<16, 1, uint16_t, float, false, false><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+                case 1: k_replay_items<16, 2, uint16_t, float, false, false><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
+                case 2: k_replay_items<32, 1, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+                default: k_replay_items<32, 2, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
+            }
         }
         TSG_LAUNCHED();
         if (p.branch) {
-            const unsigned ge = (unsigned) ((ts->v.num_chunks + 7) / 8);
-            if (p.f32) {
-                (p.polarised ? launch_eval_f32_pol : launch_eval_f32_unpol)(form, ge, st, ts->v, p, w);
-            } else {
-                (p.polarised ? launch_eval_f64_pol : launch_eval_f64_unpol)(form, ge, st, ts->v, p, w);
-            }
-            TSG_LAUNCHED();
-            k_span_windows<<<(unsigned) ((ts->v.num_spans + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
+            k_span_windows<<<(unsigned) ((ts->v.num_segs + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
             TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
                 (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, st));
@@ -1757,7 +1843,8 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         }
         if (p.site) {
             if (ts->v.num_sites > 0) {
-                k_site_windows<<<(unsigned) ((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w);
+                k_site_windows<<<(unsigned) p.Wn, 1024, 0, st>>>(p, d, w,
+                    ts->v.num_sites);
                 TSG_LAUNCHED();
             } else {
                 TSG_CUDA(cudaMemsetAsync(w.site_win, 0, (size_t) p.Wn * R * 8, st));
@@ -1775,7 +1862,8 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         TSG_CUDA(cudaEventRecord(q->ev_stop, st));
     }
     if (p.branch) {
-        k_span_scan<<<(unsigned) ((R + 7) / 8), 256, 0, st>>>(w.D, w.rs0, w.RS, NS, (int) R);
+        k_span_scan<<<(unsigned) R, 512, 0, st>>>(w.D, w.rs0, w.RS,
+            item_pipeline ? ts->v.num_segs : NS, (int) R);
         TSG_LAUNCHED();
     }
     k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w, q->span_normalise,
@@ -1929,10 +2017,10 @@ int tsg_general_stat_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint6
         const unsigned gr = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
         switch (g->form) {
-            case 0: k_replay_items<16, 1, uint16_t><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
-            case 1: k_replay_items<16, 2, uint16_t><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
-            case 2: k_replay_items<32, 1, int32_t><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
-            default: k_replay_items<32, 2, int32_t><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
+            case 0: k_replay_items<16, 1, uint16_t, float, false, false><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
+            case 1: k_replay_items<16, 2, uint16_t, float, false, false><<<gr, 512, sb, st>>>(v, p, g->d, w, 0); break;
+            case 2: k_replay_items<32, 1, int32_t, float, false, false><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
+            default: k_replay_items<32, 2, int32_t, float, false, false><<<gr, 512, 0, st>>>(v, p, g->d, w, q->slot_bytes); break;
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         ret = cudaGetLastError() == cudaSuccess ? 0 : TSG_ERR_CUDA;
@@ -2025,19 +2113,20 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
             break;
         }
         if (pb.branch) {
-            k_span_windows<<<(unsigned) ((v.num_spans + 7) / 8), 256, 0, st>>>(v, pb, g->d, g->w);
+            k_span_windows<<<(unsigned) ((v.num_segs + 7) / 8), 256, 0, st>>>(v, pb, g->d, g->w);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             if (cudaMemsetAsync(g->w.rs0, 0, (size_t) pb.R * 8, st) != cudaSuccess) {
                 ret = TSG_ERR_CUDA;
                 break;
             }
-            k_span_scan<<<(unsigned) ((pb.R + 7) / 8), 256, 0, st>>>(g->w.D, g->w.rs0, g->w.RS,
-                v.num_spans, (int) pb.R);
+            k_span_scan<<<(unsigned) pb.R, 512, 0, st>>>(g->w.D, g->w.rs0, g->w.RS,
+                v.num_segs, (int) pb.R);
             g_launches.fetch_add(1, std::memory_order_relaxed);
         }
         if (pb.site) {
             if (v.num_sites > 0) {
-                k_site_windows<<<(unsigned) ((int64_t) pb.Wn * pb.R), 256, 0, st>>>(pb, g->d, g->w);
+                k_site_windows<<<(unsigned) pb.Wn, 1024, 0, st>>>(pb, g->d, g->w,
+                    v.num_sites);
                 g_launches.fetch_add(1, std::memory_order_relaxed);
             } else if (cudaMemsetAsync(g->w.site_win, 0, (size_t) (pb.Wn * pb.R * 8), st)
                 != cudaSuccess) {

@@ -132,6 +132,51 @@ __device__ __forceinline__ F term_inv(int type, F xi, F xj, F xk, F xl, F ni, F 
     }
 }
 
+// The term's value as an exact integer numerator over its denominator (the
+// value is num * inv): every summary function but the centred relatedness is
+// an integer polynomial in the counts and set sizes over a fixed product of
+// set sizes.  With every set size below 2^15 the products stay below 2^61.
+// Returns false for the centred relatedness.
+__device__ __forceinline__ bool term_num(int type, int64_t xi, int64_t xj, int64_t xk,
+    int64_t xl, int64_t ni, int64_t nj, int64_t nk, int64_t nl, int64_t &num)
+{
+    switch (type) {
+        case TSG_DIVERSITY:
+            num = xi * (ni - xi);
+            return true;
+        case TSG_SEGREGATING_SITES:
+            num = xi > 0 ? ni - xi : 0;
+            return true;
+        case TSG_Y1:
+            num = xi * (ni - xi) * (ni - xi - 1);
+            return true;
+        case TSG_DIVERGENCE:
+            num = xi * (nj - xj);
+            return true;
+        case TSG_Y2:
+            num = xi * (nj - xj) * (nj - xj - 1);
+            return true;
+        case TSG_F2:
+            num = xi * (xi - 1) * (nj - xj) * (nj - xj - 1) - xi * (ni - xi) * (nj - xj) * xj;
+            return true;
+        case TSG_Y3:
+            num = xi * (nj - xj) * (nk - xk);
+            return true;
+        case TSG_F3:
+            num = xi * (xi - 1) * (nj - xj) * (nk - xk) - xi * (ni - xi) * (nj - xj) * xk;
+            return true;
+        case TSG_F4:
+            num = xi * xk * (nj - xj) * (nl - xl) - xi * xl * (nj - xj) * (nk - xk);
+            return true;
+        case TSG_RELATEDNESS_NONCENTRED:
+            num = xi * xj;
+            return true;
+        default:
+            num = 0;
+            return false;
+    }
+}
+
 // Means over the sets of x_k / n_k and of (n_k - x_k) / n_k (centred
 // relatedness only).
 template <typename F, int W>

@@ -703,16 +703,17 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
             goto fail;
         }
         if (num_spans <= 0) {
-            // default: about two spans per SM plus one per 2,000 edge events;
-            // a span's seek touches about two nodes per sample, its replay about
-            // a dozen per event, and its node state must fit in shared memory.
-            // Large trees (node state in global memory) cap the seek work: all
-            // spans' alive edges at most 16 times the edge count.
+            // default: one span per replay CTA (two per SM), all replayed in
+            // one wave: a span's seek touches about two nodes per sample and
+            // the spans carry equal edge-event work.  Large trees (node state
+            // in global memory) take more, shorter spans, capped so that all
+            // spans' alive edges stay within 16 times the edge count.
             const int64_t sms = std::max(device_count_sms(), 1);
-            num_spans = std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms);
+            num_spans = 2 * sms;
             const int64_t alive0 = T > 0 ? (int64_t) (h.tree_in[1] - h.tree_in[0]) : 0;
             if (alive0 > 30000) {
-                num_spans = std::min(num_spans, std::max<int64_t>(4 * sms, 16 * E / alive0));
+                num_spans = std::min(std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms),
+                    std::max<int64_t>(4 * sms, 16 * E / alive0));
             }
             num_spans = std::min<int64_t>(T, num_spans);
         }
