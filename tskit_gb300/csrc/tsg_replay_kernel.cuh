@@ -36,14 +36,18 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
     __shared__ int s_ready;  // last tree whose items are complete (EVAL)
     __shared__ int s_next;   // next chunk to evaluate, from the span's first (EVAL)
     const int64_t L = ts.max_local;
-    constexpr uint32_t TSG_NO_PARENT = SpanState<IdxT>::NONE;
+    // The replay keeps a node's "touched since the touch list opened" flag in
+    // the top bit of its parent entry, where the root-path walks read it for
+    // free; "no parent" is the all-ones value below that bit.
+    constexpr uint32_t PFLAG = sizeof(IdxT) == 2 ? 0x8000u : 0x80000000u;
+    constexpr uint32_t PMASK = PFLAG - 1u;
+    constexpr uint32_t TSG_NO_PARENT = PMASK;
+    constexpr uint32_t NO_NODE = 0xffffffffu;
     SpanState<IdxT> sp = span_state_at<IdxT>(sizeof(IdxT) == 2
             ? smem_raw
             : (unsigned char *) w.state + (int64_t) blockIdx.x * slot_bytes,
         L, KQ);
     sp.cnt = w.seekcnt + (int64_t) blockIdx.x * L;
-    // one bit per stateful node: touched since the touch list was opened
-    uint32_t *touched = (uint32_t *) span_state_end(sp, L);
     const int K = q.K;
     const int lane = threadIdx.x & 31;
     Item<KQ> *items = (Item<KQ> *) w.items;
@@ -66,9 +70,9 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
         sp.time = ts.span_time + lo;
 
         span_seek<W, KQ, IdxT>(ts, qd, w.err, sp, K, Ls, l2g, a0, a1);
-        if (q.branch) {
-            for (int32_t i = threadIdx.x; i < (Ls + 31) / 32; i += blockDim.x) {
-                touched[i] = 0;
+        for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
+            if ((uint32_t) sp.par[l] == SpanState<IdxT>::NONE) {
+                sp.par[l] = (IdxT) TSG_NO_PARENT;
             }
         }
 
@@ -115,8 +119,8 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
             s_ready = t0;
             s_next = 0;
         }
-        // the first-tree items read the first tree's counts and the touch
-        // bits must be clear: both before the replay starts
+        // the first-tree items read the first tree's counts and the parents
+        // must be in the replay's encoding: both before the replay starts
         __syncthreads();
 
         // ---- replay (warp 0).  A span replays the transitions into its
@@ -134,24 +138,26 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 __syncwarp();
                 for (int32_t i = lane; i < nopen; i += 32) {
                     const TouchEntry<KQ> en = s_list[i];
-                    const uint32_t pu = sp.par[en.u];
+                    const uint32_t pu = (uint32_t) sp.par[en.u] & PMASK;
                     if (cursor + i < climit) {
                         item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
                             st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
                             pu != TSG_NO_PARENT ? (int32_t) pu : -1);
                     }
-                    atomicAnd(&touched[en.u >> 5], ~(1u << (en.u & 31)));
+                    sp.par[en.u] = (IdxT) pu;  // clears the touch flag
                 }
                 __syncwarp();
                 cursor += nopen;
                 nopen = 0;
             };
-            // lanes with `active` set touch node u (distinct per lane) whose
-            // counts and parent are still x0, p0.  A node is touched at most
-            // once per edge event and every event ends with __syncwarp, so the
-            // touch bits need no barrier here.
-            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t p0) {
-                bool fresh = active && !((touched[u >> 5] >> (u & 31)) & 1u);
+            // Lanes with `active` set touch node u (distinct per lane) whose
+            // counts are still x0 and whose parent entry (flag and parent) is
+            // praw; returns the entry with the flag set, which the caller
+            // stores (with the node's new parent, for an edge's child).  A
+            // node is touched at most once per edge event and every event
+            // ends with __syncwarp.
+            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw) {
+                bool fresh = active && !(praw & PFLAG);
                 unsigned m = __ballot_sync(0xffffffffu, fresh);
                 if (nopen + __popc(m) > TSG_TOUCH_CAP) {
                     close_list();
@@ -160,6 +166,7 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 }
                 if (fresh) {
                     const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
+                    const uint32_t p0 = praw & PMASK;
                     TouchEntry<KQ> en;
                     en.x0[0] = x0.lo;
                     if (KQ > 1) {
@@ -168,53 +175,57 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                     en.u = u;
                     en.p0 = p0 != TSG_NO_PARENT ? (int32_t) p0 : -1;
                     s_list[at] = en;
-                    atomicOr(&touched[u >> 5], 1u << (u & 31));
                     if (cursor + at >= climit) {
                         dev_error(w.err, DEV_ITEM_PLAN);
                     }
                 }
                 nopen += __popc(m);
+                return (praw & PMASK) | PFLAG;
             };
             // one edge event; cm: membership bits of a leaf child (whose branch
             // is accounted per edge, k_leaf_areas)
             auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
                 const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
                 if (c >= 0) {
+                    const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
                     if (q.branch) {
                         touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c]);
+                        sp.par[c] = (IdxT) (np | PFLAG);
+                    } else {
+                        sp.par[c] = (IdxT) np;
                     }
-                    sp.par[c] = sign > 0 ? (IdxT) p : (IdxT) TSG_NO_PARENT;
                 }
                 uint32_t v = (uint32_t) p;
                 int32_t batches = 0;
                 while (v != TSG_NO_PARENT) {
                     // the next (up to) 32 nodes of the root path, lane j
-                    // taking the j-th
-                    uint32_t mine = TSG_NO_PARENT;
+                    // taking the j-th with its parent entry
+                    uint32_t mine = NO_NODE, mraw = 0;
 #pragma unroll 4
                     for (int j = 0; j < 32; j++) {
                         if (v == TSG_NO_PARENT) {
                             break;
                         }
+                        const uint32_t raw = (uint32_t) sp.par[v];
                         mine = lane == j ? v : mine;
-                        v = sp.par[v];
+                        mraw = lane == j ? raw : mraw;
+                        v = raw & PMASK;
                     }
                     // a root path has at most Ls nodes: more means a cycle
                     if (++batches > (Ls >> 5) + 1) {
                         dev_error(w.err, DEV_PATH_TOO_LONG);
                         v = TSG_NO_PARENT;
                     }
-                    uint32_t up = __shfl_down_sync(0xffffffffu, mine, 1);
-                    if (lane == 31) {
-                        up = v;
-                    }
-                    const bool act = mine != TSG_NO_PARENT;
+                    const bool act = mine != NO_NODE;
                     Pack xo{0, 0};
                     if (act) {
                         xo = st_load(sp, (int64_t) mine);
                     }
                     if (q.branch) {
-                        touch(act, mine, xo, up);
+                        const uint32_t f = touch(act, mine, xo, mraw);
+                        if (act) {
+                            sp.par[mine] = (IdxT) f;
+                        }
                     }
                     if (act) {
                         Pack xn;

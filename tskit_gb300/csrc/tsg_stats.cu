@@ -582,11 +582,10 @@ static int grid_for(int64_t n, int block = 256)
 
 static int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
-// bytes of the item replay's span state: the node state and one touch bit
-// per node
+// bytes of the item replay's span state (counts and parent entries)
 static int64_t replay_state_bytes(int64_t L, int W, int KQ)
 {
-    return align_up(span_state_bytes(L, W, KQ), 8) + (L + 31) / 32 * 4;
+    return align_up(span_state_bytes(L, W, KQ), 8);
 }
 
 }  // namespace tsg
@@ -1036,7 +1035,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->KQ = (int) (((int64_t) K + 3) / 4);
     q->smem_bytes = align_up(replay_state_bytes(L, 16, q->KQ), 16);
     q->slot_bytes = 0;
-    if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 65534
+    if (items_ok && K <= 8 && max_size <= 65535 && ts->v.max_local <= 32766
         && q->smem_bytes <= smem_budget(replay_kernel(16, q->KQ, p))
         && !(options & TSG_FORCE_GLOBAL_STATE)) {
         q->smem = true;
@@ -1251,7 +1250,8 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->gstate = false;
     q->smem = true;
     q->slot_bytes = 0;
-    if (!(n <= 65535 && ts->v.max_local <= 65534
+    // (the site replay's 16-bit parent entries keep their top bit for a flag)
+    if (!(n <= 65535 && ts->v.max_local <= (branch ? 65534 : 32766)
             && q->smem_bytes <= smem_budget(branch ? afs_replay_kernel((KC + 3) / 4 == 1 ? 0 : 1)
                                                    : replay_kernel(16, (KC + 3) / 4, p)))) {
         if (KC > 4 || ts->v.max_local >= INT32_MAX) {
