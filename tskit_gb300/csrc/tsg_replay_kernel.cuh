@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
             int64_t cursor = 0;  // first item of the open list
             int64_t climit = 0;  // end of the transition's items in the plan
             int32_t nopen = 0;   // nodes in the open list
+            int32_t closes = 0;  // lists closed so far
             auto close_list = [&]() {
                 __syncwarp();
                 for (int32_t i = lane; i < nopen; i += 32) {
@@ -149,15 +150,17 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 __syncwarp();
                 cursor += nopen;
                 nopen = 0;
+                closes++;
             };
             // Lanes with `active` set touch node u (distinct per lane) whose
             // counts are still x0 and whose parent entry (flag and parent) is
-            // praw; returns the entry with the flag set, which the caller
-            // stores (with the node's new parent, for an edge's child).  A
-            // node is touched at most once per edge event and every event
-            // ends with __syncwarp.
-            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw) {
-                bool fresh = active && !(praw & PFLAG);
+            // praw (its flag out of date if `stale`: no node then is in the
+            // open list); returns the entry with the flag set, which the
+            // caller stores (with the node's new parent, for an edge's
+            // child).  A node is touched at most once per edge event and
+            // every event ends with __syncwarp.
+            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw, bool stale) {
+                bool fresh = active && (stale || !(praw & PFLAG));
                 unsigned m = __ballot_sync(0xffffffffu, fresh);
                 if (nopen + __popc(m) > TSG_TOUCH_CAP) {
                     close_list();
@@ -184,45 +187,50 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
             };
             // one edge event; cm: membership bits of a leaf child (whose branch
             // is accounted per edge, k_leaf_areas)
+            // the next (up to) 32 nodes of a root path from v, lane j taking
+            // the j-th with its parent entry; advances v past them
+            auto chase = [&](uint32_t &v, uint32_t &mine, uint32_t &mraw) {
+                mine = NO_NODE;
+                mraw = 0;
+#pragma unroll 4
+                for (int j = 0; j < 32; j++) {
+                    if (v == TSG_NO_PARENT) {
+                        break;
+                    }
+                    const uint32_t raw = (uint32_t) sp.par[v];
+                    mine = lane == j ? v : mine;
+                    mraw = lane == j ? raw : mraw;
+                    v = raw & PMASK;
+                }
+            };
+            // One edge event; cm: membership bits of a leaf child (whose
+            // branch is accounted per edge, k_leaf_areas).  The first part of
+            // the parent's root path is read before the child is handled (the
+            // child is not on it), hiding the walk's latency; a touch list
+            // closed in between makes the path's touch flags stale.
             auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
+                uint32_t v = (uint32_t) p, mine, mraw;
+                chase(v, mine, mraw);
+                const int32_t gen0 = closes;
                 const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
                 if (c >= 0) {
                     const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
                     if (q.branch) {
-                        touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c]);
+                        touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c], false);
                         sp.par[c] = (IdxT) (np | PFLAG);
                     } else {
                         sp.par[c] = (IdxT) np;
                     }
                 }
-                uint32_t v = (uint32_t) p;
-                int32_t batches = 0;
-                while (v != TSG_NO_PARENT) {
-                    // the next (up to) 32 nodes of the root path, lane j
-                    // taking the j-th with its parent entry
-                    uint32_t mine = NO_NODE, mraw = 0;
-#pragma unroll 4
-                    for (int j = 0; j < 32; j++) {
-                        if (v == TSG_NO_PARENT) {
-                            break;
-                        }
-                        const uint32_t raw = (uint32_t) sp.par[v];
-                        mine = lane == j ? v : mine;
-                        mraw = lane == j ? raw : mraw;
-                        v = raw & PMASK;
-                    }
-                    // a root path has at most Ls nodes: more means a cycle
-                    if (++batches > (Ls >> 5) + 1) {
-                        dev_error(w.err, DEV_PATH_TOO_LONG);
-                        v = TSG_NO_PARENT;
-                    }
+                bool stale = closes != gen0;
+                for (int32_t batches = 1;; batches++) {
                     const bool act = mine != NO_NODE;
                     Pack xo{0, 0};
                     if (act) {
                         xo = st_load(sp, (int64_t) mine);
                     }
                     if (q.branch) {
-                        const uint32_t f = touch(act, mine, xo, mraw);
+                        const uint32_t f = touch(act, mine, xo, mraw, stale);
                         if (act) {
                             sp.par[mine] = (IdxT) f;
                         }
@@ -238,6 +246,16 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                         }
                         pk_store(sp, (int64_t) mine, xn);
                     }
+                    if (v == TSG_NO_PARENT) {
+                        break;
+                    }
+                    // a root path has at most Ls nodes: more means a cycle
+                    if (batches > (Ls >> 5) + 1) {
+                        dev_error(w.err, DEV_PATH_TOO_LONG);
+                        break;
+                    }
+                    chase(v, mine, mraw);
+                    stale = false;
                 }
                 __syncwarp();
             };
@@ -333,10 +351,16 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                             }
                         }
                         const int32_t cnt = min(32, nr + ni - base);
+                        // each event's fields are fetched one event ahead
+                        int32_t pn = __shfl_sync(0xffffffffu, pc.x, 0);
+                        int32_t cn = __shfl_sync(0xffffffffu, pc.y, 0);
+                        uint32_t mn = __shfl_sync(0xffffffffu, cm, 0);
                         for (int32_t e = 0; e < cnt; e++) {
-                            const int32_t p = __shfl_sync(0xffffffffu, pc.x, e);
-                            const int32_t c = __shfl_sync(0xffffffffu, pc.y, e);
-                            const uint32_t m = __shfl_sync(0xffffffffu, cm, e);
+                            const int32_t p = pn, c = cn;
+                            const uint32_t m = mn;
+                            pn = __shfl_sync(0xffffffffu, pc.x, (e + 1) & 31);
+                            cn = __shfl_sync(0xffffffffu, pc.y, (e + 1) & 31);
+                            mn = __shfl_sync(0xffffffffu, cm, (e + 1) & 31);
                             event(p, c, base + e < nr ? -1 : +1, m);
                         }
                     }
