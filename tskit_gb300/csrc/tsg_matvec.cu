@@ -23,7 +23,8 @@
 // each focal node adds its own v.  A group writes its partial sums per window
 // in span order; k_mv_reduce adds the groups in order, then the outputs are
 // centred over the focal nodes and span-normalised (trees.c:10667-10700,
-// 10772-10774).  All arithmetic is FP64.
+// 10772-10774).  All arithmetic is FP64.  A CTA's node state is its own, so
+// every fence between its warps is block-scoped.
 #include "tsg_query.cuh"
 
 namespace tsg {
@@ -105,7 +106,7 @@ __device__ double mv_prefix(const MvSlot &S, const MvParams &m, uint32_t p, doub
     double base = 0.0;
     while (a != MV_NONE) {
         if (ld_flag(&S.flag[a]) == MV_DONE(epoch)) {
-            __threadfence();
+            __threadfence_block();
             base = __ldcg(&S.v[(int64_t) a * 32 + lane]);
             break;
         }
@@ -159,7 +160,7 @@ __device__ double mv_prefix(const MvSlot &S, const MvParams &m, uint32_t p, doub
             }
             const double q = vb + base;
             S.v[(int64_t) b * 32 + lane] = q;
-            __threadfence();
+            __threadfence_block();
             __syncwarp();
             if (lane == 0) {
                 S.x[b] = pos;
@@ -167,7 +168,7 @@ __device__ double mv_prefix(const MvSlot &S, const MvParams &m, uint32_t p, doub
             }
             base = q;
         } else {
-            __threadfence();
+            __threadfence_block();
             base = __ldcg(&S.v[(int64_t) b * 32 + lane]);
         }
     }
@@ -293,7 +294,7 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                         dev_error(m.err, DEV_PATH_TOO_LONG);
                         break;
                     }
-                    __threadfence();
+                    __threadfence_block();
                     __syncwarp();
                     uint32_t old = 0;
                     if (lane == 0) {
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                     if ((old >> 16) + 1 != (old & 0xFFFFu)) {
                         break;
                     }
-                    __threadfence();
+                    __threadfence_block();
                     // the last child to arrive: own weight plus the children in
                     // edge order
                     double acc = __ldcg(&S.w[(int64_t) p * 32 + lane]);
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                     p = S.par[p];
                 }
             }
-            __threadfence();
+            __threadfence_block();
             __syncthreads();
 
             // ---- replay (warp 0) with window ends (all warps)
@@ -431,7 +432,7 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                         }
                     }
                 }
-                __threadfence();
+                __threadfence_block();
                 __syncthreads();
                 for (int64_t i = warp; i < m.nf; i += TSG_MV_WARPS) {
                     const int32_t j = m.focal[i];
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                     }
                 }
                 last_written = mw;
-                __threadfence();
+                __threadfence_block();
                 __syncthreads();
                 if (window_end) {
                     for (int32_t l = warp; l < Ls; l += TSG_MV_WARPS) {
@@ -469,27 +470,39 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
             };
 
             int mw = Xs < W0 ? -1 : (int) upper_bound(m.windows, (int64_t) m.Wn + 1, Xs) - 1;
-            for (int32_t t = t0; t < t1 && mw < m.Wn; t++) {
-                if (t > t0) {
-                    if (warp == 0) {
-                        transition(t);
-                    }
-                    __threadfence();
-                    __syncthreads();
+            // warp 0 replays up to the tree holding the next window boundary
+            // (the other warps wait: they are needed only at window ends),
+            // then all warps handle the boundaries that tree reaches
+            int32_t t = t0;
+            while (t < t1 && mw < m.Wn) {
+                const double B = mw < 0 ? W0 : m.windows[mw + 1];
+                int32_t te = t1 - 1;
+                if (B <= Xe) {
+                    te = t + (int32_t) lower_bound(ts.breakpoints + t + 1, (int64_t) (t1 - t), B);
                 }
-                const double right = ts.breakpoints[t + 1];
+                if (warp == 0) {
+                    for (int32_t tt = t > t0 ? t : t0 + 1; tt <= te; tt++) {
+                        transition(tt);
+                    }
+                }
+                __threadfence_block();
+                __syncthreads();
+                if (B > Xe) {
+                    break;
+                }
+                const double right = ts.breakpoints[te + 1];
                 while (mw < m.Wn) {
-                    const double B = mw < 0 ? W0 : m.windows[mw + 1];
-                    if (B > right) {
+                    const double Bw = mw < 0 ? W0 : m.windows[mw + 1];
+                    if (Bw > right) {
                         break;
                     }
                     if (mw < 0) {
                         // accumulation starts at the first window
                         for (int32_t l = threadIdx.x; l < Ls; l += nthreads) {
-                            S.x[l] = B;
+                            S.x[l] = Bw;
                         }
                         for (int64_t li = threadIdx.x; li < nL; li += nthreads) {
-                            S.lx[li] = B;
+                            S.lx[li] = Bw;
                         }
                         for (int32_t l = warp; l < Ls; l += TSG_MV_WARPS) {
                             S.v[(int64_t) l * 32 + lane] = 0.0;
@@ -500,10 +513,11 @@ __global__ void __launch_bounds__(TSG_MV_WARPS * 32) k_matvec(TSView ts, MvParam
                         __syncthreads();
                         mw = 0;
                     } else {
-                        output(B, mw, true);
+                        output(Bw, mw, true);
                         mw++;
                     }
                 }
+                t = te + 1;
             }
             if (mw >= 0 && mw < m.Wn && m.windows[mw] < Xe) {
                 output(Xe, mw, false);

@@ -705,16 +705,13 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         if (num_spans <= 0) {
             // default: one span per replay CTA (two per SM), all replayed in
             // one wave: a span's seek touches about two nodes per sample and
-            // the spans carry equal edge-event work.  Large trees (node state
-            // in global memory) take more, shorter spans, capped so that all
-            // spans' alive edges stay within 16 times the edge count.
+            // the spans carry equal edge-event work.  Large trees (more than
+            // 30,000 alive edges: node state in global memory, seeks and
+            // window outputs of O(samples) per span and weight-column block)
+            // take one span per SM.
             const int64_t sms = std::max(device_count_sms(), 1);
-            num_spans = 2 * sms;
             const int64_t alive0 = T > 0 ? (int64_t) (h.tree_in[1] - h.tree_in[0]) : 0;
-            if (alive0 > 30000) {
-                num_spans = std::min(std::max<int64_t>(2 * sms, (2 * E) / 2000 + sms),
-                    std::max<int64_t>(4 * sms, 16 * E / alive0));
-            }
+            num_spans = alive0 > 30000 ? sms : 2 * sms;
             num_spans = std::min<int64_t>(T, num_spans);
         }
         if ((ret = build_span_plan(ts, h, num_spans)) != 0) {
