@@ -514,10 +514,10 @@ def run_gpu(args):
             "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"],
             "traffic": profile_traffic(),
-            "kernel": "sweep pipeline (k_node_mask, k_replay_items, k_eval_items, "
+            "kernel": "sweep pipeline (k_node_mask, k_replay_items with item values, "
                       "k_span_windows, k_leaf_areas, k_leaf_prefix, k_leaf_terms, k_site_eval, "
-                      "k_site_windows, k_window_reduce), timed between events on the launch "
-                      "stream",
+                      "k_site_windows, k_span_scan, k_window_reduce), timed between events on "
+                      "the launch stream",
             "algorithmic_bytes_per_launch": algo,
             "kernel_ms": sweep,
             "peak_source": peak_kind,
