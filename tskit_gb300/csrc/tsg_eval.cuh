@@ -51,6 +51,15 @@ __device__ __forceinline__ void eval_chunk(const TSView &ts, const QueryParams &
     const Item<KQ> *items = (const Item<KQ> *) w.items;
     const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
     const double *time = ts.span_time + ts.span_local_off[ts.chunk_span[c]];
+    // the items' branch lengths, once per chunk into scratch (each lane
+    // reads back only its own items)
+    F *bls = (F *) w.bl;
+    for (int64_t i = b + lane; i < e; i += 32) {
+        const int4 up = *(const int4 *) &items[i].u;
+        const double tu = time[up.x];
+        bls[2 * i] = (F) (up.y >= 0 ? time[up.y] - tu : 0.0);
+        bls[2 * i + 1] = (F) (up.z >= 0 ? time[up.z] - tu : 0.0);
+    }
     for (int g0 = 0; g0 < R; g0 += GROUP) {
         F acc[GROUP], lo[GROUP];
 #pragma unroll
@@ -60,9 +69,7 @@ __device__ __forceinline__ void eval_chunk(const TSView &ts, const QueryParams &
         }
         for (int64_t i = b + lane; i < e; i += 32) {
             const Item<KQ> it = items[i];
-            double b0, b1;
-            item_branches<KQ>(it, time, b0, b1);
-            const F bl0 = (F) b0, bl1 = (F) b1;
+            const F bl0 = bls[2 * i], bl1 = bls[2 * i + 1];
             const Pack x0 = item_pack<KQ>(it.x0);
             const Pack x1 = item_pack<KQ>(it.x1);
             const bool same = x0.lo == x1.lo && x0.hi == x1.hi;

@@ -55,6 +55,7 @@ struct WsDev {
     double *RS;       // spans * R
     double *rs0;      // R
     void *items;      // replay items (item pipeline)
+    void *bl;         // per item: its two branch lengths in the evaluation's arithmetic
     void *state;      // per-CTA span node state (item pipeline, global-memory form)
     uint32_t *seekcnt;    // per-CTA seek counters (item pipeline)
     uint64_t *mcnt;   // packed counts under each mutation (shared-memory sweep)

@@ -1084,6 +1084,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     if (q->smem) {
         const int64_t item_bytes = KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
         bytes += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);  // items
+        bytes += align_up((p.branch ? ts->v.num_items : 0) * (p.f32 ? 8 : 16), 256);  // bl
         bytes += align_up(ts->v.num_mutations * 8 * KQ, 256);                   // mcnt
         bytes += align_up(ts->v.num_chunks * R * 8, 256);                        // dD (per chunk)
         bytes += align_up(ts->v.num_nodes * 4, 256);                             // node_mask
@@ -1613,6 +1614,7 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.rs0 = (double *) (b + off);
     off += align_up(R * 8, 256);
     w.items = nullptr;
+    w.bl = nullptr;
     w.state = nullptr;
     w.seekcnt = nullptr;
     w.leaf_area = nullptr;
@@ -1627,6 +1629,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
         w.items = b + off;
         off += align_up((p.branch ? ts->v.num_items : 0) * item_bytes, 256);
+        w.bl = b + off;
+        off += align_up((p.branch ? ts->v.num_items : 0) * (p.f32 ? 8 : 16), 256);
         w.mcnt = (uint64_t *) (b + off);
         off += align_up(ts->v.num_mutations * 8 * q->KQ, 256);
         w.dD = (double *) (b + off);
