@@ -721,8 +721,11 @@ def run_grm_n20k(args):
                                "breakpoints); site-mode genetic_relatedness_matrix",
                    "gram_tiles": tiles, "operand_bytes": int(n * kp),
                    "l2": "flushed between timed steps (256 MiB write); operand 10 GB"},
+        # genotypes are decoded on the device: the call uploads per-site
+        # column indexes, the sample sets and the tile list
         "e2e": {"value": pairs / e2e_s, "unit": "pair-sites/s", "ms_per_step": e2e_s * 1e3,
-                "h2d_bytes_per_step": int(S * n), "d2h_bytes_per_step": int(K.nbytes)},
+                "h2d_bytes_per_step": int(S * 8 + n * 16 + 4 + tiles * 8 + 16),
+                "d2h_bytes_per_step": int(K.nbytes)},
         "roofline": {"bound": "tensor", "achieved": executed / (ms / 1e3) / 1e12,
                      "peak": 4500.0, "unit": "TFLOP/s",
                      "frac": executed / (ms / 1e3) / 1e12 / 4500.0, "traffic": None,

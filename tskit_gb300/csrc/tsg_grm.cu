@@ -14,11 +14,12 @@
 // the multiallelic sites.  Both products run on tcgen05 (tsg_gram.cu) in exact
 // integers; sets of several samples sum the per-sample entries.
 //
-// Genotypes: decoded on the host (native threads, one tree range each, a
-// tree with child/sibling lists as the reference's variant decoder keeps;
-// isolated samples take the ancestral allele, c/tskit/trees.c:8775-8818),
-// written site-major, uploaded once, then transposed on the GPU into the
-// K-contiguous E4M3 operands (128-column segments per window).
+// Genotypes: decoded on the device (k_decode_genotypes: one CTA per span,
+// parent pointers replayed edge by edge, each sample's root path matched
+// against the tree's mutation nodes; isolated samples take the ancestral
+// allele, c/tskit/trees.c:8775-8818), written site-major, then transposed on
+// the GPU into the K-contiguous E4M3 operands (128-column segments per
+// window).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -37,117 +38,194 @@ int launch_gram(const uint8_t *G, int64_t n, int64_t ld, int64_t k0, int64_t kco
 
 static int64_t up128(int64_t v) { return (v + 127) / 128 * 128; }
 
-// Site-major allele codes of every sample (row s: n bytes), for sites
-// [s0, s1).  Returns the largest allele code seen (255 max).
-static int decode_genotypes(const tsg_treeseq_t *ts, int64_t s0, int64_t s1, uint8_t *out,
-    int *max_allele)
+#define TSG_DECODE_MUTS 256
+
+// Genotypes on the device: allele codes of every sample (site-major rows of
+// n bytes, in sample-index order) for the sites [s0, s1).  One CTA per span
+// at a time: the parents of the span's stateful nodes and of the leaves live
+// in a per-CTA global slot, rebuilt at the span start from its alive edges
+// and updated edge by edge.  At every tree holding sites, each thread walks
+// its samples' root paths against the tree's mutation nodes: a sample takes,
+// per site, the allele of the last mutation (in the site's order) at the
+// deepest of the site's mutation nodes on its path -- the decoding of
+// c/tskit/genotypes.c and trees.c:8775-8818, where a later mutation below an
+// earlier one overrides it -- and the ancestral allele 0 without one.
+__global__ void __launch_bounds__(512) k_decode_genotypes(TSView ts, int64_t s0, int64_t s1,
+    uint8_t *A, int32_t *slots, int64_t slot_words, int32_t *err)
 {
-    const HostTopology &h = ts->host;
-    const int64_t N = ts->v.num_nodes, T = ts->v.num_trees, n = ts->v.num_samples;
-    const auto &bp = ts->h_breakpoints;
-    const auto &sidx = ts->h_sample_index;
+    __shared__ int32_t s_enc[TSG_DECODE_MUTS];
+    __shared__ int16_t s_site[TSG_DECODE_MUTS];
+    __shared__ uint8_t s_allele[TSG_DECODE_MUTS];
+    const int64_t n = ts.num_samples, nL = ts.num_leaves;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    int32_t *par = slots + (int64_t) blockIdx.x * slot_words;  // max_local
+    int32_t *lpar = par + ts.max_local;                         // leaves
+    int32_t *gmap = lpar + nL;                                  // nodes
+    for (int64_t s = blockIdx.x; s < ts.num_spans; s += gridDim.x) {
+        const int32_t t0 = ts.span_tree[s], t1 = ts.span_tree[s + 1];
+        if (ts.tree_sites[t1] <= s0 || ts.tree_sites[t0] >= s1) {
+            continue;
+        }
+        const int64_t lo = ts.span_local_off[s];
+        const int32_t Ls = (int32_t) (ts.span_local_off[s + 1] - lo);
+        const int32_t *l2g = ts.span_l2g + lo;
+        for (int32_t l = tid; l < Ls; l += bd) {
+            par[l] = -1;
+            gmap[l2g[l]] = l;
+        }
+        for (int64_t li = tid; li < nL; li += bd) {
+            lpar[li] = -1;
+        }
+        __syncthreads();
+        auto set_parent = [&](int32_t c, int32_t p) {
+            if (c >= 0) {
+                par[c] = p;
+            } else {
+                lpar[ts.leaf_index[-c - 1]] = p;
+            }
+        };
+        for (int64_t i = ts.span_alive_off[s] + tid; i < ts.span_alive_off[s + 1]; i += bd) {
+            const int2 pc = ts.span_alive_enc[i];
+            set_parent(pc.y, pc.x);
+        }
+        __syncthreads();
+        for (int32_t t = t0; t < t1; t++) {
+            if (t > t0) {
+                // removals, then insertions: one event per child in each
+                for (int32_t i = ts.tree_out[t] + tid; i < ts.tree_out[t + 1]; i += bd) {
+                    set_parent(ts.rem_enc[i].y, -1);
+                }
+                __syncthreads();
+                for (int32_t i = ts.tree_in[t] + tid; i < ts.tree_in[t + 1]; i += bd) {
+                    const int2 pc = ts.ins_enc[i];
+                    set_parent(pc.y, pc.x);
+                }
+                __syncthreads();
+            }
+            int32_t sa = (int32_t) max((int64_t) ts.tree_sites[t], s0);
+            const int32_t sb = (int32_t) min((int64_t) ts.tree_sites[t + 1], s1);
+            while (sa < sb) {
+                // a batch of at most 32 sites whose mutations fit the list
+                const int32_t mb = ts.site_mut[sa];
+                int32_t se = sa + 1;
+                while (se < sb && se - sa < 32 && ts.site_mut[se + 1] - mb <= TSG_DECODE_MUTS) {
+                    se++;
+                }
+                const int32_t nm = ts.site_mut[se] - mb;
+                if (nm > TSG_DECODE_MUTS) {
+                    if (tid == 0) {
+                        dev_error(err, DEV_DECODE_MUTS);
+                    }
+                    break;
+                }
+                for (int32_t k = tid; k < nm; k += bd) {
+                    const int32_t m = mb + k;
+                    int32_t si = sa;
+                    while (ts.site_mut[si + 1] <= m) {
+                        si++;
+                    }
+                    s_enc[k] = ts.mut_enc[m];
+                    s_site[k] = (int16_t) (si - sa);
+                    s_allele[k] = (uint8_t) ts.mutation_allele[m];
+                }
+                __syncthreads();
+                const int32_t nsb = se - sa;
+                for (int64_t j = tid; j < n; j += bd) {
+                    const int32_t g = ts.samples[j];
+                    int32_t e = -(g + 1), p = -1;
+                    const int32_t li = ts.leaf_index[g];
+                    if (li >= 0) {
+                        p = lpar[li];
+                    } else {
+                        const int32_t l = gmap[g];
+                        if (l >= 0 && l < Ls && l2g[l] == g) {
+                            e = l;
+                            p = par[l];
+                        }
+                    }
+                    uint32_t found = 0;
+                    for (int32_t guard = 0;; guard++) {
+                        uint32_t here = 0;
+                        for (int32_t k = 0; k < nm; k++) {
+                            const uint32_t bit = 1u << s_site[k];
+                            if (s_enc[k] == e && !(found & bit)) {
+                                A[(int64_t) (sa + s_site[k] - s0) * n + j] = s_allele[k];
+                                here |= bit;
+                            }
+                        }
+                        found |= here;
+                        if (p < 0 || guard > Ls) {
+                            break;
+                        }
+                        e = p;
+                        p = par[p];
+                    }
+                    for (int32_t k = 0; k < nsb; k++) {
+                        if (!((found >> k) & 1u)) {
+                            A[(int64_t) (sa + k - s0) * n + j] = 0;
+                        }
+                    }
+                }
+                __syncthreads();
+                sa = se;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Run the device decoder for sites [s0, s1) into dA (ns x n bytes).
+static int decode_genotypes_device(const tsg_treeseq_t *ts, int64_t s0, int64_t s1, uint8_t *dA,
+    cudaStream_t st)
+{
+    const TSView &v = ts->v;
     if (s1 <= s0) {
-        *max_allele = 0;
         return 0;
     }
-    // trees holding the sites, split over threads
-    const int64_t t_first = std::upper_bound(h.tree_sites.begin(), h.tree_sites.end(), (int32_t) s0)
-        - h.tree_sites.begin() - 1;
-    const int64_t t_last = std::upper_bound(h.tree_sites.begin(), h.tree_sites.end(), (int32_t) (s1 - 1))
-        - h.tree_sites.begin() - 1;
-    const int64_t ntrees = t_last - t_first + 1;
-    unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-    nth = (unsigned) std::max<int64_t>(1, std::min<int64_t>(nth, ntrees));
-    std::vector<int> maxa(nth, 0), bad(nth, 0);
-    std::vector<std::thread> pool;
-    for (unsigned tid = 0; tid < nth; tid++) {
-        pool.emplace_back([&, tid]() {
-            const int64_t ta = t_first + ntrees * tid / nth;
-            const int64_t tb = t_first + ntrees * (tid + 1) / nth;
-            std::vector<int32_t> parent((size_t) N, -1), lc((size_t) N, -1), rc((size_t) N, -1),
-                ls((size_t) N, -1), rs((size_t) N, -1), stack;
-            auto insert = [&](int32_t p, int32_t c) {
-                parent[(size_t) c] = p;
-                rs[(size_t) c] = -1;
-                ls[(size_t) c] = rc[(size_t) p];
-                if (rc[(size_t) p] != -1) {
-                    rs[(size_t) rc[(size_t) p]] = c;
-                } else {
-                    lc[(size_t) p] = c;
-                }
-                rc[(size_t) p] = c;
-            };
-            auto remove = [&](int32_t p, int32_t c) {
-                const int32_t l = ls[(size_t) c], r = rs[(size_t) c];
-                if (l != -1) {
-                    rs[(size_t) l] = r;
-                } else {
-                    lc[(size_t) p] = r;
-                }
-                if (r != -1) {
-                    ls[(size_t) r] = l;
-                } else {
-                    rc[(size_t) p] = l;
-                }
-                parent[(size_t) c] = ls[(size_t) c] = rs[(size_t) c] = -1;
-            };
-            // seek: the edges alive at the first tree, in insertion order
-            const double x0 = bp[(size_t) ta];
-            for (int32_t i = 0; i < h.tree_in[(size_t) ta + 1]; i++) {
-                const int32_t e = h.ins_edge[(size_t) i];
-                if (h.right[(size_t) e] > x0) {
-                    insert(h.ins_parent[(size_t) i], h.ins_child[(size_t) i]);
-                }
-            }
-            for (int64_t t = ta; t < tb; t++) {
-                if (t > ta) {
-                    for (int32_t i = h.tree_out[(size_t) t]; i < h.tree_out[(size_t) t + 1]; i++) {
-                        remove(h.rem_parent[(size_t) i], h.rem_child[(size_t) i]);
-                    }
-                    for (int32_t i = h.tree_in[(size_t) t]; i < h.tree_in[(size_t) t + 1]; i++) {
-                        insert(h.ins_parent[(size_t) i], h.ins_child[(size_t) i]);
-                    }
-                }
-                const int64_t sa = std::max<int64_t>(s0, h.tree_sites[(size_t) t]);
-                const int64_t sb = std::min<int64_t>(s1, h.tree_sites[(size_t) t + 1]);
-                for (int64_t s = sa; s < sb; s++) {
-                    uint8_t *row = out + (s - s0) * n;
-                    std::memset(row, 0, (size_t) n);
-                    // mutations in order: a later (lower) mutation overrides
-                    for (int32_t m = h.site_mut[(size_t) s]; m < h.site_mut[(size_t) s + 1]; m++) {
-                        const int32_t a = h.mut_allele[(size_t) m];
-                        if (a > 255 || a < 0) {
-                            bad[tid] = 1;
-                            continue;
-                        }
-                        maxa[tid] = std::max(maxa[tid], a);
-                        stack.clear();
-                        stack.push_back(h.mut_node[(size_t) m]);
-                        while (!stack.empty()) {
-                            const int32_t u = stack.back();
-                            stack.pop_back();
-                            const int32_t si = sidx[(size_t) u];
-                            if (si >= 0) {
-                                row[si] = (uint8_t) a;
-                            }
-                            for (int32_t c = lc[(size_t) u]; c != -1; c = rs[(size_t) c]) {
-                                stack.push_back(c);
-                            }
-                        }
-                    }
-                }
-            }
-        });
+    const int64_t words = std::max<int64_t>(v.max_local, 1) + v.num_leaves + v.num_nodes;
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(v.num_spans,
+        2 * (int64_t) std::max(device_count_sms(), 1)));
+    int32_t *slots = nullptr, *derr = nullptr;
+    if (cudaMalloc(&slots, (size_t) (grid * words * 4)) != cudaSuccess
+        || cudaMalloc(&derr, 4) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(slots);
+        return TSG_ERR_NO_MEMORY;
     }
-    for (auto &th : pool) {
-        th.join();
-    }
-    int mx = 0;
-    for (unsigned tid = 0; tid < nth; tid++) {
-        if (bad[tid]) {
-            return TSG_ERR_BAD_PARAM_VALUE;
+    int ret = 0;
+    int32_t herr = 0;
+    if (cudaMemsetAsync(derr, 0, 4, st) != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    } else {
+        k_decode_genotypes<<<(unsigned) grid, 512, 0, st>>>(v, s0, s1, dA, slots, words, derr);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (cudaGetLastError() != cudaSuccess
+            || cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else if (herr != 0) {
+            ret = TSG_ERR_DEVICE_CHECK;
         }
-        mx = std::max(mx, maxa[tid]);
+    }
+    cudaFree(slots);
+    cudaFree(derr);
+    return ret;
+}
+
+// Largest allele code of the sites [s0, s1) (the decoder stores codes in a
+// byte: larger ones are refused).
+static int site_max_allele(const tsg_treeseq_t *ts, int64_t s0, int64_t s1, int *max_allele)
+{
+    const HostTopology &h = ts->host;
+    int mx = 0;
+    if (s1 > s0) {
+        for (int32_t m = h.site_mut[(size_t) s0]; m < h.site_mut[(size_t) s1]; m++) {
+            const int32_t a = h.mut_allele[(size_t) m];
+            if (a < 0 || a > 255) {
+                return TSG_ERR_BAD_PARAM_VALUE;
+            }
+            mx = std::max(mx, a);
+        }
     }
     *max_allele = mx;
     return 0;
@@ -358,14 +436,10 @@ static int divmat_run(const tsg_treeseq_t *ts, int64_t K, const std::vector<int3
             (int32_t) (std::lower_bound(pos.begin(), pos.end(), windows[w]) - pos.begin());
     }
     const int64_t s_lo = pl.wsite[0], s_hi = pl.wsite[(size_t) Wn];
-    // decode the sites the windows cover
+    // the sites the windows cover (decoded on the device below)
     const int64_t ns = s_hi - s_lo;
-    std::unique_ptr<uint8_t[]> A(new (std::nothrow) uint8_t[(size_t) std::max<int64_t>(ns * n, 1)]);
-    if (!A) {
-        return TSG_ERR_NO_MEMORY;
-    }
     int max_allele = 0, ret;
-    if ((ret = decode_genotypes(ts, s_lo, s_hi, A.get(), &max_allele)) != 0) {
+    if ((ret = site_max_allele(ts, s_lo, s_hi, &max_allele)) != 0) {
         return ret;
     }
     // per site: biallelic (largest code <= 1) or multiallelic
@@ -455,7 +529,11 @@ static int divmat_run(const tsg_treeseq_t *ts, int64_t K, const std::vector<int3
         return bytes == 0 || cudaMemcpyAsync(d, hsrc, (size_t) bytes, cudaMemcpyHostToDevice, st)
             == cudaSuccess;
     };
-    if (!h2d(dA, A.get(), ns * n) || !h2d(dkb, pl.kb.data(), ns * 8)
+    if ((ret = decode_genotypes_device(ts, s_lo, s_hi, dA, st)) != 0) {
+        cleanup();
+        return ret;
+    }
+    if (!h2d(dkb, pl.kb.data(), ns * 8)
         || !h2d(dkm, pl.km.data(), (int64_t) pl.km.size() * 8)
         || !h2d(dms, pl.msites.data(), (int64_t) pl.msites.size() * 4)
         || !h2d(dnall, pl.nall.data(), (int64_t) pl.nall.size() * 4)
@@ -691,17 +769,8 @@ int tsg_treeseq_genotype_operand(const tsg_treeseq_t *self, int64_t site_start,
         return TSG_ERR_BAD_PARAM_VALUE;
     }
     const int64_t ns = site_stop - site_start;
-    std::unique_ptr<uint8_t[]> A(new (std::nothrow) uint8_t[(size_t) std::max<int64_t>(ns * n, 1)]);
-    if (!A) {
-        return TSG_ERR_NO_MEMORY;
-    }
     int max_allele = 0;
-    int ret;
-    {
-        tsg_treeseq_t *mts = const_cast<tsg_treeseq_t *>(self);
-        std::lock_guard<std::mutex> lock(mts->sync_mutex);
-        ret = decode_genotypes(self, site_start, site_stop, A.get(), &max_allele);
-    }
+    int ret = site_max_allele(self, site_start, site_stop, &max_allele);
     if (ret != 0 || ns == 0) {
         return ret;
     }
@@ -717,9 +786,12 @@ int tsg_treeseq_genotype_operand(const tsg_treeseq_t *self, int64_t site_start,
         cudaFree(dA);
         return TSG_ERR_NO_MEMORY;
     }
-    ret = 0;
-    if (cudaMemcpyAsync(dA, A.get(), (size_t) (ns * n), cudaMemcpyHostToDevice, st) != cudaSuccess
-        || cudaMemcpyAsync(dkb, kb.data(), (size_t) ns * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+    if ((ret = decode_genotypes_device(self, site_start, site_stop, dA, st)) != 0) {
+        cudaFree(dA);
+        cudaFree(dkb);
+        return ret;
+    }
+    if (cudaMemcpyAsync(dkb, kb.data(), (size_t) ns * 8, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         ret = TSG_ERR_CUDA;
     } else {
         dim3 grid((unsigned) ((ns + 31) / 32), (unsigned) ((n + 31) / 32));

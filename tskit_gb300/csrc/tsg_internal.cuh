@@ -48,6 +48,7 @@ enum DeviceError : int32_t {
     DEV_ITEM_PLAN = 8,
     DEV_AFS_RANGE = 9,
     DEV_WAIT_TIMEOUT = 10,
+    DEV_DECODE_MUTS = 11,
 };
 
 __device__ __forceinline__ void dev_error(int32_t *flag, int32_t code)
