@@ -49,12 +49,24 @@ extern "C" {
 
 /* tsg_treeseq_init options */
 #define TSG_TABLES_ON_DEVICE (1u << 0)
+/* tsg_treeseq_init option: the node times are uncalibrated (time_units
+ * "uncalibrated"); branch-mode statistics then need
+ * TSG_STAT_ALLOW_TIME_UNCALIBRATED (c/tskit/trees.c:1383, 3723) */
+#define TSG_TIME_UNCALIBRATED (1u << 1)
 
 /* Error codes: the reference's values (c/tskit/core.h:255-751) where the
  * condition is the same; GPU-specific conditions below -20000. */
 #define TSG_ERR_GENERIC (-1)
 #define TSG_ERR_NO_MEMORY (-2)
+#define TSG_ERR_IO (-3)
 #define TSG_ERR_BAD_PARAM_VALUE (-4)
+#define TSG_ERR_FILE_FORMAT (-100)
+#define TSG_ERR_FILE_VERSION_TOO_OLD (-101)
+#define TSG_ERR_FILE_VERSION_TOO_NEW (-102)
+#define TSG_ERR_REQUIRED_COL_NOT_FOUND (-103)
+#define TSG_ERR_BOTH_COLUMNS_REQUIRED (-104)
+#define TSG_ERR_BAD_COLUMN_TYPE (-105)
+#define TSG_ERR_BAD_OFFSET (-200)
 #define TSG_ERR_NODE_OUT_OF_BOUNDS (-202)
 #define TSG_ERR_BAD_NODE_TIME_ORDERING (-306)
 #define TSG_ERR_DUPLICATE_SAMPLE (-600)
@@ -362,6 +374,21 @@ int tsg_noalloc_check(const tsg_query_t *query);
 /* Number of kernel launches issued by this library since load (counter used
  * by the benchmarks to report launches). */
 int64_t tsg_launch_count(void);
+
+/* .trees files.  The container tskit stores its tables in (kastore;
+ * replaces the reader behind tsk_table_collection_load, c/tskit/tables.c:
+ * 11580-11830, and c/subprojects/kastore/kastore.c): the whole file is read
+ * and its layout checked (TSG_ERR_IO, TSG_ERR_FILE_FORMAT,
+ * TSG_ERR_FILE_VERSION_TOO_OLD/NEW); tsg_kastore_get finds an item by key:
+ * its element type (0..9: int8, uint8, int16, uint16, int32, uint32, int64,
+ * uint64, float32, float64), element count and data, valid until
+ * tsg_kastore_free (TSG_ERR_REQUIRED_COL_NOT_FOUND when absent).  The
+ * Python layer (tskit_gb300.load) maps the table columns. */
+typedef struct tsg_kastore tsg_kastore_t;
+int tsg_kastore_open(const char *path, tsg_kastore_t **out);
+int tsg_kastore_get(const tsg_kastore_t *k, const char *key, int32_t *type, int64_t *len,
+    const void **data);
+int tsg_kastore_free(tsg_kastore_t *k);
 
 #ifdef __cplusplus
 }

@@ -31,3 +31,13 @@ def cuda_lib():
 
     _build.build_all()
     return _native.load()
+
+
+@pytest.fixture(scope="session")
+def cuda_lib_cpu():
+    """Build (if stale) and load the library for host-only calls (no GPU
+    needed: file reading, error strings)."""
+    from tskit_gb300 import _build, _native
+
+    _build.build_all()
+    return _native.load()

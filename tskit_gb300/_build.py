@@ -32,6 +32,7 @@ CUDA_SOURCES = [
     "tsg_gram.cu",
     "tsg_grm.cu",
     "tsg_general.cu",
+    "tsg_kastore.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

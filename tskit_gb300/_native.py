@@ -23,6 +23,7 @@ PRECISION_F32_KAHAN = 1 << 21
 FORCE_GLOBAL_SWEEP = 1 << 22
 FORCE_GLOBAL_STATE = 1 << 23
 TABLES_ON_DEVICE = 1 << 0
+TIME_UNCALIBRATED = 1 << 1
 
 (DIVERSITY, SEGREGATING_SITES, Y1, DIVERGENCE, Y2, F2, Y3, F3, F4, RELATEDNESS,
  RELATEDNESS_NONCENTRED) = range(1, 12)
@@ -32,6 +33,14 @@ MAX_OUTPUTS = 64
 
 # error codes (same values as the reference where the condition is the same)
 ERR_NO_MEMORY = -2
+ERR_IO = -3
+ERR_FILE_FORMAT = -100
+ERR_FILE_VERSION_TOO_OLD = -101
+ERR_FILE_VERSION_TOO_NEW = -102
+ERR_REQUIRED_COL_NOT_FOUND = -103
+ERR_BOTH_COLUMNS_REQUIRED = -104
+ERR_BAD_COLUMN_TYPE = -105
+ERR_BAD_OFFSET = -200
 ERR_BAD_PARAM_VALUE = -4
 ERR_NODE_OUT_OF_BOUNDS = -202
 ERR_DUPLICATE_SAMPLE = -600
@@ -44,6 +53,7 @@ ERR_INSUFFICIENT_INDEX_TUPLES = -906
 ERR_BAD_SAMPLE_SET_INDEX = -907
 ERR_EMPTY_SAMPLE_SET = -908
 ERR_UNSUPPORTED_STAT_MODE = -909
+ERR_TIME_UNCALIBRATED = -910
 ERR_CUDA = -20001
 ERR_DEVICE_CHECK = -20002
 ERR_NOALLOC_TOO_LARGE = -20007
@@ -138,6 +148,10 @@ SIGNATURES = {
     "tsg_launch_count": (_I64, []),
     "tsg_query_launch_noalloc": (ctypes.c_int, [_P, _P, _P]),
     "tsg_noalloc_check": (ctypes.c_int, [_P]),
+    "tsg_kastore_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "tsg_kastore_get": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32),
+                                       ctypes.POINTER(_I64), ctypes.POINTER(_P)]),
+    "tsg_kastore_free": (ctypes.c_int, [_P]),
 }
 
 _lib = None

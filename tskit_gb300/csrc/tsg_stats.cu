@@ -842,6 +842,11 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     if ((ret = check_sample_sets(ts, K, sizes, sets, mask)) != 0) {
         return ret;
     }
+    // c/tskit/trees.c:1383-1386
+    if (branch && (ts->options & TSG_TIME_UNCALIBRATED)
+        && !(options & TSG_STAT_ALLOW_TIME_UNCALIBRATED)) {
+        return TSG_ERR_TIME_UNCALIBRATED;
+    }
     tsg_query_t *q = new tsg_query_t();
     std::memset(&q->p, 0, sizeof(q->p));
     q->kind = TSG_KIND_STATS;
@@ -1185,6 +1190,11 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     std::vector<uint32_t> mask;
     if ((ret = check_sample_sets(ts, K, sizes, sets, mask)) != 0) {
         return ret;
+    }
+    // c/tskit/trees.c:3723-3726
+    if (branch && (ts->options & TSG_TIME_UNCALIBRATED)
+        && !(options & TSG_STAT_ALLOW_TIME_UNCALIBRATED)) {
+        return TSG_ERR_TIME_UNCALIBRATED;
     }
     if (K > TSG_AFS_KMAX) {
         return TSG_ERR_TOO_MANY_SAMPLE_SETS;

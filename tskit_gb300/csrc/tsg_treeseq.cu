@@ -12,6 +12,7 @@
 //     and, for every span start b, the list of edges with left <= b < right
 //     (the seek state of tsk_tree_position_seek_forward, trees.c:5701-5763).
 #include <algorithm>
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -386,6 +387,27 @@ const char *tsg_strerror(int err)
             return "Generic error";
         case TSG_ERR_NO_MEMORY:
             return "Out of memory";
+        case TSG_ERR_IO:
+            return errno != 0 ? strerror(errno) : "Generic IO error";
+        case TSG_ERR_FILE_FORMAT:
+            return "File format error. (TSK_ERR_FILE_FORMAT)";
+        case TSG_ERR_FILE_VERSION_TOO_OLD:
+            return "tskit file version too old. Please upgrade using the 'tskit upgrade' "
+                   "command from tskit version<0.6.2. (TSK_ERR_FILE_VERSION_TOO_OLD)";
+        case TSG_ERR_FILE_VERSION_TOO_NEW:
+            return "tskit file version is too new for this instance. Please upgrade tskit to "
+                   "the latest version. (TSK_ERR_FILE_VERSION_TOO_NEW)";
+        case TSG_ERR_REQUIRED_COL_NOT_FOUND:
+            return "A required column was not found in the file. "
+                   "(TSK_ERR_REQUIRED_COL_NOT_FOUND)";
+        case TSG_ERR_BOTH_COLUMNS_REQUIRED:
+            return "Both columns in a related pair must be provided. "
+                   "(TSK_ERR_BOTH_COLUMNS_REQUIRED)";
+        case TSG_ERR_BAD_COLUMN_TYPE:
+            return "An incompatible type for a column was found in the file. "
+                   "(TSK_ERR_BAD_COLUMN_TYPE)";
+        case TSG_ERR_BAD_OFFSET:
+            return "Bad offset provided in input array. (TSK_ERR_BAD_OFFSET)";
         case TSG_ERR_BAD_PARAM_VALUE:
             return "Bad parameter value provided";
         case TSG_ERR_NODE_OUT_OF_BOUNDS:

@@ -119,6 +119,95 @@ class Tables:
         t.build_index()
         return t
 
+    @classmethod
+    def load(cls, path):
+        """Read the statistics' columns of a ``.trees`` file (tskit's kastore
+        container; the reader is ``tsg_kastore_*`` in the native library).
+        The checks follow tsk_table_collection_load (c/tskit/tables.c:
+        11580-11830): the format name and major version, the sequence
+        length, required columns, column types, and ragged columns with
+        their offsets (32- or 64-bit)."""
+        import ctypes
+
+        from . import _native as nat
+
+        lib = nat.load()
+        handle = ctypes.c_void_p()
+        nat.check(lib.tsg_kastore_open(str(path).encode(), ctypes.byref(handle)))
+        dtypes = [np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64,
+                  np.uint64, np.float32, np.float64]
+        try:
+            def get(key, types, required=True):
+                t = ctypes.c_int32()
+                n = ctypes.c_int64()
+                ptr = ctypes.c_void_p()
+                code = lib.tsg_kastore_get(handle, key.encode(), ctypes.byref(t),
+                                           ctypes.byref(n), ctypes.byref(ptr))
+                if code != 0:
+                    if required:
+                        raise nat.LibraryError(code)
+                    return None
+                dt = np.dtype(dtypes[t.value])
+                if dt not in [np.dtype(x) for x in types]:
+                    raise nat.LibraryError(nat.ERR_BAD_COLUMN_TYPE)
+                if n.value == 0:
+                    return np.zeros(0, dtype=dt)
+                buf = (ctypes.c_char * (n.value * dt.itemsize)).from_address(ptr.value)
+                return np.frombuffer(buf, dtype=dt).copy()
+
+            def ragged(key, nrows):
+                data = get(key, [np.int8, np.uint8], required=False)
+                off = get(key + "_offset", [np.uint32, np.uint64], required=False)
+                if (data is None) != (off is None):
+                    raise nat.LibraryError(nat.ERR_BOTH_COLUMNS_REQUIRED)
+                if data is None:
+                    raise nat.LibraryError(nat.ERR_REQUIRED_COL_NOT_FOUND)
+                off = off.astype(np.uint64)
+                if len(off) != nrows + 1 or off[0] != 0 or np.any(np.diff(off.astype(np.int64)) < 0) \
+                        or off[-1] != len(data):
+                    raise nat.LibraryError(nat.ERR_BAD_OFFSET)
+                return data.view(np.uint8), off
+
+            name = get("format/name", [np.int8])
+            if name.tobytes() != b"tskit.trees":
+                raise nat.LibraryError(nat.ERR_FILE_FORMAT)
+            version = get("format/version", [np.uint32])
+            if len(version) != 2:
+                raise nat.LibraryError(nat.ERR_FILE_FORMAT)
+            if version[0] < 12:
+                raise nat.LibraryError(nat.ERR_FILE_VERSION_TOO_OLD)
+            if version[0] > 12:
+                raise nat.LibraryError(nat.ERR_FILE_VERSION_TOO_NEW)
+            L = get("sequence_length", [np.float64])
+            if len(L) != 1:
+                raise nat.LibraryError(nat.ERR_FILE_FORMAT)
+            time_units = get("time_units", [np.int8], required=False)
+
+            def cols(keys, types):
+                arrays = [get(k, t) for k, t in zip(keys, types)]
+                if len({len(a) for a in arrays}) > 1:
+                    raise nat.LibraryError(nat.ERR_FILE_FORMAT)
+                return arrays
+
+            node_time, node_flags = cols(["nodes/time", "nodes/flags"], [[np.float64], [np.uint32]])
+            left, right, parent, child = cols(
+                ["edges/left", "edges/right", "edges/parent", "edges/child"],
+                [[np.float64], [np.float64], [np.int32], [np.int32]])
+            (position,) = cols(["sites/position"], [[np.float64]])
+            anc, anc_off = ragged("sites/ancestral_state", len(position))
+            msite, mnode, mparent = cols(["mutations/site", "mutations/node", "mutations/parent"],
+                                         [[np.int32]] * 3)
+            der, der_off = ragged("mutations/derived_state", len(msite))
+        finally:
+            lib.tsg_kastore_free(handle)
+        t = cls.from_columns(float(L[0]), node_time, node_flags, left, right, parent, child,
+                             site_position=position, site_ancestral_state=(anc, anc_off),
+                             mutation_site=msite, mutation_node=mnode, mutation_parent=mparent,
+                             mutation_derived_state=(der, der_off))
+        if time_units is not None and time_units.tobytes() == b"uncalibrated":
+            t.time_uncalibrated = True
+        return t
+
     @property
     def num_nodes(self):
         return len(self.node_time)

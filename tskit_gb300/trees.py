@@ -245,8 +245,9 @@ class TreeSequence:
             setattr(tt, k, v.data_ptr())
         torch.cuda.synchronize()
         h = ctypes.c_void_p()
+        opts = nat.TABLES_ON_DEVICE | (nat.TIME_UNCALIBRATED if t.time_uncalibrated else 0)
         nat.check(self._lib.tsg_treeseq_init(ctypes.byref(h), ctypes.byref(tt), int(num_spans),
-                                             nat.TABLES_ON_DEVICE))
+                                             opts))
         self._handle = h
         self._samples = t.samples()
         self._breakpoints = None
@@ -900,3 +901,9 @@ class TreeSequence:
                 windows, np.ndarray) and not isinstance(windows, numbers.Number)):
             windows = self.parse_windows(windows)
         return Query(self, sample_sets, terms, windows, flags)
+
+
+def load(path):
+    """tskit.load: the tree sequence stored in a ``.trees`` file, resident on
+    the GPU (python/tskit/trees.py load; the statistics' columns only)."""
+    return TreeSequence(Tables.load(path))
