@@ -384,6 +384,17 @@ int64_t tsg_launch_count(void);
  * uint64, float32, float64), element count and data, valid until
  * tsg_kastore_free (TSG_ERR_REQUIRED_COL_NOT_FOUND when absent).  The
  * Python layer (tskit_gb300.load) maps the table columns. */
+/* Edge orders on the device (replaces the index build of
+ * tsk_table_collection_build_index, c/tskit/tables.c:11393-11450, and the
+ * edge order of tsk_table_collection_sort): permutations of the edges by
+ * (time[parent], parent, child, left) (sort_order), (left, time[parent],
+ * parent, child) (insertion_order) and (right, -time[parent], -parent,
+ * -child) (removal_order), ties in edge-table order.  All pointers are device
+ * arrays; an output may be null.  Synchronous on cuda_stream. */
+int tsg_edge_orders(int64_t num_edges, const double *edge_left, const double *edge_right,
+    const int32_t *edge_parent, const int32_t *edge_child, const double *node_time,
+    int32_t *sort_order, int32_t *insertion_order, int32_t *removal_order, void *cuda_stream);
+
 typedef struct tsg_kastore tsg_kastore_t;
 int tsg_kastore_open(const char *path, tsg_kastore_t **out);
 int tsg_kastore_get(const tsg_kastore_t *k, const char *key, int32_t *type, int64_t *len,

@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     "tsg_grm.cu",
     "tsg_general.cu",
     "tsg_kastore.cu",
+    "tsg_index.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

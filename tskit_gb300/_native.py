@@ -152,6 +152,7 @@ SIGNATURES = {
     "tsg_kastore_get": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32),
                                        ctypes.POINTER(_I64), ctypes.POINTER(_P)]),
     "tsg_kastore_free": (ctypes.c_int, [_P]),
+    "tsg_edge_orders": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -227,14 +227,21 @@ class TreeSequence:
             edge_right=up(t.edge_right, np.float64),
             edge_parent=up(t.edge_parent, np.int32),
             edge_child=up(t.edge_child, np.int32),
-            edge_insertion_order=up(t.edge_insertion_order, np.int32),
-            edge_removal_order=up(t.edge_removal_order, np.int32),
+            edge_insertion_order=torch.zeros(max(t.num_edges, 1), dtype=torch.int32, device=dev),
+            edge_removal_order=torch.zeros(max(t.num_edges, 1), dtype=torch.int32, device=dev),
             site_position=up(t.site_position, np.float64),
             mutation_site=up(t.mutation_site, np.int32),
             mutation_node=up(t.mutation_node, np.int32),
             mutation_allele=up(allele, np.int32),
             mutation_alt_allele=up(alt, np.int32),
         )
+        # the edge indexes, sorted on the device (tables.c:11393-11450)
+        d = self._dev
+        nat.check(self._lib.tsg_edge_orders(
+            t.num_edges, d["edge_left"].data_ptr(), d["edge_right"].data_ptr(),
+            d["edge_parent"].data_ptr(), d["edge_child"].data_ptr(), d["node_time"].data_ptr(),
+            None, d["edge_insertion_order"].data_ptr(), d["edge_removal_order"].data_ptr(),
+            torch.cuda.current_stream().cuda_stream))
         tt = nat.Tables_t()
         tt.sequence_length = t.sequence_length
         tt.num_nodes = t.num_nodes
