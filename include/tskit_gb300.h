@@ -297,6 +297,19 @@ int tsg_general_stat_states(tsg_general_t *general, int32_t *states);
 int tsg_general_stat_finish(tsg_general_t *general, const double *values, double *result);
 int tsg_general_stat_free(tsg_general_t *general);
 
+/* general_stat with real-valued weights (tsk_treeseq_general_stat,
+ * c/tskit/trees.c:2035-2095, W f64 [n x K] in sample order, K <= 8): the
+ * same prepare / states / finish steps, the states being the weights below
+ * each node as FP64 vectors.  Every state an item, a site allele or a leaf
+ * needs is listed (real states rarely repeat): the host evaluates the
+ * summary function on each of the num_states rows of
+ * tsg_general_weighted_states and passes the values to
+ * tsg_general_stat_finish; tsg_general_stat_free releases. */
+int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *self, uint64_t K,
+    const double *weights, uint64_t R, uint64_t num_windows, const double *windows,
+    uint32_t options, int64_t *num_states);
+int tsg_general_weighted_states(tsg_general_t *g, double *states);
+
 /* ----------------------------------------------- device-resident queries
  * A query is prepared once (validates and uploads sample sets, summary terms
  * and windows) and launched any number of times on a stream with a

@@ -133,6 +133,10 @@ SIGNATURES = {
     "tsg_general_stat_states": (ctypes.c_int, [_P, _P]),
     "tsg_general_stat_finish": (ctypes.c_int, [_P, _P, _P]),
     "tsg_general_stat_free": (ctypes.c_int, [_P]),
+    "tsg_general_weighted_prepare": (
+        ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _U64, _U64, _P, _U32,
+                       ctypes.POINTER(_I64)]),
+    "tsg_general_weighted_states": (ctypes.c_int, [_P, _P]),
     "tsg_query_create_afs": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),

@@ -100,4 +100,25 @@ __device__ __forceinline__ double fx_value(const unsigned long long *acc)
     return ldexp(__ull2double_rn(m), 32 * (top - 1) - sh - TSG_FX_FRAC);
 }
 
+// The exact difference of two counters, rounded once to FP64 (signed).
+__device__ __forceinline__ double fx_diff_value(const unsigned long long *a,
+    const unsigned long long *b)
+{
+    long long run[TSG_FX_LIMBS + 2];
+    for (int i = 0; i < TSG_FX_LIMBS; i++) {
+        run[i] = (long long) a[i] - (long long) b[i];
+    }
+    run[TSG_FX_LIMBS] = run[TSG_FX_LIMBS + 1] = 0;
+    for (int i = 0; i < TSG_FX_LIMBS + 1; i++) {
+        const long long cy = run[i] >> 32;
+        run[i] -= cy * (1ll << 32);
+        run[i + 1] += cy;
+    }
+    double v = 0;
+    for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
+        v = v * 4294967296.0 + (double) run[i];
+    }
+    return ldexp(v, -TSG_FX_FRAC);
+}
+
 }  // namespace tsg

@@ -407,4 +407,445 @@ int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Real-valued weights (general_stat with W f64 [n x K], c/tskit/trees.c:
+// 1352-1776 with arbitrary weights): the states are the weights below each
+// node, K doubles.  Same span plan and touch-list semantics as the counting
+// replay (the items land where the plan puts them), one warp replaying each
+// span with the node state in a per-CTA global slot; every state an item,
+// a site or a leaf needs is listed for the host's summary function (real
+// states rarely repeat, so they are not deduplicated).  Deterministic: the
+// seek adds children in edge order, one warp replays in reference order.
+
+// Replay: items (ids, and states x0 | x1 per item), states under every
+// mutation.  Lane k carries weight component k (K <= 8) in the seek; a
+// root-path batch takes one node per lane, each adding all components.
+__global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const double *W,
+    int K, double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int4 *ids, double *xs,
+    double *mstate, int32_t *err, int32_t *counter)
+{
+    __shared__ int s_span;
+    __shared__ int32_t s_list[TSG_TOUCH_CAP];
+    const int64_t L = ts.max_local;
+    double *x = slots_x + (int64_t) blockIdx.x * L * K;
+    int32_t *par = slots_par + (int64_t) blockIdx.x * L;
+    uint8_t *touched = slots_touched + (int64_t) blockIdx.x * L;
+    const int lane = threadIdx.x & 31;
+    auto leaf_w = [&](int32_t g, int k) {
+        const int32_t si = ts.sample_index[g];
+        return si >= 0 && k < K ? W[(int64_t) si * K + k] : 0.0;
+    };
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_span = atomicAdd(counter, 1);
+        }
+        __syncthreads();
+        const int s = s_span;
+        __syncthreads();
+        if (s >= ts.num_spans) {
+            break;
+        }
+        const int32_t t0 = ts.span_tree[s], t1 = ts.span_tree[s + 1];
+        const int64_t lo = ts.span_local_off[s];
+        const int32_t Ls = (int32_t) (ts.span_local_off[s + 1] - lo);
+        const int32_t *l2g = ts.span_l2g + lo;
+        const double *time = ts.span_time + lo;
+        const int64_t a0 = ts.span_alive_off[s], a1 = ts.span_alive_off[s + 1];
+        for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
+            par[l] = -1;
+            touched[l] = 0;
+            for (int k = 0; k < K; k++) {
+                x[(int64_t) l * K + k] = leaf_w(l2g[l], k);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x >= 32) {
+            continue;
+        }
+        // seek: the alive edges in edge order (children before parents);
+        // lane k adds component k
+        for (int64_t i = a0; i < a1; i++) {
+            const int2 pc = ts.span_alive_enc[i];
+            if (lane < K) {
+                const double xc = pc.y >= 0 ? x[(int64_t) pc.y * K + lane] : leaf_w(-pc.y - 1, lane);
+                x[(int64_t) pc.x * K + lane] += xc;
+            }
+            if (lane == 0 && pc.y >= 0) {
+                par[pc.y] = pc.x;
+            }
+        }
+        __syncwarp();
+        // first tree of the sequence: its stateful nodes in alive-list order
+        if (q.branch && s == 0) {
+            int64_t at = ts.tree_item_off[t0];
+            for (int64_t i = a0; i < a1; i++) {
+                const int2 pc = ts.span_alive_enc[i];
+                if (pc.y < 0) {
+                    continue;
+                }
+                if (at < ts.tree_item_off[t0 + 1]) {
+                    if (lane == 0) {
+                        ids[at] = make_int4(pc.y, -1, pc.x, 0);
+                    }
+                    if (lane < K) {
+                        xs[(2 * at) * K + lane] = 0.0;
+                        xs[(2 * at + 1) * K + lane] = x[(int64_t) pc.y * K + lane];
+                    }
+                }
+                at++;
+            }
+            if (lane == 0 && at != ts.tree_item_off[t0 + 1]) {
+                dev_error(err, DEV_ITEM_PLAN);
+            }
+        }
+        int64_t cursor = 0, climit = 0;
+        int32_t nopen = 0;
+        auto close_list = [&]() {
+            __syncwarp();
+            for (int32_t i = lane; i < nopen; i += 32) {
+                const int32_t u = s_list[i];
+                if (cursor + i < climit) {
+                    ids[cursor + i].z = par[u];
+                    for (int k = 0; k < K; k++) {
+                        xs[(2 * (cursor + i) + 1) * K + k] = x[(int64_t) u * K + k];
+                    }
+                }
+                touched[u] = 0;
+            }
+            __syncwarp();
+            cursor += nopen;
+            nopen = 0;
+        };
+        // lanes with `active` set touch node u (distinct per lane), parent p0
+        auto touch = [&](bool active, int32_t u, int32_t p0) {
+            bool fresh = active && !touched[u];
+            unsigned m = __ballot_sync(0xffffffffu, fresh);
+            if (nopen + __popc(m) > TSG_TOUCH_CAP) {
+                close_list();
+                fresh = active;
+                m = __ballot_sync(0xffffffffu, fresh);
+            }
+            if (fresh) {
+                const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
+                s_list[at] = u;
+                touched[u] = 1;
+                if (cursor + at < climit) {
+                    ids[cursor + at] = make_int4(u, p0, -1, 0);
+                    for (int k = 0; k < K; k++) {
+                        xs[(2 * (cursor + at)) * K + k] = x[(int64_t) u * K + k];
+                    }
+                } else {
+                    dev_error(err, DEV_ITEM_PLAN);
+                }
+            }
+            nopen += __popc(m);
+            __syncwarp();
+        };
+        auto event = [&](int32_t p, int32_t c, int sign) {
+            double xc[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                xc[k] = k < K ? (c >= 0 ? x[(int64_t) c * K + k] : leaf_w(-c - 1, k)) : 0.0;
+            }
+            if (c >= 0) {
+                if (q.branch) {
+                    touch(lane == 0, c, par[c]);
+                }
+                if (lane == 0) {
+                    par[c] = sign > 0 ? p : -1;
+                }
+                __syncwarp();
+            }
+            int32_t v = p;
+            int32_t batches = 0;
+            while (v >= 0) {
+                int32_t mine = -1;
+                for (int j = 0; j < 32 && v >= 0; j++) {
+                    if (lane == j) {
+                        mine = v;
+                    }
+                    v = par[v];
+                }
+                if (++batches > (Ls >> 5) + 1) {
+                    dev_error(err, DEV_PATH_TOO_LONG);
+                    v = -1;
+                }
+                int32_t up = __shfl_down_sync(0xffffffffu, mine, 1);
+                if (lane == 31) {
+                    up = v;
+                }
+                const bool act = mine >= 0;
+                if (q.branch) {
+                    touch(act, mine, act ? up : -1);
+                }
+                if (act) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        if (k < K) {
+                            x[(int64_t) mine * K + k] += sign > 0 ? xc[k] : -xc[k];
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        };
+        const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;
+        for (int32_t t = t0; t < tend; t++) {
+            if (t > t0) {
+                cursor = ts.tree_item_off[t];
+                climit = ts.tree_item_off[t + 1];
+                for (int32_t i = ts.tree_out[t]; i < ts.tree_out[t + 1]; i++) {
+                    const int2 pc = ts.rem_enc[i];
+                    event(pc.x, pc.y, -1);
+                }
+                for (int32_t i = ts.tree_in[t]; i < ts.tree_in[t + 1]; i++) {
+                    const int2 pc = ts.ins_enc[i];
+                    event(pc.x, pc.y, +1);
+                }
+                if (q.branch) {
+                    close_list();
+                    if (lane == 0 && cursor != climit) {
+                        dev_error(err, DEV_ITEM_PLAN);
+                    }
+                }
+            }
+            if (q.site && t < t1) {
+                const int32_t m0 = ts.site_mut[ts.tree_sites[t]];
+                const int32_t m1 = ts.site_mut[ts.tree_sites[t + 1]];
+                for (int32_t m = m0; m < m1; m++) {
+                    const int32_t enc = ts.mut_enc[m];
+                    if (lane < K) {
+                        mstate[(int64_t) m * K + lane] =
+                            enc >= 0 ? x[(int64_t) enc * K + lane] : leaf_w(-enc - 1, lane);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Allele states of every site (get_allele_weights, trees.c:1525-1612) and
+// the weights of every leaf, appended to the state list.
+__global__ void k_wsite_states(TSView ts, int K, const double *total, const double *mstate,
+    const int64_t *site_off, double *states)
+{
+    for (int64_t site = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; site < ts.num_sites;
+         site += (int64_t) gridDim.x * blockDim.x) {
+        const int32_t m0 = ts.site_mut[site], m1 = ts.site_mut[site + 1];
+        const int64_t A = site_off[site + 1] - site_off[site];
+        for (int64_t a = 0; a < A; a++) {
+            double *st = states + (site_off[site] + a) * K;
+            for (int k = 0; k < K; k++) {
+                double v = a == 0 ? total[k] : 0.0;
+                for (int32_t m = m0; m < m1; m++) {
+                    if (ts.mutation_allele[m] == a) {
+                        v += mstate[(int64_t) m * K + k];
+                    }
+                    if (ts.mutation_alt[m] == a) {
+                        v -= mstate[(int64_t) m * K + k];
+                    }
+                }
+                st[k] = v;
+            }
+        }
+    }
+}
+
+__global__ void k_wleaf_states(TSView ts, int K, const double *W, double *states)
+{
+    for (int64_t li = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; li < ts.num_leaves;
+         li += (int64_t) gridDim.x * blockDim.x) {
+        const int32_t si = ts.sample_index[ts.leaves[li]];
+        for (int k = 0; k < K; k++) {
+            states[li * K + k] = si >= 0 ? W[(int64_t) si * K + k] : 0.0;
+        }
+    }
+}
+
+// Item values for outputs [r0, r0 + q.R) of the values table (U x R_total:
+// item i's states at rows 2i and 2i + 1), one warp per chunk, FP64.
+__global__ void __launch_bounds__(256) k_weval_items(TSView ts, QueryParams q, WsDev w,
+    const int4 *ids, const double *vals, int32_t R_total, int32_t r0)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t c = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= ts.num_chunks) {
+        return;
+    }
+    const double *time = ts.span_time + ts.span_local_off[ts.chunk_span[c]];
+    for (int r = 0; r < q.R; r++) {
+        double acc = 0;
+        for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
+            const int4 id = ids[i];
+            const double tu = time[id.x];
+            const double bl1 = id.z >= 0 ? time[id.z] - tu : 0.0;
+            double v = bl1 * vals[(2 * i + 1) * R_total + r0 + r];
+            if (id.y >= 0) {
+                v -= (time[id.y] - tu) * vals[(2 * i) * R_total + r0 + r];
+            }
+            acc += v;
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            w.dD[c * q.R + r] = acc;
+        }
+    }
+}
+
+// Per site: the sum of its alleles' values (the ancestral one skipped when
+// polarised), term-major.
+__global__ void k_wsite_values(TSView ts, QueryParams q, WsDev w, const int64_t *site_off,
+    const double *vals, int64_t sbase, int32_t R_total, int32_t r0)
+{
+    for (int64_t site = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; site < ts.num_sites;
+         site += (int64_t) gridDim.x * blockDim.x) {
+        const int64_t a0 = q.polarised ? 1 : 0, A = site_off[site + 1] - site_off[site];
+        for (int r = 0; r < q.R; r++) {
+            double v = 0;
+            for (int64_t a = a0; a < A; a++) {
+                v += vals[(sbase + site_off[site] + a) * R_total + r0 + r];
+            }
+            w.site_val[(int64_t) r * ts.num_sites + site] = v;
+        }
+    }
+}
+
+// Leaf branches: per window and term, the exact sum over leaf edges of
+// F_r(leaf weights) x branch length x overlap, in signed fixed point
+// (positive and negative parts): partial windows get their overlap, the
+// windows in between a difference array (as k_leaf_areas).  Layout of acc:
+// [sign][partial, plus, minus][window][term][limbs].
+__global__ void __launch_bounds__(256) k_wleaf_areas(TSView ts, QueryParams q, QueryDev qd,
+    const double *vals, int64_t lbase, int32_t R_total, int32_t r0, unsigned long long *acc,
+    int32_t *err)
+{
+    const int R = q.R;
+    const int64_t block = (int64_t) q.Wn * R * TSG_FX_LIMBS;
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < ts.num_edges;
+         i += (int64_t) gridDim.x * blockDim.x) {
+        const int32_t c = ts.ins_child[i];
+        if (ts.node_is_parent[c]) {
+            continue;
+        }
+        const double bl = ts.node_time[ts.ins_parent[i]] - ts.node_time[c];
+        const double left = ts.ins_left[i], right = ts.ins_right[i];
+        int w0 = (int) upper_bound(qd.windows, (int64_t) q.Wn + 1, left) - 1;
+        int w1 = (int) lower_bound(qd.windows, (int64_t) q.Wn + 1, right) - 1;
+        w0 = w0 < 0 ? 0 : (w0 >= q.Wn ? q.Wn - 1 : w0);
+        w1 = w1 < w0 ? w0 : (w1 >= q.Wn ? q.Wn - 1 : w1);
+        const int64_t li = ts.leaf_index[c];
+        for (int r = 0; r < R; r++) {
+            const double f = vals[(lbase + li) * R_total + r0 + r] * bl;
+            unsigned long long *base = acc + (f < 0 ? 3 * block : 0);
+            const double af = f < 0 ? -f : f;
+            auto at = [&](int kind, int wi) {
+                return base + kind * block + ((int64_t) wi * R + r) * TSG_FX_LIMBS;
+            };
+            if (w0 == w1) {
+                fx_add(at(0, w0), af * (right - left), err);
+                continue;
+            }
+            fx_add(at(0, w0), af * (qd.windows[w0 + 1] - left), err);
+            fx_add(at(0, w1), af * (right - qd.windows[w1]), err);
+            if (w1 > w0 + 1) {
+                fx_add(at(1, w0 + 1), af, err);
+                fx_add(at(2, w1), af, err);
+            }
+        }
+    }
+}
+
+// One block per term: the running sum over windows of the difference arrays
+// (exact per window, then a fixed-order FP64 prefix) times the window
+// length, plus the partial windows, into w.leaf_win.
+__global__ void __launch_bounds__(256) k_wleaf_prefix(QueryParams q, QueryDev qd, WsDev w,
+    const unsigned long long *acc)
+{
+    __shared__ double s_run[256];
+    const int R = q.R, r = blockIdx.x;
+    const int64_t block = (int64_t) q.Wn * R * TSG_FX_LIMBS;
+    auto at = [&](int sign, int kind, int wi) {
+        return acc + sign * 3 * block + kind * block + ((int64_t) wi * R + r) * TSG_FX_LIMBS;
+    };
+    auto delta = [&](int wi) {
+        return fx_diff_value(at(0, 1, wi), at(0, 2, wi)) - fx_diff_value(at(1, 1, wi), at(1, 2, wi));
+    };
+    const int per = (q.Wn + blockDim.x - 1) / blockDim.x;
+    const int w0 = threadIdx.x * per, w1 = min(q.Wn, w0 + per);
+    double run = 0;
+    for (int wi = w0; wi < w1; wi++) {
+        run += delta(wi);
+    }
+    s_run[threadIdx.x] = run;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0;
+        for (int j = 0; j < (int) blockDim.x; j++) {
+            const double v = s_run[j];
+            s_run[j] = a;
+            a += v;
+        }
+    }
+    __syncthreads();
+    double active = s_run[threadIdx.x];
+    for (int wi = w0; wi < w1; wi++) {
+        active += delta(wi);
+        w.leaf_win[(int64_t) wi * R + r] = active * (qd.windows[wi + 1] - qd.windows[wi])
+            + fx_value(at(0, 0, wi)) - fx_value(at(1, 0, wi));
+    }
+}
+
+int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
+    int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
+    int32_t *err, int32_t *counter, cudaStream_t st)
+{
+    k_wreplay<<<(unsigned) grid, 64, 0, st>>>(v, q, W, K, slots_x, slots_par, slots_touched, ids,
+        xs, mstate, err, counter);
+    TSG_LAUNCHED();
+    return 0;
+}
+
+int genw_states(const TSView &v, int K, const double *W, const double *total,
+    const double *mstate, const int64_t *site_off, double *site_states, double *leaf_states,
+    cudaStream_t st)
+{
+    if (v.num_sites > 0 && site_states != nullptr) {
+        k_wsite_states<<<gen_grid(v.num_sites), 256, 0, st>>>(v, K, total, mstate, site_off,
+            site_states);
+        TSG_LAUNCHED();
+    }
+    if (v.num_leaves > 0 && leaf_states != nullptr) {
+        k_wleaf_states<<<gen_grid(v.num_leaves), 256, 0, st>>>(v, K, W, leaf_states);
+        TSG_LAUNCHED();
+    }
+    return 0;
+}
+
+int genw_eval(const TSView &v, const QueryParams &q, const QueryDev &d, const WsDev &w,
+    const int4 *ids, const double *vals, const int64_t *site_off, int64_t sbase, int64_t lbase,
+    unsigned long long *leaf_acc, int32_t R_total, int32_t r0, cudaStream_t st)
+{
+    if (q.branch) {
+        k_weval_items<<<(unsigned) ((v.num_chunks + 7) / 8), 256, 0, st>>>(v, q, w, ids, vals,
+            R_total, r0);
+        TSG_LAUNCHED();
+        TSG_CUDA(cudaMemsetAsync(leaf_acc, 0,
+            (size_t) q.Wn * q.R * TSG_FX_LIMBS * 8 * 6, st));
+        if (v.num_edges > 0 && v.num_leaves > 0) {
+            k_wleaf_areas<<<gen_grid(v.num_edges), 256, 0, st>>>(v, q, d, vals, lbase, R_total,
+                r0, leaf_acc, w.err);
+            TSG_LAUNCHED();
+        }
+        k_wleaf_prefix<<<(unsigned) q.R, 256, 0, st>>>(q, d, w, leaf_acc);
+        TSG_LAUNCHED();
+    }
+    if (q.site && v.num_sites > 0) {
+        k_wsite_values<<<gen_grid(v.num_sites), 256, 0, st>>>(v, q, w, site_off, vals, sbase,
+            R_total, r0);
+        TSG_LAUNCHED();
+    }
+    return 0;
+}
+
 }  // namespace tsg

@@ -99,26 +99,6 @@ __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, Qu
 // totals) gives the branch length alive over each whole window; area = that
 // x window length + the window's partial areas.  w.leaf_dbl: windows x
 // patterns doubles.
-__device__ __forceinline__ double fx_diff_value(const unsigned long long *a,
-    const unsigned long long *b)
-{
-    long long run[TSG_FX_LIMBS + 2];
-    for (int i = 0; i < TSG_FX_LIMBS; i++) {
-        run[i] = (long long) a[i] - (long long) b[i];
-    }
-    run[TSG_FX_LIMBS] = run[TSG_FX_LIMBS + 1] = 0;
-    for (int i = 0; i < TSG_FX_LIMBS + 1; i++) {
-        const long long cy = run[i] >> 32;
-        run[i] -= cy * (1ll << 32);
-        run[i + 1] += cy;
-    }
-    double v = 0;
-    for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
-        v = v * 4294967296.0 + (double) run[i];
-    }
-    return ldexp(v, -TSG_FX_FRAC);
-}
-
 __global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd, WsDev w)
 {
     __shared__ double s_run[256];

@@ -155,6 +155,15 @@ int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
     uint64_t *thi, int64_t *flag, int64_t *pos, void *cub_tmp, size_t cub_bytes, uint64_t *ulo,
     uint64_t *uhi, int64_t *U, cudaStream_t st);
 size_t gen_cub_bytes(int64_t n);
+int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
+    int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
+    int32_t *err, int32_t *counter, cudaStream_t st);
+int genw_states(const TSView &v, int K, const double *W, const double *total,
+    const double *mstate, const int64_t *site_off, double *site_states, double *leaf_states,
+    cudaStream_t st);
+int genw_eval(const TSView &v, const QueryParams &q, const QueryDev &d, const WsDev &w,
+    const int4 *ids, const double *vals, const int64_t *site_off, int64_t sbase, int64_t lbase,
+    unsigned long long *leaf_acc, int32_t R_total, int32_t r0, cudaStream_t st);
 int gen_eval(int form, const TSView &v, const QueryParams &q, const WsDev &w,
     const int64_t *site_off, const uint64_t *ulo, const uint64_t *uhi, int64_t U, const double *F,
     int32_t R_total, int32_t r0, cudaStream_t st);

@@ -1912,6 +1912,13 @@ struct tsg_general {
     int64_t *site_off = nullptr;
     WsDev w;
     QueryDev d;
+    // real-valued weights: states are listed, not deduplicated
+    bool weighted = false;
+    void *wbuf = nullptr;
+    double *states = nullptr;
+    int4 *ids = nullptr;
+    unsigned long long *leaf_acc = nullptr;
+    int64_t sbase = 0, lbase = 0;
 };
 
 namespace tsg {
@@ -1925,6 +1932,7 @@ static void general_release(tsg_general *g)
         cudaStreamSynchronize(g->st);
     }
     cudaFree(g->buf);
+    cudaFree(g->wbuf);
     if (g->ws != nullptr) {
         tsg_workspace_free(g->ws);
     }
@@ -2121,9 +2129,12 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
     for (int64_t r0 = 0; ret == 0 && r0 < R; r0 += rb_max) {
         QueryParams pb = q->p;
         pb.R = (int32_t) std::min<int64_t>(rb_max, R - r0);
-        if ((ret = gen_eval(g->form, v, pb, g->w, g->site_off, g->ulo, g->uhi, g->U, dF,
-                 (int32_t) R, (int32_t) r0, st))
-            != 0) {
+        ret = g->weighted
+            ? genw_eval(v, pb, g->d, g->w, g->ids, dF, g->site_off, g->sbase, g->lbase,
+                  g->leaf_acc, (int32_t) R, (int32_t) r0, st)
+            : gen_eval(g->form, v, pb, g->w, g->site_off, g->ulo, g->uhi, g->U, dF, (int32_t) R,
+                  (int32_t) r0, st);
+        if (ret != 0) {
             break;
         }
         if (pb.branch) {
@@ -2172,6 +2183,172 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
 int tsg_general_stat_free(tsg_general_t *g)
 {
     general_release(g);
+    return 0;
+}
+
+// Real-valued weights: the replay of a query with K all-sample sets (its
+// windows and workspace) and placeholder terms; the states are the weights
+// below each node.
+int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const double *weights, uint64_t R, uint64_t Wn, const double *windows, uint32_t options,
+    int64_t *num_states)
+{
+    *out = nullptr;
+    if (R < 1) {
+        return TSG_ERR_BAD_RESULT_DIMS;
+    }
+    if (K < 1) {
+        return TSG_ERR_BAD_STATE_DIMS;
+    }
+    if (K > 8) {
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    if (options & TSG_STAT_BOTH_MODES) {
+        return TSG_ERR_MULTIPLE_STAT_MODES;
+    }
+    const TSView &v = ts->v;
+    const int64_t n = v.num_samples;
+    std::vector<uint64_t> sizes((size_t) K, (uint64_t) n);
+    std::vector<int32_t> samples((size_t) n), sets((size_t) (K * n));
+    for (int64_t u = 0; u < v.num_nodes; u++) {
+        const int32_t si = ts->h_sample_index[(size_t) u];
+        if (si >= 0) {
+            samples[(size_t) si] = (int32_t) u;
+        }
+    }
+    for (uint64_t k = 0; k < K; k++) {
+        std::copy(samples.begin(), samples.end(), sets.begin() + (int64_t) (k * n));
+    }
+    const uint64_t Rb = std::min<uint64_t>(R, TSG_ITEM_RMAX);
+    std::vector<tsg_output_t> outs((size_t) Rb);
+    for (auto &o : outs) {
+        o.type = TSG_DIVERSITY;
+        o.idx[0] = o.idx[1] = o.idx[2] = o.idx[3] = 0;
+    }
+    tsg_general *g = new tsg_general();
+    g->R = (int32_t) R;
+    g->K = (int32_t) K;
+    g->weighted = true;
+    int ret = tsg_query_create(&g->q, ts, K, sizes.data(), sets.data(), Rb, outs.data(), Wn,
+        windows, options & ~(uint32_t) (TSG_PRECISION_F32_KAHAN | TSG_FORCE_GLOBAL_SWEEP));
+    if (ret != 0) {
+        delete g;
+        return ret;
+    }
+    tsg_query_t *q = g->q;
+    if (!q->smem) {
+        general_release(g);
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess
+        || tsg_workspace_create(&g->ws) != 0
+        || (ret = tsg_workspace_reserve(g->ws, q->ws_bytes)) != 0) {
+        cudaGetLastError();
+        general_release(g);
+        return ret != 0 ? ret : TSG_ERR_CUDA;
+    }
+    const QueryParams &p = q->p;
+    g->w = ws_bind(q, g->ws);
+    g->d = q->d;
+    std::vector<int64_t> site_off((size_t) v.num_sites + 1, 0);
+    for (int64_t s = 0; s < v.num_sites; s++) {
+        int32_t mx = 0;
+        for (int32_t m = ts->host.site_mut[(size_t) s]; m < ts->host.site_mut[(size_t) s + 1]; m++) {
+            mx = std::max(mx, ts->host.mut_allele[(size_t) m]);
+        }
+        site_off[(size_t) s + 1] = site_off[(size_t) s] + mx + 1;
+    }
+    const int64_t nsk = site_off[(size_t) v.num_sites];
+    const int64_t items = p.branch ? v.num_items : 0;
+    g->sbase = 2 * items;
+    g->lbase = g->sbase + (p.site ? nsk : 0);
+    const int64_t U = g->lbase + (p.branch ? v.num_leaves : 0);
+    g->U = U;
+    std::vector<double> total((size_t) K, 0.0);
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < K; k++) {
+            total[(size_t) k] += weights[j * K + k];
+        }
+    }
+    const int64_t L = std::max<int64_t>(v.max_local, 1);
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(v.num_spans,
+        2 * (int64_t) std::max(device_count_sms(), 1)));
+    // one allocation: W, totals, site offsets, per-CTA state, ids, states,
+    // mutation states, leaf accumulators, error word and span counter
+    int64_t off = 0;
+    auto take = [&](int64_t bytes) {
+        const int64_t o = off;
+        off += align_up(std::max<int64_t>(bytes, 8), 256);
+        return o;
+    };
+    const int64_t oW = take(n * (int64_t) K * 8), oT = take((int64_t) K * 8);
+    const int64_t oSO = take((v.num_sites + 1) * 8);
+    const int64_t oX = take(grid * L * (int64_t) K * 8), oP = take(grid * L * 4), oF = take(grid * L);
+    const int64_t oI = take(items * 16), oS = take(U * (int64_t) K * 8);
+    const int64_t oM = take(v.num_mutations * (int64_t) K * 8);
+    const int64_t oA = take((int64_t) Wn * (int64_t) Rb * TSG_FX_LIMBS * 8 * 6), oE = take(8);
+    if (cudaMalloc(&g->wbuf, (size_t) off) != cudaSuccess) {
+        cudaGetLastError();
+        general_release(g);
+        return TSG_ERR_NO_MEMORY;
+    }
+    char *b = (char *) g->wbuf;
+    double *dW = (double *) (b + oW), *dT = (double *) (b + oT);
+    g->site_off = (int64_t *) (b + oSO);
+    g->ids = (int4 *) (b + oI);
+    g->states = (double *) (b + oS);
+    g->leaf_acc = (unsigned long long *) (b + oA);
+    int32_t *derr = (int32_t *) (b + oE);
+    cudaStream_t st = g->st;
+    ret = 0;
+    if (cudaMemcpyAsync(dW, weights, (size_t) (n * K * 8), cudaMemcpyHostToDevice, st) != cudaSuccess
+        || cudaMemcpyAsync(dT, total.data(), (size_t) (K * 8), cudaMemcpyHostToDevice, st) != cudaSuccess
+        || cudaMemcpyAsync(g->site_off, site_off.data(), site_off.size() * 8,
+               cudaMemcpyHostToDevice, st) != cudaSuccess
+        || cudaMemsetAsync(derr, 0, 8, st) != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    }
+    if (ret == 0) {
+        ret = genw_replay(v, p, dW, (int) K, (double *) (b + oX), (int32_t *) (b + oP),
+            (uint8_t *) (b + oF), (int) grid, g->ids, g->states, (double *) (b + oM), derr,
+            derr + 1, st);
+    }
+    if (ret == 0) {
+        ret = genw_states(v, (int) K, dW, dT, (double *) (b + oM), g->site_off,
+            p.site ? g->states + g->sbase * (int64_t) K : nullptr,
+            p.branch ? g->states + g->lbase * (int64_t) K : nullptr, st);
+    }
+    if (ret == 0) {
+        int32_t herr = 0;
+        if (cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else if (herr != 0) {
+            ret = TSG_ERR_DEVICE_CHECK;
+        }
+    }
+    if (ret != 0) {
+        general_release(g);
+        return ret;
+    }
+    *num_states = U;
+    *out = g;
+    return 0;
+}
+
+int tsg_general_weighted_states(tsg_general_t *g, double *states)
+{
+    if (!g->weighted) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    if (g->U == 0) {
+        return 0;
+    }
+    if (cudaMemcpyAsync(states, g->states, (size_t) (g->U * g->K * 8), cudaMemcpyDeviceToHost,
+            g->st) != cudaSuccess
+        || cudaStreamSynchronize(g->st) != cudaSuccess) {
+        return TSG_ERR_CUDA;
+    }
     return 0;
 }
 

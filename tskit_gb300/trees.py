@@ -578,6 +578,48 @@ class TreeSequence:
             self._lib.tsg_general_stat_free(g)
         return res
 
+    def _ll_general_weighted(self, W, f, output_dim, windows, mode=None, span_normalise=True,
+                             polarised=False):
+        """The weighted sweep: f evaluated on the host at every state listed
+        by tsg_general_weighted_prepare (trees.c:1944-1972 for the
+        unpolarised branch sum f(x) + f(total - x))."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        R = int(output_dim)
+        if R < 1:
+            raise ValueError("output_dim must be at least 1")
+        K = W.shape[1]
+        g = ctypes.c_void_p()
+        U = ctypes.c_int64()
+        nat.check(self._lib.tsg_general_weighted_prepare(
+            ctypes.byref(g), self._handle, K, _ptr(W), R, len(win) - 1, _ptr(win), flags,
+            ctypes.byref(U)))
+        try:
+            states = np.zeros((U.value, K), dtype=np.float64)
+            nat.check(self._lib.tsg_general_weighted_states(g, _ptr(states)))
+            total = np.sum(W, axis=0)
+            branch = bool(flags & nat.STAT_BRANCH)
+            F = np.zeros((U.value, R))
+            for i in range(U.value):
+                v = np.asarray(f(states[i]), dtype=np.float64).reshape(-1)
+                if v.shape[0] != R:
+                    raise ValueError("summary function output has the wrong dimension")
+                if branch and not polarised:
+                    v = v + np.asarray(f(total - states[i]), dtype=np.float64).reshape(-1)
+                F[i] = v
+            res = np.zeros((len(win) - 1, R))
+            nat.check(self._lib.tsg_general_stat_finish(g, _ptr(F), _ptr(res)))
+        finally:
+            self._lib.tsg_general_stat_free(g)
+        return res
+
     def _check_summary(self, total, f, output_dim):
         """python/tskit/trees.py:7983-7993."""
         for x in [total, total * 0.0]:
@@ -590,18 +632,21 @@ class TreeSequence:
 
     def general_stat(self, W, f, output_dim, windows=None, polarised=False, mode=None,
                      span_normalise=True, strict=True):
-        """python/tskit/trees.py:7917-8004 for 0/1 weights (each column is a
-        set of samples; samples may be in several columns).  Other weights
-        are not supported on this path and raise ValueError."""
+        """python/tskit/trees.py:7917-8004.  Weights of 0 and 1 (each column a
+        set of samples) take the counting sweep, which evaluates f once per
+        distinct count vector; other real-valued weights (up to 8 columns)
+        take the weighted sweep, which evaluates f once per state it meets."""
         if mode is None:
             mode = "site"
         W = np.asarray(W, dtype=np.float64)
         if W.ndim != 2 or W.shape[0] != self.num_samples:
             raise ValueError("First dimension of W must be number of samples")
-        if not np.all((W == 0) | (W == 1)):
-            raise ValueError("Only weights of 0 or 1 are supported on this path")
         if strict:
             self._check_summary(np.sum(W, axis=0), f, output_dim)
+        if not np.all((W == 0) | (W == 1)):
+            return self.__run_windowed_stat(windows, self._ll_general_weighted, W, f, output_dim,
+                                            polarised=polarised, span_normalise=span_normalise,
+                                            mode=mode)
         samples = self.samples()
         sets = [samples[W[:, k] == 1] for k in range(W.shape[1])]
         if any(len(s) == 0 for s in sets):
