@@ -310,6 +310,16 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *self,
     uint32_t options, int64_t *num_states);
 int tsg_general_weighted_states(tsg_general_t *g, double *states);
 
+/* Replaces tsk_treeseq_genetic_relatedness_weighted (c/tskit/trees.c:
+ * 4838-4897, same arguments; weights host [n x num_weights], num_weights
+ * <= 7, index tuples pairs of weight columns, which are range-checked
+ * (TSG_ERR_BAD_SAMPLE_SET_INDEX) where the reference reads them unchecked;
+ * TSG_STAT_NONCENTRED as the reference's TSK_STAT_NONCENTRED): the weighted
+ * replay with the pair summary evaluated on the device. */
+int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_index_tuples, const int32_t *index_tuples,
+    uint64_t num_windows, const double *windows, double *result, uint32_t options);
+
 /* ----------------------------------------------- device-resident queries
  * A query is prepared once (validates and uploads sample sets, summary terms
  * and windows) and launched any number of times on a stream with a

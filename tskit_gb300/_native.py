@@ -54,6 +54,7 @@ ERR_BAD_SAMPLE_SET_INDEX = -907
 ERR_EMPTY_SAMPLE_SET = -908
 ERR_UNSUPPORTED_STAT_MODE = -909
 ERR_TIME_UNCALIBRATED = -910
+ERR_INSUFFICIENT_WEIGHTS = -913
 ERR_CUDA = -20001
 ERR_DEVICE_CHECK = -20002
 ERR_NOALLOC_TOO_LARGE = -20007
@@ -137,6 +138,8 @@ SIGNATURES = {
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _U64, _U64, _P, _U32,
                        ctypes.POINTER(_I64)]),
     "tsg_general_weighted_states": (ctypes.c_int, [_P, _P]),
+    "tsg_treeseq_genetic_relatedness_weighted": (
+        ctypes.c_int, [_P, _U64, _P, _U64, _P, _U64, _P, _P, _U32]),
     "tsg_query_create_afs": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _P, _U64, _P, _U64, _P, _U32]),
     "tsg_query_free": (ctypes.c_int, [_P]),

@@ -848,4 +848,49 @@ int genw_eval(const TSView &v, const QueryParams &q, const QueryDev &d, const Ws
     return 0;
 }
 
+// genetic_relatedness_weighted's summary (c/tskit/trees.c:4801-4837) at
+// every listed state: the weights carry a last column of 1/n; for pair k =
+// (i, j), (x_i - n_i p)(x_j - n_j p) with p the last component (centred) or
+// x_i x_j, plus the same at total - x when unpolarised branch.
+__global__ void k_wsummary_relatedness(const double *states, int64_t U, int K1,
+    const double *total, const int32_t *tuples, int R, double ones, int centred,
+    int complement, double *vals)
+{
+    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < U;
+         u += (int64_t) gridDim.x * blockDim.x) {
+        const double *x = states + u * K1;
+        for (int k = 0; k < R; k++) {
+            const int i = tuples[2 * k], j = tuples[2 * k + 1];
+            double v;
+            if (centred) {
+                const double p = x[K1 - 1];
+                v = (x[i] - total[i] * p) * (x[j] - total[j] * p);
+                if (complement) {
+                    const double pc = ones - p;
+                    v += ((total[i] - x[i]) - total[i] * pc) * ((total[j] - x[j]) - total[j] * pc);
+                }
+            } else {
+                v = x[i] * x[j];
+                if (complement) {
+                    v += (total[i] - x[i]) * (total[j] - x[j]);
+                }
+            }
+            vals[u * R + k] = v;
+        }
+    }
+}
+
+int genw_summary_relatedness(const double *states, int64_t U, int K1, const double *total,
+    const int32_t *tuples, int R, double ones, bool centred, bool complement, double *vals,
+    cudaStream_t st)
+{
+    if (U == 0) {
+        return 0;
+    }
+    k_wsummary_relatedness<<<gen_grid(U), 256, 0, st>>>(states, U, K1, total, tuples, R, ones,
+        centred ? 1 : 0, complement ? 1 : 0, vals);
+    TSG_LAUNCHED();
+    return 0;
+}
+
 }  // namespace tsg

@@ -161,6 +161,9 @@ int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, d
 int genw_states(const TSView &v, int K, const double *W, const double *total,
     const double *mstate, const int64_t *site_off, double *site_states, double *leaf_states,
     cudaStream_t st);
+int genw_summary_relatedness(const double *states, int64_t U, int K1, const double *total,
+    const int32_t *tuples, int R, double ones, bool centred, bool complement, double *vals,
+    cudaStream_t st);
 int genw_eval(const TSView &v, const QueryParams &q, const QueryDev &d, const WsDev &w,
     const int4 *ids, const double *vals, const int64_t *site_off, int64_t sbase, int64_t lbase,
     unsigned long long *leaf_acc, int32_t R_total, int32_t r0, cudaStream_t st);

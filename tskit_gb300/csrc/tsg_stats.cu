@@ -2105,26 +2105,24 @@ int tsg_general_stat_states(tsg_general_t *g, int32_t *states)
     return ret;
 }
 
-int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *result)
+}  // extern "C"
+
+namespace tsg {
+
+// The finish step with the values table (U x R) already on the device.
+static int general_finish(tsg_general *g, const double *dF, double *result)
 {
     const tsg_query_t *q = g->q;
     const TSView &v = q->ts->v;
     const int64_t Wn = q->p.Wn, R = g->R;
     const int64_t rb_max = q->p.R;
-    double *dF = nullptr, *dres = nullptr;
-    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(g->U * R * 8, 8)) != cudaSuccess
-        || cudaMalloc(&dres, (size_t) (Wn * rb_max * 8)) != cudaSuccess) {
+    double *dres = nullptr;
+    if (cudaMalloc(&dres, (size_t) (Wn * rb_max * 8)) != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(dF);
         return TSG_ERR_NO_MEMORY;
     }
     cudaStream_t st = g->st;
     int ret = 0;
-    if (g->U > 0
-        && cudaMemcpyAsync(dF, values, (size_t) (g->U * R * 8), cudaMemcpyHostToDevice, st)
-            != cudaSuccess) {
-        ret = TSG_ERR_CUDA;
-    }
     std::vector<double> block((size_t) (Wn * rb_max));
     for (int64_t r0 = 0; ret == 0 && r0 < R; r0 += rb_max) {
         QueryParams pb = q->p;
@@ -2175,10 +2173,34 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
             }
         }
     }
-    cudaFree(dF);
     cudaFree(dres);
     return ret;
 }
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *result)
+{
+    double *dF = nullptr;
+    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(g->U * g->R * 8, 8)) != cudaSuccess) {
+        cudaGetLastError();
+        return TSG_ERR_NO_MEMORY;
+    }
+    int ret = 0;
+    if (g->U > 0
+        && cudaMemcpyAsync(dF, values, (size_t) (g->U * g->R * 8), cudaMemcpyHostToDevice, g->st)
+            != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    }
+    if (ret == 0) {
+        ret = general_finish(g, dF, result);
+    }
+    cudaFree(dF);
+    return ret;
+}
+
 
 int tsg_general_stat_free(tsg_general_t *g)
 {
@@ -2334,6 +2356,74 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     *num_states = U;
     *out = g;
     return 0;
+}
+
+// tsk_treeseq_genetic_relatedness_weighted (c/tskit/trees.c:4838-4897): the
+// weights with a column of 1/n appended, the pair summary evaluated on the
+// device at every state of the weighted replay.
+int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_index_tuples, const int32_t *index_tuples,
+    uint64_t num_windows, const double *windows, double *result, uint32_t options)
+{
+    const int64_t n = self->v.num_samples;
+    if (num_weights == 0) {
+        return TSG_ERR_INSUFFICIENT_WEIGHTS;
+    }
+    for (uint64_t k = 0; k < 2 * num_index_tuples; k++) {
+        if (index_tuples[k] < 0 || (uint64_t) index_tuples[k] >= num_weights) {
+            return TSG_ERR_BAD_SAMPLE_SET_INDEX;
+        }
+    }
+    const uint64_t K1 = num_weights + 1;
+    std::vector<double> w((size_t) (n * K1)), total((size_t) K1, 0.0);
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < num_weights; k++) {
+            w[(size_t) (j * K1 + k)] = weights[j * num_weights + k];
+            total[(size_t) k] += weights[j * num_weights + k];
+        }
+        w[(size_t) (j * K1 + num_weights)] = 1.0 / (double) n;
+    }
+    // the complement of a state (unpolarised branch statistics) is taken
+    // from the weights' own column sums, as general_stat forms them; the
+    // summary's scale for the appended column is exactly 1
+    double ones = 0.0;
+    for (int64_t j = 0; j < n; j++) {
+        ones += w[(size_t) (j * K1 + num_weights)];
+    }
+    total[(size_t) num_weights] = 1.0;
+    tsg_general_t *g = nullptr;
+    int64_t U = 0;
+    int ret = tsg_general_weighted_prepare(&g, self, K1, w.data(), num_index_tuples, num_windows,
+        windows, options, &U);
+    if (ret != 0) {
+        return ret;
+    }
+    const int64_t R = (int64_t) num_index_tuples;
+    double *dF = nullptr, *dT = nullptr;
+    int32_t *dI = nullptr;
+    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(U * R * 8, 8)) != cudaSuccess
+        || cudaMalloc(&dT, (size_t) (K1 * 8)) != cudaSuccess
+        || cudaMalloc(&dI, (size_t) std::max<int64_t>(R * 8, 8)) != cudaSuccess) {
+        cudaGetLastError();
+        ret = TSG_ERR_NO_MEMORY;
+    } else if (cudaMemcpyAsync(dT, total.data(), (size_t) (K1 * 8), cudaMemcpyHostToDevice, g->st)
+            != cudaSuccess
+        || cudaMemcpyAsync(dI, index_tuples, (size_t) (R * 8), cudaMemcpyHostToDevice, g->st)
+            != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    } else {
+        const bool branch = g->q->p.branch, polarised = g->q->p.polarised;
+        ret = genw_summary_relatedness(g->states, U, (int) K1, dT, dI, (int) R,
+            ones, !(options & TSG_STAT_NONCENTRED), branch && !polarised, dF, g->st);
+        if (ret == 0) {
+            ret = general_finish(g, dF, result);
+        }
+    }
+    cudaFree(dF);
+    cudaFree(dT);
+    cudaFree(dI);
+    tsg_general_stat_free(g);
+    return ret;
 }
 
 int tsg_general_weighted_states(tsg_general_t *g, double *states)

@@ -424,6 +424,34 @@ class TreeSequence:
             _ptr(focal), _ptr(res), flags))
         return res
 
+    def _ll_genetic_relatedness_weighted(self, weights, indexes, windows, mode=None,
+                                         span_normalise=True, polarised=False, centre=True):
+        """Low-level call (python/_tskitmodule.c:7292-7370): result shape
+        (num_windows, num_index_tuples)."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        if polarised:
+            flags |= nat.STAT_POLARISED
+        if not centre:
+            flags |= nat.STAT_NONCENTRED
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.ndim != 2:
+            raise ValueError("Weights must be a 2D array")
+        if w.shape[0] != self.num_samples:
+            raise ValueError("First dimension must be num_samples")
+        idx = np.ascontiguousarray(indexes, dtype=np.int32)
+        if idx.ndim != 2 or idx.shape[0] < 1 or idx.shape[1] != 2:
+            raise ValueError("indexes must be a k x 2 array.")
+        res = np.zeros((len(win) - 1, idx.shape[0]))
+        nat.check(self._lib.tsg_treeseq_genetic_relatedness_weighted(
+            self._handle, w.shape[1], _ptr(w), idx.shape[0], _ptr(idx), len(win) - 1,
+            _ptr(win), _ptr(res), flags))
+        return res
+
     def _ll_one_way(self, typ):
         def method(sample_set_sizes, sample_sets, windows, mode=None, span_normalise=True,
                    polarised=False):
@@ -765,6 +793,39 @@ class TreeSequence:
         return self.__run_windowed_stat(windows, self._ll_genetic_relatedness_vector, W,
                                         mode=mode, span_normalise=span_normalise,
                                         centre=centre, nodes=nodes)
+
+    def genetic_relatedness_weighted(self, W, indexes=None, windows=None, mode="site",
+                                     span_normalise=True, polarised=False, centre=True):
+        """python/tskit/trees.py:9104-9155 with the argument handling of
+        __k_way_weighted_stat (trees.py:8414-8457): column k of the result
+        is sum_{a,b} W[a,i] W[b,j] C[a,b] for the k-th index pair (i, j), C
+        the genetic relatedness between samples; indexes default to (0, 1)
+        when W has exactly two columns, and a single pair drops the last
+        dimension."""
+        if len(W) != self.num_samples:
+            raise ValueError("First trait dimension must be equal to number of samples.")
+        W = np.asarray(W)
+        k = 2
+        if indexes is None:
+            if W.shape[1] != k:
+                raise ValueError(
+                    "Must specify indexes if there are not exactly {} columns "
+                    "in W.".format(k))
+            indexes = np.arange(k, dtype=np.int32)
+        drop_dimension = False
+        indexes = safe_np_int_cast(indexes, np.int32)
+        if len(indexes.shape) == 1:
+            indexes = indexes.reshape((1, indexes.shape[0]))
+            drop_dimension = True
+        if len(indexes.shape) != 2 or indexes.shape[1] != k:
+            raise ValueError(
+                "Indexes must be convertable to a 2D numpy array with {} columns".format(k))
+        stat = self.__run_windowed_stat(windows, self._ll_genetic_relatedness_weighted, W,
+                                        indexes, mode=mode, span_normalise=span_normalise,
+                                        polarised=polarised, centre=centre)
+        if drop_dimension:
+            stat = stat.reshape(stat.shape[:-1])
+        return stat
 
     def allele_frequency_spectrum(self, sample_sets=None, windows=None, time_windows=None,
                                   mode="site", span_normalise=True, polarised=False):
