@@ -295,6 +295,9 @@ int tsg_general_stat_prepare(tsg_general_t **general, const tsg_treeseq_t *self,
     int64_t *num_states);
 int tsg_general_stat_states(tsg_general_t *general, int32_t *states);
 int tsg_general_stat_finish(tsg_general_t *general, const double *values, double *result);
+/* Doubles finish writes: num_windows x num_outputs, or num_windows x
+ * num_nodes x num_outputs in node mode. */
+int64_t tsg_general_stat_result_size(const tsg_general_t *general);
 int tsg_general_stat_free(tsg_general_t *general);
 
 /* general_stat with real-valued weights (tsk_treeseq_general_stat,

@@ -137,6 +137,10 @@ class OracleTS:
     def num_samples(self):
         return len(self.samples)
 
+    @property
+    def num_nodes(self):
+        return self.tables.num_nodes
+
 
 def _windows(ts, windows):
     if windows is None:
@@ -145,7 +149,7 @@ def _windows(ts, windows):
 
 
 def _mode_flags(mode):
-    return {"branch": STAT_BRANCH, "site": STAT_SITE, None: STAT_SITE}[mode]
+    return {"branch": STAT_BRANCH, "site": STAT_SITE, "node": STAT_NODE, None: STAT_SITE}[mode]
 
 
 def sample_count_stat(ts, sample_sets, outputs, windows=None, mode="site",
@@ -169,8 +173,11 @@ def sample_count_stat(ts, sample_sets, outputs, windows=None, mode="site",
             outs[r].idx[q] = idx[q]
     win = _windows(ts, windows)
     Wn = len(win) - 1
-    res = np.zeros((Wn, len(outputs)))
     opts = _mode_flags(mode)
+    if opts & STAT_NODE:
+        res = np.zeros((Wn, ts.num_nodes, len(outputs)))
+    else:
+        res = np.zeros((Wn, len(outputs)))
     if span_normalise:
         opts |= STAT_SPAN_NORMALISE
     if polarised:
@@ -355,7 +362,8 @@ def call(ots, method, kwargs):
         out = np.ones_like(dvg)
         for i, (u, v) in enumerate(tuples):
             with np.errstate(divide="ignore", invalid="ignore"):
-                out[:, i] -= 2 * (dvs[:, u] + dvs[:, v]) / (dvs[:, u] + dvs[:, v] + 2 * dvg[:, i])
+                out[..., i] -= 2 * (dvs[..., u] + dvs[..., v]) / (
+                    dvs[..., u] + dvs[..., v] + 2 * dvg[..., i])
         return out
     if method == "Tajimas_D":
         sets = _sets(ots, kw.pop("sample_sets", None))

@@ -11,6 +11,7 @@
  *
  * Restated reference functions (paths inside the tskit project):
  *   branch sweep       c/tskit/trees.c:1352-1523  tsk_treeseq_branch_general_stat
+ *   node sweep         c/tskit/trees.c:1788-1918  tsk_treeseq_node_general_stat
  *   site sweep         c/tskit/trees.c:1654-1776  tsk_treeseq_site_general_stat
  *   allele weights     c/tskit/trees.c:1525-1652  get_allele_weights / site result
  *   unpolarised f      c/tskit/trees.c:1944-1972
@@ -286,6 +287,103 @@ out:
     return ret;
 }
 
+/* ----------------------------------------------------------- node sweep */
+/*
+ * Node mode (trees.c:1788-1918): for every node, the integral along each
+ * window of f at the node's state.  Whenever a root-path walk changes a
+ * node's state, the interval since the node's last update is added with the
+ * old summary; at each window's end every node is flushed.
+ * result: Wn x N x R.
+ */
+static int node_stat(const orc_ts_t *ts, summary_ctx_t *c, const double *W, int32_t Wn,
+    const double *windows, double *result)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, K = c->K, R = c->R;
+    const int unpol = !c->polarised;
+    int32_t *parent = malloc((size_t) (N > 0 ? N : 1) * sizeof(int32_t));
+    double *x = calloc((size_t) (N > 0 ? N : 1) * K, sizeof(double));
+    double *s = calloc((size_t) (N > 0 ? N : 1) * R, sizeof(double));
+    double *last = calloc((size_t) (N > 0 ? N : 1), sizeof(double));
+    int ret = ORC_ERR_NO_MEMORY;
+    if (!parent || !x || !s || !last) {
+        goto out;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        memcpy(x + (int64_t) ts->samples[j] * K, W + (int64_t) j * K, (size_t) K * sizeof(double));
+    }
+    for (int32_t u = 0; u < N; u++) {
+        summary(c, x + (int64_t) u * K, s + (int64_t) u * R, unpol);
+    }
+    memset(result, 0, (size_t) Wn * N * R * sizeof(double));
+    int32_t tj = 0, tk = 0, w = 0;
+    double left = 0, L = ts->sequence_length;
+    while (tj < E || left < L) {
+        for (int pass = 0; pass < 2; pass++) {
+            for (;;) {
+                int32_t e;
+                if (pass == 0) {
+                    if (!(tk < E && ts->edge_right[ts->rem[tk]] == left)) {
+                        break;
+                    }
+                    e = ts->rem[tk++];
+                } else {
+                    if (!(tj < E && ts->edge_left[ts->ins[tj]] == left)) {
+                        break;
+                    }
+                    e = ts->ins[tj++];
+                    parent[ts->edge_child[e]] = ts->edge_parent[e];
+                }
+                const int32_t ch = ts->edge_child[e];
+                const double sign = pass == 0 ? -1.0 : 1.0;
+                for (int32_t u = ts->edge_parent[e]; u != -1; u = parent[u]) {
+                    double *out = result + ((int64_t) w * N + u) * R;
+                    double *su = s + (int64_t) u * R;
+                    for (int32_t r = 0; r < R; r++) {
+                        out[r] += (left - last[u]) * su[r];
+                    }
+                    last[u] = left;
+                    for (int32_t k = 0; k < K; k++) {
+                        x[(int64_t) u * K + k] += sign * x[(int64_t) ch * K + k];
+                    }
+                    summary(c, x + (int64_t) u * K, su, unpol);
+                }
+                if (pass == 0) {
+                    parent[ch] = -1;
+                }
+            }
+        }
+        double right = L;
+        if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+            right = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+            right = ts->edge_right[ts->rem[tk]];
+        }
+        while (w < Wn && windows[w + 1] <= right) {
+            const double wr = windows[w + 1];
+            for (int32_t u = 0; u < N; u++) {
+                double *out = result + ((int64_t) w * N + u) * R;
+                for (int32_t r = 0; r < R; r++) {
+                    out[r] += (wr - last[u]) * s[(int64_t) u * R + r];
+                }
+                last[u] = wr;
+            }
+            w++;
+        }
+        left = right;
+    }
+    ret = 0;
+out:
+    free(parent);
+    free(x);
+    free(s);
+    free(last);
+    return ret;
+}
+
 /* ----------------------------------------------------------- site sweep */
 /* allele states for one site: states[a*K + k] (trees.c:1525-1612) */
 static int32_t site_allele_states(const orc_ts_t *ts, int32_t m0, int32_t m1,
@@ -417,7 +515,7 @@ static void site_stat_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
 /*
  * Sample-count statistic (tsk_treeseq_sample_count_stat + general_stat).
  * W: num_samples x K weights indexed by sample order; n: K set sizes.
- * windows: Wn+1 breakpoints.  result: Wn x R.
+ * windows: Wn+1 breakpoints.  result: Wn x R (node mode: Wn x N x R).
  */
 int orc_sample_count_stat(const orc_ts_t *ts, int32_t K, const double *W,
     const double *n, int32_t R, const orc_output_t *outs, int32_t Wn,
@@ -445,7 +543,11 @@ int orc_sample_count_stat(const orc_ts_t *ts, int32_t K, const double *W,
     c.total = total;
     c.tmp_x = tmp;
     c.tmp_y = tmp + K;
-    if (options & ORC_STAT_BRANCH) {
+    int64_t row = R;
+    if (options & ORC_STAT_NODE) {
+        ret = node_stat(ts, &c, W, Wn, windows, result);
+        row = (int64_t) ts->num_nodes * R;
+    } else if (options & ORC_STAT_BRANCH) {
         ret = branch_stat(ts, &c, W, Wn, windows, result);
     } else {
         site_stat_ctx_t s;
@@ -470,7 +572,7 @@ int orc_sample_count_stat(const orc_ts_t *ts, int32_t K, const double *W,
         free(s.y);
     }
     if (ret == 0 && (options & ORC_STAT_SPAN_NORMALISE)) {
-        span_normalise(Wn, windows, R, result);
+        span_normalise(Wn, windows, row, result);
     }
     free(total);
     free(tmp);

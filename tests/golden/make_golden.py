@@ -205,6 +205,34 @@ def cases_for(ts, rng):
     if n >= 1:
         cases.append(("diversity", dict(sample_sets=[[samples[0]]], mode="site")))
         cases.append(("diversity", dict(sample_sets=[[samples[0]]], mode="branch")))
+    # node mode (trees.c:1788-1918), on the sets drawn above (no new draws, so
+    # the earlier cases keep their inputs)
+    if n >= 2:
+        for w in wins:
+            cases.append(("diversity", dict(mode="node", windows=w)))
+            cases.append(("segregating_sites", dict(mode="node", windows=w)))
+        cases.append(("diversity", dict(mode="node", span_normalise=False)))
+    if n >= 4:
+        for w in wins:
+            cases.append(("divergence", dict(sample_sets=sets2, mode="node", windows=w)))
+            cases.append(("Fst", dict(sample_sets=sets2, mode="node", windows=w)))
+            cases.append(("genetic_relatedness", dict(sample_sets=sets2, indexes=[[0, 1], [1, 1]],
+                                                      mode="node", windows=w,
+                                                      proportion=False)))
+        cases.append(("genetic_relatedness", dict(sample_sets=sets2, indexes=[[0, 1]],
+                                                  mode="node", proportion=False, centre=False,
+                                                  polarised=False)))
+        cases.append(("Y2", dict(sample_sets=sets2, mode="node", windows=wins[1])))
+        cases.append(("f2", dict(sample_sets=sets2, mode="node")))
+        cases.append(("Y1", dict(sample_sets=sets2, mode="node")))
+        cases.append(("Tajimas_D", dict(sample_sets=sets2, mode="node")))
+    if n >= 6:
+        cases.append(("Y3", dict(sample_sets=sets3, mode="node", windows=wins[1])))
+        cases.append(("f3", dict(sample_sets=sets3, mode="node")))
+    if n >= 8:
+        cases.append(("f4", dict(sample_sets=sets4, mode="node", windows=wins[1])))
+    if n >= 1:
+        cases.append(("diversity", dict(sample_sets=[[samples[0]]], mode="node")))
     return cases
 
 

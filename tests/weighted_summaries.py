@@ -21,3 +21,15 @@ SUMMARIES = {
     "mixed": (2, 3, _mixed),
     "three": (3, 2, _three),
 }
+
+
+def _count_pair(x):
+    # sample_count_stat summaries see the set sizes through closure defaults
+    return np.array([x[0] * (6.0 - x[0]), x[0] * x[1] - 2.0 * x[1]])
+
+
+# sample_count_stat summaries: name -> (set sizes, output dimension, f); the
+# sets are the first sizes[k] samples after the previous sets
+COUNT_SUMMARIES = {
+    "pair": ((6, 5), 2, _count_pair),
+}

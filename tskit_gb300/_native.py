@@ -133,6 +133,7 @@ SIGNATURES = {
                        ctypes.POINTER(_I64)]),
     "tsg_general_stat_states": (ctypes.c_int, [_P, _P]),
     "tsg_general_stat_finish": (ctypes.c_int, [_P, _P, _P]),
+    "tsg_general_stat_result_size": (ctypes.c_int64, [_P]),
     "tsg_general_stat_free": (ctypes.c_int, [_P]),
     "tsg_general_weighted_prepare": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _U64, _U64, _P, _U32,

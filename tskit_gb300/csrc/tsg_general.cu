@@ -422,7 +422,7 @@ int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K
 // root-path batch takes one node per lane, each adding all components.
 __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const double *W,
     int K, double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int4 *ids, double *xs,
-    double *mstate, int32_t *err, int32_t *counter)
+    double *mstate, double *init, int32_t *err, int32_t *counter)
 {
     __shared__ int s_span;
     __shared__ int32_t s_list[TSG_TOUCH_CAP];
@@ -475,6 +475,20 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
             }
         }
         __syncwarp();
+        // node mode: the first tree's state of every stateful node of span 0
+        if (init != nullptr && s == 0) {
+            for (int32_t l = lane; l < Ls; l += 32) {
+                const int32_t gl = l2g[l];
+                if (gl < 0 || gl >= ts.num_nodes) {
+                    dev_error(err, DEV_NODE_OUT_OF_BOUNDS);
+                    continue;
+                }
+                for (int k = 0; k < K; k++) {
+                    init[(int64_t) gl * K + k] = x[(int64_t) l * K + k];
+                }
+            }
+            __syncwarp();
+        }
         // first tree of the sequence: its stateful nodes in alive-list order
         if (q.branch && s == 0) {
             int64_t at = ts.tree_item_off[t0];
@@ -798,10 +812,10 @@ __global__ void __launch_bounds__(256) k_wleaf_prefix(QueryParams q, QueryDev qd
 
 int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
     int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
-    int32_t *err, int32_t *counter, cudaStream_t st)
+    double *init, int32_t *err, int32_t *counter, cudaStream_t st)
 {
     k_wreplay<<<(unsigned) grid, 64, 0, st>>>(v, q, W, K, slots_x, slots_par, slots_touched, ids,
-        xs, mstate, err, counter);
+        xs, mstate, init, err, counter);
     TSG_LAUNCHED();
     return 0;
 }
@@ -890,6 +904,256 @@ int genw_summary_relatedness(const double *states, int64_t U, int K1, const doub
     k_wsummary_relatedness<<<gen_grid(U), 256, 0, st>>>(states, U, K1, total, tuples, R, ones,
         centred ? 1 : 0, complement ? 1 : 0, vals);
     TSG_LAUNCHED();
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Node mode (tsk_treeseq_node_general_stat, c/tskit/trees.c:1788-1918): per
+// node and window, the integral along the genome of f at the node's state.
+// A node's state is piecewise constant and changes only where the replay
+// touches it, so the replay's items (node, tree, state after) sorted by
+// (node, tree), with each node's state at the start of the sequence, give
+// every node's intervals: one thread per node and output walks them in
+// genome order, adding (end - start) x f(state) per interval and window in
+// the order the reference's sweep adds them.
+
+// every node's own weight (samples) or zero, before the first tree's state
+// is written over it by the replay
+__global__ void k_node_init(TSView ts, int K, const double *W, double *init)
+{
+    for (int64_t g = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; g < ts.num_nodes;
+         g += (int64_t) gridDim.x * blockDim.x) {
+        const int32_t si = ts.sample_index[g];
+        for (int k = 0; k < K; k++) {
+            init[g * K + k] = si >= 0 ? W[(int64_t) si * K + k] : 0.0;
+        }
+    }
+}
+
+// sort keys (global node << 32 | tree) of the items, one warp per chunk
+// (an item whose node is out of range is flagged and sorts last, outside
+// every node's range)
+__global__ void __launch_bounds__(256) k_node_keys(TSView ts, const int4 *ids, uint64_t *keys,
+    int32_t *idx, int32_t *err)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t c = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= ts.num_chunks) {
+        return;
+    }
+    const int32_t s = ts.chunk_span[c], t = ts.chunk_tree[c];
+    const int64_t lo = ts.span_local_off[s];
+    const int64_t Ls = ts.span_local_off[s + 1] - lo;
+    const int32_t *l2g = ts.span_l2g + lo;
+    for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c] && i < ts.num_items; i += 32) {
+        const int32_t u = ids[i].x;
+        const int32_t g = u >= 0 && u < Ls ? l2g[u] : -1;
+        idx[i] = (int32_t) i;
+        if (g < 0 || g >= ts.num_nodes) {
+            dev_error(err, DEV_ITEM_PLAN);
+            keys[i] = ~0ull;
+            continue;
+        }
+        keys[i] = ((uint64_t) (uint32_t) g << 32) | (uint32_t) t;
+    }
+}
+
+// the state list: each item's state after its transition, then each node's
+// state at the start of the sequence
+__global__ void k_node_states(int64_t I, int64_t N, int K, const double *xs, const double *init,
+    double *states)
+{
+    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < I + N;
+         u += (int64_t) gridDim.x * blockDim.x) {
+        const double *src = u < I ? xs + (2 * u + 1) * K : init + (u - I) * K;
+        for (int k = 0; k < K; k++) {
+            states[u * K + k] = src[k];
+        }
+    }
+}
+
+// result [Wn x N x R]; vals: f at state row u (U x R)
+__global__ void k_node_walk(TSView ts, int Wn, const double *windows, const uint64_t *keys,
+    const int32_t *idx, int64_t I, const double *vals, int R, int span_normalise,
+    double *result, int32_t *err)
+{
+    const int64_t N = ts.num_nodes;
+    for (int64_t tid = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; tid < N * R;
+         tid += (int64_t) gridDim.x * blockDim.x) {
+        const int64_t g = tid / R;
+        const int r = (int) (tid - g * R);
+        int64_t j = lower_bound(keys, I, (uint64_t) g << 32);
+        const int64_t hi = lower_bound(keys, I, (uint64_t) (g + 1) << 32);
+        double f = vals[(I + g) * R + r];
+        int w = 0;
+        double last = windows[0], acc = 0.0;
+        auto flush = [&]() {
+            const double v = span_normalise ? acc / (windows[w + 1] - windows[w]) : acc;
+            result[((int64_t) w * N + g) * R + r] = v;
+            acc = 0.0;
+            w++;
+            last = windows[w];
+        };
+        for (; j < hi; j++) {
+            const uint32_t t = (uint32_t) keys[j];
+            const int32_t i = idx[j];
+            if (t >= (uint64_t) ts.num_trees || i < 0 || i >= I) {
+                dev_error(err, DEV_ITEM_PLAN);
+                break;
+            }
+            // items lie strictly inside the sequence, so before the last
+            // window's end
+            const double p = ts.breakpoints[t];
+            while (w + 1 < Wn && windows[w + 1] <= p) {
+                acc += (windows[w + 1] - last) * f;
+                flush();
+            }
+            acc += (p - last) * f;
+            last = p;
+            f = vals[(int64_t) i * R + r];
+        }
+        while (w < Wn) {
+            acc += (windows[w + 1] - last) * f;
+            flush();
+        }
+    }
+}
+
+// f of the built-in summaries at real-valued states (counts as doubles),
+// with the summary functions' own divisions (c/tskit/trees.c:3934 diversity,
+// 4221 segregating sites, 4248 Y1, 4690 divergence, 4729/4755 relatedness,
+// 4899 Y2, 4938 f2, 5177 Y3, 5219 f3, 5266 f4): a node's summary is exactly
+// zero wherever the reference's is, e.g. at the root.
+__device__ double node_summary(const QueryParams &q, int r, const double *x)
+{
+    const Term &t = q.term[r];
+    const int i = t.idx[0], j = t.idx[1], k = t.idx[2], l = t.idx[3];
+    const double xi = x[i], xj = x[j], xk = x[k], xl = x[l];
+    const double ni = q.set_size[i], nj = q.set_size[j], nk = q.set_size[k], nl = q.set_size[l];
+    switch (t.type) {
+        case TSG_DIVERSITY:
+            return xi * (ni - xi) / (ni * (ni - 1));
+        case TSG_SEGREGATING_SITES:
+            return (double) (xi > 0) * (1 - xi / ni);
+        case TSG_Y1:
+            return xi * (ni - xi) * (ni - xi - 1) / (ni * (ni - 1) * (ni - 2));
+        case TSG_DIVERGENCE:
+            return xi * (nj - xj) / (ni * (nj - (double) (i == j)));
+        case TSG_Y2:
+            return xi * (nj - xj) * (nj - xj - 1) / (ni * nj * (nj - 1));
+        case TSG_F2:
+            return (xi * (xi - 1) * (nj - xj) * (nj - xj - 1) - xi * (ni - xi) * (nj - xj) * xj)
+                / (ni * (ni - 1) * nj * (nj - 1));
+        case TSG_Y3:
+            return xi * (nj - xj) * (nk - xk) / (ni * nj * nk);
+        case TSG_F3:
+            return (xi * (xi - 1) * (nj - xj) * (nk - xk) - xi * (ni - xi) * (nj - xj) * xk)
+                / (ni * (ni - 1) * nj * nk);
+        case TSG_F4:
+            return (xi * xk * (nj - xj) * (nl - xl) - xi * xl * (nj - xj) * (nk - xk))
+                / (ni * nj * nk * nl);
+        case TSG_RELATEDNESS: {
+            double sumx = 0.0;
+            for (int m = 0; m < q.K; m++) {
+                sumx += x[m] / q.set_size[m];
+            }
+            const double meanx = sumx / (double) q.K;
+            return (xi / ni - meanx) * (xj / nj - meanx);
+        }
+        case TSG_RELATEDNESS_NONCENTRED:
+            return xi * xj / (ni * nj);
+        default:
+            return NAN;
+    }
+}
+
+// plus f at the complement (set sizes - x) when unpolarised
+// (c/tskit/trees.c:1944-1972)
+__global__ void k_node_term_values(QueryParams q, const double *states, int64_t U, int K,
+    int unpol, double *vals)
+{
+    double c[TSG_KMAX];
+    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < U;
+         u += (int64_t) gridDim.x * blockDim.x) {
+        const double *x = states + u * K;
+        for (int k = 0; k < K && k < TSG_KMAX; k++) {
+            c[k] = q.set_size[k] - x[k];
+        }
+        for (int r = 0; r < q.R; r++) {
+            double v = node_summary(q, r, x);
+            if (unpol) {
+                v += node_summary(q, r, c);
+            }
+            vals[u * q.R + r] = v;
+        }
+    }
+}
+
+int node_init(const TSView &v, int K, const double *W, double *init, cudaStream_t st)
+{
+    if (v.num_nodes > 0) {
+        k_node_init<<<gen_grid(v.num_nodes), 256, 0, st>>>(v, K, W, init);
+        TSG_LAUNCHED();
+    }
+    return 0;
+}
+
+size_t node_sort_bytes(int64_t I)
+{
+    size_t temp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, temp, (const uint64_t *) nullptr,
+        (uint64_t *) nullptr, (const int32_t *) nullptr, (int32_t *) nullptr,
+        (int) std::max<int64_t>(I, 1), 0, 64);
+    return temp;
+}
+
+// items sorted by (node, tree), and the state list
+int node_order(const TSView &v, int K, const int4 *ids, const double *xs, const double *init,
+    uint64_t *keys, uint64_t *keys_sorted, int32_t *idx, int32_t *idx_sorted, void *temp,
+    size_t temp_bytes, double *states, int32_t *err, cudaStream_t st)
+{
+    const int64_t I = v.num_items, N = v.num_nodes;
+    if (I > 0 && v.num_chunks > 0) {
+        k_node_keys<<<(unsigned) ((v.num_chunks + 7) / 8), 256, 0, st>>>(v, ids, keys, idx, err);
+        TSG_LAUNCHED();
+        int bits = 32;
+        while (bits < 64 && ((uint64_t) N >> (bits - 32)) != 0) {
+            bits++;
+        }
+        size_t tb = temp_bytes;
+        if (cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_sorted, idx, idx_sorted, (int) I,
+                0, bits, st) != cudaSuccess) {
+            return TSG_ERR_CUDA;
+        }
+        TSG_LAUNCHED();
+    }
+    if (I + N > 0) {
+        k_node_states<<<gen_grid(I + N), 256, 0, st>>>(I, N, K, xs, init, states);
+        TSG_LAUNCHED();
+    }
+    return 0;
+}
+
+int node_term_values(const QueryParams &q, const double *states, int64_t U, int K, bool unpol,
+    double *vals, cudaStream_t st)
+{
+    if (U > 0) {
+        k_node_term_values<<<gen_grid(U), 256, 0, st>>>(q, states, U, K, unpol ? 1 : 0, vals);
+        TSG_LAUNCHED();
+    }
+    return 0;
+}
+
+int node_walk(const TSView &v, int Wn, const double *windows, const uint64_t *keys_sorted,
+    const int32_t *idx_sorted, const double *vals, int R, bool span_normalise, double *result,
+    int32_t *err, cudaStream_t st)
+{
+    const int64_t n = v.num_nodes * (int64_t) R;
+    if (n > 0) {
+        k_node_walk<<<gen_grid(n), 256, 0, st>>>(v, Wn, windows, keys_sorted, idx_sorted,
+            v.num_items, vals, R, span_normalise ? 1 : 0, result, err);
+        TSG_LAUNCHED();
+    }
     return 0;
 }
 

@@ -157,7 +157,18 @@ int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
 size_t gen_cub_bytes(int64_t n);
 int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
     int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
-    int32_t *err, int32_t *counter, cudaStream_t st);
+    double *init, int32_t *err, int32_t *counter, cudaStream_t st);
+// node mode
+int node_init(const TSView &v, int K, const double *W, double *init, cudaStream_t st);
+size_t node_sort_bytes(int64_t I);
+int node_order(const TSView &v, int K, const int4 *ids, const double *xs, const double *init,
+    uint64_t *keys, uint64_t *keys_sorted, int32_t *idx, int32_t *idx_sorted, void *temp,
+    size_t temp_bytes, double *states, int32_t *err, cudaStream_t st);
+int node_term_values(const QueryParams &q, const double *states, int64_t U, int K, bool unpol,
+    double *vals, cudaStream_t st);
+int node_walk(const TSView &v, int Wn, const double *windows, const uint64_t *keys_sorted,
+    const int32_t *idx_sorted, const double *vals, int R, bool span_normalise, double *result,
+    int32_t *err, cudaStream_t st);
 int genw_states(const TSView &v, int K, const double *W, const double *total,
     const double *mstate, const int64_t *site_off, double *site_states, double *leaf_states,
     cudaStream_t st);

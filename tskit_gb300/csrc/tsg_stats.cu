@@ -1919,6 +1919,11 @@ struct tsg_general {
     int4 *ids = nullptr;
     unsigned long long *leaf_acc = nullptr;
     int64_t sbase = 0, lbase = 0;
+    // node mode: items sorted by (node, tree); states are the items' states
+    // after their transitions, then every node's initial state
+    bool node = false;
+    uint64_t *node_keys = nullptr;
+    int32_t *node_idx = nullptr;
 };
 
 namespace tsg {
@@ -2110,8 +2115,49 @@ int tsg_general_stat_states(tsg_general_t *g, int32_t *states)
 namespace tsg {
 
 // The finish step with the values table (U x R) already on the device.
+// Node mode: every node's window integrals of f (values dF, one row per
+// listed state), result [Wn x N x R].
+static int node_finish(tsg_general *g, const double *dF, double *result)
+{
+    const tsg_query_t *q = g->q;
+    const TSView &v = q->ts->v;
+    const int64_t n = (int64_t) q->p.Wn * v.num_nodes * g->R;
+    const int64_t nb = align_up(std::max<int64_t>(n * 8, 8), 256);
+    double *dres = nullptr;
+    if (cudaMalloc(&dres, (size_t) (nb + 8)) != cudaSuccess) {
+        cudaGetLastError();
+        return TSG_ERR_NO_MEMORY;
+    }
+    int32_t *derr = (int32_t *) ((char *) dres + nb), herr = 0;
+    int ret = cudaMemsetAsync(derr, 0, 4, g->st) == cudaSuccess ? 0 : TSG_ERR_CUDA;
+    if (ret == 0) {
+        ret = node_walk(v, q->p.Wn, g->d.windows, g->node_keys, g->node_idx, dF, g->R,
+            q->span_normalise, dres, derr, g->st);
+    }
+    if (ret == 0
+        && (cudaGetLastError() != cudaSuccess
+            || cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, g->st) != cudaSuccess
+            || cudaStreamSynchronize(g->st) != cudaSuccess)) {
+        ret = TSG_ERR_CUDA;
+    }
+    if (ret == 0 && herr != 0) {
+        ret = TSG_ERR_DEVICE_CHECK;
+    }
+    if (ret == 0 && n > 0
+        && (cudaMemcpyAsync(result, dres, (size_t) (n * 8), cudaMemcpyDeviceToHost, g->st)
+                != cudaSuccess
+            || cudaStreamSynchronize(g->st) != cudaSuccess)) {
+        ret = TSG_ERR_CUDA;
+    }
+    cudaFree(dres);
+    return ret;
+}
+
 static int general_finish(tsg_general *g, const double *dF, double *result)
 {
+    if (g->node) {
+        return node_finish(g, dF, result);
+    }
     const tsg_query_t *q = g->q;
     const TSView &v = q->ts->v;
     const int64_t Wn = q->p.Wn, R = g->R;
@@ -2202,6 +2248,12 @@ int tsg_general_stat_finish(tsg_general_t *g, const double *values, double *resu
 }
 
 
+int64_t tsg_general_stat_result_size(const tsg_general_t *g)
+{
+    const int64_t rows = g->node ? g->q->ts->v.num_nodes : 1;
+    return (int64_t) g->q->p.Wn * rows * g->R;
+}
+
 int tsg_general_stat_free(tsg_general_t *g)
 {
     general_release(g);
@@ -2228,6 +2280,17 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     if (options & TSG_STAT_BOTH_MODES) {
         return TSG_ERR_MULTIPLE_STAT_MODES;
     }
+    // node mode replays as branch mode does (its items are the nodes' state
+    // changes) but reads no times
+    const bool node = options & TSG_STAT_NODE;
+    uint32_t qopt = options & ~(uint32_t) (TSG_PRECISION_F32_KAHAN | TSG_FORCE_GLOBAL_SWEEP);
+    if (node) {
+        if (options & (TSG_STAT_SITE | TSG_STAT_BRANCH)) {
+            return TSG_ERR_MULTIPLE_STAT_MODES;
+        }
+        qopt = (qopt & ~(uint32_t) TSG_STAT_NODE) | TSG_STAT_BRANCH
+            | TSG_STAT_ALLOW_TIME_UNCALIBRATED;
+    }
     const TSView &v = ts->v;
     const int64_t n = v.num_samples;
     std::vector<uint64_t> sizes((size_t) K, (uint64_t) n);
@@ -2251,8 +2314,9 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     g->R = (int32_t) R;
     g->K = (int32_t) K;
     g->weighted = true;
+    g->node = node;
     int ret = tsg_query_create(&g->q, ts, K, sizes.data(), sets.data(), Rb, outs.data(), Wn,
-        windows, options & ~(uint32_t) (TSG_PRECISION_F32_KAHAN | TSG_FORCE_GLOBAL_SWEEP));
+        windows, qopt);
     if (ret != 0) {
         delete g;
         return ret;
@@ -2284,7 +2348,7 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     const int64_t items = p.branch ? v.num_items : 0;
     g->sbase = 2 * items;
     g->lbase = g->sbase + (p.site ? nsk : 0);
-    const int64_t U = g->lbase + (p.branch ? v.num_leaves : 0);
+    const int64_t U = node ? v.num_items + v.num_nodes : g->lbase + (p.branch ? v.num_leaves : 0);
     g->U = U;
     std::vector<double> total((size_t) K, 0.0);
     for (int64_t j = 0; j < n; j++) {
@@ -2309,6 +2373,12 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     const int64_t oI = take(items * 16), oS = take(U * (int64_t) K * 8);
     const int64_t oM = take(v.num_mutations * (int64_t) K * 8);
     const int64_t oA = take((int64_t) Wn * (int64_t) Rb * TSG_FX_LIMBS * 8 * 6), oE = take(8);
+    // node mode: the replay's item states, the initial states, sort buffers
+    const int64_t NI = node ? items : 0, NN = node ? v.num_nodes : 0;
+    const size_t sort_bytes = node ? node_sort_bytes(NI) : 0;
+    const int64_t oXS = take(2 * NI * (int64_t) K * 8), oIN = take(NN * (int64_t) K * 8);
+    const int64_t oK0 = take(NI * 8), oK1 = take(NI * 8), oJ0 = take(NI * 4), oJ1 = take(NI * 4);
+    const int64_t oST = take((int64_t) sort_bytes);
     if (cudaMalloc(&g->wbuf, (size_t) off) != cudaSuccess) {
         cudaGetLastError();
         general_release(g);
@@ -2330,12 +2400,21 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
         || cudaMemsetAsync(derr, 0, 8, st) != cudaSuccess) {
         ret = TSG_ERR_CUDA;
     }
-    if (ret == 0) {
-        ret = genw_replay(v, p, dW, (int) K, (double *) (b + oX), (int32_t *) (b + oP),
-            (uint8_t *) (b + oF), (int) grid, g->ids, g->states, (double *) (b + oM), derr,
-            derr + 1, st);
+    double *dXS = (double *) (b + oXS), *dIN = (double *) (b + oIN);
+    if (ret == 0 && node) {
+        ret = node_init(v, (int) K, dW, dIN, st);
     }
     if (ret == 0) {
+        ret = genw_replay(v, p, dW, (int) K, (double *) (b + oX), (int32_t *) (b + oP),
+            (uint8_t *) (b + oF), (int) grid, g->ids, node ? dXS : g->states,
+            (double *) (b + oM), node ? dIN : nullptr, derr, derr + 1, st);
+    }
+    if (ret == 0 && node) {
+        g->node_keys = (uint64_t *) (b + oK1);
+        g->node_idx = (int32_t *) (b + oJ1);
+        ret = node_order(v, (int) K, g->ids, dXS, dIN, (uint64_t *) (b + oK0), g->node_keys,
+            (int32_t *) (b + oJ0), g->node_idx, b + oST, sort_bytes, g->states, derr, st);
+    } else if (ret == 0) {
         ret = genw_states(v, (int) K, dW, dT, (double *) (b + oM), g->site_off,
             p.site ? g->states + g->sbase * (int64_t) K : nullptr,
             p.branch ? g->states + g->lbase * (int64_t) K : nullptr, st);
@@ -2504,6 +2583,60 @@ static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *resu
     return ret;
 }
 
+// Sample-set statistics in node mode (tsk_treeseq_sample_count_stat with
+// TSK_STAT_NODE, c/tskit/trees.c:2174-2220 and 1788-1918): the sets as 0/1
+// weights through the weighted replay, the built-in summaries evaluated on
+// the device at every listed state.  Result [Wn x N x R].
+static int node_sets(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
+    const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
+    const double *windows, uint32_t options, double *result)
+{
+    if (options & (TSG_STAT_SITE | TSG_STAT_BRANCH | TSG_STAT_BOTH_MODES)) {
+        return TSG_ERR_MULTIPLE_STAT_MODES;
+    }
+    // the sets, terms and windows are checked as for branch mode
+    tsg_query_t *q = nullptr;
+    int ret = query_build(&q, ts, K, sizes, sets, R, outs, Wn, windows,
+        (options & ~(uint32_t) TSG_STAT_NODE) | TSG_STAT_BRANCH
+            | TSG_STAT_ALLOW_TIME_UNCALIBRATED);
+    if (ret != 0) {
+        return ret;
+    }
+    const QueryParams p = q->p;
+    tsg_query_free(q);
+    if (K > 8) {
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    const int64_t n = ts->v.num_samples;
+    std::vector<double> W((size_t) (n * (int64_t) K), 0.0);
+    uint64_t at = 0;
+    for (uint64_t k = 0; k < K; k++) {
+        for (uint64_t j = 0; j < sizes[k]; j++, at++) {
+            W[(size_t) ((int64_t) ts->h_sample_index[(size_t) sets[at]] * (int64_t) K
+                + (int64_t) k)] = 1.0;
+        }
+    }
+    tsg_general_t *g = nullptr;
+    int64_t U = 0;
+    ret = tsg_general_weighted_prepare(&g, ts, K, W.data(), R, Wn, windows, options, &U);
+    if (ret != 0) {
+        return ret;
+    }
+    double *vals = nullptr;
+    if (cudaMalloc(&vals, (size_t) std::max<int64_t>(U * (int64_t) R * 8, 8)) != cudaSuccess) {
+        cudaGetLastError();
+        ret = TSG_ERR_NO_MEMORY;
+    } else {
+        ret = node_term_values(p, g->states, U, (int) K, !p.polarised, vals, g->st);
+        if (ret == 0) {
+            ret = general_finish(g, vals, result);
+        }
+    }
+    cudaFree(vals);
+    tsg_general_stat_free(g);
+    return ret;
+}
+
 // The synchronous entry points reuse the tree sequence's own workspace and
 // staging buffer (grown on demand, serialised by a mutex), so a call makes no
 // device allocation once they are large enough.
@@ -2511,6 +2644,9 @@ static int run_sync(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
     const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
     const double *windows, uint32_t options, double *result)
 {
+    if (options & TSG_STAT_NODE) {
+        return node_sets(ts, K, sizes, sets, R, outs, Wn, windows, options, result);
+    }
     tsg_query_t *q = nullptr;
     int ret = query_build(&q, ts, K, sizes, sets, R, outs, Wn, windows, options);
     if (ret != 0) {

@@ -345,7 +345,8 @@ class TreeSequence:
     def _ll_terms(self, terms, sample_set_sizes, sample_sets, windows, mode, span_normalise,
                   polarised, extra=0):
         """Low-level fused call: returns (num_windows, num_terms) float64 (or
-        (2, num_windows, num_terms) with both modes)."""
+        (2, num_windows, num_terms) with both modes, or (num_windows,
+        num_nodes, num_terms) in node mode)."""
         flags = _parse_mode(mode) if not (extra & nat.STAT_BOTH_MODES) else 0
         if span_normalise:
             flags |= nat.STAT_SPAN_NORMALISE
@@ -367,7 +368,11 @@ class TreeSequence:
             for q in range(4):
                 outs[r].idx[q] = int(idx[q])
         nmodes = 2 if extra & nat.STAT_BOTH_MODES else 1
-        res = np.zeros((nmodes, Wn, len(terms)))
+        if flags & nat.STAT_NODE:
+            # node mode: one row of outputs per node (trees.c:1788-1918)
+            res = np.zeros((nmodes, Wn, self.num_nodes, len(terms)))
+        else:
+            res = np.zeros((nmodes, Wn, len(terms)))
         nat.check(self._lib.tsg_treeseq_sample_count_stat(
             self._handle, len(sizes), _ptr(sizes), _ptr(flat), len(terms),
             ctypes.cast(outs, ctypes.c_void_p), Wn, _ptr(win), flags, _ptr(res),
@@ -446,7 +451,10 @@ class TreeSequence:
         idx = np.ascontiguousarray(indexes, dtype=np.int32)
         if idx.ndim != 2 or idx.shape[0] < 1 or idx.shape[1] != 2:
             raise ValueError("indexes must be a k x 2 array.")
-        res = np.zeros((len(win) - 1, idx.shape[0]))
+        if flags & nat.STAT_NODE:
+            res = np.zeros((len(win) - 1, self.num_nodes, idx.shape[0]))
+        else:
+            res = np.zeros((len(win) - 1, idx.shape[0]))
         nat.check(self._lib.tsg_treeseq_genetic_relatedness_weighted(
             self._handle, w.shape[1], _ptr(w), idx.shape[0], _ptr(idx), len(win) - 1,
             _ptr(win), _ptr(res), flags))
@@ -601,6 +609,8 @@ class TreeSequence:
                     v = v + np.asarray(f(total - x), dtype=np.float64).reshape(-1)
                 F[i] = v
             res = np.zeros((len(win) - 1, R))
+            if res.size != self._lib.tsg_general_stat_result_size(g):
+                raise RuntimeError("result buffer does not match the statistic's output size")
             nat.check(self._lib.tsg_general_stat_finish(g, _ptr(F), _ptr(res)))
         finally:
             self._lib.tsg_general_stat_free(g)
@@ -633,7 +643,8 @@ class TreeSequence:
             states = np.zeros((U.value, K), dtype=np.float64)
             nat.check(self._lib.tsg_general_weighted_states(g, _ptr(states)))
             total = np.sum(W, axis=0)
-            branch = bool(flags & nat.STAT_BRANCH)
+            node = bool(flags & nat.STAT_NODE)
+            branch = bool(flags & nat.STAT_BRANCH) or node
             F = np.zeros((U.value, R))
             for i in range(U.value):
                 v = np.asarray(f(states[i]), dtype=np.float64).reshape(-1)
@@ -642,7 +653,13 @@ class TreeSequence:
                 if branch and not polarised:
                     v = v + np.asarray(f(total - states[i]), dtype=np.float64).reshape(-1)
                 F[i] = v
-            res = np.zeros((len(win) - 1, R))
+            if node:
+                # node mode: one row of outputs per node (trees.c:1788-1918)
+                res = np.zeros((len(win) - 1, self.num_nodes, R))
+            else:
+                res = np.zeros((len(win) - 1, R))
+            if res.size != self._lib.tsg_general_stat_result_size(g):
+                raise RuntimeError("result buffer does not match the statistic's output size")
             nat.check(self._lib.tsg_general_stat_finish(g, _ptr(F), _ptr(res)))
         finally:
             self._lib.tsg_general_stat_free(g)
@@ -662,8 +679,9 @@ class TreeSequence:
                      span_normalise=True, strict=True):
         """python/tskit/trees.py:7917-8004.  Weights of 0 and 1 (each column a
         set of samples) take the counting sweep, which evaluates f once per
-        distinct count vector; other real-valued weights (up to 8 columns)
-        take the weighted sweep, which evaluates f once per state it meets."""
+        distinct count vector; other real-valued weights (up to 8 columns),
+        and node mode, take the weighted sweep, which evaluates f once per
+        state it meets."""
         if mode is None:
             mode = "site"
         W = np.asarray(W, dtype=np.float64)
@@ -671,7 +689,7 @@ class TreeSequence:
             raise ValueError("First dimension of W must be number of samples")
         if strict:
             self._check_summary(np.sum(W, axis=0), f, output_dim)
-        if not np.all((W == 0) | (W == 1)):
+        if mode == "node" or not np.all((W == 0) | (W == 1)):
             return self.__run_windowed_stat(windows, self._ll_general_weighted, W, f, output_dim,
                                             polarised=polarised, span_normalise=span_normalise,
                                             mode=mode)
@@ -704,6 +722,15 @@ class TreeSequence:
         if strict:
             self._check_summary(sizes.astype(np.float64), f, output_dim)
         flat = safe_np_int_cast(np.hstack(sample_sets), np.int32)
+        if mode == "node":
+            index = np.full(self.num_nodes, -1, dtype=np.int64)
+            index[self.samples()] = np.arange(self.num_samples)
+            W = np.zeros((self.num_samples, len(sample_sets)))
+            for k, A in enumerate(sample_sets):
+                W[index[np.asarray(A, dtype=np.int64)], k] = 1.0
+            return self.__run_windowed_stat(windows, self._ll_general_weighted, W, f, output_dim,
+                                            polarised=polarised, span_normalise=span_normalise,
+                                            mode=mode)
         return self.__run_windowed_stat(windows, self._ll_general_stat, sizes, flat, f,
                                         output_dim, polarised=polarised,
                                         span_normalise=span_normalise, mode=mode)
@@ -946,7 +973,7 @@ class TreeSequence:
             terms += [(nat.SEGREGATING_SITES, (k,)) for k in range(K)]
             both = self._ll_terms(terms, sample_set_sizes, flattened, windows, mode,
                                   span_normalise, polarised)
-            T, S = both[:, :K], both[:, K:]
+            T, S = both[..., :K], both[..., K:]
             h = np.array([np.sum(1 / np.arange(1, nn)) for nn in n])
             g = np.array([np.sum(1 / np.arange(1, nn) ** 2) for nn in n])
             with np.errstate(invalid="ignore", divide="ignore"):
@@ -970,12 +997,12 @@ class TreeSequence:
             terms += [(nat.DIVERSITY, (k,)) for k in range(K)]
             both = self._ll_terms(terms, sample_set_sizes, flattened, windows, mode,
                                   span_normalise, polarised)
-            dvg, dvs = both[:, : len(idx)], both[:, len(idx):]
+            dvg, dvs = both[..., : len(idx)], both[..., len(idx):]
             fst = np.ones_like(dvg)
             for i, (u, v) in enumerate(idx):
-                denom = dvs[:, u] + dvs[:, v] + 2 * dvg[:, i]
+                denom = dvs[..., u] + dvs[..., v] + 2 * dvg[..., i]
                 with np.errstate(divide="ignore", invalid="ignore"):
-                    fst[:, i] -= 2 * (dvs[:, u] + dvs[:, v]) / denom
+                    fst[..., i] -= 2 * (dvs[..., u] + dvs[..., v]) / denom
             return fst
 
         return self.__k_way_sample_set_stat(fst_func, 2, sample_sets, indexes=indexes,
