@@ -67,6 +67,7 @@ extern "C" {
 #define TSG_ERR_BOTH_COLUMNS_REQUIRED (-104)
 #define TSG_ERR_BAD_COLUMN_TYPE (-105)
 #define TSG_ERR_BAD_OFFSET (-200)
+#define TSG_ERR_TIME_NONFINITE (-210)
 #define TSG_ERR_NODE_OUT_OF_BOUNDS (-202)
 #define TSG_ERR_BAD_NODE_TIME_ORDERING (-306)
 #define TSG_ERR_DUPLICATE_SAMPLE (-600)

@@ -43,6 +43,7 @@ ERR_BAD_COLUMN_TYPE = -105
 ERR_BAD_OFFSET = -200
 ERR_BAD_PARAM_VALUE = -4
 ERR_NODE_OUT_OF_BOUNDS = -202
+ERR_TIME_NONFINITE = -210
 ERR_DUPLICATE_SAMPLE = -600
 ERR_BAD_SAMPLES = -601
 ERR_BAD_NUM_WINDOWS = -900

@@ -408,6 +408,8 @@ const char *tsg_strerror(int err)
                    "(TSK_ERR_BAD_COLUMN_TYPE)";
         case TSG_ERR_BAD_OFFSET:
             return "Bad offset provided in input array. (TSK_ERR_BAD_OFFSET)";
+        case TSG_ERR_TIME_NONFINITE:
+            return "Times must be finite. (TSK_ERR_TIME_NONFINITE)";
         case TSG_ERR_BAD_PARAM_VALUE:
             return "Bad parameter value provided";
         case TSG_ERR_NODE_OUT_OF_BOUNDS:

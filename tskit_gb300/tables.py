@@ -59,6 +59,10 @@ class Tables:
     edge_insertion_order: np.ndarray | None = None
     edge_removal_order: np.ndarray | None = None
     time_uncalibrated: bool = False
+    # the node table's individual column and the number of individuals
+    # (read from .trees files; pca over individuals groups nodes by it)
+    node_individual: np.ndarray | None = None
+    num_individuals: int = 0
 
     # ------------------------------------------------------------ building
     @classmethod
@@ -190,6 +194,8 @@ class Tables:
                 return arrays
 
             node_time, node_flags = cols(["nodes/time", "nodes/flags"], [[np.float64], [np.uint32]])
+            node_individual = get("nodes/individual", [np.int32], required=False)
+            individual_flags = get("individuals/flags", [np.uint32], required=False)
             left, right, parent, child = cols(
                 ["edges/left", "edges/right", "edges/parent", "edges/child"],
                 [[np.float64], [np.float64], [np.int32], [np.int32]])
@@ -206,6 +212,9 @@ class Tables:
                              mutation_derived_state=(der, der_off))
         if time_units is not None and time_units.tobytes() == b"uncalibrated":
             t.time_uncalibrated = True
+        if node_individual is not None and len(node_individual) == len(node_time):
+            t.node_individual = node_individual
+            t.num_individuals = 0 if individual_flags is None else len(individual_flags)
         return t
 
     @property
@@ -242,6 +251,36 @@ class Tables:
         self.edge_removal_order = np.lexsort(
             (-self.edge_child, -self.edge_parent, -tp, self.edge_right)
         ).astype(np.int32)
+
+    def decapitated_topology(self, time):
+        """The nodes and edges of ``decapitate(time)`` (python/tskit/trees.py:
+        7396-7437: split_edges, then delete_older): edges whose child is at
+        least as old as ``time`` are removed, and every edge spanning
+        ``time`` gets its own new parent node at ``time`` (not a sample).
+        Sites and mutations are left out: this is the input of branch
+        statistics restricted to the material younger than ``time``."""
+        tp = self.node_time[self.edge_parent]
+        tc = self.node_time[self.edge_child]
+        keep = tp <= time
+        split = (tc < time) & (tp > time)
+        N = self.num_nodes
+        ns = int(np.count_nonzero(split))
+        parent = self.edge_parent.copy()
+        parent[split] = N + np.arange(ns, dtype=np.int32)
+        sel = keep | split
+        node_individual = None
+        if self.node_individual is not None:
+            node_individual = np.concatenate(
+                [self.node_individual, np.full(ns, NULL, dtype=np.int32)])
+        t = Tables.from_columns(
+            self.sequence_length,
+            np.concatenate([self.node_time, np.full(ns, float(time))]),
+            np.concatenate([self.node_flags, np.zeros(ns, dtype=np.uint32)]),
+            self.edge_left[sel], self.edge_right[sel], parent[sel], self.edge_child[sel])
+        t.time_uncalibrated = self.time_uncalibrated
+        t.node_individual = node_individual
+        t.num_individuals = self.num_individuals
+        return t
 
     # ------------------------------------------------------------ checks
     def check(self):
@@ -344,6 +383,8 @@ class Tables:
                     v = float(v)
                 elif f.name == "time_uncalibrated":
                     v = bool(v)
+                elif f.name == "num_individuals":
+                    v = int(v)
                 kw[f.name] = v
         t = cls(**kw)
         if t.edge_insertion_order is None:
