@@ -89,6 +89,7 @@ def _load():
             ctypes.c_int32, P, ctypes.c_uint32, P,
         ]
         lib.orc_genotype_matrix.argtypes = [ctypes.POINTER(_TS), P]
+        lib.orc_divergence_matrix_branch.argtypes = [ctypes.POINTER(_TS), ctypes.c_int32, P, P]
         _lib = lib
     return _lib
 
@@ -279,6 +280,22 @@ def divergence_matrix_site(ts, windows=None, span_normalise=True):
     return out
 
 
+def divergence_matrix_branch(ts, windows=None, span_normalise=True):
+    """Branch-mode divergence matrix with every sample its own set
+    (trees.c:8578-8672)."""
+    lib = _load()
+    win = _windows(ts, windows)
+    n = ts.num_samples
+    out = np.zeros((len(win) - 1, n, n))
+    err = lib.orc_divergence_matrix_branch(ctypes.byref(ts.struct), len(win) - 1, _ptr(win),
+                                           _ptr(out))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    if span_normalise:
+        out /= np.diff(win)[:, None, None]
+    return out
+
+
 def relatedness_from_divergence(D):
     """genetic_relatedness_matrix's normalisation (python/tskit/trees.py:9086-9095)
     for singleton sample sets."""
@@ -395,8 +412,13 @@ def call(ots, method, kwargs):
                                           span_normalise=span_normalise,
                                           centre=kw.pop("centre", True),
                                           nodes=kw.pop("nodes", None))
-    if method == "genetic_relatedness_matrix":
-        D = divergence_matrix_site(ots, windows=windows, span_normalise=span_normalise)
+    if method in ("divergence_matrix", "genetic_relatedness_matrix"):
+        if mode == "branch":
+            D = divergence_matrix_branch(ots, windows=windows, span_normalise=span_normalise)
+        else:
+            D = divergence_matrix_site(ots, windows=windows, span_normalise=span_normalise)
+        if method == "divergence_matrix":
+            return D
         return np.stack([relatedness_from_divergence(d) for d in D])
     if method == "genotype_matrix":
         return genotype_matrix(ots)

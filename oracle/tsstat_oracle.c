@@ -21,7 +21,7 @@
  *                      4899 (Y2), 4938 (f2), 5177 (Y3), 5219 (f3), 5266 (f4)
  *   AFS                c/tskit/trees.c:3469-3928
  *   relatedness matvec c/tskit/trees.c:10402-10816
- *   divergence matrix  c/tskit/trees.c:8684-8899 (site mode)
+ *   divergence matrix  c/tskit/trees.c:8684-8899 (site mode), 8578-8672 (branch)
  *
  * Integer allele codes per mutation replace the reference's derived-state
  * string comparisons; they are computed on the host with the same numbering
@@ -382,6 +382,100 @@ out:
     free(s);
     free(last);
     return ret;
+}
+
+/* ------------------------------------------- branch divergence matrix */
+/*
+ * Branch divergence matrix with every sample its own set
+ * (tsk_treeseq_divergence_matrix_branch, trees.c:8578-8672): for every tree
+ * and pair of samples, the span-weighted path length between them,
+ * (t_mrca - t_u) + (t_mrca - t_v), with each sample's root in place of the
+ * MRCA for samples in different subtrees.  result: Wn x n x n, symmetric
+ * with a zero diagonal, not span-normalised.
+ */
+int orc_divergence_matrix_branch(const orc_ts_t *ts, int32_t Wn, const double *windows,
+    double *result)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, n = ts->num_samples;
+    int32_t *parent = malloc((size_t) (N > 0 ? N : 1) * sizeof(int32_t));
+    int64_t *stamp = calloc((size_t) (N > 0 ? N : 1), sizeof(int64_t));
+    int64_t mark = 0;
+    if (!parent || !stamp) {
+        free(parent);
+        free(stamp);
+        return ORC_ERR_NO_MEMORY;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    memset(result, 0, (size_t) Wn * n * n * sizeof(double));
+    int32_t tj = 0, tk = 0, w = 0;
+    double left = 0, L = ts->sequence_length;
+    while (tj < E || left < L) {
+        while (tk < E && ts->edge_right[ts->rem[tk]] == left) {
+            parent[ts->edge_child[ts->rem[tk++]]] = -1;
+        }
+        while (tj < E && ts->edge_left[ts->ins[tj]] == left) {
+            const int32_t e = ts->ins[tj++];
+            parent[ts->edge_child[e]] = ts->edge_parent[e];
+        }
+        double right = L;
+        if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+            right = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+            right = ts->edge_right[ts->rem[tk]];
+        }
+        for (int32_t wi = w; wi < Wn && windows[wi] < right; wi++) {
+            const double a = left > windows[wi] ? left : windows[wi];
+            const double b = right < windows[wi + 1] ? right : windows[wi + 1];
+            if (b <= a) {
+                continue;
+            }
+            double *D = result + (int64_t) wi * n * n;
+            for (int32_t j = 0; j < n; j++) {
+                const int32_t u = ts->samples[j];
+                mark++;
+                int32_t ru = u;
+                for (int32_t x = u; x != -1; x = parent[x]) {
+                    stamp[x] = mark;
+                    ru = x;
+                }
+                for (int32_t k = j + 1; k < n; k++) {
+                    const int32_t v = ts->samples[k];
+                    int32_t y = v, rv = v, top = -1;
+                    for (; y != -1; y = parent[y]) {
+                        if (stamp[y] == mark) {
+                            top = y;
+                            break;
+                        }
+                        rv = y;
+                    }
+                    const int32_t tu_node = top != -1 ? top : ru;
+                    const int32_t tv_node = top != -1 ? top : rv;
+                    const double d = ((ts->node_time[tu_node] - ts->node_time[u])
+                                         + (ts->node_time[tv_node] - ts->node_time[v]))
+                        * (b - a);
+                    D[(int64_t) j * n + k] += d;
+                }
+            }
+        }
+        while (w < Wn && windows[w + 1] <= right) {
+            w++;
+        }
+        left = right;
+    }
+    for (int32_t wi = 0; wi < Wn; wi++) {
+        double *D = result + (int64_t) wi * n * n;
+        for (int32_t j = 0; j < n; j++) {
+            for (int32_t k = j + 1; k < n; k++) {
+                D[(int64_t) k * n + j] = D[(int64_t) j * n + k];
+            }
+        }
+    }
+    free(parent);
+    free(stamp);
+    return 0;
 }
 
 /* ----------------------------------------------------------- site sweep */

@@ -233,6 +233,14 @@ def cases_for(ts, rng):
         cases.append(("f4", dict(sample_sets=sets4, mode="node", windows=wins[1])))
     if n >= 1:
         cases.append(("diversity", dict(sample_sets=[[samples[0]]], mode="node")))
+    # branch-mode divergence and relatedness matrices (trees.c:8578-8672)
+    if n >= 2:
+        for w in wins:
+            cases.append(("divergence_matrix", dict(mode="branch", windows=w)))
+        cases.append(("divergence_matrix", dict(mode="branch", span_normalise=False)))
+        cases.append(("divergence_matrix", dict(mode="site", windows=wins[1])))
+        cases.append(("genetic_relatedness_matrix", dict(mode="branch")))
+        cases.append(("genetic_relatedness_matrix", dict(mode="branch", windows=wins[1])))
     return cases
 
 

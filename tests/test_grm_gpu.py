@@ -154,3 +154,44 @@ def test_divergence_matrix_errors(small):
     with pytest.raises(tskit_gb300.LibraryError) as e:
         ts.divergence_matrix([tables.samples()[0], tables.samples()[0]])
     assert e.value.code == -600
+
+
+def _set_means(D, sets, index):
+    """Mean pairwise entries between sets (distinct samples within a set),
+    as fill_lower_triangle_count_normalise (trees.c:8876-8899)."""
+    K = len(sets)
+    out = np.zeros((D.shape[0], K, K))
+    for a in range(K):
+        for b in range(K):
+            ia, ib = index[sets[a]], index[sets[b]]
+            block = D[:, ia][:, :, ib]
+            if a == b:
+                denom = len(ia) * (len(ia) - 1)
+                out[:, a, b] = block.sum(axis=(1, 2)) / denom if denom else block.sum(axis=(1, 2))
+            else:
+                out[:, a, b] = block.sum(axis=(1, 2)) / (len(ia) * len(ib))
+    return out
+
+
+def test_branch_divergence_matrix_sets_partial_windows(small):
+    """Branch mode through the relatedness sweep: sample sets of several
+    samples and windows that leave parts of the sequence out, against the
+    oracle's per-tree path lengths (FP64 within 1e-12 of the scale)."""
+    ts, ots, tables = small
+    L = tables.sequence_length
+    s = tables.samples()
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(s)
+    sets = [np.sort(perm[:7]), np.sort(perm[7:8]), np.sort(perm[8:40]), np.sort(perm[40:41])]
+    windows = [L / 5, L / 3, 0.7 * L]
+    got = ts.divergence_matrix(sets, windows=windows, mode="branch")
+    D = O.divergence_matrix_branch(ots, windows=windows)
+    index = np.full(tables.num_nodes, -1)
+    index[s] = np.arange(len(s))
+    exp = _set_means(D, sets, index)
+    np.testing.assert_allclose(got, exp, rtol=1e-12, atol=1e-12 * np.max(np.abs(exp)))
+    # every sample alone, the whole sequence, not normalised by span
+    got = ts.divergence_matrix(mode="branch", span_normalise=False)
+    exp = O.divergence_matrix_branch(ots, span_normalise=False)[0]
+    np.testing.assert_allclose(got, exp, rtol=1e-12, atol=1e-12 * np.max(np.abs(exp)))
+    assert np.all(np.diag(got) == 0)

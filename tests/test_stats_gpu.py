@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 GPU_METHODS = {
     "diversity", "segregating_sites", "Y1", "divergence", "Y2", "f2", "Y3", "f3", "f4",
     "genetic_relatedness", "Fst", "Tajimas_D", "allele_frequency_spectrum",
-    "genetic_relatedness_vector", "genetic_relatedness_matrix",
+    "genetic_relatedness_vector", "genetic_relatedness_matrix", "divergence_matrix",
 }
 CASES = [(n, c) for n, c in all_cases() if c["method"] in GPU_METHODS]
 _ts = {}

@@ -1,5 +1,6 @@
 // Site-mode divergence matrix and genetic relatedness matrix through an
-// exact Gram matrix on the tensor cores.
+// exact Gram matrix on the tensor cores (branch mode: k_divmat_branch, pair
+// path lengths tree by tree).
 //
 // Replaces tsk_treeseq_divergence_matrix in site mode
 // (c/tskit/trees.c:8753-8899, 8900-9001: D[u][v] counts, over the sites of a
@@ -686,6 +687,288 @@ static int divmat_sets(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *size
     return 0;
 }
 
+// Branch mode (tsk_treeseq_divergence_matrix_branch, c/tskit/trees.c:
+// 8578-8672): for every tree and pair of samples, (t_w - t_u) + (t_w - t_v)
+// times the tree's overlap with the window, w the pair's MRCA, or each
+// sample's own root for samples in different subtrees.  One CTA per 32 x 32
+// tile of sample pairs replays the whole sequence (parent pointers, the
+// events of each transition applied in parallel, one child each); per tree,
+// each tile sample's depth and root come from one walk, and each thread
+// finds its pair's MRCA by lifting the deeper sample and walking both up.
+// Each pair's window sum is added tree by tree, in the reference's order
+// and arithmetic.  out: Wn x m x m (upper triangle, zero elsewhere).
+#define TSG_DIVB_TILE 32
+__global__ void __launch_bounds__(TSG_DIVB_TILE * TSG_DIVB_TILE) k_divmat_branch(TSView ts,
+    const int32_t *focal, int32_t m, const int32_t *tiles, int32_t Wn, const double *windows,
+    int32_t *gpar, int par_in_smem, double *out, int32_t *err)
+{
+    extern __shared__ int32_t smem_par[];
+    __shared__ int32_t s_node[2 * TSG_DIVB_TILE], s_depth[2 * TSG_DIVB_TILE],
+        s_root[2 * TSG_DIVB_TILE];
+    const int64_t N = ts.num_nodes;
+    int32_t *par = par_in_smem ? smem_par : gpar + (int64_t) blockIdx.x * N;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int32_t bi = tiles[2 * blockIdx.x], bj = tiles[2 * blockIdx.x + 1];
+    // tile samples: rows bi*32 + r, columns bj*32 + c
+    if (tid < 2 * TSG_DIVB_TILE) {
+        const int32_t k = tid < TSG_DIVB_TILE ? bi * TSG_DIVB_TILE + tid
+                                               : bj * TSG_DIVB_TILE + (tid - TSG_DIVB_TILE);
+        s_node[tid] = k < m ? focal[k] : -1;
+    }
+    for (int64_t u = tid; u < N; u += bd) {
+        par[u] = -1;
+    }
+    __syncthreads();
+    const int r = tid / TSG_DIVB_TILE, c = tid % TSG_DIVB_TILE;
+    const int32_t gi = bi * TSG_DIVB_TILE + r, gj = bj * TSG_DIVB_TILE + c;
+    const bool mine = gi < m && gj < m && gi < gj;
+    const int32_t u = s_node[r], v = s_node[TSG_DIVB_TILE + c];
+    const double tu0 = mine ? ts.node_time[u] : 0.0, tv0 = mine ? ts.node_time[v] : 0.0;
+    int32_t w = 0;
+    double acc = 0.0;
+    auto flush = [&]() {
+        if (mine) {
+            out[((int64_t) w * m + gi) * m + gj] = acc;
+        }
+        acc = 0.0;
+        w++;
+    };
+    for (int32_t t = 0; t < (int32_t) ts.num_trees && w < Wn; t++) {
+        for (int32_t i = ts.tree_out[t] + tid; i < ts.tree_out[t + 1]; i += bd) {
+            par[ts.rem_child[i]] = -1;
+        }
+        __syncthreads();
+        for (int32_t i = ts.tree_in[t] + tid; i < ts.tree_in[t + 1]; i += bd) {
+            par[ts.ins_child[i]] = ts.ins_parent[i];
+        }
+        __syncthreads();
+        const double left = ts.breakpoints[t], right = ts.breakpoints[t + 1];
+        if (right <= windows[w]) {
+            continue;  // before the current window
+        }
+        // depth and root of each tile sample
+        if (tid < 2 * TSG_DIVB_TILE) {
+            int32_t x = s_node[tid], depth = 0, root = x;
+            if (x >= 0) {
+                for (int32_t y = par[x]; y >= 0; y = par[y]) {
+                    root = y;
+                    if (++depth > N) {
+                        dev_error(err, DEV_PATH_TOO_LONG);
+                        break;
+                    }
+                }
+            }
+            s_depth[tid] = depth;
+            s_root[tid] = root;
+        }
+        __syncthreads();
+        double d = 0.0;
+        if (mine) {
+            int32_t a = u, b = v, da = s_depth[r], db = s_depth[TSG_DIVB_TILE + c];
+            int32_t top_u, top_v;
+            if (s_root[r] != s_root[TSG_DIVB_TILE + c]) {
+                top_u = s_root[r];
+                top_v = s_root[TSG_DIVB_TILE + c];
+            } else {
+                for (; da > db; da--) {
+                    a = par[a];
+                }
+                for (; db > da; db--) {
+                    b = par[b];
+                }
+                // at equal depths below one root the walks meet (at most
+                // depth steps; node times increase along parents)
+                for (int32_t steps = 0; a != b && a >= 0 && b >= 0; steps++) {
+                    if (steps > da) {
+                        dev_error(err, DEV_PATH_TOO_LONG);
+                        a = b = -1;
+                        break;
+                    }
+                    a = par[a];
+                    b = par[b];
+                }
+                top_u = top_v = a;
+            }
+            if (top_u >= 0 && top_v >= 0) {
+                d = (ts.node_time[top_u] - tu0) + (ts.node_time[top_v] - tv0);
+            }
+        }
+        // the tree's overlap with each window it meets
+        for (int32_t ww = w; ww < Wn && windows[ww] < right; ww++) {
+            const double a = left > windows[ww] ? left : windows[ww];
+            const double b = right < windows[ww + 1] ? right : windows[ww + 1];
+            if (b <= a) {
+                continue;
+            }
+            while (w < ww) {
+                flush();
+            }
+            acc += d * (b - a);
+        }
+        while (w < Wn && windows[w + 1] <= right) {
+            flush();
+        }
+        __syncthreads();
+    }
+    while (w < Wn) {
+        flush();
+    }
+}
+
+static int divmat_branch(const tsg_treeseq_t *ts, int64_t K, const std::vector<int32_t> &off,
+    const std::vector<int32_t> &samples, int64_t Wn, const double *windows, uint32_t options,
+    bool relatedness, const std::vector<double> &nsz, double *result)
+{
+    const int64_t n = ts->v.num_samples, m = (int64_t) samples.size(), N = ts->v.num_nodes;
+    std::vector<int32_t> node_of((size_t) std::max<int64_t>(n, 1));
+    for (int64_t u = 0; u < N; u++) {
+        const int32_t si = ts->h_sample_index[(size_t) u];
+        if (si >= 0) {
+            node_of[(size_t) si] = (int32_t) u;
+        }
+    }
+    std::vector<int32_t> focal((size_t) std::max<int64_t>(m, 1));
+    for (int64_t j = 0; j < m; j++) {
+        focal[(size_t) j] = node_of[(size_t) samples[(size_t) j]];
+    }
+    const int64_t nb = (m + TSG_DIVB_TILE - 1) / TSG_DIVB_TILE;
+    std::vector<int32_t> tiles;
+    for (int64_t a = 0; a < nb; a++) {
+        for (int64_t b = a; b < nb; b++) {
+            tiles.push_back((int32_t) a);
+            tiles.push_back((int32_t) b);
+        }
+    }
+    const int64_t ntiles = (int64_t) tiles.size() / 2;
+    const size_t smem_bytes = (size_t) std::max<int64_t>(N, 1) * 4;
+    const bool in_smem = smem_bytes <= 160 * 1024;
+    tsg_treeseq_t *mts = const_cast<tsg_treeseq_t *>(ts);
+    std::lock_guard<std::mutex> lock(mts->sync_mutex);
+    cudaStream_t st = ts->sync_stream;
+    std::vector<double> D((size_t) (Wn * m * m));
+    double *dD = nullptr, *dwin = nullptr, *dout = nullptr, *dy = nullptr, *dnsz = nullptr;
+    int32_t *dfocal = nullptr, *dtiles = nullptr, *dpar = nullptr, *derr = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dD);
+        cudaFree(dwin);
+        cudaFree(dout);
+        cudaFree(dy);
+        cudaFree(dnsz);
+        cudaFree(dfocal);
+        cudaFree(dtiles);
+        cudaFree(dpar);
+        cudaFree(derr);
+    };
+    auto alloc = [&](void **p, int64_t bytes) {
+        return cudaMalloc(p, (size_t) std::max<int64_t>(bytes, 256)) == cudaSuccess;
+    };
+    if (!alloc((void **) &dD, Wn * m * m * 8) || !alloc((void **) &dwin, (Wn + 1) * 8)
+        || !alloc((void **) &dfocal, m * 4) || !alloc((void **) &dtiles, ntiles * 8)
+        || !alloc((void **) &derr, 4)
+        || (!in_smem && !alloc((void **) &dpar, ntiles * N * 4))
+        || !alloc((void **) &dout, K * K * 8) || !alloc((void **) &dy, K * 8)
+        || !alloc((void **) &dnsz, K * 8)) {
+        cudaGetLastError();
+        cleanup();
+        return TSG_ERR_NO_MEMORY;
+    }
+    int ret = 0;
+    if (cudaMemsetAsync(dD, 0, (size_t) (Wn * m * m * 8), st) != cudaSuccess
+        || cudaMemsetAsync(derr, 0, 4, st) != cudaSuccess
+        || cudaMemcpyAsync(dwin, windows, (size_t) ((Wn + 1) * 8), cudaMemcpyHostToDevice, st)
+            != cudaSuccess
+        || (m > 0 && cudaMemcpyAsync(dfocal, focal.data(), (size_t) (m * 4),
+                         cudaMemcpyHostToDevice, st) != cudaSuccess)
+        || (ntiles > 0 && cudaMemcpyAsync(dtiles, tiles.data(), (size_t) (ntiles * 8),
+                              cudaMemcpyHostToDevice, st) != cudaSuccess)
+        || cudaMemcpyAsync(dnsz, nsz.data(), (size_t) (K * 8), cudaMemcpyHostToDevice, st)
+            != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    }
+    if (ret == 0 && ntiles > 0) {
+        if (in_smem && smem_bytes > 48 * 1024
+            && cudaFuncSetAttribute(k_divmat_branch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                   (int) smem_bytes) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        } else {
+            k_divmat_branch<<<(unsigned) ntiles, TSG_DIVB_TILE * TSG_DIVB_TILE,
+                in_smem ? smem_bytes : 0, st>>>(ts->v, dfocal, (int32_t) m, dtiles, (int32_t) Wn,
+                dwin, dpar, in_smem ? 1 : 0, dD, derr);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+            if (cudaGetLastError() != cudaSuccess) {
+                ret = TSG_ERR_CUDA;
+            }
+        }
+    }
+    int32_t herr = 0;
+    if (ret == 0
+        && (cudaMemcpyAsync(D.data(), dD, (size_t) (Wn * m * m * 8), cudaMemcpyDeviceToHost, st)
+                != cudaSuccess
+            || cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess
+            || cudaStreamSynchronize(st) != cudaSuccess)) {
+        ret = TSG_ERR_CUDA;
+    }
+    if (ret == 0 && herr != 0) {
+        ret = TSG_ERR_DEVICE_CHECK;
+    }
+    // sets: sums over their pairs, normalised as fill_lower_triangle_count_normalise
+    // (trees.c:8876-8899), then by the window's span
+    std::vector<double> out((size_t) (Wn * K * K), 0.0);
+    for (int64_t w = 0; ret == 0 && w < Wn; w++) {
+        const double *Dw = D.data() + w * m * m;
+        auto pair = [&](int64_t i, int64_t j) {
+            return i < j ? Dw[i * m + j] : Dw[j * m + i];
+        };
+        for (int64_t a = 0; a < K; a++) {
+            for (int64_t b = a; b < K; b++) {
+                double sum = 0.0;
+                for (int32_t i = off[(size_t) a]; i < off[(size_t) a + 1]; i++) {
+                    for (int32_t j = off[(size_t) b]; j < off[(size_t) b + 1]; j++) {
+                        if (i != j) {
+                            sum += pair(i, j);
+                        }
+                    }
+                }
+                const double na = nsz[(size_t) a], nb2 = nsz[(size_t) b];
+                const double denom = a == b ? na * (na - 1) : na * nb2;
+                if (denom != 0) {
+                    sum /= denom;
+                }
+                if (options & TSG_STAT_SPAN_NORMALISE) {
+                    sum /= windows[w + 1] - windows[w];
+                }
+                out[(size_t) (w * K * K + a * K + b)] = sum;
+                out[(size_t) (w * K * K + b * K + a)] = sum;
+            }
+        }
+    }
+    for (int64_t w = 0; ret == 0 && w < Wn; w++) {
+        if (!relatedness || K == 0) {
+            std::copy(out.begin() + w * K * K, out.begin() + (w + 1) * K * K, result + w * K * K);
+            continue;
+        }
+        if (cudaMemcpyAsync(dout, out.data() + w * K * K, (size_t) (K * K * 8),
+                cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+            break;
+        }
+        k_grm_colmeans<<<(unsigned) K, 256, 0, st>>>(dout, (int32_t) K, dnsz, dy);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        k_grm_apply<<<(unsigned) K, 256, 0, st>>>(dout, (int32_t) K, dy);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (cudaGetLastError() != cudaSuccess
+            || cudaMemcpyAsync(result + w * K * K, dout, (size_t) (K * K * 8),
+                   cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+            ret = TSG_ERR_CUDA;
+        }
+    }
+    if (ret == 0 && cudaStreamSynchronize(st) != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    }
+    cleanup();
+    return ret;
+}
+
 static int divmat_entry(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
     const int32_t *sets, uint64_t Wn, const double *windows, uint32_t options, bool relatedness,
     double *result)
@@ -703,8 +986,10 @@ static int divmat_entry(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *siz
     if (options & TSG_STAT_POLARISED) {
         return TSG_ERR_STAT_POLARISED_UNSUPPORTED;
     }
-    if (branch) {
-        return TSG_ERR_UNSUPPORTED_STAT_MODE;  // branch mode: not on this path
+    // c/tskit/trees.c:8628-8631
+    if (branch && (ts->options & TSG_TIME_UNCALIBRATED)
+        && !(options & TSG_STAT_ALLOW_TIME_UNCALIBRATED)) {
+        return TSG_ERR_TIME_UNCALIBRATED;
     }
     const double L = ts->v.sequence_length;
     double default_windows[2] = { 0, L };
@@ -731,6 +1016,10 @@ static int divmat_entry(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *siz
     int ret = divmat_sets(ts, K, sizes, sets, off, samples, singletons, nsz, nsets);
     if (ret != 0) {
         return ret;
+    }
+    if (branch) {
+        return divmat_branch(ts, nsets, off, samples, (int64_t) Wn, windows, options,
+            relatedness, nsz, result);
     }
     tsg_treeseq_t *mts = const_cast<tsg_treeseq_t *>(ts);
     std::lock_guard<std::mutex> lock(mts->sync_mutex);

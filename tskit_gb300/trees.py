@@ -798,17 +798,19 @@ class TreeSequence:
 
     def divergence_matrix(self, sample_sets=None, *, windows=None, num_threads=0, mode=None,
                           span_normalise=True):
-        """python/tskit/trees.py:8739-8829 (site mode): mean divergence between
-        the samples of each pair of sets, shape (windows, sets, sets), the
-        window dimension dropped when not given.  num_threads is accepted for
-        compatibility (the work runs on the GPU)."""
+        """python/tskit/trees.py:8739-8829: mean divergence between the
+        samples of each pair of sets, shape (windows, sets, sets), the window
+        dimension dropped when not given; site mode through the exact Gram on
+        the tensor cores, branch mode through the relatedness matrix-vector
+        sweep.  num_threads is accepted for compatibility (the work runs on
+        the GPU)."""
         return self._divmat(self._lib.tsg_treeseq_divergence_matrix, sample_sets, windows, mode,
                             span_normalise)
 
     def genetic_relatedness_matrix(self, sample_sets=None, *, windows=None, num_threads=0,
                                    mode=None, span_normalise=True):
-        """python/tskit/trees.py:8978-9102 (site mode): the divergence matrix
-        normalised to centred relatedness, on the GPU."""
+        """python/tskit/trees.py:8978-9102 (site or branch mode): the
+        divergence matrix normalised to centred relatedness, on the GPU."""
         return self._divmat(self._lib.tsg_treeseq_genetic_relatedness_matrix, sample_sets,
                             windows, mode, span_normalise)
 
