@@ -302,7 +302,7 @@ int64_t tsg_general_stat_result_size(const tsg_general_t *general);
 int tsg_general_stat_free(tsg_general_t *general);
 
 /* general_stat with real-valued weights (tsk_treeseq_general_stat,
- * c/tskit/trees.c:2035-2095, W f64 [n x K] in sample order, K <= 8): the
+ * c/tskit/trees.c:2035-2095, W f64 [n x K] in sample order, K <= 32): the
  * same prepare / states / finish steps, the states being the weights below
  * each node as FP64 vectors.  Every state an item, a site allele or a leaf
  * needs is listed (real states rarely repeat): the host evaluates the
@@ -316,7 +316,7 @@ int tsg_general_weighted_states(tsg_general_t *g, double *states);
 
 /* Replaces tsk_treeseq_genetic_relatedness_weighted (c/tskit/trees.c:
  * 4838-4897, same arguments; weights host [n x num_weights], num_weights
- * <= 7, index tuples pairs of weight columns, which are range-checked
+ * <= 31, index tuples pairs of weight columns, which are range-checked
  * (TSG_ERR_BAD_SAMPLE_SET_INDEX) where the reference reads them unchecked;
  * TSG_STAT_NONCENTRED as the reference's TSK_STAT_NONCENTRED): the weighted
  * replay with the pair summary evaluated on the device. */

@@ -77,9 +77,46 @@ def test_node_mode_errors(cuda_lib):
     with pytest.raises(LibraryError) as e:
         ts.allele_frequency_spectrum([s], mode="node")
     assert e.value.code == nat.ERR_UNSUPPORTED_STAT_MODE
-    # node mode takes at most 8 sample sets or weight columns here
-    with pytest.raises(LibraryError):
-        ts.diversity([[u] for u in s[:9]], mode="node")
+    # node mode takes at most 32 sample sets or weight columns here
+    ts_b, _ = _load("b")
+    with pytest.raises(LibraryError) as e:
+        ts_b.diversity([[u] for u in ts_b.samples()[:33]], mode="node")
+    assert e.value.code == nat.ERR_TOO_MANY_SAMPLE_SETS
+
+
+@pytest.mark.parametrize("mode", ["node", "branch", "site"])
+def test_many_sets_weighted_paths(mode, cuda_lib):
+    """More than 8 sets or weight columns: the weighted replay reads the
+    child's state per component.  Node mode against the oracle; real
+    weights in every mode against the same statistic from 0/1 weights
+    scaled (general_stat is linear in a summary that is linear)."""
+    import oracle as O
+
+    ts, _ = _load("b")
+    s = ts.samples()
+    sets = [s[4 * k:4 * k + 4] for k in range(10)]
+    if mode == "node":
+        got = ts.diversity(sets, windows=[0, ts.sequence_length / 2, ts.sequence_length],
+                           mode="node")
+        exp = O.call(O.OracleTS(ts.tables), "diversity",
+                     dict(sample_sets=sets, windows=[0, ts.sequence_length / 2,
+                                                     ts.sequence_length], mode="node"))
+        np.testing.assert_allclose(got, np.asarray(exp).reshape(got.shape), rtol=1e-12,
+                                   atol=1e-13)
+    rng = np.random.default_rng(3)
+    W = rng.normal(size=(ts.num_samples, 12))
+
+    def f(x):
+        return np.array([np.sum(x), x[11] - 2 * x[0]])
+
+    got = ts.general_stat(W, f, 2, mode=mode, polarised=True, strict=False)
+    # f linear: the statistic of W equals that of its column sums' combination
+    v = W.sum(axis=1, keepdims=True), (W[:, 11] - 2 * W[:, 0])[:, None]
+    exp = np.concatenate([ts.general_stat(v[0], lambda x: x, 1, mode=mode, polarised=True,
+                                          strict=False),
+                          ts.general_stat(v[1], lambda x: x, 1, mode=mode, polarised=True,
+                                          strict=False)], axis=-1)
+    np.testing.assert_allclose(got, exp, rtol=1e-10, atol=1e-10 * np.max(np.abs(exp)))
 
 
 def test_node_mode_deterministic(cuda_lib):

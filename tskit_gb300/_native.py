@@ -57,6 +57,7 @@ ERR_UNSUPPORTED_STAT_MODE = -909
 ERR_TIME_UNCALIBRATED = -910
 ERR_INSUFFICIENT_WEIGHTS = -913
 ERR_CUDA = -20001
+ERR_TOO_MANY_SAMPLE_SETS = -20003
 ERR_DEVICE_CHECK = -20002
 ERR_NOALLOC_TOO_LARGE = -20007
 NOALLOC_SCRATCH_BYTES = 32 << 20

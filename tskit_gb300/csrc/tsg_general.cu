@@ -418,7 +418,7 @@ int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K
 // seek adds children in edge order, one warp replays in reference order.
 
 // Replay: items (ids, and states x0 | x1 per item), states under every
-// mutation.  Lane k carries weight component k (K <= 8) in the seek; a
+// mutation.  Lane k carries weight component k (K <= 32) in the seek; a
 // root-path batch takes one node per lane, each adding all components.
 __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const double *W,
     int K, double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int4 *ids, double *xs,
@@ -592,12 +592,19 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
                 if (q.branch) {
                     touch(act, mine, act ? up : -1);
                 }
-                if (act) {
+                if (act && K <= 8) {
 #pragma unroll
                     for (int k = 0; k < 8; k++) {
                         if (k < K) {
                             x[(int64_t) mine * K + k] += sign > 0 ? xc[k] : -xc[k];
                         }
+                    }
+                } else if (act) {
+                    // more components than registers: the child's state
+                    // (not on the path, so unchanged here) read again
+                    for (int k = 0; k < K; k++) {
+                        const double xk = c >= 0 ? x[(int64_t) c * K + k] : leaf_w(-c - 1, k);
+                        x[(int64_t) mine * K + k] += sign > 0 ? xk : -xk;
                     }
                 }
                 __syncwarp();
@@ -1072,11 +1079,11 @@ __device__ double node_summary(const QueryParams &q, int r, const double *x)
 __global__ void k_node_term_values(QueryParams q, const double *states, int64_t U, int K,
     int unpol, double *vals)
 {
-    double c[TSG_KMAX];
+    double c[TSG_MAX_SAMPLE_SETS];
     for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < U;
          u += (int64_t) gridDim.x * blockDim.x) {
         const double *x = states + u * K;
-        for (int k = 0; k < K && k < TSG_KMAX; k++) {
+        for (int k = 0; k < K && k < TSG_MAX_SAMPLE_SETS; k++) {
             c[k] = q.set_size[k] - x[k];
         }
         for (int r = 0; r < q.R; r++) {

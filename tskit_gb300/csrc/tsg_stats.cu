@@ -2274,7 +2274,7 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     if (K < 1) {
         return TSG_ERR_BAD_STATE_DIMS;
     }
-    if (K > 8) {
+    if (K > TSG_MAX_SAMPLE_SETS) {
         return TSG_ERR_TOO_MANY_SAMPLE_SETS;
     }
     if (options & TSG_STAT_BOTH_MODES) {
@@ -2293,16 +2293,15 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     }
     const TSView &v = ts->v;
     const int64_t n = v.num_samples;
-    std::vector<uint64_t> sizes((size_t) K, (uint64_t) n);
-    std::vector<int32_t> samples((size_t) n), sets((size_t) (K * n));
+    // the query carries the windows, the mode and the workspace plan: one
+    // set of all samples (the weights are the replay's own)
+    std::vector<uint64_t> sizes(1, (uint64_t) n);
+    std::vector<int32_t> sets((size_t) n);
     for (int64_t u = 0; u < v.num_nodes; u++) {
         const int32_t si = ts->h_sample_index[(size_t) u];
         if (si >= 0) {
-            samples[(size_t) si] = (int32_t) u;
+            sets[(size_t) si] = (int32_t) u;
         }
-    }
-    for (uint64_t k = 0; k < K; k++) {
-        std::copy(samples.begin(), samples.end(), sets.begin() + (int64_t) (k * n));
     }
     const uint64_t Rb = std::min<uint64_t>(R, TSG_ITEM_RMAX);
     std::vector<tsg_output_t> outs((size_t) Rb);
@@ -2315,7 +2314,7 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     g->K = (int32_t) K;
     g->weighted = true;
     g->node = node;
-    int ret = tsg_query_create(&g->q, ts, K, sizes.data(), sets.data(), Rb, outs.data(), Wn,
+    int ret = tsg_query_create(&g->q, ts, 1, sizes.data(), sets.data(), Rb, outs.data(), Wn,
         windows, qopt);
     if (ret != 0) {
         delete g;
@@ -2604,9 +2603,6 @@ static int node_sets(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
     }
     const QueryParams p = q->p;
     tsg_query_free(q);
-    if (K > 8) {
-        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
-    }
     const int64_t n = ts->v.num_samples;
     std::vector<double> W((size_t) (n * (int64_t) K), 0.0);
     uint64_t at = 0;

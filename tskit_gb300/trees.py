@@ -693,7 +693,7 @@ class TreeSequence:
                      span_normalise=True, strict=True):
         """python/tskit/trees.py:7917-8004.  Weights of 0 and 1 (each column a
         set of samples) take the counting sweep, which evaluates f once per
-        distinct count vector; other real-valued weights (up to 8 columns),
+        distinct count vector; other real-valued weights (up to 32 columns),
         and node mode, take the weighted sweep, which evaluates f once per
         state it meets."""
         if mode is None:
