@@ -324,6 +324,22 @@ int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t
     const double *weights, uint64_t num_index_tuples, const int32_t *index_tuples,
     uint64_t num_windows, const double *windows, double *result, uint32_t options);
 
+/* Replace tsk_treeseq_trait_covariance / trait_correlation /
+ * trait_linear_model (c/tskit/trees.c:3976-4218, same arguments; weights
+ * host [n x num_weights], covariates [n x num_covariates] already
+ * standardised as the reference's Python layer does; at most 32 columns in
+ * all, counting the appended frequency or count column).  Result
+ * num_windows x num_weights (x num_nodes before num_weights in node mode). */
+int tsg_treeseq_trait_covariance(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows, uint32_t options,
+    double *result);
+int tsg_treeseq_trait_correlation(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows, uint32_t options,
+    double *result);
+int tsg_treeseq_trait_linear_model(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_covariates, const double *covariates,
+    uint64_t num_windows, const double *windows, uint32_t options, double *result);
+
 /* ----------------------------------------------- device-resident queries
  * A query is prepared once (validates and uploads sample sets, summary terms
  * and windows) and launched any number of times on a stream with a

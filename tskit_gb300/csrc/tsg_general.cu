@@ -901,6 +901,80 @@ __global__ void k_wsummary_relatedness(const double *states, int64_t U, int K1,
     }
 }
 
+// The trait statistics' summaries (c/tskit/trees.c:3961-3974 covariance,
+// 4026-4044 correlation, 4108-4152 linear model) at every listed state,
+// plus the complement (total - x) when unpolarised.  kind 0: covariance, K
+// columns; 1: correlation, K - 1 traits and the frequency last; 2: linear
+// model, R traits, K - R - 1 covariates, the sample count last, V the
+// traits' projections on the covariates (R x (K - R - 1)).
+__device__ double trait_summary(int kind, const double *x, int K, int R, int r, double n,
+    const double *V)
+{
+    switch (kind) {
+        case 0:
+            return (x[r] * x[r]) / (2 * (n - 1) * (n - 1));
+        case 1: {
+            const double p = x[K - 1];
+            if ((p > 0.0) && (p < 1.0)) {
+                return (x[r] * x[r]) / (2 * (p * (1 - p)) * n * (n - 1));
+            }
+            return 0.0;
+        }
+        default: {
+            const double m = x[K - 1];
+            const int nc = K - R - 1;
+            if (!((m > 0.0) && (m < n))) {
+                return 0.0;
+            }
+            double a = x[r], denom = m;
+            for (int j = 0; j < nc; j++) {
+                const double z = x[R + j];
+                a -= z * V[(int64_t) r * nc + j];
+                denom -= z * z;
+            }
+            // the reference's tolerance for a trait in the covariates' span
+            if (denom < 1e-8) {
+                return 0.0;
+            }
+            return (a * a) / (2 * denom * denom);
+        }
+    }
+}
+
+__global__ void k_wsummary_trait(const double *states, int64_t U, int K, int R, int kind,
+    double n, const double *V, const double *total, int complement, double *vals)
+{
+    double c[TSG_MAX_SAMPLE_SETS];
+    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < U;
+         u += (int64_t) gridDim.x * blockDim.x) {
+        const double *x = states + u * K;
+        if (complement) {
+            for (int k = 0; k < K && k < TSG_MAX_SAMPLE_SETS; k++) {
+                c[k] = total[k] - x[k];
+            }
+        }
+        for (int r = 0; r < R; r++) {
+            double v = trait_summary(kind, x, K, R, r, n, V);
+            if (complement) {
+                v += trait_summary(kind, c, K, R, r, n, V);
+            }
+            vals[u * R + r] = v;
+        }
+    }
+}
+
+int genw_summary_trait(const double *states, int64_t U, int K, int R, int kind, double n,
+    const double *V, const double *total, bool complement, double *vals, cudaStream_t st)
+{
+    if (U == 0) {
+        return 0;
+    }
+    k_wsummary_trait<<<gen_grid(U), 256, 0, st>>>(states, U, K, R, kind, n, V, total,
+        complement ? 1 : 0, vals);
+    TSG_LAUNCHED();
+    return 0;
+}
+
 int genw_summary_relatedness(const double *states, int64_t U, int K1, const double *total,
     const int32_t *tuples, int R, double ones, bool centred, bool complement, double *vals,
     cudaStream_t st)

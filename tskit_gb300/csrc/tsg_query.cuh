@@ -172,6 +172,8 @@ int node_walk(const TSView &v, int Wn, const double *windows, const uint64_t *ke
 int genw_states(const TSView &v, int K, const double *W, const double *total,
     const double *mstate, const int64_t *site_off, double *site_states, double *leaf_states,
     cudaStream_t st);
+int genw_summary_trait(const double *states, int64_t U, int K, int R, int kind, double n,
+    const double *V, const double *total, bool complement, double *vals, cudaStream_t st);
 int genw_summary_relatedness(const double *states, int64_t U, int K1, const double *total,
     const int32_t *tuples, int R, double ones, bool centred, bool complement, double *vals,
     cudaStream_t st);

@@ -2504,6 +2504,190 @@ int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t
     return ret;
 }
 
+}  // extern "C"
+
+namespace tsg {
+
+// general_stat with real weights w (n x K, sample order) and a summary
+// evaluated on the device: summary(g, U, total, complement, values) fills
+// the values of the U listed states (U x R), complement saying whether the
+// unpolarised branch / node wrapper applies (f(x) + f(total - x), with the
+// weights' own column sums, c/tskit/trees.c:1944-1972).
+template <typename Summary>
+static int weighted_device_stat(const tsg_treeseq_t *ts, uint64_t K, const std::vector<double> &w,
+    uint64_t R, uint64_t Wn, const double *windows, uint32_t options, Summary summary,
+    double *result)
+{
+    const int64_t n = ts->v.num_samples;
+    std::vector<double> total((size_t) K, 0.0);
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < K; k++) {
+            total[(size_t) k] += w[(size_t) (j * (int64_t) K + (int64_t) k)];
+        }
+    }
+    tsg_general_t *g = nullptr;
+    int64_t U = 0;
+    int ret = tsg_general_weighted_prepare(&g, ts, K, w.data(), R, Wn, windows, options, &U);
+    if (ret != 0) {
+        return ret;
+    }
+    double *dF = nullptr, *dT = nullptr;
+    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(U * (int64_t) R * 8, 8)) != cudaSuccess
+        || cudaMalloc(&dT, (size_t) (K * 8)) != cudaSuccess) {
+        cudaGetLastError();
+        ret = TSG_ERR_NO_MEMORY;
+    } else if (cudaMemcpyAsync(dT, total.data(), (size_t) (K * 8), cudaMemcpyHostToDevice, g->st)
+        != cudaSuccess) {
+        ret = TSG_ERR_CUDA;
+    } else {
+        ret = summary(g, U, dT, g->q->p.branch && !g->q->p.polarised, dF);
+        if (ret == 0) {
+            ret = general_finish(g, dF, result);
+        }
+    }
+    cudaFree(dF);
+    cudaFree(dT);
+    tsg_general_stat_free(g);
+    return ret;
+}
+
+// trait statistics: kind 0 covariance, 1 correlation, 2 linear model
+static int trait_stat(const tsg_treeseq_t *ts, int kind, uint64_t K, const std::vector<double> &w,
+    uint64_t R, const std::vector<double> &V, uint64_t Wn, const double *windows,
+    uint32_t options, double *result)
+{
+    if (K > TSG_MAX_SAMPLE_SETS) {
+        return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    const double n = (double) ts->v.num_samples;
+    double *dV = nullptr;
+    if (!V.empty()) {
+        if (cudaMalloc(&dV, V.size() * 8) != cudaSuccess) {
+            cudaGetLastError();
+            return TSG_ERR_NO_MEMORY;
+        }
+        if (cudaMemcpy(dV, V.data(), V.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(dV);
+            return TSG_ERR_CUDA;
+        }
+    }
+    const int ret = weighted_device_stat(ts, K, w, R, Wn, windows, options,
+        [&](tsg_general *g, int64_t U, const double *dT, bool complement, double *dF) {
+            return genw_summary_trait(g->states, U, (int) K, (int) R, kind, n, dV, dT, complement,
+                dF, g->st);
+        },
+        result);
+    cudaFree(dV);
+    return ret;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+// tsk_treeseq_trait_covariance (c/tskit/trees.c:3976-4022): the weights
+// centred, f = x^2 / (2 (n - 1)^2) per column.
+int tsg_treeseq_trait_covariance(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows, uint32_t options,
+    double *result)
+{
+    const int64_t n = self->v.num_samples;
+    if (num_weights == 0) {
+        return TSG_ERR_INSUFFICIENT_WEIGHTS;
+    }
+    const uint64_t K = num_weights;
+    std::vector<double> means((size_t) K, 0.0), w((size_t) (n * (int64_t) K));
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < K; k++) {
+            means[(size_t) k] += weights[j * (int64_t) K + (int64_t) k];
+        }
+    }
+    for (uint64_t k = 0; k < K; k++) {
+        means[(size_t) k] /= (double) n;
+    }
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < K; k++) {
+            w[(size_t) (j * (int64_t) K + (int64_t) k)] =
+                weights[j * (int64_t) K + (int64_t) k] - means[(size_t) k];
+        }
+    }
+    return trait_stat(self, 0, K, w, K, {}, num_windows, windows, options, result);
+}
+
+// tsk_treeseq_trait_correlation (c/tskit/trees.c:4047-4104): the weights
+// standardised (sample standard deviation) with a column of 1/n appended,
+// f = x^2 / (2 p (1 - p) n (n - 1)) for a frequency p strictly in (0, 1).
+int tsg_treeseq_trait_correlation(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_windows, const double *windows, uint32_t options,
+    double *result)
+{
+    const int64_t n = self->v.num_samples;
+    if (num_weights < 1) {
+        return TSG_ERR_INSUFFICIENT_WEIGHTS;
+    }
+    const uint64_t nw = num_weights, K = nw + 1;
+    std::vector<double> means((size_t) nw, 0.0), meansqs((size_t) nw, 0.0), sds((size_t) nw);
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < nw; k++) {
+            const double x = weights[j * (int64_t) nw + (int64_t) k];
+            means[(size_t) k] += x;
+            meansqs[(size_t) k] += x * x;
+        }
+    }
+    for (uint64_t k = 0; k < nw; k++) {
+        means[(size_t) k] /= (double) n;
+        meansqs[(size_t) k] -= means[(size_t) k] * means[(size_t) k] * (double) n;
+        meansqs[(size_t) k] /= (double) (n - 1);
+        sds[(size_t) k] = std::sqrt(meansqs[(size_t) k]);
+    }
+    std::vector<double> w((size_t) (n * (int64_t) K));
+    for (int64_t j = 0; j < n; j++) {
+        for (uint64_t k = 0; k < nw; k++) {
+            w[(size_t) (j * (int64_t) K + (int64_t) k)] =
+                (weights[j * (int64_t) nw + (int64_t) k] - means[(size_t) k]) / sds[(size_t) k];
+        }
+        w[(size_t) (j * (int64_t) K + (int64_t) nw)] = 1.0 / (double) n;
+    }
+    return trait_stat(self, 1, K, w, nw, {}, num_windows, windows, options, result);
+}
+
+// tsk_treeseq_trait_linear_model (c/tskit/trees.c:4154-4218): traits,
+// covariates (already standardised by the caller) and a column of ones;
+// V = W^T Z; f as trait_linear_model_summary_func.
+int tsg_treeseq_trait_linear_model(const tsg_treeseq_t *self, uint64_t num_weights,
+    const double *weights, uint64_t num_covariates, const double *covariates,
+    uint64_t num_windows, const double *windows, uint32_t options, double *result)
+{
+    const int64_t n = self->v.num_samples;
+    if (num_weights < 1) {
+        return TSG_ERR_INSUFFICIENT_WEIGHTS;
+    }
+    const uint64_t nw = num_weights, nc = num_covariates, K = nw + nc + 1;
+    std::vector<double> V((size_t) (nw * nc), 0.0), w((size_t) (n * (int64_t) K));
+    for (int64_t k = 0; k < n; k++) {
+        for (uint64_t i = 0; i < nw; i++) {
+            for (uint64_t j = 0; j < nc; j++) {
+                V[(size_t) (i * nc + j)] += weights[k * (int64_t) nw + (int64_t) i]
+                    * covariates[k * (int64_t) nc + (int64_t) j];
+            }
+        }
+    }
+    for (int64_t k = 0; k < n; k++) {
+        double *row = w.data() + k * (int64_t) K;
+        for (uint64_t i = 0; i < nw; i++) {
+            row[i] = weights[k * (int64_t) nw + (int64_t) i];
+        }
+        for (uint64_t i = 0; i < nc; i++) {
+            row[nw + i] = covariates[k * (int64_t) nc + (int64_t) i];
+        }
+        row[nw + nc] = 1.0;
+    }
+    if (V.empty()) {
+        V.push_back(0.0);
+    }
+    return trait_stat(self, 2, K, w, nw, V, num_windows, windows, options, result);
+}
+
 int tsg_general_weighted_states(tsg_general_t *g, double *states)
 {
     if (!g->weighted) {

@@ -837,6 +837,94 @@ class TreeSequence:
                                         mode=mode, span_normalise=span_normalise,
                                         centre=centre, nodes=nodes)
 
+    # --------------------------------------------------------------- traits
+    def _ll_trait(self, fn, weights, windows, covariates=None, mode=None, span_normalise=True):
+        """Low-level trait statistic (python/_tskitmodule.c weighted-stat
+        methods): result (num_windows, num_weights), or (num_windows,
+        num_nodes, num_weights) in node mode."""
+        flags = _parse_mode(mode)
+        if span_normalise:
+            flags |= nat.STAT_SPAN_NORMALISE
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.ndim != 2:
+            raise ValueError("Weights must be a 2D array")
+        if w.shape[0] != self.num_samples:
+            raise ValueError("First dimension must be num_samples")
+        win = np.ascontiguousarray(windows, dtype=np.float64)
+        if win.ndim != 1 or len(win) < 2:
+            raise ValueError("Windows arrays must have at least 2 elements")
+        if flags & nat.STAT_NODE:
+            res = np.zeros((len(win) - 1, self.num_nodes, w.shape[1]))
+        else:
+            res = np.zeros((len(win) - 1, w.shape[1]))
+        if covariates is None:
+            nat.check(fn(self._handle, w.shape[1], _ptr(w), len(win) - 1, _ptr(win), flags,
+                         _ptr(res)))
+        else:
+            z = np.ascontiguousarray(covariates, dtype=np.float64)
+            if z.ndim != 2 or z.shape[0] != self.num_samples:
+                raise ValueError("First dimension of Z must equal the number of samples.")
+            nat.check(fn(self._handle, w.shape[1], _ptr(w), z.shape[1], _ptr(z), len(win) - 1,
+                         _ptr(win), flags, _ptr(res)))
+        return res
+
+    def trait_covariance(self, W, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:9559-9619: mean squared covariance of each
+        column of W with inheritance (alleles, branches or nodes)."""
+        if W.shape[0] != self.num_samples:
+            raise ValueError("First trait dimension must be equal to number of samples.")
+        return self.__run_windowed_stat(
+            windows, lambda *a, **k: self._ll_trait(self._lib.tsg_treeseq_trait_covariance,
+                                                    *a, **k),
+            W, mode=mode, span_normalise=span_normalise)
+
+    def trait_correlation(self, W, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:9621-9688: the covariance divided by each
+        column's sample variance and p (1 - p), p the inheriting fraction."""
+        if W.shape[0] != self.num_samples:
+            raise ValueError("First trait dimension must be equal to number of samples.")
+        sds = np.std(W, axis=0)
+        if np.any(sds == 0):
+            raise ValueError(
+                "Weight columns must have positive variance", "to compute correlation.")
+        return self.__run_windowed_stat(
+            windows, lambda *a, **k: self._ll_trait(self._lib.tsg_treeseq_trait_correlation,
+                                                    *a, **k),
+            W, mode=mode, span_normalise=span_normalise)
+
+    def trait_regression(self, *args, **kwargs):
+        """Deprecated synonym for trait_linear_model (python/tskit/trees.py:
+        9690-9700)."""
+        import warnings
+
+        warnings.warn("This is deprecated: please use trait_linear_model( ) instead.",
+                      FutureWarning, stacklevel=4)
+        return self.trait_linear_model(*args, **kwargs)
+
+    def trait_linear_model(self, W, Z=None, windows=None, mode="site", span_normalise=True):
+        """python/tskit/trees.py:9702-9787: the squared coefficient of
+        inheritance in the least-squares fit of each trait on inheritance
+        and the covariates Z (with an intercept), the covariates
+        orthonormalised as the reference does."""
+        if W.shape[0] != self.num_samples:
+            raise ValueError("First trait dimension must be equal to number of samples.")
+        if Z is None:
+            Z = np.ones((self.num_samples, 1))
+        else:
+            tZ = np.column_stack([Z, np.ones((Z.shape[0], 1))])
+            if np.linalg.matrix_rank(tZ) == tZ.shape[1]:
+                Z = tZ
+        if Z.shape[0] != self.num_samples:
+            raise ValueError("First dimension of Z must equal the number of samples.")
+        if np.linalg.matrix_rank(Z) < Z.shape[1]:
+            raise ValueError("Matrix of covariates is computationally singular.")
+        K = np.linalg.cholesky(np.matmul(Z.T, Z)).T
+        Z = np.matmul(Z, np.linalg.inv(K))
+        return self.__run_windowed_stat(
+            windows, lambda W_, Z_, **k: self._ll_trait(
+                self._lib.tsg_treeseq_trait_linear_model, W_, covariates=Z_, **k),
+            W, Z, mode=mode, span_normalise=span_normalise)
+
     # ------------------------------------------------------------------ pca
     def _expand_indices(self, x, indices):
         """python/tskit/trees.py:9220-9224 (rows placed by node id)."""
