@@ -285,6 +285,46 @@ __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsD
     }
     const int32_t a0 = q.polarised ? 1 : 0;
     const int32_t na = A - a0;
+    if (q.site_int) {
+        // exact integer numerators summed over the alleles (each below
+        // 2^60 with set sizes below 2^15): the windows sum them exactly and
+        // scale once (k_site_windows), no FP64 work per site; the states of
+        // up to four alleles stay in registers
+        Pack ps[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            ps[j] = j < na && na <= 4 ? site_allele_state<W, KQ>(ts, q, w, m0, m1, a0 + j)
+                                      : Pack{0, 0};
+        }
+        int64_t *num_out = (int64_t *) w.site_val;
+#pragma unroll 1
+        for (int r = 0; r < R; r++) {
+            const Term &t = q.term[r];
+            auto numer = [&](const Pack &x) {
+                int64_t num;
+                term_num(t.type, (int64_t) pk_get<W>(x, t.idx[0]), (int64_t) pk_get<W>(x, t.idx[1]),
+                    (int64_t) pk_get<W>(x, t.idx[2]), (int64_t) pk_get<W>(x, t.idx[3]),
+                    (int64_t) q.set_size[t.idx[0]], (int64_t) q.set_size[t.idx[1]],
+                    (int64_t) q.set_size[t.idx[2]], (int64_t) q.set_size[t.idx[3]], num);
+                return num;
+            };
+            int64_t acc = 0;
+            if (na <= 4) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (j < na) {
+                        acc += numer(ps[j]);
+                    }
+                }
+            } else {
+                for (int32_t a = a0; a < A; a++) {
+                    acc += numer(site_allele_state<W, KQ>(ts, q, w, m0, m1, a));
+                }
+            }
+            num_out[(int64_t) r * ts.num_sites + site] = acc;
+        }
+        return;
+    }
     if (na <= 4) {
         Pack ps[4];
 #pragma unroll
@@ -314,15 +354,56 @@ __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsD
     }
 }
 
+// Exact sum of 128-bit integers across a warp (lane 0 holds it).
+__device__ __forceinline__ __int128 warp_sum_i128(__int128 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long lo = __shfl_down_sync(0xffffffffu, (unsigned long long) v, o);
+        const unsigned long long hi =
+            __shfl_down_sync(0xffffffffu, (unsigned long long) (v >> 64), o);
+        v += (__int128) (((unsigned __int128) hi << 64) | (unsigned __int128) lo);
+    }
+    return v;
+}
+
+// A 128-bit integer as the nearest double (one rounding while it fits 64
+// bits; two beyond).
+__device__ __forceinline__ double i128_to_double(__int128 v)
+{
+    const long long lo = (long long) v;
+    if ((__int128) lo == v) {
+        return (double) lo;
+    }
+    return (double) (long long) (v >> 64) * 18446744073709551616.0
+        + (double) (unsigned long long) v;
+}
+
 // Per window: the sum of its sites' summaries for every term, one block of
 // 32 warps per window, warp j taking terms j, j + 32, ...: lanes sum strided
-// sites (term-major, coalesced), then a fixed-order warp reduction.
+// sites (term-major, coalesced), then a fixed-order warp reduction; with
+// integer numerators the sums are exact (128-bit) and scaled once.
 __global__ void __launch_bounds__(1024) k_site_windows(QueryParams q, QueryDev qd, WsDev w,
-    int64_t S)
+    int64_t S, int integer)
 {
     const int64_t wdx = blockIdx.x;
     const int lane = threadIdx.x & 31;
     const int64_t b = qd.win_site_lo[wdx], e = qd.win_site_lo[wdx + 1];
+    if (integer) {
+        // integer numerators (k_site_eval): summed exactly, scaled once
+        for (int r = threadIdx.x >> 5; r < q.R; r += blockDim.x >> 5) {
+            const int64_t *num = (const int64_t *) w.site_val + (int64_t) r * S;
+            __int128 v = 0;
+            for (int64_t i = b + lane; i < e; i += 32) {
+                v += num[i];
+            }
+            v = warp_sum_i128(v);
+            if (lane == 0) {
+                w.site_win[wdx * q.R + r] = i128_to_double(v) * q.inv[r];
+            }
+        }
+        return;
+    }
     for (int r = threadIdx.x >> 5; r < q.R; r += blockDim.x >> 5) {
         const double *val = w.site_val + (int64_t) r * S;
         double v = 0;

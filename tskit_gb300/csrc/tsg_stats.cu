@@ -1858,7 +1858,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         if (p.site) {
             if (ts->v.num_sites > 0) {
                 k_site_windows<<<(unsigned) p.Wn, 1024, 0, st>>>(p, d, w,
-                    ts->v.num_sites);
+                    ts->v.num_sites, p.site_int);
                 TSG_LAUNCHED();
             } else {
                 TSG_CUDA(cudaMemsetAsync(w.site_win, 0, (size_t) p.Wn * R * 8, st));
@@ -2195,7 +2195,7 @@ static int general_finish(tsg_general *g, const double *dF, double *result)
         if (pb.site) {
             if (v.num_sites > 0) {
                 k_site_windows<<<(unsigned) pb.Wn, 1024, 0, st>>>(pb, g->d, g->w,
-                    v.num_sites);
+                    v.num_sites, 0);
                 g_launches.fetch_add(1, std::memory_order_relaxed);
             } else if (cudaMemsetAsync(g->w.site_win, 0, (size_t) (pb.Wn * pb.R * 8), st)
                 != cudaSuccess) {
