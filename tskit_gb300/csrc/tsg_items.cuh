@@ -232,7 +232,7 @@ __device__ __forceinline__ Pack site_allele_state(const TSView &ts, const QueryP
     int64_t st[KM];
 #pragma unroll
     for (int k = 0; k < KM; k++) {
-        st[k] = (a == 0 && k < q.K) ? (int64_t) q.set_size[k] : 0;
+        st[k] = (a == 0 && k < q.K) ? (int64_t) q.set_size_i[k] : 0;
     }
     for (int32_t m = m0; m < m1; m++) {
         Pack xm;
@@ -304,8 +304,8 @@ __global__ void __launch_bounds__(256) k_site_eval(TSView ts, QueryParams q, WsD
                 int64_t num;
                 term_num(t.type, (int64_t) pk_get<W>(x, t.idx[0]), (int64_t) pk_get<W>(x, t.idx[1]),
                     (int64_t) pk_get<W>(x, t.idx[2]), (int64_t) pk_get<W>(x, t.idx[3]),
-                    (int64_t) q.set_size[t.idx[0]], (int64_t) q.set_size[t.idx[1]],
-                    (int64_t) q.set_size[t.idx[2]], (int64_t) q.set_size[t.idx[3]], num);
+                    (int64_t) q.set_size_i[t.idx[0]], (int64_t) q.set_size_i[t.idx[1]],
+                    (int64_t) q.set_size_i[t.idx[2]], (int64_t) q.set_size_i[t.idx[3]], num);
                 return num;
             };
             int64_t acc = 0;

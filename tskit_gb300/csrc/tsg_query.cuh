@@ -17,6 +17,7 @@ struct QueryParams {
     int32_t num_slots;
     double inv_K;
     double set_size[TSG_MAX_SAMPLE_SETS];
+    int32_t set_size_i[TSG_MAX_SAMPLE_SETS];  // the same as integers (integer kernels)
     double inv_size[TSG_MAX_SAMPLE_SETS];  // 1 / n_k
     double inv[TSG_MAX_OUTPUTS];           // reciprocal denominator of each term
     // the same in FP32 (rounded once on the host) for the FP32 evaluation

@@ -867,6 +867,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     p.f32 = !!(options & TSG_PRECISION_F32_KAHAN);
     for (uint64_t k = 0; k < K; k++) {
         p.set_size[k] = (double) sizes[k];
+        p.set_size_i[k] = (int32_t) sizes[k];
         if (sizes[k] >= ((uint64_t) 1 << 23)) {
             p.f32 = 0;  // the FP32 form needs every count exact in FP32
         }
