@@ -198,6 +198,19 @@ def cpu_oracle_run(tables, sets, windows, pairs, triples):
     return dt, raw, len(calls)
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest of a per-rank figure over the job (the slowest rank's
+    time); the value itself on one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     """--impl reference: the CPU path with all host threads, rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
@@ -414,11 +427,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
     launches = (lib.tsg_launch_count() - launches0) / args.steps
     q.check(ws)
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(float(np.mean(step_ms)), world)
     value = world * logical / (ms / 1e3)
     raw_batched = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
 
@@ -470,7 +479,7 @@ def run_gpu(args):
         dt = time.perf_counter() - t0
         if j >= args.warmup:
             e2e_ms.append(dt * 1e3)
-    e2e_value = world * logical / (float(np.mean(e2e_ms)) / 1e3)
+    e2e_value = world * logical / (max_over_ranks(float(np.mean(e2e_ms)), world) / 1e3)
     h2d = int(sizes.nbytes + flat.nbytes + windows.nbytes + ts.num_samples * 4)
     d2h = int(host.nbytes)
 
