@@ -77,10 +77,11 @@ def test_node_mode_errors(cuda_lib):
     with pytest.raises(LibraryError) as e:
         ts.allele_frequency_spectrum([s], mode="node")
     assert e.value.code == nat.ERR_UNSUPPORTED_STAT_MODE
-    # node mode takes at most 32 sample sets or weight columns here
+    # real weights take at most 32 columns here
     ts_b, _ = _load("b")
     with pytest.raises(LibraryError) as e:
-        ts_b.diversity([[u] for u in ts_b.samples()[:33]], mode="node")
+        ts_b.general_stat(np.random.default_rng(1).normal(size=(ts_b.num_samples, 33)),
+                          lambda x: x[:1], 1, mode="node", strict=False)
     assert e.value.code == nat.ERR_TOO_MANY_SAMPLE_SETS
 
 

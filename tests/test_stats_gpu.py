@@ -227,3 +227,45 @@ def test_global_state_form_large_n(cuda_lib, n, breaks):
             got = r.cpu().numpy().reshape(exp.shape)
             rtol = RTOL_F64 if (precision == "f64" or mode == "site") else RTOL_F32
             np.testing.assert_allclose(got, exp, rtol=rtol, err_msg=f"{mode} {precision}")
+
+
+@pytest.mark.parametrize("mode", ["site", "branch"])
+def test_many_sets_and_outputs_split(medium, mode):
+    """More sets than one sweep holds (40 > 32) and more outputs (105 > 64):
+    groups of outputs swept with just their sets, columns back in place;
+    against the oracle.  The centred relatedness over more than 32 sets is
+    refused (its mean runs over every set)."""
+    import tskit_gb300
+
+    ts, ots, tables = medium
+    sets = _sets(tables, 40, seed=3)
+    win = np.linspace(0, tables.sequence_length, 4)
+    got = ts.diversity(sets, windows=win, mode=mode)
+    exp = O.one_way(ots, O.DIVERSITY, sets, windows=win, mode=mode)
+    np.testing.assert_allclose(got, exp, rtol=RTOL_F64, atol=1e-13)
+    sets15 = sets[:15]
+    pairs = [(i, j) for i in range(15) for j in range(i, 15)][:105]
+    got = ts.divergence(sets15, indexes=pairs, windows=win, mode=mode)
+    exp = O.k_way(ots, O.DIVERGENCE, sets15, pairs, windows=win, mode=mode)
+    np.testing.assert_allclose(got, exp, rtol=RTOL_F64, atol=1e-13)
+    triples = [(i, (i + 7) % 40, (i + 19) % 40) for i in range(40)]
+    got = ts.Y3(sets, indexes=triples, windows=win, mode=mode)
+    exp = O.k_way(ots, O.Y3, sets, triples, windows=win, mode=mode)
+    np.testing.assert_allclose(got, exp, rtol=RTOL_F64, atol=1e-13)
+    with pytest.raises(tskit_gb300.LibraryError):
+        ts.genetic_relatedness(sets, indexes=[(0, 1)], mode=mode, proportion=False)
+    # a duplicate sample in a set no output uses is still an error
+    bad = [list(s) for s in sets[:33]]
+    bad[32] = bad[32] + [bad[32][0]]
+    with pytest.raises(tskit_gb300.LibraryError) as e:
+        ts.divergence(bad, indexes=[(0, 1)], mode=mode)
+    assert e.value.code == -600
+
+
+def test_many_sets_node_mode(medium):
+    ts, ots, tables = medium
+    sets = _sets(tables, 36, seed=4)
+    got = ts.diversity(sets, mode="node")
+    exp = O.one_way(ots, O.DIVERSITY, sets, mode="node")
+    np.testing.assert_allclose(got, np.asarray(exp).reshape(got.shape), rtol=RTOL_F64,
+                               atol=1e-13)

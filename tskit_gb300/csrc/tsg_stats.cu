@@ -2825,6 +2825,105 @@ static int run_sync(const tsg_treeseq_t *ts, uint64_t K, const uint64_t *sizes,
     const int32_t *sets, uint64_t R, const tsg_output_t *outs, uint64_t Wn,
     const double *windows, uint32_t options, double *result)
 {
+    if (R > TSG_MAX_OUTPUTS || K > TSG_MAX_SAMPLE_SETS) {
+        // more outputs or sets than one sweep carries: groups of outputs
+        // whose sets fit one sweep, each swept with just its sets, their
+        // columns put back in place (the centred relatedness averages over
+        // all sets, so it cannot be split by sets)
+        // every set checked as the reference does, used by an output or not
+        std::vector<int64_t> seen((size_t) ts->v.num_samples, -1);
+        for (uint64_t k = 0, j = 0; k < K; k++) {
+            if (sizes[k] == 0) {
+                return TSG_ERR_EMPTY_SAMPLE_SET;
+            }
+            for (uint64_t l = 0; l < sizes[k]; l++) {
+                const int32_t u = sets[j++];
+                if (u < 0 || u >= ts->v.num_nodes) {
+                    return TSG_ERR_NODE_OUT_OF_BOUNDS;
+                }
+                const int32_t si = ts->h_sample_index[(size_t) u];
+                if (si < 0) {
+                    return TSG_ERR_BAD_SAMPLES;
+                }
+                if (seen[(size_t) si] == (int64_t) k) {
+                    return TSG_ERR_DUPLICATE_SAMPLE;
+                }
+                seen[(size_t) si] = (int64_t) k;
+            }
+        }
+        if (K > TSG_MAX_SAMPLE_SETS) {
+            for (uint64_t r = 0; r < R; r++) {
+                if (outs[r].type == TSG_RELATEDNESS) {
+                    return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+                }
+            }
+        }
+        std::vector<uint64_t> off((size_t) K + 1, 0);
+        for (uint64_t k = 0; k < K; k++) {
+            off[(size_t) k + 1] = off[(size_t) k] + sizes[k];
+        }
+        const int64_t nmodes = (options & TSG_STAT_BOTH_MODES) ? 2 : 1;
+        const int64_t rows = (options & TSG_STAT_NODE) ? ts->v.num_nodes : 1;
+        const int64_t nw = windows == nullptr ? 1 : (int64_t) Wn;
+        uint64_t r0 = 0;
+        while (r0 < R) {
+            // the group: outputs r0.. while their sets number at most
+            // TSG_MAX_SAMPLE_SETS and they at most TSG_MAX_OUTPUTS
+            std::vector<int32_t> map((size_t) K, -1), used;
+            uint64_t r1 = r0;
+            while (r1 < R && r1 - r0 < TSG_MAX_OUTPUTS) {
+                const int wdt = tuple_width(outs[r1].type);
+                std::vector<int32_t> add;
+                for (int j = 0; j < wdt; j++) {
+                    const int32_t ix = outs[r1].idx[j];
+                    if (ix < 0 || (uint64_t) ix >= K) {
+                        return TSG_ERR_BAD_SAMPLE_SET_INDEX;
+                    }
+                    if (map[(size_t) ix] < 0
+                        && std::find(add.begin(), add.end(), ix) == add.end()) {
+                        add.push_back(ix);
+                    }
+                }
+                if (used.size() + add.size() > TSG_MAX_SAMPLE_SETS) {
+                    break;
+                }
+                for (int32_t ix : add) {
+                    map[(size_t) ix] = (int32_t) used.size();
+                    used.push_back(ix);
+                }
+                r1++;
+            }
+            if (r1 == r0) {
+                return TSG_ERR_TOO_MANY_SAMPLE_SETS;
+            }
+            std::vector<uint64_t> gsizes;
+            std::vector<int32_t> gsets;
+            for (int32_t k : used) {
+                gsizes.push_back(sizes[k]);
+                gsets.insert(gsets.end(), sets + off[(size_t) k], sets + off[(size_t) k + 1]);
+            }
+            std::vector<tsg_output_t> gouts(outs + r0, outs + r1);
+            for (auto &o : gouts) {
+                const int wdt = tuple_width(o.type);
+                for (int j = 0; j < wdt; j++) {
+                    o.idx[j] = map[(size_t) o.idx[j]];
+                }
+            }
+            const uint64_t rc = r1 - r0;
+            std::vector<double> part((size_t) (nmodes * nw * rows * (int64_t) rc), 0.0);
+            const int ret = run_sync(ts, used.size(), gsizes.data(), gsets.data(), rc,
+                gouts.data(), Wn, windows, options, part.data());
+            if (ret != 0) {
+                return ret;
+            }
+            for (int64_t b = 0; b < nmodes * nw * rows; b++) {
+                std::copy(part.begin() + b * (int64_t) rc, part.begin() + (b + 1) * (int64_t) rc,
+                    result + b * (int64_t) R + (int64_t) r0);
+            }
+            r0 = r1;
+        }
+        return 0;
+    }
     if (options & TSG_STAT_NODE) {
         return node_sets(ts, K, sizes, sets, R, outs, Wn, windows, options, result);
     }
