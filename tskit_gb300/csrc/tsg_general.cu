@@ -555,26 +555,22 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
             nopen += __popc(m);
             __syncwarp();
         };
+        // touches in the counting replay's batches: a stateful child on
+        // lane 0 with the first 31 nodes of the parent's root path, then 32
+        // path nodes at a time (the span plan counts items so)
         auto event = [&](int32_t p, int32_t c, int sign) {
             double xc[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 xc[k] = k < K ? (c >= 0 ? x[(int64_t) c * K + k] : leaf_w(-c - 1, k)) : 0.0;
             }
-            if (c >= 0) {
-                if (q.branch) {
-                    touch(lane == 0, c, par[c]);
-                }
-                if (lane == 0) {
-                    par[c] = sign > 0 ? p : -1;
-                }
-                __syncwarp();
-            }
             int32_t v = p;
             int32_t batches = 0;
+            bool first = true;
             while (v >= 0) {
+                const bool is_child = first && c >= 0 && lane == 0;
                 int32_t mine = -1;
-                for (int j = 0; j < 32 && v >= 0; j++) {
+                for (int j = (first && c >= 0) ? 1 : 0; j < 32 && v >= 0; j++) {
                     if (lane == j) {
                         mine = v;
                     }
@@ -588,11 +584,17 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
                 if (lane == 31) {
                     up = v;
                 }
+                if (is_child) {
+                    mine = c;
+                    up = par[c];
+                }
                 const bool act = mine >= 0;
                 if (q.branch) {
                     touch(act, mine, act ? up : -1);
                 }
-                if (act && K <= 8) {
+                if (is_child) {
+                    par[c] = sign > 0 ? p : -1;
+                } else if (act && K <= 8) {
 #pragma unroll
                     for (int k = 0; k < 8; k++) {
                         if (k < K) {
@@ -608,6 +610,7 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
                     }
                 }
                 __syncwarp();
+                first = false;
             }
         };
         const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;

@@ -203,8 +203,9 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     // (the child of an edge event when stateful -- leaves are accounted per
     // edge -- and every node on the parent's root path), counted once per
     // touch list: the replay keeps at most TSG_TOUCH_CAP nodes in a list
-    // and, when a touch (a single child, or a batch of up to 32 consecutive
-    // path nodes) would overflow it, closes the list and opens a new one.
+    // and, when a touch batch (the stateful child with the first 31 nodes of
+    // the parent's root path, then 32 path nodes at a time) would overflow
+    // it, closes the list and opens a new one.
     // The transitions into a span's trees after the first and into the next
     // span's first tree belong to the span.  The path lengths are
     // topology-only, so the replay is simulated here.
@@ -286,14 +287,16 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
                             }
                         }
                     };
-                    // the stateful child c (if any), then the root path from v
+                    // the stateful child c (if any) and the root path from v,
+                    // touched in batches of 32: the child with the path's
+                    // first 31 nodes, then 32 path nodes at a time
                     auto event = [&](int32_t c, int32_t v) {
-                        if (c >= 0) {
-                            path.assign(1, c);
-                            list_touch(0, 1);
-                        }
                         path.clear();
-                        while (v >= 0 && path.size() <= Ls) {
+                        if (c >= 0) {
+                            path.push_back(c);
+                        }
+                        const size_t base = path.size();
+                        while (v >= 0 && path.size() - base <= Ls) {
                             touch(v);
                             path.push_back(v);
                             v = par[(size_t) v];

@@ -134,7 +134,6 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
             int64_t cursor = 0;  // first item of the open list
             int64_t climit = 0;  // end of the transition's items in the plan
             int32_t nopen = 0;   // nodes in the open list
-            int32_t closes = 0;  // lists closed so far
             auto close_list = [&]() {
                 __syncwarp();
                 for (int32_t i = lane; i < nopen; i += 32) {
@@ -150,17 +149,15 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 __syncwarp();
                 cursor += nopen;
                 nopen = 0;
-                closes++;
             };
             // Lanes with `active` set touch node u (distinct per lane) whose
             // counts are still x0 and whose parent entry (flag and parent) is
-            // praw (its flag out of date if `stale`: no node then is in the
-            // open list); returns the entry with the flag set, which the
-            // caller stores (with the node's new parent, for an edge's
-            // child).  A node is touched at most once per edge event and
-            // every event ends with __syncwarp.
-            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw, bool stale) {
-                bool fresh = active && (stale || !(praw & PFLAG));
+            // praw, read after the previous batch's touches; returns the
+            // entry with the flag set, which the caller stores (with the
+            // node's new parent, for an edge's child).  A node is touched at
+            // most once per edge event and every event ends with __syncwarp.
+            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw) {
+                bool fresh = active && !(praw & PFLAG);
                 unsigned m = __ballot_sync(0xffffffffu, fresh);
                 if (nopen + __popc(m) > TSG_TOUCH_CAP) {
                     close_list();
@@ -185,15 +182,14 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 nopen += __popc(m);
                 return (praw & PMASK) | PFLAG;
             };
-            // one edge event; cm: membership bits of a leaf child (whose branch
-            // is accounted per edge, k_leaf_areas)
-            // the next (up to) 32 nodes of a root path from v, lane j taking
-            // the j-th with its parent entry; advances v past them
-            auto chase = [&](uint32_t &v, uint32_t &mine, uint32_t &mraw) {
+            // the next (up to) 32 - first nodes of a root path from v, lane
+            // first + j taking the j-th with its parent entry; advances v
+            // past them
+            auto chase = [&](uint32_t &v, uint32_t &mine, uint32_t &mraw, int first) {
                 mine = NO_NODE;
                 mraw = 0;
 #pragma unroll 4
-                for (int j = 0; j < 32; j++) {
+                for (int j = first; j < 32; j++) {
                     if (v == TSG_NO_PARENT) {
                         break;
                     }
@@ -204,38 +200,40 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                 }
             };
             // One edge event; cm: membership bits of a leaf child (whose
-            // branch is accounted per edge, k_leaf_areas).  The first part of
-            // the parent's root path is read before the child is handled (the
-            // child is not on it), hiding the walk's latency; a touch list
-            // closed in between makes the path's touch flags stale.
+            // branch is accounted per edge, k_leaf_areas).  The nodes are
+            // touched in batches of 32 lanes: a stateful child on lane 0
+            // with the first 31 nodes of the parent's root path (the child is
+            // not on it), then 32 path nodes at a time -- one touch-list
+            // step per batch (the span plan counts items with the same
+            // batches).  The child keeps its counts and takes its new parent;
+            // the path nodes add or remove the child's counts.
             auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
                 uint32_t v = (uint32_t) p, mine, mraw;
-                chase(v, mine, mraw);
-                const int32_t gen0 = closes;
-                const Pack xc = c >= 0 ? st_load(sp, c) : pk_from_mask<W>(cm, K);
-                if (c >= 0) {
-                    const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
-                    if (q.branch) {
-                        touch(lane == 0, (uint32_t) c, xc, (uint32_t) sp.par[c], false);
-                        sp.par[c] = (IdxT) (np | PFLAG);
-                    } else {
-                        sp.par[c] = (IdxT) np;
-                    }
+                const bool child = c >= 0;
+                chase(v, mine, mraw, child ? 1 : 0);
+                const Pack xc = child ? st_load(sp, c) : pk_from_mask<W>(cm, K);
+                bool is_child = false;
+                if (child && lane == 0) {
+                    mine = (uint32_t) c;
+                    mraw = (uint32_t) sp.par[c];
+                    is_child = true;
                 }
-                bool stale = closes != gen0;
+                const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
                 for (int32_t batches = 1;; batches++) {
                     const bool act = mine != NO_NODE;
                     Pack xo{0, 0};
                     if (act) {
-                        xo = st_load(sp, (int64_t) mine);
+                        xo = is_child ? xc : st_load(sp, (int64_t) mine);
                     }
                     if (q.branch) {
-                        const uint32_t f = touch(act, mine, xo, mraw, stale);
+                        const uint32_t f = touch(act, mine, xo, mraw);
                         if (act) {
-                            sp.par[mine] = (IdxT) f;
+                            sp.par[mine] = (IdxT) (is_child ? (np | PFLAG) : f);
                         }
+                    } else if (is_child) {
+                        sp.par[mine] = (IdxT) np;
                     }
-                    if (act) {
+                    if (act && !is_child) {
                         Pack xn;
                         if (sign > 0) {
                             xn.lo = xo.lo + xc.lo;
@@ -254,8 +252,8 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
                         dev_error(w.err, DEV_PATH_TOO_LONG);
                         break;
                     }
-                    chase(v, mine, mraw);
-                    stale = false;
+                    chase(v, mine, mraw, 0);
+                    is_child = false;
                 }
                 __syncwarp();
             };
