@@ -324,6 +324,12 @@ int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t
     const double *weights, uint64_t num_index_tuples, const int32_t *index_tuples,
     uint64_t num_windows, const double *windows, double *result, uint32_t options);
 
+/* Replaces tsk_treeseq_mean_descendants (c/tskit/trees.c:1076-1220): the
+ * reference sets (any nodes) flattened with their sizes instead of an array
+ * of pointers; at most 31 sets.  Result num_nodes x num_sets. */
+int tsg_treeseq_mean_descendants(const tsg_treeseq_t *self, uint64_t num_sets,
+    const uint64_t *set_sizes, const int32_t *sets, uint32_t options, double *result);
+
 /* Replace tsk_treeseq_trait_covariance / trait_correlation /
  * trait_linear_model (c/tskit/trees.c:3976-4218, same arguments; weights
  * host [n x num_weights], covariates [n x num_covariates] already

@@ -421,8 +421,8 @@ int gen_unpack(int W, const uint64_t *ulo, const uint64_t *uhi, int64_t U, int K
 // mutation.  Lane k carries weight component k (K <= 32) in the seek; a
 // root-path batch takes one node per lane, each adding all components.
 __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const double *W,
-    int K, double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int4 *ids, double *xs,
-    double *mstate, double *init, int32_t *err, int32_t *counter)
+    int node_w, int K, double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int4 *ids,
+    double *xs, double *mstate, double *init, int32_t *err, int32_t *counter)
 {
     __shared__ int s_span;
     __shared__ int32_t s_list[TSG_TOUCH_CAP];
@@ -431,7 +431,11 @@ __global__ void __launch_bounds__(64) k_wreplay(TSView ts, QueryParams q, const 
     int32_t *par = slots_par + (int64_t) blockIdx.x * L;
     uint8_t *touched = slots_touched + (int64_t) blockIdx.x * L;
     const int lane = threadIdx.x & 31;
+    // a node's own weight: W by sample index, or by node id (node_w)
     auto leaf_w = [&](int32_t g, int k) {
+        if (node_w) {
+            return k < K ? W[(int64_t) g * K + k] : 0.0;
+        }
         const int32_t si = ts.sample_index[g];
         return si >= 0 && k < K ? W[(int64_t) si * K + k] : 0.0;
     };
@@ -820,12 +824,12 @@ __global__ void __launch_bounds__(256) k_wleaf_prefix(QueryParams q, QueryDev qd
     }
 }
 
-int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
-    int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
-    double *init, int32_t *err, int32_t *counter, cudaStream_t st)
+int genw_replay(const TSView &v, const QueryParams &q, const double *W, bool node_w, int K,
+    double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs,
+    double *mstate, double *init, int32_t *err, int32_t *counter, cudaStream_t st)
 {
-    k_wreplay<<<(unsigned) grid, 64, 0, st>>>(v, q, W, K, slots_x, slots_par, slots_touched, ids,
-        xs, mstate, init, err, counter);
+    k_wreplay<<<(unsigned) grid, 64, 0, st>>>(v, q, W, node_w ? 1 : 0, K, slots_x, slots_par,
+        slots_touched, ids, xs, mstate, init, err, counter);
     TSG_LAUNCHED();
     return 0;
 }
@@ -978,6 +982,33 @@ int genw_summary_trait(const double *states, int64_t U, int K, int R, int kind, 
     return 0;
 }
 
+// mean_descendants (c/tskit/trees.c:1076-1220): per state, the counts of
+// the K - 1 reference sets and whether the union count is positive; the
+// node walk integrates them into each node's spans, divided on the host.
+__global__ void k_wsummary_descendants(const double *states, int64_t U, int K, double *vals)
+{
+    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < U;
+         u += (int64_t) gridDim.x * blockDim.x) {
+        const double *x = states + u * K;
+        const double any = x[K - 1] > 0 ? 1.0 : 0.0;
+        for (int k = 0; k < K - 1; k++) {
+            vals[u * K + k] = any * x[k];
+        }
+        vals[u * K + K - 1] = any;
+    }
+}
+
+int genw_summary_descendants(const double *states, int64_t U, int K, double *vals,
+    cudaStream_t st)
+{
+    if (U == 0) {
+        return 0;
+    }
+    k_wsummary_descendants<<<gen_grid(U), 256, 0, st>>>(states, U, K, vals);
+    TSG_LAUNCHED();
+    return 0;
+}
+
 int genw_summary_relatedness(const double *states, int64_t U, int K1, const double *total,
     const int32_t *tuples, int R, double ones, bool centred, bool complement, double *vals,
     cudaStream_t st)
@@ -1001,15 +1032,15 @@ int genw_summary_relatedness(const double *states, int64_t U, int K1, const doub
 // genome order, adding (end - start) x f(state) per interval and window in
 // the order the reference's sweep adds them.
 
-// every node's own weight (samples) or zero, before the first tree's state
-// is written over it by the replay
-__global__ void k_node_init(TSView ts, int K, const double *W, double *init)
+// every node's own weight (by sample index, or by node id with node_w),
+// before the first tree's state is written over it by the replay
+__global__ void k_node_init(TSView ts, int K, const double *W, int node_w, double *init)
 {
     for (int64_t g = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; g < ts.num_nodes;
          g += (int64_t) gridDim.x * blockDim.x) {
         const int32_t si = ts.sample_index[g];
         for (int k = 0; k < K; k++) {
-            init[g * K + k] = si >= 0 ? W[(int64_t) si * K + k] : 0.0;
+            init[g * K + k] = node_w ? W[g * K + k] : si >= 0 ? W[(int64_t) si * K + k] : 0.0;
         }
     }
 }
@@ -1173,10 +1204,11 @@ __global__ void k_node_term_values(QueryParams q, const double *states, int64_t 
     }
 }
 
-int node_init(const TSView &v, int K, const double *W, double *init, cudaStream_t st)
+int node_init(const TSView &v, int K, const double *W, bool node_w, double *init,
+    cudaStream_t st)
 {
     if (v.num_nodes > 0) {
-        k_node_init<<<gen_grid(v.num_nodes), 256, 0, st>>>(v, K, W, init);
+        k_node_init<<<gen_grid(v.num_nodes), 256, 0, st>>>(v, K, W, node_w ? 1 : 0, init);
         TSG_LAUNCHED();
     }
     return 0;

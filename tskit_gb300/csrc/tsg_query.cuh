@@ -156,11 +156,14 @@ int gen_collect(int form, const TSView &v, const QueryParams &q, const WsDev &w,
     uint64_t *thi, int64_t *flag, int64_t *pos, void *cub_tmp, size_t cub_bytes, uint64_t *ulo,
     uint64_t *uhi, int64_t *U, cudaStream_t st);
 size_t gen_cub_bytes(int64_t n);
-int genw_replay(const TSView &v, const QueryParams &q, const double *W, int K, double *slots_x,
-    int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs, double *mstate,
-    double *init, int32_t *err, int32_t *counter, cudaStream_t st);
+int genw_replay(const TSView &v, const QueryParams &q, const double *W, bool node_w, int K,
+    double *slots_x, int32_t *slots_par, uint8_t *slots_touched, int grid, int4 *ids, double *xs,
+    double *mstate, double *init, int32_t *err, int32_t *counter, cudaStream_t st);
 // node mode
-int node_init(const TSView &v, int K, const double *W, double *init, cudaStream_t st);
+int node_init(const TSView &v, int K, const double *W, bool node_w, double *init,
+    cudaStream_t st);
+int genw_summary_descendants(const double *states, int64_t U, int K, double *vals,
+    cudaStream_t st);
 size_t node_sort_bytes(int64_t I);
 int node_order(const TSView &v, int K, const int4 *ids, const double *xs, const double *init,
     uint64_t *keys, uint64_t *keys_sorted, int32_t *idx, int32_t *idx_sorted, void *temp,

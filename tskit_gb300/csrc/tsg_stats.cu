@@ -2261,12 +2261,18 @@ int tsg_general_stat_free(tsg_general_t *g)
     return 0;
 }
 
-// Real-valued weights: the replay of a query with K all-sample sets (its
+}  // extern "C"
+
+namespace tsg {
+
+// Real-valued weights: the replay of a query with one all-sample set (its
 // windows and workspace) and placeholder terms; the states are the weights
-// below each node.
-int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint64_t K,
-    const double *weights, uint64_t R, uint64_t Wn, const double *windows, uint32_t options,
-    int64_t *num_states)
+// below each node.  weights: n x K by sample index, or N x K by node id
+// (node_weights: any node may carry weight, as mean_descendants' reference
+// sets do).
+static int weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const double *weights, bool node_weights, uint64_t R, uint64_t Wn, const double *windows,
+    uint32_t options, int64_t *num_states)
 {
     *out = nullptr;
     if (R < 1) {
@@ -2352,10 +2358,12 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     g->U = U;
     std::vector<double> total((size_t) K, 0.0);
     for (int64_t j = 0; j < n; j++) {
+        const int64_t row = node_weights ? (int64_t) sets[(size_t) j] : j;
         for (uint64_t k = 0; k < K; k++) {
-            total[(size_t) k] += weights[j * K + k];
+            total[(size_t) k] += weights[row * (int64_t) K + (int64_t) k];
         }
     }
+    const int64_t wrows = node_weights ? v.num_nodes : n;
     const int64_t L = std::max<int64_t>(v.max_local, 1);
     const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(v.num_spans,
         2 * (int64_t) std::max(device_count_sms(), 1)));
@@ -2367,7 +2375,7 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
         off += align_up(std::max<int64_t>(bytes, 8), 256);
         return o;
     };
-    const int64_t oW = take(n * (int64_t) K * 8), oT = take((int64_t) K * 8);
+    const int64_t oW = take(wrows * (int64_t) K * 8), oT = take((int64_t) K * 8);
     const int64_t oSO = take((v.num_sites + 1) * 8);
     const int64_t oX = take(grid * L * (int64_t) K * 8), oP = take(grid * L * 4), oF = take(grid * L);
     const int64_t oI = take(items * 16), oS = take(U * (int64_t) K * 8);
@@ -2393,7 +2401,8 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     int32_t *derr = (int32_t *) (b + oE);
     cudaStream_t st = g->st;
     ret = 0;
-    if (cudaMemcpyAsync(dW, weights, (size_t) (n * K * 8), cudaMemcpyHostToDevice, st) != cudaSuccess
+    if (cudaMemcpyAsync(dW, weights, (size_t) (wrows * (int64_t) K * 8), cudaMemcpyHostToDevice,
+            st) != cudaSuccess
         || cudaMemcpyAsync(dT, total.data(), (size_t) (K * 8), cudaMemcpyHostToDevice, st) != cudaSuccess
         || cudaMemcpyAsync(g->site_off, site_off.data(), site_off.size() * 8,
                cudaMemcpyHostToDevice, st) != cudaSuccess
@@ -2402,10 +2411,10 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     }
     double *dXS = (double *) (b + oXS), *dIN = (double *) (b + oIN);
     if (ret == 0 && node) {
-        ret = node_init(v, (int) K, dW, dIN, st);
+        ret = node_init(v, (int) K, dW, node_weights, dIN, st);
     }
     if (ret == 0) {
-        ret = genw_replay(v, p, dW, (int) K, (double *) (b + oX), (int32_t *) (b + oP),
+        ret = genw_replay(v, p, dW, node_weights, (int) K, (double *) (b + oX), (int32_t *) (b + oP),
             (uint8_t *) (b + oF), (int) grid, g->ids, node ? dXS : g->states,
             (double *) (b + oM), node ? dIN : nullptr, derr, derr + 1, st);
     }
@@ -2434,6 +2443,76 @@ int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, u
     }
     *num_states = U;
     *out = g;
+    return 0;
+}
+
+}  // namespace tsg
+
+extern "C" {
+
+int tsg_general_weighted_prepare(tsg_general_t **out, const tsg_treeseq_t *ts, uint64_t K,
+    const double *weights, uint64_t R, uint64_t Wn, const double *windows, uint32_t options,
+    int64_t *num_states)
+{
+    return weighted_prepare(out, ts, K, weights, false, R, Wn, windows, options, num_states);
+}
+
+// tsk_treeseq_mean_descendants (c/tskit/trees.c:1076-1220): for every node
+// and reference set, the mean number of the set's nodes below it over the
+// parts of the sequence where it is above any reference node.  The sets
+// (any nodes, flattened with their sizes) become node weights with a last
+// column for their union; node mode integrates each set's count and the
+// union's indicator along the genome for every node.
+int tsg_treeseq_mean_descendants(const tsg_treeseq_t *self, uint64_t num_sets,
+    const uint64_t *set_sizes, const int32_t *sets, uint32_t options, double *result)
+{
+    (void) options;
+    const int64_t N = self->v.num_nodes;
+    if (num_sets == 0 || num_sets + 1 > TSG_MAX_SAMPLE_SETS) {
+        return num_sets == 0 ? TSG_ERR_BAD_PARAM_VALUE : TSG_ERR_TOO_MANY_SAMPLE_SETS;
+    }
+    const uint64_t K = num_sets + 1;
+    std::vector<double> w((size_t) (N * (int64_t) K), 0.0);
+    for (uint64_t k = 0, j = 0; k < num_sets; k++) {
+        for (uint64_t l = 0; l < set_sizes[k]; l++, j++) {
+            const int32_t u = sets[j];
+            if (u < 0 || u >= N) {
+                return TSG_ERR_NODE_OUT_OF_BOUNDS;
+            }
+            w[(size_t) ((int64_t) u * (int64_t) K + (int64_t) k)] = 1.0;
+            w[(size_t) ((int64_t) u * (int64_t) K + (int64_t) num_sets)] = 1.0;
+        }
+    }
+    tsg_general_t *g = nullptr;
+    int64_t U = 0;
+    int ret = weighted_prepare(&g, self, K, w.data(), true, K, 0, nullptr,
+        TSG_STAT_NODE | TSG_STAT_POLARISED, &U);
+    if (ret != 0) {
+        return ret;
+    }
+    std::vector<double> sums((size_t) (N * (int64_t) K));
+    double *dF = nullptr;
+    if (cudaMalloc(&dF, (size_t) std::max<int64_t>(U * (int64_t) K * 8, 8)) != cudaSuccess) {
+        cudaGetLastError();
+        ret = TSG_ERR_NO_MEMORY;
+    } else {
+        ret = genw_summary_descendants(g->states, U, (int) K, dF, g->st);
+        if (ret == 0) {
+            ret = general_finish(g, dF, sums.data());
+        }
+    }
+    cudaFree(dF);
+    tsg_general_stat_free(g);
+    if (ret != 0) {
+        return ret;
+    }
+    for (int64_t u = 0; u < N; u++) {
+        const double *row = sums.data() + u * (int64_t) K;
+        const double span = row[num_sets];
+        for (uint64_t k = 0; k < num_sets; k++) {
+            result[u * (int64_t) num_sets + (int64_t) k] = span > 0 ? row[k] / span : 0.0;
+        }
+    }
     return 0;
 }
 

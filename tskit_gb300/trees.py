@@ -837,6 +837,20 @@ class TreeSequence:
                                         mode=mode, span_normalise=span_normalise,
                                         centre=centre, nodes=nodes)
 
+    def mean_descendants(self, sample_sets):
+        """python/tskit/trees.py:10430-10450: for every node and set, the
+        mean number of the set's nodes descending from it, over the parts of
+        the genome where it is an ancestor of any node of the sets; shape
+        (num_nodes, num_sets)."""
+        sizes = np.array([len(s) for s in sample_sets], dtype=np.uint64)
+        flat = (safe_np_int_cast(np.hstack([np.asarray(s) for s in sample_sets]), np.int32)
+                if len(sample_sets) else np.zeros(0, dtype=np.int32))
+        flat = np.ascontiguousarray(flat, dtype=np.int32)
+        res = np.zeros((self.num_nodes, len(sample_sets)))
+        nat.check(self._lib.tsg_treeseq_mean_descendants(
+            self._handle, len(sizes), _ptr(sizes), _ptr(flat), 0, _ptr(res)))
+        return res
+
     # --------------------------------------------------------------- traits
     def _ll_trait(self, fn, weights, windows, covariates=None, mode=None, span_normalise=True):
         """Low-level trait statistic (python/_tskitmodule.c weighted-stat
