@@ -324,6 +324,14 @@ int tsg_treeseq_genetic_relatedness_weighted(const tsg_treeseq_t *self, uint64_t
     const double *weights, uint64_t num_index_tuples, const int32_t *index_tuples,
     uint64_t num_windows, const double *windows, double *result, uint32_t options);
 
+/* Replaces tsk_treeseq_genealogical_nearest_neighbours (c/tskit/trees.c:
+ * 891-1074): the reference sets (any nodes, no node in two sets) flattened
+ * with their sizes instead of an array of pointers.  Result num_focal x
+ * num_sets. */
+int tsg_treeseq_genealogical_nearest_neighbours(const tsg_treeseq_t *self,
+    const int32_t *focal, uint64_t num_focal, uint64_t num_sets, const uint64_t *set_sizes,
+    const int32_t *sets, uint32_t options, double *result);
+
 /* Replaces tsk_treeseq_mean_descendants (c/tskit/trees.c:1076-1220): the
  * reference sets (any nodes) flattened with their sizes instead of an array
  * of pointers; at most 31 sets.  Result num_nodes x num_sets. */

@@ -34,6 +34,7 @@ CUDA_SOURCES = [
     "tsg_general.cu",
     "tsg_kastore.cu",
     "tsg_index.cu",
+    "tsg_gnn.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -141,6 +141,8 @@ SIGNATURES = {
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _U64, _U64, _P, _U32,
                        ctypes.POINTER(_I64)]),
     "tsg_general_weighted_states": (ctypes.c_int, [_P, _P]),
+    "tsg_treeseq_genealogical_nearest_neighbours": (
+        ctypes.c_int, [_P, _P, _U64, _U64, _P, _P, _U32, _P]),
     "tsg_treeseq_mean_descendants": (ctypes.c_int, [_P, _U64, _P, _P, _U32, _P]),
     "tsg_treeseq_trait_covariance": (ctypes.c_int, [_P, _U64, _P, _U64, _P, _U32, _P]),
     "tsg_treeseq_trait_correlation": (ctypes.c_int, [_P, _U64, _P, _U64, _P, _U32, _P]),

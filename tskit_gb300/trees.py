@@ -837,6 +837,23 @@ class TreeSequence:
                                         mode=mode, span_normalise=span_normalise,
                                         centre=centre, nodes=nodes)
 
+    def genealogical_nearest_neighbours(self, focal, sample_sets, num_threads=0):
+        """python/tskit/trees.py:10452-10530: for every focal node, the
+        reference sets' mean shares of its nearest neighbours (the smallest
+        subtree above it holding another reference node) over the trees;
+        shape (num_focal, num_sets).  num_threads is accepted for
+        compatibility (the work runs on the GPU)."""
+        focal = np.ascontiguousarray(safe_np_int_cast(focal, np.int32), dtype=np.int32)
+        sizes = np.array([len(s) for s in sample_sets], dtype=np.uint64)
+        flat = (safe_np_int_cast(np.hstack([np.asarray(s) for s in sample_sets]), np.int32)
+                if len(sample_sets) else np.zeros(0, dtype=np.int32))
+        flat = np.ascontiguousarray(flat, dtype=np.int32)
+        res = np.zeros((len(focal), len(sample_sets)))
+        nat.check(self._lib.tsg_treeseq_genealogical_nearest_neighbours(
+            self._handle, _ptr(focal), len(focal), len(sizes), _ptr(sizes), _ptr(flat), 0,
+            _ptr(res)))
+        return res
+
     def mean_descendants(self, sample_sets):
         """python/tskit/trees.py:10430-10450: for every node and set, the
         mean number of the set's nodes descending from it, over the parts of
