@@ -367,7 +367,7 @@ def run_gpu(args):
     import torch
 
     import tskit_gb300
-    from tskit_gb300 import _build, _native as nat
+    from tskit_gb300 import _build, _native as nat, tune
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -388,13 +388,23 @@ def run_gpu(args):
     traversals = REFERENCE_TRAVERSALS_PER_MODE * len(MODES)
     logical = events * traversals
 
-    ts = tskit_gb300.TreeSequence(tables)
-    q = ts.query(sets, terms, windows=windows, both_modes=True, span_normalise=False,
-                 precision="f32")
-    ws = tskit_gb300.Workspace(q.workspace_bytes)
-    res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
+
+    def prepare(ts):
+        q = ts.query(sets, terms, windows=windows, both_modes=True, span_normalise=False,
+                     precision="f32")
+        ws = tskit_gb300.Workspace(q.workspace_bytes)
+        res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+        return q, ws, res
+
+    def tuning_step(ts):
+        q, ws, res = prepare(ts)
+        return lambda: q.launch(ws, res, stream)
+
+    # the span count is autotuned for this tree sequence and fused query
+    ts, tuned = tune.tune_num_spans(tables, tuning_step, key=WORKLOAD, steps=3, warmup=1)
+    q, ws, res = prepare(ts)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     ev_sweep0, ev_sweep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # torch creates the CUDA events on first record; the library re-records
     # them around the sweep kernel of every launch
@@ -505,7 +515,8 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32-kahan bulk, f64 windows; int32 counts",
         "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
-        "config": workload_config(tables),
+        "config": dict(workload_config(tables), num_spans=tuned["num_spans"],
+                       span_tuning_ms={str(k): v for k, v in tuned["ms"].items()}),
         "queries_per_s": world * traversals / (ms / 1e3),
         "physical_edge_updates_per_s": world * events / (ms / 1e3),
         "plain_fp64": {
@@ -583,7 +594,7 @@ def run_afs_n200k(args):
     import torch
 
     import tskit_gb300
-    from tskit_gb300 import _build, _native as nat, sim
+    from tskit_gb300 import _build, _native as nat, sim, tune
     from tskit_gb300.trees import AfsQuery, RelatednessVectorQuery
 
     torch.cuda.set_device(0)
@@ -598,22 +609,29 @@ def run_afs_n200k(args):
     L = tables.sequence_length
     windows = np.linspace(0, L, 11)
     W = np.random.default_rng(seed + 2).normal(size=(len(tables.samples()), 64))
-    ts = tskit_gb300.TreeSequence(tables)
     stream = torch.cuda.current_stream()
     span = nat.STAT_SPAN_NORMALISE
-    qs = [AfsQuery(ts, s, windows, None, m | span)
-          for s in (allset, joint) for m in (nat.STAT_SITE, nat.STAT_BRANCH)]
-    mv = RelatednessVectorQuery(ts, 64, None, None, nat.STAT_BRANCH | span)
     Wd = torch.from_numpy(W).cuda()
-    mv.set_weights(Wd)
-    qs.append(mv)
-    ws = tskit_gb300.Workspace(max(q.workspace_bytes for q in qs))
-    outs = [torch.zeros(q.result_size, dtype=torch.float64, device="cuda") for q in qs]
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def step():
-        for q, o in zip(qs, outs):
-            q.launch(ws, o, stream)
+    def prepare(ts):
+        qs = [AfsQuery(ts, s, windows, None, m | span)
+              for s in (allset, joint) for m in (nat.STAT_SITE, nat.STAT_BRANCH)]
+        mv = RelatednessVectorQuery(ts, 64, None, None, nat.STAT_BRANCH | span)
+        mv.set_weights(Wd)
+        qs.append(mv)
+        ws = tskit_gb300.Workspace(max(q.workspace_bytes for q in qs))
+        outs = [torch.zeros(q.result_size, dtype=torch.float64, device="cuda") for q in qs]
+
+        def step():
+            for q, o in zip(qs, outs):
+                q.launch(ws, o, stream)
+        return qs, ws, outs, step
+
+    # the span count is autotuned for this tree sequence and step
+    ts, tuned = tune.tune_num_spans(tables, lambda t: prepare(t)[3], key="afs_n200k",
+                                    steps=2, warmup=1)
+    qs, ws, outs, step = prepare(ts)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     launches0 = lib.tsg_launch_count()
     with ClockSampler(0) as clocks:
@@ -647,7 +665,9 @@ def run_afs_n200k(args):
                    "ms_per_query": dict(zip(["afs_site_all", "afs_branch_all", "afs_site_joint",
                                              "afs_branch_joint", "relatedness_vector_w64"],
                                             per_q)),
-                   "l2": "flushed between timed steps (256 MiB write)"},
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "num_spans": tuned["num_spans"],
+                   "span_tuning_ms": {str(k): v for k, v in tuned["ms"].items()}},
         "queries_per_s": len(qs) / (ms / 1e3),
         "e2e": {"value": len(qs) * events / e2e_s, "unit": "edge-updates/s",
                 "ms_per_step": e2e_s * 1e3,

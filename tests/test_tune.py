@@ -1,0 +1,87 @@
+"""The span-count autotuner: selection logic with host fakes (no GPU) and, on
+a GPU, a tuned tree sequence whose statistics equal the default plan's."""
+import numpy as np
+import pytest
+
+from tskit_gb300 import tune
+
+
+class FakeTS:
+    def __init__(self, n, num_trees=1000):
+        self.num_spans = n if n > 0 else 297
+        self.num_trees = num_trees
+        self.num_edges = 4000
+        self.num_samples = 100
+
+
+def fake_timer(ms_of):
+    calls = []
+
+    def timer(step, steps, warmup):
+        calls.append(step())
+        return ms_of[calls[-1]]
+    return timer, calls
+
+
+def test_candidates_bounded_by_trees():
+    assert tune.span_candidates(297, 10_000, 152) == [76, 152, 297, 304, 456, 608]
+    assert tune.span_candidates(5, 40, 152) == [5, 40]
+
+
+def test_picks_fastest_and_reports_every_count():
+    ms = {297: 2.2, 76: 3.0, 152: 2.5, 304: 2.1, 456: 2.4, 608: 2.9}
+    timer, calls = fake_timer(ms)
+    ts, rep = tune.tune_num_spans(None, lambda t: (lambda: t.num_spans), build=FakeTS,
+                                  timer=timer, num_sms=152)
+    assert ts.num_spans == 304 and rep["num_spans"] == 304 and not rep["cached"]
+    assert rep["ms"] == ms
+    assert calls[0] == 297  # the default plan is timed first
+
+
+def test_ties_go_to_fewer_spans_and_duplicates_timed_once():
+    ms = {297: 2.0, 152: 2.0, 40: 9.0}
+    timer, calls = fake_timer(ms)
+
+    def build(n):
+        return FakeTS(min(n, 40) if n not in (0, 152, 297) else n)
+    ts, rep = tune.tune_num_spans(None, lambda t: (lambda: t.num_spans), build=build,
+                                  timer=timer, candidates=[40, 80, 152, 297], num_sms=152)
+    assert ts.num_spans == 152
+    assert sorted(calls) == [40, 152, 297]
+
+
+def test_cache_skips_measurement():
+    cache = {}
+    timer, calls = fake_timer({297: 2.0, 76: 1.0, 152: 3.0, 304: 3.0, 456: 3.0, 608: 3.0})
+    ts, rep = tune.tune_num_spans(None, lambda t: (lambda: t.num_spans), key="w", cache=cache,
+                                  build=FakeTS, timer=timer, num_sms=152)
+    assert ts.num_spans == 76 and len(cache) == 1
+    n = len(calls)
+    ts2, rep2 = tune.tune_num_spans(None, lambda t: (lambda: t.num_spans), key="w",
+                                    cache=cache, build=FakeTS, timer=timer, num_sms=152)
+    assert ts2.num_spans == 76 and rep2["cached"] and len(calls) == n
+
+
+@pytest.mark.gpu
+def test_tuned_plan_same_statistics():
+    import tskit_gb300
+    from tskit_gb300 import sim
+
+    tables = sim.simulate(300, 1e6, 600, 3000, 31)
+    rng = np.random.default_rng(5)
+    sets = [np.sort(p) for p in np.array_split(rng.permutation(tables.samples()), 3)]
+    windows = np.linspace(0, tables.sequence_length, 7)
+
+    def make_step(ts):
+        return lambda: ts.diversity(sets, windows=windows, mode="branch")
+    ts, rep = tune.tune_num_spans(tables, make_step, candidates=[1, 3, 17], steps=2, warmup=1)
+    assert rep["num_spans"] in rep["ms"] and len(rep["ms"]) >= 3
+    ref = tskit_gb300.TreeSequence(tables)
+    for mode in ("branch", "site"):
+        np.testing.assert_allclose(ts.diversity(sets, windows=windows, mode=mode),
+                                   ref.diversity(sets, windows=windows, mode=mode),
+                                   rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(
+            ts.divergence(sets, indexes=[(0, 1), (1, 2)], windows=windows, mode=mode),
+            ref.divergence(sets, indexes=[(0, 1), (1, 2)], windows=windows, mode=mode),
+            rtol=1e-12, atol=1e-14)
