@@ -234,11 +234,14 @@ int tsg_treeseq_genetic_relatedness_vector(const tsg_treeseq_t *self, uint64_t n
 
 /* ------------------------------------------------- divergence matrix (site)
  * Replaces tsk_treeseq_divergence_matrix (c/tskit/trees.c:8900-9001) for
- * site mode: same arguments, option bits, error codes and result
+ * site and branch mode: same arguments, option bits, error codes and result
  * (num_windows x K x K, K = num_sample_sets, or every sample alone when
- * sample_sets is NULL).  Branch mode returns TSG_ERR_UNSUPPORTED_STAT_MODE
- * (not on this path).  The pair counts come from an exact Gram matrix of
- * the 0/1 genotypes on the tensor cores.  Host pointers; synchronous. */
+ * sample_sets is NULL).  Site mode: the pair counts come from an exact Gram
+ * matrix of the 0/1 genotypes on the tensor cores.  Branch mode: each pair's
+ * path length through its MRCA per tree (c/tskit/trees.c:8578-8672), one CTA
+ * per 32 x 32 tile of pairs.  Node mode returns
+ * TSG_ERR_UNSUPPORTED_STAT_MODE, as the reference does.  Host pointers;
+ * synchronous. */
 int tsg_treeseq_divergence_matrix(const tsg_treeseq_t *self, uint64_t num_sample_sets,
     const uint64_t *sample_set_sizes, const int32_t *sample_sets, uint64_t num_windows,
     const double *windows, uint32_t options, double *result);
@@ -422,8 +425,10 @@ int tsg_workspace_free(tsg_workspace_t *ws);
  *     needs cleared: calls whose kernels overlap on the GPU (different
  *     streams, or different host threads) race and corrupt each other's
  *     results.  Order them on one stream.
- * tsg_noalloc_check reads the device-side check word of the last such
- * launch of `query` (synchronous), like tsg_workspace_check. */
+ * tsg_noalloc_check reads the device-side check word of the last
+ * no-allocation launch on the current device, whichever query it ran
+ * (synchronous; `query` is not used), like tsg_workspace_check: each launch
+ * copies its word to a fixed device word when it ends. */
 #define TSG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int tsg_query_launch_noalloc(const tsg_query_t *query, double *result_device, void *cuda_stream);
 int tsg_noalloc_check(const tsg_query_t *query);

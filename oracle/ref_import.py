@@ -3,8 +3,8 @@
 Test infrastructure only (never imported by the product).  The reference's
 CPython extension ``_tskit`` is compiled by ``make -C oracle ref`` into
 ``oracle/_ref/``; the reference's pure-Python package is read from the
-reference checkout, whose location is given by ``TSKIT_REFERENCE`` (default:
-the read-only checkout this project was developed against).  The package
+reference checkout, whose location is given by ``TSKIT_REFERENCE`` or else
+by the source location that build recorded in ``oracle/_ref/SOURCE``.  The package
 imports ``jsonschema`` at module import; ``oracle/shim`` supplies a no-op
 stand-in because jsonschema is not installed.
 """
@@ -15,11 +15,22 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def reference_root():
-    return os.environ.get("TSKIT_REFERENCE", "/root/reference")
+    """The reference checkout: ``TSKIT_REFERENCE``, else the one the
+    ``oracle/_ref`` build was made from (None when neither is known)."""
+    root = os.environ.get("TSKIT_REFERENCE")
+    if root:
+        return root
+    try:
+        with open(os.path.join(_HERE, "_ref", "SOURCE")) as f:
+            return f.read().strip() or None
+    except OSError:
+        return None
 
 
 def available():
     root = reference_root()
+    if root is None:
+        return False
     return os.path.isdir(os.path.join(root, "python", "tskit")) and any(
         f.startswith("_tskit") for f in os.listdir(os.path.join(_HERE, "_ref"))
     ) if os.path.isdir(os.path.join(_HERE, "_ref")) else False

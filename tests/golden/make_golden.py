@@ -1,8 +1,7 @@
 """Generate the golden fixtures in this directory from the reference tskit.
 
-Run in a checkout where the reference is available (it is read from
-``TSKIT_REFERENCE``, default the development checkout) after
-``make -C oracle ref``:
+Run where the reference is available (it is read from ``TSKIT_REFERENCE``,
+else from where ``make -C oracle ref`` built it) after that build:
 
     python tests/golden/make_golden.py
 

@@ -59,21 +59,14 @@ __device__ __forceinline__ void fx_add(unsigned long long *acc, double v, int32_
     }
 }
 
-// The counter's exact value rounded once to FP64.
-__device__ __forceinline__ double fx_value(const unsigned long long *acc)
+// A non-negative integer held in n 32-bit limbs (least significant first),
+// times 2^-TSG_FX_FRAC, rounded once to FP64 (round to nearest even: the
+// top 64 bits below the leading one are kept and every lower bit folds into a
+// sticky bit, which the single integer-to-double conversion then rounds
+// correctly).
+__device__ __forceinline__ double fx_round_limbs(const uint32_t *limb, int n)
 {
-    uint32_t limb[TSG_FX_LIMBS + 2];
-    unsigned long long carry = 0;
-#pragma unroll
-    for (int i = 0; i < TSG_FX_LIMBS; i++) {
-        const unsigned long long s = acc[i] + carry;
-        const unsigned long long ov = s < carry ? 1ull : 0ull;
-        limb[i] = (uint32_t) s;
-        carry = (s >> 32) + (ov << 32);
-    }
-    limb[TSG_FX_LIMBS] = (uint32_t) carry;
-    limb[TSG_FX_LIMBS + 1] = (uint32_t) (carry >> 32);
-    int top = TSG_FX_LIMBS + 1;
+    int top = n - 1;
     while (top >= 0 && limb[top] == 0) {
         top--;
     }
@@ -100,7 +93,27 @@ __device__ __forceinline__ double fx_value(const unsigned long long *acc)
     return ldexp(__ull2double_rn(m), 32 * (top - 1) - sh - TSG_FX_FRAC);
 }
 
-// The exact difference of two counters, rounded once to FP64 (signed).
+// The counter's exact value rounded once to FP64.
+__device__ __forceinline__ double fx_value(const unsigned long long *acc)
+{
+    uint32_t limb[TSG_FX_LIMBS + 2];
+    unsigned long long carry = 0;
+#pragma unroll
+    for (int i = 0; i < TSG_FX_LIMBS; i++) {
+        const unsigned long long s = acc[i] + carry;
+        const unsigned long long ov = s < carry ? 1ull : 0ull;
+        limb[i] = (uint32_t) s;
+        carry = (s >> 32) + (ov << 32);
+    }
+    limb[TSG_FX_LIMBS] = (uint32_t) carry;
+    limb[TSG_FX_LIMBS + 1] = (uint32_t) (carry >> 32);
+    return fx_round_limbs(limb, TSG_FX_LIMBS + 2);
+}
+
+// The exact difference a - b of two counters, rounded once to FP64: the
+// limb-wise differences are normalised into 32-bit limbs with a signed top
+// limb, a negative result is negated (two's complement over all limbs) and
+// the magnitude rounded as fx_value rounds.
 __device__ __forceinline__ double fx_diff_value(const unsigned long long *a,
     const unsigned long long *b)
 {
@@ -114,11 +127,21 @@ __device__ __forceinline__ double fx_diff_value(const unsigned long long *a,
         run[i] -= cy * (1ll << 32);
         run[i + 1] += cy;
     }
-    double v = 0;
-    for (int i = TSG_FX_LIMBS + 1; i >= 0; i--) {
-        v = v * 4294967296.0 + (double) run[i];
+    const bool neg = run[TSG_FX_LIMBS + 1] < 0;
+    uint32_t limb[TSG_FX_LIMBS + 2];
+    unsigned long long c = 1;
+    for (int i = 0; i < TSG_FX_LIMBS + 2; i++) {
+        const uint32_t v = (uint32_t) run[i];
+        if (neg) {
+            const unsigned long long t = (unsigned long long) (uint32_t) ~v + c;
+            limb[i] = (uint32_t) t;
+            c = t >> 32;
+        } else {
+            limb[i] = v;
+        }
     }
-    return ldexp(v, -TSG_FX_FRAC);
+    const double mag = fx_round_limbs(limb, TSG_FX_LIMBS + 2);
+    return neg ? -mag : mag;
 }
 
 }  // namespace tsg

@@ -3146,6 +3146,11 @@ int tsg_treeseq_genetic_relatedness(const tsg_treeseq_t *self, uint64_t K, const
 // loads the library, for as long as the process lives.
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[TSG_NOALLOC_SCRATCH_BYTES];
+// The device-side check word of the last no-allocation launch on this GPU,
+// copied out of the scratch array when the launch ends: a later launch of
+// another query lays the array out differently and would overwrite the
+// word's old position with its own data.
+static __device__ __align__(16) int32_t g_noalloc_err[4];
 
 namespace tsg {
 
@@ -3153,8 +3158,9 @@ namespace tsg {
 // device current (the host-side symbol is not a device address).
 static std::mutex g_noalloc_mutex;
 static void *g_noalloc_ptr[64];
+static int32_t *g_noalloc_err_ptr[64];
 
-static int noalloc_scratch(void **out)
+static int noalloc_scratch(void **out, int32_t **err_word)
 {
     int dev = 0;
     TSG_CUDA(cudaGetDevice(&dev));
@@ -3163,15 +3169,22 @@ static int noalloc_scratch(void **out)
     }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (g_noalloc_ptr[dev] == nullptr) {
-        void *p = nullptr;
+        void *p = nullptr, *pe = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) {
             set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
             return TSG_ERR_CUDA;
         }
+        e = cudaGetSymbolAddress(&pe, g_noalloc_err);
+        if (e != cudaSuccess) {
+            set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_err)");
+            return TSG_ERR_CUDA;
+        }
+        g_noalloc_err_ptr[dev] = (int32_t *) pe;
         g_noalloc_ptr[dev] = p;
     }
     *out = g_noalloc_ptr[dev];
+    *err_word = g_noalloc_err_ptr[dev];
     return 0;
 }
 
@@ -3185,7 +3198,8 @@ int tsg_query_launch_noalloc(const tsg_query_t *q, double *result_device, void *
         return TSG_ERR_NOALLOC_TOO_LARGE;
     }
     void *scratch = nullptr;
-    int ret = noalloc_scratch(&scratch);
+    int32_t *err_word = nullptr;
+    int ret = noalloc_scratch(&scratch, &err_word);
     if (ret != 0) {
         return ret;
     }
@@ -3194,20 +3208,29 @@ int tsg_query_launch_noalloc(const tsg_query_t *q, double *result_device, void *
     tsg_workspace_t ws;
     ws.ptr = scratch;
     ws.bytes = (int64_t) TSG_NOALLOC_SCRATCH_BYTES;
-    return tsg_query_launch(q, &ws, result_device, cuda_stream);
+    ret = tsg_query_launch(q, &ws, result_device, cuda_stream);
+    if (ret != 0) {
+        return ret;
+    }
+    // keep this launch's check word where tsg_noalloc_check reads it,
+    // whatever query runs next (the word sits at the tail of the layout)
+    TSG_CUDA(cudaMemcpyAsync(err_word, (const char *) scratch + q->ws_bytes - 256,
+        sizeof(int32_t), cudaMemcpyDeviceToDevice, (cudaStream_t) cuda_stream));
+    return 0;
 }
 
 int tsg_noalloc_check(const tsg_query_t *q)
 {
+    (void) q;
     void *scratch = nullptr;
-    int ret = noalloc_scratch(&scratch);
+    int32_t *err_word = nullptr;
+    int ret = noalloc_scratch(&scratch, &err_word);
     if (ret != 0) {
         return ret;
     }
-    tsg_workspace_t ws;
-    ws.ptr = scratch;
-    ws.bytes = (int64_t) TSG_NOALLOC_SCRATCH_BYTES;
-    return tsg_workspace_check(&ws, q);
+    int32_t h = 0;
+    TSG_CUDA(cudaMemcpy(&h, err_word, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return h == 0 ? 0 : TSG_ERR_DEVICE_CHECK;
 }
 
 }  // extern "C"
