@@ -89,6 +89,10 @@ def _load():
             ctypes.c_int32, P, ctypes.c_uint32, P,
         ]
         lib.orc_genotype_matrix.argtypes = [ctypes.POINTER(_TS), P]
+        lib.orc_branch_count_stat_dd.argtypes = [
+            ctypes.POINTER(_TS), ctypes.c_int32, P, P, ctypes.c_int32, P,
+            ctypes.c_int32, P, ctypes.c_uint32, P,
+        ]
         lib.orc_divergence_matrix_branch.argtypes = [ctypes.POINTER(_TS), ctypes.c_int32, P, P]
         _lib = lib
     return _lib
@@ -187,6 +191,40 @@ def sample_count_stat(ts, sample_sets, outputs, windows=None, mode="site",
         ctypes.byref(ts.struct), K, _ptr(W), _ptr(n), len(outputs),
         ctypes.cast(outs, ctypes.c_void_p), Wn, _ptr(win), opts, _ptr(res),
     )
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return res
+
+
+def branch_count_stat_dd(ts, sample_sets, outputs, windows=None, span_normalise=True,
+                         polarised=False):
+    """Branch-mode sample-count statistic from the compensated (double-double)
+    restatement of the sweep: the reference values to about 1e-16 relative,
+    for attributing FP64 disagreements.  Integer summaries only (no centred
+    relatedness) and sets below 2^15 samples.  Returns (num_windows,
+    len(outputs))."""
+    lib = _load()
+    K = len(sample_sets)
+    member = np.zeros((ts.num_samples, K), dtype=np.uint8)
+    for k, s in enumerate(sample_sets):
+        member[ts.sample_index[np.asarray(s, dtype=np.int64)], k] = 1
+    n = np.array([len(s) for s in sample_sets], dtype=np.int64)
+    outs = (_Output * len(outputs))()
+    for r, (typ, idx) in enumerate(outputs):
+        outs[r].type = typ
+        idx = list(idx) + [0] * (4 - len(idx))
+        for q in range(4):
+            outs[r].idx[q] = idx[q]
+    win = _windows(ts, windows)
+    res = np.zeros((len(win) - 1, len(outputs)))
+    opts = STAT_BRANCH
+    if span_normalise:
+        opts |= STAT_SPAN_NORMALISE
+    if polarised:
+        opts |= STAT_POLARISED
+    err = lib.orc_branch_count_stat_dd(
+        ctypes.byref(ts.struct), K, _ptr(member), _ptr(n), len(outputs),
+        ctypes.cast(outs, ctypes.c_void_p), len(win) - 1, _ptr(win), opts, _ptr(res))
     if err != 0:
         raise RuntimeError(f"oracle error {err}")
     return res

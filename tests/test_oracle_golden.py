@@ -87,3 +87,55 @@ def test_oracle_afs_parentless_stretches_vs_reference(mode):
             a = ref.allele_frequency_spectrum([list(s) for s in sets], **kw)
             b = O.allele_frequency_spectrum(ots, sets, **kw).reshape(a.shape)
             np.testing.assert_allclose(b, a, rtol=1e-12, atol=1e-15)
+
+
+_DD_METHODS = {"diversity", "segregating_sites", "Y1", "divergence", "Y2", "f2", "Y3", "f3",
+               "f4"}
+DD_CASES = [(n, c) for n, c in CASES
+            if c["method"] in _DD_METHODS and c["kwargs"].get("mode") == "branch"]
+
+
+@pytest.mark.parametrize("name,case", DD_CASES,
+                         ids=[f"{n}-{c['key']}-{c['method']}" for n, c in DD_CASES])
+def test_compensated_branch_oracle_matches_reference(name, case):
+    """The double-double restatement of the branch sweep (the attribution
+    oracle) agrees with the reference's FP64 values on every branch-mode
+    sample-count golden case."""
+    ots, data = ots_for(name)
+    expected = data[case["key"]]
+    kw = resolve(case["kwargs"], data)
+    method = case["method"]
+    sets = O._sets(ots, kw.get("sample_sets"))
+    if method in O._ONE_WAY:
+        outs = [(O._ONE_WAY[method], (k,)) for k in range(len(sets))]
+    else:
+        typ, k = O._K_WAY[method]
+        outs = [(typ, tuple(t)) for t in O._tuples(kw.get("indexes"), k, len(sets))]
+    if any(len(s) >= 1 << 15 for s in sets):
+        pytest.skip("set too large for the integer numerators")
+    got = O.branch_count_stat_dd(ots, sets, outs, windows=kw.get("windows"),
+                                 span_normalise=kw.get("span_normalise", True))
+    got = np.asarray(got).reshape(expected.shape)
+    np.testing.assert_allclose(got, expected, rtol=1e-12, atol=1e-13, equal_nan=True)
+
+
+def test_compensated_branch_oracle_vs_fp64_large():
+    """On a seeded tree sequence with thousands of trees the FP64 sweep and the
+    double-double sweep agree to well below 1e-12 normwise (the FP64 form's
+    running-sum drift is the difference)."""
+    from tskit_gb300 import sim
+
+    t = sim.simulate(200, 1e6, 3000, 5000, 17)
+    ots = O.OracleTS(t)
+    rng = np.random.default_rng(2)
+    perm = rng.permutation(t.samples())
+    sets = [np.sort(p) for p in np.array_split(perm, 4)]
+    terms = [(O.DIVERSITY, (0,)), (O.SEGSITES, (1,)), (O.DIVERGENCE, (0, 1)),
+             (O.Y3, (0, 1, 2)), (O.F4, (0, 1, 2, 3)), (O.F2, (2, 3)), (O.Y2, (1, 3)),
+             (O.Y1, (3,)), (O.F3, (0, 2, 3)), (O.RELATEDNESS_NC, (0, 3))]
+    win = np.linspace(0, t.sequence_length, 41)
+    for pol in (False, True):
+        a = O.sample_count_stat(ots, sets, terms, windows=win, mode="branch", polarised=pol)
+        b = O.branch_count_stat_dd(ots, sets, terms, windows=win, polarised=pol)
+        err = np.max(np.abs(a - b), axis=0) / np.max(np.abs(b), axis=0)
+        assert np.all(err < 1e-13), err
