@@ -304,6 +304,25 @@ int tsg_general_stat_finish(tsg_general_t *general, const double *values, double
 int64_t tsg_general_stat_result_size(const tsg_general_t *general);
 int tsg_general_stat_free(tsg_general_t *general);
 
+/* Replaces tsk_treeseq_general_stat (c/tskit/trees.h:1032-1036,
+ * c/tskit/trees.c:2035-2095) with the reference's callback form: same
+ * arguments (sample_weights host [num_samples x state_dim] in sample order,
+ * f called as f(state_dim, state, result_dim, out, f_params), a non-zero
+ * return aborting the call with that value), option bits, default mode
+ * (site), default windows (NULL: the whole genome) and errors.  f is called
+ * on the host once per state the device sweep lists (each distinct count
+ * vector when every weight is 0 or 1, else each state an item, a site allele
+ * or a leaf needs), plus at total - state for branch and node mode without
+ * TSG_STAT_POLARISED, where the reference calls it once per state change.
+ * state_dim <= 32.  result: num_windows x result_dim (x num_nodes before
+ * result_dim in node mode). */
+typedef int tsg_general_stat_func_t(uint64_t state_dim, const double *state,
+    uint64_t result_dim, double *result, void *params);
+int tsg_treeseq_general_stat(const tsg_treeseq_t *self, uint64_t state_dim,
+    const double *sample_weights, uint64_t result_dim, tsg_general_stat_func_t *f,
+    void *f_params, uint64_t num_windows, const double *windows, uint32_t options,
+    double *result);
+
 /* general_stat with real-valued weights (tsk_treeseq_general_stat,
  * c/tskit/trees.c:2035-2095, W f64 [n x K] in sample order, K <= 32): the
  * same prepare / states / finish steps, the states being the weights below

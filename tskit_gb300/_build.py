@@ -35,6 +35,7 @@ CUDA_SOURCES = [
     "tsg_kastore.cu",
     "tsg_index.cu",
     "tsg_gnn.cu",
+    "tsg_callback.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

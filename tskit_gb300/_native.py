@@ -97,6 +97,12 @@ _I64 = ctypes.c_int64
 _U32 = ctypes.c_uint32
 _ONE_WAY = [_P, _U64, _P, _P, _U64, _P, _U32, _P]
 _K_WAY = [_P, _U64, _P, _P, _U64, _P, _U64, _P, _U32, _P]
+# int f(uint64_t state_dim, const double *state, uint64_t result_dim,
+#       double *result, void *params): tsg_general_stat_func_t
+GENERAL_STAT_FUNC = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.c_void_p)
+
 SIGNATURES = {
     "tsg_treeseq_init": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(Tables_t), _I64, _U32]),
     "tsg_treeseq_free": (ctypes.c_int, [_P]),
@@ -137,6 +143,8 @@ SIGNATURES = {
     "tsg_general_stat_finish": (ctypes.c_int, [_P, _P, _P]),
     "tsg_general_stat_result_size": (ctypes.c_int64, [_P]),
     "tsg_general_stat_free": (ctypes.c_int, [_P]),
+    "tsg_treeseq_general_stat": (
+        ctypes.c_int, [_P, _U64, _P, _U64, _P, _P, _U64, _P, _U32, _P]),
     "tsg_general_weighted_prepare": (
         ctypes.c_int, [ctypes.POINTER(_P), _P, _U64, _P, _U64, _U64, _P, _U32,
                        ctypes.POINTER(_I64)]),
