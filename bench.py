@@ -5,7 +5,8 @@ L=1e8 and 100,000 breakpoints (~5 sites per breakpoint), four disjoint random
 sample sets of 2,500 and 1,000 equal windows.  One step computes diversity
 (4 sets), divergence (6 pairs), Fst (6 pairs), Tajima's D (4 sets) and Y3
 (4 triples) in both branch and site modes with span normalisation, as ONE
-fused sweep (FP32-Kahan bulk, FP64 windows).
+fused sweep at FP64 (the FP32-compensated form of the same sweep is timed
+beside it).
 
 Metric: edge-updates/s, counted as the reference runs the same queries: each
 low-level call is one traversal applying every edge insertion and removal
@@ -114,7 +115,8 @@ def finish(raw, windows, sets, pairs):
             a = (n + 1) / (3 * (n - 1) * h) - 1 / h**2
             b = 2 * (n**2 + n + 3) / (9 * n * (n - 1)) - (n + 2) / (h * n) + g / h**2
             tajd = (T - seg / h) / np.sqrt(a * seg + (b / (h**2 + g)) * seg * (seg - 1))
-        out[mode] = dict(diversity=div, divergence=dvg, Fst=fst, Tajimas_D=tajd, Y3=y3)
+        out[mode] = dict(diversity=div, divergence=dvg, Fst=fst, Tajimas_D=tajd, Y3=y3,
+                         _T=T, _S=seg)
     return out
 
 
@@ -390,56 +392,76 @@ def run_gpu(args):
 
     stream = torch.cuda.current_stream()
 
-    def prepare(ts):
+    def prepare(ts, precision):
         q = ts.query(sets, terms, windows=windows, both_modes=True, span_normalise=False,
-                     precision="f32")
+                     precision=precision)
         ws = tskit_gb300.Workspace(q.workspace_bytes)
         res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
         return q, ws, res
 
     def tuning_step(ts):
-        q, ws, res = prepare(ts)
+        q, ws, res = prepare(ts, "f64")
         return lambda: q.launch(ws, res, stream)
 
     # the span count is autotuned for this tree sequence and fused query
     ts, tuned = tune.tune_num_spans(tables, tuning_step, key=WORKLOAD, steps=3, warmup=1)
-    q, ws, res = prepare(ts)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    ev_sweep0, ev_sweep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # torch creates the CUDA events on first record; the library re-records
-    # them around the sweep kernel of every launch
-    ev_sweep0.record(stream)
-    ev_sweep1.record(stream)
-    torch.cuda.synchronize()
-    lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
 
-    for _ in range(args.warmup):
-        flush.zero_()
-        q.launch(ws, res, stream)
-    torch.cuda.synchronize()
-    q.check(ws)
-
-    step_ms, sweep_ms = [], []
-    launches0 = lib.tsg_launch_count()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            q.launch(ws, res, stream)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-            sweep_ms.append(ev_sweep0.elapsed_time(ev_sweep1))
+    def timed_fused(precision, steps, with_clocks=False):
+        """Warm-up, then `steps` launches each after an L2 flush; returns the
+        mean step and sweep-kernel times (CUDA events on the launch stream),
+        the launches per step, the (2, windows, terms) raw result and the
+        clock sampler."""
+        q, ws, res = prepare(ts, precision)
+        ev_sweep0 = torch.cuda.Event(enable_timing=True)
+        ev_sweep1 = torch.cuda.Event(enable_timing=True)
+        # torch creates the CUDA events on first record; the library
+        # re-records them around the sweep kernels of every launch
+        ev_sweep0.record(stream)
+        ev_sweep1.record(stream)
         torch.cuda.synchronize()
-    launches = (lib.tsg_launch_count() - launches0) / args.steps
-    q.check(ws)
-    ms = max_over_ranks(float(np.mean(step_ms)), world)
+        lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
+        for _ in range(args.warmup):
+            flush.zero_()
+            q.launch(ws, res, stream)
+        torch.cuda.synchronize()
+        q.check(ws)
+        step_ms, sweep_ms = [], []
+        launches0 = lib.tsg_launch_count()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if with_clocks else None
+        if sampler is not None:
+            sampler.__enter__()
+        try:
+            for _ in range(steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                q.launch(ws, res, stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                step_ms.append(e0.elapsed_time(e1))
+                sweep_ms.append(ev_sweep0.elapsed_time(ev_sweep1))
+            torch.cuda.synchronize()
+        finally:
+            if sampler is not None:
+                sampler.__exit__(None, None, None)
+        launches = (lib.tsg_launch_count() - launches0) / steps
+        q.check(ws)
+        raw = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
+        return (max_over_ranks(float(np.mean(step_ms)), world), float(np.mean(sweep_ms)),
+                launches, raw, sampler)
+
+    # the headline: one fused sweep at the reference's precision (FP64 window
+    # and running sums; summaries as exact integer numerators with about one
+    # FP64 fused multiply-add per item)
+    ms, sweep, launches, raw_batched, clocks = timed_fused("f64", args.steps, with_clocks=True)
     value = world * logical / (ms / 1e3)
-    raw_batched = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
+    # the FP32-compensated form of the same sweep
+    ms32, sweep32, _, raw_f32, _ = timed_fused("f32", max(3, min(args.steps, 10)))
 
     # plain FP64 per-query form: one launch per low-level call, FP64 throughout
     plain = []
@@ -476,20 +498,23 @@ def run_gpu(args):
         raw_plain[m] = np.concatenate([pout[(mode, "diversity")], pout[(mode, "TajD.segsites")],
                                        pout[(mode, "divergence")], pout[(mode, "Y3")]], axis=1)
 
-    # e2e through the host-pointer C ABI: host sample sets/windows in, host result out
-    flags = nat.STAT_BOTH_MODES | nat.PRECISION_F32_KAHAN
+    # e2e through the host-pointer C ABI (the headline's FP64 fused form):
+    # host sample sets/windows in, host result out
     sizes = np.array([len(s) for s in sets], dtype=np.uint64)
     flat = np.concatenate(sets).astype(np.int32)
     e2e_ms = []
+    host = None
     for j in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        host = ts._ll_terms(terms, sizes, flat, windows, None, False, False, extra=flags)
+        host = ts._ll_terms(terms, sizes, flat, windows, None, False, False,
+                            extra=nat.STAT_BOTH_MODES)
         dt = time.perf_counter() - t0
         if j >= args.warmup:
             e2e_ms.append(dt * 1e3)
-    e2e_value = world * logical / (max_over_ranks(float(np.mean(e2e_ms)), world) / 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(e2e_ms)), world)
+    e2e_value = world * logical / (e2e_ms / 1e3)
     h2d = int(sizes.nbytes + flat.nbytes + windows.nbytes + ts.num_samples * 4)
     d2h = int(host.nbytes)
 
@@ -499,7 +524,6 @@ def run_gpu(args):
         return
 
     peaks, peak_kind = measured_peaks()
-    sweep = float(np.mean(sweep_ms))
     algo = algorithmic_bytes(tables, sets, len(terms))
     achieved = algo / (sweep / 1e3) / 1e9
     line = {
@@ -513,19 +537,27 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32-kahan bulk, f64 windows; int32 counts",
+        "dtype": "f64 (window and running sums FP64; summaries as exact integer numerators, "
+                 "about one FP64 FMA per item); int32 counts",
         "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
         "config": dict(workload_config(tables), num_spans=tuned["num_spans"],
                        span_tuning_ms={str(k): v for k, v in tuned["ms"].items()}),
         "queries_per_s": world * traversals / (ms / 1e3),
         "physical_edge_updates_per_s": world * events / (ms / 1e3),
+        "batched_f32_kahan": {
+            "ms_per_step": ms32,
+            "value": world * logical / (ms32 / 1e3),
+            "kernel_ms": sweep32,
+            "dtype": "f32 summaries with exact products and compensated sums; f64 windows",
+        },
         "plain_fp64": {
             "ms_per_step": plain_step_ms,
             "value": world * logical / (plain_step_ms / 1e3),
             "launches": len(plain),
             "speedup_batched_vs_plain": plain_step_ms / ms,
+            "speedup_batched_f32_vs_plain": plain_step_ms / ms32,
         },
-        "e2e": {"value": e2e_value, "unit": "edge-updates/s", "ms_per_step": float(np.mean(e2e_ms)),
+        "e2e": {"value": e2e_value, "unit": "edge-updates/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {
             "bound": "hbm",
@@ -534,10 +566,8 @@ def run_gpu(args):
             "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"],
             "traffic": profile_traffic(),
-            "kernel": "sweep pipeline (k_node_mask, k_replay_items with item values, "
-                      "k_span_windows, k_leaf_areas, k_leaf_prefix, k_leaf_terms, k_site_eval, "
-                      "k_site_windows, k_span_scan, k_window_reduce), timed between events on "
-                      "the launch stream",
+            "kernel": "sweep pipeline (every kernel of one fused launch from the node masks "
+                      "to the window reduction), timed between events on the launch stream",
             "algorithmic_bytes_per_launch": algo,
             "kernel_ms": sweep,
             "peak_source": peak_kind,
@@ -545,7 +575,6 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
-    # error of the batched FP32-Kahan form and of the plain FP64 form
     if not args.no_cpu_baseline:
         cpu_s, raw_oracle, ncalls = cpu_oracle_run(tables, sets, windows, pairs, triples)
         line["cpu_baseline"] = {
@@ -553,18 +582,108 @@ def run_gpu(args):
             "sample": f"the full workload: {ncalls} single-stat traversals of the C oracle "
                       "(restated reference algorithm), one core",
         }
-        fin_b, fin_p, fin_o = (finish(r, windows, sets, pairs)
-                               for r in (raw_batched, raw_plain, raw_oracle))
-        err = {}
-        for mode in MODES:
-            for stat in fin_o[mode]:
-                err[f"{mode}.{stat}.batched_f32k"] = rel_err(fin_b[mode][stat], fin_o[mode][stat])
-                err[f"{mode}.{stat}.plain_f64"] = rel_err(fin_p[mode][stat], fin_o[mode][stat])
-        line["error_vs_fp64_oracle"] = err
+        raw_dd = compensated_branch(tables, sets, windows, terms)
+        line["error"] = error_report(
+            {"batched_f64": raw_batched, "batched_f32k": raw_f32, "plain_f64": raw_plain,
+             "e2e_f64": host.reshape(raw_batched.shape), "oracle_f64": raw_oracle},
+            raw_oracle, raw_dd, windows, sets, pairs)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.barrier()
 
+
+def compensated_branch(tables, sets, windows, terms):
+    """Branch-mode raw terms (not span-normalised) from the oracle's
+    double-double restatement of the sweep."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    ots = O.OracleTS(tables)
+    return O.branch_count_stat_dd(ots, sets, terms, windows=windows, span_normalise=False)
+
+
+# Stated error bounds of the two arithmetic forms (normwise, conditioning
+# scaled, see error_report): the FP64 form against the compensated oracle
+# (branch) or the FP64 oracle (site, whose GPU sums are exact integers rounded
+# once); the FP32-compensated form against the same.
+ERROR_BOUNDS = {"f64": 1e-12, "f32k": 1e-5}
+
+
+def error_report(forms, raw_oracle, raw_dd, windows, sets, pairs):
+    """Errors of each form's statistics (raw terms and derived) against the
+    FP64 oracle and, in branch mode, against the compensated oracle, with the
+    stated bounds and every bound exceeded."""
+    fin_o = finish(raw_oracle, windows, sets, pairs)
+    dd = raw_oracle.copy()
+    dd[0] = raw_dd
+    fin_dd = finish(dd, windows, sets, pairs)
+    out = {"vs_fp64_oracle": {}, "vs_compensated_oracle": {}, "bounds": ERROR_BOUNDS,
+           "measure": "normwise per statistic column: max over windows of |error| / max over "
+                      "windows of the statistic's componentwise condition scale in its raw "
+                      "terms (|value| for raw terms; sum |d stat / d term| |term| for Fst and "
+                      "Tajima's D), worst column",
+           "exceeded": []}
+    for name, raw in forms.items():
+        fin = finish(raw, windows, sets, pairs)
+        bound = ERROR_BOUNDS.get(name.split("_")[-1])
+        for mode in MODES:
+            for stat in fin_o[mode]:
+                if stat.startswith("_"):
+                    continue
+                e = None
+                if name != "oracle_f64":
+                    e = cond_err(fin[mode], fin_o[mode], stat, pairs, sets)
+                    out["vs_fp64_oracle"][f"{mode}.{stat}.{name}"] = e
+                if mode == "branch":
+                    e = cond_err(fin[mode], fin_dd[mode], stat, pairs, sets)
+                    out["vs_compensated_oracle"][f"{mode}.{stat}.{name}"] = e
+                if name != "oracle_f64" and bound is not None and not (e <= bound):
+                    out["exceeded"].append(f"{mode}.{stat}.{name}")
+    return out
+
+
+def cond_scale(fin, stat, pairs, sets):
+    """Componentwise condition scale of each window value of a statistic in
+    the raw (span-normalised) terms it is computed from."""
+    if stat == "Fst":
+        div, dvg = fin["diversity"], fin["divergence"]
+        out = np.zeros_like(dvg)
+        for i, (u, v) in enumerate(pairs):
+            a = np.abs(div[:, u]) + np.abs(div[:, v])
+            b = div[:, u] + div[:, v] + 2 * dvg[:, i]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                out[:, i] = 8 * np.abs(dvg[:, i]) * a / b ** 2
+        return out
+    if stat == "Tajimas_D":
+        T, S = fin["_T"], fin["_S"]
+        n = np.array([len(s) for s in sets], dtype=np.float64)
+        h = np.array([np.sum(1 / np.arange(1, nn)) for nn in n])
+        g = np.array([np.sum(1 / np.arange(1, nn) ** 2) for nn in n])
+        a = (n + 1) / (3 * (n - 1) * h) - 1 / h**2
+        b = 2 * (n**2 + n + 3) / (9 * n * (n - 1)) - (n + 2) / (h * n) + g / h**2
+        c = b / (h**2 + g)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            V = a * S + c * S * (S - 1)
+            dT = 1 / np.sqrt(V)
+            dS = -1 / (h * np.sqrt(V)) - (T - S / h) * (a + c * (2 * S - 1)) / (2 * V ** 1.5)
+            return np.abs(dT * T) + np.abs(dS * S)
+    return np.abs(fin[stat])
+
+
+def cond_err(fin, ref, stat, pairs, sets):
+    """Normwise error of one statistic, scaled by its condition (see
+    cond_scale); equal infinities and NaNs count as agreement."""
+    got, exp = np.asarray(fin[stat], dtype=np.float64), np.asarray(ref[stat], dtype=np.float64)
+    if got.size == 0:
+        return 0.0
+    scale = cond_scale(ref, stat, pairs, sets)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        both_inf = np.isinf(got) & np.isinf(exp) & (np.sign(got) == np.sign(exp))
+        diff = np.where(both_inf | (np.isnan(got) & np.isnan(exp)), 0.0, np.abs(got - exp))
+        num = np.nanmax(np.where(np.isfinite(scale), diff, 0.0), axis=0)
+        den = np.nanmax(np.where(np.isfinite(scale), scale, 0.0), axis=0)
+        e = np.where(den > 0, num / den, num)
+    return float(np.nanmax(e))
 
 
 # ------------------------------------------------------- other configurations

@@ -157,6 +157,16 @@ int tsg_treeseq_free(tsg_treeseq_t *ts);
 int64_t tsg_treeseq_get_num_trees(const tsg_treeseq_t *ts);
 int64_t tsg_treeseq_get_num_samples(const tsg_treeseq_t *ts);
 int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts);
+/* The compact replay plan behind the sample-count statistics (no reference
+ * counterpart): short spans whose node state holds only the nodes their
+ * edge events touch, for tree sequences of up to 65,535 samples.  get: its
+ * span count (0 when the tree sequence uses the general replay).  set:
+ * rebuild it with about num_spans spans (0: use the general replay; a count
+ * whose spans touch more than 4,096 nodes also leaves the general replay
+ * serving); queries prepared before must not run concurrently with it.
+ * Results do not depend on the span count. */
+int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts);
+int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans);
 /* breakpoints: host array of num_trees + 1 doubles */
 int tsg_treeseq_get_breakpoints(const tsg_treeseq_t *ts, double *breakpoints);
 const char *tsg_strerror(int err);

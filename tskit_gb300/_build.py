@@ -36,6 +36,7 @@ CUDA_SOURCES = [
     "tsg_index.cu",
     "tsg_gnn.cu",
     "tsg_callback.cu",
+    "tsg_cplan.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

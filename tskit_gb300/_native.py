@@ -109,6 +109,8 @@ SIGNATURES = {
     "tsg_treeseq_get_num_trees": (_I64, [_P]),
     "tsg_treeseq_get_num_samples": (_I64, [_P]),
     "tsg_treeseq_get_num_spans": (_I64, [_P]),
+    "tsg_treeseq_get_num_compact_spans": (_I64, [_P]),
+    "tsg_treeseq_set_compact_spans": (ctypes.c_int, [_P, _I64]),
     "tsg_treeseq_get_breakpoints": (ctypes.c_int, [_P, _P]),
     "tsg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "tsg_treeseq_diversity": (ctypes.c_int, _ONE_WAY),

@@ -2,8 +2,9 @@
 // item evaluation for every count form, its launcher and its kernel handle.
 // Included by a translation unit that defines TSG_EVAL_F (float or double),
 // TSG_EVAL_UNPOL (true or false), TSG_EVAL_NAME (the launcher's name) and
-// TSG_EVAL_FN (the handle's name), so that the instantiations compile in
-// parallel.
+// TSG_EVAL_FN (the handle's name), and TSG_CHUNKS_NAME (the launcher of the
+// chunk evaluation after the compact replay), so that the instantiations
+// compile in parallel.
 #include "tsg_replay_kernel.cuh"
 
 namespace tsg {
@@ -37,6 +38,16 @@ TSG_REPLAY_EVAL_LAUNCHER(TSG_EVAL_NAME)
             k_replay_items<32, 2, int32_t, TSG_EVAL_F, TSG_EVAL_UNPOL, true>
                 <<<grid, 512, 0, st>>>(v, p, d, w, slot_bytes);
             break;
+    }
+}
+
+TSG_CHUNK_EVAL_LAUNCHER(TSG_CHUNKS_NAME)
+{
+    const unsigned grid = (unsigned) std::min<int64_t>((v.num_chunks + 7) / 8, 1 << 20);
+    if (kq == 1) {
+        k_eval_chunks<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<grid, 256, 0, st>>>(v, p, w);
+    } else {
+        k_eval_chunks<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<grid, 256, 0, st>>>(v, p, w);
     }
 }
 

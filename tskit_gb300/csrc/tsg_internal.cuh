@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -139,7 +140,30 @@ struct TSView {
     const double *ins_right;      // insertion order: edge right
     const double *ins_lu;         // insertion order: the child's last update before the
                                   // insertion (null when always the insertion position)
+    // compact replay plan (tsg_cplan.cu; c_num_spans 0 when the tree sequence
+    // has none): short spans whose node state holds only the nodes their
+    // transitions touch and their mutations' nodes
+    int64_t c_num_spans;
+    int64_t c_max_local;          // largest compact node set of a span
+    const int32_t *c_span_tree;   // c_num_spans + 1
+    const int64_t *c_local_off;   // c_num_spans + 2: node sets (the last: the anchors)
+    const double *c_time;         // node times, by local id
+    const uint16_t *c_par0;       // parent at the span start (local id; 0x7FFF: none)
+    const int64_t *c_ep_off;      // c_num_spans + 1
+    const int2 *c_ep;             // sample-range endpoints (position, local << 1 | is_end)
+    const uint16_t *c_order;      // c_num_spans x num_samples: sample indexes, depth-first
+    const int2 *c_ins_enc;        // insertion order: (parent, child), compact encoding
+    const int2 *c_rem_enc;        // removal order: (parent, child), compact encoding
+    const int32_t *c_mut_enc;     // per mutation: compact encoding of its node
+    const int32_t *c_chunk_span;  // per chunk: the numbering of its items
+    int64_t c_num_anchors;        // the first tree's items
+    const int32_t *c_anchor_par;  // their parents (anchor ids)
+    const int2 *c_anchor_range;   // their sample ranges in the first span's order
 };
+
+// largest compact node set a span may have (its node state is in shared
+// memory); a tree sequence whose plan exceeds it uses the general replay
+#define TSG_COMPACT_MAX_LOCAL 4096
 
 // items per evaluation chunk (one warp)
 #define TSG_ITEM_CHUNK 256
@@ -176,6 +200,8 @@ int device_count_sms();
 struct tsg_treeseq;
 namespace tsg {
 int build_span_plan(tsg_treeseq *ts, const HostTopology &h, int64_t num_spans);
+int build_compact_plan(tsg_treeseq *ts, const HostTopology &h, int64_t num_spans);
+int64_t compact_default_spans(int64_t T, int64_t events, int64_t n);
 }
 
 // Opaque handle definitions.
@@ -192,9 +218,12 @@ struct tsg_treeseq {
     std::vector<double> h_site_position;
     int64_t max_alive;
     int64_t max_children = 0;  // most children of a node in any span's seek tree
+    int64_t h_tree_item0 = 0;  // the first tree's items
+    std::vector<int64_t> h_tree_chunk_off;  // num_trees + 1: first chunk of each tree
     tsg::HostTopology host;    // host copy of the topology (span plan, genotype decoding)
     // device allocations owned by this object
     std::vector<void *> owned;
+    std::vector<void *> compact_owned;  // the compact plan's (rebuilt on demand)
     // state of the synchronous (host-pointer) entry points
     std::mutex sync_mutex;
     tsg_workspace *sync_ws = nullptr;
@@ -207,3 +236,20 @@ struct tsg_workspace {
     void *ptr;
     int64_t bytes;
 };
+
+namespace tsg {
+// Upload a host vector into a device allocation recorded in `owner`.
+template <typename T>
+int upload_host_vec(std::vector<void *> &owner, const std::vector<T> &h, T **out)
+{
+    void *d = nullptr;
+    const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    TSG_CUDA(cudaMalloc(&d, bytes));
+    owner.push_back(d);
+    if (!h.empty()) {
+        TSG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    *out = (T *) d;
+    return 0;
+}
+}  // namespace tsg

@@ -544,6 +544,8 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     ts->v.num_items = tree_item_off[(size_t) T];
     ts->max_alive = max_alive;
     ts->h_local_off = local_off;
+    ts->h_tree_item0 = T > 0 ? tree_items[0] : 0;
+    ts->h_tree_chunk_off = tree_chunk_off;
     return 0;
 }
 

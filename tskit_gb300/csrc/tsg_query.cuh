@@ -67,6 +67,8 @@ struct WsDev {
     unsigned long long *leaf_area;  // 3 x windows x 2^K patterns: leaf branch areas (fixed point)
     double *leaf_dbl;     // windows x 2^K patterns: the areas
     double *leaf_win;     // windows * R: the leaves' part of the branch sums
+    uint64_t *cp0;        // (samples + 1) x 2: prefix sums along the first span's order
+                          // (compact replay)
     int32_t *err;
     int32_t *counter;
 };
@@ -208,6 +210,14 @@ TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_pol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_unpol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_pol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_unpol);
+// Every chunk's item values after the compact replay (kq: count words per
+// node, 1 or 2).
+#define TSG_CHUNK_EVAL_LAUNCHER(name)                                                    \
+    void name(int kq, cudaStream_t st, const TSView &v, const QueryParams &p, const WsDev &w)
+TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f32_pol);
+TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f32_unpol);
+TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f64_pol);
+TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f64_unpol);
 
 }  // namespace tsg
 

@@ -1,0 +1,239 @@
+// The compact replay: the item pipeline's replay over the compact span plan
+// (tsg_cplan.cu).  One block of TSG_COMPACT_THREADS threads per span at a
+// time, the span's node state (16-bit counts packed in 64-bit words and
+// 16-bit parent entries) in shared memory: a few kilobytes, so many blocks
+// -- and many sequential replays -- run on every SM.
+//
+//   seek     both warps: the prefix sum of the sample-set bits along the
+//            span's depth-first sample order, 64 samples per step (warp
+//            shuffles and the warp totals), and at each sorted range endpoint
+//            a node's count: P[hi] - P[lo] (the start is stored first, the
+//            end then subtracts it);
+//   replay   warp 0: replay_span over the compact encodings.
+//
+// The first tree's items (its stateful nodes, the anchors) are written by
+// k_compact_anchors from the prefix sum of the first span's order
+// (k_compact_prefix) before the replay starts, and k_eval_chunks values every
+// chunk of items after it, all chunks in parallel.
+#pragma once
+
+#include "tsg_replay_kernel.cuh"
+
+namespace tsg {
+
+#define TSG_COMPACT_THREADS 64
+
+// Counts of span s's compact nodes at the span start into sp.xq.  s_pre:
+// (TSG_COMPACT_THREADS + 1) x 2 words; s_wsum: 2 words per warp.  Ends with
+// the block synchronised.
+template <int KQ>
+__device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &qd, int K, int s,
+    const SpanState<uint16_t> &sp, uint64_t *s_pre, uint64_t *s_wsum)
+{
+    const int64_t n = ts.num_samples;
+    const uint16_t *order = ts.c_order + (int64_t) s * n;
+    const int2 *ep = ts.c_ep + ts.c_ep_off[s];
+    const int64_t nep = ts.c_ep_off[s + 1] - ts.c_ep_off[s];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    constexpr int NW = TSG_COMPACT_THREADS / 32;
+    uint64_t run_lo = 0, run_hi = 0;
+    int64_t cur = 0;
+    for (int64_t base = 0; base < n; base += TSG_COMPACT_THREADS) {
+        const int64_t i = base + tid;
+        Pack v{0, 0};
+        if (i < n) {
+            v = pk_from_mask<16>(qd.sample_mask[order[i]], K);
+        }
+        // inclusive scan within the warp (fields never carry: prefix counts
+        // stay within the set sizes)
+        uint64_t inc_lo = v.lo, inc_hi = v.hi;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
+            const uint64_t b = KQ > 1 ? __shfl_up_sync(0xffffffffu, inc_hi, o) : 0ull;
+            if (lane >= o) {
+                inc_lo += a;
+                inc_hi += b;
+            }
+        }
+        if (lane == 31) {
+            s_wsum[2 * wid] = inc_lo;
+            s_wsum[2 * wid + 1] = inc_hi;
+        }
+        __syncthreads();
+        uint64_t wp_lo = 0, wp_hi = 0, tot_lo = 0, tot_hi = 0;
+#pragma unroll
+        for (int j = 0; j < NW; j++) {
+            const uint64_t a = s_wsum[2 * j], b = s_wsum[2 * j + 1];
+            if (j < wid) {
+                wp_lo += a;
+                wp_hi += b;
+            }
+            tot_lo += a;
+            tot_hi += b;
+        }
+        // P at position i (the samples before it)
+        s_pre[2 * tid] = run_lo + wp_lo + inc_lo - v.lo;
+        s_pre[2 * tid + 1] = run_hi + wp_hi + inc_hi - v.hi;
+        if (tid == 0) {
+            s_pre[2 * TSG_COMPACT_THREADS] = run_lo + tot_lo;
+            s_pre[2 * TSG_COMPACT_THREADS + 1] = run_hi + tot_hi;
+        }
+        __syncthreads();
+        // every endpoint at a position up to base + TSG_COMPACT_THREADS (the
+        // sorted list's next entries; earlier positions were taken by
+        // earlier steps)
+        const int64_t lim = base + TSG_COMPACT_THREADS;
+        for (;;) {
+            const int64_t j = cur + tid;
+            int2 e = make_int2(0, 0);
+            bool mine = false;
+            if (j < nep) {
+                e = ep[j];
+                mine = e.x <= lim;
+            }
+            const int cnt = __syncthreads_count(mine);
+            const int64_t l = e.y >> 1;
+            const int at = (int) (e.x - base);
+            if (mine && !(e.y & 1)) {
+                sp.xq[l * KQ] = s_pre[2 * at];
+                if (KQ > 1) {
+                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = s_pre[2 * at + 1];
+                }
+            }
+            __syncthreads();
+            if (mine && (e.y & 1)) {
+                sp.xq[l * KQ] = s_pre[2 * at] - sp.xq[l * KQ];
+                if (KQ > 1) {
+                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] =
+                        s_pre[2 * at + 1] - sp.xq[l * KQ + (KQ > 1 ? 1 : 0)];
+                }
+            }
+            cur += cnt;
+            if (cnt < TSG_COMPACT_THREADS) {
+                break;
+            }
+            __syncthreads();
+        }
+        run_lo = s_pre[2 * TSG_COMPACT_THREADS];
+        run_hi = s_pre[2 * TSG_COMPACT_THREADS + 1];
+        __syncthreads();
+    }
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView ts, QueryParams q,
+    QueryDev qd, WsDev w)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_span;
+    __shared__ TouchEntry<KQ> s_list[TSG_TOUCH_CAP];  // the open touch list
+    __shared__ ReplayStage s_stage[4];                 // prefetch ring, trees t .. t + 3
+    __shared__ uint64_t s_pre[2 * (TSG_COMPACT_THREADS + 1)];
+    __shared__ uint64_t s_wsum[2 * (TSG_COMPACT_THREADS / 32)];
+    SpanState<uint16_t> sp = span_state_at<uint16_t>(smem_raw, ts.c_max_local, KQ);
+    sp.cnt = nullptr;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_span = atomicAdd(w.counter, 1);
+        }
+        __syncthreads();
+        const int s = s_span;
+        __syncthreads();
+        if (s >= ts.c_num_spans) {
+            break;
+        }
+        const int32_t t0 = ts.c_span_tree[s], t1 = ts.c_span_tree[s + 1];
+        const int64_t lo = ts.c_local_off[s];
+        const int32_t Ls = (int32_t) (ts.c_local_off[s + 1] - lo);
+        sp.time = ts.c_time + lo;
+        // parents at the span start (0x7FFF, no parent, is the replay's
+        // "no parent" entry)
+        for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
+            sp.par[l] = ts.c_par0[lo + l];
+        }
+        compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum);
+        if (threadIdx.x < 32) {
+            replay_span<16, KQ, uint16_t, false>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
+                t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
+        }
+        __syncthreads();
+    }
+}
+
+// Prefix sums of the sample-set bits along the first span's sample order,
+// P0[i] for i = 0 .. n (two words each), in one block of 1024 threads.
+template <int KQ>
+__global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams q, QueryDev qd,
+    uint64_t *P0)
+{
+    __shared__ uint64_t s_w[2 * 32];
+    const int64_t n = ts.num_samples;
+    const uint16_t *order = ts.c_order;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int nw = (int) (blockDim.x >> 5);
+    uint64_t run_lo = 0, run_hi = 0;
+    for (int64_t base = 0; base < n; base += blockDim.x) {
+        const int64_t i = base + tid;
+        Pack v{0, 0};
+        if (i < n) {
+            v = pk_from_mask<16>(qd.sample_mask[order[i]], q.K);
+        }
+        uint64_t inc_lo = v.lo, inc_hi = v.hi;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
+            const uint64_t b = __shfl_up_sync(0xffffffffu, inc_hi, o);
+            if (lane >= o) {
+                inc_lo += a;
+                inc_hi += b;
+            }
+        }
+        if (lane == 31) {
+            s_w[2 * wid] = inc_lo;
+            s_w[2 * wid + 1] = inc_hi;
+        }
+        __syncthreads();
+        uint64_t wp_lo = 0, wp_hi = 0, tot_lo = 0, tot_hi = 0;
+        for (int j = 0; j < nw; j++) {
+            const uint64_t a = s_w[2 * j], b = s_w[2 * j + 1];
+            if (j < wid) {
+                wp_lo += a;
+                wp_hi += b;
+            }
+            tot_lo += a;
+            tot_hi += b;
+        }
+        if (i < n) {
+            P0[2 * i] = run_lo + wp_lo + inc_lo - v.lo;
+            P0[2 * i + 1] = run_hi + wp_hi + inc_hi - v.hi;
+        }
+        run_lo += tot_lo;
+        run_hi += tot_hi;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        P0[2 * n] = run_lo;
+        P0[2 * n + 1] = run_hi;
+    }
+}
+
+// The first tree's items: one per anchor (a stateful node alive in the first
+// tree, in edge order) with its counts, P0[hi] - P0[lo], and its parent, in
+// the anchors' numbering.
+template <int KQ>
+__global__ void k_compact_anchors(TSView ts, const uint64_t *P0, WsDev w)
+{
+    Item<KQ> *items = (Item<KQ> *) w.items;
+    const int64_t base = ts.tree_item_off[0];
+    for (int64_t k = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; k < ts.c_num_anchors;
+         k += (int64_t) gridDim.x * blockDim.x) {
+        const int2 r = ts.c_anchor_range[k];
+        Pack x;
+        x.lo = P0[2 * r.y] - P0[2 * r.x];
+        x.hi = P0[2 * r.y + 1] - P0[2 * r.x + 1];
+        item_put<KQ>(items + base + k, Pack{0, 0}, x, (int32_t) k, -1, ts.c_anchor_par[k]);
+    }
+}
+
+}  // namespace tsg

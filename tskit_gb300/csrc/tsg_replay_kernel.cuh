@@ -16,13 +16,369 @@ namespace tsg {
 // bound of an evaluating warp's wait for one tree (with 128 ns sleeps: far
 // longer than any span's replay); past it the kernel records an error
 #define TSG_REPLAY_SPIN_LIMIT (1u << 27)
-// terms per pass of the evaluating warps over a chunk's items: one term at a
-// time keeps their code small (they share the SM's instruction cache with
-// the latency-bound replay warp) and their registers within the replay's
-// launch bounds
-#define TSG_FUSED_EVAL_GROUP 1
 // the replay publishes its progress every few trees (a fence each time)
 #define TSG_PUBLISH_EVERY 8
+
+// The edge events of the transitions a span replays, and its mutations, in
+// the span's node encoding (local ids of stateful nodes, -(global + 1) of
+// leaves): the general plan's or the compact plan's.
+struct ReplayEnc {
+    const int2 *rem;
+    const int2 *ins;
+    const int32_t *mut;
+};
+
+// The sequential replay of one span by warp 0 of the block, integer only,
+// in reference order (c/tskit/trees.c:1424-1507), from the state at the span
+// start in `sp` (parents in the replay's encoding): the transitions into the
+// span's trees after the first and, for branch items, into the next span's
+// first tree; one item per stateful node a transition touches (its counts
+// and parent before the first touch and after the transition); the counts
+// under every mutation of the span's trees for site statistics.  With EVAL
+// the replay publishes its completed trees in *s_ready every few trees.
+template <int W, int KQ, typename IdxT, bool EVAL>
+__device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams &q,
+    const QueryDev &qd, const WsDev &w, const SpanState<IdxT> &sp, TouchEntry<KQ> *s_list,
+    ReplayStage *s_stage, int *s_ready, int32_t t0, int32_t t1, int32_t Ls, const ReplayEnc code)
+{
+    constexpr uint32_t PFLAG = sizeof(IdxT) == 2 ? 0x8000u : 0x80000000u;
+    constexpr uint32_t PMASK = PFLAG - 1u;
+    constexpr uint32_t TSG_NO_PARENT = PMASK;
+    constexpr uint32_t NO_NODE = 0xffffffffu;
+    const int K = q.K;
+    const int lane = threadIdx.x & 31;
+    Item<KQ> *items = (Item<KQ> *) w.items;
+    int64_t cursor = 0;  // first item of the open list
+    int64_t climit = 0;  // end of the transition's items in the plan
+    int32_t nopen = 0;   // nodes in the open list
+    auto close_list = [&]() {
+        __syncwarp();
+        for (int32_t i = lane; i < nopen; i += 32) {
+            const TouchEntry<KQ> en = s_list[i];
+            const uint32_t pu = (uint32_t) sp.par[en.u] & PMASK;
+            if (cursor + i < climit) {
+                item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
+                    st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
+                    pu != TSG_NO_PARENT ? (int32_t) pu : -1);
+            }
+            sp.par[en.u] = (IdxT) pu;  // clears the touch flag
+        }
+        __syncwarp();
+        cursor += nopen;
+        nopen = 0;
+    };
+    // Lanes with `active` set touch node u (distinct per lane) whose
+    // counts are still x0 and whose parent entry (flag and parent) is
+    // praw, read after the previous batch's touches; returns the
+    // entry with the flag set, which the caller stores (with the
+    // node's new parent, for an edge's child).  A node is touched at
+    // most once per edge event and every event ends with __syncwarp.
+    auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw) {
+        bool fresh = active && !(praw & PFLAG);
+        unsigned m = __ballot_sync(0xffffffffu, fresh);
+        if (nopen + __popc(m) > TSG_TOUCH_CAP) {
+            close_list();
+            fresh = active;
+            m = __ballot_sync(0xffffffffu, fresh);
+        }
+        if (fresh) {
+            const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
+            const uint32_t p0 = praw & PMASK;
+            TouchEntry<KQ> en;
+            en.x0[0] = x0.lo;
+            if (KQ > 1) {
+                en.x0[KQ > 1 ? 1 : 0] = x0.hi;
+            }
+            en.u = u;
+            en.p0 = p0 != TSG_NO_PARENT ? (int32_t) p0 : -1;
+            s_list[at] = en;
+            if (cursor + at >= climit) {
+                dev_error(w.err, DEV_ITEM_PLAN);
+            }
+        }
+        nopen += __popc(m);
+        return (praw & PMASK) | PFLAG;
+    };
+    // the next (up to) 32 - first nodes of a root path from v, lane
+    // first + j taking the j-th with its parent entry; advances v
+    // past them
+    auto chase = [&](uint32_t &v, uint32_t &mine, uint32_t &mraw, int first) {
+        mine = NO_NODE;
+        mraw = 0;
+#pragma unroll 4
+        for (int j = first; j < 32; j++) {
+            if (v == TSG_NO_PARENT) {
+                break;
+            }
+            const uint32_t raw = (uint32_t) sp.par[v];
+            mine = lane == j ? v : mine;
+            mraw = lane == j ? raw : mraw;
+            v = raw & PMASK;
+        }
+    };
+    // One edge event; cm: membership bits of a leaf child (whose
+    // branch is accounted per edge, k_leaf_areas).  The nodes are
+    // touched in batches of 32 lanes: a stateful child on lane 0
+    // with the first 31 nodes of the parent's root path (the child is
+    // not on it), then 32 path nodes at a time -- one touch-list
+    // step per batch (the span plan counts items with the same
+    // batches).  The child keeps its counts and takes its new parent;
+    // the path nodes add or remove the child's counts.
+    auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
+        uint32_t v = (uint32_t) p, mine, mraw;
+        const bool child = c >= 0;
+        chase(v, mine, mraw, child ? 1 : 0);
+        const Pack xc = child ? st_load(sp, c) : pk_from_mask<W>(cm, K);
+        bool is_child = false;
+        if (child && lane == 0) {
+            mine = (uint32_t) c;
+            mraw = (uint32_t) sp.par[c];
+            is_child = true;
+        }
+        const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
+        for (int32_t batches = 1;; batches++) {
+            const bool act = mine != NO_NODE;
+            Pack xo{0, 0};
+            if (act) {
+                xo = is_child ? xc : st_load(sp, (int64_t) mine);
+            }
+            if (q.branch) {
+                const uint32_t f = touch(act, mine, xo, mraw);
+                if (act) {
+                    sp.par[mine] = (IdxT) (is_child ? (np | PFLAG) : f);
+                }
+            } else if (is_child) {
+                sp.par[mine] = (IdxT) np;
+            }
+            if (act && !is_child) {
+                Pack xn;
+                if (sign > 0) {
+                    xn.lo = xo.lo + xc.lo;
+                    xn.hi = xo.hi + xc.hi;
+                } else {
+                    xn.lo = xo.lo - xc.lo;
+                    xn.hi = xo.hi - xc.hi;
+                }
+                pk_store(sp, (int64_t) mine, xn);
+            }
+            if (v == TSG_NO_PARENT) {
+                break;
+            }
+            // a root path has at most Ls nodes: more means a cycle
+            if (batches > (Ls >> 5) + 1) {
+                dev_error(w.err, DEV_PATH_TOO_LONG);
+                break;
+            }
+            chase(v, mine, mraw, 0);
+            is_child = false;
+        }
+        __syncwarp();
+    };
+    const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;
+    const bool site = q.site;
+    // Prefetch ring: tree t's inputs are staged in three dependent
+    // steps -- (a) its event, mutation and item ranges, (b) its event
+    // and mutation encodings, (c) the masks of its leaf children and
+    // leaf mutation nodes -- issued three, two and one trees ahead.
+    auto stage_a = [&](int32_t t) {
+        ReplayStage &S = s_stage[t & 3];
+        if (lane == 0) {
+            cp_async16(&S.ev, &ts.tree_ev[t]);
+        } else if (lane == 1) {
+            cp_async8(&S.mr, &ts.tree_mut[t]);
+        } else if (lane == 2) {
+            cp_async8(&S.ioff[0], &ts.tree_item_off[t]);
+        } else if (lane == 3) {
+            cp_async8(&S.ioff[1], &ts.tree_item_off[t + 1]);
+        }
+    };
+    auto stage_b = [&](int32_t t) {
+        ReplayStage &S = s_stage[t & 3];
+        const int4 ev = S.ev;
+        if (t > t0 && lane < ev.y + ev.w) {
+            cp_async8(&S.pc[lane], lane < ev.y ? (const void *) &code.rem[ev.x + lane]
+                                               : (const void *) &code.ins[ev.z + lane - ev.y]);
+        }
+        if (site && t < t1 && lane < S.mr.y - S.mr.x) {
+            cp_async4(&S.menc[lane], &code.mut[S.mr.x + lane]);
+        }
+    };
+    auto stage_c = [&](int32_t t) {
+        ReplayStage &S = s_stage[t & 3];
+        const int4 ev = S.ev;
+        if (t > t0 && lane < ev.y + ev.w && S.pc[lane].y < 0) {
+            cp_async4(&S.cm[lane], &qd.node_mask[-S.pc[lane].y - 1]);
+        }
+        if (site && t < t1 && lane < S.mr.y - S.mr.x && S.menc[lane] < 0) {
+            cp_async4(&S.mmask[lane], &qd.node_mask[-S.menc[lane] - 1]);
+        }
+    };
+    for (int32_t k = 0; k < 3; k++) {
+        if (t0 + k < tend) {
+            stage_a(t0 + k);
+        }
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    for (int32_t k = 0; k < 2; k++) {
+        if (t0 + k < tend) {
+            stage_b(t0 + k);
+        }
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    if (t0 < tend) {
+        stage_c(t0);
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    for (int32_t t = t0; t < tend; t++) {
+        if (t + 3 < tend) {
+            stage_a(t + 3);
+        }
+        if (t + 2 < tend) {
+            stage_b(t + 2);
+        }
+        if (t + 1 < tend) {
+            stage_c(t + 1);
+        }
+        cp_async_commit();
+        const ReplayStage &S = s_stage[t & 3];
+        if (t > t0) {
+            cursor = S.ioff[0];
+            climit = S.ioff[1];
+            const int32_t r0 = S.ev.x, nr = S.ev.y, i0 = S.ev.z, ni = S.ev.w;
+            for (int32_t base = 0; base < nr + ni; base += 32) {
+                // up to 32 events of the transition at once (the
+                // first 32 from the ring)
+                const int32_t j = base + lane;
+                int2 pc = make_int2(0, 0);
+                uint32_t cm = 0;
+                if (j < nr + ni) {
+                    if (base == 0) {
+                        pc = S.pc[lane];
+                        cm = pc.y < 0 ? S.cm[lane] : 0u;
+                    } else {
+                        pc = j < nr ? code.rem[r0 + j] : code.ins[i0 + (j - nr)];
+                        if (pc.y < 0) {
+                            cm = qd.node_mask[-pc.y - 1];
+                        }
+                    }
+                }
+                const int32_t cnt = min(32, nr + ni - base);
+                // each event's fields are fetched one event ahead
+                int32_t pn = __shfl_sync(0xffffffffu, pc.x, 0);
+                int32_t cn = __shfl_sync(0xffffffffu, pc.y, 0);
+                uint32_t mn = __shfl_sync(0xffffffffu, cm, 0);
+                for (int32_t e = 0; e < cnt; e++) {
+                    const int32_t p = pn, c = cn;
+                    const uint32_t m = mn;
+                    pn = __shfl_sync(0xffffffffu, pc.x, (e + 1) & 31);
+                    cn = __shfl_sync(0xffffffffu, pc.y, (e + 1) & 31);
+                    mn = __shfl_sync(0xffffffffu, cm, (e + 1) & 31);
+                    event(p, c, base + e < nr ? -1 : +1, m);
+                }
+            }
+            if (q.branch) {
+                close_list();
+                if (cursor != climit) {
+                    dev_error(w.err, DEV_ITEM_PLAN);
+                }
+                if (EVAL && (t - t0) % TSG_PUBLISH_EVERY == 0) {
+                    // publish the tree's items to the evaluating warps
+                    __threadfence_block();
+                    __syncwarp();
+                    if (lane == 0) {
+                        *(volatile int *) s_ready = t;
+                    }
+                }
+            }
+        }
+        if (site && t < t1) {
+            const int32_t m0 = S.mr.x, m1 = S.mr.y;
+            for (int32_t m = m0 + lane; m < m1; m += 32) {
+                int32_t enc;
+                uint32_t mask = 0;
+                if (m - m0 < 32) {
+                    enc = S.menc[lane];
+                    if (enc < 0) {
+                        mask = S.mmask[lane];
+                    }
+                } else {
+                    enc = code.mut[m];
+                    if (enc < 0) {
+                        mask = qd.node_mask[-enc - 1];
+                    }
+                }
+                const Pack x = enc >= 0 ? st_load(sp, enc) : pk_from_mask<W>(mask, K);
+                w.mcnt[(int64_t) m * KQ] = x.lo;
+                if (KQ > 1) {
+                    w.mcnt[(int64_t) m * KQ + (KQ > 1 ? 1 : 0)] = x.hi;
+                }
+            }
+        }
+        cp_async_wait_all();
+        __syncwarp();
+    }
+    if (EVAL && q.branch) {
+        __threadfence_block();
+        __syncwarp();
+        if (lane == 0) {
+            *(volatile int *) s_ready = tend;
+        }
+    }
+}
+
+// The evaluating warps of a span's block: they take the span's evaluation
+// chunks in order and value each once the replay has completed its tree (a
+// bounded wait).
+template <typename F, bool UNPOL, int W, int KQ>
+__device__ __forceinline__ void eval_span_chunks(const TSView &ts, const QueryParams &q,
+    const WsDev &w, int s, int32_t t0, int32_t t1, int *s_ready, int *s_next)
+{
+    const int lane = threadIdx.x & 31;
+    // ---- the other warps value the span's chunks as the replay
+    // completes their trees
+    const int32_t ta = s == 0 ? 0 : t0 + 1;
+    const int32_t tb = t1 < ts.num_trees ? t1 + 1 : t1;
+    const int64_t cfirst = ts.tree_chunk_off[ta], clast = ts.tree_chunk_off[tb];
+    for (;;) {
+        int c0 = 0;
+        if (lane == 0) {
+            c0 = atomicAdd(s_next, 1);
+        }
+        const int64_t c = cfirst + __shfl_sync(0xffffffffu, c0, 0);
+        if (c >= clast) {
+            break;
+        }
+        const int32_t tc = ts.chunk_tree[c];
+        for (uint32_t spin = 0; *(volatile int *) s_ready < tc; spin++) {
+            if (spin > TSG_REPLAY_SPIN_LIMIT) {
+                dev_error(w.err, DEV_WAIT_TIMEOUT);
+                break;
+            }
+            __nanosleep(128);
+        }
+        __threadfence_block();
+        eval_chunk<F, UNPOL, W, KQ>(ts, q, w, c, lane,
+            ts.span_time + ts.span_local_off[ts.chunk_span[c]]);
+    }
+}
+
+// Every evaluation chunk of the item pipeline, one warp per chunk, after a
+// replay that did not value its items (the compact replay): the chunks'
+// items carry the compact plan's local ids.
+template <typename F, bool UNPOL, int KQ>
+__global__ void __launch_bounds__(256) k_eval_chunks(TSView ts, QueryParams q, WsDev w)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
+    for (int64_t c = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
+         c < ts.num_chunks; c += nwarps) {
+        eval_chunk<F, UNPOL, 16, KQ>(ts, q, w, c, lane,
+            ts.c_time + ts.c_local_off[ts.c_chunk_span[c]]);
+    }
+}
 
 template <int W, int KQ, typename IdxT, typename F, bool UNPOL, bool EVAL>
 __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams q, QueryDev qd,
@@ -131,311 +487,12 @@ __global__ void __launch_bounds__(512, 2) k_replay_items(TSView ts, QueryParams 
         // most TSG_TOUCH_CAP nodes; a longer transition closes the list and
         // opens a new one (the span plan counts items the same way).
         if (threadIdx.x < 32) {
-            int64_t cursor = 0;  // first item of the open list
-            int64_t climit = 0;  // end of the transition's items in the plan
-            int32_t nopen = 0;   // nodes in the open list
-            auto close_list = [&]() {
-                __syncwarp();
-                for (int32_t i = lane; i < nopen; i += 32) {
-                    const TouchEntry<KQ> en = s_list[i];
-                    const uint32_t pu = (uint32_t) sp.par[en.u] & PMASK;
-                    if (cursor + i < climit) {
-                        item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
-                            st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
-                            pu != TSG_NO_PARENT ? (int32_t) pu : -1);
-                    }
-                    sp.par[en.u] = (IdxT) pu;  // clears the touch flag
-                }
-                __syncwarp();
-                cursor += nopen;
-                nopen = 0;
-            };
-            // Lanes with `active` set touch node u (distinct per lane) whose
-            // counts are still x0 and whose parent entry (flag and parent) is
-            // praw, read after the previous batch's touches; returns the
-            // entry with the flag set, which the caller stores (with the
-            // node's new parent, for an edge's child).  A node is touched at
-            // most once per edge event and every event ends with __syncwarp.
-            auto touch = [&](bool active, uint32_t u, const Pack &x0, uint32_t praw) {
-                bool fresh = active && !(praw & PFLAG);
-                unsigned m = __ballot_sync(0xffffffffu, fresh);
-                if (nopen + __popc(m) > TSG_TOUCH_CAP) {
-                    close_list();
-                    fresh = active;
-                    m = __ballot_sync(0xffffffffu, fresh);
-                }
-                if (fresh) {
-                    const int32_t at = nopen + __popc(m & ((1u << lane) - 1u));
-                    const uint32_t p0 = praw & PMASK;
-                    TouchEntry<KQ> en;
-                    en.x0[0] = x0.lo;
-                    if (KQ > 1) {
-                        en.x0[KQ > 1 ? 1 : 0] = x0.hi;
-                    }
-                    en.u = u;
-                    en.p0 = p0 != TSG_NO_PARENT ? (int32_t) p0 : -1;
-                    s_list[at] = en;
-                    if (cursor + at >= climit) {
-                        dev_error(w.err, DEV_ITEM_PLAN);
-                    }
-                }
-                nopen += __popc(m);
-                return (praw & PMASK) | PFLAG;
-            };
-            // the next (up to) 32 - first nodes of a root path from v, lane
-            // first + j taking the j-th with its parent entry; advances v
-            // past them
-            auto chase = [&](uint32_t &v, uint32_t &mine, uint32_t &mraw, int first) {
-                mine = NO_NODE;
-                mraw = 0;
-#pragma unroll 4
-                for (int j = first; j < 32; j++) {
-                    if (v == TSG_NO_PARENT) {
-                        break;
-                    }
-                    const uint32_t raw = (uint32_t) sp.par[v];
-                    mine = lane == j ? v : mine;
-                    mraw = lane == j ? raw : mraw;
-                    v = raw & PMASK;
-                }
-            };
-            // One edge event; cm: membership bits of a leaf child (whose
-            // branch is accounted per edge, k_leaf_areas).  The nodes are
-            // touched in batches of 32 lanes: a stateful child on lane 0
-            // with the first 31 nodes of the parent's root path (the child is
-            // not on it), then 32 path nodes at a time -- one touch-list
-            // step per batch (the span plan counts items with the same
-            // batches).  The child keeps its counts and takes its new parent;
-            // the path nodes add or remove the child's counts.
-            auto event = [&](int32_t p, int32_t c, int sign, uint32_t cm) {
-                uint32_t v = (uint32_t) p, mine, mraw;
-                const bool child = c >= 0;
-                chase(v, mine, mraw, child ? 1 : 0);
-                const Pack xc = child ? st_load(sp, c) : pk_from_mask<W>(cm, K);
-                bool is_child = false;
-                if (child && lane == 0) {
-                    mine = (uint32_t) c;
-                    mraw = (uint32_t) sp.par[c];
-                    is_child = true;
-                }
-                const uint32_t np = sign > 0 ? (uint32_t) p : TSG_NO_PARENT;
-                for (int32_t batches = 1;; batches++) {
-                    const bool act = mine != NO_NODE;
-                    Pack xo{0, 0};
-                    if (act) {
-                        xo = is_child ? xc : st_load(sp, (int64_t) mine);
-                    }
-                    if (q.branch) {
-                        const uint32_t f = touch(act, mine, xo, mraw);
-                        if (act) {
-                            sp.par[mine] = (IdxT) (is_child ? (np | PFLAG) : f);
-                        }
-                    } else if (is_child) {
-                        sp.par[mine] = (IdxT) np;
-                    }
-                    if (act && !is_child) {
-                        Pack xn;
-                        if (sign > 0) {
-                            xn.lo = xo.lo + xc.lo;
-                            xn.hi = xo.hi + xc.hi;
-                        } else {
-                            xn.lo = xo.lo - xc.lo;
-                            xn.hi = xo.hi - xc.hi;
-                        }
-                        pk_store(sp, (int64_t) mine, xn);
-                    }
-                    if (v == TSG_NO_PARENT) {
-                        break;
-                    }
-                    // a root path has at most Ls nodes: more means a cycle
-                    if (batches > (Ls >> 5) + 1) {
-                        dev_error(w.err, DEV_PATH_TOO_LONG);
-                        break;
-                    }
-                    chase(v, mine, mraw, 0);
-                    is_child = false;
-                }
-                __syncwarp();
-            };
-            const int32_t tend = q.branch && t1 < ts.num_trees ? t1 + 1 : t1;
-            const bool site = q.site;
-            // Prefetch ring: tree t's inputs are staged in three dependent
-            // steps -- (a) its event, mutation and item ranges, (b) its event
-            // and mutation encodings, (c) the masks of its leaf children and
-            // leaf mutation nodes -- issued three, two and one trees ahead.
-            auto stage_a = [&](int32_t t) {
-                ReplayStage &S = s_stage[t & 3];
-                if (lane == 0) {
-                    cp_async16(&S.ev, &ts.tree_ev[t]);
-                } else if (lane == 1) {
-                    cp_async8(&S.mr, &ts.tree_mut[t]);
-                } else if (lane == 2) {
-                    cp_async8(&S.ioff[0], &ts.tree_item_off[t]);
-                } else if (lane == 3) {
-                    cp_async8(&S.ioff[1], &ts.tree_item_off[t + 1]);
-                }
-            };
-            auto stage_b = [&](int32_t t) {
-                ReplayStage &S = s_stage[t & 3];
-                const int4 ev = S.ev;
-                if (t > t0 && lane < ev.y + ev.w) {
-                    cp_async8(&S.pc[lane], lane < ev.y ? (const void *) &ts.rem_enc[ev.x + lane]
-                                                       : (const void *) &ts.ins_enc[ev.z + lane - ev.y]);
-                }
-                if (site && t < t1 && lane < S.mr.y - S.mr.x) {
-                    cp_async4(&S.menc[lane], &ts.mut_enc[S.mr.x + lane]);
-                }
-            };
-            auto stage_c = [&](int32_t t) {
-                ReplayStage &S = s_stage[t & 3];
-                const int4 ev = S.ev;
-                if (t > t0 && lane < ev.y + ev.w && S.pc[lane].y < 0) {
-                    cp_async4(&S.cm[lane], &qd.node_mask[-S.pc[lane].y - 1]);
-                }
-                if (site && t < t1 && lane < S.mr.y - S.mr.x && S.menc[lane] < 0) {
-                    cp_async4(&S.mmask[lane], &qd.node_mask[-S.menc[lane] - 1]);
-                }
-            };
-            for (int32_t k = 0; k < 3; k++) {
-                if (t0 + k < tend) {
-                    stage_a(t0 + k);
-                }
-            }
-            cp_async_wait_all();
-            __syncwarp();
-            for (int32_t k = 0; k < 2; k++) {
-                if (t0 + k < tend) {
-                    stage_b(t0 + k);
-                }
-            }
-            cp_async_wait_all();
-            __syncwarp();
-            if (t0 < tend) {
-                stage_c(t0);
-            }
-            cp_async_wait_all();
-            __syncwarp();
-            for (int32_t t = t0; t < tend; t++) {
-                if (t + 3 < tend) {
-                    stage_a(t + 3);
-                }
-                if (t + 2 < tend) {
-                    stage_b(t + 2);
-                }
-                if (t + 1 < tend) {
-                    stage_c(t + 1);
-                }
-                cp_async_commit();
-                const ReplayStage &S = s_stage[t & 3];
-                if (t > t0) {
-                    cursor = S.ioff[0];
-                    climit = S.ioff[1];
-                    const int32_t r0 = S.ev.x, nr = S.ev.y, i0 = S.ev.z, ni = S.ev.w;
-                    for (int32_t base = 0; base < nr + ni; base += 32) {
-                        // up to 32 events of the transition at once (the
-                        // first 32 from the ring)
-                        const int32_t j = base + lane;
-                        int2 pc = make_int2(0, 0);
-                        uint32_t cm = 0;
-                        if (j < nr + ni) {
-                            if (base == 0) {
-                                pc = S.pc[lane];
-                                cm = pc.y < 0 ? S.cm[lane] : 0u;
-                            } else {
-                                pc = j < nr ? ts.rem_enc[r0 + j] : ts.ins_enc[i0 + (j - nr)];
-                                if (pc.y < 0) {
-                                    cm = qd.node_mask[-pc.y - 1];
-                                }
-                            }
-                        }
-                        const int32_t cnt = min(32, nr + ni - base);
-                        // each event's fields are fetched one event ahead
-                        int32_t pn = __shfl_sync(0xffffffffu, pc.x, 0);
-                        int32_t cn = __shfl_sync(0xffffffffu, pc.y, 0);
-                        uint32_t mn = __shfl_sync(0xffffffffu, cm, 0);
-                        for (int32_t e = 0; e < cnt; e++) {
-                            const int32_t p = pn, c = cn;
-                            const uint32_t m = mn;
-                            pn = __shfl_sync(0xffffffffu, pc.x, (e + 1) & 31);
-                            cn = __shfl_sync(0xffffffffu, pc.y, (e + 1) & 31);
-                            mn = __shfl_sync(0xffffffffu, cm, (e + 1) & 31);
-                            event(p, c, base + e < nr ? -1 : +1, m);
-                        }
-                    }
-                    if (q.branch) {
-                        close_list();
-                        if (cursor != climit) {
-                            dev_error(w.err, DEV_ITEM_PLAN);
-                        }
-                        if (EVAL && (t - t0) % TSG_PUBLISH_EVERY == 0) {
-                            // publish the tree's items to the evaluating warps
-                            __threadfence_block();
-                            __syncwarp();
-                            if (lane == 0) {
-                                *(volatile int *) &s_ready = t;
-                            }
-                        }
-                    }
-                }
-                if (site && t < t1) {
-                    const int32_t m0 = S.mr.x, m1 = S.mr.y;
-                    for (int32_t m = m0 + lane; m < m1; m += 32) {
-                        int32_t enc;
-                        uint32_t mask = 0;
-                        if (m - m0 < 32) {
-                            enc = S.menc[lane];
-                            if (enc < 0) {
-                                mask = S.mmask[lane];
-                            }
-                        } else {
-                            enc = ts.mut_enc[m];
-                            if (enc < 0) {
-                                mask = qd.node_mask[-enc - 1];
-                            }
-                        }
-                        const Pack x = enc >= 0 ? st_load(sp, enc) : pk_from_mask<W>(mask, K);
-                        w.mcnt[(int64_t) m * KQ] = x.lo;
-                        if (KQ > 1) {
-                            w.mcnt[(int64_t) m * KQ + (KQ > 1 ? 1 : 0)] = x.hi;
-                        }
-                    }
-                }
-                cp_async_wait_all();
-                __syncwarp();
-            }
-            if (EVAL && q.branch) {
-                __threadfence_block();
-                __syncwarp();
-                if (lane == 0) {
-                    *(volatile int *) &s_ready = tend;
-                }
-            }
+            replay_span<W, KQ, IdxT, EVAL>(ts, q, qd, w, sp, s_list, s_stage, &s_ready, t0, t1, Ls,
+                ReplayEnc{ts.rem_enc, ts.ins_enc, ts.mut_enc});
         } else if (EVAL && q.branch && (threadIdx.x >> 5) % 4 != 0) {
             // ---- the other warps value the span's chunks as the replay
             // completes their trees
-            const int32_t ta = s == 0 ? 0 : t0 + 1;
-            const int32_t tb = t1 < ts.num_trees ? t1 + 1 : t1;
-            const int64_t cfirst = ts.tree_chunk_off[ta], clast = ts.tree_chunk_off[tb];
-            for (;;) {
-                int c0 = 0;
-                if (lane == 0) {
-                    c0 = atomicAdd(&s_next, 1);
-                }
-                const int64_t c = cfirst + __shfl_sync(0xffffffffu, c0, 0);
-                if (c >= clast) {
-                    break;
-                }
-                const int32_t tc = ts.chunk_tree[c];
-                for (uint32_t spin = 0; *(volatile int *) &s_ready < tc; spin++) {
-                    if (spin > TSG_REPLAY_SPIN_LIMIT) {
-                        dev_error(w.err, DEV_WAIT_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(128);
-                }
-                __threadfence_block();
-                eval_chunk<F, UNPOL, W, KQ, TSG_FUSED_EVAL_GROUP>(ts, q, w, c, lane);
-            }
+            eval_span_chunks<F, UNPOL, W, KQ>(ts, q, w, s, t0, t1, &s_ready, &s_next);
         }
         __syncthreads();
     }

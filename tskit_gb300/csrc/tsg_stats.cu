@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "tsg_items.cuh"
+#include "tsg_replay_compact.cuh"
 #include "tsg_query.cuh"
 
 namespace tsg {
@@ -462,6 +463,12 @@ static void *replay_kernel(int W, int KQ, const QueryParams &p)
     }
 }
 
+// The compact replay (tsg_replay_compact.cuh).
+static void *compact_kernel(int KQ)
+{
+    return KQ == 1 ? (void *) k_replay_compact<1> : (void *) k_replay_compact<2>;
+}
+
 // bytes of one span's node state: packed counts and parent ids (node times
 // come from the span plan, seek counters from per-CTA scratch)
 static int64_t span_state_bytes(int64_t L, int W, int KQ)
@@ -607,6 +614,7 @@ struct tsg_query {
     int64_t ws_bytes;
     bool smem;               // item pipeline (either form); else the general sweep
     bool gstate;             // item pipeline with node state in global memory
+    bool compact_ok;         // the compact replay serves when the tree sequence has its plan
     int W, KQ;               // count field width, 64-bit count words per node
     int64_t smem_bytes, smem_grid, slot_bytes;
     int span_normalise;
@@ -1076,6 +1084,11 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         slots = 0;  // no per-slot node arrays of the general sweep
         q->num_slots = 0;
     }
+    q->compact_ok = q->smem && !q->gstate && q->W == 16 && q->KQ <= 2;
+    if (q->compact_ok) {
+        void *fn = compact_kernel(q->KQ);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
+    }
     // window accumulators: per span (general sweep) or per segment (item
     // pipeline)
     const int64_t TSW = std::max(q->total_span_windows, q->total_seg_windows);
@@ -1101,6 +1114,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * TSG_FX_LIMBS * 8 * 3, 256);  // leaf areas
         bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * 8, 256);          // leaf_dbl
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // leaf_win
+        bytes += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256); // cp0
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -1636,6 +1650,7 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.node_mask = nullptr;
     w.site_val = nullptr;
     w.site_win = nullptr;
+    w.cp0 = nullptr;
     if (q->smem) {
         const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
         w.items = b + off;
@@ -1662,6 +1677,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up((p.branch ? (int64_t) p.Wn << p.K : 0) * 8, 256);
         w.leaf_win = (double *) (b + off);
         off += align_up((int64_t) p.Wn * R * 8, 256);
+        w.cp0 = (uint64_t *) (b + off);
+        off += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
@@ -1810,7 +1827,47 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         const unsigned g = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
         const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
-        if (p.branch) {
+        if (q->compact_ok && ts->v.c_num_spans > 0) {
+            // the compact replay: the first tree's items, one block per span
+            // at a time, then every chunk's item values
+            const int kq = q->KQ;
+            if (p.branch && ts->v.c_num_anchors > 0) {
+                if (kq == 1) {
+                    k_compact_prefix<1><<<1, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                } else {
+                    k_compact_prefix<2><<<1, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                }
+                TSG_LAUNCHED();
+                const unsigned ga = (unsigned) grid_for(ts->v.c_num_anchors);
+                if (kq == 1) {
+                    k_compact_anchors<1><<<ga, 256, 0, st>>>(ts->v, w.cp0, w);
+                } else {
+                    k_compact_anchors<2><<<ga, 256, 0, st>>>(ts->v, w.cp0, w);
+                }
+                TSG_LAUNCHED();
+            }
+            const size_t csb = (size_t) align_up(replay_state_bytes(ts->v.c_max_local, 16, kq), 16);
+            void *fn = compact_kernel(kq);
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TSG_COMPACT_THREADS, csb);
+            const unsigned cg = (unsigned) std::min<int64_t>(
+                (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()), ts->v.c_num_spans);
+            if (kq == 1) {
+                k_replay_compact<1><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
+            } else {
+                k_replay_compact<2><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
+            }
+            if (p.branch) {
+                TSG_LAUNCHED();
+                if (p.f32) {
+                    (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
+                        ts->v, p, w);
+                } else {
+                    (p.polarised ? launch_eval_chunks_f64_pol : launch_eval_chunks_f64_unpol)(kq, st,
+                        ts->v, p, w);
+                }
+            }
+        } else if (p.branch) {
             // replay and item values in one kernel
             if (p.f32) {
                 (p.polarised ? launch_replay_eval_f32_pol : launch_replay_eval_f32_unpol)(form, g, sb,

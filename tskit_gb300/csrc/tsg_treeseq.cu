@@ -483,6 +483,9 @@ int tsg_treeseq_free(tsg_treeseq_t *ts)
     for (void *p : ts->owned) {
         cudaFree(p);
     }
+    for (void *p : ts->compact_owned) {
+        cudaFree(p);
+    }
     if (ts->sync_ws != nullptr) {
         tsg_workspace_free(ts->sync_ws);
     }
@@ -494,6 +497,21 @@ int tsg_treeseq_free(tsg_treeseq_t *ts)
 int64_t tsg_treeseq_get_num_trees(const tsg_treeseq_t *ts) { return ts->v.num_trees; }
 int64_t tsg_treeseq_get_num_samples(const tsg_treeseq_t *ts) { return ts->v.num_samples; }
 int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts) { return ts->v.num_spans; }
+int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts) { return ts->v.c_num_spans; }
+
+int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans)
+{
+    if (ts == nullptr || num_spans < 0) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    std::lock_guard<std::mutex> lock(ts->sync_mutex);
+    TSG_CUDA(cudaDeviceSynchronize());
+    if (num_spans == 0 || ts->v.num_trees < 1) {
+        ts->v.c_num_spans = 0;
+        return 0;
+    }
+    return tsg::build_compact_plan(ts, ts->host, std::min<int64_t>(num_spans, ts->v.num_trees));
+}
 
 int tsg_treeseq_get_breakpoints(const tsg_treeseq_t *ts, double *bp)
 {
@@ -740,6 +758,13 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         }
         if ((ret = build_span_plan(ts, h, num_spans)) != 0) {
             goto fail;
+        }
+        {
+            const int64_t events = (int64_t) h.tree_in[(size_t) T] + (int64_t) h.tree_out[(size_t) T];
+            const int64_t nc = compact_default_spans(T, events, ts->v.num_samples);
+            if ((ret = build_compact_plan(ts, h, nc)) != 0) {
+                goto fail;
+            }
         }
         ts->host = std::move(h);
         if ((ret = d2h(ts->h_site_position, t.site_pos, S)) != 0) {

@@ -313,6 +313,19 @@ class TreeSequence:
         return self._lib.tsg_treeseq_get_num_spans(self._handle)
 
     @property
+    def num_compact_spans(self):
+        """Spans of the compact replay plan (0: the general replay serves the
+        sample-count statistics)."""
+        return self._lib.tsg_treeseq_get_num_compact_spans(self._handle)
+
+    def set_compact_spans(self, num_spans):
+        """Rebuild the compact replay plan with about ``num_spans`` spans (0:
+        use the general replay); returns the span count built.  Results do
+        not depend on it."""
+        nat.check(self._lib.tsg_treeseq_set_compact_spans(self._handle, int(num_spans)))
+        return self.num_compact_spans
+
+    @property
     def sites_position(self):
         return self.tables.site_position
 
