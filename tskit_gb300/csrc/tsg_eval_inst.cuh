@@ -43,11 +43,19 @@ TSG_REPLAY_EVAL_LAUNCHER(TSG_EVAL_NAME)
 
 TSG_CHUNK_EVAL_LAUNCHER(TSG_CHUNKS_NAME)
 {
-    const unsigned grid = (unsigned) std::min<int64_t>((v.num_chunks + 7) / 8, 1 << 20);
+    const int64_t C = v.num_chunks;
+    int64_t total = 0;
+    for (int g = 0; g < p.ngroups; g++) {
+        total += group_warps(p, C, g);
+    }
+    const unsigned gb = (unsigned) std::min<int64_t>((C + 7) / 8, 1 << 20);
+    const unsigned ge = (unsigned) std::min<int64_t>((total + 7) / 8, 1 << 20);
     if (kq == 1) {
-        k_eval_chunks<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<grid, 256, 0, st>>>(v, p, w);
+        k_item_bls<TSG_EVAL_F, 1><<<gb, 256, 0, st>>>(v, p, w);
+        k_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<ge, 256, 0, st>>>(v, p, w, total);
     } else {
-        k_eval_chunks<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<grid, 256, 0, st>>>(v, p, w);
+        k_item_bls<TSG_EVAL_F, 2><<<gb, 256, 0, st>>>(v, p, w);
+        k_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<ge, 256, 0, st>>>(v, p, w, total);
     }
 }
 

@@ -26,6 +26,11 @@ struct QueryParams {
     float inv_f[TSG_MAX_OUTPUTS];
     float inv_K_f;
     Term term[TSG_MAX_OUTPUTS];
+    // the terms grouped by summary type (the grouped item evaluation gives
+    // each warp one type): group g holds gterm[gfirst[g] .. gfirst[g + 1])
+    int32_t ngroups;
+    int32_t gfirst[TSG_MAX_OUTPUTS + 1];
+    int32_t gterm[TSG_MAX_OUTPUTS];
 };
 
 struct QueryDev {

@@ -13,8 +13,9 @@
 //
 // The first tree's items (its stateful nodes, the anchors) are written by
 // k_compact_anchors from the prefix sum of the first span's order
-// (k_compact_prefix) before the replay starts, and k_eval_chunks values every
-// chunk of items after it, all chunks in parallel.
+// (k_compact_prefix) before the replay starts, and k_item_bls and
+// k_eval_grouped value every chunk of items after it, all chunks in
+// parallel.
 #pragma once
 
 #include "tsg_replay_kernel.cuh"

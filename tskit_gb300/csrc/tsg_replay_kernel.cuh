@@ -365,18 +365,144 @@ __device__ __forceinline__ void eval_span_chunks(const TSView &ts, const QueryPa
     }
 }
 
-// Every evaluation chunk of the item pipeline, one warp per chunk, after a
-// replay that did not value its items (the compact replay): the chunks'
-// items carry the compact plan's local ids.
-template <typename F, bool UNPOL, int KQ>
-__global__ void __launch_bounds__(256) k_eval_chunks(TSView ts, QueryParams q, WsDev w)
+// The item values after a replay that did not value its items (the compact
+// replay; the items carry the compact plan's local ids), in two kernels.
+//
+// k_item_bls, a warp per chunk and a lane per item: each item's branch
+// lengths in the evaluation's arithmetic, (bl1, bl0) -- in the integer form
+// (bl1 - bl0, bl0) for an item with the same counts before and after.
+template <typename F, int KQ>
+__global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDev w)
 {
     const int lane = threadIdx.x & 31;
+    const Item<KQ> *items = (const Item<KQ> *) w.items;
+    const bool num_form = sizeof(F) == sizeof(double) && q.site_int;
+    F *bls = (F *) w.bl;
     const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
     for (int64_t c = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
          c < ts.num_chunks; c += nwarps) {
-        eval_chunk<F, UNPOL, 16, KQ>(ts, q, w, c, lane,
-            ts.c_time + ts.c_local_off[ts.c_chunk_span[c]]);
+        const double *time = ts.c_time + ts.c_local_off[ts.c_chunk_span[c]];
+        for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
+            const Item<KQ> it = items[i];
+            const double tu = time[it.u];
+            const double bl0 = it.p0 >= 0 ? time[it.p0] - tu : 0.0;
+            const double bl1 = it.p1 >= 0 ? time[it.p1] - tu : 0.0;
+            bool same = it.x0[0] == it.x1[0];
+            if (KQ > 1) {
+                same = same && it.x0[KQ > 1 ? 1 : 0] == it.x1[KQ > 1 ? 1 : 0];
+            }
+            bls[2 * i] = (F) (num_form && same ? bl1 - bl0 : bl1);
+            bls[2 * i + 1] = (F) bl0;
+        }
+    }
+}
+
+// Warps of the grouped evaluation of a query: each warp takes one group of
+// terms of one summary type (q.gfirst / q.gterm) over 32 / (group size)
+// consecutive chunks.
+__host__ __device__ __forceinline__ int64_t group_warps(const QueryParams &q, int64_t C, int g)
+{
+    const int gs = q.gfirst[g + 1] - q.gfirst[g];
+    const int cpw = 32 / gs;
+    return (C + cpw - 1) / cpw;
+}
+
+// k_eval_grouped: a lane per (chunk, term) with every lane of a warp on terms
+// of one summary type, so the warp runs one code path; each lane walks its
+// chunk's items in order (no sum crosses lanes).  FP64 with integer
+// summaries: exact numerators, about one FP64 fused multiply-add per item
+// and lane (as eval_chunk); otherwise the summary functions in F (FP32:
+// exact item values into a compensated pair).
+template <typename F, bool UNPOL, int KQ>
+__global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
+    int64_t total_warps)
+{
+    constexpr bool F32 = sizeof(F) == sizeof(float);
+    const int lane = threadIdx.x & 31;
+    const Item<KQ> *items = (const Item<KQ> *) w.items;
+    const F *bls = (const F *) w.bl;
+    const int64_t C = ts.num_chunks;
+    const int R = q.R;
+    const bool num_form = !F32 && q.site_int;
+    const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
+    for (int64_t gw = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
+         gw < total_warps; gw += nwarps) {
+        int g = 0;
+        int64_t first = 0;
+        for (; g + 1 < q.ngroups; g++) {
+            const int64_t nw = group_warps(q, C, g);
+            if (gw < first + nw) {
+                break;
+            }
+            first += nw;
+        }
+        const int gs = q.gfirst[g + 1] - q.gfirst[g];
+        const int cpw = 32 / gs;
+        const int j = lane / gs;
+        const int64_t c = (gw - first) * cpw + j;
+        if (j >= cpw || c >= C) {
+            continue;
+        }
+        const int r = q.gterm[q.gfirst[g] + lane % gs];
+        const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
+        if (num_form) {
+            const Term t = q.term[r];
+            double acc = 0;
+            for (int64_t i = b; i < e; i++) {
+                const Item<KQ> it = items[i];
+                const double fa = (double) bls[2 * i], fb = (double) bls[2 * i + 1];
+                const Pack x0 = item_pack<KQ>(it.x0);
+                const Pack x1 = item_pack<KQ>(it.x1);
+                const bool same = x0.lo == x1.lo && x0.hi == x1.hi;
+                const int64_t n1 = item_num<UNPOL, 16>(t, q.set_size_i, x1);
+                const uint64_t ba = (uint64_t) __double_as_longlong(fa);
+                const uint64_t bb = (uint64_t) __double_as_longlong(fb);
+                if (same || bb == 0) {
+                    acc = fma(fa, i64_to_f64(n1), acc);
+                } else {
+                    const int64_t n0 = item_num<UNPOL, 16>(t, q.set_size_i, x0);
+                    if (ba == bb) {
+                        acc = fma(fa, i64_to_f64(n1 - n0), acc);
+                    } else {
+                        acc = fma(fa, i64_to_f64(n1), fma(-fb, i64_to_f64(n0), acc));
+                    }
+                }
+            }
+            // a term whose denominator is zero (a set too small for it) is
+            // NaN wherever the running sum takes a node's value, as in the
+            // reference
+            const double inv = q.inv[r];
+            w.dD[c * R + r] = e <= b ? 0.0 : isfinite(inv) ? acc * inv : (double) NAN;
+            continue;
+        }
+        F acc = 0, lo = 0;
+        for (int64_t i = b; i < e; i++) {
+            const Item<KQ> it = items[i];
+            const F bl1 = bls[2 * i], bl0 = bls[2 * i + 1];
+            const Pack x0 = item_pack<KQ>(it.x0);
+            const Pack x1 = item_pack<KQ>(it.x1);
+            const bool same = x0.lo == x1.lo && x0.hi == x1.hi;
+            F m1x, m1c;
+            pk_means<F, 16>(q, x1, m1x, m1c);
+            const F f1 = term_F<F, UNPOL, 16>(q, r, x1, m1x, m1c);
+            if (!same && bl0 != 0) {
+                F m0x, m0c;
+                pk_means<F, 16>(q, x0, m0x, m0c);
+                const F f0 = term_F<F, UNPOL, 16>(q, r, x0, m0x, m0c);
+                if constexpr (F32) {
+                    acc2_add(acc, lo, bl1, f1, bl0, f0);
+                } else {
+                    acc += bl0 == bl1 ? bl1 * (f1 - f0) : bl1 * f1 - bl0 * f0;
+                }
+            } else {
+                if constexpr (F32) {
+                    acc2_add(acc, lo, bl1, f1, bl0, same ? f1 : (F) 0);
+                } else {
+                    acc += (same ? bl1 - bl0 : bl1) * f1;
+                }
+            }
+        }
+        w.dD[c * R + r] = (double) acc + (double) lo;
     }
 }
 

@@ -952,6 +952,25 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     for (uint64_t r = 0; r < R; r++) {
         p.site_int &= outputs[r].type != TSG_RELATEDNESS ? 1 : 0;
     }
+    // terms grouped by type, in term order within a group
+    p.ngroups = 0;
+    {
+        int32_t at = 0;
+        std::vector<bool> used((size_t) R, false);
+        for (uint64_t r = 0; r < R; r++) {
+            if (used[(size_t) r]) {
+                continue;
+            }
+            p.gfirst[p.ngroups++] = at;
+            for (uint64_t u = r; u < R; u++) {
+                if (!used[(size_t) u] && outputs[u].type == outputs[r].type) {
+                    used[(size_t) u] = true;
+                    p.gterm[at++] = (int32_t) u;
+                }
+            }
+        }
+        p.gfirst[p.ngroups] = at;
+    }
     p.inv_K = 1.0 / (double) K;
     for (uint64_t k = 0; k < K; k++) {
         p.set_size_f[k] = (float) p.set_size[k];
@@ -1858,6 +1877,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 k_replay_compact<2><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
             }
             if (p.branch) {
+                // two kernels: the items' branch lengths, then their values
                 TSG_LAUNCHED();
                 if (p.f32) {
                     (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
@@ -1866,6 +1886,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                     (p.polarised ? launch_eval_chunks_f64_pol : launch_eval_chunks_f64_unpol)(kq, st,
                         ts->v, p, w);
                 }
+                TSG_LAUNCHED();
             }
         } else if (p.branch) {
             // replay and item values in one kernel
