@@ -407,12 +407,79 @@ __host__ __device__ __forceinline__ int64_t group_warps(const QueryParams &q, in
     return (C + cpw - 1) / cpw;
 }
 
+// A summary term's integer numerator with its type fixed at compile time
+// (term_num32's cases), plus the same at n - x when unpolarised.
+template <int TYPE, bool UNPOL>
+__device__ __forceinline__ int64_t typed_num(int32_t xi, int32_t xj, int32_t xk, int32_t xl,
+    int32_t ni, int32_t nj, int32_t nk, int32_t nl)
+{
+    int64_t v = term_num32(TYPE, xi, xj, xk, xl, ni, nj, nk, nl);
+    if (UNPOL) {
+        v += term_num32(TYPE, ni - xi, nj - xj, nk - xk, nl - xl, ni, nj, nk, nl);
+    }
+    return v;
+}
+
+// One lane's walk over its chunk's items for a term of type TYPE (integer
+// numerators, FP64 sums): the four counts the term reads are taken out of
+// the packed words with shifts fixed per lane; about one FP64 fused
+// multiply-add per item.  Returns the chunk's unscaled sum.
+template <int TYPE, bool UNPOL, int KQ>
+__device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const double *bls,
+    int64_t b, int64_t e, const Term &t, const int32_t *set_size)
+{
+    const int32_t i0 = t.idx[0], i1 = t.idx[1], i2 = t.idx[2], i3 = t.idx[3];
+    const int32_t ni = set_size[i0], nj = set_size[i1], nk = set_size[i2], nl = set_size[i3];
+    const int s0 = 16 * (i0 & 3), s1 = 16 * (i1 & 3), s2 = 16 * (i2 & 3), s3 = 16 * (i3 & 3);
+    const bool h0 = i0 >= 4, h1 = i1 >= 4, h2 = i2 >= 4, h3 = i3 >= 4;
+    auto cnt = [](uint64_t lo, uint64_t hi, bool h, int sh) {
+        return (int32_t) (((h ? hi : lo) >> sh) & 0xFFFFull);
+    };
+    auto num = [&](uint64_t lo, uint64_t hi) {
+        return typed_num<TYPE, UNPOL>(cnt(lo, hi, h0, s0), cnt(lo, hi, h1, s1),
+            cnt(lo, hi, h2, s2), cnt(lo, hi, h3, s3), ni, nj, nk, nl);
+    };
+    double acc = 0;
+    for (int64_t i = b; i < e; i++) {
+        uint64_t x0lo, x0hi = 0, x1lo, x1hi = 0;
+        if (KQ == 1) {
+            const ulonglong2 xx = *(const ulonglong2 *) items[i].x0;
+            x0lo = xx.x;
+            x1lo = xx.y;
+        } else {
+            const ulonglong2 a = *(const ulonglong2 *) items[i].x0;
+            const ulonglong2 c = *(const ulonglong2 *) items[i].x1;
+            x0lo = a.x;
+            x0hi = a.y;
+            x1lo = c.x;
+            x1hi = c.y;
+        }
+        const double2 f = *(const double2 *) (bls + 2 * i);
+        const bool same = x0lo == x1lo && x0hi == x1hi;
+        const uint64_t ba = (uint64_t) __double_as_longlong(f.x);
+        const uint64_t bb = (uint64_t) __double_as_longlong(f.y);
+        const int64_t n1 = num(x1lo, x1hi);
+        if (same || bb == 0) {
+            acc = fma(f.x, i64_to_f64(n1), acc);
+        } else {
+            const int64_t n0 = num(x0lo, x0hi);
+            if (ba == bb) {
+                acc = fma(f.x, i64_to_f64(n1 - n0), acc);
+            } else {
+                acc = fma(f.x, i64_to_f64(n1), fma(-f.y, i64_to_f64(n0), acc));
+            }
+        }
+    }
+    return acc;
+}
+
 // k_eval_grouped: a lane per (chunk, term) with every lane of a warp on terms
-// of one summary type, so the warp runs one code path; each lane walks its
-// chunk's items in order (no sum crosses lanes).  FP64 with integer
-// summaries: exact numerators, about one FP64 fused multiply-add per item
-// and lane (as eval_chunk); otherwise the summary functions in F (FP32:
-// exact item values into a compensated pair).
+// of one summary type, so the warp runs one code path (a loop specialised
+// to the type for integer numerators); each lane walks its chunk's items in
+// order (no sum crosses lanes).  FP64 with integer summaries: exact
+// numerators, about one FP64 fused multiply-add per item and lane (as
+// eval_chunk); otherwise the summary functions in F (FP32: exact item
+// values into a compensated pair).
 template <typename F, bool UNPOL, int KQ>
 __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
     int64_t total_warps)
@@ -447,26 +514,41 @@ __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, 
         const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
         if (num_form) {
             const Term t = q.term[r];
+            const double *bd = (const double *) bls;
             double acc = 0;
-            for (int64_t i = b; i < e; i++) {
-                const Item<KQ> it = items[i];
-                const double fa = (double) bls[2 * i], fb = (double) bls[2 * i + 1];
-                const Pack x0 = item_pack<KQ>(it.x0);
-                const Pack x1 = item_pack<KQ>(it.x1);
-                const bool same = x0.lo == x1.lo && x0.hi == x1.hi;
-                const int64_t n1 = item_num<UNPOL, 16>(t, q.set_size_i, x1);
-                const uint64_t ba = (uint64_t) __double_as_longlong(fa);
-                const uint64_t bb = (uint64_t) __double_as_longlong(fb);
-                if (same || bb == 0) {
-                    acc = fma(fa, i64_to_f64(n1), acc);
-                } else {
-                    const int64_t n0 = item_num<UNPOL, 16>(t, q.set_size_i, x0);
-                    if (ba == bb) {
-                        acc = fma(fa, i64_to_f64(n1 - n0), acc);
-                    } else {
-                        acc = fma(fa, i64_to_f64(n1), fma(-fb, i64_to_f64(n0), acc));
-                    }
-                }
+            switch (t.type) {
+                case TSG_DIVERSITY:
+                    acc = lane_walk_num<TSG_DIVERSITY, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_SEGREGATING_SITES:
+                    acc = lane_walk_num<TSG_SEGREGATING_SITES, UNPOL, KQ>(items, bd, b, e, t,
+                        q.set_size_i);
+                    break;
+                case TSG_DIVERGENCE:
+                    acc = lane_walk_num<TSG_DIVERGENCE, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_Y3:
+                    acc = lane_walk_num<TSG_Y3, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_Y1:
+                    acc = lane_walk_num<TSG_Y1, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_Y2:
+                    acc = lane_walk_num<TSG_Y2, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_F2:
+                    acc = lane_walk_num<TSG_F2, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_F3:
+                    acc = lane_walk_num<TSG_F3, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                case TSG_F4:
+                    acc = lane_walk_num<TSG_F4, UNPOL, KQ>(items, bd, b, e, t, q.set_size_i);
+                    break;
+                default:
+                    acc = lane_walk_num<TSG_RELATEDNESS_NONCENTRED, UNPOL, KQ>(items, bd, b, e, t,
+                        q.set_size_i);
+                    break;
             }
             // a term whose denominator is zero (a set too small for it) is
             // NaN wherever the running sum takes a node's value, as in the
