@@ -403,8 +403,10 @@ def run_gpu(args):
         q, ws, res = prepare(ts, "f64")
         return lambda: q.launch(ws, res, stream)
 
-    # the span count is autotuned for this tree sequence and fused query
-    ts, tuned = tune.tune_num_spans(tables, tuning_step, key=WORKLOAD, steps=3, warmup=1)
+    # the compact replay's span count is autotuned for this tree sequence
+    # and fused query
+    ts = tskit_gb300.TreeSequence(tables)
+    tuned = tune.tune_compact_spans(ts, tuning_step, key=WORKLOAD, steps=3, warmup=1)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def timed_fused(precision, steps, with_clocks=False):
@@ -540,7 +542,7 @@ def run_gpu(args):
         "dtype": "f64 (window and running sums FP64; summaries as exact integer numerators, "
                  "about one FP64 FMA per item); int32 counts",
         "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
-        "config": dict(workload_config(tables), num_spans=tuned["num_spans"],
+        "config": dict(workload_config(tables), num_compact_spans=tuned["num_spans"],
                        span_tuning_ms={str(k): v for k, v in tuned["ms"].items()}),
         "queries_per_s": world * traversals / (ms / 1e3),
         "physical_edge_updates_per_s": world * events / (ms / 1e3),

@@ -85,3 +85,47 @@ def test_tuned_plan_same_statistics():
             ts.divergence(sets, indexes=[(0, 1), (1, 2)], windows=windows, mode=mode),
             ref.divergence(sets, indexes=[(0, 1), (1, 2)], windows=windows, mode=mode),
             rtol=1e-12, atol=1e-14)
+
+
+class FakeCompactTS:
+    """Host stand-in for a tree sequence with a compact plan."""
+
+    def __init__(self, default=1000, num_trees=10_000, cap=None):
+        self.num_compact_spans = default
+        self.num_trees = num_trees
+        self.num_edges = 4000
+        self.num_samples = 100
+        self.cap = cap
+        self.built = []
+
+    def set_compact_spans(self, n):
+        self.built.append(n)
+        self.num_compact_spans = 0 if (self.cap and n > self.cap) else n
+        return self.num_compact_spans
+
+
+def test_compact_candidates():
+    assert tune.compact_candidates(1000, 10_000) == [500, 1000, 2000, 4000]
+    assert tune.compact_candidates(1000, 1500) == [500, 1000, 1500]
+
+
+def test_tune_compact_picks_fastest_and_skips_unbuildable():
+    ts = FakeCompactTS(cap=2500)
+    ms = {1000: 2.0, 500: 2.5, 2000: 1.5}
+    timer, calls = fake_timer(ms)
+    rep = tune.tune_compact_spans(ts, lambda t: (lambda: t.num_compact_spans), timer=timer)
+    assert rep["num_spans"] == 2000 and ts.num_compact_spans == 2000
+    assert rep["ms"] == ms          # 4000 spans could not be built: not timed
+    assert calls[0] == 1000         # the default plan first
+    cache = {}
+    tune.tune_compact_spans(ts, lambda t: (lambda: t.num_compact_spans), timer=timer,
+                            cache=cache)
+    ts2 = FakeCompactTS(cap=2500)
+    rep2 = tune.tune_compact_spans(ts2, lambda t: (lambda: 0), cache=cache)
+    assert rep2["cached"] and ts2.num_compact_spans == 2000
+
+
+def test_tune_compact_without_plan():
+    ts = FakeCompactTS(default=0)
+    rep = tune.tune_compact_spans(ts, lambda t: (lambda: 0), timer=lambda *a: 1.0)
+    assert rep == {"num_spans": 0, "ms": {}, "cached": False}

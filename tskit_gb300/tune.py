@@ -17,6 +17,11 @@ statistics asked of it, so it is measured rather than guessed:
 * the fastest count kept (ties go to the fewer spans), its tree sequence
   returned, the others released.
 
+Tree sequences of up to 65,535 samples also carry a compact replay plan
+(short spans holding only the nodes their edge events touch) that the
+sample-count statistics use; ``tune_compact_spans`` picks its span count the
+same way on one tree sequence, rebuilding only that plan per candidate.
+
 The CTA shape is not tuned: every replay kernel is compiled for one block
 size (its launch bounds) and fills the SMs by occupancy.  An optional
 ``cache`` dict, keyed by the caller's workload key and the tree sequence's
@@ -108,3 +113,46 @@ def tune_num_spans(tables, make_step, key="", candidates=None, steps=3, warmup=1
     if cache is not None:
         cache[shape] = int(best.num_spans)
     return best, {"num_spans": int(best.num_spans), "ms": times, "cached": False}
+
+
+def compact_candidates(default_spans, num_trees):
+    """Compact span counts to try: half to four times the default, each at
+    most one span per tree."""
+    c = {max(1, int(default_spans * f)) for f in (0.5, 1, 2, 4)}
+    return sorted({min(x, max(1, int(num_trees))) for x in c})
+
+
+def tune_compact_spans(ts, make_step, key="", candidates=None, steps=3, warmup=1, cache=None,
+                       timer=None):
+    """Pick the compact plan's span count for ``ts`` and the workload
+    ``make_step(ts)`` (as :func:`tune_num_spans`); leaves ``ts`` with the
+    fastest plan and returns ``{"num_spans": chosen, "ms": {count: ms},
+    "cached": bool}`` (``num_spans`` 0 when ``ts`` has no compact plan)."""
+    if timer is None:
+        timer = time_step
+    default = int(ts.num_compact_spans)
+    if default == 0:
+        return {"num_spans": 0, "ms": {}, "cached": False}
+    shape = _shape_key(ts, key) + "|compact"
+    if cache is not None and shape in cache:
+        n = int(cache[shape])
+        if n != default:
+            ts.set_compact_spans(n)
+        return {"num_spans": int(ts.num_compact_spans), "ms": {}, "cached": True}
+    if candidates is None:
+        candidates = compact_candidates(default, ts.num_trees)
+    times = {}
+    best, best_ms = default, None
+    for n in [default] + [c for c in candidates if c != default]:
+        actual = int(ts.set_compact_spans(n)) if n != int(ts.num_compact_spans) else n
+        if actual in times or actual == 0:
+            continue
+        times[actual] = timer(make_step(ts), steps, warmup)
+        if best_ms is None or times[actual] < best_ms or (
+                times[actual] == best_ms and actual < best):
+            best, best_ms = actual, times[actual]
+    if int(ts.num_compact_spans) != best:
+        ts.set_compact_spans(best)
+    if cache is not None:
+        cache[shape] = int(best)
+    return {"num_spans": int(ts.num_compact_spans), "ms": times, "cached": False}
