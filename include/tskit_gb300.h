@@ -161,7 +161,8 @@ int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts);
  * counterpart): short spans whose node state holds only the nodes their
  * edge events touch, for tree sequences of up to 65,535 samples.  get: its
  * span count (0 when the tree sequence uses the general replay).  set:
- * rebuild it with about num_spans spans (0: use the general replay; a count
+ * rebuild it with about num_spans spans (-1: the default count; 0: use the
+ * general replay; a count
  * whose spans touch more than 4,096 nodes also leaves the general replay
  * serving); queries prepared before must not run concurrently with it.
  * Results do not depend on the span count. */

@@ -100,6 +100,8 @@ class FakeCompactTS:
 
     def set_compact_spans(self, n):
         self.built.append(n)
+        if n < 0:
+            n = 1000
         self.num_compact_spans = 0 if (self.cap and n > self.cap) else n
         return self.num_compact_spans
 

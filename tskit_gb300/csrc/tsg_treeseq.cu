@@ -501,7 +501,7 @@ int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts) { return ts->
 
 int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans)
 {
-    if (ts == nullptr || num_spans < 0) {
+    if (ts == nullptr || num_spans < -1) {
         return TSG_ERR_BAD_PARAM_VALUE;
     }
     std::lock_guard<std::mutex> lock(ts->sync_mutex);
@@ -509,6 +509,12 @@ int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans)
     if (num_spans == 0 || ts->v.num_trees < 1) {
         ts->v.c_num_spans = 0;
         return 0;
+    }
+    if (num_spans < 0) {
+        const tsg::HostTopology &h = ts->host;
+        const int64_t T = ts->v.num_trees;
+        num_spans = tsg::compact_default_spans(T,
+            (int64_t) h.tree_in[(size_t) T] + (int64_t) h.tree_out[(size_t) T], ts->v.num_samples);
     }
     return tsg::build_compact_plan(ts, ts->host, std::min<int64_t>(num_spans, ts->v.num_trees));
 }

@@ -319,9 +319,9 @@ class TreeSequence:
         return self._lib.tsg_treeseq_get_num_compact_spans(self._handle)
 
     def set_compact_spans(self, num_spans):
-        """Rebuild the compact replay plan with about ``num_spans`` spans (0:
-        use the general replay); returns the span count built.  Results do
-        not depend on it."""
+        """Rebuild the compact replay plan with about ``num_spans`` spans (-1:
+        the default count; 0: use the general replay); returns the span count
+        built.  Results do not depend on it."""
         nat.check(self._lib.tsg_treeseq_set_compact_spans(self._handle, int(num_spans)))
         return self.num_compact_spans
 

@@ -142,17 +142,24 @@ def tune_compact_spans(ts, make_step, key="", candidates=None, steps=3, warmup=1
     if candidates is None:
         candidates = compact_candidates(default, ts.num_trees)
     times = {}
+    # the count asked for that built each plan (the plan's own count can be
+    # lower: spans never split a tree)
+    asked = {default: None}
     best, best_ms = default, None
     for n in [default] + [c for c in candidates if c != default]:
-        actual = int(ts.set_compact_spans(n)) if n != int(ts.num_compact_spans) else n
+        actual = int(ts.set_compact_spans(n)) if n != default else default
         if actual in times or actual == 0:
             continue
+        asked.setdefault(actual, n)
         times[actual] = timer(make_step(ts), steps, warmup)
         if best_ms is None or times[actual] < best_ms or (
                 times[actual] == best_ms and actual < best):
             best, best_ms = actual, times[actual]
     if int(ts.num_compact_spans) != best:
-        ts.set_compact_spans(best)
+        if asked.get(best) is None:
+            ts.set_compact_spans(-1)  # the default plan
+        else:
+            ts.set_compact_spans(asked[best])
     if cache is not None:
         cache[shape] = int(best)
     return {"num_spans": int(ts.num_compact_spans), "ms": times, "cached": False}
