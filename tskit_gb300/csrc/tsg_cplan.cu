@@ -439,9 +439,19 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
         }
     }
 
+    // evaluation order: the chunks by decreasing item count, so that the
+    // chunks one warp values side by side take about the same time
+    std::vector<int32_t> chunk_order(chunk_span.size());
+    for (size_t c = 0; c < chunk_order.size(); c++) {
+        chunk_order[c] = (int32_t) c;
+    }
+    std::stable_sort(chunk_order.begin(), chunk_order.end(), [&](int32_t a, int32_t b) {
+        return ts->h_chunk_items[(size_t) a] > ts->h_chunk_items[(size_t) b];
+    });
+
     int ret;
     std::vector<void *> &own = ts->compact_owned;
-    int32_t *d_st, *d_mut_enc, *d_chunk_span, *d_apar;
+    int32_t *d_st, *d_mut_enc, *d_chunk_span, *d_apar, *d_chunk_order;
     int64_t *d_local_off, *d_ep_off;
     double *d_time;
     uint16_t *d_par0, *d_order;
@@ -453,6 +463,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
         || (ret = upload_host_vec(own, ins_enc, &d_ins)) || (ret = upload_host_vec(own, rem_enc, &d_rem))
         || (ret = upload_host_vec(own, mut_enc, &d_mut_enc))
         || (ret = upload_host_vec(own, chunk_span, &d_chunk_span))
+        || (ret = upload_host_vec(own, chunk_order, &d_chunk_order))
         || (ret = upload_host_vec(own, a_par, &d_apar))
         || (ret = upload_host_vec(own, a_range, &d_arange))) {
         return ret;
@@ -469,6 +480,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     v.c_rem_enc = d_rem;
     v.c_mut_enc = d_mut_enc;
     v.c_chunk_span = d_chunk_span;
+    v.c_chunk_order = d_chunk_order;
     v.c_anchor_par = d_apar;
     v.c_anchor_range = d_arange;
     v.c_num_anchors = (int64_t) a_par.size();

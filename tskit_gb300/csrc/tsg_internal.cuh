@@ -156,6 +156,7 @@ struct TSView {
     const int2 *c_rem_enc;        // removal order: (parent, child), compact encoding
     const int32_t *c_mut_enc;     // per mutation: compact encoding of its node
     const int32_t *c_chunk_span;  // per chunk: the numbering of its items
+    const int32_t *c_chunk_order; // the chunks by decreasing item count (evaluation order)
     int64_t c_num_anchors;        // the first tree's items
     const int32_t *c_anchor_par;  // their parents (anchor ids)
     const int2 *c_anchor_range;   // their sample ranges in the first span's order
@@ -220,6 +221,7 @@ struct tsg_treeseq {
     int64_t max_children = 0;  // most children of a node in any span's seek tree
     int64_t h_tree_item0 = 0;  // the first tree's items
     std::vector<int64_t> h_tree_chunk_off;  // num_trees + 1: first chunk of each tree
+    std::vector<int32_t> h_chunk_items;     // items of each evaluation chunk
     tsg::HostTopology host;    // host copy of the topology (span plan, genotype decoding)
     // device allocations owned by this object
     std::vector<void *> owned;

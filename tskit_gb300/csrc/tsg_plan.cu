@@ -546,6 +546,10 @@ int build_span_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t num_spans)
     ts->h_local_off = local_off;
     ts->h_tree_item0 = T > 0 ? tree_items[0] : 0;
     ts->h_tree_chunk_off = tree_chunk_off;
+    ts->h_chunk_items.resize(chunk_end.size());
+    for (size_t c = 0; c < chunk_end.size(); c++) {
+        ts->h_chunk_items[c] = (int32_t) (chunk_end[c] - chunk_begin[c]);
+    }
     return 0;
 }
 

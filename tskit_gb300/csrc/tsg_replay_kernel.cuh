@@ -475,8 +475,8 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
 
 // k_eval_grouped: a lane per (chunk, term) with every lane of a warp on terms
 // of one summary type, so the warp runs one code path (a loop specialised
-// to the type for integer numerators); each lane walks its chunk's items in
-// order (no sum crosses lanes).  FP64 with integer summaries: exact
+// to the type for integer numerators), the chunks taken in decreasing item
+// count; each lane walks its chunk's items in order (no sum crosses lanes).  FP64 with integer summaries: exact
 // numerators, about one FP64 fused multiply-add per item and lane (as
 // eval_chunk); otherwise the summary functions in F (FP32: exact item
 // values into a compensated pair).
@@ -506,10 +506,13 @@ __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, 
         const int gs = q.gfirst[g + 1] - q.gfirst[g];
         const int cpw = 32 / gs;
         const int j = lane / gs;
-        const int64_t c = (gw - first) * cpw + j;
-        if (j >= cpw || c >= C) {
+        const int64_t o = (gw - first) * cpw + j;
+        if (j >= cpw || o >= C) {
             continue;
         }
+        // chunks by decreasing item count: the chunks of a warp take about
+        // the same time
+        const int64_t c = ts.c_chunk_order[o];
         const int r = q.gterm[q.gfirst[g] + lane % gs];
         const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
         if (num_form) {
