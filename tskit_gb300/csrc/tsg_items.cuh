@@ -379,6 +379,100 @@ __device__ __forceinline__ double i128_to_double(__int128 v)
         + (double) (unsigned long long) v;
 }
 
+// Exact per-window sums of the sites' integer numerators in one pass (the
+// integer form of k_site_eval + k_site_windows, without the per-site array):
+// a thread per site forms its allele states and each term's numerator
+// summed over its alleles; a warp whose sites all lie in one window adds its
+// exact 128-bit total, else every lane its own, into the window's counter
+// pair (low 32 bits unsigned, the rest signed: the 64-bit atomic adds never
+// carry, so their order does not matter and the sums are exact).
+template <int W, int KQ>
+__global__ void __launch_bounds__(256) k_site_sums(TSView ts, QueryParams q, QueryDev qd, WsDev w)
+{
+    const int64_t site = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
+    const bool valid = site < ts.num_sites;
+    const int R = q.R;
+    int32_t m0 = 0, m1 = 0, A = 1;
+    int64_t wdx = 0;
+    if (valid) {
+        m0 = ts.site_mut[site];
+        m1 = ts.site_mut[site + 1];
+        for (int32_t m = m0; m < m1; m++) {
+            A = max(A, ts.mutation_allele[m] + 1);
+        }
+        wdx = upper_bound(qd.win_site_lo, (int64_t) q.Wn + 1, (int32_t) site) - 1;
+    }
+    const int32_t a0 = q.polarised ? 1 : 0;
+    const int32_t na = valid ? A - a0 : 0;
+    const int64_t w_first = __shfl_sync(0xffffffffu, wdx, 0);
+    const bool one_window = __all_sync(0xffffffffu, !valid || wdx == w_first)
+        && __shfl_sync(0xffffffffu, (int) valid, 0);
+    Pack ps[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        ps[j] = j < na && na <= 4 ? site_allele_state<W, KQ>(ts, q, w, m0, m1, a0 + j) : Pack{0, 0};
+    }
+    unsigned long long *acc = (unsigned long long *) w.site_acc;
+#pragma unroll 1
+    for (int r = 0; r < R; r++) {
+        const Term &t = q.term[r];
+        auto numer = [&](const Pack &x) {
+            int64_t num;
+            term_num(t.type, (int64_t) pk_get<W>(x, t.idx[0]), (int64_t) pk_get<W>(x, t.idx[1]),
+                (int64_t) pk_get<W>(x, t.idx[2]), (int64_t) pk_get<W>(x, t.idx[3]),
+                (int64_t) q.set_size_i[t.idx[0]], (int64_t) q.set_size_i[t.idx[1]],
+                (int64_t) q.set_size_i[t.idx[2]], (int64_t) q.set_size_i[t.idx[3]], num);
+            return num;
+        };
+        __int128 v = 0;
+        if (na <= 4) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (j < na) {
+                    v += numer(ps[j]);
+                }
+            }
+        } else {
+            for (int32_t a = a0; a < A; a++) {
+                v += numer(site_allele_state<W, KQ>(ts, q, w, m0, m1, a));
+            }
+        }
+        auto add = [&](int64_t wi, __int128 x) {
+            unsigned long long *c = acc + 2 * (wi * R + r);
+            const unsigned long long lo = (unsigned long long) x & 0xFFFFFFFFull;
+            const long long hi = (long long) (x >> 32);
+            if (lo) {
+                atomicAdd(c, lo);
+            }
+            if (hi) {
+                atomicAdd(c + 1, (unsigned long long) hi);
+            }
+        };
+        if (one_window) {
+            v = warp_sum_i128(v);
+            if ((threadIdx.x & 31) == 0) {
+                add(w_first, v);
+            }
+        } else if (valid) {
+            add(wdx, v);
+        }
+    }
+}
+
+// The window sums of k_site_sums, each rounded once and scaled by the
+// term's reciprocal denominator.
+__global__ void k_site_sums_finish(QueryParams q, WsDev w)
+{
+    const int64_t total = (int64_t) q.Wn * q.R;
+    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < total;
+         i += (int64_t) gridDim.x * blockDim.x) {
+        const unsigned long long lo = w.site_acc[2 * i];
+        const long long hi = (long long) w.site_acc[2 * i + 1];
+        const __int128 v = ((__int128) hi << 32) + (__int128) lo;
+        w.site_win[i] = i128_to_double(v) * q.inv[i % q.R];
+    }
+}
+
 // Per window: the sum of its sites' summaries for every term, one block of
 // 32 warps per window, warp j taking terms j, j + 32, ...: lanes sum strided
 // sites (term-major, coalesced), then a fixed-order warp reduction; with

@@ -72,6 +72,7 @@ struct WsDev {
     unsigned long long *leaf_area;  // 3 x windows x 2^K patterns: leaf branch areas (fixed point)
     double *leaf_dbl;     // windows x 2^K patterns: the areas
     double *leaf_win;     // windows * R: the leaves' part of the branch sums
+    unsigned long long *site_acc;  // windows x R x 2: exact site-sum counters (integer form)
     uint64_t *cp0;        // (samples + 1) x 2: prefix sums along the first span's order
                           // (compact replay)
     int32_t *err;

@@ -163,59 +163,86 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
 }
 
 // Prefix sums of the sample-set bits along the first span's sample order,
-// P0[i] for i = 0 .. n (two words each), in one block of 1024 threads.
+// P0[i] for i = 0 .. n (two words each): block b takes samples
+// [1024 b, 1024 (b + 1)), first summing every sample before them (a strided
+// sum and a block reduction; the orders are short), then scanning its own.
 template <int KQ>
 __global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams q, QueryDev qd,
     uint64_t *P0)
 {
     __shared__ uint64_t s_w[2 * 32];
+    __shared__ uint64_t s_off[2];
     const int64_t n = ts.num_samples;
     const uint16_t *order = ts.c_order;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nw = (int) (blockDim.x >> 5);
-    uint64_t run_lo = 0, run_hi = 0;
-    for (int64_t base = 0; base < n; base += blockDim.x) {
-        const int64_t i = base + tid;
-        Pack v{0, 0};
-        if (i < n) {
-            v = pk_from_mask<16>(qd.sample_mask[order[i]], q.K);
-        }
-        uint64_t inc_lo = v.lo, inc_hi = v.hi;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
-            const uint64_t b = __shfl_up_sync(0xffffffffu, inc_hi, o);
-            if (lane >= o) {
-                inc_lo += a;
-                inc_hi += b;
-            }
-        }
-        if (lane == 31) {
-            s_w[2 * wid] = inc_lo;
-            s_w[2 * wid + 1] = inc_hi;
-        }
-        __syncthreads();
-        uint64_t wp_lo = 0, wp_hi = 0, tot_lo = 0, tot_hi = 0;
-        for (int j = 0; j < nw; j++) {
-            const uint64_t a = s_w[2 * j], b = s_w[2 * j + 1];
-            if (j < wid) {
-                wp_lo += a;
-                wp_hi += b;
-            }
-            tot_lo += a;
-            tot_hi += b;
-        }
-        if (i < n) {
-            P0[2 * i] = run_lo + wp_lo + inc_lo - v.lo;
-            P0[2 * i + 1] = run_hi + wp_hi + inc_hi - v.hi;
-        }
-        run_lo += tot_lo;
-        run_hi += tot_hi;
-        __syncthreads();
+    const int64_t base = (int64_t) blockIdx.x * blockDim.x;
+    // the samples before this block
+    uint64_t pre_lo = 0, pre_hi = 0;
+    for (int64_t i = tid; i < base && i < n; i += blockDim.x) {
+        const Pack v = pk_from_mask<16>(qd.sample_mask[order[i]], q.K);
+        pre_lo += v.lo;
+        pre_hi += v.hi;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        pre_lo += __shfl_xor_sync(0xffffffffu, pre_lo, o);
+        pre_hi += __shfl_xor_sync(0xffffffffu, pre_hi, o);
+    }
+    if (lane == 0) {
+        s_w[2 * wid] = pre_lo;
+        s_w[2 * wid + 1] = pre_hi;
+    }
+    __syncthreads();
     if (tid == 0) {
-        P0[2 * n] = run_lo;
-        P0[2 * n + 1] = run_hi;
+        uint64_t a = 0, b = 0;
+        for (int j = 0; j < nw; j++) {
+            a += s_w[2 * j];
+            b += s_w[2 * j + 1];
+        }
+        s_off[0] = a;
+        s_off[1] = b;
+    }
+    __syncthreads();
+    const uint64_t run_lo = s_off[0], run_hi = s_off[1];
+    // this block's samples
+    const int64_t i = base + tid;
+    Pack v{0, 0};
+    if (i < n) {
+        v = pk_from_mask<16>(qd.sample_mask[order[i]], q.K);
+    }
+    uint64_t inc_lo = v.lo, inc_hi = v.hi;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
+        const uint64_t b = __shfl_up_sync(0xffffffffu, inc_hi, o);
+        if (lane >= o) {
+            inc_lo += a;
+            inc_hi += b;
+        }
+    }
+    __syncthreads();
+    if (lane == 31) {
+        s_w[2 * wid] = inc_lo;
+        s_w[2 * wid + 1] = inc_hi;
+    }
+    __syncthreads();
+    uint64_t wp_lo = 0, wp_hi = 0, tot_lo = 0, tot_hi = 0;
+    for (int j = 0; j < nw; j++) {
+        const uint64_t a = s_w[2 * j], b = s_w[2 * j + 1];
+        if (j < wid) {
+            wp_lo += a;
+            wp_hi += b;
+        }
+        tot_lo += a;
+        tot_hi += b;
+    }
+    if (i < n) {
+        P0[2 * i] = run_lo + wp_lo + inc_lo - v.lo;
+        P0[2 * i + 1] = run_hi + wp_hi + inc_hi - v.hi;
+    }
+    if (tid == 0 && base + (int64_t) blockDim.x >= n) {
+        P0[2 * n] = run_lo + tot_lo;
+        P0[2 * n + 1] = run_hi + tot_hi;
     }
 }
 

@@ -1127,6 +1127,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up(ts->v.num_chunks * R * 8, 256);                        // dD (per chunk)
         bytes += align_up(ts->v.num_nodes * 4, 256);                             // node_mask
         bytes += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);          // site_val
+        bytes += align_up((p.site && p.site_int ? (int64_t) Wn : 0) * R * 16, 256);    // site_acc
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // site_win
         bytes += align_up(q->gstate ? q->smem_grid * q->slot_bytes : 0, 256);    // node state
         bytes += align_up(q->smem_grid * L * 4, 256);                            // seek counters
@@ -1670,6 +1671,7 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.site_val = nullptr;
     w.site_win = nullptr;
     w.cp0 = nullptr;
+    w.site_acc = nullptr;
     if (q->smem) {
         const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
         w.items = b + off;
@@ -1684,6 +1686,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up(ts->v.num_nodes * 4, 256);
         w.site_val = (double *) (b + off);
         off += align_up((p.site ? ts->v.num_sites : 0) * R * 8, 256);
+        w.site_acc = (unsigned long long *) (b + off);
+        off += align_up((p.site && p.site_int ? (int64_t) p.Wn : 0) * R * 16, 256);
         w.site_win = (double *) (b + off);
         off += align_up((int64_t) p.Wn * R * 8, 256);
         w.state = b + off;
@@ -1851,10 +1855,11 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             // at a time, then every chunk's item values
             const int kq = q->KQ;
             if (p.branch && ts->v.c_num_anchors > 0) {
+                const unsigned gp = (unsigned) ((ts->v.num_samples + 1023) / 1024);
                 if (kq == 1) {
-                    k_compact_prefix<1><<<1, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                    k_compact_prefix<1><<<gp, 1024, 0, st>>>(ts->v, p, d, w.cp0);
                 } else {
-                    k_compact_prefix<2><<<1, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                    k_compact_prefix<2><<<gp, 1024, 0, st>>>(ts->v, p, d, w.cp0);
                 }
                 TSG_LAUNCHED();
                 const unsigned ga = (unsigned) grid_for(ts->v.c_num_anchors);
@@ -1924,7 +1929,20 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             }
             TSG_LAUNCHED();
         }
-        if (p.site && ts->v.num_sites > 0) {
+        if (p.site && p.site_int && ts->v.num_sites > 0) {
+            // integer numerators summed exactly per window in one pass
+            TSG_CUDA(cudaMemsetAsync(w.site_acc, 0, (size_t) p.Wn * R * 16, st));
+            const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
+            switch (form) {
+                case 0: k_site_sums<16, 1><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
+                case 1: k_site_sums<16, 2><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
+                case 2: k_site_sums<32, 1><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
+                default: k_site_sums<32, 2><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
+            }
+            TSG_LAUNCHED();
+            k_site_sums_finish<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
+            TSG_LAUNCHED();
+        } else if (p.site && ts->v.num_sites > 0) {
             const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
             switch (form) {
                 case 0: k_site_eval<TSG_ITEM_RMAX, 16, 1><<<gsite, 256, 0, st>>>(ts->v, p, w); break;
@@ -1934,7 +1952,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             }
             TSG_LAUNCHED();
         }
-        if (p.site) {
+        if (p.site && !(p.site_int && ts->v.num_sites > 0)) {
             if (ts->v.num_sites > 0) {
                 k_site_windows<<<(unsigned) p.Wn, 1024, 0, st>>>(p, d, w,
                     ts->v.num_sites, p.site_int);
