@@ -356,13 +356,29 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
-    p = os.path.join(REPO, "profiles", "sweep_pipeline_windowed_n10k.json")
+    """DRAM bytes (read + write) of one compact replay launch on this
+    workload, from the committed ncu summary, if any."""
+    p = os.path.join(REPO, "profiles", "replay_compact_windowed_n10k.json")
     try:
         with open(p) as f:
             return json.load(f).get("dram_bytes_per_launch")
     except Exception:
         return None
+
+
+def replay_algorithmic_bytes(tables, plan, kq=1):
+    """Compulsory bytes of one compact replay launch (k_replay_compact):
+    per edge its insertion and removal encodings (16) and at most one leaf
+    mask per event (8); per tree its event, mutation and item ranges (40); per
+    mutation its encoding (4) and the counts written under it (8 per count
+    word); per span its depth-first sample order (2 per sample), sample-range
+    endpoints (8 each) and start parents (2 per node); every item written
+    (16 per count word + 16); the samples' set masks (4 each)."""
+    E, M = tables.num_edges, tables.num_mutations
+    n = len(tables.samples())
+    return (24 * E + 40 * plan["num_trees"] + (4 + 8 * kq) * M
+            + 2 * n * plan["num_compact_spans"] + 8 * plan["compact_endpoints"]
+            + 2 * plan["compact_nodes"] + (16 * kq + 16) * plan["num_items"] + 4 * n)
 
 
 def run_gpu(args):
@@ -417,18 +433,22 @@ def run_gpu(args):
         q, ws, res = prepare(ts, precision)
         ev_sweep0 = torch.cuda.Event(enable_timing=True)
         ev_sweep1 = torch.cuda.Event(enable_timing=True)
+        ev_rep0 = torch.cuda.Event(enable_timing=True)
+        ev_rep1 = torch.cuda.Event(enable_timing=True)
         # torch creates the CUDA events on first record; the library
-        # re-records them around the sweep kernels of every launch
-        ev_sweep0.record(stream)
-        ev_sweep1.record(stream)
+        # re-records them around the sweep kernels and around the replay
+        # kernel of every launch
+        for ev in (ev_sweep0, ev_sweep1, ev_rep0, ev_rep1):
+            ev.record(stream)
         torch.cuda.synchronize()
         lib.tsg_query_set_sweep_events(q.handle, ev_sweep0.cuda_event, ev_sweep1.cuda_event)
+        lib.tsg_query_set_replay_events(q.handle, ev_rep0.cuda_event, ev_rep1.cuda_event)
         for _ in range(args.warmup):
             flush.zero_()
             q.launch(ws, res, stream)
         torch.cuda.synchronize()
         q.check(ws)
-        step_ms, sweep_ms = [], []
+        step_ms, sweep_ms, rep_ms = [], [], []
         launches0 = lib.tsg_launch_count()
         if world > 1:
             torch.distributed.barrier()
@@ -447,6 +467,7 @@ def run_gpu(args):
                 torch.cuda.synchronize()
                 step_ms.append(e0.elapsed_time(e1))
                 sweep_ms.append(ev_sweep0.elapsed_time(ev_sweep1))
+                rep_ms.append(ev_rep0.elapsed_time(ev_rep1))
             torch.cuda.synchronize()
         finally:
             if sampler is not None:
@@ -455,15 +476,16 @@ def run_gpu(args):
         q.check(ws)
         raw = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
         return (max_over_ranks(float(np.mean(step_ms)), world), float(np.mean(sweep_ms)),
-                launches, raw, sampler)
+                launches, raw, sampler, float(np.mean(rep_ms)))
 
     # the headline: one fused sweep at the reference's precision (FP64 window
     # and running sums; summaries as exact integer numerators with about one
     # FP64 fused multiply-add per item)
-    ms, sweep, launches, raw_batched, clocks = timed_fused("f64", args.steps, with_clocks=True)
+    ms, sweep, launches, raw_batched, clocks, rep = timed_fused("f64", args.steps,
+                                                                 with_clocks=True)
     value = world * logical / (ms / 1e3)
     # the FP32-compensated form of the same sweep
-    ms32, sweep32, _, raw_f32, _ = timed_fused("f32", max(3, min(args.steps, 10)))
+    ms32, sweep32, _, raw_f32, _, _ = timed_fused("f32", max(3, min(args.steps, 10)))
 
     # plain FP64 per-query form: one launch per low-level call, FP64 throughout
     plain = []
@@ -528,6 +550,9 @@ def run_gpu(args):
     peaks, peak_kind = measured_peaks()
     algo = algorithmic_bytes(tables, sets, len(terms))
     achieved = algo / (sweep / 1e3) / 1e9
+    plan = ts.plan_sizes()
+    rep_algo = replay_algorithmic_bytes(tables, plan)
+    rep_achieved = rep_algo / (rep / 1e3) / 1e9
     line = {
         "metric": "edge-updates/s",
         "value": value,
@@ -563,16 +588,25 @@ def run_gpu(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {
             "bound": "hbm",
-            "achieved": achieved,
+            "achieved": rep_achieved,
             "peak": peaks["hbm_gbs"],
             "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"],
+            "frac": rep_achieved / peaks["hbm_gbs"],
             "traffic": profile_traffic(),
-            "kernel": "sweep pipeline (every kernel of one fused launch from the node masks "
-                      "to the window reduction), timed between events on the launch stream",
-            "algorithmic_bytes_per_launch": algo,
-            "kernel_ms": sweep,
+            "kernel": "k_replay_compact (the dominant kernel), timed between events on the "
+                      "launch stream around it",
+            "algorithmic_bytes_per_launch": rep_algo,
+            "kernel_ms": rep,
             "peak_source": peak_kind,
+            "plan": plan,
+        },
+        "pipeline": {
+            "kernel_ms": sweep,
+            "algorithmic_bytes_per_launch": algo,
+            "achieved_gbs": achieved,
+            "frac": achieved / peaks["hbm_gbs"],
+            "note": "every kernel of one fused launch from the node masks to the site sums, "
+                    "against the traversal's compulsory bytes",
         },
         "gpu_launches": launches,
         "clocks": clocks.summary(),

@@ -167,6 +167,12 @@ int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts);
  * serving); queries prepared before must not run concurrently with it.
  * Results do not depend on the span count. */
 int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts);
+/* Sizes of the tree sequence's replay plans (no reference counterpart; for
+ * measuring): sizes[0..7] = trees, spans of the general plan, spans of the
+ * compact plan, compact nodes over all spans, their sample-range endpoints,
+ * replay items, evaluation chunks, first-tree items of the compact plan (the
+ * compact entries 0 without a compact plan). */
+int tsg_treeseq_get_plan_sizes(const tsg_treeseq_t *ts, int64_t *sizes);
 int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans);
 /* breakpoints: host array of num_trees + 1 doubles */
 int tsg_treeseq_get_breakpoints(const tsg_treeseq_t *ts, double *breakpoints);
@@ -424,6 +430,10 @@ int tsg_query_launch(const tsg_query_t *query, tsg_workspace_t *ws, double *resu
  * launch stream immediately before and after the sweep kernel of every later
  * launch of `query`, so callers can time the dominant kernel alone. */
 int tsg_query_set_sweep_events(tsg_query_t *query, void *start_event, void *stop_event);
+/* The same around the replay kernel alone (the compact replay, or the
+ * general replay with its item values) of every later launch: the pipeline's
+ * dominant kernel. */
+int tsg_query_set_replay_events(tsg_query_t *query, void *start_event, void *stop_event);
 /* Synchronous read of the device-side check word left by the last launch of
  * `query` on `ws`: 0, or TSG_ERR_DEVICE_CHECK when a kernel found an
  * inconsistent tree sequence (node id out of range, a cycle). */

@@ -110,6 +110,7 @@ SIGNATURES = {
     "tsg_treeseq_get_num_samples": (_I64, [_P]),
     "tsg_treeseq_get_num_spans": (_I64, [_P]),
     "tsg_treeseq_get_num_compact_spans": (_I64, [_P]),
+    "tsg_treeseq_get_plan_sizes": (ctypes.c_int, [_P, _P]),
     "tsg_treeseq_set_compact_spans": (ctypes.c_int, [_P, _I64]),
     "tsg_treeseq_get_breakpoints": (ctypes.c_int, [_P, _P]),
     "tsg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
@@ -167,6 +168,7 @@ SIGNATURES = {
     "tsg_query_result_size": (_I64, [_P]),
     "tsg_query_launch": (ctypes.c_int, [_P, _P, _P, _P]),
     "tsg_query_set_sweep_events": (ctypes.c_int, [_P, _P, _P]),
+    "tsg_query_set_replay_events": (ctypes.c_int, [_P, _P, _P]),
     "tsg_workspace_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "tsg_workspace_reserve": (ctypes.c_int, [_P, _I64]),
     "tsg_workspace_bytes": (_I64, [_P]),

@@ -486,6 +486,8 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     v.c_num_anchors = (int64_t) a_par.size();
     v.c_max_local = max_local;
     v.c_num_spans = NC;
+    ts->h_compact_nodes = local_off[(size_t) NC];
+    ts->h_compact_endpoints = ep_off[(size_t) NC];
     return 0;
 }
 

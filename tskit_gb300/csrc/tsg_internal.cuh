@@ -222,6 +222,8 @@ struct tsg_treeseq {
     int64_t h_tree_item0 = 0;  // the first tree's items
     std::vector<int64_t> h_tree_chunk_off;  // num_trees + 1: first chunk of each tree
     std::vector<int32_t> h_chunk_items;     // items of each evaluation chunk
+    int64_t h_compact_nodes = 0;            // compact plan: nodes over all spans
+    int64_t h_compact_endpoints = 0;        // compact plan: sample-range endpoints
     tsg::HostTopology host;    // host copy of the topology (span plan, genotype decoding)
     // device allocations owned by this object
     std::vector<void *> owned;

@@ -608,6 +608,7 @@ struct tsg_query {
     int64_t off[12];         // offsets in the image: mask, windows, wlo, woff, wsl, wsh, wsite,
                              // time windows (allele frequency spectrum)
     cudaEvent_t ev_start, ev_stop;  // optional events around the sweep kernel
+    cudaEvent_t ev_rstart = nullptr, ev_rstop = nullptr;  // ... around the replay kernel
     int64_t total_span_windows;
     int64_t total_seg_windows;  // window segments x windows they overlap (item pipeline)
     int64_t num_slots;
@@ -1781,6 +1782,13 @@ int tsg_query_set_sweep_events(tsg_query_t *q, void *start_event, void *stop_eve
     return 0;
 }
 
+int tsg_query_set_replay_events(tsg_query_t *q, void *start_event, void *stop_event)
+{
+    q->ev_rstart = (cudaEvent_t) start_event;
+    q->ev_rstop = (cudaEvent_t) stop_event;
+    return 0;
+}
+
 int tsg_workspace_create(tsg_workspace_t **ws)
 {
     *ws = new tsg_workspace_t();
@@ -1876,10 +1884,16 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TSG_COMPACT_THREADS, csb);
             const unsigned cg = (unsigned) std::min<int64_t>(
                 (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()), ts->v.c_num_spans);
+            if (q->ev_rstart != nullptr) {
+                TSG_CUDA(cudaEventRecord(q->ev_rstart, st));
+            }
             if (kq == 1) {
                 k_replay_compact<1><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
             } else {
                 k_replay_compact<2><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
+            }
+            if (q->ev_rstop != nullptr) {
+                TSG_CUDA(cudaEventRecord(q->ev_rstop, st));
             }
             if (p.branch) {
                 // two kernels: the items' branch lengths, then their values
@@ -1895,12 +1909,18 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             }
         } else if (p.branch) {
             // replay and item values in one kernel
+            if (q->ev_rstart != nullptr) {
+                TSG_CUDA(cudaEventRecord(q->ev_rstart, st));
+            }
             if (p.f32) {
                 (p.polarised ? launch_replay_eval_f32_pol : launch_replay_eval_f32_unpol)(form, g, sb,
                     q->slot_bytes, st, ts->v, p, d, w);
             } else {
                 (p.polarised ? launch_replay_eval_f64_pol : launch_replay_eval_f64_unpol)(form, g, sb,
                     q->slot_bytes, st, ts->v, p, d, w);
+            }
+            if (q->ev_rstop != nullptr) {
+                TSG_CUDA(cudaEventRecord(q->ev_rstop, st));
             }
         } else {
             switch (form) {

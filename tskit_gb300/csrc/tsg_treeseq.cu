@@ -499,6 +499,23 @@ int64_t tsg_treeseq_get_num_samples(const tsg_treeseq_t *ts) { return ts->v.num_
 int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts) { return ts->v.num_spans; }
 int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts) { return ts->v.c_num_spans; }
 
+int tsg_treeseq_get_plan_sizes(const tsg_treeseq_t *ts, int64_t *sizes)
+{
+    if (ts == nullptr || sizes == nullptr) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    const bool c = ts->v.c_num_spans > 0;
+    sizes[0] = ts->v.num_trees;
+    sizes[1] = ts->v.num_spans;
+    sizes[2] = ts->v.c_num_spans;
+    sizes[3] = c ? ts->h_compact_nodes : 0;
+    sizes[4] = c ? ts->h_compact_endpoints : 0;
+    sizes[5] = ts->v.num_items;
+    sizes[6] = ts->v.num_chunks;
+    sizes[7] = c ? ts->v.c_num_anchors : 0;
+    return 0;
+}
+
 int tsg_treeseq_set_compact_spans(tsg_treeseq_t *ts, int64_t num_spans)
 {
     if (ts == nullptr || num_spans < -1) {

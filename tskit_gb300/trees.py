@@ -318,6 +318,14 @@ class TreeSequence:
         sample-count statistics)."""
         return self._lib.tsg_treeseq_get_num_compact_spans(self._handle)
 
+    def plan_sizes(self):
+        """Sizes of the replay plans (tsg_treeseq_get_plan_sizes)."""
+        out = np.zeros(8, dtype=np.int64)
+        nat.check(self._lib.tsg_treeseq_get_plan_sizes(self._handle, _ptr(out)))
+        keys = ("num_trees", "num_spans", "num_compact_spans", "compact_nodes",
+                "compact_endpoints", "num_items", "num_chunks", "num_anchors")
+        return dict(zip(keys, (int(v) for v in out)))
+
     def set_compact_spans(self, num_spans):
         """Rebuild the compact replay plan with about ``num_spans`` spans (-1:
         the default count; 0: use the general replay); returns the span count
