@@ -44,10 +44,7 @@ TSG_REPLAY_EVAL_LAUNCHER(TSG_EVAL_NAME)
 TSG_CHUNK_EVAL_LAUNCHER(TSG_CHUNKS_NAME)
 {
     const int64_t C = v.num_chunks;
-    int64_t total = 0;
-    for (int g = 0; g < p.ngroups; g++) {
-        total += group_warps(p, C, g);
-    }
+    const int64_t total = (C + TSG_EVAL_BLOCK - 1) / TSG_EVAL_BLOCK * p.gwpb;
     const unsigned gb = (unsigned) std::min<int64_t>((C + 7) / 8, 1 << 20);
     const unsigned ge = (unsigned) std::min<int64_t>((total + 7) / 8, 1 << 20);
     if (kq == 1) {

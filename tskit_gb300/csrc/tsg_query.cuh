@@ -31,7 +31,15 @@ struct QueryParams {
     int32_t ngroups;
     int32_t gfirst[TSG_MAX_OUTPUTS + 1];
     int32_t gterm[TSG_MAX_OUTPUTS];
+    // the warps of one block of TSG_EVAL_BLOCK chunks: warp `sub` of a block
+    // takes group gw_group[sub], lanes gw_k[sub] * 32 .. of its (chunk, term)
+    // pairs
+    int32_t gwpb;
+    int32_t gw_group[TSG_MAX_OUTPUTS];
+    int32_t gw_k[TSG_MAX_OUTPUTS];
 };
+// chunks per block of the grouped item evaluation
+#define TSG_EVAL_BLOCK 8
 
 struct QueryDev {
     const uint32_t *sample_mask;  // per sample index: bit k = member of set k

@@ -397,16 +397,6 @@ __global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDe
     }
 }
 
-// Warps of the grouped evaluation of a query: each warp takes one group of
-// terms of one summary type (q.gfirst / q.gterm) over 32 / (group size)
-// consecutive chunks.
-__host__ __device__ __forceinline__ int64_t group_warps(const QueryParams &q, int64_t C, int g)
-{
-    const int gs = q.gfirst[g + 1] - q.gfirst[g];
-    const int cpw = 32 / gs;
-    return (C + cpw - 1) / cpw;
-}
-
 // A summary term's integer numerator with its type fixed at compile time
 // (term_num32's cases), plus the same at n - x when unpolarised.
 template <int TYPE, bool UNPOL>
@@ -475,8 +465,9 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
 
 // k_eval_grouped: a lane per (chunk, term) with every lane of a warp on terms
 // of one summary type, so the warp runs one code path (a loop specialised
-// to the type for integer numerators), the chunks taken in decreasing item
-// count; each lane walks its chunk's items in order (no sum crosses lanes).  FP64 with integer summaries: exact
+// to the type for integer numerators); the chunks are taken in decreasing
+// item count, TSG_EVAL_BLOCK at a time by q.gwpb consecutive warps; each lane
+// walks its chunk's items in order (no sum crosses lanes).  FP64 with integer summaries: exact
 // numerators, about one FP64 fused multiply-add per item and lane (as
 // eval_chunk); otherwise the summary functions in F (FP32: exact item
 // values into a compensated pair).
@@ -494,26 +485,22 @@ __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, 
     const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
     for (int64_t gw = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
          gw < total_warps; gw += nwarps) {
-        int g = 0;
-        int64_t first = 0;
-        for (; g + 1 < q.ngroups; g++) {
-            const int64_t nw = group_warps(q, C, g);
-            if (gw < first + nw) {
-                break;
-            }
-            first += nw;
-        }
+        // consecutive warps share a block of chunks, so a chunk's items are
+        // read by the type groups while they are still in cache
+        const int64_t blk = gw / q.gwpb;
+        const int sub = (int) (gw % q.gwpb);
+        const int g = q.gw_group[sub];
         const int gs = q.gfirst[g + 1] - q.gfirst[g];
-        const int cpw = 32 / gs;
-        const int j = lane / gs;
-        const int64_t o = (gw - first) * cpw + j;
-        if (j >= cpw || o >= C) {
+        const int pos = q.gw_k[sub] * 32 + lane;
+        const int j = pos / gs;
+        const int64_t o = blk * TSG_EVAL_BLOCK + j;
+        if (j >= TSG_EVAL_BLOCK || o >= C) {
             continue;
         }
         // chunks by decreasing item count: the chunks of a warp take about
         // the same time
         const int64_t c = ts.c_chunk_order[o];
-        const int r = q.gterm[q.gfirst[g] + lane % gs];
+        const int r = q.gterm[q.gfirst[g] + pos % gs];
         const int64_t b = ts.chunk_begin[c], e = ts.chunk_end[c];
         if (num_form) {
             const Term t = q.term[r];

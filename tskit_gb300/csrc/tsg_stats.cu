@@ -971,6 +971,16 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
             }
         }
         p.gfirst[p.ngroups] = at;
+        p.gwpb = 0;
+        for (int g = 0; g < p.ngroups; g++) {
+            const int gs = p.gfirst[g + 1] - p.gfirst[g];
+            const int nw = (TSG_EVAL_BLOCK * gs + 31) / 32;
+            for (int k = 0; k < nw && p.gwpb < TSG_MAX_OUTPUTS; k++) {
+                p.gw_group[p.gwpb] = g;
+                p.gw_k[p.gwpb] = k;
+                p.gwpb++;
+            }
+        }
     }
     p.inv_K = 1.0 / (double) K;
     for (uint64_t k = 0; k < K; k++) {
