@@ -49,6 +49,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["f64", "f32"], default=None,
+                    help="profiling mode: only warmup + steps launches of the headline fused "
+                         "query in this arithmetic (default compact plan, no tuning, no other "
+                         "legs), for ncu captures")
     ap.add_argument("--workload", default=WORKLOAD,
                     choices=[WORKLOAD, "afs_n200k", "grm_n20k", "serve_mix"],
                     help="the headline workload (default) or one of the other "
@@ -977,8 +981,35 @@ def run_serve_mix(args):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    """--profile: the headline query alone, warmup + steps launches."""
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _build
+
+    torch.cuda.set_device(0)
+    _build.build_all()
+    tables, sets, windows = make_workload()
+    terms, _, _ = term_list()
+    ts = tskit_gb300.TreeSequence(tables)
+    q = ts.query(sets, terms, windows=windows, both_modes=True, span_normalise=False,
+                 precision=args.profile)
+    ws = tskit_gb300.Workspace(q.workspace_bytes)
+    res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup + args.steps):
+        q.launch(ws, res)
+    torch.cuda.synchronize()
+    q.check(ws)
+    print(json.dumps({"profile": args.profile, "launches": args.warmup + args.steps,
+                      "plan": ts.plan_sizes()}))
+
+
 def main():
     args = parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.workload == "afs_n200k":
         run_afs_n200k(args)
     elif args.workload == "grm_n20k":
