@@ -46,6 +46,12 @@ extern "C" {
 /* Run the item pipeline with its span node state in global memory (32-bit
  * counts) even when it fits in shared memory (for testing that form). */
 #define TSG_FORCE_GLOBAL_STATE (1u << 23)
+/* For testing the bounded device waits: the evaluating warps of the general
+ * replay (tree sequences without a compact plan) give up their wait for the
+ * replay at once instead of after 2^27 polls, so a launch
+ * records TSG_ERR_DEVICE_CHECK in its check word (its result is then not
+ * valid) and returns normally; the next launch without the bit is clean. */
+#define TSG_TEST_WAIT_EXPIRES (1u << 24)
 
 /* tsg_treeseq_init options */
 #define TSG_TABLES_ON_DEVICE (1u << 0)

@@ -22,6 +22,7 @@ STAT_BOTH_MODES = 1 << 20
 PRECISION_F32_KAHAN = 1 << 21
 FORCE_GLOBAL_SWEEP = 1 << 22
 FORCE_GLOBAL_STATE = 1 << 23
+TEST_WAIT_EXPIRES = 1 << 24
 TABLES_ON_DEVICE = 1 << 0
 TIME_UNCALIBRATED = 1 << 1
 

@@ -15,6 +15,7 @@ struct QueryParams {
     int32_t branch, site, polarised, f32, need_mean;
     int32_t site_int;  // site summaries from exact integer numerators (term_num)
     int32_t num_slots;
+    uint32_t spin_limit;  // polls of a bounded wait before it gives up
     double inv_K;
     double set_size[TSG_MAX_SAMPLE_SETS];
     int32_t set_size_i[TSG_MAX_SAMPLE_SETS];  // the same as integers (integer kernels)

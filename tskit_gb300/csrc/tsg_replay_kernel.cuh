@@ -353,7 +353,7 @@ __device__ __forceinline__ void eval_span_chunks(const TSView &ts, const QueryPa
         }
         const int32_t tc = ts.chunk_tree[c];
         for (uint32_t spin = 0; *(volatile int *) s_ready < tc; spin++) {
-            if (spin > TSG_REPLAY_SPIN_LIMIT) {
+            if (spin >= q.spin_limit) {
                 dev_error(w.err, DEV_WAIT_TIMEOUT);
                 break;
             }

@@ -874,6 +874,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     p.site = site;
     p.polarised = !!(options & TSG_STAT_POLARISED);
     p.f32 = !!(options & TSG_PRECISION_F32_KAHAN);
+    p.spin_limit = (options & TSG_TEST_WAIT_EXPIRES) ? 0u : (uint32_t) TSG_REPLAY_SPIN_LIMIT;
     for (uint64_t k = 0; k < K; k++) {
         p.set_size[k] = (double) sizes[k];
         p.set_size_i[k] = (int32_t) sizes[k];

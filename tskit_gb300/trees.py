@@ -13,13 +13,13 @@ sweep whose summary terms are the same functions.
 from __future__ import annotations
 
 import ctypes
-import dataclasses
 import math
 import numbers
 
 import numpy as np
 
 from . import _native as nat
+from .pca import PCAResult  # noqa: F401 (re-exported)
 from .tables import Tables
 
 
@@ -68,19 +68,6 @@ def _parse_mode(mode):
 
 def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size > 0 else None
-
-
-@dataclasses.dataclass
-class PCAResult:
-    """The result of TreeSequence.pca (python/tskit/trees.py:11500-11535):
-    factors (orthonormal columns, one row per sample or individual),
-    eigenvalues of the relatedness matrix, the range sketch (a starting
-    point for a further call) and the randomized algorithm's error bound."""
-
-    factors: np.ndarray
-    eigenvalues: np.ndarray
-    range_sketch: np.ndarray
-    error_bound: np.ndarray
 
 
 class Workspace:
@@ -978,42 +965,11 @@ class TreeSequence:
             W, Z, mode=mode, span_normalise=span_normalise)
 
     # ------------------------------------------------------------------ pca
-    def _expand_indices(self, x, indices):
-        """python/tskit/trees.py:9220-9224 (rows placed by node id)."""
-        y = np.zeros((self.num_samples, x.shape[1]))
-        y[indices] = x
-        return y
-
-    def _genetic_relatedness_vector_node(self, arr, indices, mode, centre=True, windows=None):
-        """python/tskit/trees.py:9226-9246: the unnormalised relatedness of
-        the nodes ``indices`` times ``arr``, centred in both directions."""
-        x = arr - arr.mean(axis=0) if centre else arr
-        x = self._expand_indices(x, indices)
-        x = self.genetic_relatedness_vector(W=x, windows=windows, mode=mode, centre=False,
-                                            nodes=indices, span_normalise=False)[0]
-        return x - x.mean(axis=0) if centre else x
-
     def _individual_nodes(self, i):
         ni = self.tables.node_individual
         if ni is None or not (0 <= int(i) < self.tables.num_individuals):
             raise ValueError(f"Individual {i} out of bounds")
         return np.flatnonzero(ni == int(i))
-
-    def _genetic_relatedness_vector_individual(self, arr, indices, mode, centre=True,
-                                               windows=None):
-        """python/tskit/trees.py:9248-9282: as the node form, with each
-        individual the average of its nodes."""
-        ij = np.vstack([[n, k] for k, i in enumerate(indices) for n in self._individual_nodes(i)])
-        samples, sample_individuals = ij[:, 0], ij[:, 1]
-        ploidy = np.bincount(sample_individuals)
-        x = arr - arr.mean(axis=0) if centre else arr
-        x = x[sample_individuals] / ploidy[sample_individuals, np.newaxis]
-        x = self._expand_indices(x, samples)
-        x = self.genetic_relatedness_vector(W=x, windows=windows, mode=mode, centre=False,
-                                            nodes=samples, span_normalise=False)[0]
-        x = np.apply_along_axis(lambda w: np.bincount(sample_individuals, w) / ploidy,
-                                axis=0, arr=x)
-        return x - x.mean(axis=0) if centre else x
 
     def _decapitated(self, time):
         """This tree sequence's topology younger than ``time`` on the device
@@ -1026,106 +982,16 @@ class TreeSequence:
             time_windows=None, mode="branch", centre=True, num_iterations=5,
             num_oversamples=None, random_seed=None, range_sketch=None):
         """python/tskit/trees.py:9284-9537: principal components of the
-        genetic relatedness matrix by randomized SVD (Algorithms 8 and 9 of
-        Martinsson and Tropp, arXiv:2002.01387), every product with the
-        matrix one relatedness matrix-vector sweep on the GPU; the same
-        arguments, checks, random sketch and result as the reference."""
-        if (not isinstance(num_iterations, int)) or num_iterations < 1:
-            raise ValueError("num_iterations should be a positive integer.")
-        if samples is None and individuals is None:
-            samples = self.samples()
-        if samples is not None and individuals is not None:
-            raise ValueError("Samples and individuals cannot be used at the same time")
-        elif samples is not None:
-            output_type = "node"
-            dim = len(samples)
-        else:
-            output_type = "individual"
-            dim = len(individuals)
-        if time_windows is None:
-            ts_low, ts_high = None, self
-        else:
-            assert time_windows[0] < time_windows[1], "The second argument should be larger."
-            ts_low, ts_high = self._decapitated(time_windows[0]), self._decapitated(time_windows[1])
-        drop_windows = windows is None
-        windows = self.parse_windows(windows)
-        num_windows = len(windows) - 1
-        if num_windows < 1:
-            raise ValueError("Must have at least one window.")
-        if num_components > dim:
-            raise ValueError(
-                "Number of components must be less than or equal to "
-                "the number of samples (or individuals, if specified).")
-        if num_oversamples is not None and range_sketch is not None:
-            raise ValueError("Cannot specify both num_oversamples and range_sketch.")
-        if range_sketch is None:
-            if num_oversamples is None:
-                num_oversamples = min(10, dim - num_components)
-            rng = np.random.default_rng(random_seed)
-            range_sketch = rng.normal(size=(num_windows, dim, num_components + num_oversamples))
-        else:
-            if drop_windows:
-                range_sketch = np.expand_dims(range_sketch, 0)
-            if range_sketch.shape[-1] < num_components:
-                raise ValueError(
-                    "range_sketch must have at least as many columns as num_components")
-            num_oversamples = range_sketch.shape[-1] - num_components
-        num_vectors = num_components + num_oversamples
-        if num_vectors > dim:
-            raise ValueError(
-                "Number of columns in range_sketch "
-                "(num_components + num_oversamples) must be less"
-                " than or equal to the number of samples"
-                " (or individuals, if specified).")
-        rs_exp_dims = (num_windows, dim, num_vectors)
-        rs_obs_dims = range_sketch.shape
-        if rs_obs_dims != rs_exp_dims:
-            if drop_windows:
-                rs_obs_dims, rs_exp_dims = rs_obs_dims[1:], rs_exp_dims[1:]
-            raise ValueError(
-                f"Incorrect shape of range_sketch: expected {rs_exp_dims}; got {rs_obs_dims}.")
+        genetic relatedness matrix by randomized SVD (tskit_gb300.pca), every
+        product with the matrix one relatedness matrix-vector sweep on the
+        GPU."""
+        from . import pca as _pca
 
-        def range_finder(operator, depth, Q):
-            for _ in range(depth):
-                Q = np.linalg.qr(Q)[0]
-                Q = operator(Q)
-            return np.linalg.qr(Q)[0]
-
-        def rand_svd(operator, operator_dim, rank, depth, sketch):
-            Q = range_finder(operator, depth, sketch)
-            C = operator(Q).T
-            U_hat, D, _ = np.linalg.svd(C, full_matrices=False)
-            U = Q @ U_hat
-            error_factor = np.power(1 + 4 * np.sqrt(2 * operator_dim / max(1, (rank - 1))),
-                                    1 / (2 * depth + 1))
-            error_bound = D[rank] * (1 + error_factor)
-            return U[:, :rank], D[:rank], Q, error_bound
-
-        def vec(ts):
-            if output_type == "node":
-                return ts._genetic_relatedness_vector_node
-            return ts._genetic_relatedness_vector_individual
-
-        indices = samples if output_type == "node" else individuals
-        U = np.empty((num_windows, dim, num_components))
-        D = np.empty((num_windows, num_components))
-        Q = np.empty((num_windows, dim, num_vectors))
-        E = np.empty(num_windows)
-        for i in range(num_windows):
-            def G(x, i=i):
-                high = vec(ts_high)(arr=x, indices=indices, mode=mode, centre=centre,
-                                    windows=windows[i:i + 2])
-                if time_windows is None:
-                    return high
-                low = vec(ts_low)(arr=x, indices=indices, mode=mode, centre=centre,
-                                  windows=windows[i:i + 2])
-                return high - low
-
-            U[i], D[i], Q[i], E[i] = rand_svd(G, dim, num_components, num_iterations,
-                                              range_sketch[i])
-        if drop_windows:
-            U, D, Q, E = U[0], D[0], Q[0], E[0]
-        return PCAResult(factors=U, eigenvalues=D, range_sketch=Q, error_bound=E)
+        return _pca.pca(self, num_components, windows=windows, samples=samples,
+                        individuals=individuals, time_windows=time_windows, mode=mode,
+                        centre=centre, num_iterations=num_iterations,
+                        num_oversamples=num_oversamples, random_seed=random_seed,
+                        range_sketch=range_sketch)
 
     def genetic_relatedness_weighted(self, W, indexes=None, windows=None, mode="site",
                                      span_normalise=True, polarised=False, centre=True):
