@@ -89,6 +89,10 @@ def _load():
             ctypes.c_int32, P, ctypes.c_uint32, P,
         ]
         lib.orc_genotype_matrix.argtypes = [ctypes.POINTER(_TS), P]
+        lib.orc_genotype_rows.argtypes = [ctypes.POINTER(_TS), ctypes.c_int32, ctypes.c_int32, P]
+        lib.orc_divergence_matrix_site_range.argtypes = [
+            ctypes.POINTER(_TS), ctypes.c_int32, ctypes.c_int32, P]
+        lib.orc_site_path_sums.argtypes = [ctypes.POINTER(_TS), ctypes.c_int32, P, P]
         lib.orc_branch_count_stat_dd.argtypes = [
             ctypes.POINTER(_TS), ctypes.c_int32, P, P, ctypes.c_int32, P,
             ctypes.c_int32, P, ctypes.c_uint32, P,
@@ -292,6 +296,82 @@ def genotype_matrix(ts):
     if err != 0:
         raise RuntimeError(f"oracle error {err}")
     return G
+
+
+def genotype_rows(ts, site_start, site_stop):
+    """int8 (site_stop - site_start, num_samples) allele indexes."""
+    lib = _load()
+    G = np.zeros((site_stop - site_start, ts.num_samples), dtype=np.int8)
+    err = lib.orc_genotype_rows(ctypes.byref(ts.struct), site_start, site_stop, _ptr(G))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return G
+
+
+def divergence_counts_site_range(ts, site_start, site_stop, symmetric=True):
+    """Unnormalised site divergence counts over sites [site_start, site_stop)
+    with every sample its own set, by the reference's pairwise loop
+    (trees.c:8685-8716); float64 num_samples x num_samples, symmetric (else
+    the upper triangle the loop fills)."""
+    lib = _load()
+    n = ts.num_samples
+    D = np.zeros((n, n))
+    err = lib.orc_divergence_matrix_site_range(ctypes.byref(ts.struct), site_start, site_stop,
+                                               _ptr(D))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return D + D.T if symmetric else D
+
+
+def site_path_sums(ts, sample_sets):
+    """int64 (num_samples, 1 + K): per sample index j, the number of
+    mutations above j and, per set k, the sum over those mutations of the
+    set-k samples below the mutation (orc_site_path_sums)."""
+    lib = _load()
+    member = np.zeros((ts.num_samples, len(sample_sets)), dtype=np.uint8)
+    index = np.full(ts.tables.num_nodes, -1, dtype=np.int64)
+    index[ts.samples] = np.arange(ts.num_samples)
+    for k, s in enumerate(sample_sets):
+        member[index[np.asarray(s, dtype=np.int64)], k] = 1
+    out = np.zeros((ts.num_samples, 1 + len(sample_sets)), dtype=np.int64)
+    err = lib.orc_site_path_sums(ctypes.byref(ts.struct), len(sample_sets), _ptr(member),
+                                 _ptr(out))
+    if err != 0:
+        raise RuntimeError(f"oracle error {err}")
+    return out
+
+
+def _infinite_sites_biallelic(ts):
+    t = ts.tables
+    site = np.asarray(t.mutation_site)
+    allele = ts.arrays["mutation_allele"]
+    return (len(site) == t.num_sites and np.array_equal(site, np.arange(t.num_sites))
+            and np.all(allele == 1))
+
+
+def relatedness_rows_site(ts, rows):
+    """Rows ``rows`` (sample indexes) of the site-mode
+    genetic_relatedness_matrix with every sample its own set, one window,
+    span-normalised, for infinite-sites biallelic data, exactly: with a_j
+    the derived count of sample j and G[i][j] the shared derived count, the
+    per-pair differing-site count is a_i + a_j - 2 G[i][j]; the divergence
+    row sums are R_j = n a_j + sum(a) - 2 sum_s g_js c_s; and the
+    normalisation of trees.py:9086-9095 gives
+    K[i][j] = -(n^2 d_ij + sum(R) - n R_i - n R_j) / (2 n^2 L),
+    its numerator an exact integer, rounded once.  Returns (K rows float64,
+    shared-derived rows G[rows] int64)."""
+    if not _infinite_sites_biallelic(ts):
+        raise ValueError("relatedness_rows_site needs one biallelic mutation per site")
+    rows = np.asarray(rows, dtype=np.int64)
+    samples = ts.samples
+    sums = site_path_sums(ts, [samples] + [[samples[i]] for i in rows])
+    a, b, G = sums[:, 0], sums[:, 1], sums[:, 2:].T
+    n = np.int64(ts.num_samples)
+    R = n * a + a.sum() - 2 * b
+    d = a[rows][:, None] + a[None, :] - 2 * G
+    num = n * n * d + R.sum() - n * R[rows][:, None] - n * R[None, :]
+    K = -num.astype(np.float64) / (2.0 * float(n) ** 2 * ts.tables.sequence_length)
+    return K, G
 
 
 def divergence_matrix_site(ts, windows=None, span_normalise=True):

@@ -1395,9 +1395,9 @@ out:
 /* ------------------------------------------------------ genotype matrix */
 typedef struct {
     const orc_ts_t *ts;
-    const int32_t *latest; /* scratch: latest mutation index per node, -1 */
+    int32_t s0, s1;        /* decoded site range */
     int32_t *mut_at_node;
-    int8_t *G;             /* num_sites x num_samples */
+    int8_t *G;             /* (s1 - s0) x num_samples */
 } geno_ctx_t;
 
 static void geno_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
@@ -1406,6 +1406,9 @@ static void geno_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
     (void) x;
     geno_ctx_t *g = (geno_ctx_t *) vctx;
     const orc_ts_t *ts = g->ts;
+    if (site < g->s0 || site >= g->s1) {
+        return;
+    }
     for (int32_t m = m0; m < m1; m++) {
         g->mut_at_node[ts->mutation_node[m]] = m;
     }
@@ -1417,7 +1420,7 @@ static void geno_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
                 break;
             }
         }
-        g->G[(int64_t) site * ts->num_samples + j] = (int8_t) a;
+        g->G[(int64_t) (site - g->s0) * ts->num_samples + j] = (int8_t) a;
     }
     for (int32_t m = m0; m < m1; m++) {
         g->mut_at_node[ts->mutation_node[m]] = -1;
@@ -1425,13 +1428,17 @@ static void geno_visit(void *vctx, int32_t site, int32_t m0, int32_t m1,
 }
 
 /*
- * Allele index per (site, sample): the allele of the nearest mutation above
- * the sample at the site (later mutations on the same node win), 0 if none
- * (c/tskit/genotypes.c, decoding with isolated samples not missing).
+ * Allele index per (site, sample) for sites [s0, s1): the allele of the
+ * nearest mutation above the sample at the site (later mutations on the same
+ * node win), 0 if none (c/tskit/genotypes.c, decoding with isolated samples
+ * not missing).
  */
-int orc_genotype_matrix(const orc_ts_t *ts, int8_t *G)
+int orc_genotype_rows(const orc_ts_t *ts, int32_t s0, int32_t s1, int8_t *G)
 {
     geno_ctx_t g;
+    if (s0 < 0 || s1 > ts->num_sites || s1 < s0) {
+        return ORC_ERR_BAD_PARAM;
+    }
     int32_t *mut_at_node = malloc((size_t) ts->num_nodes * sizeof(int32_t));
     double *Wz = calloc((size_t) ts->num_samples, sizeof(double));
     int ret;
@@ -1444,11 +1451,207 @@ int orc_genotype_matrix(const orc_ts_t *ts, int8_t *G)
         mut_at_node[u] = -1;
     }
     g.ts = ts;
-    g.latest = NULL;
+    g.s0 = s0;
+    g.s1 = s1;
     g.mut_at_node = mut_at_node;
     g.G = G;
     ret = site_sweep(ts, 1, Wz, geno_visit, &g);
     free(mut_at_node);
     free(Wz);
     return ret;
+}
+
+int orc_genotype_matrix(const orc_ts_t *ts, int8_t *G)
+{
+    return orc_genotype_rows(ts, 0, ts->num_sites, G);
+}
+
+/*
+ * Site-mode divergence matrix with every sample its own set, over sites
+ * [s0, s1) in one window, unnormalised: the reference's loop
+ * (c/tskit/trees.c:8685-8716 update_site_divergence, driven by
+ * 8753-8826): per site the samples are grouped by allele and every pair of
+ * samples carrying different alleles adds 1 to D[u][v], u < v (upper
+ * triangle only, row-major num_samples x num_samples).  D is not cleared.
+ */
+int orc_divergence_matrix_site_range(const orc_ts_t *ts, int32_t s0, int32_t s1, double *D)
+{
+    const int64_t n = ts->num_samples;
+    const int32_t chunk = 64;
+    int8_t *G = malloc((size_t) chunk * (size_t) n);
+    int32_t *A = malloc((size_t) n * sizeof(int32_t));
+    int64_t *off = NULL;
+    int32_t max_allele = 0;
+    int ret = 0;
+    if (!G || !A) {
+        ret = ORC_ERR_NO_MEMORY;
+        goto out;
+    }
+    for (int32_t c0 = s0; c0 < s1 && ret == 0; c0 += chunk) {
+        const int32_t c1 = c0 + chunk < s1 ? c0 + chunk : s1;
+        if ((ret = orc_genotype_rows(ts, c0, c1, G)) != 0) {
+            break;
+        }
+        for (int32_t s = c0; s < c1; s++) {
+            const int8_t *g = G + (int64_t) (s - c0) * n;
+            int32_t na = 0;
+            for (int64_t j = 0; j < n; j++) {
+                na = g[j] + 1 > na ? g[j] + 1 : na;
+            }
+            if (na > max_allele) {
+                free(off);
+                off = malloc((size_t) (na + 1) * sizeof(int64_t));
+                if (!off) {
+                    ret = ORC_ERR_NO_MEMORY;
+                    goto out;
+                }
+                max_allele = na;
+            }
+            /* group the samples by allele, in sample order within a group */
+            for (int32_t a = 0; a <= na; a++) {
+                off[a] = 0;
+            }
+            for (int64_t j = 0; j < n; j++) {
+                off[g[j] + 1]++;
+            }
+            for (int32_t a = 0; a < na; a++) {
+                off[a + 1] += off[a];
+            }
+            for (int64_t j = 0; j < n; j++) {
+                A[off[g[j]]++] = (int32_t) j;
+            }
+            for (int32_t a = na; a > 0; a--) {
+                off[a] = off[a - 1];
+            }
+            off[0] = 0;
+            for (int32_t a = 0; a < na; a++) {
+                for (int32_t b = a + 1; b < na; b++) {
+                    for (int64_t j = off[a]; j < off[a + 1]; j++) {
+                        for (int64_t k = off[b]; k < off[b + 1]; k++) {
+                            int64_t u = A[j], v = A[k];
+                            if (u > v) {
+                                int64_t t = u;
+                                u = v;
+                                v = t;
+                            }
+                            D[u * n + v] += 1.0;
+                        }
+                    }
+                }
+            }
+        }
+    }
+out:
+    free(G);
+    free(A);
+    free(off);
+    return ret;
+}
+
+/*
+ * Exact per-sample sums over the mutations above each sample: for sample
+ * index j,
+ *   out[j][0]     = #{mutations m with j below node(m) in m's tree}
+ *   out[j][1 + k] = sum over those m of x_k(node(m)),
+ * x_k(u) the number of set-k samples below u in that tree (member is
+ * num_samples x K, 0/1).  For infinite-sites biallelic data (one mutation per
+ * site, no parent mutation) out[j][0] is sample j's derived-allele count and
+ * out[j][1 + k] the number of (site, set-k sample) pairs sharing j's derived
+ * allele; with set k = {i} that is the shared-derived count G[i][j].
+ *
+ * One tree sweep with lazy path sums, O(edges x depth x K): acc[u] holds
+ * increments for every sample below u, so a sample's total is the sum of acc
+ * over its root path.  Removing edge (c, p) pushes the path sum above c into
+ * acc[c]; inserting one subtracts the new path sum above c; at the end every
+ * edge is removed and a sample's total is its own acc.
+ */
+int orc_site_path_sums(const orc_ts_t *ts, int32_t K, const uint8_t *member, int64_t *out)
+{
+    const int32_t N = ts->num_nodes, E = ts->num_edges, A = K + 1;
+    int32_t *parent = malloc((size_t) N * sizeof(int32_t));
+    int64_t *x = calloc((size_t) N * (size_t) (K > 0 ? K : 1), sizeof(int64_t));
+    int64_t *acc = calloc((size_t) N * (size_t) A, sizeof(int64_t));
+    int64_t *sum = calloc((size_t) A, sizeof(int64_t));
+    if (!parent || !x || !acc || !sum) {
+        free(parent);
+        free(x);
+        free(acc);
+        free(sum);
+        return ORC_ERR_NO_MEMORY;
+    }
+    for (int32_t u = 0; u < N; u++) {
+        parent[u] = -1;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        for (int32_t k = 0; k < K; k++) {
+            x[(int64_t) ts->samples[j] * K + k] = member[(int64_t) j * K + k];
+        }
+    }
+    int32_t tj = 0, tk = 0, mut = 0;
+    double left = 0, L = ts->sequence_length;
+    for (;;) {
+        const int done = !(tj < E || left < L);
+        while (tk < E && (done || ts->edge_right[ts->rem[tk]] == left)) {
+            int32_t e = ts->rem[tk++];
+            int32_t ch = ts->edge_child[e];
+            memset(sum, 0, (size_t) A * sizeof(int64_t));
+            for (int32_t u = ts->edge_parent[e]; u != -1; u = parent[u]) {
+                for (int32_t a = 0; a < A; a++) {
+                    sum[a] += acc[(int64_t) u * A + a];
+                }
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] -= x[(int64_t) ch * K + k];
+                }
+            }
+            for (int32_t a = 0; a < A; a++) {
+                acc[(int64_t) ch * A + a] += sum[a];
+            }
+            parent[ch] = -1;
+        }
+        if (done) {
+            break;
+        }
+        while (tj < E && ts->edge_left[ts->ins[tj]] == left) {
+            int32_t e = ts->ins[tj++];
+            int32_t ch = ts->edge_child[e];
+            parent[ch] = ts->edge_parent[e];
+            memset(sum, 0, (size_t) A * sizeof(int64_t));
+            for (int32_t u = parent[ch]; u != -1; u = parent[u]) {
+                for (int32_t a = 0; a < A; a++) {
+                    sum[a] += acc[(int64_t) u * A + a];
+                }
+                for (int32_t k = 0; k < K; k++) {
+                    x[(int64_t) u * K + k] += x[(int64_t) ch * K + k];
+                }
+            }
+            for (int32_t a = 0; a < A; a++) {
+                acc[(int64_t) ch * A + a] -= sum[a];
+            }
+        }
+        double right = L;
+        if (tj < E && ts->edge_left[ts->ins[tj]] < right) {
+            right = ts->edge_left[ts->ins[tj]];
+        }
+        if (tk < E && ts->edge_right[ts->rem[tk]] < right) {
+            right = ts->edge_right[ts->rem[tk]];
+        }
+        while (mut < ts->num_mutations
+               && ts->site_position[ts->mutation_site[mut]] < right) {
+            const int32_t u = ts->mutation_node[mut++];
+            acc[(int64_t) u * A] += 1;
+            for (int32_t k = 0; k < K; k++) {
+                acc[(int64_t) u * A + 1 + k] += x[(int64_t) u * K + k];
+            }
+        }
+        left = right;
+    }
+    for (int32_t j = 0; j < ts->num_samples; j++) {
+        memcpy(out + (int64_t) j * A, acc + (int64_t) ts->samples[j] * A,
+            (size_t) A * sizeof(int64_t));
+    }
+    free(parent);
+    free(x);
+    free(acc);
+    free(sum);
+    return 0;
 }

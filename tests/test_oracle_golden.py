@@ -139,3 +139,33 @@ def test_compensated_branch_oracle_vs_fp64_large():
         b = O.branch_count_stat_dd(ots, sets, terms, windows=win, polarised=pol)
         err = np.max(np.abs(a - b), axis=0) / np.max(np.abs(b), axis=0)
         assert np.all(err < 1e-13), err
+
+
+def test_site_range_oracles_vs_full_matrix():
+    """The site-range genotype decode and the reference's pairwise site
+    divergence loop agree with the whole-matrix oracle, and the exact
+    full-size relatedness rows (path sums) equal the normalised divergence
+    matrix's rows."""
+    from tskit_gb300 import sim
+
+    t = sim.simulate(150, 1e6, 400, 900, 23)
+    ots = O.OracleTS(t)
+    G = O.genotype_matrix(ots)
+    S = t.num_sites
+    np.testing.assert_array_equal(O.genotype_rows(ots, 100, 300), G[100:300])
+    assert O.genotype_rows(ots, 5, 5).shape == (0, ots.num_samples)
+    full = O.divergence_matrix_site(ots, span_normalise=False)[0]
+    np.testing.assert_array_equal(O.divergence_counts_site_range(ots, 0, S), full)
+    part = O.divergence_counts_site_range(ots, 0, 300) + O.divergence_counts_site_range(ots, 300, S)
+    np.testing.assert_array_equal(part, full)
+    # path sums: derived counts and shared-derived counts, exactly
+    rows = [0, 7, 149, 60]
+    Gi = G.astype(np.int64)
+    sums = O.site_path_sums(ots, [ots.samples] + [[ots.samples[i]] for i in rows])
+    np.testing.assert_array_equal(sums[:, 0], Gi.sum(axis=0))
+    np.testing.assert_array_equal(sums[:, 1], Gi.T @ Gi.sum(axis=1))
+    np.testing.assert_array_equal(sums[:, 2:].T, (Gi.T @ Gi)[rows])
+    K, shared = O.relatedness_rows_site(ots, rows)
+    exp = O.relatedness_from_divergence(O.divergence_matrix_site(ots)[0])[rows]
+    np.testing.assert_array_equal(shared, (Gi.T @ Gi)[rows])
+    assert np.max(np.abs(K - exp)) <= 1e-13 * np.max(np.abs(exp))
