@@ -53,6 +53,11 @@ def parse_args():
                     help="profiling mode: only warmup + steps launches of the headline fused "
                          "query in this arithmetic (default compact plan, no tuning, no other "
                          "legs), for ncu captures")
+    ap.add_argument("--serve-queries", type=int, default=2000,
+                    help="serve_mix: requests in the stream")
+    ap.add_argument("--serve-rate", type=float, default=5000.0,
+                    help="serve_mix: Poisson arrival rate (requests/s), above what the "
+                         "server absorbs, so that queries/s measures the server")
     ap.add_argument("--workload", default=WORKLOAD,
                     choices=[WORKLOAD, "afs_n200k", "grm_n20k", "serve_mix"],
                     help="the headline workload (default) or one of the other "
@@ -853,10 +858,21 @@ def run_afs_n200k(args):
                                 "cores": 1, "kind": "port",
                                 "sample": "the full step (4 AFS + 1 relatedness-vector call) "
                                           "through the C oracle, one core"}
-        line["error_vs_fp64_oracle"] = {
-            name: rel_err(np.asarray(h).reshape(-1), np.asarray(r).reshape(-1))
-            for name, h, r in zip(["afs_site_all", "afs_branch_all", "afs_site_joint",
-                                   "afs_branch_joint", "relatedness_vector_w64"], host, ref)}
+        names = ["afs_site_all", "afs_branch_all", "afs_site_joint", "afs_branch_joint",
+                 "relatedness_vector_w64"]
+        errs = {name: rel_err(np.asarray(h).reshape(-1), np.asarray(r).reshape(-1))
+                for name, h, r in zip(names, host, ref)}
+        line["error_vs_fp64_oracle"] = errs
+        # site AFS bins are exact counts scaled by the window span: identical
+        # bit for bit; branch AFS and the relatedness product: normwise 1e-12
+        site_identical = {name: bool(np.array_equal(np.asarray(h).reshape(-1),
+                                                    np.asarray(r).reshape(-1)))
+                          for name, h, r in zip(names, host, ref) if "site" in name}
+        line["parity"] = {
+            "site_afs_identical": site_identical,
+            "bound": 1e-12,
+            "pass": all(site_identical.values())
+                    and all(v <= 1e-12 for k, v in errs.items() if "site" not in k)}
     print(json.dumps(line))
 
 
@@ -923,26 +939,107 @@ def run_grm_n20k(args):
         "gpu_launches": 1, "clocks": clocks.summary(),
     }
     if not args.no_cpu_baseline:
-        # all host cores: FP64 BLAS Gram (exact for these integers) of a site sample
-        sample = 512
-        rng = np.random.default_rng(0)
-        Xs = (rng.random((sample, n)) < 0.05).astype(np.float64)
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle as O
+
+        ots = O.OracleTS(tables)
+        line["parity"] = grm_parity(O, ots, G, P, K, n, S, kp)
+        # the reference's site divergence-matrix loop (variant decode, then
+        # every pair of samples carrying different alleles), one core, on a
+        # run of sites from the middle of the genome
+        sample, s0 = 64, S // 2
         t0 = time.perf_counter()
-        Xs.T @ Xs
+        O.divergence_counts_site_range(ots, s0, s0 + sample, symmetric=False)
         cpu_s = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": n * (n - 1) / 2 * sample / cpu_s,
-                                "unit": "pair-sites/s", "cores": os.cpu_count(),
-                                "kind": "port",
-                                "sample": f"FP64 BLAS X^T X over {sample} sites x {n} samples "
-                                          "(numpy, all host threads); the reference's own pair "
-                                          "loop is far slower"}
+                                "unit": "pair-sites/s", "cores": 1, "kind": "port",
+                                "sample": f"sites {s0}..{s0 + sample - 1} of {S}: the reference's "
+                                          "site divergence-matrix loop (trees.c:8685-8826) "
+                                          "through the C oracle, one core, scaled per "
+                                          "pair-site"}
     print(json.dumps(line))
 
 
+def grm_parity(O, ots, G, P, K, n, S, kp):
+    """Full-size parity of the site-mode relatedness matrix.
+
+    1. Operand: the device-decoded genotypes of 2,048 sites equal the
+       oracle's decode for all samples.
+    2. Gram: 64 tiles of 128 x 256 (8 random row blocks x 8 random column
+       blocks) of the int32 product equal a CPU integer product of the same
+       operand rows (float32 BLAS over 32,768-site slices, exact since each
+       slice's sums stay below 2^24, summed in int64).  Entries of tiles the
+       Gram skips (below the diagonal band) are read from the transposed
+       entry.
+    3. Rows: 8 random full rows of the product equal the oracle's exact
+       shared-derived counts, and the same rows of the final matrix are
+       within 1e-12 (normwise per row) of the oracle's exact rows."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    out = {}
+    # 1. operand vs the oracle's genotypes
+    s0 = int(rng.integers(0, S - 2048))
+    geno = O.genotype_rows(ots, s0, s0 + 2048)
+    dev = (G[:, s0:s0 + 2048] == 0x38).cpu().numpy().T
+    # every operand byte is E4M3 0 or 1 (0x38), the padding columns 0
+    bad = 0
+    for i in range(0, n, 2048):
+        g = G[i:i + 2048]
+        bad += int(((g[:, :S] != 0) & (g[:, :S] != 0x38)).sum()) + int((g[:, S:] != 0).sum())
+    out["operand_sites"] = [s0, s0 + 2048]
+    out["operand_bad_bytes"] = bad
+    out["operand_equal"] = bool(np.array_equal(dev, geno != 0)) and bad == 0
+
+    def full(rows, cols):
+        """Product entries (rows x cols), each read from a tile the Gram
+        computes: tile (r, c) is computed when c + 256 > r."""
+        r = torch.as_tensor(rows, device=P.device)
+        c = torch.as_tensor(cols, device=P.device)
+        direct = P.index_select(0, r).index_select(1, c)
+        transposed = P.index_select(1, r).index_select(0, c).T
+        computed = (c // 256 * 256 + 256)[None, :] > (r // 128 * 128)[:, None]
+        return torch.where(computed, direct, transposed).cpu().numpy().astype(np.int64)
+
+    # 2. tiles vs a CPU integer product of the operand
+    rb = np.sort(rng.choice(n // 128, 8, replace=False)) * 128
+    cb = np.sort(rng.choice(n // 256, 8, replace=False)) * 256
+    rows = (rb[:, None] + np.arange(128)).reshape(-1)
+    cols = (cb[:, None] + np.arange(256)).reshape(-1)
+    Xr = G[torch.as_tensor(rows, device=G.device)].cpu().numpy()
+    Xc = G[torch.as_tensor(cols, device=G.device)].cpu().numpy()
+    cpu = np.zeros((len(rows), len(cols)), dtype=np.int64)
+    t0 = time.perf_counter()
+    for k0 in range(0, kp, 32768):
+        a = (Xr[:, k0:k0 + 32768] == 0x38).astype(np.float32)
+        b = (Xc[:, k0:k0 + 32768] == 0x38).astype(np.float32)
+        cpu += (a @ b.T).astype(np.int64)
+    gpu = full(rows, cols)
+    out["tiles"] = {"count": 64, "row_blocks": rb.tolist(), "col_blocks": cb.tolist(),
+                    "entries": int(cpu.size), "mismatches": int(np.sum(cpu != gpu)),
+                    "cpu_s": time.perf_counter() - t0}
+    # 3. full rows vs the oracle's exact rows
+    pick = np.sort(rng.choice(n, 8, replace=False))
+    Kexp, Gexp = O.relatedness_rows_site(ots, pick)
+    Grow = full(pick, np.arange(n))
+    Krow = K[pick]
+    out["rows"] = {"samples": pick.tolist(), "product_mismatches": int(np.sum(Grow != Gexp)),
+                   "relatedness_max_rel_err": float(np.max(np.abs(Krow - Kexp))
+                                                    / np.max(np.abs(Kexp))),
+                   "bound": 1e-12}
+    out["pass"] = (out["operand_equal"] and out["tiles"]["mismatches"] == 0
+                   and out["rows"]["product_mismatches"] == 0
+                   and out["rows"]["relatedness_max_rel_err"] <= 1e-12)
+    return out
+
+
 def run_serve_mix(args):
-    """Eight resident tree sequences (n = 1k..200k, breakpoints = 5n); a
-    Poisson stream of diversity / divergence / Fst / AFS / relatedness x 8
-    requests, served batched and one at a time."""
+    """Eight resident tree sequences (n = 1k..200k, L = 1e8, breakpoints =
+    5n); a Poisson stream of diversity / divergence / Fst / AFS / relatedness
+    x 8 requests (sets of 10-10,000 samples, 1-1,000 equal windows, branch or
+    site) arriving faster than the server absorbs them, served batched
+    (fused queries grouped across tree sequences, 8 stream slots) and one at
+    a time with a synchronous FP64 launch each."""
     import torch
 
     import tskit_gb300
@@ -954,31 +1051,49 @@ def run_serve_mix(args):
     ns = [1000, 2000, 5000, 20000, 20000, 50000, 100000, 200000]
     resident = {f"n{n}_{i}": tskit_gb300.TreeSequence(sim.simulate(n, 1e8, 5 * n, 5 * n, 2000 + i))
                 for i, n in enumerate(ns)}
-    num = max(50, args.steps * 40)
-    reqs = poisson_requests(resident, num, 50.0, 7)
+    num, rate = args.serve_queries, args.serve_rate
+    reqs = poisson_requests(resident, num, rate, 7)
     be = GpuBackend(resident, num_slots=8)
-    Server(be, num_slots=8).run(poisson_requests(resident, 40, 1e4, 8))  # warm-up
+    Server(be, num_slots=8).run(poisson_requests(resident, 60, 1e4, 8))  # warm-up
     with ClockSampler(0) as clocks:
+        launches0 = be_launches()
         b = Server(be, num_slots=8).run(reqs)
+        launches = be_launches() - launches0
     p = Server(GpuBackend(resident, num_slots=1), num_slots=1).run(reqs, mode="plain")
+    served = [r for r in reqs if r.rid in b.results]
+    h2d = sum(sum(len(s) * 4 for s in r.sample_sets)
+              + (r.weights.nbytes if r.weights is not None else 0) for r in served)
+    d2h = sum(np.asarray(b.results[r.rid]).nbytes for r in served)
     line = {
         "metric": "queries/s", "value": b.queries_per_s, "unit": "queries/s", "n_gpus": 1,
-        "steps": num, "warmup": 40, "ms_per_step": 1e3 / b.queries_per_s,
+        "steps": b.num, "warmup": 60, "ms_per_step": 1e3 / b.queries_per_s,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded SMC generator; Poisson arrivals, 50 requests/s)",
+        "data": f"synthetic (seeded SMC generator; Poisson arrivals at {rate:g} requests/s, "
+                "above the server's rate)",
         "config": {"workload": "serve_mix: 8 resident tree sequences n=" + ",".join(map(str, ns))
                                + ", L=1e8, breakpoints=5n; requests diversity / divergence / Fst "
                                  "/ AFS / relatedness x 8, sets of 10-10000, 1/10/100/1000 "
                                  "windows, branch or site",
+                   "stream": f"{num} requests (a subset of the 100,000-request stream: at the "
+                             "measured rates the full stream takes tens of minutes per arm); "
+                             "results over 256 MiB rejected and counted",
                    "batched": b.summary(), "plain_one_at_a_time": p.summary()},
         "p50_ms": b.percentile_ms(50), "p99_ms": b.percentile_ms(99),
+        "rejected": len(b.rejected),
         "plain": {"queries_per_s": p.queries_per_s, "p50_ms": p.percentile_ms(50),
                   "p99_ms": p.percentile_ms(99)},
-        "e2e": {"value": b.queries_per_s, "unit": "queries/s", "h2d_bytes_per_step": None,
-                "d2h_bytes_per_step": None},
-        "gpu_launches": b.launches, "clocks": clocks.summary(),
+        "e2e": {"value": b.queries_per_s, "unit": "queries/s",
+                "h2d_bytes_per_step": int(h2d / max(1, b.num)),
+                "d2h_bytes_per_step": int(d2h / max(1, b.num))},
+        "gpu_launches": launches / max(1, b.num), "clocks": clocks.summary(),
     }
     print(json.dumps(line))
+
+
+def be_launches():
+    from tskit_gb300 import _native as nat
+
+    return nat.load().tsg_launch_count()
 
 
 def run_profile(args):

@@ -425,6 +425,10 @@ int tsg_query_create_relatedness_vector(tsg_query_t **query, const tsg_treeseq_t
     uint64_t num_weights, uint64_t num_windows, const double *windows,
     uint64_t num_focal_nodes, const int32_t *focal_nodes, uint32_t options);
 int tsg_query_set_weights(tsg_query_t *query, const double *weights_device);
+/* Frees the query's device arrays in stream order (cudaFreeAsync on the
+ * legacy default stream), so that freeing never waits for the device: free
+ * a query only after its launches have completed (or from a stream ordered
+ * after them).  tsg_batch_free does the same for a batch. */
 int tsg_query_free(tsg_query_t *query);
 /* Device bytes the query needs in a workspace. */
 int64_t tsg_query_workspace_bytes(const tsg_query_t *query);
@@ -451,6 +455,37 @@ int tsg_workspace_create(tsg_workspace_t **ws);
 int tsg_workspace_reserve(tsg_workspace_t *ws, int64_t bytes);
 int64_t tsg_workspace_bytes(const tsg_workspace_t *ws);
 int tsg_workspace_free(tsg_workspace_t *ws);
+
+/* ----------------------------------------------------- batched launches
+ * No counterpart in the reference (one call runs one statistic on one tree
+ * sequence there).  A batch fuses prepared queries on any resident tree
+ * sequences into one launch per pipeline stage: sample-count queries that
+ * use the compact replay (tree sequences of up to 65,535 samples, up to 8
+ * sample sets, integer site summaries) share each stage's kernel, the replay
+ * being one persistent kernel whose blocks take (query, span) items from one
+ * counter over all the queries' spans; the other queries launch on their own
+ * in the same stream.  Every result is bitwise the result of the query's own
+ * launch.
+ *   - tsg_batch_workspace_bytes: the workspace the batch needs (the queries'
+ *     own workspaces side by side, plus its counters).
+ *   - tsg_batch_create binds the queries, one device result pointer each
+ *     (layouts as tsg_query_launch) and the workspace; the queries, results
+ *     and workspace must outlive the batch.
+ *   - tsg_batch_launch enqueues the kernels on the stream (no allocation, no
+ *     synchronisation; capturable in a CUDA graph).  Launches of one batch,
+ *     or of batches sharing its workspace, must be ordered on one stream.
+ *   - tsg_batch_check: synchronous read of every query's check word after a
+ *     launch (TSG_ERR_DEVICE_CHECK with the first failing query's index).
+ *   - tsg_batch_num_fused: how many of the queries run in the fused kernels. */
+typedef struct tsg_batch tsg_batch_t;
+int tsg_batch_workspace_bytes(uint64_t num_queries, const tsg_query_t *const *queries,
+    int64_t *bytes);
+int tsg_batch_create(tsg_batch_t **batch, uint64_t num_queries,
+    const tsg_query_t *const *queries, double *const *results, tsg_workspace_t *ws);
+int tsg_batch_launch(const tsg_batch_t *batch, void *cuda_stream);
+int tsg_batch_check(const tsg_batch_t *batch, uint64_t *failed_query);
+int tsg_batch_num_fused(const tsg_batch_t *batch);
+void tsg_batch_free(tsg_batch_t *batch);
 
 /* ------------------------------------------ launch without any allocation
  * No counterpart in the reference.  For callers that must not allocate device

@@ -40,14 +40,22 @@ class FakeBackend:
     def max_sets(self, key):
         return 8 if self.resident[key].num_samples <= 65535 else 4
 
-    def workspace_bytes(self, reqs):
-        return 1000 * sum(1 + len(r.sample_sets) for r in reqs)
+    def output_bytes(self, r):
+        nwin = 1 if r.windows is None else len(r.windows) - 1
+        if r.kind == "rv":
+            return nwin * self.resident[r.ts].num_samples * r.weights.shape[1] * 8
+        return nwin * 8
 
-    def discard(self, reqs):
+    def workspace_bytes(self, groups):
+        return 1000 * sum(1 + len(r.sample_sets) for g in groups for r in g)
+
+    def discard(self, groups):
         pass
 
-    def launch(self, reqs, slot):
-        w = {"reqs": reqs, "t": self.clock.t, "slot": slot, "bytes": self.workspace_bytes(reqs)}
+    def launch(self, groups, slot):
+        reqs = [r for g in groups for r in g]
+        w = {"reqs": reqs, "groups": groups, "t": self.clock.t, "slot": slot,
+             "bytes": self.workspace_bytes(groups)}
         self.live[slot] = w["bytes"]
         self.inflight_bytes.append(sum(self.live.values()))
         self.launched.append(w)
@@ -81,14 +89,17 @@ def test_all_requests_complete_once_and_batch():
     assert all(st.results[r.rid] == ("done", r.rid) for r in reqs)
     assert np.all(st.latencies_s > 0)
     assert st.launches < len(reqs)  # batching happened
+    assert st.fused_queries == sum(len(w["groups"]) for w in be.launched)
+    assert any(len({g[0].ts for g in w["groups"]}) > 1 for w in be.launched)  # across sequences
     for w in be.launched:
-        rs = w["reqs"]
-        keys = {r.batch_key() for r in rs}
-        assert len(keys) == 1
-        if rs[0].kind == "counts":
-            assert sum(len(r.sample_sets) for r in rs) <= be.max_sets(rs[0].ts)
-        if rs[0].kind == "afs":
-            assert len(rs) == 1
+        assert 1 <= len(w["groups"]) <= 8
+        for rs in w["groups"]:
+            keys = {r.batch_key() for r in rs}
+            assert len(keys) == 1
+            if rs[0].kind == "counts":
+                assert sum(len(r.sample_sets) for r in rs) <= be.max_sets(rs[0].ts)
+            if rs[0].kind == "afs":
+                assert len(rs) == 1
 
 
 def test_memory_budget_respected():
@@ -108,7 +119,24 @@ def test_plain_mode_one_request_per_launch():
     be = FakeBackend(clock, resident)
     st = Server(be, num_slots=4).run(reqs, mode="plain", clock=clock)
     assert st.launches == len(reqs)
-    assert all(len(w["reqs"]) == 1 for w in be.launched)
+    assert all(len(w["reqs"]) == 1 and len(w["groups"]) == 1 for w in be.launched)
+
+
+def test_oversized_requests_rejected_and_counted():
+    resident = {"a": FakeTS(1000), "b": FakeTS(100000)}
+    reqs = poisson_requests(resident, 300, 20000.0, 6, window_choices=(1, 10, 100, 1000))
+    clock = FakeClock()
+    be = FakeBackend(clock, resident)
+    cap = 64 << 20
+    st = Server(be, num_slots=4, max_output_bytes=cap).run(reqs, clock=clock)
+    over = {r.rid for r in reqs if be.output_bytes(r) > cap}
+    assert over and all(r.kind == "rv" for r in reqs if r.rid in over)
+    assert set(st.rejected) == over
+    assert st.num == len(reqs) - len(over) == len(st.results) == len(st.latencies_s)
+    assert not over & set(st.results)
+    # the requests keep the windows they were drawn with
+    assert any(r.kind == "rv" and r.windows is not None and len(r.windows) == 1001
+               for r in reqs)
 
 
 def test_request_mix_shapes():

@@ -7,6 +7,6 @@ sm_103a CUDA kernels behind a C ABI (include/tskit_gb300.h).
 """
 from ._native import LibraryError  # noqa: F401
 from .tables import Tables  # noqa: F401
-from .trees import PCAResult, Query, TreeSequence, Workspace, load  # noqa: F401
+from .trees import PCAResult, Query, QueryBatch, TreeSequence, Workspace, load  # noqa: F401
 
 __version__ = "0.1.0"

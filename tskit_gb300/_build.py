@@ -23,6 +23,7 @@ CUDA_SOURCES = [
     "tsg_treeseq.cu",
     "tsg_plan.cu",
     "tsg_stats.cu",
+    "tsg_batch.cu",
     "tsg_eval_f32_pol.cu",
     "tsg_eval_f32_unpol.cu",
     "tsg_eval_f64_pol.cu",

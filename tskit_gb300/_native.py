@@ -178,6 +178,12 @@ SIGNATURES = {
     "tsg_launch_count": (_I64, []),
     "tsg_query_launch_noalloc": (ctypes.c_int, [_P, _P, _P]),
     "tsg_noalloc_check": (ctypes.c_int, [_P]),
+    "tsg_batch_workspace_bytes": (ctypes.c_int, [_U64, _P, ctypes.POINTER(_I64)]),
+    "tsg_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), _U64, _P, _P, _P]),
+    "tsg_batch_launch": (ctypes.c_int, [_P, _P]),
+    "tsg_batch_check": (ctypes.c_int, [_P, ctypes.POINTER(_U64)]),
+    "tsg_batch_num_fused": (ctypes.c_int, [_P]),
+    "tsg_batch_free": (None, [_P]),
     "tsg_kastore_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "tsg_kastore_get": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32),
                                        ctypes.POINTER(_I64), ctypes.POINTER(_P)]),

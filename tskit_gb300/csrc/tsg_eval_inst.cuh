@@ -56,4 +56,41 @@ TSG_CHUNK_EVAL_LAUNCHER(TSG_CHUNKS_NAME)
     }
 }
 
+template <typename F, int KQ>
+__global__ void __launch_bounds__(256) kb_item_bls(const BatchQuery *bq, const int64_t *off, int nq)
+{
+    TSG_BATCH_QUERY();
+    item_bls_body<F, KQ>(Q.v, Q.p, Q.w, bid, nb);
+}
+
+template <typename F, bool UNPOL, int KQ>
+__global__ void __launch_bounds__(256) kb_eval_grouped(const BatchQuery *bq, const int64_t *off,
+    int nq)
+{
+    TSG_BATCH_QUERY();
+    const int64_t total = (Q.v.num_chunks + TSG_EVAL_BLOCK - 1) / TSG_EVAL_BLOCK * Q.p.gwpb;
+    eval_grouped_body<F, UNPOL, KQ>(Q.v, Q.p, Q.w, total, bid, nb);
+}
+
+TSG_CHUNK_EVAL_BATCH_LAUNCHER(TSG_CHUNKS_BATCH_NAME)
+{
+    if (kq == 1) {
+        if (blocks_bls > 0) {
+            kb_item_bls<TSG_EVAL_F, 1><<<(unsigned) blocks_bls, 256, 0, st>>>(bq, off_bls, nq);
+        }
+        if (blocks_eval > 0) {
+            kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<(unsigned) blocks_eval, 256, 0, st>>>(
+                bq, off_eval, nq);
+        }
+    } else {
+        if (blocks_bls > 0) {
+            kb_item_bls<TSG_EVAL_F, 2><<<(unsigned) blocks_bls, 256, 0, st>>>(bq, off_bls, nq);
+        }
+        if (blocks_eval > 0) {
+            kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<(unsigned) blocks_eval, 256, 0, st>>>(
+                bq, off_eval, nq);
+        }
+    }
+}
+
 }  // namespace tsg

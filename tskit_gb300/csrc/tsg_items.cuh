@@ -40,13 +40,19 @@
 namespace tsg {
 
 // node -> sample-set membership bits for this query
-__global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
+__device__ __forceinline__ void node_mask_body(const TSView &ts, const QueryDev &qd, uint32_t *node_mask,
+    const int64_t bid, const int64_t nb)
 {
-    for (int64_t u = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; u < ts.num_nodes;
-         u += (int64_t) gridDim.x * blockDim.x) {
+    for (int64_t u = bid * (int64_t) blockDim.x + threadIdx.x; u < ts.num_nodes;
+         u += (int64_t) nb * blockDim.x) {
         const int32_t si = ts.sample_index[u];
         node_mask[u] = si >= 0 ? qd.sample_mask[si] : 0u;
     }
+}
+
+static __global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
+{
+    node_mask_body(ts, qd, node_mask, blockIdx.x, gridDim.x);
 }
 
 // Leaves (nodes that are never a parent) keep their sample-set bits and
@@ -59,14 +65,14 @@ __global__ void k_node_mask(TSView ts, QueryDev qd, uint32_t *node_mask)
 // so that an edge costs at most four exact fixed-point adds
 // (tsg_fixed.cuh) whatever its length.  Layout of w.leaf_area: partial,
 // plus and minus arrays of windows x patterns counters each.
-__global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, QueryDev qd,
-    WsDev w)
+__device__ __forceinline__ void leaf_areas_body(const TSView &ts, const QueryParams &q, const QueryDev &qd, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     const int NP = 1 << q.K;
     const int64_t block = (int64_t) q.Wn * NP * TSG_FX_LIMBS;
     unsigned long long *part = w.leaf_area, *plus = part + block, *minus = plus + block;
-    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < ts.num_edges;
-         i += (int64_t) gridDim.x * blockDim.x) {
+    for (int64_t i = bid * (int64_t) blockDim.x + threadIdx.x; i < ts.num_edges;
+         i += (int64_t) nb * blockDim.x) {
         const int32_t c = ts.ins_child[i];
         if (ts.node_is_parent[c]) {
             continue;
@@ -93,17 +99,24 @@ __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, Qu
     }
 }
 
+static __global__ void __launch_bounds__(256) k_leaf_areas(TSView ts, QueryParams q, QueryDev qd,
+    WsDev w)
+{
+    leaf_areas_body(ts, q, qd, w, blockIdx.x, gridDim.x);
+}
+
 // One block per pattern: the running sum over windows of the difference
 // array (each window's exact plus - minus rounded once, then an FP64 prefix
 // in a fixed order: per-thread runs of windows, a block scan of the run
 // totals) gives the branch length alive over each whole window; area = that
 // x window length + the window's partial areas.  w.leaf_dbl: windows x
 // patterns doubles.
-__global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd, WsDev w)
+__device__ __forceinline__ void leaf_prefix_body(const QueryParams &q, const QueryDev &qd, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     __shared__ double s_run[256];
     const int NP = 1 << q.K;
-    const int pat = blockIdx.x;
+    const int pat = bid;
     const int64_t block = (int64_t) q.Wn * NP * TSG_FX_LIMBS;
     const unsigned long long *part = w.leaf_area, *plus = part + block, *minus = plus + block;
     const int per = (q.Wn + blockDim.x - 1) / blockDim.x;
@@ -133,15 +146,21 @@ __global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd,
     }
 }
 
+static __global__ void __launch_bounds__(256) k_leaf_prefix(QueryParams q, QueryDev qd, WsDev w)
+{
+    leaf_prefix_body(q, qd, w, blockIdx.x, gridDim.x);
+}
+
 // The leaves' window sums: sum over patterns of F_r(pattern) x A[w][pattern]
 // (FP64), one thread per (window, term).
 template <int W>
-__global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
+__device__ __forceinline__ void leaf_terms_body(const QueryParams &q, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     const int NP = 1 << q.K;
     const int64_t total = (int64_t) q.Wn * q.R;
-    for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t) gridDim.x * blockDim.x) {
+    for (int64_t idx = bid * (int64_t) blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t) nb * blockDim.x) {
         const int64_t wi = idx / q.R;
         const int r = (int) (idx % q.R);
         double v = 0;
@@ -160,6 +179,12 @@ __global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
     }
 }
 
+template <int W>
+__global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
+{
+    leaf_terms_body<W>(q, w, blockIdx.x, gridDim.x);
+}
+
 // Windows of the branch running sum, one warp per window segment (a run of
 // consecutive trees), lane r for term r: the running sum's change into each
 // tree is the sum of its chunks (the first tree's is the sum itself); the
@@ -167,11 +192,11 @@ __global__ void __launch_bounds__(256) k_leaf_terms(QueryParams q, WsDev w)
 // changes (FP64); windows accumulate it times each tree's overlap (B) and
 // the segment's overlap (A); the segment's total change (D) goes to
 // k_span_scan, which gives every segment its starting sum in a fixed order.
-__global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, QueryDev qd,
-    WsDev w)
+__device__ __forceinline__ void span_windows_body(const TSView &ts, const QueryParams &q, const QueryDev &qd, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     const int lane = threadIdx.x & 31;
-    const int64_t u = (int64_t) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t u = (int64_t) bid * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (u >= ts.num_segs) {
         return;
     }
@@ -217,6 +242,12 @@ __global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, 
     if (lane < R) {
         w.D[u * R + lane] = cum;
     }
+}
+
+static __global__ void __launch_bounds__(256) k_span_windows(TSView ts, QueryParams q, QueryDev qd,
+    WsDev w)
+{
+    span_windows_body(ts, q, qd, w, blockIdx.x, gridDim.x);
 }
 
 // Each site's summary, summed over its alleles (skipping the ancestral one
@@ -387,9 +418,10 @@ __device__ __forceinline__ double i128_to_double(__int128 v)
 // pair (low 32 bits unsigned, the rest signed: the 64-bit atomic adds never
 // carry, so their order does not matter and the sums are exact).
 template <int W, int KQ>
-__global__ void __launch_bounds__(256) k_site_sums(TSView ts, QueryParams q, QueryDev qd, WsDev w)
+__device__ __forceinline__ void site_sums_body(const TSView &ts, const QueryParams &q, const QueryDev &qd, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
-    const int64_t site = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
+    const int64_t site = bid * (int64_t) blockDim.x + threadIdx.x;
     const bool valid = site < ts.num_sites;
     const int R = q.R;
     int32_t m0 = 0, m1 = 0, A = 1;
@@ -459,13 +491,20 @@ __global__ void __launch_bounds__(256) k_site_sums(TSView ts, QueryParams q, Que
     }
 }
 
+template <int W, int KQ>
+__global__ void __launch_bounds__(256) k_site_sums(TSView ts, QueryParams q, QueryDev qd, WsDev w)
+{
+    site_sums_body<W, KQ>(ts, q, qd, w, blockIdx.x, gridDim.x);
+}
+
 // The window sums of k_site_sums, each rounded once and scaled by the
 // term's reciprocal denominator.
-__global__ void k_site_sums_finish(QueryParams q, WsDev w)
+__device__ __forceinline__ void site_sums_finish_body(const QueryParams &q, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     const int64_t total = (int64_t) q.Wn * q.R;
-    for (int64_t i = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; i < total;
-         i += (int64_t) gridDim.x * blockDim.x) {
+    for (int64_t i = bid * (int64_t) blockDim.x + threadIdx.x; i < total;
+         i += (int64_t) nb * blockDim.x) {
         const unsigned long long lo = w.site_acc[2 * i];
         const long long hi = (long long) w.site_acc[2 * i + 1];
         const __int128 v = ((__int128) hi << 32) + (__int128) lo;
@@ -473,11 +512,16 @@ __global__ void k_site_sums_finish(QueryParams q, WsDev w)
     }
 }
 
+static __global__ void k_site_sums_finish(QueryParams q, WsDev w)
+{
+    site_sums_finish_body(q, w, blockIdx.x, gridDim.x);
+}
+
 // Per window: the sum of its sites' summaries for every term, one block of
 // 32 warps per window, warp j taking terms j, j + 32, ...: lanes sum strided
 // sites (term-major, coalesced), then a fixed-order warp reduction; with
 // integer numerators the sums are exact (128-bit) and scaled once.
-__global__ void __launch_bounds__(1024) k_site_windows(QueryParams q, QueryDev qd, WsDev w,
+static __global__ void __launch_bounds__(1024) k_site_windows(QueryParams q, QueryDev qd, WsDev w,
     int64_t S, int integer)
 {
     const int64_t wdx = blockIdx.x;
@@ -509,6 +553,108 @@ __global__ void __launch_bounds__(1024) k_site_windows(QueryParams q, QueryDev q
             w.site_win[wdx * q.R + r] = v;
         }
     }
+}
+
+// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one block per r, each thread a
+// contiguous run of units, then a scan of the run totals across the block
+// (warp shuffles, then the warp totals in shared memory); fixed order.
+__device__ __forceinline__ void span_scan_body(const double *D, const double *rs0, double *RS, int64_t NS, int R,
+    const int64_t bid, const int64_t nb)
+{
+    __shared__ double s_warp[16];
+    const int r = bid;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t run = (NS + blockDim.x - 1) / blockDim.x;
+    const int64_t b = (int64_t) threadIdx.x * run < NS ? (int64_t) threadIdx.x * run : NS;
+    const int64_t e = b + run < NS ? b + run : NS;
+    double sum = 0;
+    for (int64_t i = b; i < e; i++) {
+        sum += D[i * R + r];
+    }
+    double incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) {
+            incl += y;
+        }
+    }
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    excl = lane > 0 ? excl : 0.0;
+    if (lane == 31) {
+        s_warp[wid] = incl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = rs0[r];
+        for (int j = 0; j < (int) (blockDim.x >> 5); j++) {
+            const double v = s_warp[j];
+            s_warp[j] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    double acc = s_warp[wid] + excl;
+    for (int64_t i = b; i < e; i++) {
+        RS[i * R + r] = acc;
+        acc += D[i * R + r];
+    }
+}
+
+static __global__ void __launch_bounds__(512) k_span_scan(const double *D, const double *rs0, double *RS,
+    int64_t NS, int R)
+{
+    span_scan_body(D, rs0, RS, NS, R, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void window_reduce_body(const QueryParams &q, const QueryDev &qd, const WsDev &w, int span_normalise, int items_mode, double *result,
+    const int64_t bid, const int64_t nb)
+{
+    const int R = q.R;
+    const int64_t total = (int64_t) q.Wn * R;
+    for (int64_t idx = bid * (int64_t) blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t) nb * blockDim.x) {
+        const int wdx = (int) (idx / R), r = (int) (idx % R);
+        // units: window segments (item pipeline) or spans (general sweep)
+        const int32_t *uwlo = items_mode ? qd.seg_wlo : qd.span_wlo;
+        const int64_t *uwoff = items_mode ? qd.seg_woff : qd.span_woff;
+        const int32_t s0 = items_mode ? qd.win_seg_lo[wdx] : qd.win_span_lo[wdx];
+        const int32_t s1 = items_mode ? qd.win_seg_hi[wdx] : qd.win_span_hi[wdx];
+        double vb = 0, vs = 0;
+        for (int32_t s = s0; s <= s1; s++) {
+            int64_t li = uwoff[s] + (wdx - uwlo[s]);
+            if (q.branch) {
+                vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
+            }
+            if (q.site && !items_mode) {
+                vs += w.SITE[li * R + r];
+            }
+        }
+        if (q.site && items_mode) {
+            vs = w.site_win[(int64_t) wdx * R + r];
+        }
+        if (q.branch && items_mode && w.leaf_win != nullptr) {
+            vb += w.leaf_win[(int64_t) wdx * R + r];
+        }
+        double span = qd.windows[wdx + 1] - qd.windows[wdx];
+        if (span_normalise) {
+            vb /= span;
+            vs /= span;
+        }
+        int64_t o = 0;
+        if (q.branch) {
+            result[idx] = vb;
+            o = total;
+        }
+        if (q.site) {
+            result[o + idx] = vs;
+        }
+    }
+}
+
+static __global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_normalise,
+    int items_mode, double *result)
+{
+    window_reduce_body(q, qd, w, span_normalise, items_mode, result, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tsg

@@ -234,6 +234,65 @@ TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f32_unpol);
 TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f64_pol);
 TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f64_unpol);
 
+// One query of a batched launch (tsg_batch_*), device-resident: the batched
+// kernels give each query its own range of blocks (a prefix array of block
+// counts per stage) and run the query's stage body on its descriptor.
+struct BatchQuery {
+    TSView v;
+    QueryParams p;
+    QueryDev d;
+    WsDev w;
+    double *result;
+    int32_t span_normalise;
+    int32_t pad;
+};
+
+// The query owning global block `blk`: the last b in [0, nq) with
+// off[b] <= blk (queries with no blocks in a stage have off[b] == off[b + 1]).
+__device__ __forceinline__ int batch_find(const int64_t *off, int nq, int64_t blk)
+{
+    int lo = 0, hi = nq;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= blk) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
+}
+
+// Prologue of a batched stage kernel: Q, this block's query; bid, nb: the
+// block's index within the query's range and the range's length.
+#define TSG_BATCH_QUERY()                                                     \
+    const int b_ = batch_find(off, nq, (int64_t) blockIdx.x);                \
+    const BatchQuery &Q = bq[b_];                                             \
+    const int64_t bid = (int64_t) blockIdx.x - off[b_];                       \
+    const int64_t nb = off[b_ + 1] - off[b_]
+
+// The chunk evaluation of a batch (kq as above): item branch lengths, then
+// item values, each one launch over the batch's queries.
+#define TSG_CHUNK_EVAL_BATCH_LAUNCHER(name)                                              \
+    void name(int kq, cudaStream_t st, const BatchQuery *bq, int nq, const int64_t *off_bls, \
+        int64_t blocks_bls, const int64_t *off_eval, int64_t blocks_eval)
+TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f32_pol);
+TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f32_unpol);
+TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f64_pol);
+TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f64_unpol);
+
+// The other stages of a batch (tsg_batch.cu).
+enum BatchStage {
+    BS_ZERO, BS_NODE_MASK, BS_PREFIX, BS_ANCHORS, BS_BLS, BS_EVAL, BS_SPAN_WINDOWS,
+    BS_LEAF_AREAS, BS_LEAF_PREFIX, BS_LEAF_TERMS, BS_SITE_SUMS, BS_SITE_FINISH, BS_SPAN_SCAN,
+    BS_REDUCE, BS_COUNT
+};
+int batch_launch_stage(int stage, int kq, int64_t blocks, cudaStream_t st, const BatchQuery *bq,
+    int nq, const int64_t *off);
+int batch_launch_replay(int kq, unsigned grid, size_t smem, cudaStream_t st, const BatchQuery *bq,
+    int nq, const int64_t *span_off, int32_t *counter);
+void *batch_replay_kernel(int kq);
+
 }  // namespace tsg
 
 #include "tsg_terms.cuh"

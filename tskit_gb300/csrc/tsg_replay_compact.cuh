@@ -122,18 +122,50 @@ __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &q
     }
 }
 
+// Span s of the compact plan, by one block: the span-start parents and
+// counts, then warp 0 replays the span's trees.  Ends with the block
+// synchronised.
+template <int KQ>
+__device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams &q,
+    const QueryDev &qd, const WsDev &w, int s, unsigned char *smem_raw,
+    TouchEntry<KQ> *s_list, ReplayStage *s_stage, uint64_t *s_pre, uint64_t *s_wsum)
+{
+    SpanState<uint16_t> sp = span_state_at<uint16_t>(smem_raw, ts.c_max_local, KQ);
+    sp.cnt = nullptr;
+    const int32_t t0 = ts.c_span_tree[s], t1 = ts.c_span_tree[s + 1];
+    const int64_t lo = ts.c_local_off[s];
+    const int32_t Ls = (int32_t) (ts.c_local_off[s + 1] - lo);
+    sp.time = ts.c_time + lo;
+    // parents at the span start (0x7FFF, no parent, is the replay's
+    // "no parent" entry)
+    for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
+        sp.par[l] = ts.c_par0[lo + l];
+    }
+    compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum);
+    if (threadIdx.x < 32) {
+        replay_span<16, KQ, uint16_t, false>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
+            t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
+    }
+    __syncthreads();
+}
+
+// The block-shared arrays of the compact replay besides the span state.
+template <int KQ>
+struct CompactShared {
+    TouchEntry<KQ> list[TSG_TOUCH_CAP];  // the open touch list
+    ReplayStage stage[4];                // prefetch ring, trees t .. t + 3
+    uint64_t pre[2 * (TSG_COMPACT_THREADS + 1)];
+    uint64_t wsum[2 * (TSG_COMPACT_THREADS / 32)];
+};
+
+// Persistent blocks take spans from the query's counter until none is left.
 template <int KQ>
 __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView ts, QueryParams q,
     QueryDev qd, WsDev w)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_span;
-    __shared__ TouchEntry<KQ> s_list[TSG_TOUCH_CAP];  // the open touch list
-    __shared__ ReplayStage s_stage[4];                 // prefetch ring, trees t .. t + 3
-    __shared__ uint64_t s_pre[2 * (TSG_COMPACT_THREADS + 1)];
-    __shared__ uint64_t s_wsum[2 * (TSG_COMPACT_THREADS / 32)];
-    SpanState<uint16_t> sp = span_state_at<uint16_t>(smem_raw, ts.c_max_local, KQ);
-    sp.cnt = nullptr;
+    __shared__ CompactShared<KQ> sh;
     for (;;) {
         if (threadIdx.x == 0) {
             s_span = atomicAdd(w.counter, 1);
@@ -144,21 +176,7 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
         if (s >= ts.c_num_spans) {
             break;
         }
-        const int32_t t0 = ts.c_span_tree[s], t1 = ts.c_span_tree[s + 1];
-        const int64_t lo = ts.c_local_off[s];
-        const int32_t Ls = (int32_t) (ts.c_local_off[s + 1] - lo);
-        sp.time = ts.c_time + lo;
-        // parents at the span start (0x7FFF, no parent, is the replay's
-        // "no parent" entry)
-        for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
-            sp.par[l] = ts.c_par0[lo + l];
-        }
-        compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum);
-        if (threadIdx.x < 32) {
-            replay_span<16, KQ, uint16_t, false>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
-                t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
-        }
-        __syncthreads();
+        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.pre, sh.wsum);
     }
 }
 
@@ -167,8 +185,8 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
 // [1024 b, 1024 (b + 1)), first summing every sample before them (a strided
 // sum and a block reduction; the orders are short), then scanning its own.
 template <int KQ>
-__global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams q, QueryDev qd,
-    uint64_t *P0)
+__device__ __forceinline__ void compact_prefix_body(const TSView &ts, const QueryParams &q, const QueryDev &qd, uint64_t *P0,
+    const int64_t bid, const int64_t nb)
 {
     __shared__ uint64_t s_w[2 * 32];
     __shared__ uint64_t s_off[2];
@@ -176,7 +194,7 @@ __global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams 
     const uint16_t *order = ts.c_order;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nw = (int) (blockDim.x >> 5);
-    const int64_t base = (int64_t) blockIdx.x * blockDim.x;
+    const int64_t base = (int64_t) bid * blockDim.x;
     // the samples before this block
     uint64_t pre_lo = 0, pre_hi = 0;
     for (int64_t i = tid; i < base && i < n; i += blockDim.x) {
@@ -246,22 +264,36 @@ __global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams 
     }
 }
 
+template <int KQ>
+__global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams q, QueryDev qd,
+    uint64_t *P0)
+{
+    compact_prefix_body<KQ>(ts, q, qd, P0, blockIdx.x, gridDim.x);
+}
+
 // The first tree's items: one per anchor (a stateful node alive in the first
 // tree, in edge order) with its counts, P0[hi] - P0[lo], and its parent, in
 // the anchors' numbering.
 template <int KQ>
-__global__ void k_compact_anchors(TSView ts, const uint64_t *P0, WsDev w)
+__device__ __forceinline__ void compact_anchors_body(const TSView &ts, const uint64_t *P0, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     Item<KQ> *items = (Item<KQ> *) w.items;
     const int64_t base = ts.tree_item_off[0];
-    for (int64_t k = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; k < ts.c_num_anchors;
-         k += (int64_t) gridDim.x * blockDim.x) {
+    for (int64_t k = bid * (int64_t) blockDim.x + threadIdx.x; k < ts.c_num_anchors;
+         k += (int64_t) nb * blockDim.x) {
         const int2 r = ts.c_anchor_range[k];
         Pack x;
         x.lo = P0[2 * r.y] - P0[2 * r.x];
         x.hi = P0[2 * r.y + 1] - P0[2 * r.x + 1];
         item_put<KQ>(items + base + k, Pack{0, 0}, x, (int32_t) k, -1, ts.c_anchor_par[k]);
     }
+}
+
+template <int KQ>
+__global__ void k_compact_anchors(TSView ts, const uint64_t *P0, WsDev w)
+{
+    compact_anchors_body<KQ>(ts, P0, w, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tsg

@@ -372,14 +372,15 @@ __device__ __forceinline__ void eval_span_chunks(const TSView &ts, const QueryPa
 // lengths in the evaluation's arithmetic, (bl1, bl0) -- in the integer form
 // (bl1 - bl0, bl0) for an item with the same counts before and after.
 template <typename F, int KQ>
-__global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDev w)
+__device__ __forceinline__ void item_bls_body(const TSView &ts, const QueryParams &q, const WsDev &w,
+    const int64_t bid, const int64_t nb)
 {
     const int lane = threadIdx.x & 31;
     const Item<KQ> *items = (const Item<KQ> *) w.items;
     const bool num_form = sizeof(F) == sizeof(double) && q.site_int;
     F *bls = (F *) w.bl;
-    const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
-    for (int64_t c = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t) nb * (blockDim.x >> 5);
+    for (int64_t c = bid * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
          c < ts.num_chunks; c += nwarps) {
         const double *time = ts.c_time + ts.c_local_off[ts.c_chunk_span[c]];
         for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
@@ -395,6 +396,12 @@ __global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDe
             bls[2 * i + 1] = (F) bl0;
         }
     }
+}
+
+template <typename F, int KQ>
+__global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDev w)
+{
+    item_bls_body<F, KQ>(ts, q, w, blockIdx.x, gridDim.x);
 }
 
 // A summary term's integer numerator with its type fixed at compile time
@@ -472,8 +479,8 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
 // eval_chunk); otherwise the summary functions in F (FP32: exact item
 // values into a compensated pair).
 template <typename F, bool UNPOL, int KQ>
-__global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
-    int64_t total_warps)
+__device__ __forceinline__ void eval_grouped_body(const TSView &ts, const QueryParams &q, const WsDev &w, int64_t total_warps,
+    const int64_t bid, const int64_t nb)
 {
     constexpr bool F32 = sizeof(F) == sizeof(float);
     const int lane = threadIdx.x & 31;
@@ -482,8 +489,8 @@ __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, 
     const int64_t C = ts.num_chunks;
     const int R = q.R;
     const bool num_form = !F32 && q.site_int;
-    const int64_t nwarps = (int64_t) gridDim.x * (blockDim.x >> 5);
-    for (int64_t gw = blockIdx.x * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t) nb * (blockDim.x >> 5);
+    for (int64_t gw = bid * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
          gw < total_warps; gw += nwarps) {
         // consecutive warps share a block of chunks, so a chunk's items are
         // read by the type groups while they are still in cache
@@ -576,6 +583,13 @@ __global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, 
         }
         w.dD[c * R + r] = (double) acc + (double) lo;
     }
+}
+
+template <typename F, bool UNPOL, int KQ>
+__global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
+    int64_t total_warps)
+{
+    eval_grouped_body<F, UNPOL, KQ>(ts, q, w, total_warps, blockIdx.x, gridDim.x);
 }
 
 template <int W, int KQ, typename IdxT, typename F, bool UNPOL, bool EVAL>

@@ -491,96 +491,6 @@ static int64_t smem_budget(const void *kernel)
     return (int64_t) optin - (int64_t) attr.sharedSizeBytes;
 }
 
-// RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one block per r, each thread a
-// contiguous run of units, then a scan of the run totals across the block
-// (warp shuffles, then the warp totals in shared memory); fixed order.
-__global__ void __launch_bounds__(512) k_span_scan(const double *D, const double *rs0, double *RS,
-    int64_t NS, int R)
-{
-    __shared__ double s_warp[16];
-    const int r = blockIdx.x;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t run = (NS + blockDim.x - 1) / blockDim.x;
-    const int64_t b = (int64_t) threadIdx.x * run < NS ? (int64_t) threadIdx.x * run : NS;
-    const int64_t e = b + run < NS ? b + run : NS;
-    double sum = 0;
-    for (int64_t i = b; i < e; i++) {
-        sum += D[i * R + r];
-    }
-    double incl = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) {
-            incl += y;
-        }
-    }
-    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
-    excl = lane > 0 ? excl : 0.0;
-    if (lane == 31) {
-        s_warp[wid] = incl;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double acc = rs0[r];
-        for (int j = 0; j < (int) (blockDim.x >> 5); j++) {
-            const double v = s_warp[j];
-            s_warp[j] = acc;
-            acc += v;
-        }
-    }
-    __syncthreads();
-    double acc = s_warp[wid] + excl;
-    for (int64_t i = b; i < e; i++) {
-        RS[i * R + r] = acc;
-        acc += D[i * R + r];
-    }
-}
-
-__global__ void k_window_reduce(QueryParams q, QueryDev qd, WsDev w, int span_normalise,
-    int items_mode, double *result)
-{
-    const int R = q.R;
-    const int64_t total = (int64_t) q.Wn * R;
-    for (int64_t idx = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t) gridDim.x * blockDim.x) {
-        const int wdx = (int) (idx / R), r = (int) (idx % R);
-        // units: window segments (item pipeline) or spans (general sweep)
-        const int32_t *uwlo = items_mode ? qd.seg_wlo : qd.span_wlo;
-        const int64_t *uwoff = items_mode ? qd.seg_woff : qd.span_woff;
-        const int32_t s0 = items_mode ? qd.win_seg_lo[wdx] : qd.win_span_lo[wdx];
-        const int32_t s1 = items_mode ? qd.win_seg_hi[wdx] : qd.win_span_hi[wdx];
-        double vb = 0, vs = 0;
-        for (int32_t s = s0; s <= s1; s++) {
-            int64_t li = uwoff[s] + (wdx - uwlo[s]);
-            if (q.branch) {
-                vb += w.RS[(int64_t) s * R + r] * w.A[li] + w.B[li * R + r];
-            }
-            if (q.site && !items_mode) {
-                vs += w.SITE[li * R + r];
-            }
-        }
-        if (q.site && items_mode) {
-            vs = w.site_win[(int64_t) wdx * R + r];
-        }
-        if (q.branch && items_mode && w.leaf_win != nullptr) {
-            vb += w.leaf_win[(int64_t) wdx * R + r];
-        }
-        double span = qd.windows[wdx + 1] - qd.windows[wdx];
-        if (span_normalise) {
-            vb /= span;
-            vs /= span;
-        }
-        int64_t o = 0;
-        if (q.branch) {
-            result[idx] = vb;
-            o = total;
-        }
-        if (q.site) {
-            result[o + idx] = vs;
-        }
-    }
-}
-
 static int grid_for(int64_t n, int block = 256)
 {
     int64_t g = (n + block - 1) / block;
@@ -717,7 +627,11 @@ extern "C" {
 int tsg_query_free(tsg_query_t *q)
 {
     if (q != nullptr) {
-        cudaFree(q->dbuf);
+        // stream-ordered: no device-wide synchronisation (a serving loop
+        // frees queries while other streams run)
+        if (q->dbuf != nullptr) {
+            cudaFreeAsync(q->dbuf, 0);
+        }
         delete q;
     }
     return 0;
@@ -1726,8 +1640,9 @@ extern "C" {
 
 static int query_upload(tsg_query_t *q, tsg_query_t **out)
 {
-    if (cudaMalloc(&q->dbuf, q->blob.size()) != cudaSuccess) {
+    if (cudaMallocAsync(&q->dbuf, q->blob.size(), 0) != cudaSuccess) {
         cudaGetLastError();
+        q->dbuf = nullptr;
         delete q;
         return TSG_ERR_NO_MEMORY;
     }
@@ -2012,6 +1927,312 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         item_pipeline ? 1 : 0, result);
     TSG_LAUNCHED();
     return 0;
+}
+
+// ------------------------------------------------------------ batched launch
+// A batch fuses prepared queries on any resident tree sequences into one
+// launch per pipeline stage.  Sample-count queries on the compact replay are
+// grouped by count words and arithmetic (the kernels' template forms); every
+// group runs each stage as one kernel over its queries (tsg_batch.cu), the
+// replay as one persistent kernel over all the group's spans.  Other queries
+// (allele frequency spectrum, relatedness vector, the general replay) run
+// their own launches in the same stream.  Each query keeps its own region of
+// the batch workspace, bound when the batch is made.
+struct tsg_batch {
+    struct Group {
+        int kq = 1, f32 = 0, pol = 0;
+        std::vector<int> idx;           // queries of the group
+        int64_t blocks[BS_COUNT] = {};  // blocks of each stage over the group
+        int64_t stage_off = 0;          // offset of the group's stage arrays in dbuf
+        int64_t span_off = 0;           // ... of its span prefix
+        int64_t desc_off = 0;           // ... of its descriptors
+        int64_t spans = 0;
+        int64_t max_local = 0;
+        bool branch = false, site = false;
+        int32_t *counter = nullptr;     // the replay's span counter (workspace)
+    };
+    std::vector<const tsg_query_t *> q;
+    std::vector<double *> results;
+    std::vector<int64_t> ws_off;
+    std::vector<Group> groups;
+    std::vector<int> single;
+    char *ws_base = nullptr;
+    void *dbuf = nullptr;
+};
+
+namespace tsg {
+
+static bool batch_fusable(const tsg_query_t *q)
+{
+    const tsg_treeseq_t *ts = q->ts;
+    return q->kind == TSG_KIND_STATS && q->smem && q->compact_ok && ts->v.c_num_spans > 0
+        && q->W == 16 && (!q->p.site || (q->p.site_int && ts->v.num_sites > 0));
+}
+
+// Blocks of each stage for one fusable query, as its own launch sizes them.
+static void batch_stage_blocks(const tsg_query_t *q, int64_t *nb)
+{
+    const tsg_treeseq_t *ts = q->ts;
+    const QueryParams &p = q->p;
+    const int64_t R = p.R;
+    for (int k = 0; k < BS_COUNT; k++) {
+        nb[k] = 0;
+    }
+    const int64_t leaf = p.branch ? ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 3 : 0;
+    const int64_t site = p.site && p.site_int ? (int64_t) p.Wn * R * 2 : 0;
+    nb[BS_ZERO] = std::min<int64_t>((1 + R + leaf + site + 255) / 256, 4096);
+    nb[BS_NODE_MASK] = grid_for(ts->v.num_nodes);
+    if (p.branch) {
+        if (ts->v.c_num_anchors > 0) {
+            nb[BS_PREFIX] = (ts->v.num_samples + 1023) / 1024;
+            nb[BS_ANCHORS] = grid_for(ts->v.c_num_anchors);
+        }
+        const int64_t C = ts->v.num_chunks;
+        const int64_t total = (C + TSG_EVAL_BLOCK - 1) / TSG_EVAL_BLOCK * p.gwpb;
+        nb[BS_BLS] = std::min<int64_t>((C + 7) / 8, 1 << 20);
+        nb[BS_EVAL] = std::min<int64_t>((total + 7) / 8, 1 << 20);
+        nb[BS_SPAN_WINDOWS] = (ts->v.num_segs + 7) / 8;
+        nb[BS_LEAF_AREAS] = ts->v.num_edges > 0 ? grid_for(ts->v.num_edges) : 0;
+        nb[BS_LEAF_PREFIX] = (int64_t) 1 << p.K;
+        nb[BS_LEAF_TERMS] = grid_for((int64_t) p.Wn * R);
+        nb[BS_SPAN_SCAN] = R;
+    }
+    if (p.site) {
+        nb[BS_SITE_SUMS] = (ts->v.num_sites + 255) / 256;
+        nb[BS_SITE_FINISH] = grid_for((int64_t) p.Wn * R);
+    }
+    nb[BS_REDUCE] = grid_for((int64_t) p.Wn * R);
+}
+
+}  // namespace tsg
+
+int tsg_batch_workspace_bytes(uint64_t num_queries, const tsg_query_t *const *queries,
+    int64_t *bytes)
+{
+    if (queries == nullptr || bytes == nullptr) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    int64_t off = 0;
+    for (uint64_t i = 0; i < num_queries; i++) {
+        if (queries[i] == nullptr) {
+            return TSG_ERR_BAD_PARAM_VALUE;
+        }
+        off += align_up(queries[i]->ws_bytes, 256);
+    }
+    *bytes = off + 256 * 8;  // the groups' span counters
+    return 0;
+}
+
+int tsg_batch_create(tsg_batch_t **out, uint64_t num_queries, const tsg_query_t *const *queries,
+    double *const *results, tsg_workspace_t *ws)
+{
+    if (out == nullptr || results == nullptr || ws == nullptr || num_queries == 0) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    int64_t need = 0;
+    int ret = tsg_batch_workspace_bytes(num_queries, queries, &need);
+    if (ret != 0) {
+        return ret;
+    }
+    if (ws->bytes < need) {
+        return TSG_ERR_WORKSPACE_TOO_SMALL;
+    }
+    tsg_batch_t *b = new tsg_batch_t();
+    b->ws_base = (char *) ws->ptr;
+    int64_t off = 0;
+    for (uint64_t i = 0; i < num_queries; i++) {
+        b->q.push_back(queries[i]);
+        b->results.push_back(results[i]);
+        b->ws_off.push_back(off);
+        off += align_up(queries[i]->ws_bytes, 256);
+    }
+    // groups by the kernels' template forms (at most eight of them share
+    // the span-counter words at the workspace's end)
+    for (uint64_t i = 0; i < num_queries; i++) {
+        const tsg_query_t *q = queries[i];
+        if (!batch_fusable(q)) {
+            b->single.push_back((int) i);
+            continue;
+        }
+        tsg_batch_t::Group *g = nullptr;
+        for (auto &h : b->groups) {
+            if (h.kq == q->KQ && h.f32 == q->p.f32 && h.pol == q->p.polarised) {
+                g = &h;
+            }
+        }
+        if (g == nullptr) {
+            b->groups.emplace_back();
+            g = &b->groups.back();
+            g->kq = q->KQ;
+            g->f32 = q->p.f32;
+            g->pol = q->p.polarised;
+        }
+        g->idx.push_back((int) i);
+    }
+    // device image: per group its descriptors, stage prefix arrays and span
+    // prefix
+    std::vector<char> img;
+    auto grow = [&](int64_t bytes) {
+        const int64_t at = align_up((int64_t) img.size(), 256);
+        img.resize((size_t) (at + bytes), 0);
+        return at;
+    };
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        auto &g = b->groups[gi];
+        const int nq = (int) g.idx.size();
+        g.counter = (int32_t *) (b->ws_base + off + 256 * (int64_t) gi);
+        g.desc_off = grow((int64_t) nq * (int64_t) sizeof(BatchQuery));
+        g.stage_off = grow((int64_t) BS_COUNT * (nq + 1) * 8);
+        g.span_off = grow((int64_t) (nq + 1) * 8);
+        for (int j = 0; j < nq; j++) {
+            const tsg_query_t *q = queries[g.idx[(size_t) j]];
+            tsg_workspace_t region{b->ws_base + b->ws_off[(size_t) g.idx[(size_t) j]], q->ws_bytes};
+            BatchQuery d;
+            memset(&d, 0, sizeof(d));
+            d.v = q->ts->v;
+            d.p = q->p;
+            d.w = ws_bind(q, &region);
+            d.d = q->d;
+            d.d.node_mask = d.w.node_mask;
+            d.result = results[g.idx[(size_t) j]];
+            d.span_normalise = q->span_normalise;
+            memcpy(img.data() + g.desc_off + (int64_t) j * (int64_t) sizeof(BatchQuery), &d,
+                sizeof(d));
+            int64_t nb[BS_COUNT];
+            batch_stage_blocks(q, nb);
+            int64_t *so = (int64_t *) (img.data() + g.stage_off);
+            for (int k = 0; k < BS_COUNT; k++) {
+                so[(int64_t) k * (nq + 1) + j + 1] = so[(int64_t) k * (nq + 1) + j] + nb[k];
+            }
+            int64_t *sp = (int64_t *) (img.data() + g.span_off);
+            sp[j + 1] = sp[j] + q->ts->v.c_num_spans;
+            g.branch = g.branch || q->p.branch;
+            g.site = g.site || q->p.site;
+            g.max_local = std::max<int64_t>(g.max_local, q->ts->v.c_max_local);
+        }
+        const int64_t *so = (const int64_t *) (img.data() + g.stage_off);
+        for (int k = 0; k < BS_COUNT; k++) {
+            g.blocks[k] = so[(int64_t) k * (nq + 1) + nq];
+        }
+        g.spans = ((const int64_t *) (img.data() + g.span_off))[nq];
+    }
+    if (!img.empty()) {
+        if (cudaMallocAsync(&b->dbuf, img.size(), 0) != cudaSuccess) {
+            cudaGetLastError();
+            b->dbuf = nullptr;
+            delete b;
+            return TSG_ERR_NO_MEMORY;
+        }
+        if (cudaMemcpy(b->dbuf, img.data(), img.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFreeAsync(b->dbuf, 0);
+            delete b;
+            return TSG_ERR_CUDA;
+        }
+    }
+    *out = b;
+    return 0;
+}
+
+int tsg_batch_launch(const tsg_batch_t *b, void *cuda_stream)
+{
+    if (b == nullptr) {
+        return TSG_ERR_BAD_PARAM_VALUE;
+    }
+    cudaStream_t st = (cudaStream_t) cuda_stream;
+    const char *base = (const char *) b->dbuf;
+    for (const auto &g : b->groups) {
+        const int nq = (int) g.idx.size();
+        const BatchQuery *bq = (const BatchQuery *) (base + g.desc_off);
+        auto off = [&](int k) { return (const int64_t *) (base + g.stage_off) + (int64_t) k * (nq + 1); };
+        auto stage = [&](int k) {
+            int r = batch_launch_stage(k, g.kq, g.blocks[k], st, bq, nq, off(k));
+            if (r == 0 && g.blocks[k] > 0) {
+                TSG_LAUNCHED();
+            }
+            return r;
+        };
+        int ret = 0;
+        TSG_CUDA(cudaMemsetAsync(g.counter, 0, sizeof(int32_t), st));
+        if ((ret = stage(BS_ZERO)) != 0 || (ret = stage(BS_NODE_MASK)) != 0
+            || (ret = stage(BS_PREFIX)) != 0 || (ret = stage(BS_ANCHORS)) != 0) {
+            return ret;
+        }
+        const size_t csb = (size_t) align_up(replay_state_bytes(g.max_local, 16, g.kq), 16);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_replay_kernel(g.kq),
+            TSG_COMPACT_THREADS, csb);
+        const unsigned grid = (unsigned) std::min<int64_t>(
+            (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()), g.spans);
+        if ((ret = batch_launch_replay(g.kq, grid, csb, st, bq, nq,
+                 (const int64_t *) (base + g.span_off), g.counter)) != 0) {
+            return ret;
+        }
+        TSG_LAUNCHED();
+        if (g.branch) {
+            if (g.f32) {
+                (g.pol ? launch_eval_chunks_batch_f32_pol : launch_eval_chunks_batch_f32_unpol)(
+                    g.kq, st, bq, nq, off(BS_BLS), g.blocks[BS_BLS], off(BS_EVAL), g.blocks[BS_EVAL]);
+            } else {
+                (g.pol ? launch_eval_chunks_batch_f64_pol : launch_eval_chunks_batch_f64_unpol)(
+                    g.kq, st, bq, nq, off(BS_BLS), g.blocks[BS_BLS], off(BS_EVAL), g.blocks[BS_EVAL]);
+            }
+            TSG_LAUNCHED();
+            TSG_LAUNCHED();
+            if (cudaGetLastError() != cudaSuccess) {
+                return TSG_ERR_CUDA;
+            }
+        }
+        const int rest[] = {BS_SPAN_WINDOWS, BS_LEAF_AREAS, BS_LEAF_PREFIX, BS_LEAF_TERMS,
+            BS_SITE_SUMS, BS_SITE_FINISH, BS_SPAN_SCAN, BS_REDUCE};
+        for (int k : rest) {
+            if ((ret = stage(k)) != 0) {
+                return ret;
+            }
+        }
+    }
+    for (int i : b->single) {
+        const tsg_query_t *q = b->q[(size_t) i];
+        tsg_workspace_t region{b->ws_base + b->ws_off[(size_t) i], q->ws_bytes};
+        int ret = tsg_query_launch(q, &region, b->results[(size_t) i], cuda_stream);
+        if (ret != 0) {
+            return ret;
+        }
+    }
+    return 0;
+}
+
+int tsg_batch_num_fused(const tsg_batch_t *b)
+{
+    int n = 0;
+    for (const auto &g : b->groups) {
+        n += (int) g.idx.size();
+    }
+    return n;
+}
+
+int tsg_batch_check(const tsg_batch_t *b, uint64_t *failed)
+{
+    for (size_t i = 0; i < b->q.size(); i++) {
+        tsg_workspace_t region{b->ws_base + b->ws_off[i], b->q[i]->ws_bytes};
+        const int ret = tsg_workspace_check(&region, b->q[i]);
+        if (ret != 0) {
+            if (failed != nullptr) {
+                *failed = (uint64_t) i;
+            }
+            return ret;
+        }
+    }
+    return 0;
+}
+
+void tsg_batch_free(tsg_batch_t *b)
+{
+    if (b != nullptr) {
+        if (b->dbuf != nullptr) {
+            cudaFreeAsync(b->dbuf, 0);
+        }
+        delete b;
+    }
 }
 
 // Error word of the last launch on this workspace (synchronous read).

@@ -4,13 +4,18 @@ Several tree sequences stay on the device with their span plans.  Requests
 (diversity, divergence, Fst, allele frequency spectrum, relatedness x
 vectors) arrive over time; the loop
 
-* admits every request that has arrived,
-* batches compatible waiting requests into one fused launch -- sample-count
-  statistics on the same tree sequence, mode and windows share one sweep
-  (up to 8 sample sets; 4 when sample counts need 32 bits), and
-  relatedness-vector requests on the same tree sequence and windows share
-  one product with their weight columns side by side,
-* launches a batch as soon as a stream slot is free and the device memory
+* admits every request that has arrived, rejecting (and counting) those whose
+  result alone exceeds the output cap,
+* fuses compatible waiting requests into one query -- sample-count statistics
+  on the same tree sequence, mode and windows share one sweep (up to 8
+  sample sets; 4 when sample counts need 32 bits), and relatedness-vector
+  requests on the same tree sequence and windows share one product with
+  their weight columns side by side,
+* groups up to ``group_size`` such fused queries -- on any of the resident
+  tree sequences -- into one batched launch (``QueryBatch``: one kernel per
+  pipeline stage for all of them, the replay one persistent kernel over all
+  their spans),
+* launches a group as soon as a stream slot is free and the device memory
   its workspace needs fits the budget (continuous batching: new requests
   join while earlier launches are still running, and launches on different
   slots overlap on the device),
@@ -26,6 +31,7 @@ the batched loop is compared with.
 from __future__ import annotations
 
 import time
+from collections import deque
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -63,7 +69,8 @@ def poisson_requests(resident, num, rate, seed, window_choices=(1, 10, 100, 1000
     ``sequence_length``): statistics drawn uniformly, sample sets of
     set_range samples (uniform), windows equal over the genome with a count
     drawn from window_choices, mode branch or site (relatedness vectors are
-    branch-only)."""
+    branch-only).  Requests are kept as drawn: the server rejects those
+    whose result is too large."""
     rng = np.random.default_rng(seed)
     keys = sorted(resident)
     stats = list(KINDS)
@@ -86,11 +93,6 @@ def poisson_requests(resident, num, rate, seed, window_choices=(1, 10, 100, 1000
         sets = [np.sort(perm[j * m:(j + 1) * m]) for j in range(nsets)]
         weights = None
         if stat == "relatedness_vector":
-            # an output of windows x samples x columns: at most 64 MiB
-            cap = max(1, (64 << 20) // (len(samples) * rv_columns * 8))
-            if nwin > cap:
-                nwin = 1
-                windows = None
             sets = []
             weights = rng.normal(size=(len(samples), rv_columns))
         out.append(Request(rid, t, key, stat, sets, windows, mode, weights))
@@ -99,7 +101,8 @@ def poisson_requests(resident, num, rate, seed, window_choices=(1, 10, 100, 1000
 
 @dataclass
 class Batch:
-    requests: list
+    requests: list            # every request of the launch
+    groups: list = None       # its fused queries (lists of requests)
     work: object = None       # the backend's launch record
     slot: int = -1
     nbytes: int = 0
@@ -109,11 +112,13 @@ class Batch:
 @dataclass
 class ServeStats:
     mode: str
-    num: int
+    num: int                  # requests served
     wall_s: float
     latencies_s: np.ndarray
     launches: int
     results: dict = field(default_factory=dict)
+    rejected: list = field(default_factory=list)  # request ids over the output cap
+    fused_queries: int = 0    # fused queries launched (groups hold several)
 
     @property
     def queries_per_s(self):
@@ -123,68 +128,134 @@ class ServeStats:
         return float(np.percentile(self.latencies_s, p) * 1e3) if self.num else 0.0
 
     def summary(self):
-        return {"mode": self.mode, "queries": self.num, "wall_s": round(self.wall_s, 4),
+        return {"mode": self.mode, "queries": self.num, "rejected": len(self.rejected),
+                "wall_s": round(self.wall_s, 4),
                 "queries_per_s": round(self.queries_per_s, 2),
                 "p50_ms": round(self.percentile_ms(50), 3),
-                "p99_ms": round(self.percentile_ms(99), 3), "launches": self.launches}
+                "p99_ms": round(self.percentile_ms(99), 3), "launches": self.launches,
+                "fused_queries": self.fused_queries}
+
+
+class _Pending:
+    """Waiting requests in arrival order, with a queue per batch key; taken
+    requests are dropped lazily from both."""
+
+    def __init__(self):
+        self.order = deque()
+        self.by_key = {}
+        self.taken = set()
+        self.count = 0
+
+    def add(self, r):
+        self.order.append(r)
+        self.by_key.setdefault(r.batch_key(), deque()).append(r)
+        self.count += 1
+
+    def take(self, reqs):
+        for r in reqs:
+            self.taken.add(r.rid)
+        self.count -= len(reqs)
+
+    def _trim(self, q):
+        while q and q[0].rid in self.taken:
+            q.popleft()
+
+    def untaken(self):
+        """Waiting requests, oldest first."""
+        self._trim(self.order)
+        for r in self.order:
+            if r.rid not in self.taken:
+                yield r
+
+    def key_queue(self, key):
+        q = self.by_key.get(key)
+        if q is not None:
+            self._trim(q)
+        return q or ()
+
+    def __bool__(self):
+        return self.count > 0
 
 
 class Server:
     """The request loop over a backend (see GpuBackend for the interface)."""
 
     def __init__(self, backend, num_slots=8, hbm_budget=64 << 30, max_batch=32,
-                 max_output_bytes=256 << 20):
+                 max_output_bytes=256 << 20, group_size=8, scan_limit=128):
         self.backend = backend
         self.num_slots = num_slots
         self.hbm_budget = hbm_budget
         self.max_batch = max_batch
         self.max_output_bytes = max_output_bytes
+        self.group_size = group_size
+        self.scan_limit = scan_limit
 
-    def _form_batch(self, pending):
-        """The oldest waiting request and the compatible ones behind it."""
-        head = pending[0]
-        key = head.batch_key()
+    def _fuse(self, pend, head, chosen):
+        """The request `head` and the compatible waiting ones behind it."""
         taken = [head]
-        if head.kind != "afs":
-            sets_cap = self.backend.max_sets(head.ts)
-            nsets = len(head.sample_sets)
-            nwin = 1 if head.windows is None else len(head.windows) - 1
-            cols = 0 if head.weights is None else head.weights.shape[1]
-            for r in pending[1:]:
-                if len(taken) >= self.max_batch:
-                    break
-                if r.batch_key() != key or (r.windows is not None and not np.array_equal(
-                        r.windows, head.windows)):
+        if head.kind == "afs":
+            return taken
+        sets_cap = self.backend.max_sets(head.ts)
+        nsets = len(head.sample_sets)
+        nwin = 1 if head.windows is None else len(head.windows) - 1
+        cols = 0 if head.weights is None else head.weights.shape[1]
+        out_cap = self.max_output_bytes
+        for i, r in enumerate(pend.key_queue(head.batch_key())):
+            if len(taken) >= self.max_batch or i >= self.scan_limit:
+                break
+            if r is head or r.rid in chosen or r.rid in pend.taken:
+                continue
+            if r.windows is not None and not np.array_equal(r.windows, head.windows):
+                continue
+            if head.kind == "counts":
+                if nsets + len(r.sample_sets) > sets_cap:
                     continue
-                if head.kind == "counts":
-                    if nsets + len(r.sample_sets) > sets_cap:
-                        continue
-                    nsets += len(r.sample_sets)
-                else:
-                    c = cols + r.weights.shape[1]
-                    if nwin * len(r.weights) * c * 8 > self.max_output_bytes:
-                        continue
-                    cols = c
-                taken.append(r)
+                nsets += len(r.sample_sets)
+            else:
+                c = cols + r.weights.shape[1]
+                if nwin * len(r.weights) * c * 8 > out_cap:
+                    continue
+                cols = c
+            taken.append(r)
         return taken
+
+    def _form_group(self, pend):
+        """Up to group_size fused queries, oldest requests first."""
+        chosen = set()
+        groups = []
+        for head in pend.untaken():
+            if head.rid in chosen:
+                continue
+            g = self._fuse(pend, head, chosen)
+            chosen.update(r.rid for r in g)
+            groups.append(g)
+            if len(groups) >= self.group_size:
+                break
+        return groups
 
     def run(self, requests, mode="batched", clock=time.perf_counter, idle=None):
         reqs = sorted(requests, key=lambda r: r.arrival)
         n = len(reqs)
-        lat = np.zeros(n)
+        lat = np.full(n, np.nan)
         pos = {r.rid: i for i, r in enumerate(reqs)}
         results = {}
-        pending = []
+        rejected = []
+        pend = _Pending()
         busy = {}  # slot -> Batch
         slot_bytes = [0] * self.num_slots
         nxt = 0
         done = 0
         launches = 0
+        fused = 0
         t0 = clock()
-        while done < n:
+        while done + len(rejected) < n:
             now = clock() - t0
             while nxt < n and reqs[nxt].arrival <= now:
-                pending.append(reqs[nxt])
+                r = reqs[nxt]
+                if self.backend.output_bytes(r) > self.max_output_bytes:
+                    rejected.append(r.rid)
+                else:
+                    pend.add(r)
                 nxt += 1
             progressed = False
             # completions
@@ -199,25 +270,30 @@ class Server:
                     del busy[s]
                     progressed = True
             # admissions
-            while pending and (mode == "batched" or not busy):
+            while pend and (mode == "batched" or not busy):
                 free = [s for s in range(self.num_slots) if s not in busy]
                 if not free:
                     break
-                batch = Batch(self._form_batch(pending) if mode == "batched" else [pending[0]])
-                b_bytes = self.backend.workspace_bytes(batch.requests)
+                if mode == "batched":
+                    groups = self._form_group(pend)
+                else:
+                    groups = [[next(pend.untaken())]]
+                b_bytes = self.backend.workspace_bytes(groups)
                 s = free[0]
                 others = sum(slot_bytes[o] for o in busy)
                 need = max(slot_bytes[s], b_bytes)
                 if busy and others + need > self.hbm_budget:
-                    self.backend.discard(batch.requests)
+                    self.backend.discard(groups)
                     break  # wait for memory
-                for r in batch.requests:
-                    pending.remove(r)
+                flat = [r for g in groups for r in g]
+                pend.take(flat)
                 slot_bytes[s] = need
-                batch.work = self.backend.launch(batch.requests, s)
+                batch = Batch(flat, groups)
+                batch.work = self.backend.launch(groups, s)
                 batch.slot = s
                 busy[s] = batch
                 launches += 1
+                fused += len(groups)
                 progressed = True
                 if mode == "plain":
                     self.backend.wait(batch.work)
@@ -229,7 +305,8 @@ class Server:
                     if gap > 2e-4:
                         time.sleep(gap - 1e-4)
         wall = clock() - t0
-        return ServeStats(mode, n, wall, lat, launches, results)
+        served = lat[~np.isnan(lat)]
+        return ServeStats(mode, done, wall, served, launches, results, rejected, fused)
 
 
 # ---------------------------------------------------------------- GPU backend
@@ -253,7 +330,17 @@ class GpuBackend:
     def max_sets(self, key):
         return 8 if self.resident[key].num_samples <= 65535 else 4
 
-    # ---- preparation (host): one fused query per batch
+    def output_bytes(self, r):
+        """Bytes of one request's result."""
+        ts = self.resident[r.ts]
+        nwin = 1 if r.windows is None else len(r.windows) - 1
+        if r.kind == "rv":
+            return nwin * ts.num_samples * r.weights.shape[1] * 8
+        if r.kind == "afs":
+            return nwin * int(np.prod([len(s) + 1 for s in r.sample_sets])) * 8
+        return nwin * 3 * 8
+
+    # ---- preparation (host): one fused query per group
     def _prepare(self, reqs):
         from .trees import AfsQuery, Query, RelatednessVectorQuery
 
@@ -285,33 +372,64 @@ class GpuBackend:
         q = Query(ts, sets, terms, head.windows, flags)
         return q, plan
 
-    def workspace_bytes(self, reqs):
-        key = tuple(r.rid for r in reqs)
+    @staticmethod
+    def _key(reqs):
+        return tuple(r.rid for r in reqs)
+
+    def _get(self, reqs):
+        key = self._key(reqs)
         if key not in self._prepared:
             self._prepared[key] = self._prepare(reqs)
-        return self._prepared[key][0].workspace_bytes
+        return self._prepared[key]
 
-    def discard(self, reqs):
-        self._prepared.pop(tuple(r.rid for r in reqs), None)
+    def workspace_bytes(self, groups):
+        """The launch's workspace: the fused queries' side by side (the
+        batch's layout), or the one query's."""
+        sizes = [self._get(g)[0].workspace_bytes for g in groups]
+        if len(sizes) == 1:
+            return sizes[0]
+        return sum((b + 255) // 256 * 256 for b in sizes) + 8 * 256
 
-    def launch(self, reqs, slot):
+    def discard(self, groups):
+        for g in groups:
+            self._prepared.pop(self._key(g), None)
+
+    def launch(self, groups, slot):
+        from .trees import QueryBatch
+
         torch = self.torch
-        key = tuple(r.rid for r in reqs)
-        q, extra = self._prepared.pop(key) if key in self._prepared else self._prepare(reqs)
+        preps = []
+        for g in groups:
+            key = self._key(g)
+            preps.append(self._prepared.pop(key) if key in self._prepared else self._prepare(g))
         st = self.streams[slot]
+        ws = self.workspaces[slot]
         with torch.cuda.stream(st):
-            res = torch.empty(q.result_size, dtype=torch.float64, device="cuda")
-            W = None
-            if reqs[0].kind == "rv":
-                W = torch.from_numpy(extra).to("cuda", non_blocking=False)
-                q.set_weights(W)
-            q.launch(self.workspaces[slot], res, stream=st)
-            host = torch.empty(q.result_size, dtype=torch.float64, pin_memory=True)
-            host.copy_(res, non_blocking=True)
+            res = [torch.empty(q.result_size, dtype=torch.float64, device="cuda")
+                   for q, _ in preps]
+            weights = []
+            for (q, extra), g in zip(preps, groups):
+                if g[0].kind == "rv":
+                    W = torch.from_numpy(extra).to("cuda", non_blocking=False)
+                    q.set_weights(W)
+                    weights.append(W)
+            batch = None
+            if len(preps) == 1:
+                q = preps[0][0]
+                q.launch(ws, res[0], stream=st)
+            else:
+                batch = QueryBatch([q for q, _ in preps], res, ws)
+                batch.launch(st)
+            total = sum(q.result_size for q, _ in preps)
+            host = torch.empty(total, dtype=torch.float64, pin_memory=True)
+            o = 0
+            for (q, _), r in zip(preps, res):
+                host[o:o + q.result_size].copy_(r, non_blocking=True)
+                o += q.result_size
             ev = torch.cuda.Event()
             ev.record(st)
-        return {"q": q, "extra": extra, "reqs": reqs, "res": res, "host": host, "ev": ev,
-                "W": W, "slot": slot}
+        return {"preps": preps, "groups": groups, "res": res, "host": host, "ev": ev,
+                "W": weights, "slot": slot, "batch": batch}
 
     def ready(self, work):
         return work["ev"].query()
@@ -320,27 +438,33 @@ class GpuBackend:
         work["ev"].synchronize()
 
     def results(self, work):
-        q, reqs = work["q"], work["reqs"]
-        q.check(self.workspaces[work["slot"]])
-        y = work["host"].numpy()
-        out = {}
-        head = reqs[0]
-        if head.kind == "afs":
-            out[head.rid] = y.reshape(q.shape)
-        elif head.kind == "rv":
-            Y = y.reshape(q.shape)
-            c = 0
-            for r in reqs:
-                k = r.weights.shape[1]
-                out[r.rid] = Y[:, :, c:c + k]
-                c += k
+        if work["batch"] is not None:
+            work["batch"].check()
         else:
-            Y = y.reshape(q.num_windows, q.num_terms)
-            for r, a, b in work["extra"]:
-                v = Y[:, a:b]
-                if r.stat == "Fst":
-                    du, dv, dx = v[:, 0], v[:, 1], v[:, 2]
-                    with np.errstate(divide="ignore", invalid="ignore"):
-                        v = (1 - 2 * (du + dv) / (du + dv + 2 * dx))[:, None]
-                out[r.rid] = v
+            work["preps"][0][0].check(self.workspaces[work["slot"]])
+        y_all = work["host"].numpy()
+        out = {}
+        o = 0
+        for (q, extra), reqs in zip(work["preps"], work["groups"]):
+            y = y_all[o:o + q.result_size]
+            o += q.result_size
+            head = reqs[0]
+            if head.kind == "afs":
+                out[head.rid] = y.reshape(q.shape)
+            elif head.kind == "rv":
+                Y = y.reshape(q.shape)
+                c = 0
+                for r in reqs:
+                    k = r.weights.shape[1]
+                    out[r.rid] = Y[:, :, c:c + k]
+                    c += k
+            else:
+                Y = y.reshape(q.num_windows, q.num_terms)
+                for r, a, b in extra:
+                    v = Y[:, a:b]
+                    if r.stat == "Fst":
+                        du, dv, dx = v[:, 0], v[:, 1], v[:, 2]
+                        with np.errstate(divide="ignore", invalid="ignore"):
+                            v = (1 - 2 * (du + dv) / (du + dv + 2 * dx))[:, None]
+                    out[r.rid] = v
         return out

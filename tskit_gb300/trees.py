@@ -203,6 +203,58 @@ class RelatednessVectorQuery(Query):
                                                   ctypes.c_void_p(weights.data_ptr())))
 
 
+class QueryBatch:
+    """Prepared queries on any resident tree sequences fused into one launch
+    per pipeline stage (``tsg_batch_*``): the sample-count queries on the
+    compact replay share each stage's kernel -- the replay one persistent
+    kernel over all their spans -- and the others launch on their own in the
+    same stream.  ``results`` are float64 CUDA tensors, one per query, of the
+    queries' ``result_size``; the batch binds them and ``workspace`` (grown
+    here to what the batch needs), and holds references to all three."""
+
+    def __init__(self, queries, results, workspace):
+        self._lib = nat.load()
+        self.queries = list(queries)
+        self.results = list(results)
+        self.workspace = workspace
+        n = len(self.queries)
+        if n == 0 or len(self.results) != n:
+            raise ValueError("a batch needs one result per query")
+        handles = (ctypes.c_void_p * n)(*[q.handle.value for q in self.queries])
+        need = ctypes.c_int64()
+        nat.check(self._lib.tsg_batch_workspace_bytes(n, ctypes.cast(handles, ctypes.c_void_p),
+                                                      ctypes.byref(need)))
+        if workspace.nbytes < need.value:
+            workspace.reserve(need.value)
+        for q, r in zip(self.queries, self.results):
+            if r.numel() < q.result_size:
+                raise ValueError("result tensor smaller than its query's result")
+        ptrs = (ctypes.c_void_p * n)(*[r.data_ptr() for r in self.results])
+        h = ctypes.c_void_p()
+        nat.check(self._lib.tsg_batch_create(ctypes.byref(h), n,
+                                             ctypes.cast(handles, ctypes.c_void_p),
+                                             ctypes.cast(ptrs, ctypes.c_void_p), workspace.handle))
+        self.handle = h
+        self.workspace_bytes = need.value
+        self.num_fused = self._lib.tsg_batch_num_fused(h)
+
+    def launch(self, stream=None):
+        torch = _require_torch_cuda()
+        if stream is None:
+            stream = torch.cuda.current_stream()
+        nat.check(self._lib.tsg_batch_launch(self.handle, ctypes.c_void_p(stream.cuda_stream)))
+
+    def check(self):
+        failed = ctypes.c_uint64()
+        nat.check(self._lib.tsg_batch_check(self.handle, ctypes.byref(failed)))
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self._lib.tsg_batch_free(h)
+            self.handle = None
+
+
 class TreeSequence:
     """A tree sequence resident on the GPU with the reference's statistics API."""
 
