@@ -1051,6 +1051,7 @@ def run_serve_mix(args):
     ns = [1000, 2000, 5000, 20000, 20000, 50000, 100000, 200000]
     resident = {f"n{n}_{i}": tskit_gb300.TreeSequence(sim.simulate(n, 1e8, 5 * n, 5 * n, 2000 + i))
                 for i, n in enumerate(ns)}
+    batch_cmp = batch_vs_single(resident)
     num, rate = args.serve_queries, args.serve_rate
     reqs = poisson_requests(resident, num, rate, 7)
     be = GpuBackend(resident, num_slots=8)
@@ -1086,8 +1087,64 @@ def run_serve_mix(args):
                 "h2d_bytes_per_step": int(h2d / max(1, b.num)),
                 "d2h_bytes_per_step": int(d2h / max(1, b.num))},
         "gpu_launches": launches / max(1, b.num), "clocks": clocks.summary(),
+        "batch_across_tree_sequences": batch_cmp,
     }
     print(json.dumps(line))
+
+
+def batch_vs_single(resident, reps=20):
+    """One fused query per resident tree sequence the batched kernels take
+    (diversity and divergence of two random sets of 200, 10 windows, both
+    modes, FP64), launched one by one on one stream and as one QueryBatch;
+    device time per round of all the queries (CUDA events, median of
+    `reps`), and the results compared bit for bit."""
+    import torch
+
+    import tskit_gb300
+    from tskit_gb300 import _native as nat
+
+    qs = []
+    for i, (key, ts) in enumerate(sorted(resident.items())):
+        if ts.num_samples > 65535:
+            continue
+        rng = np.random.default_rng(50 + i)
+        perm = rng.permutation(ts.samples())
+        sets = [np.sort(perm[:200]), np.sort(perm[200:400])]
+        L = ts.sequence_length
+        qs.append(ts.query(sets, [(nat.DIVERSITY, (0,)), (nat.DIVERSITY, (1,)),
+                                  (nat.DIVERGENCE, (0, 1))],
+                           windows=np.linspace(0, L, 11), both_modes=True))
+    ws1 = [tskit_gb300.Workspace(q.workspace_bytes) for q in qs]
+    own = [torch.zeros(q.result_size, dtype=torch.float64, device="cuda") for q in qs]
+    res = [torch.zeros(q.result_size, dtype=torch.float64, device="cuda") for q in qs]
+    batch = tskit_gb300.QueryBatch(qs, res, tskit_gb300.Workspace())
+    st = torch.cuda.current_stream()
+
+    def time_it(fn):
+        ts_ = []
+        for r in range(reps + 3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            fn()
+            b.record(st)
+            torch.cuda.synchronize()
+            if r >= 3:
+                ts_.append(a.elapsed_time(b))
+        return float(np.median(ts_))
+
+    lib = nat.load()
+    l0 = lib.tsg_launch_count()
+    single_ms = time_it(lambda: [q.launch(w, o, st) for q, w, o in zip(qs, ws1, own)])
+    l1 = lib.tsg_launch_count()
+    batch_ms = time_it(lambda: batch.launch(st))
+    l2 = lib.tsg_launch_count()
+    batch.check()
+    equal = all(torch.equal(a.view(torch.int64), b.view(torch.int64)) for a, b in zip(own, res))
+    return {"queries": len(qs), "fused": batch.num_fused,
+            "tree_sequences": [int(q.ts.num_samples) for q in qs],
+            "one_by_one_ms": single_ms, "batched_ms": batch_ms,
+            "launches_one_by_one": (l1 - l0) / (reps + 3), "launches_batched": (l2 - l1) / (reps + 3),
+            "bitwise_equal": bool(equal)}
 
 
 def be_launches():

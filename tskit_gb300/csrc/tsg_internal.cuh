@@ -239,6 +239,11 @@ struct tsg_treeseq {
 struct tsg_workspace {
     void *ptr;
     int64_t bytes;
+    // side streams and events for a launch's independent stages (made by
+    // tsg_workspace_create; null in descriptors made otherwise, whose
+    // launches run on the caller's stream alone)
+    cudaStream_t aux[2];
+    cudaEvent_t ev[4];
 };
 
 namespace tsg {

@@ -216,28 +216,55 @@ __device__ __forceinline__ void span_windows_body(const TSView &ts, const QueryP
         w.A[woff + j] = b - a;
     }
     __syncwarp();
-    double cum = 0;
+    // the running sum and the open window's sum stay in registers (the
+    // window's sum is stored once, when the window closes); each tree's
+    // chunk offsets, right end and first chunk change are loaded one tree
+    // ahead
+    const int64_t C = ts.num_chunks;
+    double cum = 0, bacc = 0;
+    bool open = false;
     int32_t wi = wlo;
+    int64_t co0 = ts.tree_chunk_off[t0], co1 = ts.tree_chunk_off[t0 + 1];
+    double tl = slo, tr = ts.breakpoints[t0 + 1];
+    double first = (lane < R && co0 < co1) ? w.dD[co0 * R + lane] : 0.0;
     for (int32_t t = t0; t < t1; t++) {
-        const double tl = ts.breakpoints[t], tr = ts.breakpoints[t + 1];
-        if (lane < R) {
-            for (int64_t c = ts.tree_chunk_off[t]; c < ts.tree_chunk_off[t + 1]; c++) {
+        int64_t co2 = co1;
+        double trn = tr, firstn = 0.0;
+        if (t + 1 < t1) {
+            co2 = ts.tree_chunk_off[t + 2];
+            trn = ts.breakpoints[t + 2];
+            firstn = (lane < R && co1 < C) ? w.dD[co1 * R + lane] : 0.0;
+        }
+        if (lane < R && co0 < co1) {
+            cum += first;
+            for (int64_t c = co0 + 1; c < co1; c++) {
                 cum += w.dD[c * R + lane];
             }
         }
         while (wi < q.Wn && win[wi] < tr) {
             const double a = tl > win[wi] ? tl : win[wi];
             const double b = tr < win[wi + 1] ? tr : win[wi + 1];
-            const int64_t li = woff + (wi - wlo);
-            if (lane < R) {
-                w.B[li * R + lane] += cum * (b - a);
-            }
+            bacc += cum * (b - a);
+            open = true;
             if (win[wi + 1] <= tr) {
+                if (lane < R) {
+                    w.B[(woff + (wi - wlo)) * R + lane] = bacc;
+                }
+                bacc = 0;
+                open = false;
                 wi++;
             } else {
                 break;
             }
         }
+        co0 = co1;
+        co1 = co2;
+        tl = tr;
+        tr = trn;
+        first = firstn;
+    }
+    if (open && lane < R) {
+        w.B[(woff + (wi - wlo)) * R + lane] = bacc;
     }
     if (lane < R) {
         w.D[u * R + lane] = cum;

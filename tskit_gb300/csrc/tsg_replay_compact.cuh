@@ -24,30 +24,59 @@ namespace tsg {
 
 #define TSG_COMPACT_THREADS 64
 
-// Counts of span s's compact nodes at the span start into sp.xq.  s_pre:
-// (TSG_COMPACT_THREADS + 1) x 2 words; s_wsum: 2 words per warp.  Ends with
-// the block synchronised.
+// samples per thread in one step of the seek
+#define TSG_SEEK_PER 4
+
+// Counts of span s's compact nodes at the span start into sp.xq.  The seek
+// takes TSG_COMPACT_THREADS x TSG_SEEK_PER samples of the span's order per
+// step, each thread TSG_SEEK_PER consecutive ones, and loads the next step's
+// order entries and sample masks while it scans the current one.  s_pre:
+// (TSG_COMPACT_THREADS + 1) x 2 words, each thread's exclusive prefix (and
+// the step's total); s_mask: the step's masks; s_wsum: 2 words per warp.
+// Ends with the block synchronised.
 template <int KQ>
 __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &qd, int K, int s,
-    const SpanState<uint16_t> &sp, uint64_t *s_pre, uint64_t *s_wsum)
+    const SpanState<uint16_t> &sp, uint64_t *s_pre, uint64_t *s_wsum, uint32_t *s_mask)
 {
+    constexpr int T = TSG_COMPACT_THREADS, PER = TSG_SEEK_PER, STEP = T * PER;
+    constexpr int NW = T / 32;
     const int64_t n = ts.num_samples;
     const uint16_t *order = ts.c_order + (int64_t) s * n;
     const int2 *ep = ts.c_ep + ts.c_ep_off[s];
     const int64_t nep = ts.c_ep_off[s + 1] - ts.c_ep_off[s];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    constexpr int NW = TSG_COMPACT_THREADS / 32;
+    uint32_t cur_m[PER], nxt_m[PER];
+    auto fetch = [&](int64_t base, uint32_t (&mm)[PER]) {
+        uint32_t o[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int64_t i = base + (int64_t) tid * PER + j;
+            o[j] = i < n ? (uint32_t) order[i] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int64_t i = base + (int64_t) tid * PER + j;
+            mm[j] = i < n ? qd.sample_mask[o[j]] : 0u;
+        }
+    };
+    fetch(0, cur_m);
     uint64_t run_lo = 0, run_hi = 0;
     int64_t cur = 0;
-    for (int64_t base = 0; base < n; base += TSG_COMPACT_THREADS) {
-        const int64_t i = base + tid;
-        Pack v{0, 0};
-        if (i < n) {
-            v = pk_from_mask<16>(qd.sample_mask[order[i]], K);
+    for (int64_t base = 0; base < n; base += STEP) {
+        if (base + STEP < n) {
+            fetch(base + STEP, nxt_m);
         }
-        // inclusive scan within the warp (fields never carry: prefix counts
-        // stay within the set sizes)
-        uint64_t inc_lo = v.lo, inc_hi = v.hi;
+        uint64_t t_lo = 0, t_hi = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            s_mask[tid * PER + j] = cur_m[j];
+            const Pack v = pk_from_mask<16>(cur_m[j], K);
+            t_lo += v.lo;
+            t_hi += v.hi;
+        }
+        // inclusive scan of the threads' totals within the warp (fields
+        // never carry: prefix counts stay within the set sizes)
+        uint64_t inc_lo = t_lo, inc_hi = t_hi;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
@@ -73,18 +102,18 @@ __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &q
             tot_lo += a;
             tot_hi += b;
         }
-        // P at position i (the samples before it)
-        s_pre[2 * tid] = run_lo + wp_lo + inc_lo - v.lo;
-        s_pre[2 * tid + 1] = run_hi + wp_hi + inc_hi - v.hi;
+        // P at position base + tid * PER (the samples before it)
+        s_pre[2 * tid] = run_lo + wp_lo + inc_lo - t_lo;
+        s_pre[2 * tid + 1] = run_hi + wp_hi + inc_hi - t_hi;
         if (tid == 0) {
-            s_pre[2 * TSG_COMPACT_THREADS] = run_lo + tot_lo;
-            s_pre[2 * TSG_COMPACT_THREADS + 1] = run_hi + tot_hi;
+            s_pre[2 * T] = run_lo + tot_lo;
+            s_pre[2 * T + 1] = run_hi + tot_hi;
         }
         __syncthreads();
-        // every endpoint at a position up to base + TSG_COMPACT_THREADS (the
-        // sorted list's next entries; earlier positions were taken by
-        // earlier steps)
-        const int64_t lim = base + TSG_COMPACT_THREADS;
+        // every endpoint at a position up to base + STEP (the sorted list's
+        // next entries; earlier positions were taken by earlier steps):
+        // P there is its thread's prefix plus the masks before it
+        const int64_t lim = base + STEP;
         for (;;) {
             const int64_t j = cur + tid;
             int2 e = make_int2(0, 0);
@@ -95,30 +124,44 @@ __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &q
             }
             const int cnt = __syncthreads_count(mine);
             const int64_t l = e.y >> 1;
-            const int at = (int) (e.x - base);
+            uint64_t p_lo = 0, p_hi = 0;
+            if (mine) {
+                const int at = (int) (e.x - base);
+                const int tt = at / PER, jj = at - tt * PER;
+                p_lo = s_pre[2 * tt];
+                p_hi = s_pre[2 * tt + 1];
+                for (int q = 0; q < jj; q++) {
+                    const Pack v = pk_from_mask<16>(s_mask[tt * PER + q], K);
+                    p_lo += v.lo;
+                    p_hi += v.hi;
+                }
+            }
             if (mine && !(e.y & 1)) {
-                sp.xq[l * KQ] = s_pre[2 * at];
+                sp.xq[l * KQ] = p_lo;
                 if (KQ > 1) {
-                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = s_pre[2 * at + 1];
+                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = p_hi;
                 }
             }
             __syncthreads();
             if (mine && (e.y & 1)) {
-                sp.xq[l * KQ] = s_pre[2 * at] - sp.xq[l * KQ];
+                sp.xq[l * KQ] = p_lo - sp.xq[l * KQ];
                 if (KQ > 1) {
-                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] =
-                        s_pre[2 * at + 1] - sp.xq[l * KQ + (KQ > 1 ? 1 : 0)];
+                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = p_hi - sp.xq[l * KQ + (KQ > 1 ? 1 : 0)];
                 }
             }
             cur += cnt;
-            if (cnt < TSG_COMPACT_THREADS) {
+            if (cnt < T) {
                 break;
             }
             __syncthreads();
         }
-        run_lo = s_pre[2 * TSG_COMPACT_THREADS];
-        run_hi = s_pre[2 * TSG_COMPACT_THREADS + 1];
+        run_lo = s_pre[2 * T];
+        run_hi = s_pre[2 * T + 1];
         __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            cur_m[j] = nxt_m[j];
+        }
     }
 }
 
@@ -128,7 +171,8 @@ __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &q
 template <int KQ>
 __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams &q,
     const QueryDev &qd, const WsDev &w, int s, unsigned char *smem_raw,
-    TouchEntry<KQ> *s_list, ReplayStage *s_stage, uint64_t *s_pre, uint64_t *s_wsum)
+    TouchEntry<KQ> *s_list, ReplayStage *s_stage, uint64_t *s_pre, uint64_t *s_wsum,
+    uint32_t *s_mask)
 {
     SpanState<uint16_t> sp = span_state_at<uint16_t>(smem_raw, ts.c_max_local, KQ);
     sp.cnt = nullptr;
@@ -141,7 +185,7 @@ __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams
     for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
         sp.par[l] = ts.c_par0[lo + l];
     }
-    compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum);
+    compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum, s_mask);
     if (threadIdx.x < 32) {
         replay_span<16, KQ, uint16_t, false>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
             t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
@@ -156,6 +200,7 @@ struct CompactShared {
     ReplayStage stage[4];                // prefetch ring, trees t .. t + 3
     uint64_t pre[2 * (TSG_COMPACT_THREADS + 1)];
     uint64_t wsum[2 * (TSG_COMPACT_THREADS / 32)];
+    uint32_t mask[TSG_COMPACT_THREADS * TSG_SEEK_PER];
 };
 
 // Persistent blocks take spans from the query's counter until none is left.
@@ -176,7 +221,7 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
         if (s >= ts.c_num_spans) {
             break;
         }
-        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.pre, sh.wsum);
+        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.pre, sh.wsum, sh.mask);
     }
 }
 

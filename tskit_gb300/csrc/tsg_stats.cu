@@ -1717,9 +1717,34 @@ int tsg_query_set_replay_events(tsg_query_t *q, void *start_event, void *stop_ev
 
 int tsg_workspace_create(tsg_workspace_t **ws)
 {
-    *ws = new tsg_workspace_t();
-    (*ws)->ptr = nullptr;
-    (*ws)->bytes = 0;
+    tsg_workspace_t *w = new tsg_workspace_t();
+    w->ptr = nullptr;
+    w->bytes = 0;
+    // the launch forks independent stages onto these (optional: without
+    // them everything runs on the caller's stream)
+    bool ok = true;
+    for (int i = 0; i < 2; i++) {
+        ok = ok && cudaStreamCreateWithFlags(&w->aux[i], cudaStreamNonBlocking) == cudaSuccess;
+    }
+    for (int i = 0; i < 4; i++) {
+        ok = ok && cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        for (int i = 0; i < 2; i++) {
+            if (w->aux[i] != nullptr) {
+                cudaStreamDestroy(w->aux[i]);
+                w->aux[i] = nullptr;
+            }
+        }
+        for (int i = 0; i < 4; i++) {
+            if (w->ev[i] != nullptr) {
+                cudaEventDestroy(w->ev[i]);
+                w->ev[i] = nullptr;
+            }
+        }
+    }
+    *ws = w;
     return 0;
 }
 
@@ -1746,6 +1771,16 @@ int64_t tsg_workspace_bytes(const tsg_workspace_t *ws) { return ws->bytes; }
 int tsg_workspace_free(tsg_workspace_t *ws)
 {
     if (ws != nullptr) {
+        for (int i = 0; i < 2; i++) {
+            if (ws->aux[i] != nullptr) {
+                cudaStreamDestroy(ws->aux[i]);
+            }
+        }
+        for (int i = 0; i < 4; i++) {
+            if (ws->ev[i] != nullptr) {
+                cudaEventDestroy(ws->ev[i]);
+            }
+        }
         cudaFree(ws->ptr);
         delete ws;
     }
@@ -1778,12 +1813,74 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     const bool item_pipeline = q->smem;
     QueryDev d = q->d;
     d.node_mask = w.node_mask;
+    // independent stages of the item pipeline run on the workspace's side
+    // streams, joined before the window reduction: the leaves' areas (after
+    // the node masks) beside the replay, the exact site sums (after the
+    // replay) beside the item evaluation
+    const bool fork = item_pipeline && ws->aux[0] != nullptr && ws->aux[1] != nullptr;
+    const bool site_sums = p.site && p.site_int && ts->v.num_sites > 0;
+    const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+    auto leaf_stage = [&](cudaStream_t s) -> int {
+        TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
+            (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, s));
+        if (ts->v.num_edges > 0) {
+            k_leaf_areas<<<grid_for(ts->v.num_edges), 256, 0, s>>>(ts->v, p, d, w);
+            TSG_LAUNCHED();
+        }
+        k_leaf_prefix<<<(unsigned) (1 << p.K), 256, 0, s>>>(p, d, w);
+        TSG_LAUNCHED();
+        if (q->W == 16) {
+            k_leaf_terms<16><<<grid_for((int64_t) p.Wn * R), 256, 0, s>>>(p, w);
+        } else {
+            k_leaf_terms<32><<<grid_for((int64_t) p.Wn * R), 256, 0, s>>>(p, w);
+        }
+        TSG_LAUNCHED();
+        return 0;
+    };
+    auto site_stage = [&](cudaStream_t s) -> int {
+        // integer numerators summed exactly per window in one pass
+        TSG_CUDA(cudaMemsetAsync(w.site_acc, 0, (size_t) p.Wn * R * 16, s));
+        const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
+        switch (form) {
+            case 0: k_site_sums<16, 1><<<gsite, 256, 0, s>>>(ts->v, p, d, w); break;
+            case 1: k_site_sums<16, 2><<<gsite, 256, 0, s>>>(ts->v, p, d, w); break;
+            case 2: k_site_sums<32, 1><<<gsite, 256, 0, s>>>(ts->v, p, d, w); break;
+            default: k_site_sums<32, 2><<<gsite, 256, 0, s>>>(ts->v, p, d, w); break;
+        }
+        TSG_LAUNCHED();
+        k_site_sums_finish<<<grid_for((int64_t) p.Wn * R), 256, 0, s>>>(p, w);
+        TSG_LAUNCHED();
+        return 0;
+    };
+    bool forked_leaf = false, forked_site = false;
     if (q->smem) {
         k_node_mask<<<grid_for(N), 256, 0, st>>>(ts->v, d, w.node_mask);
         TSG_LAUNCHED();
+        if (fork && p.branch) {
+            TSG_CUDA(cudaEventRecord(ws->ev[0], st));
+            TSG_CUDA(cudaStreamWaitEvent(ws->aux[0], ws->ev[0], 0));
+            int r = leaf_stage(ws->aux[0]);
+            if (r != 0) {
+                return r;
+            }
+            TSG_CUDA(cudaEventRecord(ws->ev[1], ws->aux[0]));
+            forked_leaf = true;
+        }
         const unsigned g = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
-        const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
+        auto fork_site = [&]() -> int {
+            if (fork && site_sums) {
+                TSG_CUDA(cudaEventRecord(ws->ev[2], st));
+                TSG_CUDA(cudaStreamWaitEvent(ws->aux[1], ws->ev[2], 0));
+                int r = site_stage(ws->aux[1]);
+                if (r != 0) {
+                    return r;
+                }
+                TSG_CUDA(cudaEventRecord(ws->ev[3], ws->aux[1]));
+                forked_site = true;
+            }
+            return 0;
+        };
         if (q->compact_ok && ts->v.c_num_spans > 0) {
             // the compact replay: the first tree's items, one block per span
             // at a time, then every chunk's item values
@@ -1821,9 +1918,13 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             if (q->ev_rstop != nullptr) {
                 TSG_CUDA(cudaEventRecord(q->ev_rstop, st));
             }
+            TSG_LAUNCHED();
+            int r = fork_site();
+            if (r != 0) {
+                return r;
+            }
             if (p.branch) {
                 // two kernels: the items' branch lengths, then their values
-                TSG_LAUNCHED();
                 if (p.f32) {
                     (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
                         ts->v, p, w);
@@ -1831,6 +1932,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                     (p.polarised ? launch_eval_chunks_f64_pol : launch_eval_chunks_f64_unpol)(kq, st,
                         ts->v, p, w);
                 }
+                TSG_LAUNCHED();
                 TSG_LAUNCHED();
             }
         } else if (p.branch) {
@@ -1848,6 +1950,11 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             if (q->ev_rstop != nullptr) {
                 TSG_CUDA(cudaEventRecord(q->ev_rstop, st));
             }
+            TSG_LAUNCHED();
+            int r = fork_site();
+            if (r != 0) {
+                return r;
+            }
         } else {
             switch (form) {
                 case 0: k_replay_items<16, 1, uint16_t, float, false, false><<<g, 512, sb, st>>>(ts->v, p, d, w, 0); break;
@@ -1855,39 +1962,29 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 case 2: k_replay_items<32, 1, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
                 default: k_replay_items<32, 2, int32_t, float, false, false><<<g, 512, 0, st>>>(ts->v, p, d, w, q->slot_bytes); break;
             }
+            TSG_LAUNCHED();
+            int r = fork_site();
+            if (r != 0) {
+                return r;
+            }
         }
-        TSG_LAUNCHED();
         if (p.branch) {
             k_span_windows<<<(unsigned) ((ts->v.num_segs + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
-            TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
-                (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, st));
-            if (ts->v.num_edges > 0) {
-                k_leaf_areas<<<grid_for(ts->v.num_edges), 256, 0, st>>>(ts->v, p, d, w);
-                TSG_LAUNCHED();
+            if (!forked_leaf) {
+                int r = leaf_stage(st);
+                if (r != 0) {
+                    return r;
+                }
             }
-            k_leaf_prefix<<<(unsigned) (1 << p.K), 256, 0, st>>>(p, d, w);
-            TSG_LAUNCHED();
-            if (q->W == 16) {
-                k_leaf_terms<16><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
-            } else {
-                k_leaf_terms<32><<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
-            }
-            TSG_LAUNCHED();
         }
-        if (p.site && p.site_int && ts->v.num_sites > 0) {
-            // integer numerators summed exactly per window in one pass
-            TSG_CUDA(cudaMemsetAsync(w.site_acc, 0, (size_t) p.Wn * R * 16, st));
-            const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
-            switch (form) {
-                case 0: k_site_sums<16, 1><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
-                case 1: k_site_sums<16, 2><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
-                case 2: k_site_sums<32, 1><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
-                default: k_site_sums<32, 2><<<gsite, 256, 0, st>>>(ts->v, p, d, w); break;
+        if (site_sums) {
+            if (!forked_site) {
+                int r = site_stage(st);
+                if (r != 0) {
+                    return r;
+                }
             }
-            TSG_LAUNCHED();
-            k_site_sums_finish<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, w);
-            TSG_LAUNCHED();
         } else if (p.site && ts->v.num_sites > 0) {
             const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
             switch (form) {
@@ -1922,6 +2019,12 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         k_span_scan<<<(unsigned) R, 512, 0, st>>>(w.D, w.rs0, w.RS,
             item_pipeline ? ts->v.num_segs : NS, (int) R);
         TSG_LAUNCHED();
+    }
+    if (forked_leaf) {
+        TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[1], 0));
+    }
+    if (forked_site) {
+        TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[3], 0));
     }
     k_window_reduce<<<grid_for((int64_t) p.Wn * R), 256, 0, st>>>(p, d, w, q->span_normalise,
         item_pipeline ? 1 : 0, result);
@@ -3553,7 +3656,7 @@ int tsg_query_launch_noalloc(const tsg_query_t *q, double *result_device, void *
     }
     // a workspace descriptor over the static array: no device allocation;
     // every word the launch needs zeroed is cleared by the launch itself
-    tsg_workspace_t ws;
+    tsg_workspace_t ws{};
     ws.ptr = scratch;
     ws.bytes = (int64_t) TSG_NOALLOC_SCRATCH_BYTES;
     ret = tsg_query_launch(q, &ws, result_device, cuda_stream);
