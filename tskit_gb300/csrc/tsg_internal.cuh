@@ -243,7 +243,7 @@ struct tsg_workspace {
     // tsg_workspace_create; null in descriptors made otherwise, whose
     // launches run on the caller's stream alone)
     cudaStream_t aux[2];
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[6];
 };
 
 namespace tsg {

@@ -217,51 +217,73 @@ __device__ __forceinline__ void span_windows_body(const TSView &ts, const QueryP
     }
     __syncwarp();
     // the running sum and the open window's sum stay in registers (the
-    // window's sum is stored once, when the window closes); each tree's
-    // chunk offsets, right end and first chunk change are loaded one tree
-    // ahead
-    const int64_t C = ts.num_chunks;
+    // window's sum is stored once, when the window closes); trees are taken
+    // four at a time, their chunk ranges, right ends and first chunk
+    // changes loaded together (two round trips per four trees).  Genome
+    // positions (never negative) are compared as the integers of their bits
+    // (the same order), keeping the FP64 pipe -- a warp instruction every 16
+    // cycles -- for the three sums per tree.
+    auto key = [](double x) { return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL; };
     double cum = 0, bacc = 0;
     bool open = false;
     int32_t wi = wlo;
-    int64_t co0 = ts.tree_chunk_off[t0], co1 = ts.tree_chunk_off[t0 + 1];
-    double tl = slo, tr = ts.breakpoints[t0 + 1];
-    double first = (lane < R && co0 < co1) ? w.dD[co0 * R + lane] : 0.0;
-    for (int32_t t = t0; t < t1; t++) {
-        int64_t co2 = co1;
-        double trn = tr, firstn = 0.0;
-        if (t + 1 < t1) {
-            co2 = ts.tree_chunk_off[t + 2];
-            trn = ts.breakpoints[t + 2];
-            firstn = (lane < R && co1 < C) ? w.dD[co1 * R + lane] : 0.0;
+    double tl = slo;
+    long long ktl = key(tl);
+    double w_lo = win[wi], w_hi = win[wi + 1];
+    long long kwlo = key(w_lo), kwhi = key(w_hi);
+    for (int32_t tg = t0; tg < t1; tg += 4) {
+        const int ng = t1 - tg < 4 ? t1 - tg : 4;
+        int64_t co[5];
+        double tr[4], fi[4];
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            co[j] = ts.tree_chunk_off[tg + j < t1 ? tg + j : t1];
         }
-        if (lane < R && co0 < co1) {
-            cum += first;
-            for (int64_t c = co0 + 1; c < co1; c++) {
-                cum += w.dD[c * R + lane];
-            }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            tr[j] = ts.breakpoints[tg + j + 1 < t1 ? tg + j + 1 : t1];
         }
-        while (wi < q.Wn && win[wi] < tr) {
-            const double a = tl > win[wi] ? tl : win[wi];
-            const double b = tr < win[wi + 1] ? tr : win[wi + 1];
-            bacc += cum * (b - a);
-            open = true;
-            if (win[wi + 1] <= tr) {
-                if (lane < R) {
-                    w.B[(woff + (wi - wlo)) * R + lane] = bacc;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            fi[j] = (lane < R && j < ng && co[j] < co[j + 1]) ? w.dD[co[j] * R + lane] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j < ng) {
+                const double trj = tr[j];
+                const long long ktr = key(trj);
+                if (lane < R && co[j] < co[j + 1]) {
+                    cum += fi[j];
+                    for (int64_t c = co[j] + 1; c < co[j + 1]; c++) {
+                        cum += w.dD[c * R + lane];
+                    }
                 }
-                bacc = 0;
-                open = false;
-                wi++;
-            } else {
-                break;
+                while (wi < q.Wn && kwlo < ktr) {
+                    const double a = ktl > kwlo ? tl : w_lo;
+                    const double b = ktr < kwhi ? trj : w_hi;
+                    bacc += cum * (b - a);
+                    open = true;
+                    if (kwhi <= ktr) {
+                        if (lane < R) {
+                            w.B[(woff + (wi - wlo)) * R + lane] = bacc;
+                        }
+                        bacc = 0;
+                        open = false;
+                        wi++;
+                        if (wi < q.Wn) {
+                            w_lo = w_hi;
+                            kwlo = kwhi;
+                            w_hi = win[wi + 1];
+                            kwhi = key(w_hi);
+                        }
+                    } else {
+                        break;
+                    }
+                }
+                tl = trj;
+                ktl = ktr;
             }
         }
-        co0 = co1;
-        co1 = co2;
-        tl = tr;
-        tr = trn;
-        first = firstn;
     }
     if (open && lane < R) {
         w.B[(woff + (wi - wlo)) * R + lane] = bacc;

@@ -586,7 +586,7 @@ __device__ __forceinline__ void eval_grouped_body(const TSView &ts, const QueryP
 }
 
 template <typename F, bool UNPOL, int KQ>
-__global__ void __launch_bounds__(256) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
+__global__ void __launch_bounds__(256, 4) k_eval_grouped(TSView ts, QueryParams q, WsDev w,
     int64_t total_warps)
 {
     eval_grouped_body<F, UNPOL, KQ>(ts, q, w, total_warps, blockIdx.x, gridDim.x);

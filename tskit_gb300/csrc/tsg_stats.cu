@@ -1726,7 +1726,7 @@ int tsg_workspace_create(tsg_workspace_t **ws)
     for (int i = 0; i < 2; i++) {
         ok = ok && cudaStreamCreateWithFlags(&w->aux[i], cudaStreamNonBlocking) == cudaSuccess;
     }
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < 6; i++) {
         ok = ok && cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming) == cudaSuccess;
     }
     if (!ok) {
@@ -1737,7 +1737,7 @@ int tsg_workspace_create(tsg_workspace_t **ws)
                 w->aux[i] = nullptr;
             }
         }
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < 6; i++) {
             if (w->ev[i] != nullptr) {
                 cudaEventDestroy(w->ev[i]);
                 w->ev[i] = nullptr;
@@ -1776,7 +1776,7 @@ int tsg_workspace_free(tsg_workspace_t *ws)
                 cudaStreamDestroy(ws->aux[i]);
             }
         }
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < 6; i++) {
             if (ws->ev[i] != nullptr) {
                 cudaEventDestroy(ws->ev[i]);
             }
@@ -1885,21 +1885,34 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             // the compact replay: the first tree's items, one block per span
             // at a time, then every chunk's item values
             const int kq = q->KQ;
+            bool forked_anchors = false;
             if (p.branch && ts->v.c_num_anchors > 0) {
+                // the first tree's items are read only by the evaluation:
+                // on a side stream beside the replay when there is one
+                cudaStream_t sa = st;
+                if (fork) {
+                    TSG_CUDA(cudaEventRecord(ws->ev[4], st));
+                    TSG_CUDA(cudaStreamWaitEvent(ws->aux[1], ws->ev[4], 0));
+                    sa = ws->aux[1];
+                    forked_anchors = true;
+                }
                 const unsigned gp = (unsigned) ((ts->v.num_samples + 1023) / 1024);
                 if (kq == 1) {
-                    k_compact_prefix<1><<<gp, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                    k_compact_prefix<1><<<gp, 1024, 0, sa>>>(ts->v, p, d, w.cp0);
                 } else {
-                    k_compact_prefix<2><<<gp, 1024, 0, st>>>(ts->v, p, d, w.cp0);
+                    k_compact_prefix<2><<<gp, 1024, 0, sa>>>(ts->v, p, d, w.cp0);
                 }
                 TSG_LAUNCHED();
                 const unsigned ga = (unsigned) grid_for(ts->v.c_num_anchors);
                 if (kq == 1) {
-                    k_compact_anchors<1><<<ga, 256, 0, st>>>(ts->v, w.cp0, w);
+                    k_compact_anchors<1><<<ga, 256, 0, sa>>>(ts->v, w.cp0, w);
                 } else {
-                    k_compact_anchors<2><<<ga, 256, 0, st>>>(ts->v, w.cp0, w);
+                    k_compact_anchors<2><<<ga, 256, 0, sa>>>(ts->v, w.cp0, w);
                 }
                 TSG_LAUNCHED();
+                if (forked_anchors) {
+                    TSG_CUDA(cudaEventRecord(ws->ev[5], ws->aux[1]));
+                }
             }
             const size_t csb = (size_t) align_up(replay_state_bytes(ts->v.c_max_local, 16, kq), 16);
             void *fn = compact_kernel(kq);
@@ -1924,6 +1937,9 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 return r;
             }
             if (p.branch) {
+                if (forked_anchors) {
+                    TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[5], 0));
+                }
                 // two kernels: the items' branch lengths, then their values
                 if (p.f32) {
                     (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
