@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) kb_replay_compact(const B
         const int b = batch_find(span_off, nq, g);
         const BatchQuery &Q = bq[b];
         compact_span<KQ>(Q.v, Q.p, Q.d, Q.w, (int) (g - span_off[b]), smem_raw, sh.list, sh.stage,
-            sh.pre, sh.wsum, sh.mask);
+            sh.seek.pre, sh.wsum, sh.seek.mask);
     }
 }
 

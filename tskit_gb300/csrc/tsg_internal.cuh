@@ -171,7 +171,7 @@ struct TSView {
 // nodes one touch list of the item replay holds (a transition touching more
 // stateful nodes closes the list and opens another); the span plan counts
 // items with the same rule
-#define TSG_TOUCH_CAP 256
+#define TSG_TOUCH_CAP 128
 
 // Host copies of the topology the span plan is built from.
 struct HostTopology {
@@ -195,6 +195,12 @@ int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp,
     cudaStream_t stream);
 
 int device_count_sms();
+// per device and kernel, asked of the runtime once: resident blocks per SM
+// at a block size and dynamic shared memory, the dynamic shared memory a
+// block may have (opt-in maximum less static), and that maximum allowed
+int occupancy_blocks(const void *fn, int block, size_t smem);
+int64_t kernel_smem_budget(const void *fn);
+void allow_max_dynamic_smem(const void *fn);
 
 }  // namespace tsg
 

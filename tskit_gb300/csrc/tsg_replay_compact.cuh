@@ -22,7 +22,7 @@
 
 namespace tsg {
 
-#define TSG_COMPACT_THREADS 64
+#define TSG_COMPACT_THREADS 32
 
 // samples per thread in one step of the seek
 #define TSG_SEEK_PER 4
@@ -193,14 +193,20 @@ __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams
     __syncthreads();
 }
 
-// The block-shared arrays of the compact replay besides the span state.
+// The block-shared arrays of the compact replay besides the span state
+// (the seek's scratch and the replay's staging ring are never live at the
+// same time: they share their bytes).
 template <int KQ>
 struct CompactShared {
     TouchEntry<KQ> list[TSG_TOUCH_CAP];  // the open touch list
-    ReplayStage stage[4];                // prefetch ring, trees t .. t + 3
-    uint64_t pre[2 * (TSG_COMPACT_THREADS + 1)];
+    union {
+        ReplayStage stage[4];            // prefetch ring, trees t .. t + 3
+        struct {
+            uint64_t pre[2 * (TSG_COMPACT_THREADS + 1)];
+            uint32_t mask[TSG_COMPACT_THREADS * TSG_SEEK_PER];
+        } seek;
+    };
     uint64_t wsum[2 * (TSG_COMPACT_THREADS / 32)];
-    uint32_t mask[TSG_COMPACT_THREADS * TSG_SEEK_PER];
 };
 
 // Persistent blocks take spans from the query's counter until none is left.
@@ -221,7 +227,8 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
         if (s >= ts.c_num_spans) {
             break;
         }
-        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.pre, sh.wsum, sh.mask);
+        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.seek.pre, sh.wsum,
+            sh.seek.mask);
     }
 }
 

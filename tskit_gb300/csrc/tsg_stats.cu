@@ -480,15 +480,7 @@ static int64_t span_state_bytes(int64_t L, int W, int KQ)
 // maximum less the kernel's static shared memory.
 static int64_t smem_budget(const void *kernel)
 {
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaFuncAttributes attr;
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess
-        || cudaFuncGetAttributes(&attr, kernel) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return (int64_t) optin - (int64_t) attr.sharedSizeBytes;
+    return kernel_smem_budget(kernel);
 }
 
 static int grid_for(int64_t n, int block = 256)
@@ -966,9 +958,9 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     // workspace: per-slot node state + per-span accumulators
     int blocks_per_sm = 0;
     if (p.f32) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_sweep<float>, 256, 0);
+        blocks_per_sm = occupancy_blocks((const void *) k_sweep<float>, 256, (size_t) (0));
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_sweep<double>, 256, 0);
+        blocks_per_sm = occupancy_blocks((const void *) k_sweep<double>, 256, (size_t) (0));
     }
     int64_t slots = (int64_t) std::max(1, blocks_per_sm) * std::max(1, device_count_sms());
     const int64_t per_slot = align_up(ts->v.num_nodes * (12 + 4 * (int64_t) p.KP), 256);
@@ -1016,10 +1008,10 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
             QueryParams plain;
             std::memset(&plain, 0, sizeof(plain));
             void *fn0 = replay_kernel(q->W, q->KQ, plain);
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
-            cudaFuncSetAttribute(fn0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn0));
+            allow_max_dynamic_smem(fn);
+            allow_max_dynamic_smem(fn0);
         }
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
+        per_sm = occupancy_blocks((const void *) fn, 512, (size_t) ((size_t) q->smem_bytes));
         int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
         if (q->gstate) {
             // node state of every resident CTA at most 8 GiB
@@ -1032,7 +1024,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     q->compact_ok = q->smem && !q->gstate && q->W == 16 && q->KQ <= 2;
     if (q->compact_ok) {
         void *fn = compact_kernel(q->KQ);
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
+        allow_max_dynamic_smem(fn);
     }
     // window accumulators: per span (general sweep) or per segment (item
     // pipeline)
@@ -1250,10 +1242,10 @@ static int afs_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         void *fn = branch ? afs_replay_kernel(form) : replay_kernel(q->W, q->KQ, p);
         if (!q->gstate) {
             // a cap, not a reservation: every query of every tree sequence fits
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem_budget(fn));
+            allow_max_dynamic_smem(fn);
         }
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 512, (size_t) q->smem_bytes);
+        per_sm = occupancy_blocks((const void *) fn, 512, (size_t) ((size_t) q->smem_bytes));
         cudaGetLastError();
         int64_t grid = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
         if (q->gstate) {
@@ -1360,7 +1352,7 @@ static int matvec_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t W, 
 
     // resident CTAs, bounded by 64 GiB of node state
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_matvec_ptr(), TSG_MV_WARPS * 32, 0);
+    per_sm = occupancy_blocks((const void *) k_matvec_ptr(), TSG_MV_WARPS * 32, (size_t) (0));
     cudaGetLastError();
     int64_t slots = (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms());
     slots = std::min<int64_t>(slots, std::max<int64_t>(1, ((int64_t) 64 << 30) / m.slot_bytes));
@@ -1917,7 +1909,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             const size_t csb = (size_t) align_up(replay_state_bytes(ts->v.c_max_local, 16, kq), 16);
             void *fn = compact_kernel(kq);
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TSG_COMPACT_THREADS, csb);
+            per_sm = occupancy_blocks((const void *) fn, TSG_COMPACT_THREADS, (size_t) (csb));
             const unsigned cg = (unsigned) std::min<int64_t>(
                 (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()), ts->v.c_num_spans);
             if (q->ev_rstart != nullptr) {
@@ -2278,8 +2270,7 @@ int tsg_batch_launch(const tsg_batch_t *b, void *cuda_stream)
         }
         const size_t csb = (size_t) align_up(replay_state_bytes(g.max_local, 16, g.kq), 16);
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_replay_kernel(g.kq),
-            TSG_COMPACT_THREADS, csb);
+        per_sm = occupancy_blocks((const void *) batch_replay_kernel(g.kq), TSG_COMPACT_THREADS, (size_t) (csb));
         const unsigned grid = (unsigned) std::min<int64_t>(
             (int64_t) std::max(per_sm, 1) * std::max(1, device_count_sms()), g.spans);
         if ((ret = batch_launch_replay(g.kq, grid, csb, st, bq, nq,

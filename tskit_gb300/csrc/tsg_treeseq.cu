@@ -15,7 +15,10 @@
 #include <cerrno>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <set>
+#include <tuple>
 
 #include "tsg_internal.cuh"
 
@@ -41,6 +44,66 @@ int device_count_sms()
         return 0;
     }
     return sms;
+}
+
+// Kernel attributes asked for at every query's preparation, answered once
+// per device and kernel: the runtime's answers do not change for a loaded
+// kernel, and the calls cost far more than a lookup.
+static std::mutex g_attr_mutex;
+static std::map<std::tuple<int, const void *, int, size_t>, int> g_occupancy;
+static std::map<std::pair<int, const void *>, int64_t> g_smem_budget;
+static std::set<std::pair<int, const void *>> g_smem_allowed;
+
+int occupancy_blocks(const void *fn, int block, size_t smem)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, fn, block, smem);
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    auto it = g_occupancy.find(key);
+    if (it != g_occupancy.end()) {
+        return it->second;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    g_occupancy[key] = per_sm;
+    return per_sm;
+}
+
+int64_t kernel_smem_budget(const void *fn)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_pair(dev, fn);
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    auto it = g_smem_budget.find(key);
+    if (it != g_smem_budget.end()) {
+        return it->second;
+    }
+    int optin = 0;
+    cudaFuncAttributes attr;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess
+        || cudaFuncGetAttributes(&attr, fn) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int64_t b = (int64_t) optin - (int64_t) attr.sharedSizeBytes;
+    g_smem_budget[key] = b;
+    return b;
+}
+
+void allow_max_dynamic_smem(const void *fn)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int64_t budget = kernel_smem_budget(fn);
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    if (g_smem_allowed.insert(std::make_pair(dev, fn)).second) {
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) budget);
+    }
 }
 
 // ------------------------------------------------------------------ scan
