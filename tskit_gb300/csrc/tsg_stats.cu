@@ -691,10 +691,22 @@ static void window_units(const std::vector<double> &bp, const int32_t *ut, int64
     std::vector<int32_t> whi((size_t) NU);
     o.wlo.assign((size_t) NU, 0);
     o.woff.assign((size_t) NU + 1, 0);
+    // the units' ends and the windows both increase: one merge walk finds
+    // every unit's first window (the upper bound of its start) and last
+    // window (the lower bound of its end) -- the binary searches they replace
+    // cost most of a query's preparation on thousands of units
+    const int64_t nw = (int64_t) Wn + 1;
+    int64_t ub = 0, lb = 0;
     for (int64_t u = 0; u < NU; u++) {
         double b0 = bp[(size_t) ut[u]], b1 = bp[(size_t) ut[u + 1]];
-        int64_t lo = upper_bound(windows, (int64_t) Wn + 1, b0) - 1;
-        int64_t hi = lower_bound(windows, (int64_t) Wn + 1, b1) - 1;
+        while (ub < nw && windows[ub] <= b0) {
+            ub++;
+        }
+        while (lb < nw && windows[lb] < b1) {
+            lb++;
+        }
+        int64_t lo = ub - 1;
+        int64_t hi = lb - 1;
         lo = std::max<int64_t>(0, std::min<int64_t>(lo, (int64_t) Wn - 1));
         hi = std::max<int64_t>(lo, std::min<int64_t>(hi, (int64_t) Wn - 1));
         o.wlo[(size_t) u] = (int32_t) lo;
@@ -924,10 +936,19 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     int64_t total = align_up(off_gwsh + (int64_t) Wn * 4, 256);
     std::vector<int32_t> wsite((size_t) Wn + 1);
     {
+        // each window's first site: a branch-free binary search per window
+        // (conditional moves instead of unpredictable branches)
         const auto &sp = ts->h_site_position;
+        const int64_t S = (int64_t) sp.size();
         for (uint64_t wdx = 0; wdx <= Wn; wdx++) {
-            wsite[(size_t) wdx] = (int32_t) (std::lower_bound(sp.begin(), sp.end(), windows[wdx])
-                - sp.begin());
+            const double x = windows[wdx];
+            int64_t base = 0, len = S;
+            while (len > 1) {
+                const int64_t half = len >> 1;
+                base = sp[(size_t) (base + half - 1)] < x ? base + half : base;
+                len -= half;
+            }
+            wsite[(size_t) wdx] = (int32_t) (base + (len == 1 && sp[(size_t) base] < x ? 1 : 0));
         }
     }
     q->blob.assign((size_t) total, 0);
@@ -3292,12 +3313,18 @@ static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *resu
         q->weights = (const double *) ((char *) ts->stage + blob);
     }
     if ((ret = tsg_query_launch(q, ts->sync_ws, d_res, st)) == 0) {
+        // the result and the launch's check word come back in the same
+        // stream, one synchronisation for both
+        int32_t herr = 0;
+        const char *werr = (const char *) ts->sync_ws->ptr + q->ws_bytes - 256;
         if (cudaMemcpyAsync(result, d_res, (size_t) nres * 8, cudaMemcpyDeviceToHost, st)
+                != cudaSuccess
+            || cudaMemcpyAsync(&herr, werr, sizeof(int32_t), cudaMemcpyDeviceToHost, st)
                 != cudaSuccess
             || cudaStreamSynchronize(st) != cudaSuccess) {
             ret = TSG_ERR_CUDA;
         } else {
-            ret = tsg_workspace_check(ts->sync_ws, q);
+            ret = herr == 0 ? 0 : TSG_ERR_DEVICE_CHECK;
         }
     }
     tsg_query_free(q);
