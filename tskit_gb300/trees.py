@@ -70,6 +70,16 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size > 0 else None
 
 
+def _outputs(terms):
+    """The summary terms as the C ABI's tsg_output_t array (type, four set
+    indexes; int32 each), built as one numpy array."""
+    rows = []
+    for typ, idx in terms:
+        ix = [int(i) for i in list(idx)[:4]]
+        rows.append([int(typ)] + ix + [0] * (4 - len(ix)))
+    return np.array(rows if rows else [(0, 0, 0, 0, 0)], dtype=np.int32).reshape(-1, 5)
+
+
 class Workspace:
     """Device scratch for query launches (owned by the caller)."""
 
@@ -111,18 +121,12 @@ class Query:
         flat = (np.concatenate([np.asarray(s) for s in sample_sets])
                 if len(sample_sets) else np.zeros(0))
         flat = safe_np_int_cast(flat, np.int32)
-        outs = (nat.Output_t * max(1, len(terms)))()
-        for r, (typ, idx) in enumerate(terms):
-            outs[r].type = int(typ)
-            idx = list(idx) + [0] * (4 - len(idx))
-            for q in range(4):
-                outs[r].idx[q] = int(idx[q])
+        outs = _outputs(terms)
         win = None if windows is None else np.ascontiguousarray(windows, dtype=np.float64)
         h = ctypes.c_void_p()
         nat.check(self._lib.tsg_query_create(
             ctypes.byref(h), ts._handle, len(sizes), _ptr(sizes), _ptr(flat), len(terms),
-            ctypes.cast(outs, ctypes.c_void_p), 0 if win is None else len(win) - 1, _ptr(win),
-            flags,
+            _ptr(outs), 0 if win is None else len(win) - 1, _ptr(win), flags,
         ))
         self.handle = h
         self.num_terms = len(terms)
@@ -435,12 +439,7 @@ class TreeSequence:
         if win.ndim != 1 or len(win) < 2:
             raise ValueError("Windows arrays must have at least 2 elements")
         Wn = len(win) - 1
-        outs = (nat.Output_t * max(1, len(terms)))()
-        for r, (typ, idx) in enumerate(terms):
-            outs[r].type = int(typ)
-            idx = list(idx) + [0] * (4 - len(idx))
-            for q in range(4):
-                outs[r].idx[q] = int(idx[q])
+        outs = _outputs(terms)
         nmodes = 2 if extra & nat.STAT_BOTH_MODES else 1
         if flags & nat.STAT_NODE:
             # node mode: one row of outputs per node (trees.c:1788-1918)
@@ -449,7 +448,7 @@ class TreeSequence:
             res = np.zeros((nmodes, Wn, len(terms)))
         nat.check(self._lib.tsg_treeseq_sample_count_stat(
             self._handle, len(sizes), _ptr(sizes), _ptr(flat), len(terms),
-            ctypes.cast(outs, ctypes.c_void_p), Wn, _ptr(win), flags, _ptr(res),
+            _ptr(outs), Wn, _ptr(win), flags, _ptr(res),
         ))
         return res if nmodes == 2 else res[0]
 
