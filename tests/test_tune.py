@@ -132,3 +132,16 @@ def test_tune_compact_without_plan():
     ts = FakeCompactTS(default=0)
     rep = tune.tune_compact_spans(ts, lambda t: (lambda: 0), timer=lambda *a: 1.0)
     assert rep == {"num_spans": 0, "ms": {}, "cached": False}
+
+
+def test_cache_round_trip_and_key(tmp_path):
+    cache = {}
+    timer, _ = fake_timer({297: 2.0, 76: 1.0, 152: 3.0, 304: 3.0, 456: 3.0, 608: 3.0})
+    tune.tune_num_spans(None, lambda t: (lambda: t.num_spans), key="diversity", cache=cache,
+                        build=FakeTS, timer=timer, num_sms=152)
+    (key, val), = cache.items()
+    assert key.startswith("diversity|edges=4000|trees=1000|samples=100|sms=") and val == 76
+    path = str(tmp_path / "tune.json")
+    tune.save_cache(cache, path)
+    assert tune.load_cache(path) == cache
+    assert tune.load_cache(str(tmp_path / "missing.json")) == {}

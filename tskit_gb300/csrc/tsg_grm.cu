@@ -1098,6 +1098,7 @@ int tsg_treeseq_genotype_operand(const tsg_treeseq_t *self, int64_t site_start,
 int tsg_gram_e4m3(const uint8_t *G, int64_t n, int64_t ld, int64_t k, int32_t *P, int64_t ldp,
     void *cuda_stream)
 {
+    NvtxRange nvtx("tsg.gram");
     cudaStream_t st = (cudaStream_t) cuda_stream;
     std::vector<int32_t> tiles;
     gram_tiles(n, tiles);

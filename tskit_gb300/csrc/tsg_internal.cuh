@@ -1,6 +1,7 @@
 // Internal definitions shared by the CUDA translation units.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -195,6 +196,16 @@ int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *tmp,
     cudaStream_t stream);
 
 int device_count_sms();
+
+// Host-side phase ranges for timeline tools (NVTX; nothing happens unless a
+// tool is attached): the enqueue of a launch's seek + replay, evaluation,
+// window and site stages, a query's preparation, a Gram.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 // per device and kernel, asked of the runtime once: resident blocks per SM
 // at a block size and dynamic shared memory, the dynamic shared memory a
 // block may have (opt-in maximum less static), and that maximum allowed

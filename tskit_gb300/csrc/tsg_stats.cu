@@ -735,6 +735,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     const uint64_t *sizes, const int32_t *sets, uint64_t R, const tsg_output_t *outputs,
     uint64_t Wn, const double *windows, uint32_t options)
 {
+    NvtxRange nvtx("tsg.query_build");
     *out = nullptr;
     int ret;
     const uint32_t modes = options & (TSG_STAT_SITE | TSG_STAT_BRANCH | TSG_STAT_NODE);
@@ -1472,6 +1473,7 @@ static int matvec_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t W, 
 static int matvec_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     cudaStream_t st)
 {
+    NvtxRange nvtx("tsg.relatedness_vector");
     const int64_t nres = tsg_query_result_size(q);
     if (q->mv.W == 0 || q->mv.nf == 0) {
         return 0;
@@ -1502,6 +1504,7 @@ static int matvec_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *resu
 
 static int afs_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result, cudaStream_t st)
 {
+    NvtxRange nvtx("tsg.afs");
     const tsg_treeseq_t *ts = q->ts;
     const AfsLayout l = afs_layout(q);
     char *b = (char *) ws->ptr;
@@ -1813,6 +1816,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->kind == TSG_KIND_MATVEC) {
         return matvec_launch(q, ws, result, st);
     }
+    NvtxRange nvtx("tsg.query_launch");
     const tsg_treeseq_t *ts = q->ts;
     const QueryParams &p = q->p;
     const int64_t N = ts->v.num_nodes, NS = ts->v.num_spans;
@@ -1834,6 +1838,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     const bool site_sums = p.site && p.site_int && ts->v.num_sites > 0;
     const int form = (q->W == 16 ? 0 : 2) + (q->KQ == 1 ? 0 : 1);
     auto leaf_stage = [&](cudaStream_t s) -> int {
+        NvtxRange r("tsg.leaves");
         TSG_CUDA(cudaMemsetAsync(w.leaf_area, 0,
             (size_t) ((int64_t) p.Wn << p.K) * TSG_FX_LIMBS * 8 * 3, s));
         if (ts->v.num_edges > 0) {
@@ -1851,6 +1856,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         return 0;
     };
     auto site_stage = [&](cudaStream_t s) -> int {
+        NvtxRange r("tsg.site_sums");
         // integer numerators summed exactly per window in one pass
         TSG_CUDA(cudaMemsetAsync(w.site_acc, 0, (size_t) p.Wn * R * 16, s));
         const unsigned gsite = (unsigned) ((ts->v.num_sites + 255) / 256);
@@ -1936,6 +1942,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             if (q->ev_rstart != nullptr) {
                 TSG_CUDA(cudaEventRecord(q->ev_rstart, st));
             }
+            NvtxRange nvtx_replay("tsg.seek_replay");
             if (kq == 1) {
                 k_replay_compact<1><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
             } else {
@@ -1953,6 +1960,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 if (forked_anchors) {
                     TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[5], 0));
                 }
+                NvtxRange nvtx_eval("tsg.evaluate");
                 // two kernels: the items' branch lengths, then their values
                 if (p.f32) {
                     (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
@@ -1998,6 +2006,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             }
         }
         if (p.branch) {
+            NvtxRange nvtx_win("tsg.windows");
             k_span_windows<<<(unsigned) ((ts->v.num_segs + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
             if (!forked_leaf) {
@@ -2049,6 +2058,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             item_pipeline ? ts->v.num_segs : NS, (int) R);
         TSG_LAUNCHED();
     }
+    NvtxRange nvtx_reduce("tsg.reduce");
     if (forked_leaf) {
         TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[1], 0));
     }
@@ -2270,6 +2280,7 @@ int tsg_batch_launch(const tsg_batch_t *b, void *cuda_stream)
     if (b == nullptr) {
         return TSG_ERR_BAD_PARAM_VALUE;
     }
+    NvtxRange nvtx("tsg.batch_launch");
     cudaStream_t st = (cudaStream_t) cuda_stream;
     const char *base = (const char *) b->dbuf;
     for (const auto &g : b->groups) {
@@ -3273,6 +3284,7 @@ namespace tsg {
 static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *result,
     const void *extra = nullptr, int64_t extra_bytes = 0)
 {
+    NvtxRange nvtx("tsg.sync_query");
     tsg_treeseq_t *ts = const_cast<tsg_treeseq_t *>(cts);
     int ret;
     std::lock_guard<std::mutex> lock(ts->sync_mutex);

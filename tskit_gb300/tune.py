@@ -24,9 +24,10 @@ same way on one tree sequence, rebuilding only that plan per candidate.
 
 The CTA shape is not tuned: every replay kernel is compiled for one block
 size (its launch bounds) and fills the SMs by occupancy.  An optional
-``cache`` dict, keyed by the caller's workload key and the tree sequence's
-shape, skips the measurement for a tree sequence seen before; it can be kept
-across processes as JSON by the caller.
+``cache`` dict, keyed by the caller's workload key (the statistic family),
+the tree sequence's shape and the SM count, skips the measurement for a tree
+sequence seen before; ``save_cache`` / ``load_cache`` keep it across
+processes as JSON.
 """
 import numpy as np
 
@@ -61,8 +62,44 @@ def time_step(step, steps=3, warmup=1):
     return float(np.median(times))
 
 
+def _sm_count():
+    """SMs of the current CUDA device (0 without one)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return int(torch.cuda.get_device_properties(torch.cuda.current_device())
+                       .multi_processor_count)
+    except Exception:
+        pass
+    return 0
+
+
 def _shape_key(ts, key):
-    return f"{key}|edges={ts.num_edges}|trees={ts.num_trees}|samples={ts.num_samples}"
+    """Cache key: the caller's workload (statistic family) key, the tree
+    sequence's shape and the device's SM count."""
+    return (f"{key}|edges={ts.num_edges}|trees={ts.num_trees}|samples={ts.num_samples}"
+            f"|sms={_sm_count()}")
+
+
+def load_cache(path):
+    """A tuning cache saved by :func:`save_cache` (empty if there is none)."""
+    import json
+    import os
+
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return {str(k): int(v) for k, v in json.load(f).items()}
+
+
+def save_cache(cache, path):
+    """Write a tuning cache (keys: workload, tree-sequence shape and SM
+    count; values: span counts) as JSON."""
+    import json
+
+    with open(path, "w") as f:
+        json.dump(dict(sorted(cache.items())), f, indent=1)
 
 
 def tune_num_spans(tables, make_step, key="", candidates=None, steps=3, warmup=1, cache=None,
