@@ -909,8 +909,9 @@ def run_grm_n20k(args):
 
     with ClockSampler(0) as clocks:
         ms = _timed_steps(gram, args.steps, args.warmup, flush, stream)
-    tiles = sum(1 for r in range(0, n, 128) for c in range(0, n, 256) if c + 256 > r)
-    executed = tiles * 128 * 256 * kp * 2
+    nb = (n + 255) // 256
+    tiles = nb * (nb + 1) // 2  # 256 x 256 tiles, row block <= column block
+    executed = tiles * 256 * 256 * kp * 2
     t0 = time.perf_counter()
     K = ts.genetic_relatedness_matrix()
     e2e_s = time.perf_counter() - t0
@@ -965,12 +966,12 @@ def grm_parity(O, ots, G, P, K, n, S, kp):
 
     1. Operand: the device-decoded genotypes of 2,048 sites equal the
        oracle's decode for all samples.
-    2. Gram: 64 tiles of 128 x 256 (8 random row blocks x 8 random column
+    2. Gram: 64 blocks of 128 x 256 (8 random row blocks x 8 random column
        blocks) of the int32 product equal a CPU integer product of the same
        operand rows (float32 BLAS over 32,768-site slices, exact since each
-       slice's sums stay below 2^24, summed in int64).  Entries of tiles the
-       Gram skips (below the diagonal band) are read from the transposed
-       entry.
+       slice's sums stay below 2^24, summed in int64).  Entries below the
+       diagonal, which the Gram does not compute, are read from the
+       transposed entry.
     3. Rows: 8 random full rows of the product equal the oracle's exact
        shared-derived counts, and the same rows of the final matrix are
        within 1e-12 (normwise per row) of the oracle's exact rows."""
@@ -993,12 +994,12 @@ def grm_parity(O, ots, G, P, K, n, S, kp):
 
     def full(rows, cols):
         """Product entries (rows x cols), each read from a tile the Gram
-        computes: tile (r, c) is computed when c + 256 > r."""
+        computes: 256 x 256 tiles with row block <= column block."""
         r = torch.as_tensor(rows, device=P.device)
         c = torch.as_tensor(cols, device=P.device)
         direct = P.index_select(0, r).index_select(1, c)
         transposed = P.index_select(1, r).index_select(0, c).T
-        computed = (c // 256 * 256 + 256)[None, :] > (r // 128 * 128)[:, None]
+        computed = (c // 256)[None, :] >= (r // 256)[:, None]
         return torch.where(computed, direct, transposed).cpu().numpy().astype(np.int64)
 
     # 2. tiles vs a CPU integer product of the operand

@@ -33,18 +33,17 @@ def _gram(lib, G01):
 
 
 def _upper_tiles_mask(n):
-    """Entries the kernel writes: tiles of 128 rows x 256 columns in the
-    upper triangle."""
+    """Entries the kernel writes: 256 x 256 tiles with row block <= column
+    block (every entry of the upper triangle and the diagonal)."""
     m = np.zeros((n, n), dtype=bool)
-    for r in range(0, n, 128):
-        for c in range(0, n, 256):
-            if c + 256 > r:
-                m[r:r + 128, c:c + 256] = True
+    for r in range(0, n, 256):
+        m[r:r + 256, r:] = True
+    assert m[np.triu_indices(n)].all()
     return m
 
 
 @pytest.mark.parametrize("n,k,p", [(128, 128, 0.5), (300, 1024, 0.3), (777, 128 * 37, 0.05),
-                                   (1000, 4096, 0.9), (256, 128 * 300, 0.5)])
+                                   (1000, 4096, 0.9), (256, 128 * 300, 0.5), (1100, 512, 0.2)])
 def test_gram_exact(cuda_lib, n, k, p):
     rng = np.random.default_rng(n + k)
     G01 = (rng.random((n, k)) < p).astype(np.int64)

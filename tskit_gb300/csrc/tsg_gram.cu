@@ -8,16 +8,20 @@
 // integer multiplier) into an int32 result.  (tcgen05.mma .kind::i8 is not
 // available for sm_103a; .kind::f8f6f4 computes the same integers.)
 //
-// One CTA per 128 x 256 output tile of the upper triangle:
-//   warp 0       TMA producer: 128 x 128-byte A and 256 x 128-byte B tiles,
-//                128-byte swizzle, into a 4-stage shared-memory ring
-//                (mbarrier full/empty pairs);
-//   warp 1       allocates 256 TMEM columns (FP32 accumulator, row = lane)
-//                and issues tcgen05.mma (M 128, N 256, K 32) from one thread;
+// One CTA per 256 x 256 output tile of the upper triangle (block row <=
+// block column), two 128-row halves sharing the B operand -- half the
+// L2-to-SM operand bytes per FLOP of separate 128 x 256 tiles, the bound of
+// this contraction:
+//   warp 0       TMA producer: two 128 x 128-byte A tiles and one 256 x
+//                128-byte B tile, 128-byte swizzle, into a 3-stage
+//                shared-memory ring (mbarrier full/empty pairs);
+//   warp 1       allocates all 512 TMEM columns (two FP32 accumulators of
+//                256 columns, row = lane) and issues tcgen05.mma (M 128,
+//                N 256, K 32) twice per K step, one per half, from one thread;
 //                tcgen05.commit frees each stage and finally signals the
-//                accumulator;
-//   warps 2..5   epilogue: tcgen05.ld 32 lanes x 32 columns at a time, convert
-//                to integers, add into the result.
+//                accumulators;
+//   warps 2..5   epilogue: tcgen05.ld 32 lanes x 32 columns at a time, both
+//                halves, convert to integers, add into the result.
 // Every wait is bounded: on expiry the CTA records an error, drains its own
 // copies in flight, frees its TMEM and returns.
 #include <cuda.h>
@@ -26,15 +30,17 @@
 
 namespace tsg {
 
-#define GRAM_BM 128
+#define GRAM_BM 128                // rows of one MMA (one half of a tile)
+#define GRAM_HALVES 2              // halves of a tile sharing the B operand
+#define GRAM_TILE_ROWS (GRAM_BM * GRAM_HALVES)
 #define GRAM_BN 256
 #define GRAM_BK 128
-#define GRAM_STAGES 4
+#define GRAM_STAGES 3
 #define GRAM_A_BYTES (GRAM_BM * GRAM_BK)
 #define GRAM_B_BYTES (GRAM_BN * GRAM_BK)
-#define GRAM_STAGE_BYTES (GRAM_A_BYTES + GRAM_B_BYTES)
+#define GRAM_STAGE_BYTES (GRAM_HALVES * GRAM_A_BYTES + GRAM_B_BYTES)
 #define GRAM_SMEM_BYTES (GRAM_STAGES * GRAM_STAGE_BYTES + 1024 + 256)
-#define GRAM_TMEM_COLS 256
+#define GRAM_TMEM_COLS (GRAM_HALVES * GRAM_BN)
 #define GRAM_SPIN_LIMIT (1u << 26)
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
@@ -189,8 +195,10 @@ __global__ void __launch_bounds__(192, 1) k_gram_f8(const __grid_constant__ CUte
                 const uint32_t full = smem_addr(&bars[s]);
                 const uint32_t sa = smem_addr(smem + s * GRAM_STAGE_BYTES);
                 mbar_expect_tx(full, GRAM_STAGE_BYTES);
+                // rows past n (a last half outside the matrix) arrive as zeros
                 tma_load_2d(sa, &mapA, kb * GRAM_BK, tile.row, full);
-                tma_load_2d(sa + GRAM_A_BYTES, &mapB, kb * GRAM_BK, tile.col, full);
+                tma_load_2d(sa + GRAM_A_BYTES, &mapA, kb * GRAM_BK, tile.row + GRAM_BM, full);
+                tma_load_2d(sa + GRAM_HALVES * GRAM_A_BYTES, &mapB, kb * GRAM_BK, tile.col, full);
                 issued = kb + 1;
             }
         }
@@ -209,12 +217,16 @@ __global__ void __launch_bounds__(192, 1) k_gram_f8(const __grid_constant__ CUte
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t sa = smem_addr(smem + s * GRAM_STAGE_BYTES);
-                const uint64_t da = umma_desc(sa), db = umma_desc(sa + GRAM_A_BYTES);
+                const uint64_t da0 = umma_desc(sa), da1 = umma_desc(sa + GRAM_A_BYTES);
+                const uint64_t db = umma_desc(sa + GRAM_HALVES * GRAM_A_BYTES);
 #pragma unroll
                 for (int k = 0; k < GRAM_BK / 32; k++) {
-                    // 32 E4M3 = 32 bytes along K: advance the start address
-                    umma_f8(tmem, da + (uint64_t) (k * 2), db + (uint64_t) (k * 2), idesc,
-                        (kb > 0 || k > 0) ? 1u : 0u);
+                    // 32 E4M3 = 32 bytes along K: advance the start address;
+                    // the second half accumulates 256 TMEM columns further
+                    const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+                    umma_f8(tmem, da0 + (uint64_t) (k * 2), db + (uint64_t) (k * 2), idesc, acc);
+                    umma_f8(tmem + GRAM_BN, da1 + (uint64_t) (k * 2), db + (uint64_t) (k * 2), idesc,
+                        acc);
                 }
                 umma_commit(smem_addr(&bars[GRAM_STAGES + s]));
             }
@@ -232,11 +244,14 @@ __global__ void __launch_bounds__(192, 1) k_gram_f8(const __grid_constant__ CUte
             atomicExch(&s_abort, 1);
             dev_error(err, 1);
         } else if (!*(volatile int *) &s_abort) {
-            const int row = tile.row + quarter * 32 + lane;
+#pragma unroll 1
+          for (int h = 0; h < GRAM_HALVES; h++) {
+            const int row = tile.row + h * GRAM_BM + quarter * 32 + lane;
 #pragma unroll 1
             for (int c0 = 0; c0 < GRAM_BN; c0 += 32) {
                 uint32_t v[32];
-                const uint32_t taddr = tmem + ((uint32_t) (quarter * 32) << 16) + (uint32_t) c0;
+                const uint32_t taddr = tmem + ((uint32_t) (quarter * 32) << 16)
+                    + (uint32_t) (h * GRAM_BN + c0);
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
                     "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
@@ -263,6 +278,7 @@ __global__ void __launch_bounds__(192, 1) k_gram_f8(const __grid_constant__ CUte
                     }
                 }
             }
+          }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -322,17 +338,15 @@ static int make_map(CUtensorMap *map, const uint8_t *G, int64_t rows, int64_t ld
     return r == CUDA_SUCCESS ? 0 : TSG_ERR_CUDA;
 }
 
-// Tiles of the upper triangle (row block i, column block j with some
-// column >= some row), row-major order.
+// Tiles of the upper triangle: 256 x 256 blocks (row block <= column
+// block), row-major order; together they hold every entry (i, j), i <= j.
 int gram_tiles(int64_t n, std::vector<int32_t> &out)
 {
     out.clear();
-    for (int64_t r = 0; r < n; r += GRAM_BM) {
-        for (int64_t c = 0; c < n; c += GRAM_BN) {
-            if (c + GRAM_BN > r) {
-                out.push_back((int32_t) r);
-                out.push_back((int32_t) c);
-            }
+    for (int64_t r = 0; r < n; r += GRAM_TILE_ROWS) {
+        for (int64_t c = r; c < n; c += GRAM_BN) {
+            out.push_back((int32_t) r);
+            out.push_back((int32_t) c);
         }
     }
     return 0;
