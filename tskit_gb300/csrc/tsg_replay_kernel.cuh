@@ -437,7 +437,6 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
             cnt(lo, hi, h2, s2), cnt(lo, hi, h3, s3), ni, nj, nk, nl);
     };
     double acc = 0;
-#pragma unroll 2
     for (int64_t i = b; i < e; i++) {
         uint64_t x0lo, x0hi = 0, x1lo, x1hi = 0;
         if (KQ == 1) {
