@@ -1,21 +1,20 @@
 // The compact replay: the item pipeline's replay over the compact span plan
-// (tsg_cplan.cu).  One block of TSG_COMPACT_THREADS threads per span at a
+// (tsg_cplan.cu).  One block of one warp (TSG_COMPACT_THREADS) per span at a
 // time, the span's node state (16-bit counts packed in 64-bit words and
-// 16-bit parent entries) in shared memory: a few kilobytes, so many blocks
-// -- and many sequential replays -- run on every SM.
+// 16-bit parent entries) in shared memory: a few kilobytes, so about twenty
+// blocks -- twenty sequential replays -- run on every SM.
 //
-//   seek     both warps: the prefix sum of the sample-set bits along the
-//            span's depth-first sample order, 64 samples per step (warp
-//            shuffles and the warp totals), and at each sorted range endpoint
-//            a node's count: P[hi] - P[lo] (the start is stored first, the
-//            end then subtracts it);
-//   replay   warp 0: replay_span over the compact encodings.
+//   seek     the prefix sum of the sample-set bits along the span's
+//            depth-first sample order, TSG_SEEK_PER samples per lane and
+//            step (warp shuffles), the next step's loads in flight, and at
+//            each sorted range endpoint a node's count: P[hi] - P[lo] (the
+//            start is stored first, the end then subtracts it);
+//   replay   replay_span over the compact encodings.
 //
 // The first tree's items (its stateful nodes, the anchors) are written by
 // k_compact_anchors from the prefix sum of the first span's order
-// (k_compact_prefix) before the replay starts, and k_item_bls and
-// k_eval_grouped value every chunk of items after it, all chunks in
-// parallel.
+// (k_compact_prefix), and k_item_bls and k_eval_grouped value every chunk
+// of items after the replay, all chunks in parallel.
 #pragma once
 
 #include "tsg_replay_kernel.cuh"
