@@ -455,17 +455,24 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
         const bool same = x0lo == x1lo && x0hi == x1hi;
         const uint64_t ba = (uint64_t) __double_as_longlong(f.x);
         const uint64_t bb = (uint64_t) __double_as_longlong(f.y);
+        // one uniform FP64 fused multiply-add per item: the multiplier is
+        // N(x1) with unchanged counts (bl1 - bl0 in f.x) or no old branch,
+        // N(x1) - N(x0) with an unchanged branch (exact in integers), N(x1)
+        // when both changed -- whose bl0 N(x0) term, the only other FP64
+        // operation, is taken first (the lanes of a warp walk different
+        // items, so per-case FP64 instructions would each issue with part
+        // of the warp: the FP64 pipe issues a warp instruction every 16
+        // cycles whatever its active lanes)
         const int64_t n1 = num(x1lo, x1hi);
-        if (same || bb == 0) {
-            acc = fma(f.x, i64_to_f64(n1), acc);
-        } else {
-            const int64_t n0 = num(x0lo, x0hi);
-            if (ba == bb) {
-                acc = fma(f.x, i64_to_f64(n1 - n0), acc);
-            } else {
-                acc = fma(f.x, i64_to_f64(n1), fma(-f.y, i64_to_f64(n0), acc));
-            }
+        const bool plain = same || bb == 0;
+        const int64_t n0 = plain ? 0 : num(x0lo, x0hi);
+        const bool both = !plain && ba != bb;
+        const int64_t d = (plain || both) ? n1 : n1 - n0;
+        double a0 = acc;
+        if (both) {
+            a0 = fma(-f.y, i64_to_f64(n0), acc);
         }
+        acc = fma(f.x, i64_to_f64(d), a0);
     }
     return acc;
 }
