@@ -620,6 +620,15 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if rank == 0:
+        # batching across resident tree sequences (outside the timed region):
+        # one fused query each on six smaller sequences, one launch per
+        # stage for all of them against their own launches
+        from tskit_gb300 import sim
+
+        small = {f"n{n}_{i}": tskit_gb300.TreeSequence(sim.simulate(n, 1e7, 5 * n, 5 * n, 3000 + i))
+                 for i, n in enumerate([1000, 2000, 5000, 10000, 20000, 20000])}
+        line["batch_across_tree_sequences"] = batch_vs_single(small)
     if not args.no_cpu_baseline:
         cpu_s, raw_oracle, ncalls = cpu_oracle_run(tables, sets, windows, pairs, triples)
         line["cpu_baseline"] = {
