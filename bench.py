@@ -308,23 +308,48 @@ class ClockSampler:
         self.proc = None
         self.path = os.path.join(REPO, ".cache", f"clocks_{os.getpid()}.csv")
 
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return sum(1 for _ in f)
+        except OSError:
+            return 0
+
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
             self.f = open(self.path, "w")
+            # line-buffered (stdbuf) so that each sample reaches the file
+            # as it is taken, not when the sampler is stopped
+            import shutil
+
+            prefix = ["stdbuf", "-oL"] if shutil.which("stdbuf") else []
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index),
+                prefix + ["nvidia-smi", "-i", str(self.index),
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=self.f, stderr=subprocess.DEVNULL, bufsize=0)
         except Exception:
             self.proc = None
+        # the sampler is running (its first sample written) before the
+        # region starts, so a region shorter than its start-up is covered
+        self.start_lines = 0
+        if self.proc is not None:
+            t0 = time.time()
+            while self._lines() < 1 and time.time() - t0 < 5 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.start_lines = self._lines()
         return self
 
     def __exit__(self, *a):
         if self.proc is not None:
+            # at least one sample taken after the region started
+            t0 = time.time()
+            while (self._lines() <= self.start_lines and time.time() - t0 < 2
+                   and self.proc.poll() is None):
+                time.sleep(0.01)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
