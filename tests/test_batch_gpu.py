@@ -171,3 +171,33 @@ def test_batch_in_cuda_graph(resident):
     batch.check()
     for mine, r in zip(own, results):
         np.testing.assert_array_equal(_bits(r.cpu().numpy()), _bits(mine))
+
+
+def test_query_launch_in_cuda_graph(resident):
+    """A single query's launch -- its independent stages forked onto the
+    workspace's side streams and joined by events -- replays from a captured
+    CUDA graph with the eager launch's results."""
+    import torch
+
+    import tskit_gb300
+
+    qs = [(q, d) for q, d in _queries(resident) if d["kind"] == "counts"
+          and resident[d["ts"]][0].num_compact_spans > 0 and d["both"]][:3]
+    assert qs
+    st = torch.cuda.Stream()
+    for q, _ in qs:
+        ws = tskit_gb300.Workspace(q.workspace_bytes)
+        eager = _own(q)
+        res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(st):
+            q.launch(ws, res, st)  # warm-up outside the capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st):
+            q.launch(ws, res, st)
+        res.zero_()
+        g.replay()
+        g.replay()
+        torch.cuda.synchronize()
+        q.check(ws)
+        np.testing.assert_array_equal(_bits(res.cpu().numpy()), _bits(eager))
