@@ -250,8 +250,6 @@ struct tsg_treeseq {
     tsg_workspace *sync_ws = nullptr;
     void *stage = nullptr;
     int64_t stage_bytes = 0;
-    void *hstage = nullptr;       // pinned host copy of stage: the copies run at full speed
-    int64_t hstage_bytes = 0;
     cudaStream_t sync_stream = nullptr;
 };
 

@@ -3311,43 +3311,12 @@ static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *resu
         }
         ts->stage_bytes = need;
     }
-    // pinned host staging of the same layout plus the check word: the
-    // query image goes up and the result comes back as single full-speed
-    // copies (pageable copies are staged by the driver in pieces)
-    // (small queries only: a large result is faster copied straight into
-    // the caller's memory than through a second host copy)
-    const int64_t hneed = need + 256;
-    const bool pinned = hneed <= ((int64_t) 8 << 20);
-    if (pinned && hneed > ts->hstage_bytes) {
-        if (ts->hstage != nullptr) {
-            cudaFreeHost(ts->hstage);
-        }
-        ts->hstage = nullptr;
-        ts->hstage_bytes = 0;
-        if (cudaMallocHost(&ts->hstage, (size_t) hneed) == cudaSuccess) {
-            ts->hstage_bytes = hneed;
-        } else {
-            cudaGetLastError();
-        }
-    }
-    char *hs = pinned && hneed <= ts->hstage_bytes ? (char *) ts->hstage : nullptr;
     double *d_res = (double *) ((char *) ts->stage + blob + xb);
-    bool up_ok;
-    if (hs != nullptr) {
-        std::memcpy(hs, q->blob.data(), q->blob.size());
-        if (extra_bytes > 0) {
-            std::memcpy(hs + blob, extra, (size_t) extra_bytes);
-        }
-        up_ok = cudaMemcpyAsync(ts->stage, hs, (size_t) (blob + (extra_bytes > 0 ? xb : 0)),
-                    cudaMemcpyHostToDevice, st) == cudaSuccess;
-    } else {
-        up_ok = cudaMemcpyAsync(ts->stage, q->blob.data(), q->blob.size(), cudaMemcpyHostToDevice,
-                    st) == cudaSuccess
-            && (extra_bytes == 0
-                || cudaMemcpyAsync((char *) ts->stage + blob, extra, (size_t) extra_bytes,
-                       cudaMemcpyHostToDevice, st) == cudaSuccess);
-    }
-    if (!up_ok) {
+    if (cudaMemcpyAsync(ts->stage, q->blob.data(), q->blob.size(), cudaMemcpyHostToDevice, st)
+            != cudaSuccess
+        || (extra_bytes > 0
+            && cudaMemcpyAsync((char *) ts->stage + blob, extra, (size_t) extra_bytes,
+                   cudaMemcpyHostToDevice, st) != cudaSuccess)) {
         tsg_query_free(q);
         return TSG_ERR_CUDA;
     }
@@ -3360,19 +3329,13 @@ static int run_sync_query(const tsg_treeseq_t *cts, tsg_query_t *q, double *resu
         // stream, one synchronisation for both
         int32_t herr = 0;
         const char *werr = (const char *) ts->sync_ws->ptr + q->ws_bytes - 256;
-        double *hres = hs != nullptr ? (double *) (hs + blob + xb) : result;
-        int32_t *herrp = hs != nullptr ? (int32_t *) (hs + need) : &herr;
-        if (cudaMemcpyAsync(hres, d_res, (size_t) nres * 8, cudaMemcpyDeviceToHost, st)
+        if (cudaMemcpyAsync(result, d_res, (size_t) nres * 8, cudaMemcpyDeviceToHost, st)
                 != cudaSuccess
-            || cudaMemcpyAsync(herrp, werr, sizeof(int32_t), cudaMemcpyDeviceToHost, st)
+            || cudaMemcpyAsync(&herr, werr, sizeof(int32_t), cudaMemcpyDeviceToHost, st)
                 != cudaSuccess
             || cudaStreamSynchronize(st) != cudaSuccess) {
             ret = TSG_ERR_CUDA;
         } else {
-            if (hs != nullptr) {
-                std::memcpy(result, hres, (size_t) nres * 8);
-                herr = *herrp;
-            }
             ret = herr == 0 ? 0 : TSG_ERR_DEVICE_CHECK;
         }
     }

@@ -553,9 +553,6 @@ int tsg_treeseq_free(tsg_treeseq_t *ts)
         tsg_workspace_free(ts->sync_ws);
     }
     cudaFree(ts->stage);
-    if (ts->hstage != nullptr) {
-        cudaFreeHost(ts->hstage);
-    }
     delete ts;
     return 0;
 }
