@@ -437,21 +437,37 @@ __device__ __forceinline__ double lane_walk_num(const Item<KQ> *items, const dou
             cnt(lo, hi, h2, s2), cnt(lo, hi, h3, s3), ni, nj, nk, nl);
     };
     double acc = 0;
+    // the next item's counts and branch lengths are loaded while this one
+    // is valued (the walk is bound by these loads' latency)
+    ulonglong2 na = make_ulonglong2(0, 0), nc = make_ulonglong2(0, 0);
+    double2 nf = make_double2(0, 0);
+    if (b < e) {
+        na = *(const ulonglong2 *) items[b].x0;
+        if (KQ > 1) {
+            nc = *(const ulonglong2 *) items[b].x1;
+        }
+        nf = *(const double2 *) (bls + 2 * b);
+    }
     for (int64_t i = b; i < e; i++) {
+        const ulonglong2 ca = na, cc = nc;
+        const double2 f = nf;
+        if (i + 1 < e) {
+            na = *(const ulonglong2 *) items[i + 1].x0;
+            if (KQ > 1) {
+                nc = *(const ulonglong2 *) items[i + 1].x1;
+            }
+            nf = *(const double2 *) (bls + 2 * (i + 1));
+        }
         uint64_t x0lo, x0hi = 0, x1lo, x1hi = 0;
         if (KQ == 1) {
-            const ulonglong2 xx = *(const ulonglong2 *) items[i].x0;
-            x0lo = xx.x;
-            x1lo = xx.y;
+            x0lo = ca.x;
+            x1lo = ca.y;
         } else {
-            const ulonglong2 a = *(const ulonglong2 *) items[i].x0;
-            const ulonglong2 c = *(const ulonglong2 *) items[i].x1;
-            x0lo = a.x;
-            x0hi = a.y;
-            x1lo = c.x;
-            x1hi = c.y;
+            x0lo = ca.x;
+            x0hi = ca.y;
+            x1lo = cc.x;
+            x1hi = cc.y;
         }
-        const double2 f = *(const double2 *) (bls + 2 * i);
         const bool same = x0lo == x1lo && x0hi == x1hi;
         const uint64_t ba = (uint64_t) __double_as_longlong(f.x);
         const uint64_t bb = (uint64_t) __double_as_longlong(f.y);
