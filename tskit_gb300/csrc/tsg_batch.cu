@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) kb_compact_anchors(const BatchQuery *bq, 
     int nq)
 {
     TSG_BATCH_QUERY();
-    compact_anchors_body<KQ>(Q.v, Q.w.cp0, Q.w, bid, nb);
+    compact_anchors_body<KQ>(Q.v, Q.p, Q.w.cp0, Q.w, bid, nb);
 }
 
 __global__ void __launch_bounds__(256) kb_span_windows(const BatchQuery *bq, const int64_t *off,

@@ -43,24 +43,15 @@ TSG_REPLAY_EVAL_LAUNCHER(TSG_EVAL_NAME)
 
 TSG_CHUNK_EVAL_LAUNCHER(TSG_CHUNKS_NAME)
 {
+    // the replay wrote each item's branch lengths with the item
     const int64_t C = v.num_chunks;
     const int64_t total = (C + TSG_EVAL_BLOCK - 1) / TSG_EVAL_BLOCK * p.gwpb;
-    const unsigned gb = (unsigned) std::min<int64_t>((C + 7) / 8, 1 << 20);
     const unsigned ge = (unsigned) std::min<int64_t>((total + 7) / 8, 1 << 20);
     if (kq == 1) {
-        k_item_bls<TSG_EVAL_F, 1><<<gb, 256, 0, st>>>(v, p, w);
         k_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<ge, 256, 0, st>>>(v, p, w, total);
     } else {
-        k_item_bls<TSG_EVAL_F, 2><<<gb, 256, 0, st>>>(v, p, w);
         k_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<ge, 256, 0, st>>>(v, p, w, total);
     }
-}
-
-template <typename F, int KQ>
-__global__ void __launch_bounds__(256) kb_item_bls(const BatchQuery *bq, const int64_t *off, int nq)
-{
-    TSG_BATCH_QUERY();
-    item_bls_body<F, KQ>(Q.v, Q.p, Q.w, bid, nb);
 }
 
 template <typename F, bool UNPOL, int KQ>
@@ -74,22 +65,15 @@ __global__ void __launch_bounds__(256) kb_eval_grouped(const BatchQuery *bq, con
 
 TSG_CHUNK_EVAL_BATCH_LAUNCHER(TSG_CHUNKS_BATCH_NAME)
 {
+    if (blocks_eval <= 0) {
+        return;
+    }
     if (kq == 1) {
-        if (blocks_bls > 0) {
-            kb_item_bls<TSG_EVAL_F, 1><<<(unsigned) blocks_bls, 256, 0, st>>>(bq, off_bls, nq);
-        }
-        if (blocks_eval > 0) {
-            kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<(unsigned) blocks_eval, 256, 0, st>>>(
-                bq, off_eval, nq);
-        }
+        kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 1><<<(unsigned) blocks_eval, 256, 0, st>>>(
+            bq, off_eval, nq);
     } else {
-        if (blocks_bls > 0) {
-            kb_item_bls<TSG_EVAL_F, 2><<<(unsigned) blocks_bls, 256, 0, st>>>(bq, off_bls, nq);
-        }
-        if (blocks_eval > 0) {
-            kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<(unsigned) blocks_eval, 256, 0, st>>>(
-                bq, off_eval, nq);
-        }
+        kb_eval_grouped<TSG_EVAL_F, TSG_EVAL_UNPOL, 2><<<(unsigned) blocks_eval, 256, 0, st>>>(
+            bq, off_eval, nq);
     }
 }
 

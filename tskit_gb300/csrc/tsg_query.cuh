@@ -225,8 +225,8 @@ TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_pol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f32_unpol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_pol);
 TSG_REPLAY_EVAL_FN(replay_eval_fn_f64_unpol);
-// Every chunk's item values after the compact replay (kq: count words per
-// node, 1 or 2).
+// Every chunk's item values after the compact replay, which wrote each
+// item's branch lengths with it (kq: count words per node, 1 or 2).
 #define TSG_CHUNK_EVAL_LAUNCHER(name)                                                    \
     void name(int kq, cudaStream_t st, const TSView &v, const QueryParams &p, const WsDev &w)
 TSG_CHUNK_EVAL_LAUNCHER(launch_eval_chunks_f32_pol);
@@ -271,11 +271,11 @@ __device__ __forceinline__ int batch_find(const int64_t *off, int nq, int64_t bl
     const int64_t bid = (int64_t) blockIdx.x - off[b_];                       \
     const int64_t nb = off[b_ + 1] - off[b_]
 
-// The chunk evaluation of a batch (kq as above): item branch lengths, then
-// item values, each one launch over the batch's queries.
+// The chunk evaluation of a batch (kq as above): the item values, one launch
+// over the batch's queries.
 #define TSG_CHUNK_EVAL_BATCH_LAUNCHER(name)                                              \
-    void name(int kq, cudaStream_t st, const BatchQuery *bq, int nq, const int64_t *off_bls, \
-        int64_t blocks_bls, const int64_t *off_eval, int64_t blocks_eval)
+    void name(int kq, cudaStream_t st, const BatchQuery *bq, int nq, const int64_t *off_eval, \
+        int64_t blocks_eval)
 TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f32_pol);
 TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f32_unpol);
 TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f64_pol);
@@ -283,7 +283,7 @@ TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f64_unpol);
 
 // The other stages of a batch (tsg_batch.cu).
 enum BatchStage {
-    BS_ZERO, BS_NODE_MASK, BS_PREFIX, BS_ANCHORS, BS_BLS, BS_EVAL, BS_SPAN_WINDOWS,
+    BS_ZERO, BS_NODE_MASK, BS_PREFIX, BS_ANCHORS, BS_EVAL, BS_SPAN_WINDOWS,
     BS_LEAF_AREAS, BS_LEAF_PREFIX, BS_LEAF_TERMS, BS_SITE_SUMS, BS_SITE_FINISH, BS_SPAN_SCAN,
     BS_REDUCE, BS_COUNT
 };

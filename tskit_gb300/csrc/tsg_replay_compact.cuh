@@ -13,8 +13,9 @@
 //
 // The first tree's items (its stateful nodes, the anchors) are written by
 // k_compact_anchors from the prefix sum of the first span's order
-// (k_compact_prefix), and k_item_bls and k_eval_grouped value every chunk
-// of items after the replay, all chunks in parallel.
+// (k_compact_prefix); the replay writes every other item with its branch
+// lengths, and k_eval_grouped values every chunk of items after it, all
+// chunks in parallel.
 #pragma once
 
 #include "tsg_replay_kernel.cuh"
@@ -186,7 +187,7 @@ __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams
     }
     compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum, s_mask);
     if (threadIdx.x < 32) {
-        replay_span<16, KQ, uint16_t, false>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
+        replay_span<16, KQ, uint16_t, false, true>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
             t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
     }
     __syncthreads();
@@ -326,25 +327,39 @@ __global__ void __launch_bounds__(1024) k_compact_prefix(TSView ts, QueryParams 
 // tree, in edge order) with its counts, P0[hi] - P0[lo], and its parent, in
 // the anchors' numbering.
 template <int KQ>
-__device__ __forceinline__ void compact_anchors_body(const TSView &ts, const uint64_t *P0, const WsDev &w,
-    const int64_t bid, const int64_t nb)
+__device__ __forceinline__ void compact_anchors_body(const TSView &ts, const QueryParams &q,
+    const uint64_t *P0, const WsDev &w, const int64_t bid, const int64_t nb)
 {
     Item<KQ> *items = (Item<KQ> *) w.items;
     const int64_t base = ts.tree_item_off[0];
+    // the first tree's items read the node times of the span that numbers them
+    const double *time = ts.c_time + ts.c_local_off[ts.c_chunk_span[ts.tree_chunk_off[0]]];
     for (int64_t k = bid * (int64_t) blockDim.x + threadIdx.x; k < ts.c_num_anchors;
          k += (int64_t) nb * blockDim.x) {
         const int2 r = ts.c_anchor_range[k];
         Pack x;
         x.lo = P0[2 * r.y] - P0[2 * r.x];
         x.hi = P0[2 * r.y + 1] - P0[2 * r.x + 1];
-        item_put<KQ>(items + base + k, Pack{0, 0}, x, (int32_t) k, -1, ts.c_anchor_par[k]);
+        const int32_t p1 = ts.c_anchor_par[k];
+        item_put<KQ>(items + base + k, Pack{0, 0}, x, (int32_t) k, -1, p1);
+        // branch lengths (no branch before: bl0 = 0)
+        const double bl1 = p1 >= 0 ? time[p1] - time[k] : 0.0;
+        if (q.f32) {
+            float *bls = (float *) w.bl;
+            bls[2 * (base + k)] = (float) bl1;
+            bls[2 * (base + k) + 1] = 0.0f;
+        } else {
+            double *bls = (double *) w.bl;
+            bls[2 * (base + k)] = bl1;
+            bls[2 * (base + k) + 1] = 0.0;
+        }
     }
 }
 
 template <int KQ>
-__global__ void k_compact_anchors(TSView ts, const uint64_t *P0, WsDev w)
+__global__ void k_compact_anchors(TSView ts, QueryParams q, const uint64_t *P0, WsDev w)
 {
-    compact_anchors_body<KQ>(ts, P0, w, blockIdx.x, gridDim.x);
+    compact_anchors_body<KQ>(ts, q, P0, w, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tsg

@@ -36,7 +36,7 @@ struct ReplayEnc {
 // and parent before the first touch and after the transition); the counts
 // under every mutation of the span's trees for site statistics.  With EVAL
 // the replay publishes its completed trees in *s_ready every few trees.
-template <int W, int KQ, typename IdxT, bool EVAL>
+template <int W, int KQ, typename IdxT, bool EVAL, bool BLS = false>
 __device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams &q,
     const QueryDev &qd, const WsDev &w, const SpanState<IdxT> &sp, TouchEntry<KQ> *s_list,
     ReplayStage *s_stage, int *s_ready, int32_t t0, int32_t t1, int32_t Ls, const ReplayEnc code)
@@ -57,9 +57,33 @@ __device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams 
             const TouchEntry<KQ> en = s_list[i];
             const uint32_t pu = (uint32_t) sp.par[en.u] & PMASK;
             if (cursor + i < climit) {
-                item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0),
-                    st_load(sp, (int64_t) en.u), (int32_t) en.u, en.p0,
-                    pu != TSG_NO_PARENT ? (int32_t) pu : -1);
+                const Pack x1 = st_load(sp, (int64_t) en.u);
+                const int32_t p1 = pu != TSG_NO_PARENT ? (int32_t) pu : -1;
+                item_put<KQ>(items + cursor + i, item_pack<KQ>(en.x0), x1, (int32_t) en.u,
+                    en.p0, p1);
+                if (BLS) {
+                    // the item's branch lengths in the evaluation's
+                    // arithmetic: (bl1, bl0), or (bl1 - bl0, bl0) for FP64
+                    // integer summaries of an item whose counts did not
+                    // change
+                    const double tu = sp.time[en.u];
+                    const double bl0 = en.p0 >= 0 ? sp.time[en.p0] - tu : 0.0;
+                    const double bl1 = p1 >= 0 ? sp.time[p1] - tu : 0.0;
+                    bool same = en.x0[0] == x1.lo;
+                    if (KQ > 1) {
+                        same = same && en.x0[KQ > 1 ? 1 : 0] == x1.hi;
+                    }
+                    const int64_t at = cursor + i;
+                    if (q.f32) {
+                        float *bls = (float *) w.bl;
+                        bls[2 * at] = (float) bl1;
+                        bls[2 * at + 1] = (float) bl0;
+                    } else {
+                        double *bls = (double *) w.bl;
+                        bls[2 * at] = q.site_int && same ? bl1 - bl0 : bl1;
+                        bls[2 * at + 1] = bl0;
+                    }
+                }
             }
             sp.par[en.u] = (IdxT) pu;  // clears the touch flag
         }
@@ -363,45 +387,6 @@ __device__ __forceinline__ void eval_span_chunks(const TSView &ts, const QueryPa
         eval_chunk<F, UNPOL, W, KQ>(ts, q, w, c, lane,
             ts.span_time + ts.span_local_off[ts.chunk_span[c]]);
     }
-}
-
-// The item values after a replay that did not value its items (the compact
-// replay; the items carry the compact plan's local ids), in two kernels.
-//
-// k_item_bls, a warp per chunk and a lane per item: each item's branch
-// lengths in the evaluation's arithmetic, (bl1, bl0) -- in the integer form
-// (bl1 - bl0, bl0) for an item with the same counts before and after.
-template <typename F, int KQ>
-__device__ __forceinline__ void item_bls_body(const TSView &ts, const QueryParams &q, const WsDev &w,
-    const int64_t bid, const int64_t nb)
-{
-    const int lane = threadIdx.x & 31;
-    const Item<KQ> *items = (const Item<KQ> *) w.items;
-    const bool num_form = sizeof(F) == sizeof(double) && q.site_int;
-    F *bls = (F *) w.bl;
-    const int64_t nwarps = (int64_t) nb * (blockDim.x >> 5);
-    for (int64_t c = bid * (int64_t) (blockDim.x >> 5) + (threadIdx.x >> 5);
-         c < ts.num_chunks; c += nwarps) {
-        const double *time = ts.c_time + ts.c_local_off[ts.c_chunk_span[c]];
-        for (int64_t i = ts.chunk_begin[c] + lane; i < ts.chunk_end[c]; i += 32) {
-            const Item<KQ> it = items[i];
-            const double tu = time[it.u];
-            const double bl0 = it.p0 >= 0 ? time[it.p0] - tu : 0.0;
-            const double bl1 = it.p1 >= 0 ? time[it.p1] - tu : 0.0;
-            bool same = it.x0[0] == it.x1[0];
-            if (KQ > 1) {
-                same = same && it.x0[KQ > 1 ? 1 : 0] == it.x1[KQ > 1 ? 1 : 0];
-            }
-            bls[2 * i] = (F) (num_form && same ? bl1 - bl0 : bl1);
-            bls[2 * i + 1] = (F) bl0;
-        }
-    }
-}
-
-template <typename F, int KQ>
-__global__ void __launch_bounds__(256) k_item_bls(TSView ts, QueryParams q, WsDev w)
-{
-    item_bls_body<F, KQ>(ts, q, w, blockIdx.x, gridDim.x);
 }
 
 // A summary term's integer numerator with its type fixed at compile time

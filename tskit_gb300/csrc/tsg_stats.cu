@@ -1924,9 +1924,9 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 TSG_LAUNCHED();
                 const unsigned ga = (unsigned) grid_for(ts->v.c_num_anchors);
                 if (kq == 1) {
-                    k_compact_anchors<1><<<ga, 256, 0, sa>>>(ts->v, w.cp0, w);
+                    k_compact_anchors<1><<<ga, 256, 0, sa>>>(ts->v, p, w.cp0, w);
                 } else {
-                    k_compact_anchors<2><<<ga, 256, 0, sa>>>(ts->v, w.cp0, w);
+                    k_compact_anchors<2><<<ga, 256, 0, sa>>>(ts->v, p, w.cp0, w);
                 }
                 TSG_LAUNCHED();
                 if (forked_anchors) {
@@ -1961,7 +1961,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                     TSG_CUDA(cudaStreamWaitEvent(st, ws->ev[5], 0));
                 }
                 NvtxRange nvtx_eval("tsg.evaluate");
-                // two kernels: the items' branch lengths, then their values
+                // the items' values (the replay wrote their branch lengths)
                 if (p.f32) {
                     (p.polarised ? launch_eval_chunks_f32_pol : launch_eval_chunks_f32_unpol)(kq, st,
                         ts->v, p, w);
@@ -1969,7 +1969,6 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                     (p.polarised ? launch_eval_chunks_f64_pol : launch_eval_chunks_f64_unpol)(kq, st,
                         ts->v, p, w);
                 }
-                TSG_LAUNCHED();
                 TSG_LAUNCHED();
             }
         } else if (p.branch) {
@@ -2131,7 +2130,6 @@ static void batch_stage_blocks(const tsg_query_t *q, int64_t *nb)
         }
         const int64_t C = ts->v.num_chunks;
         const int64_t total = (C + TSG_EVAL_BLOCK - 1) / TSG_EVAL_BLOCK * p.gwpb;
-        nb[BS_BLS] = std::min<int64_t>((C + 7) / 8, 1 << 20);
         nb[BS_EVAL] = std::min<int64_t>((total + 7) / 8, 1 << 20);
         nb[BS_SPAN_WINDOWS] = (ts->v.num_segs + 7) / 8;
         nb[BS_LEAF_AREAS] = ts->v.num_edges > 0 ? grid_for(ts->v.num_edges) : 0;
@@ -2313,12 +2311,11 @@ int tsg_batch_launch(const tsg_batch_t *b, void *cuda_stream)
         if (g.branch) {
             if (g.f32) {
                 (g.pol ? launch_eval_chunks_batch_f32_pol : launch_eval_chunks_batch_f32_unpol)(
-                    g.kq, st, bq, nq, off(BS_BLS), g.blocks[BS_BLS], off(BS_EVAL), g.blocks[BS_EVAL]);
+                    g.kq, st, bq, nq, off(BS_EVAL), g.blocks[BS_EVAL]);
             } else {
                 (g.pol ? launch_eval_chunks_batch_f64_pol : launch_eval_chunks_batch_f64_unpol)(
-                    g.kq, st, bq, nq, off(BS_BLS), g.blocks[BS_BLS], off(BS_EVAL), g.blocks[BS_EVAL]);
+                    g.kq, st, bq, nq, off(BS_EVAL), g.blocks[BS_EVAL]);
             }
-            TSG_LAUNCHED();
             TSG_LAUNCHED();
             if (cudaGetLastError() != cudaSuccess) {
                 return TSG_ERR_CUDA;
