@@ -53,6 +53,14 @@ __global__ void __launch_bounds__(1024) kb_compact_prefix(const BatchQuery *bq, 
 }
 
 template <int KQ>
+__global__ void __launch_bounds__(TSG_ROWS_THREADS) kb_compact_rows(const BatchQuery *bq,
+    const int64_t *off, int nq)
+{
+    TSG_BATCH_QUERY();
+    compact_rows_body<KQ>(Q.v, Q.p, Q.d, Q.w, bid, nb);
+}
+
+template <int KQ>
 __global__ void __launch_bounds__(256) kb_compact_anchors(const BatchQuery *bq, const int64_t *off,
     int nq)
 {
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(256) kb_window_reduce(const BatchQuery *bq, co
 // indexes from `counter` (zeroed before the launch); span_off[b] is query
 // b's first global span.
 template <int KQ>
-__global__ void __launch_bounds__(TSG_COMPACT_THREADS) kb_replay_compact(const BatchQuery *bq,
+__global__ void __launch_bounds__(TSG_COMPACT_THREADS, 24) kb_replay_compact(const BatchQuery *bq,
     const int64_t *span_off, int nq, int32_t *counter)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,8 +144,8 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) kb_replay_compact(const B
         }
         const int b = batch_find(span_off, nq, g);
         const BatchQuery &Q = bq[b];
-        compact_span<KQ>(Q.v, Q.p, Q.d, Q.w, (int) (g - span_off[b]), smem_raw, sh.list, sh.stage,
-            sh.seek.pre, sh.wsum, sh.seek.mask);
+        compact_span<KQ>(Q.v, Q.p, Q.d, Q.w, (int) (g - span_off[b]), smem_raw, sh.list,
+            sh.stage);
     }
 }
 
@@ -179,6 +187,13 @@ int batch_launch_stage(int stage, int kq, int64_t blocks, cudaStream_t st, const
                 kb_compact_anchors<1><<<g, 256, 0, st>>>(bq, off, nq);
             } else {
                 kb_compact_anchors<2><<<g, 256, 0, st>>>(bq, off, nq);
+            }
+            break;
+        case BS_ROWS:
+            if (kq == 1) {
+                kb_compact_rows<1><<<g, TSG_ROWS_THREADS, 0, st>>>(bq, off, nq);
+            } else {
+                kb_compact_rows<2><<<g, TSG_ROWS_THREADS, 0, st>>>(bq, off, nq);
             }
             break;
         case BS_SPAN_WINDOWS: kb_span_windows<<<g, 256, 0, st>>>(bq, off, nq); break;

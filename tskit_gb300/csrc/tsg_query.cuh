@@ -84,6 +84,12 @@ struct WsDev {
     unsigned long long *site_acc;  // windows x R x 2: exact site-sum counters (integer form)
     uint64_t *cp0;        // (samples + 1) x 2: prefix sums along the first span's order
                           // (compact replay)
+    // the compact spans' depth-first orders in rows of 32 positions: per
+    // span and row, 4 x KQ membership words (bit i: the row's i-th sample
+    // is in set k) and the KQ packed counts before the row (the row after
+    // the last holds the span's totals)
+    uint32_t *c_bits;
+    uint64_t *c_rowpre;
     int32_t *err;
     int32_t *counter;
 };
@@ -285,7 +291,7 @@ TSG_CHUNK_EVAL_BATCH_LAUNCHER(launch_eval_chunks_batch_f64_unpol);
 enum BatchStage {
     BS_ZERO, BS_NODE_MASK, BS_PREFIX, BS_ANCHORS, BS_EVAL, BS_SPAN_WINDOWS,
     BS_LEAF_AREAS, BS_LEAF_PREFIX, BS_LEAF_TERMS, BS_SITE_SUMS, BS_SITE_FINISH, BS_SPAN_SCAN,
-    BS_REDUCE, BS_COUNT
+    BS_REDUCE, BS_ROWS, BS_COUNT
 };
 int batch_launch_stage(int stage, int kq, int64_t blocks, cudaStream_t st, const BatchQuery *bq,
     int nq, const int64_t *off);

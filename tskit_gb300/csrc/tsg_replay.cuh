@@ -69,6 +69,13 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// A hint to bring the global-memory line holding p into L2 (no data
+// returned, no register held); p must lie inside an allocation.
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
 // One tree's replay inputs, staged in shared memory ahead of use: the edge
 // events into the tree, its mutations, its item range, and the first 32
 // event encodings, mutation encodings and leaf sample-set masks of each.

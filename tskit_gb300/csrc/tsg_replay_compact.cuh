@@ -4,11 +4,13 @@
 // 16-bit parent entries) in shared memory: a few kilobytes, so about twenty
 // blocks -- twenty sequential replays -- run on every SM.
 //
-//   seek     the prefix sum of the sample-set bits along the span's
-//            depth-first sample order, TSG_SEEK_PER samples per lane and
-//            step (warp shuffles), the next step's loads in flight, and at
-//            each sorted range endpoint a node's count: P[hi] - P[lo] (the
-//            start is stored first, the end then subtracts it);
+//   rows     (k_compact_rows, before the replay, every span at once) each
+//            span's depth-first sample order in rows of 32 positions: per
+//            row a membership word per set (ballots) and the packed counts
+//            before the row (prefix sums of population counts);
+//   seek     at each of the span's sorted range endpoints a node's count,
+//            P[hi] - P[lo], P read from the rows in O(1) (the start is
+//            stored first, the end then subtracts it);
 //   replay   replay_span over the compact encodings.
 //
 // The first tree's items (its stateful nodes, the anchors) are written by
@@ -24,144 +26,181 @@ namespace tsg {
 
 #define TSG_COMPACT_THREADS 32
 
-// samples per thread in one step of the seek
-#define TSG_SEEK_PER 4
-
-// Counts of span s's compact nodes at the span start into sp.xq.  The seek
-// takes TSG_COMPACT_THREADS x TSG_SEEK_PER samples of the span's order per
-// step, each thread TSG_SEEK_PER consecutive ones, and loads the next step's
-// order entries and sample masks while it scans the current one.  s_pre:
-// (TSG_COMPACT_THREADS + 1) x 2 words, each thread's exclusive prefix (and
-// the step's total); s_mask: the step's masks; s_wsum: 2 words per warp.
-// Ends with the block synchronised.
-template <int KQ>
-__device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &qd, int K, int s,
-    const SpanState<uint16_t> &sp, uint64_t *s_pre, uint64_t *s_wsum, uint32_t *s_mask)
+// rows of 32 positions of a compact span's depth-first sample order, plus
+// the row holding the span's totals (k_compact_rows)
+__host__ __device__ __forceinline__ int64_t compact_row_stride(int64_t n)
 {
-    constexpr int T = TSG_COMPACT_THREADS, PER = TSG_SEEK_PER, STEP = T * PER;
-    constexpr int NW = T / 32;
+    return (n + 31) / 32 + 1;
+}
+
+#define TSG_ROWS_THREADS 256
+// rows a warp of k_compact_rows loads at once
+#define TSG_ROWS_BATCH 8
+
+// The rows of compact span s's order (one block of TSG_ROWS_THREADS per span
+// at a time, a lane per position): warp w takes rows w, w + 8, ... --
+// TSG_ROWS_BATCH of them per round, their order entries and then their
+// sample masks loaded together -- and ballots each set's membership bits
+// into a 32-bit word (4 x KQ words per row, w.c_bits) whose population
+// counts give the row's packed counts; then warp 0 turns the counts (held in
+// w.c_rowpre) into exclusive prefix sums in row order, the row after the
+// last taking the span's totals.  Counts fit their 16-bit fields (at most
+// the set sizes), so packed words add without carries.
+template <int KQ>
+__device__ __forceinline__ void compact_rows_body(const TSView &ts, const QueryParams &q,
+    const QueryDev &qd, const WsDev &w, const int64_t bid, const int64_t nb)
+{
+    constexpr int NW = TSG_ROWS_THREADS / 32, RB = TSG_ROWS_BATCH, KW = 4 * KQ;
     const int64_t n = ts.num_samples;
-    const uint16_t *order = ts.c_order + (int64_t) s * n;
+    const int64_t nrows = (n + 31) / 32, stride = compact_row_stride(n);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int K = q.K;
+    for (int64_t s = bid; s < ts.c_num_spans; s += nb) {
+        const uint16_t *order = ts.c_order + s * n;
+        uint32_t *bits = w.c_bits + s * stride * KW;
+        uint64_t *pre = w.c_rowpre + s * stride * KQ;
+        for (int64_t r0 = wid; r0 < nrows; r0 += (int64_t) NW * RB) {
+            uint32_t m[RB];
+#pragma unroll
+            for (int b = 0; b < RB; b++) {
+                const int64_t i = (r0 + (int64_t) b * NW) * 32 + lane;
+                m[b] = i < n ? (uint32_t) order[i] : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int b = 0; b < RB; b++) {
+                m[b] = m[b] != 0xFFFFFFFFu ? qd.sample_mask[m[b]] : 0u;
+            }
+#pragma unroll
+            for (int b = 0; b < RB; b++) {
+                const int64_t r = r0 + (int64_t) b * NW;
+                if (r >= nrows) {
+                    break;
+                }
+                uint64_t c[KQ];
+#pragma unroll
+                for (int h = 0; h < KQ; h++) {
+                    c[h] = 0;
+                }
+#pragma unroll
+                for (int k = 0; k < KW; k++) {
+                    const uint32_t word = __ballot_sync(0xffffffffu, k < K && ((m[b] >> k) & 1u));
+                    if (lane == k) {
+                        bits[r * KW + k] = word;
+                    }
+                    c[k / 4] += (uint64_t) __popc(word) << (16 * (k % 4));
+                }
+                if (lane == 0) {
+#pragma unroll
+                    for (int h = 0; h < KQ; h++) {
+                        pre[r * KQ + h] = c[h];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (wid == 0) {
+            uint64_t run[KQ];
+#pragma unroll
+            for (int h = 0; h < KQ; h++) {
+                run[h] = 0;
+            }
+            for (int64_t r0 = 0; r0 < nrows; r0 += 32) {
+                const int64_t r = r0 + lane;
+#pragma unroll
+                for (int h = 0; h < KQ; h++) {
+                    const uint64_t v = r < nrows ? pre[r * KQ + h] : 0ull;
+                    uint64_t inc = v;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint64_t a = __shfl_up_sync(0xffffffffu, inc, o);
+                        if (lane >= o) {
+                            inc += a;
+                        }
+                    }
+                    if (r < nrows) {
+                        pre[r * KQ + h] = run[h] + inc - v;
+                    }
+                    run[h] += __shfl_sync(0xffffffffu, inc, 31);
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int h = 0; h < KQ; h++) {
+                    pre[nrows * KQ + h] = run[h];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(TSG_ROWS_THREADS) k_compact_rows(TSView ts, QueryParams q,
+    QueryDev qd, WsDev w)
+{
+    compact_rows_body<KQ>(ts, q, qd, w, blockIdx.x, gridDim.x);
+}
+
+// Counts of span s's compact nodes at the span start into sp.xq, from the
+// span's rows (k_compact_rows): the members before depth-first position x
+// are the prefix of x's row plus, per set, the population count of the
+// row's membership word below x.  The span's range endpoints, sorted, are
+// taken TSG_COMPACT_THREADS at a time, a thread each; a node's start count
+// is stored first and its end then subtracts it.  Ends with the block
+// synchronised.
+template <int KQ>
+__device__ __forceinline__ void compact_seek(const TSView &ts, const WsDev &w, int s,
+    const SpanState<uint16_t> &sp)
+{
+    constexpr int T = TSG_COMPACT_THREADS, KW = 4 * KQ;
+    const int64_t stride = compact_row_stride(ts.num_samples);
+    const uint32_t *bits = w.c_bits + (int64_t) s * stride * KW;
+    const uint64_t *pre = w.c_rowpre + (int64_t) s * stride * KQ;
     const int2 *ep = ts.c_ep + ts.c_ep_off[s];
     const int64_t nep = ts.c_ep_off[s + 1] - ts.c_ep_off[s];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint32_t cur_m[PER], nxt_m[PER];
-    auto fetch = [&](int64_t base, uint32_t (&mm)[PER]) {
-        uint32_t o[PER];
+    const int tid = threadIdx.x;
+    for (int64_t j0 = 0; j0 < nep; j0 += T) {
+        const int64_t j = j0 + tid;
+        const bool act = j < nep;
+        int2 e = make_int2(0, 0);
+        uint64_t p[KQ];
 #pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int64_t i = base + (int64_t) tid * PER + j;
-            o[j] = i < n ? (uint32_t) order[i] : 0u;
+        for (int h = 0; h < KQ; h++) {
+            p[h] = 0;
         }
+        if (act) {
+            e = ep[j];
+            const int64_t row = e.x >> 5;
+            const uint32_t below = (1u << (e.x & 31)) - 1u;
 #pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int64_t i = base + (int64_t) tid * PER + j;
-            mm[j] = i < n ? qd.sample_mask[o[j]] : 0u;
-        }
-    };
-    fetch(0, cur_m);
-    uint64_t run_lo = 0, run_hi = 0;
-    int64_t cur = 0;
-    for (int64_t base = 0; base < n; base += STEP) {
-        if (base + STEP < n) {
-            fetch(base + STEP, nxt_m);
-        }
-        uint64_t t_lo = 0, t_hi = 0;
-#pragma unroll
-        for (int j = 0; j < PER; j++) {
-            s_mask[tid * PER + j] = cur_m[j];
-            const Pack v = pk_from_mask<16>(cur_m[j], K);
-            t_lo += v.lo;
-            t_hi += v.hi;
-        }
-        // inclusive scan of the threads' totals within the warp (fields
-        // never carry: prefix counts stay within the set sizes)
-        uint64_t inc_lo = t_lo, inc_hi = t_hi;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t a = __shfl_up_sync(0xffffffffu, inc_lo, o);
-            const uint64_t b = KQ > 1 ? __shfl_up_sync(0xffffffffu, inc_hi, o) : 0ull;
-            if (lane >= o) {
-                inc_lo += a;
-                inc_hi += b;
+            for (int h = 0; h < KQ; h++) {
+                p[h] = pre[row * KQ + h];
             }
-        }
-        if (lane == 31) {
-            s_wsum[2 * wid] = inc_lo;
-            s_wsum[2 * wid + 1] = inc_hi;
-        }
-        __syncthreads();
-        uint64_t wp_lo = 0, wp_hi = 0, tot_lo = 0, tot_hi = 0;
+            if (below != 0) {
 #pragma unroll
-        for (int j = 0; j < NW; j++) {
-            const uint64_t a = s_wsum[2 * j], b = s_wsum[2 * j + 1];
-            if (j < wid) {
-                wp_lo += a;
-                wp_hi += b;
-            }
-            tot_lo += a;
-            tot_hi += b;
-        }
-        // P at position base + tid * PER (the samples before it)
-        s_pre[2 * tid] = run_lo + wp_lo + inc_lo - t_lo;
-        s_pre[2 * tid + 1] = run_hi + wp_hi + inc_hi - t_hi;
-        if (tid == 0) {
-            s_pre[2 * T] = run_lo + tot_lo;
-            s_pre[2 * T + 1] = run_hi + tot_hi;
-        }
-        __syncthreads();
-        // every endpoint at a position up to base + STEP (the sorted list's
-        // next entries; earlier positions were taken by earlier steps):
-        // P there is its thread's prefix plus the masks before it
-        const int64_t lim = base + STEP;
-        for (;;) {
-            const int64_t j = cur + tid;
-            int2 e = make_int2(0, 0);
-            bool mine = false;
-            if (j < nep) {
-                e = ep[j];
-                mine = e.x <= lim;
-            }
-            const int cnt = __syncthreads_count(mine);
-            const int64_t l = e.y >> 1;
-            uint64_t p_lo = 0, p_hi = 0;
-            if (mine) {
-                const int at = (int) (e.x - base);
-                const int tt = at / PER, jj = at - tt * PER;
-                p_lo = s_pre[2 * tt];
-                p_hi = s_pre[2 * tt + 1];
-                for (int q = 0; q < jj; q++) {
-                    const Pack v = pk_from_mask<16>(s_mask[tt * PER + q], K);
-                    p_lo += v.lo;
-                    p_hi += v.hi;
+                for (int h = 0; h < KQ; h++) {
+                    const uint4 b = *(const uint4 *) (bits + row * KW + 4 * h);
+                    p[h] += (uint64_t) __popc(b.x & below) + ((uint64_t) __popc(b.y & below) << 16)
+                        + ((uint64_t) __popc(b.z & below) << 32)
+                        + ((uint64_t) __popc(b.w & below) << 48);
                 }
             }
-            if (mine && !(e.y & 1)) {
-                sp.xq[l * KQ] = p_lo;
-                if (KQ > 1) {
-                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = p_hi;
-                }
-            }
-            __syncthreads();
-            if (mine && (e.y & 1)) {
-                sp.xq[l * KQ] = p_lo - sp.xq[l * KQ];
-                if (KQ > 1) {
-                    sp.xq[l * KQ + (KQ > 1 ? 1 : 0)] = p_hi - sp.xq[l * KQ + (KQ > 1 ? 1 : 0)];
-                }
-            }
-            cur += cnt;
-            if (cnt < T) {
-                break;
-            }
-            __syncthreads();
         }
-        run_lo = s_pre[2 * T];
-        run_hi = s_pre[2 * T + 1];
-        __syncthreads();
+        const int64_t l = e.y >> 1;
+        if (act && !(e.y & 1)) {
 #pragma unroll
-        for (int j = 0; j < PER; j++) {
-            cur_m[j] = nxt_m[j];
+            for (int h = 0; h < KQ; h++) {
+                sp.xq[l * KQ + h] = p[h];
+            }
         }
+        __syncthreads();
+        if (act && (e.y & 1)) {
+#pragma unroll
+            for (int h = 0; h < KQ; h++) {
+                sp.xq[l * KQ + h] = p[h] - sp.xq[l * KQ + h];
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -171,8 +210,7 @@ __device__ __forceinline__ void compact_seek(const TSView &ts, const QueryDev &q
 template <int KQ>
 __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams &q,
     const QueryDev &qd, const WsDev &w, int s, unsigned char *smem_raw,
-    TouchEntry<KQ> *s_list, ReplayStage *s_stage, uint64_t *s_pre, uint64_t *s_wsum,
-    uint32_t *s_mask)
+    TouchEntry<KQ> *s_list, ReplayStage *s_stage)
 {
     SpanState<uint16_t> sp = span_state_at<uint16_t>(smem_raw, ts.c_max_local, KQ);
     sp.cnt = nullptr;
@@ -185,7 +223,7 @@ __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams
     for (int32_t l = threadIdx.x; l < Ls; l += blockDim.x) {
         sp.par[l] = ts.c_par0[lo + l];
     }
-    compact_seek<KQ>(ts, qd, q.K, s, sp, s_pre, s_wsum, s_mask);
+    compact_seek<KQ>(ts, w, s, sp);
     if (threadIdx.x < 32) {
         replay_span<16, KQ, uint16_t, false, true>(ts, q, qd, w, sp, s_list, s_stage, nullptr, t0,
             t1, Ls, ReplayEnc{ts.c_rem_enc, ts.c_ins_enc, ts.c_mut_enc});
@@ -193,25 +231,16 @@ __device__ __forceinline__ void compact_span(const TSView &ts, const QueryParams
     __syncthreads();
 }
 
-// The block-shared arrays of the compact replay besides the span state
-// (the seek's scratch and the replay's staging ring are never live at the
-// same time: they share their bytes).
+// The block-shared arrays of the compact replay besides the span state.
 template <int KQ>
 struct CompactShared {
     TouchEntry<KQ> list[TSG_TOUCH_CAP];  // the open touch list
-    union {
-        ReplayStage stage[4];            // prefetch ring, trees t .. t + 3
-        struct {
-            uint64_t pre[2 * (TSG_COMPACT_THREADS + 1)];
-            uint32_t mask[TSG_COMPACT_THREADS * TSG_SEEK_PER];
-        } seek;
-    };
-    uint64_t wsum[2 * (TSG_COMPACT_THREADS / 32)];
+    ReplayStage stage[4];                // prefetch ring, trees t .. t + 3
 };
 
 // Persistent blocks take spans from the query's counter until none is left.
 template <int KQ>
-__global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView ts, QueryParams q,
+__global__ void __launch_bounds__(TSG_COMPACT_THREADS, 24) k_replay_compact(TSView ts, QueryParams q,
     QueryDev qd, WsDev w)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -227,8 +256,7 @@ __global__ void __launch_bounds__(TSG_COMPACT_THREADS) k_replay_compact(TSView t
         if (s >= ts.c_num_spans) {
             break;
         }
-        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage, sh.seek.pre, sh.wsum,
-            sh.seek.mask);
+        compact_span<KQ>(ts, q, qd, w, s, smem_raw, sh.list, sh.stage);
     }
 }
 

@@ -469,6 +469,13 @@ static void *compact_kernel(int KQ)
     return KQ == 1 ? (void *) k_replay_compact<1> : (void *) k_replay_compact<2>;
 }
 
+// rows of the compact spans' order arrays (k_compact_rows) per span
+static int64_t compact_rows(const tsg_treeseq_t *ts)
+{
+    return compact_row_stride(ts->v.num_samples);
+}
+
+
 // bytes of one span's node state: packed counts and parent ids (node times
 // come from the span plan, seek counters from per-CTA scratch)
 static int64_t span_state_bytes(int64_t L, int W, int KQ)
@@ -518,6 +525,8 @@ struct tsg_query {
     bool smem;               // item pipeline (either form); else the general sweep
     bool gstate;             // item pipeline with node state in global memory
     bool compact_ok;         // the compact replay serves when the tree sequence has its plan
+    int64_t c_rows_cap;      // compact spans the workspace's row arrays hold (the plan's
+                             // span count when the query was prepared)
     int W, KQ;               // count field width, 64-bit count words per node
     int64_t smem_bytes, smem_grid, slot_bytes;
     int span_normalise;
@@ -536,6 +545,14 @@ struct tsg_query {
 #define TSG_KIND_MATVEC 2
 
 namespace tsg {
+
+// whether the compact replay serves a launch of q: the tree sequence has a
+// compact plan and q's row arrays hold its spans (a plan rebuilt with more
+// spans after q was prepared leaves q on the general replay)
+static bool compact_serves(const tsg_query_t *q)
+{
+    return q->compact_ok && q->ts->v.c_num_spans > 0 && q->ts->v.c_num_spans <= q->c_rows_cap;
+}
 
 // Check the sample sets (c/tskit/trees.c:2114-2149 and the duplicate check of
 // 2174-2220) and build per-sample membership masks.
@@ -1044,6 +1061,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         q->num_slots = 0;
     }
     q->compact_ok = q->smem && !q->gstate && q->W == 16 && q->KQ <= 2;
+    q->c_rows_cap = q->compact_ok ? ts->v.c_num_spans : 0;
     if (q->compact_ok) {
         void *fn = compact_kernel(q->KQ);
         allow_max_dynamic_smem(fn);
@@ -1075,6 +1093,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * 8, 256);          // leaf_dbl
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // leaf_win
         bytes += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256); // cp0
+        bytes += align_up(q->c_rows_cap * compact_rows(ts) * 16 * KQ, 256);     // c_bits
+        bytes += align_up(q->c_rows_cap * compact_rows(ts) * 8 * KQ, 256);      // c_rowpre
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -1613,6 +1633,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.site_val = nullptr;
     w.site_win = nullptr;
     w.cp0 = nullptr;
+    w.c_bits = nullptr;
+    w.c_rowpre = nullptr;
     w.site_acc = nullptr;
     if (q->smem) {
         const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
@@ -1644,6 +1666,10 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up((int64_t) p.Wn * R * 8, 256);
         w.cp0 = (uint64_t *) (b + off);
         off += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256);
+        w.c_bits = (uint32_t *) (b + off);
+        off += align_up(q->c_rows_cap * compact_rows(ts) * 16 * q->KQ, 256);
+        w.c_rowpre = (uint64_t *) (b + off);
+        off += align_up(q->c_rows_cap * compact_rows(ts) * 8 * q->KQ, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
@@ -1875,15 +1901,31 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
     if (q->smem) {
         k_node_mask<<<grid_for(N), 256, 0, st>>>(ts->v, d, w.node_mask);
         TSG_LAUNCHED();
-        if (fork && p.branch) {
-            TSG_CUDA(cudaEventRecord(ws->ev[0], st));
-            TSG_CUDA(cudaStreamWaitEvent(ws->aux[0], ws->ev[0], 0));
-            int r = leaf_stage(ws->aux[0]);
+        // the leaves' stage on side stream 0 from this point of the main
+        // stream: right after the node masks for the general replay; after
+        // the order rows for the compact one, so that the replay's blocks,
+        // launched first, are spread over every SM before the leaves' blocks
+        // take some
+        auto fork_leaf = [&](bool record) -> int {
+            if (fork && p.branch) {
+                if (record) {
+                    TSG_CUDA(cudaEventRecord(ws->ev[0], st));
+                }
+                TSG_CUDA(cudaStreamWaitEvent(ws->aux[0], ws->ev[0], 0));
+                int r = leaf_stage(ws->aux[0]);
+                if (r != 0) {
+                    return r;
+                }
+                TSG_CUDA(cudaEventRecord(ws->ev[1], ws->aux[0]));
+                forked_leaf = true;
+            }
+            return 0;
+        };
+        if (!compact_serves(q)) {
+            int r = fork_leaf(true);
             if (r != 0) {
                 return r;
             }
-            TSG_CUDA(cudaEventRecord(ws->ev[1], ws->aux[0]));
-            forked_leaf = true;
         }
         const unsigned g = (unsigned) q->smem_grid;
         const size_t sb = (size_t) q->smem_bytes;
@@ -1900,21 +1942,24 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             }
             return 0;
         };
-        if (q->compact_ok && ts->v.c_num_spans > 0) {
-            // the compact replay: the first tree's items, one block per span
-            // at a time, then every chunk's item values
+        if (compact_serves(q)) {
+            // the compact replay: every span's order rows, then one block per
+            // span at a time (seek and replay); the first tree's items and
+            // the leaves' stage beside it on the side streams, forked after
+            // the rows and submitted after the replay so that the replay's
+            // blocks are spread over every SM first; then every chunk's item
+            // values
             const int kq = q->KQ;
-            bool forked_anchors = false;
-            if (p.branch && ts->v.c_num_anchors > 0) {
-                // the first tree's items are read only by the evaluation:
-                // on a side stream beside the replay when there is one
-                cudaStream_t sa = st;
-                if (fork) {
-                    TSG_CUDA(cudaEventRecord(ws->ev[4], st));
-                    TSG_CUDA(cudaStreamWaitEvent(ws->aux[1], ws->ev[4], 0));
-                    sa = ws->aux[1];
-                    forked_anchors = true;
-                }
+            const unsigned gr = (unsigned) std::min<int64_t>(ts->v.c_num_spans, 1 << 20);
+            if (kq == 1) {
+                k_compact_rows<1><<<gr, TSG_ROWS_THREADS, 0, st>>>(ts->v, p, d, w);
+            } else {
+                k_compact_rows<2><<<gr, TSG_ROWS_THREADS, 0, st>>>(ts->v, p, d, w);
+            }
+            TSG_LAUNCHED();
+            const bool anchors = p.branch && ts->v.c_num_anchors > 0;
+            // the first tree's items are read only by the evaluation
+            auto anchor_stage = [&](cudaStream_t sa) -> int {
                 const unsigned gp = (unsigned) ((ts->v.num_samples + 1023) / 1024);
                 if (kq == 1) {
                     k_compact_prefix<1><<<gp, 1024, 0, sa>>>(ts->v, p, d, w.cp0);
@@ -1929,9 +1974,13 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                     k_compact_anchors<2><<<ga, 256, 0, sa>>>(ts->v, p, w.cp0, w);
                 }
                 TSG_LAUNCHED();
-                if (forked_anchors) {
-                    TSG_CUDA(cudaEventRecord(ws->ev[5], ws->aux[1]));
-                }
+                return 0;
+            };
+            bool forked_anchors = false;
+            if (fork) {
+                TSG_CUDA(cudaEventRecord(ws->ev[0], st));
+            } else if (anchors) {
+                anchor_stage(st);
             }
             const size_t csb = (size_t) align_up(replay_state_bytes(ts->v.c_max_local, 16, kq), 16);
             void *fn = compact_kernel(kq);
@@ -1947,6 +1996,18 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
                 k_replay_compact<1><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
             } else {
                 k_replay_compact<2><<<cg, TSG_COMPACT_THREADS, csb, st>>>(ts->v, p, d, w);
+            }
+            if (fork) {
+                int r = fork_leaf(false);
+                if (r != 0) {
+                    return r;
+                }
+                if (anchors) {
+                    TSG_CUDA(cudaStreamWaitEvent(ws->aux[1], ws->ev[0], 0));
+                    anchor_stage(ws->aux[1]);
+                    TSG_CUDA(cudaEventRecord(ws->ev[5], ws->aux[1]));
+                    forked_anchors = true;
+                }
             }
             if (q->ev_rstop != nullptr) {
                 TSG_CUDA(cudaEventRecord(q->ev_rstop, st));
@@ -2106,7 +2167,7 @@ namespace tsg {
 static bool batch_fusable(const tsg_query_t *q)
 {
     const tsg_treeseq_t *ts = q->ts;
-    return q->kind == TSG_KIND_STATS && q->smem && q->compact_ok && ts->v.c_num_spans > 0
+    return q->kind == TSG_KIND_STATS && q->smem && compact_serves(q)
         && q->W == 16 && (!q->p.site || (q->p.site_int && ts->v.num_sites > 0));
 }
 
@@ -2123,6 +2184,7 @@ static void batch_stage_blocks(const tsg_query_t *q, int64_t *nb)
     const int64_t site = p.site && p.site_int ? (int64_t) p.Wn * R * 2 : 0;
     nb[BS_ZERO] = std::min<int64_t>((1 + R + leaf + site + 255) / 256, 4096);
     nb[BS_NODE_MASK] = grid_for(ts->v.num_nodes);
+    nb[BS_ROWS] = std::min<int64_t>(ts->v.c_num_spans, 1 << 20);
     if (p.branch) {
         if (ts->v.c_num_anchors > 0) {
             nb[BS_PREFIX] = (ts->v.num_samples + 1023) / 1024;
@@ -2295,7 +2357,8 @@ int tsg_batch_launch(const tsg_batch_t *b, void *cuda_stream)
         int ret = 0;
         TSG_CUDA(cudaMemsetAsync(g.counter, 0, sizeof(int32_t), st));
         if ((ret = stage(BS_ZERO)) != 0 || (ret = stage(BS_NODE_MASK)) != 0
-            || (ret = stage(BS_PREFIX)) != 0 || (ret = stage(BS_ANCHORS)) != 0) {
+            || (ret = stage(BS_PREFIX)) != 0 || (ret = stage(BS_ANCHORS)) != 0
+            || (ret = stage(BS_ROWS)) != 0) {
             return ret;
         }
         const size_t csb = (size_t) align_up(replay_state_bytes(g.max_local, 16, g.kq), 16);
