@@ -107,25 +107,25 @@ class FakeCompactTS:
 
 
 def test_compact_candidates():
-    assert tune.compact_candidates(1000, 10_000) == [500, 1000, 1250, 1500, 2000, 4000]
-    assert tune.compact_candidates(1000, 1500) == [500, 1000, 1250, 1500]
+    assert tune.compact_candidates(1000, 10_000) == [500, 750, 1000, 1250, 1500, 2000]
+    assert tune.compact_candidates(1000, 1300) == [500, 750, 1000, 1250, 1300]
 
 
 def test_tune_compact_picks_fastest_and_skips_unbuildable():
-    ts = FakeCompactTS(cap=2500)
-    ms = {1000: 2.0, 500: 2.5, 1250: 1.8, 1500: 1.7, 2000: 1.5}
+    ts = FakeCompactTS(cap=1800)
+    ms = {1000: 2.0, 500: 2.5, 750: 2.2, 1250: 1.8, 1500: 1.7}
     timer, calls = fake_timer(ms)
     rep = tune.tune_compact_spans(ts, lambda t: (lambda: t.num_compact_spans), timer=timer)
-    assert rep["num_spans"] == 2000 and ts.num_compact_spans == 2000
-    assert rep["ms"] == ms          # 4000 spans could not be built: not timed
+    assert rep["num_spans"] == 1500 and ts.num_compact_spans == 1500
+    assert rep["ms"] == ms          # 2000 spans could not be built: not timed
     assert calls[0] == 1000         # the default plan first
     cache = {}
-    timer2, _ = fake_timer({**ms, 2500: 1.9})
+    timer2, _ = fake_timer({**ms, 1125: 1.9})
     tune.tune_compact_spans(ts, lambda t: (lambda: t.num_compact_spans), timer=timer2,
                             cache=cache)
-    ts2 = FakeCompactTS(cap=2500)
+    ts2 = FakeCompactTS(cap=1800)
     rep2 = tune.tune_compact_spans(ts2, lambda t: (lambda: 0), cache=cache)
-    assert rep2["cached"] and ts2.num_compact_spans == 2000
+    assert rep2["cached"] and ts2.num_compact_spans == 1500
 
 
 def test_tune_compact_without_plan():

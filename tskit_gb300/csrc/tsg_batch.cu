@@ -53,11 +53,12 @@ __global__ void __launch_bounds__(1024) kb_compact_prefix(const BatchQuery *bq, 
 }
 
 template <int KQ>
-__global__ void __launch_bounds__(TSG_ROWS_THREADS) kb_compact_rows(const BatchQuery *bq,
+__global__ void __launch_bounds__(TSG_ROWS_THREADS, 8) kb_compact_rows(const BatchQuery *bq,
     const int64_t *off, int nq)
 {
+    __shared__ RowsWarp<KQ> sh[TSG_ROWS_THREADS / 32];
     TSG_BATCH_QUERY();
-    compact_rows_body<KQ>(Q.v, Q.p, Q.d, Q.w, bid, nb);
+    compact_rows_body<KQ>(Q.v, Q.p, Q.d, Q.w, sh, bid, nb);
 }
 
 template <int KQ>
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256) kb_window_reduce(const BatchQuery *bq, co
 // indexes from `counter` (zeroed before the launch); span_off[b] is query
 // b's first global span.
 template <int KQ>
-__global__ void __launch_bounds__(TSG_COMPACT_THREADS, 24) kb_replay_compact(const BatchQuery *bq,
+__global__ void __launch_bounds__(TSG_COMPACT_THREADS, 20) kb_replay_compact(const BatchQuery *bq,
     const int64_t *span_off, int nq, int32_t *counter)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

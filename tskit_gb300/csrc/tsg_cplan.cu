@@ -134,9 +134,9 @@ int64_t compact_default_spans(int64_t T, int64_t events, int64_t n)
     if (n <= 0 || n > 65535 || T <= 1) {
         return 0;
     }
-    // about 384 edge events per span (a few hundred touched nodes), and at
+    // about 256 edge events per span (a few hundred touched nodes), and at
     // most 2^26 sample-order entries in all
-    int64_t NC = std::max<int64_t>(1, events / 384);
+    int64_t NC = std::max<int64_t>(1, events / 256);
     NC = std::min<int64_t>(NC, std::max<int64_t>(1, ((int64_t) 1 << 26) / n));
     return std::min<int64_t>(NC, T);
 }
@@ -186,7 +186,10 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     }
 
     std::vector<SpanOut> out((size_t) NC);
-    std::vector<uint16_t> order((size_t) (NC * n));
+    // each span's order padded to a multiple of 8 entries (16 bytes), so that
+    // every span's starts 16-byte aligned
+    const int64_t nst = compact_order_stride(n);
+    std::vector<uint16_t> order((size_t) (NC * nst), 0);
     std::vector<int2> ins_enc((size_t) E, make_int2(0, 0)), rem_enc((size_t) E, make_int2(0, 0));
     std::vector<int32_t> mut_enc((size_t) M, 0);
     // the first tree's sample ranges (anchors), from the first span's order
@@ -227,7 +230,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
                 const int32_t t0 = st[(size_t) s], t1 = st[(size_t) s + 1];
                 SpanOut &o = out[(size_t) s];
                 // depth-first sample order of the tree at the span start
-                uint16_t *ord = order.data() + s * n;
+                uint16_t *ord = order.data() + s * nst;
                 int32_t pos = 0;
                 for (int32_t r = f.rhead; r >= 0; r = f.rnext[(size_t) r]) {
                     int32_t u = r;
@@ -426,6 +429,22 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     for (size_t k = 0; k < a_l2g.size(); k++) {
         time[(size_t) local_off[(size_t) NC] + k] = h.node_time[(size_t) a_l2g[k]];
     }
+    // per span and chunk of order rows, its first endpoint (the endpoints
+    // are sorted by position, so each chunk's are consecutive)
+    const int64_t CH = compact_row_chunks(n);
+    std::vector<int32_t> ep_chunk((size_t) (NC * (CH + 1)));
+    for (int64_t s = 0; s < NC; s++) {
+        const std::vector<int2> &e = out[(size_t) s].ep;
+        int32_t *row = ep_chunk.data() + s * (CH + 1);
+        int64_t j = 0;
+        for (int64_t c = 0; c < CH; c++) {
+            while (j < (int64_t) e.size() && compact_chunk_of(e[(size_t) j].x, n) < c) {
+                j++;
+            }
+            row[c] = (int32_t) j;
+        }
+        row[CH] = (int32_t) e.size();
+    }
     // the numbering of each evaluation chunk's items: the anchors for the
     // first tree, else the span replaying the transition into the tree
     const std::vector<int64_t> &tco = ts->h_tree_chunk_off;
@@ -451,7 +470,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
 
     int ret;
     std::vector<void *> &own = ts->compact_owned;
-    int32_t *d_st, *d_mut_enc, *d_chunk_span, *d_apar, *d_chunk_order;
+    int32_t *d_st, *d_mut_enc, *d_chunk_span, *d_apar, *d_chunk_order, *d_ep_chunk;
     int64_t *d_local_off, *d_ep_off;
     double *d_time;
     uint16_t *d_par0, *d_order;
@@ -459,6 +478,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     if ((ret = upload_host_vec(own, st, &d_st)) || (ret = upload_host_vec(own, local_off, &d_local_off))
         || (ret = upload_host_vec(own, time, &d_time)) || (ret = upload_host_vec(own, par0, &d_par0))
         || (ret = upload_host_vec(own, ep_off, &d_ep_off)) || (ret = upload_host_vec(own, ep, &d_ep))
+        || (ret = upload_host_vec(own, ep_chunk, &d_ep_chunk))
         || (ret = upload_host_vec(own, order, &d_order))
         || (ret = upload_host_vec(own, ins_enc, &d_ins)) || (ret = upload_host_vec(own, rem_enc, &d_rem))
         || (ret = upload_host_vec(own, mut_enc, &d_mut_enc))
@@ -475,6 +495,7 @@ int build_compact_plan(tsg_treeseq_t *ts, const HostTopology &h, int64_t want)
     v.c_par0 = d_par0;
     v.c_ep_off = d_ep_off;
     v.c_ep = d_ep;
+    v.c_ep_chunk = d_ep_chunk;
     v.c_order = d_order;
     v.c_ins_enc = d_ins;
     v.c_rem_enc = d_rem;

@@ -152,7 +152,10 @@ struct TSView {
     const uint16_t *c_par0;       // parent at the span start (local id; 0x7FFF: none)
     const int64_t *c_ep_off;      // c_num_spans + 1
     const int2 *c_ep;             // sample-range endpoints (position, local << 1 | is_end)
-    const uint16_t *c_order;      // c_num_spans x num_samples: sample indexes, depth-first
+    const int32_t *c_ep_chunk;    // c_num_spans x (chunks + 1): per chunk of order rows,
+                                  // its first endpoint (within the span's)
+    const uint16_t *c_order;      // c_num_spans x compact_order_stride(num_samples): sample
+                                  // indexes, depth-first
     const int2 *c_ins_enc;        // insertion order: (parent, child), compact encoding
     const int2 *c_rem_enc;        // removal order: (parent, child), compact encoding
     const int32_t *c_mut_enc;     // per mutation: compact encoding of its node
@@ -167,12 +170,37 @@ struct TSView {
 // memory); a tree sequence whose plan exceeds it uses the general replay
 #define TSG_COMPACT_MAX_LOCAL 4096
 
+// The compact spans' depth-first sample orders are read in rows of 32
+// positions, TSG_ROWS_PER_CHUNK rows (one warp's work) to a chunk; an
+// endpoint at position x belongs to row x / 32's chunk (the last chunk for
+// x = num_samples).  A compact plan's spans (at most 65,535 samples, 2,048
+// rows) have at most 32 chunks.
+#define TSG_ROWS_PER_CHUNK 64
+// entries of one span's order in the plan: the samples, padded to a
+// multiple of 8 (each span's order starts 16-byte aligned)
+__host__ __device__ __forceinline__ int64_t compact_order_stride(int64_t n)
+{
+    return (n + 7) & ~(int64_t) 7;
+}
+__host__ __device__ __forceinline__ int64_t compact_row_chunks(int64_t n)
+{
+    const int64_t c = ((n + 31) / 32 + TSG_ROWS_PER_CHUNK - 1) / TSG_ROWS_PER_CHUNK;
+    return c > 0 ? c : 1;
+}
+__host__ __device__ __forceinline__ int64_t compact_chunk_of(int64_t x, int64_t n)
+{
+    const int64_t c = (x >> 5) / TSG_ROWS_PER_CHUNK, last = compact_row_chunks(n) - 1;
+    return c < last ? c : last;
+}
+
 // items per evaluation chunk (one warp)
 #define TSG_ITEM_CHUNK 256
 // nodes one touch list of the item replay holds (a transition touching more
 // stateful nodes closes the list and opens another); the span plan counts
-// items with the same rule
-#define TSG_TOUCH_CAP 128
+// items with the same rule.  Transitions touch a few dozen nodes, and the
+// list's shared memory (16 bytes a node) bounds how many compact replays an
+// SM holds at once.
+#define TSG_TOUCH_CAP 64
 
 // Host copies of the topology the span plan is built from.
 struct HostTopology {

@@ -84,12 +84,11 @@ struct WsDev {
     unsigned long long *site_acc;  // windows x R x 2: exact site-sum counters (integer form)
     uint64_t *cp0;        // (samples + 1) x 2: prefix sums along the first span's order
                           // (compact replay)
-    // the compact spans' depth-first orders in rows of 32 positions: per
-    // span and row, 4 x KQ membership words (bit i: the row's i-th sample
-    // is in set k) and the KQ packed counts before the row (the row after
-    // the last holds the span's totals)
-    uint32_t *c_bits;
-    uint64_t *c_rowpre;
+    // compact plan, per sample-range endpoint: the KQ packed counts of the
+    // members before its position within its chunk of order rows; per span
+    // and chunk, the chunk's total (k_compact_rows)
+    uint64_t *c_pep;
+    uint64_t *c_ctot;
     int32_t *err;
     int32_t *counter;
 };

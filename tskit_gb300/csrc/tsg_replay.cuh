@@ -69,24 +69,24 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// A hint to bring the global-memory line holding p into L2 (no data
-// returned, no register held); p must lie inside an allocation.
-__device__ __forceinline__ void prefetch_l2(const void *p)
-{
-    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
-}
+// events and mutations of a tree staged in shared memory ahead of the
+// replay (a tree's further ones are read from global memory when used):
+// trees have about eight edge events and a few mutations, and the ring's
+// bytes bound how many compact replays an SM holds at once
+#define TSG_STAGE_N 16
 
 // One tree's replay inputs, staged in shared memory ahead of use: the edge
-// events into the tree, its mutations, its item range, and the first 32
-// event encodings, mutation encodings and leaf sample-set masks of each.
+// events into the tree, its mutations, its item range, and the first
+// TSG_STAGE_N event encodings, mutation encodings and leaf sample-set masks
+// of each.
 struct __align__(16) ReplayStage {
     int4 ev;           // removal offset, removals, insertion offset, insertions
     int2 mr;           // mutations [first, end)
     int64_t ioff[2];   // items [first, end)
-    int2 pc[32];       // event (parent, child) encodings
-    uint32_t cm[32];   // leaf child masks
-    int32_t menc[32];  // mutation node encodings
-    uint32_t mmask[32];  // leaf mutation node masks
+    int2 pc[TSG_STAGE_N];       // event (parent, child) encodings
+    uint32_t cm[TSG_STAGE_N];   // leaf child masks
+    int32_t menc[TSG_STAGE_N];  // mutation node encodings
+    uint32_t mmask[TSG_STAGE_N];  // leaf mutation node masks
 };
 
 // an entry of the replay's open touch list (shared memory)

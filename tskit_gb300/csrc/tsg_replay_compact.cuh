@@ -25,179 +25,271 @@
 namespace tsg {
 
 #define TSG_COMPACT_THREADS 32
+// blocks an SM should hold at once (the register budget per thread follows:
+// 64 with one count word per node, 80 with two)
+#define TSG_COMPACT_MIN_BLOCKS(KQ) ((KQ) == 1 ? 32 : 24)
 
-// rows of 32 positions of a compact span's depth-first sample order, plus
-// the row holding the span's totals (k_compact_rows)
-__host__ __device__ __forceinline__ int64_t compact_row_stride(int64_t n)
-{
-    return (n + 31) / 32 + 1;
-}
-
-#define TSG_ROWS_THREADS 256
-// rows a warp of k_compact_rows loads at once
+#define TSG_ROWS_THREADS 128
+// rows whose sample masks a warp of k_compact_rows loads at once
 #define TSG_ROWS_BATCH 8
+// endpoints per lane a warp of k_compact_rows loads before its rows
+#define TSG_ROWS_EPR 8
 
-// The rows of compact span s's order (one block of TSG_ROWS_THREADS per span
-// at a time, a lane per position): warp w takes rows w, w + 8, ... --
-// TSG_ROWS_BATCH of them per round, their order entries and then their
-// sample masks loaded together -- and ballots each set's membership bits
-// into a 32-bit word (4 x KQ words per row, w.c_bits) whose population
-// counts give the row's packed counts; then warp 0 turns the counts (held in
-// w.c_rowpre) into exclusive prefix sums in row order, the row after the
-// last taking the span's totals.  Counts fit their 16-bit fields (at most
-// the set sizes), so packed words add without carries.
+// A warp's shared arrays in k_compact_rows: its chunk's order entries, and
+// per row the membership words (bit i: the row's i-th sample is in set k)
+// and the packed counts of the chunk's rows before it (the entry after the
+// last: the chunk's total).
+template <int KQ>
+struct __align__(16) RowsWarp {
+    uint16_t ord[TSG_ROWS_PER_CHUNK * 32];
+    uint4 word[TSG_ROWS_PER_CHUNK][KQ];
+    uint64_t pre[TSG_ROWS_PER_CHUNK + 1][KQ];
+};
+
+// The members of every sample set before each compact span's range
+// endpoints, a warp per (span, chunk of TSG_ROWS_PER_CHUNK rows of 32
+// depth-first positions):
+//   * the chunk's first TSG_ROWS_EPR x 32 endpoints are loaded, and its
+//     order entries copied into shared memory (16 bytes a copy; each span's
+//     order is padded to a multiple of 8 entries);
+//   * a lane per position, TSG_ROWS_BATCH rows per round (their sample masks
+//     loaded together): each set's membership bits of a row balloted into a
+//     word, the row's 4 x KQ words stored by lane 0;
+//   * a lane per two rows: their packed counts (population counts) and an
+//     exclusive scan over the lanes give each row's count of the chunk's
+//     members before it, and the chunk's total (w.c_ctot);
+//   * a lane per endpoint: the count before its row plus the members of its
+//     row below it, into w.c_pep (local to the chunk; the seek adds the
+//     totals of the chunks before).
+// Counts fit their 16-bit fields (at most the set sizes), so packed words
+// add without carries.
 template <int KQ>
 __device__ __forceinline__ void compact_rows_body(const TSView &ts, const QueryParams &q,
-    const QueryDev &qd, const WsDev &w, const int64_t bid, const int64_t nb)
+    const QueryDev &qd, const WsDev &w, RowsWarp<KQ> *sh, const int64_t bid, const int64_t nb)
 {
-    constexpr int NW = TSG_ROWS_THREADS / 32, RB = TSG_ROWS_BATCH, KW = 4 * KQ;
+    static_assert(TSG_ROWS_PER_CHUNK == 64, "two rows per lane");
+    constexpr int NW = TSG_ROWS_THREADS / 32, RB = TSG_ROWS_BATCH, EPR = TSG_ROWS_EPR;
+    constexpr int CPR = TSG_ROWS_PER_CHUNK;
     const int64_t n = ts.num_samples;
-    const int64_t nrows = (n + 31) / 32, stride = compact_row_stride(n);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int32_t nrows = (int32_t) ((n + 31) / 32);
+    const int64_t CH = compact_row_chunks(n), nst = compact_order_stride(n);
+    const int lane = threadIdx.x & 31;
     const int K = q.K;
-    for (int64_t s = bid; s < ts.c_num_spans; s += nb) {
-        const uint16_t *order = ts.c_order + s * n;
-        uint32_t *bits = w.c_bits + s * stride * KW;
-        uint64_t *pre = w.c_rowpre + s * stride * KQ;
-        for (int64_t r0 = wid; r0 < nrows; r0 += (int64_t) NW * RB) {
+    RowsWarp<KQ> &my = sh[threadIdx.x >> 5];
+    const int64_t items = ts.c_num_spans * CH;
+    for (int64_t it = bid * NW + (threadIdx.x >> 5); it < items; it += nb * NW) {
+        const int64_t s = it / CH;
+        const int32_t c = (int32_t) (it - s * CH);
+        const int32_t rb = c * CPR;
+        const int32_t nr = rb + CPR < nrows ? CPR : nrows - rb;
+        const int2 *ep = ts.c_ep + ts.c_ep_off[s];
+        uint64_t *pep = w.c_pep + ts.c_ep_off[s] * KQ;
+        const int32_t *ec = ts.c_ep_chunk + s * (CH + 1);
+        const int32_t ea = ec[c], eb = ec[c + 1];
+        int2 epv[EPR];
+#pragma unroll
+        for (int u = 0; u < EPR; u++) {
+            const int32_t j = ea + u * 32 + lane;
+            epv[u] = j < eb ? ep[j] : make_int2(-1, 0);
+        }
+        {
+            const uint16_t *order = ts.c_order + s * nst + rb * 32;
+            const int32_t pend = (rb + nr) * 32 < (int32_t) nst ? (rb + nr) * 32 : (int32_t) nst;
+            const int32_t pieces = (pend - rb * 32) / 8;
+            for (int32_t k = lane; k < pieces; k += 32) {
+                cp_async16(&my.ord[k * 8], order + k * 8);
+            }
+            cp_async_wait_all();
+            __syncwarp();
+        }
+        for (int32_t l0 = 0; l0 < nr; l0 += RB) {
             uint32_t m[RB];
 #pragma unroll
             for (int b = 0; b < RB; b++) {
-                const int64_t i = (r0 + (int64_t) b * NW) * 32 + lane;
-                m[b] = i < n ? (uint32_t) order[i] : 0xFFFFFFFFu;
+                const int32_t i = (rb + l0 + b) * 32 + lane;
+                m[b] = l0 + b < nr && i < n ? qd.sample_mask[my.ord[(l0 + b) * 32 + lane]] : 0u;
             }
 #pragma unroll
             for (int b = 0; b < RB; b++) {
-                m[b] = m[b] != 0xFFFFFFFFu ? qd.sample_mask[m[b]] : 0u;
-            }
-#pragma unroll
-            for (int b = 0; b < RB; b++) {
-                const int64_t r = r0 + (int64_t) b * NW;
-                if (r >= nrows) {
+                const int32_t l = l0 + b;
+                if (l >= nr) {
                     break;
                 }
-                uint64_t c[KQ];
+                uint32_t wd[4 * KQ];
 #pragma unroll
-                for (int h = 0; h < KQ; h++) {
-                    c[h] = 0;
-                }
-#pragma unroll
-                for (int k = 0; k < KW; k++) {
-                    const uint32_t word = __ballot_sync(0xffffffffu, k < K && ((m[b] >> k) & 1u));
-                    if (lane == k) {
-                        bits[r * KW + k] = word;
-                    }
-                    c[k / 4] += (uint64_t) __popc(word) << (16 * (k % 4));
+                for (int k = 0; k < 4 * KQ; k++) {
+                    wd[k] = __ballot_sync(0xffffffffu, k < K && ((m[b] >> k) & 1u));
                 }
                 if (lane == 0) {
 #pragma unroll
                     for (int h = 0; h < KQ; h++) {
-                        pre[r * KQ + h] = c[h];
+                        my.word[l][h] = make_uint4(wd[4 * h], wd[4 * h + 1], wd[4 * h + 2],
+                            wd[4 * h + 3]);
                     }
                 }
             }
         }
-        __syncthreads();
-        if (wid == 0) {
-            uint64_t run[KQ];
+        __syncwarp();
+        // rows 2 lane and 2 lane + 1: packed counts, then the scan
+        {
+            uint64_t c0[KQ], c1[KQ];
 #pragma unroll
             for (int h = 0; h < KQ; h++) {
-                run[h] = 0;
-            }
-            for (int64_t r0 = 0; r0 < nrows; r0 += 32) {
-                const int64_t r = r0 + lane;
-#pragma unroll
-                for (int h = 0; h < KQ; h++) {
-                    const uint64_t v = r < nrows ? pre[r * KQ + h] : 0ull;
-                    uint64_t inc = v;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint64_t a = __shfl_up_sync(0xffffffffu, inc, o);
-                        if (lane >= o) {
-                            inc += a;
-                        }
-                    }
-                    if (r < nrows) {
-                        pre[r * KQ + h] = run[h] + inc - v;
-                    }
-                    run[h] += __shfl_sync(0xffffffffu, inc, 31);
+                c0[h] = 0;
+                c1[h] = 0;
+                if (2 * lane < nr) {
+                    const uint4 a = my.word[2 * lane][h];
+                    c0[h] = (uint64_t) __popc(a.x) + ((uint64_t) __popc(a.y) << 16)
+                        + ((uint64_t) __popc(a.z) << 32) + ((uint64_t) __popc(a.w) << 48);
                 }
-            }
-            if (lane == 0) {
+                if (2 * lane + 1 < nr) {
+                    const uint4 a = my.word[2 * lane + 1][h];
+                    c1[h] = (uint64_t) __popc(a.x) + ((uint64_t) __popc(a.y) << 16)
+                        + ((uint64_t) __popc(a.z) << 32) + ((uint64_t) __popc(a.w) << 48);
+                }
+                const uint64_t v = c0[h] + c1[h];
+                uint64_t inc = v;
 #pragma unroll
-                for (int h = 0; h < KQ; h++) {
-                    pre[nrows * KQ + h] = run[h];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint64_t x = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) {
+                        inc += x;
+                    }
+                }
+                const uint64_t ex = inc - v;
+                if (2 * lane < nr) {
+                    my.pre[2 * lane][h] = ex;
+                }
+                if (2 * lane + 1 < nr) {
+                    my.pre[2 * lane + 1][h] = ex + c0[h];
+                }
+                if (lane == 31) {
+                    my.pre[nr][h] = inc;
+                    w.c_ctot[(s * CH + c) * KQ + h] = inc;
                 }
             }
         }
-        __syncthreads();
+        __syncwarp();
+        auto value = [&](int32_t j, int32_t x) {
+            const int32_t l = (x >> 5) - rb;  // nr only for x = n, n a multiple of 32
+            const uint32_t below = (1u << (x & 31)) - 1u;
+#pragma unroll
+            for (int h = 0; h < KQ; h++) {
+                uint64_t p = my.pre[l][h];
+                if (below != 0) {
+                    const uint4 a = my.word[l][h];
+                    p += (uint64_t) __popc(a.x & below) + ((uint64_t) __popc(a.y & below) << 16)
+                        + ((uint64_t) __popc(a.z & below) << 32)
+                        + ((uint64_t) __popc(a.w & below) << 48);
+                }
+                pep[(int64_t) j * KQ + h] = p;
+            }
+        };
+#pragma unroll
+        for (int u = 0; u < EPR; u++) {
+            if (epv[u].x >= 0) {
+                value(ea + u * 32 + lane, epv[u].x);
+            }
+        }
+        for (int32_t j = ea + EPR * 32 + lane; j < eb; j += 32) {
+            value(j, ep[j].x);
+        }
+        __syncwarp();
     }
 }
 
 template <int KQ>
-__global__ void __launch_bounds__(TSG_ROWS_THREADS) k_compact_rows(TSView ts, QueryParams q,
+__global__ void __launch_bounds__(TSG_ROWS_THREADS, 8) k_compact_rows(TSView ts, QueryParams q,
     QueryDev qd, WsDev w)
 {
-    compact_rows_body<KQ>(ts, q, qd, w, blockIdx.x, gridDim.x);
+    __shared__ RowsWarp<KQ> sh[TSG_ROWS_THREADS / 32];
+    compact_rows_body<KQ>(ts, q, qd, w, sh, blockIdx.x, gridDim.x);
 }
 
-// Counts of span s's compact nodes at the span start into sp.xq, from the
-// span's rows (k_compact_rows): the members before depth-first position x
-// are the prefix of x's row plus, per set, the population count of the
-// row's membership word below x.  The span's range endpoints, sorted, are
-// taken TSG_COMPACT_THREADS at a time, a thread each; a node's start count
-// is stored first and its end then subtracts it.  Ends with the block
-// synchronised.
+// endpoints a thread of the seek takes at once
+#define TSG_SEEK_EPL 4
+
+// Counts of span s's compact nodes at the span start into sp.xq, from
+// k_compact_rows' counts at the span's range endpoints plus the totals of
+// the chunks before each endpoint's (an exclusive scan over the lanes, lane
+// c holding chunk c's offset).  The endpoints, sorted, are taken
+// TSG_COMPACT_THREADS x TSG_SEEK_EPL at a time (each thread's loads issued
+// together); within such a group every start count is stored before any end
+// subtracts its node's start, and a node's start never follows its end in
+// the sorted order.  Ends with the block synchronised.
 template <int KQ>
 __device__ __forceinline__ void compact_seek(const TSView &ts, const WsDev &w, int s,
     const SpanState<uint16_t> &sp)
 {
-    constexpr int T = TSG_COMPACT_THREADS, KW = 4 * KQ;
-    const int64_t stride = compact_row_stride(ts.num_samples);
-    const uint32_t *bits = w.c_bits + (int64_t) s * stride * KW;
-    const uint64_t *pre = w.c_rowpre + (int64_t) s * stride * KQ;
-    const int2 *ep = ts.c_ep + ts.c_ep_off[s];
-    const int64_t nep = ts.c_ep_off[s + 1] - ts.c_ep_off[s];
+    static_assert(TSG_COMPACT_THREADS == 32, "the seek's chunk offsets live in one warp");
+    constexpr int T = TSG_COMPACT_THREADS, EPL = TSG_SEEK_EPL;
+    const int64_t n = ts.num_samples;
+    const int64_t CH = compact_row_chunks(n);
+    const int64_t e0 = ts.c_ep_off[s];
+    const int2 *ep = ts.c_ep + e0;
+    const uint64_t *pep = w.c_pep + e0 * KQ;
+    const int64_t nep = ts.c_ep_off[s + 1] - e0;
     const int tid = threadIdx.x;
-    for (int64_t j0 = 0; j0 < nep; j0 += T) {
-        const int64_t j = j0 + tid;
-        const bool act = j < nep;
-        int2 e = make_int2(0, 0);
-        uint64_t p[KQ];
+    uint64_t coff[KQ];
 #pragma unroll
-        for (int h = 0; h < KQ; h++) {
-            p[h] = 0;
+    for (int h = 0; h < KQ; h++) {
+        const uint64_t v = tid < CH ? w.c_ctot[((int64_t) s * CH + tid) * KQ + h] : 0ull;
+        uint64_t inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t a = __shfl_up_sync(0xffffffffu, inc, o);
+            if (tid >= o) {
+                inc += a;
+            }
         }
-        if (act) {
-            e = ep[j];
-            const int64_t row = e.x >> 5;
-            const uint32_t below = (1u << (e.x & 31)) - 1u;
+        coff[h] = inc - v;
+    }
+    for (int64_t j0 = 0; j0 < nep; j0 += (int64_t) T * EPL) {
+        int2 e[EPL];
+        uint64_t p[EPL][KQ];
+#pragma unroll
+        for (int u = 0; u < EPL; u++) {
+            const int64_t j = j0 + (int64_t) u * T + tid;
+            e[u] = make_int2(-1, 0);
 #pragma unroll
             for (int h = 0; h < KQ; h++) {
-                p[h] = pre[row * KQ + h];
+                p[u][h] = 0;
             }
-            if (below != 0) {
+            if (j < nep) {
+                e[u] = ep[j];
 #pragma unroll
                 for (int h = 0; h < KQ; h++) {
-                    const uint4 b = *(const uint4 *) (bits + row * KW + 4 * h);
-                    p[h] += (uint64_t) __popc(b.x & below) + ((uint64_t) __popc(b.y & below) << 16)
-                        + ((uint64_t) __popc(b.z & below) << 32)
-                        + ((uint64_t) __popc(b.w & below) << 48);
+                    p[u][h] = pep[j * KQ + h];
                 }
             }
         }
-        const int64_t l = e.y >> 1;
-        if (act && !(e.y & 1)) {
+#pragma unroll
+        for (int u = 0; u < EPL; u++) {
+            const int src = e[u].x >= 0 ? (int) compact_chunk_of(e[u].x, n) : 0;
 #pragma unroll
             for (int h = 0; h < KQ; h++) {
-                sp.xq[l * KQ + h] = p[h];
+                p[u][h] += __shfl_sync(0xffffffffu, coff[h], src);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < EPL; u++) {
+            if (e[u].x >= 0 && !(e[u].y & 1)) {
+                const int64_t l = e[u].y >> 1;
+#pragma unroll
+                for (int h = 0; h < KQ; h++) {
+                    sp.xq[l * KQ + h] = p[u][h];
+                }
             }
         }
         __syncthreads();
-        if (act && (e.y & 1)) {
 #pragma unroll
-            for (int h = 0; h < KQ; h++) {
-                sp.xq[l * KQ + h] = p[h] - sp.xq[l * KQ + h];
+        for (int u = 0; u < EPL; u++) {
+            if (e[u].x >= 0 && (e[u].y & 1)) {
+                const int64_t l = e[u].y >> 1;
+#pragma unroll
+                for (int h = 0; h < KQ; h++) {
+                    sp.xq[l * KQ + h] = p[u][h] - sp.xq[l * KQ + h];
+                }
             }
         }
         __syncthreads();
@@ -240,7 +332,7 @@ struct CompactShared {
 
 // Persistent blocks take spans from the query's counter until none is left.
 template <int KQ>
-__global__ void __launch_bounds__(TSG_COMPACT_THREADS, 24) k_replay_compact(TSView ts, QueryParams q,
+__global__ void __launch_bounds__(TSG_COMPACT_THREADS, TSG_COMPACT_MIN_BLOCKS(KQ)) k_replay_compact(TSView ts, QueryParams q,
     QueryDev qd, WsDev w)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

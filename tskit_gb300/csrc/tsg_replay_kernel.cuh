@@ -219,21 +219,22 @@ __device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams 
     auto stage_b = [&](int32_t t) {
         ReplayStage &S = s_stage[t & 3];
         const int4 ev = S.ev;
-        if (t > t0 && lane < ev.y + ev.w) {
+        if (t > t0 && lane < TSG_STAGE_N && lane < ev.y + ev.w) {
             cp_async8(&S.pc[lane], lane < ev.y ? (const void *) &code.rem[ev.x + lane]
                                                : (const void *) &code.ins[ev.z + lane - ev.y]);
         }
-        if (site && t < t1 && lane < S.mr.y - S.mr.x) {
+        if (site && t < t1 && lane < TSG_STAGE_N && lane < S.mr.y - S.mr.x) {
             cp_async4(&S.menc[lane], &code.mut[S.mr.x + lane]);
         }
     };
     auto stage_c = [&](int32_t t) {
         ReplayStage &S = s_stage[t & 3];
         const int4 ev = S.ev;
-        if (t > t0 && lane < ev.y + ev.w && S.pc[lane].y < 0) {
+        if (t > t0 && lane < TSG_STAGE_N && lane < ev.y + ev.w && S.pc[lane].y < 0) {
             cp_async4(&S.cm[lane], &qd.node_mask[-S.pc[lane].y - 1]);
         }
-        if (site && t < t1 && lane < S.mr.y - S.mr.x && S.menc[lane] < 0) {
+        if (site && t < t1 && lane < TSG_STAGE_N && lane < S.mr.y - S.mr.x
+            && S.menc[lane] < 0) {
             cp_async4(&S.mmask[lane], &qd.node_mask[-S.menc[lane] - 1]);
         }
     };
@@ -274,12 +275,12 @@ __device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams 
             const int32_t r0 = S.ev.x, nr = S.ev.y, i0 = S.ev.z, ni = S.ev.w;
             for (int32_t base = 0; base < nr + ni; base += 32) {
                 // up to 32 events of the transition at once (the
-                // first 32 from the ring)
+                // first TSG_STAGE_N from the ring)
                 const int32_t j = base + lane;
                 int2 pc = make_int2(0, 0);
                 uint32_t cm = 0;
                 if (j < nr + ni) {
-                    if (base == 0) {
+                    if (j < TSG_STAGE_N) {
                         pc = S.pc[lane];
                         cm = pc.y < 0 ? S.cm[lane] : 0u;
                     } else {
@@ -323,7 +324,7 @@ __device__ __forceinline__ void replay_span(const TSView &ts, const QueryParams 
             for (int32_t m = m0 + lane; m < m1; m += 32) {
                 int32_t enc;
                 uint32_t mask = 0;
-                if (m - m0 < 32) {
+                if (m - m0 < TSG_STAGE_N) {
                     enc = S.menc[lane];
                     if (enc < 0) {
                         mask = S.mmask[lane];

@@ -469,10 +469,12 @@ static void *compact_kernel(int KQ)
     return KQ == 1 ? (void *) k_replay_compact<1> : (void *) k_replay_compact<2>;
 }
 
-// rows of the compact spans' order arrays (k_compact_rows) per span
-static int64_t compact_rows(const tsg_treeseq_t *ts)
+// blocks of k_compact_rows: a warp per (span, chunk of rows)
+static int64_t compact_rows_blocks(const tsg_treeseq_t *ts)
 {
-    return compact_row_stride(ts->v.num_samples);
+    const int64_t warps = ts->v.c_num_spans * compact_row_chunks(ts->v.num_samples);
+    return std::min<int64_t>((warps + TSG_ROWS_THREADS / 32 - 1) / (TSG_ROWS_THREADS / 32),
+        1 << 20);
 }
 
 
@@ -525,8 +527,8 @@ struct tsg_query {
     bool smem;               // item pipeline (either form); else the general sweep
     bool gstate;             // item pipeline with node state in global memory
     bool compact_ok;         // the compact replay serves when the tree sequence has its plan
-    int64_t c_rows_cap;      // compact spans the workspace's row arrays hold (the plan's
-                             // span count when the query was prepared)
+    int64_t c_rows_cap;      // compact spans and sample-range endpoints the workspace's
+    int64_t c_ep_cap;        // arrays hold (the plan's when the query was prepared)
     int W, KQ;               // count field width, 64-bit count words per node
     int64_t smem_bytes, smem_grid, slot_bytes;
     int span_normalise;
@@ -551,7 +553,8 @@ namespace tsg {
 // spans after q was prepared leaves q on the general replay)
 static bool compact_serves(const tsg_query_t *q)
 {
-    return q->compact_ok && q->ts->v.c_num_spans > 0 && q->ts->v.c_num_spans <= q->c_rows_cap;
+    return q->compact_ok && q->ts->v.c_num_spans > 0 && q->ts->v.c_num_spans <= q->c_rows_cap
+        && q->ts->h_compact_endpoints <= q->c_ep_cap;
 }
 
 // Check the sample sets (c/tskit/trees.c:2114-2149 and the duplicate check of
@@ -1062,6 +1065,7 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
     }
     q->compact_ok = q->smem && !q->gstate && q->W == 16 && q->KQ <= 2;
     q->c_rows_cap = q->compact_ok ? ts->v.c_num_spans : 0;
+    q->c_ep_cap = q->compact_ok ? ts->h_compact_endpoints : 0;
     if (q->compact_ok) {
         void *fn = compact_kernel(q->KQ);
         allow_max_dynamic_smem(fn);
@@ -1093,8 +1097,8 @@ static int query_build(tsg_query_t **out, const tsg_treeseq_t *ts, uint64_t K,
         bytes += align_up((p.branch ? (int64_t) Wn << K : 0) * 8, 256);          // leaf_dbl
         bytes += align_up((int64_t) Wn * R * 8, 256);                            // leaf_win
         bytes += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256); // cp0
-        bytes += align_up(q->c_rows_cap * compact_rows(ts) * 16 * KQ, 256);     // c_bits
-        bytes += align_up(q->c_rows_cap * compact_rows(ts) * 8 * KQ, 256);      // c_rowpre
+        bytes += align_up(q->c_ep_cap * 8 * KQ, 256);                                  // c_pep
+        bytes += align_up(q->c_rows_cap * compact_row_chunks(ts->v.num_samples) * 8 * KQ, 256);
     }
     bytes += 256;                                                     // err, counter
     q->ws_bytes = bytes;
@@ -1633,8 +1637,8 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
     w.site_val = nullptr;
     w.site_win = nullptr;
     w.cp0 = nullptr;
-    w.c_bits = nullptr;
-    w.c_rowpre = nullptr;
+    w.c_pep = nullptr;
+    w.c_ctot = nullptr;
     w.site_acc = nullptr;
     if (q->smem) {
         const int64_t item_bytes = q->KQ == 1 ? (int64_t) sizeof(Item<1>) : (int64_t) sizeof(Item<2>);
@@ -1666,10 +1670,10 @@ static WsDev ws_bind(const tsg_query_t *q, tsg_workspace_t *ws)
         off += align_up((int64_t) p.Wn * R * 8, 256);
         w.cp0 = (uint64_t *) (b + off);
         off += align_up(q->compact_ok ? (ts->v.num_samples + 1) * 16 : 0, 256);
-        w.c_bits = (uint32_t *) (b + off);
-        off += align_up(q->c_rows_cap * compact_rows(ts) * 16 * q->KQ, 256);
-        w.c_rowpre = (uint64_t *) (b + off);
-        off += align_up(q->c_rows_cap * compact_rows(ts) * 8 * q->KQ, 256);
+        w.c_pep = (uint64_t *) (b + off);
+        off += align_up(q->c_ep_cap * 8 * q->KQ, 256);
+        w.c_ctot = (uint64_t *) (b + off);
+        off += align_up(q->c_rows_cap * compact_row_chunks(ts->v.num_samples) * 8 * q->KQ, 256);
     }
     w.err = (int32_t *) (b + off);
     w.counter = w.err + 1;
@@ -1950,7 +1954,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
             // blocks are spread over every SM first; then every chunk's item
             // values
             const int kq = q->KQ;
-            const unsigned gr = (unsigned) std::min<int64_t>(ts->v.c_num_spans, 1 << 20);
+            const unsigned gr = (unsigned) compact_rows_blocks(ts);
             if (kq == 1) {
                 k_compact_rows<1><<<gr, TSG_ROWS_THREADS, 0, st>>>(ts->v, p, d, w);
             } else {
@@ -2184,7 +2188,7 @@ static void batch_stage_blocks(const tsg_query_t *q, int64_t *nb)
     const int64_t site = p.site && p.site_int ? (int64_t) p.Wn * R * 2 : 0;
     nb[BS_ZERO] = std::min<int64_t>((1 + R + leaf + site + 255) / 256, 4096);
     nb[BS_NODE_MASK] = grid_for(ts->v.num_nodes);
-    nb[BS_ROWS] = std::min<int64_t>(ts->v.c_num_spans, 1 << 20);
+    nb[BS_ROWS] = compact_rows_blocks(ts);
     if (p.branch) {
         if (ts->v.c_num_anchors > 0) {
             nb[BS_PREFIX] = (ts->v.num_samples + 1023) / 1024;

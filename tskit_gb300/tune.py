@@ -153,10 +153,10 @@ def tune_num_spans(tables, make_step, key="", candidates=None, steps=3, warmup=1
 
 
 def compact_candidates(default_spans, num_trees):
-    """Compact span counts to try: half to four times the default (finer
-    steps up to twice it, where one wave of resident blocks ends), each at
-    most one span per tree."""
-    c = {max(1, int(default_spans * f)) for f in (0.5, 1, 1.25, 1.5, 2, 4)}
+    """Compact span counts to try: half to twice the default in quarter
+    steps (the fastest is about the most spans whose blocks are all resident
+    at once), each at most one span per tree."""
+    c = {max(1, int(default_spans * f)) for f in (0.5, 0.75, 1, 1.25, 1.5, 2)}
     return sorted({min(x, max(1, int(num_trees))) for x in c})
 
 
