@@ -74,7 +74,8 @@ __device__ __forceinline__ void compact_rows_body(const TSView &ts, const QueryP
     const int32_t nrows = (int32_t) ((n + 31) / 32);
     const int64_t CH = compact_row_chunks(n), nst = compact_order_stride(n);
     const int lane = threadIdx.x & 31;
-    const int K = q.K;
+    // the sets' bits of a sample mask (bits past the last set are clear)
+    const uint32_t kmask = q.K >= 32 ? 0xFFFFFFFFu : (1u << q.K) - 1u;
     RowsWarp<KQ> &my = sh[threadIdx.x >> 5];
     const int64_t items = ts.c_num_spans * CH;
     for (int64_t it = bid * NW + (threadIdx.x >> 5); it < items; it += nb * NW) {
@@ -107,7 +108,8 @@ __device__ __forceinline__ void compact_rows_body(const TSView &ts, const QueryP
 #pragma unroll
             for (int b = 0; b < RB; b++) {
                 const int32_t i = (rb + l0 + b) * 32 + lane;
-                m[b] = l0 + b < nr && i < n ? qd.sample_mask[my.ord[(l0 + b) * 32 + lane]] : 0u;
+                m[b] = l0 + b < nr && i < n ? qd.sample_mask[my.ord[(l0 + b) * 32 + lane]] & kmask
+                                            : 0u;
             }
 #pragma unroll
             for (int b = 0; b < RB; b++) {
@@ -118,7 +120,7 @@ __device__ __forceinline__ void compact_rows_body(const TSView &ts, const QueryP
                 uint32_t wd[4 * KQ];
 #pragma unroll
                 for (int k = 0; k < 4 * KQ; k++) {
-                    wd[k] = __ballot_sync(0xffffffffu, k < K && ((m[b] >> k) & 1u));
+                    wd[k] = __ballot_sync(0xffffffffu, (m[b] & (1u << k)) != 0u);
                 }
                 if (lane == 0) {
 #pragma unroll
