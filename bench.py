@@ -405,14 +405,16 @@ def replay_algorithmic_bytes(tables, plan, kq=1):
     per edge its insertion and removal encodings (16) and at most one leaf
     mask per event (8); per tree its event, mutation and item ranges (40); per
     mutation its encoding (4) and the counts written under it (8 per count
-    word); per span its depth-first sample order (2 per sample), sample-range
-    endpoints (8 each) and start parents (2 per node); every item written
-    (16 per count word + 16); the samples' set masks (4 each)."""
+    word); per span its sample-range endpoints (8 each) with the set-member
+    counts before them (8 per count word, written by k_compact_rows), and its
+    nodes' start parents and times (2 + 8 per node); every item written (16
+    per count word + 16) with its two FP64 branch lengths (16).  The
+    depth-first sample orders and the sample masks are read by
+    k_compact_rows, not by the replay."""
     E, M = tables.num_edges, tables.num_mutations
-    n = len(tables.samples())
     return (24 * E + 40 * plan["num_trees"] + (4 + 8 * kq) * M
-            + 2 * n * plan["num_compact_spans"] + 8 * plan["compact_endpoints"]
-            + 2 * plan["compact_nodes"] + (16 * kq + 16) * plan["num_items"] + 4 * n)
+            + (8 + 8 * kq) * plan["compact_endpoints"] + 10 * plan["compact_nodes"]
+            + (16 * kq + 32) * plan["num_items"])
 
 
 def run_gpu(args):

@@ -170,8 +170,11 @@ int64_t tsg_treeseq_get_num_spans(const tsg_treeseq_t *ts);
  * rebuild it with about num_spans spans (-1: the default count; 0: use the
  * general replay; a count
  * whose spans touch more than 4,096 nodes also leaves the general replay
- * serving); queries prepared before must not run concurrently with it.
- * Results do not depend on the span count. */
+ * serving); queries prepared before must not run concurrently with it, and
+ * a query prepared against a plan with fewer spans or range endpoints than
+ * the rebuilt one runs on the general replay (its workspace holds the
+ * compact replay's per-endpoint counts for the plan it was prepared
+ * against).  Results do not depend on the span count. */
 int64_t tsg_treeseq_get_num_compact_spans(const tsg_treeseq_t *ts);
 /* Sizes of the tree sequence's replay plans (no reference counterpart; for
  * measuring): sizes[0..7] = trees, spans of the general plan, spans of the

@@ -83,3 +83,30 @@ def test_compact_site_only_and_default_plan(case):
     assert ts.set_compact_spans(200) > 0
     got = _run(ts, sets, terms, windows, "f64", both=False)
     np.testing.assert_array_equal(got, general)
+
+
+def test_query_prepared_before_a_larger_plan(case):
+    """A query's workspace holds the compact replay's per-endpoint counts for
+    the plan it was prepared against; after the plan is rebuilt with more
+    spans the query still runs (on the general replay) with the same
+    results, and a query prepared again uses the new plan."""
+    import torch
+
+    import tskit_gb300
+
+    ts, tables, sets, terms, windows = case
+    ts.set_compact_spans(0)
+    general = _run(ts, sets, terms, windows, "f64")
+    assert ts.set_compact_spans(2) > 0
+    q = ts.query(sets, terms, windows=windows, both_modes=True, mode="site",
+                 span_normalise=False, precision="f64")
+    ws = tskit_gb300.Workspace(q.workspace_bytes)
+    res = torch.zeros(q.result_size, dtype=torch.float64, device="cuda")
+    built = ts.set_compact_spans(64)
+    q.launch(ws, res)
+    torch.cuda.synchronize()
+    q.check(ws)
+    np.testing.assert_array_equal(res.cpu().numpy(), general)
+    if built > 0:
+        np.testing.assert_array_equal(_run(ts, sets, terms, windows, "f64"), general)
+    ts.set_compact_spans(-1)
