@@ -1,16 +1,18 @@
 // The compact replay: the item pipeline's replay over the compact span plan
 // (tsg_cplan.cu).  One block of one warp (TSG_COMPACT_THREADS) per span at a
 // time, the span's node state (16-bit counts packed in 64-bit words and
-// 16-bit parent entries) in shared memory: a few kilobytes, so about twenty
-// blocks -- twenty sequential replays -- run on every SM.
+// 16-bit parent entries) in shared memory with a 64-entry touch list and a
+// 16-entry staging ring: about 8 KB, so some thirty blocks -- thirty
+// sequential replays -- run on every SM.
 //
 //   rows     (k_compact_rows, before the replay, every span at once) each
 //            span's depth-first sample order in rows of 32 positions: per
-//            row a membership word per set (ballots) and the packed counts
-//            before the row (prefix sums of population counts);
-//   seek     at each of the span's sorted range endpoints a node's count,
-//            P[hi] - P[lo], P read from the rows in O(1) (the start is
-//            stored first, the end then subtracts it);
+//            row a membership word per set (ballots), the rows' counts
+//            scanned per chunk of 64 rows, and at each of the span's range
+//            endpoints the members before it within its chunk;
+//   seek     at each of the span's sorted range endpoints P, that count plus
+//            the totals of the chunks before, and a node's count P[hi] -
+//            P[lo] (the start is stored first, the end then subtracts it);
 //   replay   replay_span over the compact encodings.
 //
 // The first tree's items (its stateful nodes, the anchors) are written by
