@@ -99,6 +99,7 @@ struct TSView {
     const int32_t *sample_index;  // node -> sample index or -1
     const int32_t *samples;       // sample index -> node
     const double *breakpoints;    // num_trees + 1
+    const double *tree_len;       // num_trees: breakpoints[t + 1] - breakpoints[t]
     const int32_t *tree_in;       // num_trees + 1: insertion-order offsets
     const int32_t *tree_out;      // num_trees + 1: removal-order offsets
     const int32_t *tree_sites;    // num_trees + 1

@@ -2071,7 +2071,7 @@ int tsg_query_launch(const tsg_query_t *q, tsg_workspace_t *ws, double *result,
         }
         if (p.branch) {
             NvtxRange nvtx_win("tsg.windows");
-            k_span_windows<<<(unsigned) ((ts->v.num_segs + 7) / 8), 256, 0, st>>>(ts->v, p, d, w);
+            k_span_windows<<<(unsigned) ((ts->v.num_segs + 3) / 4), 128, 0, st>>>(ts->v, p, d, w);
             TSG_LAUNCHED();
             if (!forked_leaf) {
                 int r = leaf_stage(st);
@@ -2737,7 +2737,7 @@ static int general_finish(tsg_general *g, const double *dF, double *result)
             break;
         }
         if (pb.branch) {
-            k_span_windows<<<(unsigned) ((v.num_segs + 7) / 8), 256, 0, st>>>(v, pb, g->d, g->w);
+            k_span_windows<<<(unsigned) ((v.num_segs + 3) / 4), 128, 0, st>>>(v, pb, g->d, g->w);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             if (cudaMemsetAsync(g->w.rs0, 0, (size_t) pb.R * 8, st) != cudaSuccess) {
                 ret = TSG_ERR_CUDA;

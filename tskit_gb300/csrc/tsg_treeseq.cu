@@ -336,6 +336,15 @@ __global__ void k_compact_distinct(const double *a, const int64_t *pos, int64_t 
     }
 }
 
+// each tree's length, as the window sums difference its ends
+__global__ void k_tree_len(const double *bp, int64_t T, double *len)
+{
+    const int64_t t = blockIdx.x * (int64_t) blockDim.x + threadIdx.x;
+    if (t < T) {
+        len[t] = bp[t + 1] - bp[t];
+    }
+}
+
 __global__ void k_tree_ranges(const double *bp, int64_t T, const double *ins_left,
     const double *rem_right, int64_t E, const double *site_pos, int64_t S, int32_t *tree_in,
     int32_t *tree_out, int32_t *tree_sites)
@@ -775,10 +784,16 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
 
         int32_t *tree_in = nullptr, *tree_out = nullptr, *tree_sites = nullptr,
                 *site_mut = nullptr;
+        double *tree_len = nullptr;
         if ((ret = dev_alloc(ts, &tree_in, T + 1)) || (ret = dev_alloc(ts, &tree_out, T + 1))
             || (ret = dev_alloc(ts, &tree_sites, T + 1))
-            || (ret = dev_alloc(ts, &site_mut, S + 1))) {
+            || (ret = dev_alloc(ts, &site_mut, S + 1))
+            || (ret = dev_alloc(ts, &tree_len, T > 0 ? T : 1))) {
             goto fail;
+        }
+        if (T > 0) {
+            k_tree_len<<<grid_for(T), 256, 0, st>>>(bp, T, tree_len);
+            TSG_LAUNCHED();
         }
         k_tree_ranges<<<grid_for(T + 1), 256, 0, st>>>(bp, T, ins_left, rem_right, E, t.site_pos,
             S, tree_in, tree_out, tree_sites);
@@ -794,6 +809,7 @@ int tsg_treeseq_init(tsg_treeseq_t **out, const tsg_tables_t *tables, int64_t nu
         ts->v.sequence_length = L;
         ts->v.node_time = t.node_time;
         ts->v.breakpoints = bp;
+        ts->v.tree_len = tree_len;
         ts->v.tree_in = tree_in;
         ts->v.tree_out = tree_out;
         ts->v.tree_sites = tree_sites;
