@@ -614,6 +614,9 @@ static __global__ void __launch_bounds__(1024) k_site_windows(QueryParams q, Que
     }
 }
 
+// values a thread of the span scan loads at once
+#define TSG_SCAN_U 8
+
 // RS[s][r] = rs0[r] + sum_{s' < s} D[s'][r]: one block per r, each thread a
 // contiguous run of units, then a scan of the run totals across the block
 // (warp shuffles, then the warp totals in shared memory); fixed order.
@@ -626,9 +629,23 @@ __device__ __forceinline__ void span_scan_body(const double *D, const double *rs
     const int64_t run = (NS + blockDim.x - 1) / blockDim.x;
     const int64_t b = (int64_t) threadIdx.x * run < NS ? (int64_t) threadIdx.x * run : NS;
     const int64_t e = b + run < NS ? b + run : NS;
+    // a thread's values are loaded TSG_SCAN_U at a time (independent loads)
+    // and added in order; with at most TSG_SCAN_U they stay in registers for
+    // the second pass
+    constexpr int U = TSG_SCAN_U;
+    double v[U];
     double sum = 0;
-    for (int64_t i = b; i < e; i++) {
-        sum += D[i * R + r];
+    for (int64_t i0 = b; i0 < e; i0 += U) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            v[u] = i0 + u < e ? D[(i0 + u) * R + r] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (i0 + u < e) {
+                sum += v[u];
+            }
+        }
     }
     double incl = sum;
     for (int o = 1; o < 32; o <<= 1) {
@@ -653,9 +670,20 @@ __device__ __forceinline__ void span_scan_body(const double *D, const double *rs
     }
     __syncthreads();
     double acc = s_warp[wid] + excl;
-    for (int64_t i = b; i < e; i++) {
-        RS[i * R + r] = acc;
-        acc += D[i * R + r];
+    for (int64_t i0 = b; i0 < e; i0 += U) {
+        if (e - b > U) {
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                v[u] = i0 + u < e ? D[(i0 + u) * R + r] : 0.0;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (i0 + u < e) {
+                RS[(i0 + u) * R + r] = acc;
+                acc += v[u];
+            }
+        }
     }
 }
 
