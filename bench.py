@@ -514,11 +514,68 @@ def run_gpu(args):
         return (max_over_ranks(float(np.mean(step_ms)), world), float(np.mean(sweep_ms)),
                 launches, raw, sampler, float(np.mean(rep_ms)))
 
+    def timed_graph(precision, steps):
+        """The same fused launch captured once in a CUDA graph (the side
+        streams' forks and joins become graph edges) and replayed each step
+        after an L2 flush; returns the mean step time (CUDA events on the
+        launch stream, max over ranks), the clock sampler and the raw
+        result."""
+        q, ws, res = prepare(ts, precision)
+        st = torch.cuda.Stream()
+        st.wait_stream(stream)
+        with torch.cuda.stream(st):
+            for _ in range(2):
+                q.launch(ws, res, st)
+        st.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st):
+            q.launch(ws, res, st)
+        torch.cuda.synchronize()
+        for _ in range(args.warmup):
+            flush.zero_()
+            g.replay()
+        torch.cuda.synchronize()
+        q.check(ws)
+        times = []
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local)
+        sampler.__enter__()
+        try:
+            for _ in range(steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                g.replay()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+        finally:
+            sampler.__exit__(None, None, None)
+        q.check(ws)
+        raw = res.cpu().numpy().reshape(2, NUM_WINDOWS, len(terms))
+        return max_over_ranks(float(np.mean(times)), world), sampler, raw
+
     # the headline: one fused sweep at the reference's precision (FP64 window
     # and running sums; summaries as exact integer numerators with about one
-    # FP64 fused multiply-add per item)
+    # FP64 fused multiply-add per item), enqueued from the host each step ...
     ms, sweep, launches, raw_batched, clocks, rep = timed_fused("f64", args.steps,
                                                                  with_clocks=True)
+    eager = {"ms_per_step": ms, "value": world * logical / (ms / 1e3),
+             "note": "the fused launch enqueued from the host each step (14 kernels, "
+                     "memsets and the side streams' event forks and joins)"}
+    # ... and replayed from a captured CUDA graph: the same kernels and work
+    # each step, without the host's enqueue between them
+    try:
+        gms, gclocks, graw = timed_graph("f64", args.steps)
+        eager["graph_result_equals_eager"] = bool(np.array_equal(graw, raw_batched))
+        if eager["graph_result_equals_eager"]:
+            ms, clocks = gms, gclocks
+            eager["headline"] = "graph replay"
+    except Exception as exc:  # the eager figure stands
+        eager["graph_error"] = str(exc).splitlines()[0][:200]
     value = world * logical / (ms / 1e3)
     # the FP32-compensated form of the same sweep
     ms32, sweep32, _, raw_f32, _, _ = timed_fused("f32", max(3, min(args.steps, 10)))
@@ -605,6 +662,7 @@ def run_gpu(args):
         "data": "synthetic (seeded SMC generator, tskit_gb300.sim)",
         "config": dict(workload_config(tables), num_compact_spans=tuned["num_spans"],
                        span_tuning_ms={str(k): v for k, v in tuned["ms"].items()}),
+        "eager_launch": eager,
         "queries_per_s": world * traversals / (ms / 1e3),
         "physical_edge_updates_per_s": world * events / (ms / 1e3),
         "batched_f32_kahan": {
