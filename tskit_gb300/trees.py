@@ -67,7 +67,10 @@ def _parse_mode(mode):
 
 
 def _ptr(a):
-    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size > 0 else None
+    """A numpy array's data address for a ``void *`` argument (every native
+    function's signature is declared, so the integer is passed as a
+    pointer); None for an empty or absent array."""
+    return a.ctypes.data if a is not None and a.size > 0 else None
 
 
 def _outputs(terms):
